@@ -1,0 +1,188 @@
+/*
+ * openvort_gpu.h - C ABI of libovgpu, the GB300 (sm_103a) implementation of
+ * OpenVort's vortex-filament velocity and time-step path.
+ *
+ * Plain C types only: pointers, sizes, doubles, ints.  No CUDA or torch type
+ * crosses this boundary.  Every call returns an ov_status (0 = OV_OK); the
+ * message of the last failure on a context is read with ov_last_error().
+ *
+ * Two layers:
+ *   1. Context API (ov_ctx_*, ov_upload_*, ov_update_*, ov_rk4_step, ...):
+ *      the tangle lives in HBM between calls, parameters come from an explicit
+ *      ov_params, results are read back with ov_download_*.
+ *   2. Drop-in layer (include/ov_dropin.h, built from ov_dropin.c): void
+ *      functions with the reference's own signatures that read the
+ *      reference's process-global parameters, upload, compute and download
+ *      around a hidden per-process context.
+ *
+ * Reference interfaces replaced (OpenVort, paths within the project):
+ *   update_tangents_normals  include/tangle.h:104,  src/tangle.c:509
+ *   update_velocity          include/tangle.h:106,  src/tangle.c:600
+ *   update_velocities        include/tangle.h:108,  src/tangle.c:733
+ *   remesh                   include/tangle.h:110,  src/tangle.c:1018
+ *   eliminate_small_loops    include/tangle.h:112,  src/tangle.c:1063
+ *   enforce_periodic_boundaries include/tangle.h:98, src/tangle.c:793
+ *   update_tangle            include/tangle.h:114-118 (static inline)
+ *   rk4_step                 include/vortex_dynamics.h:21, src/vortex_dynamics.c:50
+ *   reconnect                include/vortex_dynamics.h:32, src/vortex_dynamics.c:186
+ *   smooth                   include/vortex_smooth.h:11, src/vortex_smooth.c:459
+ *   octree_build / octree_get_vs / octree_destroy
+ *                            include/octree.h:54-66, src/octree.c:139,296,41
+ */
+#ifndef OPENVORT_GPU_H
+#define OPENVORT_GPU_H
+
+#include <stdint.h>
+#include "ov_tangle.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+typedef enum ov_status {
+    OV_OK = 0,
+    OV_ERR_ARG = 1,      /* bad argument (null pointer, negative size, ...) */
+    OV_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+    OV_ERR_ALLOC = 3,    /* device or host allocation failed */
+    OV_ERR_DEPTH = 4,    /* two nodes share a cell at the deepest tree level */
+    OV_ERR_STACK = 5,    /* a traversal exceeded its iteration bound */
+    OV_ERR_NAN = 6,      /* a non-finite position or velocity was produced */
+    OV_ERR_TIMEOUT = 7,  /* a bounded device wait gave up */
+    OV_ERR_TOPOLOGY = 8, /* connections are not a consistent set of loops */
+    OV_ERR_NODEVICE = 9, /* no CUDA device is visible */
+    OV_ERR_STATE = 10    /* call made before the tangle was uploaded */
+} ov_status;
+
+/* --------------------------------------------------------------- params */
+/*
+ * Run parameters.  Field-for-field the process globals of the reference
+ * (include/vortex_constants.h:11-60, defaults src/initial_conditions.c:12-91)
+ * plus the three external-velocity configurations (vn_conf, vs_conf, vb_conf).
+ */
+typedef struct ov_params {
+    double kappa;                     /* KAPPA [cm^2/s] */
+    double vortex_width;              /* VORTEX_WIDTH, a0 [cm] */
+    double alpha;                     /* alpha (mutual friction) */
+    double alpha_p;                   /* alpha' (mutual friction) */
+    int use_mutual_friction;          /* use_mutual_friction */
+    int use_bh;                       /* use_BH: 1 = tree, 0 = direct sum */
+    double bh_resolution;             /* BH_resolution, opening angle theta */
+    ov_ext_vel vn;                    /* vn_conf: normal-fluid velocity */
+    ov_ext_vel vs;                    /* vs_conf: external superfluid velocity */
+    ov_ext_vel vb;                    /* vb_conf: boundary velocity */
+    double dl_min;                    /* global_dl_min */
+    double dl_max;                    /* global_dl_max */
+    double rec_dist;                  /* rec_dist */
+    double reconnection_angle_cutoff; /* reconnection_angle_cutoff [rad] */
+    int small_loop_cutoff;            /* small_loop_cutoff */
+    int use_freq_filter;              /* use_freq_filter */
+    double freq_to_cutoff;            /* freq_to_cutoff */
+    int num_threads;                  /* global_num_threads (host passes) */
+    int pin_mode;                     /* pin_mode */
+} ov_params;
+
+/* Fill `p` with the reference's compiled-in defaults (initial_conditions.c:12-91). */
+void ov_params_default(ov_params *p);
+
+/* ------------------------------------------------------------ precision */
+enum {
+    OV_PREC_FP64 = 0,   /* bit-faithful FP64 traversal (reference semantics) */
+    OV_PREC_MIXED = 1   /* FP32 traversal on grid-split positions, compensated sums,
+                           FP64 for LIA, near field, guard-band decisions, RK4 update */
+};
+
+/* Download field mask for ov_download_tangle. */
+enum {
+    OV_F_POS = 1, OV_F_VELS = 2, OV_F_VS = 4, OV_F_TANGENTS = 8, OV_F_NORMALS = 16,
+    OV_F_TOPOLOGY = 32, OV_F_ALL = 63
+};
+
+/* Counters of the last velocity evaluation (and topology passes). */
+typedef struct ov_stats {
+    int64_t node_evals;        /* target nodes evaluated */
+    int64_t cells;             /* cells in the linear octree */
+    int64_t max_depth;         /* deepest cell level */
+    int64_t visits;            /* per-target cell visits (open or accept) */
+    int64_t accepts;           /* per-target monopole/leaf interactions */
+    int64_t warp_steps;        /* warp-cooperative traversal iterations */
+    int64_t fp64_fallbacks;    /* mixed path: guard-band decisions redone in FP64 */
+    int64_t near_field_fp64;   /* mixed path: near-field interactions done in FP64 */
+    int64_t out_of_root;       /* nodes outside the root box (root-only members) */
+    int64_t reconnections;     /* last reconnect pass */
+    int64_t remesh_added;      /* last remesh pass */
+    int64_t remesh_removed;    /* last remesh pass */
+    int64_t small_loops_removed;
+    int64_t error_word;        /* device error flags, 0 when clean */
+} ov_stats;
+
+typedef struct ov_ctx ov_ctx;
+
+/* ---------------------------------------------------------- context API */
+int ov_ctx_create(ov_ctx **out, int device);
+int ov_ctx_destroy(ov_ctx *ctx);
+const char *ov_last_error(const ov_ctx *ctx);
+int ov_set_params(ov_ctx *ctx, const ov_params *p);
+int ov_set_precision(ov_ctx *ctx, int precision);
+/* cudaStream_t the context launches on, as an opaque pointer (for callers that
+   time or order their own work against it). */
+void *ov_ctx_stream(ov_ctx *ctx);
+
+/* Copy a host tangle (reference layout) into HBM.  All node-indexed arrays
+   of `t` are read for t->N slots; box and image set are taken from `t`. */
+int ov_upload_tangle(ov_ctx *ctx, const ov_tangle_state *t);
+/* Copy the selected fields (OV_F_* mask) back into the host tangle. The
+   host arrays must hold at least the context's node capacity (ov_capacity). */
+int ov_download_tangle(ov_ctx *ctx, ov_tangle_state *t, unsigned fields);
+int ov_capacity(const ov_ctx *ctx);
+
+/* ------------------------------------------------------- velocity path */
+/* Tangents and normals of every node: update_tangents_normals (tangle.c:509). */
+int ov_update_tangents_normals(ov_ctx *ctx);
+/* Tree build + fused per-node velocity (LIA, v_s, BH over 1+n_img images,
+   mutual friction): update_velocities (tangle.c:733). */
+int ov_update_velocities(ov_ctx *ctx, double t);
+/* update_tangle (tangle.h:114): tangents/normals then velocities. */
+int ov_update_tangle(ov_ctx *ctx, double t);
+/* One RK4 step (vortex_dynamics.c:50): the three further stage evaluations
+   and the combine, from the velocities already held in the context (k1). */
+int ov_rk4_step(ov_ctx *ctx, double t, double dt);
+/* Exact FP64 direct O(N * (1+n_img)) Biot-Savart velocities of the listed
+   nodes, the `tree == NULL` branch of update_velocity (tangle.c:652-687).
+   Writes n vec3 to vels_out and vs_out (host arrays; either may be NULL). */
+int ov_direct_velocities(ov_ctx *ctx, const int *nodes, int n, double t,
+                         double *vels_out, double *vs_out);
+
+/* ------------------------------------------------------ topology passes */
+int ov_enforce_periodic_boundaries(ov_ctx *ctx);
+int ov_eliminate_small_loops(ov_ctx *ctx);
+/* reconnect (vortex_dynamics.c:186). *nrecs receives the count; if log_k /
+   log_l are non-NULL the (k,l) of each reconnection is written, in order,
+   up to log_cap entries. */
+int ov_reconnect(ov_ctx *ctx, double t, int *nrecs, int *log_k, int *log_l, int log_cap);
+/* remesh (tangle.c:1018). */
+int ov_remesh(ov_ctx *ctx, double min_dist, double max_dist, double t);
+/* smooth (vortex_smooth.c:459): per-loop low-pass filter when use_freq_filter. */
+int ov_smooth(ov_ctx *ctx);
+/* One iteration of the reference's main loop body (main.c:125-141), without
+   injection, frame output and wall clipping: small loops, reconnect, small
+   loops, smooth, periodic wrap, remesh, small loops, update_tangle, rk4_step,
+   periodic wrap. */
+int ov_step(ov_ctx *ctx, double t, double dt);
+
+int ov_get_stats(const ov_ctx *ctx, ov_stats *out);
+
+/* -------------------------------------------------------------- timing */
+/* CUDA-event timing on the context's stream (for benchmarks). */
+int ov_timer_start(ov_ctx *ctx);
+int ov_timer_stop(ov_ctx *ctx, float *ms);   /* synchronizes */
+/* Write `bytes` of junk into a device buffer owned by the context (L2 flush). */
+int ov_flush_l2(ov_ctx *ctx, size_t bytes);
+int ov_synchronize(ov_ctx *ctx);
+/* Number of kernels this context launched since creation. */
+int64_t ov_kernel_launches(const ov_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OPENVORT_GPU_H */

@@ -1,0 +1,164 @@
+"""ctypes mirror of the C ABI (include/ov_tangle.h, include/openvort_gpu.h).
+
+The tangle layout is OpenVort's ``struct tangle_state`` (include/tangle.h:47-66
+of the reference); parameters are its process globals
+(include/vortex_constants.h:11-60) gathered into one struct.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import itertools
+
+import numpy as np
+
+OV_EMPTY, OV_FREE, OV_PINNED, OV_PINNED_SLIP = -1, 0, 1, 2
+OV_WALL_OPEN, OV_WALL_PERIODIC, OV_WALL_MIRROR = 0, 1, 2
+OV_NO_FLOW, OV_SIMPLE, OV_DECREASING = 0, 1, 2
+OV_PREC_FP64, OV_PREC_MIXED = 0, 1
+OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS, OV_F_TOPOLOGY, OV_F_ALL = 1, 2, 4, 8, 16, 32, 63
+
+STATUS_NAMES = {
+    0: "OV_OK", 1: "OV_ERR_ARG", 2: "OV_ERR_CUDA", 3: "OV_ERR_ALLOC", 4: "OV_ERR_DEPTH",
+    5: "OV_ERR_STACK", 6: "OV_ERR_NAN", 7: "OV_ERR_TIMEOUT", 8: "OV_ERR_TOPOLOGY",
+    9: "OV_ERR_NODEVICE", 10: "OV_ERR_STATE",
+}
+
+
+class Vec3(C.Structure):
+    _fields_ = [("p", C.c_double * 3)]
+
+
+class Neighbour(C.Structure):
+    _fields_ = [("forward", C.c_int), ("reverse", C.c_int)]
+
+
+class NodeStatus(C.Structure):
+    _fields_ = [("status", C.c_int), ("pin_wall", C.c_int)]
+
+
+class DomainBox(C.Structure):
+    _fields_ = [("bottom_left_back", Vec3), ("top_right_front", Vec3), ("wall", C.c_int * 6)]
+
+
+class ImageTangle(C.Structure):
+    _fields_ = [("shift", C.c_int * 3), ("reflect", C.c_int * 3), ("number_of_reflects", C.c_int)]
+
+
+class BoundaryImages(C.Structure):
+    _fields_ = [("images", C.POINTER(ImageTangle)), ("n", C.c_int)]
+
+
+class TangleState(C.Structure):
+    _fields_ = [
+        ("vnodes", C.POINTER(Vec3)), ("vels", C.POINTER(Vec3)), ("vs", C.POINTER(Vec3)),
+        ("tangents", C.POINTER(Vec3)), ("normals", C.POINTER(Vec3)),
+        ("recalculate", C.POINTER(C.c_int)), ("connections", C.POINTER(Neighbour)),
+        ("status", C.POINTER(NodeStatus)), ("box", DomainBox), ("bimg", BoundaryImages),
+        ("N", C.c_int), ("next_empty", C.c_int), ("total_empty", C.c_int),
+    ]
+
+
+class ExtVel(C.Structure):
+    _fields_ = [("type", C.c_int), ("strength", C.c_double), ("time_of_linear_decrease", C.c_double),
+                ("starting_strength", C.c_double), ("direction", Vec3)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("kappa", C.c_double), ("vortex_width", C.c_double), ("alpha", C.c_double),
+        ("alpha_p", C.c_double), ("use_mutual_friction", C.c_int), ("use_bh", C.c_int),
+        ("bh_resolution", C.c_double), ("vn", ExtVel), ("vs", ExtVel), ("vb", ExtVel),
+        ("dl_min", C.c_double), ("dl_max", C.c_double), ("rec_dist", C.c_double),
+        ("reconnection_angle_cutoff", C.c_double), ("small_loop_cutoff", C.c_int),
+        ("use_freq_filter", C.c_int), ("freq_to_cutoff", C.c_double), ("num_threads", C.c_int),
+        ("pin_mode", C.c_int),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "node_evals", "cells", "max_depth", "visits", "accepts", "warp_steps", "fp64_fallbacks",
+        "near_field_fp64", "out_of_root", "reconnections", "remesh_added", "remesh_removed",
+        "small_loops_removed", "error_word")]
+
+
+assert C.sizeof(TangleState) == 168 and C.sizeof(DomainBox) == 72 and C.sizeof(ExtVel) == 56
+
+
+def image_shifts(n_images: int) -> list[tuple[int, int, int]]:
+    """Periodic image shifts in the reference's table order.
+
+    periodic_6/18/26 (src/boundary_images.c:13-72) list the shifts of
+    {-1,0,1}^3 minus the origin with at most 1, 2 or 3 non-zero entries, in
+    lexicographic order; ``0`` gives open boundaries.
+    """
+    maxnz = {0: 0, 6: 1, 18: 2, 26: 3}[n_images]
+    out = [s for s in itertools.product((-1, 0, 1), repeat=3) if 0 < sum(map(abs, s)) <= maxnz]
+    assert len(out) == n_images
+    return out
+
+
+def image_table(n_images: int):
+    """ctypes array of ImageTangle for a periodic image set (kept alive by caller)."""
+    arr = (ImageTangle * max(n_images, 1))()
+    for i, s in enumerate(image_shifts(n_images)):
+        arr[i].shift[:] = s
+        arr[i].reflect[:] = (-1, -1, -1)
+        arr[i].number_of_reflects = 0
+    return arr
+
+
+def make_params(**kw) -> Params:
+    """Reference defaults (src/initial_conditions.c:12-91) overridden by kw.
+
+    Flow keywords: ``vn=(type, strength, (dx,dy,dz))`` and likewise vs, vb.
+    """
+    p = Params()
+    p.kappa = 9.97e-4
+    p.vortex_width = 1e-8
+    p.alpha = 0.034
+    p.alpha_p = 1.383e-2
+    p.use_mutual_friction = 1
+    p.use_bh = 1
+    p.bh_resolution = 0.4
+    _set_flow(p.vn, (OV_SIMPLE, 10.493799, (1.0, 0.0, 0.0)))
+    _set_flow(p.vs, (OV_SIMPLE, 0.493799, (-1.0, 0.0, 0.0)))
+    _set_flow(p.vb, (OV_NO_FLOW, 0.0, (0.0, 0.0, 0.0)))
+    p.dl_min = 0.5e-3
+    p.dl_max = 1.5e-3
+    p.rec_dist = 4e-4
+    p.reconnection_angle_cutoff = 5.0 * np.pi / 180.0
+    p.small_loop_cutoff = 5
+    p.use_freq_filter = 1
+    p.freq_to_cutoff = 4.0 / 5
+    p.num_threads = 1
+    p.pin_mode = OV_PINNED
+    for k, v in kw.items():
+        if k in ("vn", "vs", "vb"):
+            _set_flow(getattr(p, k), v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def _set_flow(ev: ExtVel, spec):
+    typ, strength, direction = spec[:3]
+    ev.type = int(typ)
+    ev.strength = float(strength)
+    ev.direction.p[:] = [float(x) for x in direction]
+    ev.time_of_linear_decrease = float(spec[3]) if len(spec) > 3 else 0.0
+    ev.starting_strength = float(spec[4]) if len(spec) > 4 else 0.0
+
+
+def vec3_view(ptr, n: int) -> np.ndarray:
+    """(n,3) float64 numpy view on a C array of vec3."""
+    if n == 0:
+        return np.zeros((0, 3))
+    return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_double)), shape=(n, 3))
+
+
+def int_view(ptr, n: int, width: int = 1) -> np.ndarray:
+    if n == 0:
+        return np.zeros((0, width) if width > 1 else (0,), dtype=np.int32)
+    shape = (n, width) if width > 1 else (n,)
+    return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_int)), shape=shape)

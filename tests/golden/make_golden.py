@@ -1,0 +1,149 @@
+"""Generate the golden vectors in tests/golden/ from OpenVort itself.
+
+Runs the reference compiled from its own sources (oracle/Makefile, target
+``ref``: needs the OpenVort checkout, so this script runs where that exists)
+and stores inputs and outputs as small .npz files.  The GPU machine has no
+reference checkout; there the tests compare against these files and against
+the C restatement (oracle/ov_oracle.c), which these files also pin.
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from openvort_gb300 import workloads as W  # noqa: E402
+from oracle.pyoracle import Checker, build  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def params_dict(p):
+    return {f: getattr(p, f) for f, _ in p._fields_ if f not in ("vn", "vs", "vb")} | {
+        f"{k}_{g}": (list(getattr(getattr(p, k), g).p) if g == "direction" else getattr(getattr(p, k), g))
+        for k in ("vn", "vs", "vb") for g in ("type", "strength", "direction")}
+
+
+def save(name, **arrays):
+    path = os.path.join(OUT, name)
+    np.savez_compressed(path, **arrays)
+    print("wrote", path, f"{os.path.getsize(path) / 1024:.1f} KiB")
+
+
+def tangle_arrays(ht):
+    return dict(pos=ht.pos, conn=ht.conn, status=ht.stat, box_lo=ht.box_lo, box_hi=ht.box_hi,
+                n_images=ht.n_images)
+
+
+def ref_step(c, t, time, dt):
+    """main.c:125-141 for a periodic box without injection or smoothing."""
+    c.eliminate_small_loops(t)
+    n = c.reconnect(t, 0.0)
+    c.eliminate_small_loops(t)
+    c.enforce_periodic(t)
+    c.remesh(t, c.params.dl_min, c.params.dl_max, 0.0)
+    c.eliminate_small_loops(t)
+    c.update_tangle(t, time)
+    c.rk4_step(t, time, dt)
+    c.enforce_periodic(t)
+    return n
+
+
+def main():
+    build(ref=True)
+    ref = Checker("reference")
+
+    # 1. BH velocities (theta 0.4, 0.3 and 0.5) and direct sums on a small random-walk tangle
+    ht = W.random_walk_tangle(16, 64, D=0.1, seed=3)
+    p = W.config_params("rw")
+    p.num_threads = 8
+    out = tangle_arrays(ht)
+    for theta in (0.3, 0.4, 0.5):
+        p.bh_resolution = theta
+        ref.set_params(p)
+        t = ref.tangle(ht)
+        ref.update_tangle(t, 0.0)
+        tag = f"{int(theta * 10)}"
+        out[f"vels_{tag}"] = t.copy("vels")
+        out[f"vs_{tag}"] = t.copy("vs")
+        if theta == 0.4:
+            out["tangents"] = t.copy("tangents")
+            out["normals"] = t.copy("normals")
+            nodes = np.arange(0, ht.n, 7, dtype=np.int32)
+            dv, dvs = ref.direct_velocities(t, nodes, 0.0)
+            out["direct_nodes"], out["direct_vels"], out["direct_vs"] = nodes, dv, dvs
+        t.free()
+    p.bh_resolution = 0.4
+    save("rw16x64.npz", **out)
+
+    # 2. Ring configuration (8 rings, 496 nodes): 20 full steps with the event counts
+    ht = W.ring_tangle()
+    p = W.config_params("rings8")
+    p.num_threads = 8
+    ref.set_params(p)
+    t = ref.tangle(ht)
+    dt = 5e-5
+    traj, recs = [], []
+    v0 = None
+    for s in range(20):
+        recs.append(ref_step(ref, t, s * dt, dt))
+        if s == 0:
+            v0 = t.copy("vels")
+        traj.append(t.copy("pos"))
+    keep = [0, 4, 9, 19]
+    save("rings8_steps.npz", **tangle_arrays(ht), traj=np.stack(traj)[keep], traj_steps=np.array(keep),
+         recs=np.array(recs),
+         vels_step0=v0, conn_final=t.copy("conn"), status_final=t.copy("status"), dt=dt)
+    t.free()
+
+    # 3. Dense random walk: reconnections and remeshing in the first steps
+    ht = W.random_walk_tangle(24, 64, D=0.03, seed=5)
+    p = W.config_params("rw")
+    p.num_threads = 8
+    ref.set_params(p)
+    t = ref.tangle(ht)
+    recs, conns, stats, poss = [], [], [], []
+    for s in range(4):
+        recs.append(ref_step(ref, t, s * dt, dt))
+        conns.append(t.copy("conn"))
+        stats.append(t.copy("status"))
+        poss.append(t.copy("pos"))
+    save("dense_steps.npz", **tangle_arrays(ht), recs=np.array(recs), conn_steps=np.stack(conns),
+         status_steps=np.stack(stats), traj=np.stack(poss), dt=dt)
+    t.free()
+
+    # 4. Remesh in both directions (coarse walk -> inserts, fine walk -> removals)
+    out = {}
+    for tag, delta in (("coarse", 2.2e-3), ("fine", 3e-4)):
+        ht = W.random_walk_tangle(8, 48, D=0.1, delta=delta, seed=9)
+        ref.set_params(W.config_params("rw"))
+        t = ref.tangle(ht)
+        ref.remesh(t, 5e-4, 1.5e-3, 0.0)
+        for k, v in tangle_arrays(ht).items():
+            out[f"{tag}_in_{k}"] = v
+        out[f"{tag}_pos"], out[f"{tag}_conn"], out[f"{tag}_status"] = t.copy("pos"), t.copy("conn"), t.copy("status")
+        out[f"{tag}_N"] = t.n
+        t.free()
+    save("remesh.npz", **out)
+
+    # 5. Config-B-sized tangle: velocities of a fixed node subsample from the full BH evaluation
+    ht = W.random_walk_tangle(256, 256, D=0.1, seed=1)
+    p = W.config_params("rw")
+    p.num_threads = 8
+    ref.set_params(p)
+    t = ref.tangle(ht)
+    ref.update_tangle(t, 0.0)
+    sub = np.arange(0, ht.n, 97, dtype=np.int32)
+    save("rw256x256_sub.npz", nodes=sub, pos_sub=ht.pos[sub], vels=t.copy("vels")[sub], vs=t.copy("vs")[sub],
+         pos_checksum=np.array([ht.pos.sum(), (ht.pos ** 2).sum()]))
+    t.free()
+
+
+if __name__ == "__main__":
+    main()
