@@ -135,6 +135,11 @@ int ov_upload_tangle(ov_ctx *ctx, const ov_tangle_state *t);
    host arrays must hold at least the context's node capacity (ov_capacity). */
 int ov_download_tangle(ov_ctx *ctx, ov_tangle_state *t, unsigned fields);
 int ov_capacity(const ov_ctx *ctx);
+/* Upload only the OV_F_* fields selected (positions and topology are all
+   update_tangle needs; update_velocities also reads tangents/normals).  The
+   first upload into a context, or one that changes the node count, always
+   transfers positions and topology as well. */
+int ov_upload_tangle_fields(ov_ctx *ctx, const ov_tangle_state *t, unsigned fields);
 
 /* ------------------------------------------------------- velocity path */
 /* Tangents and normals of every node: update_tangents_normals (tangle.c:509). */
@@ -181,6 +186,15 @@ int ov_flush_l2(ov_ctx *ctx, size_t bytes);
 int ov_synchronize(ov_ctx *ctx);
 /* Number of kernels this context launched since creation. */
 int64_t ov_kernel_launches(const ov_ctx *ctx);
+/* Per-phase device times of the last velocity evaluation, recorded with CUDA
+   events when phase timing is on: ms[0] tangents, ms[1] tree build,
+   ms[2] traversal. */
+int ov_set_phase_timing(ov_ctx *ctx, int on);
+int ov_phase_times(ov_ctx *ctx, float ms[3]);
+/* Measured multiply-add throughput of this GPU in TFLOP/s for FP64
+   (precision OV_PREC_FP64) or FP32 (OV_PREC_MIXED): the roofline peak of
+   the traversal, which is FMA-pipe bound. */
+int ov_measure_fma_peak(ov_ctx *ctx, int precision, double *tflops);
 
 #ifdef __cplusplus
 }

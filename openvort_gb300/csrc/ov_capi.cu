@@ -1,0 +1,556 @@
+// ov_capi.cu - the C ABI of libovgpu (include/openvort_gpu.h).
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "ov_internal.cuh"
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+int ov_fail(ov_ctx *c, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+// vec3_normalize (vec3_math.c:208-217): multiply by the reciprocal length.
+static void normalize_ref(const double in[3], double out[3])
+{
+    double s = 0;
+    s += in[0] * in[0];
+    s += in[1] * in[1];
+    s += in[2] * in[2];
+    if (in[0] == 0 && in[1] == 0 && in[2] == 0) {
+        out[0] = in[0]; out[1] = in[1]; out[2] = in[2];
+        return;
+    }
+    double inv = 1 / sqrt(s);
+    for (int a = 0; a < 3; ++a) out[a] = in[a] * inv;
+}
+
+DevParams ov_dev_params(const ov_params &p)
+{
+    DevParams d;
+    memset(&d, 0, sizeof d);
+    d.kappa = p.kappa;
+    d.a0 = p.vortex_width;
+    d.alpha = p.alpha;
+    d.alpha_p = p.alpha_p;
+    d.theta = p.bh_resolution;
+    d.friction = p.use_mutual_friction;
+    d.use_bh = p.use_bh;
+    const ov_ext_vel *src[3] = {&p.vn, &p.vs, &p.vb};
+    int *types[3] = {&d.vn_type, &d.vs_type, &d.vb_type};
+    double *dirs[3] = {d.vn_dir, d.vs_dir, d.vb_dir};
+    double *s0[3] = {&d.vn_s0, &d.vs_s0, &d.vb_s0}, *s1[3] = {&d.vn_s1, &d.vs_s1, &d.vb_s1};
+    double *tld[3] = {&d.vn_tld, &d.vs_tld, &d.vb_tld};
+    for (int i = 0; i < 3; ++i) {
+        *types[i] = src[i]->type;
+        normalize_ref(src[i]->direction.p, dirs[i]);
+        *s0[i] = src[i]->starting_strength;
+        *s1[i] = src[i]->strength;
+        *tld[i] = src[i]->time_of_linear_decrease;
+    }
+    return d;
+}
+
+extern "C" {
+
+void ov_params_default(ov_params *p)
+{
+    memset(p, 0, sizeof *p);
+    p->kappa = 9.97e-4;
+    p->vortex_width = 1e-8;
+    p->alpha = 0.034;
+    p->alpha_p = 1.383e-2;
+    p->use_mutual_friction = 1;
+    p->use_bh = 1;
+    p->bh_resolution = 0.4;
+    p->vn.type = OV_SIMPLE;
+    p->vn.strength = 10.493799;
+    p->vn.direction.p[0] = 1.0;
+    p->vs.type = OV_SIMPLE;
+    p->vs.strength = 0.493799;
+    p->vs.direction.p[0] = -1.0;
+    p->vb.type = OV_NO_FLOW;
+    p->dl_min = 0.5e-3;
+    p->dl_max = 1.5e-3;
+    p->rec_dist = 4e-4;
+    p->reconnection_angle_cutoff = 5.0 * M_PI / 180.0;
+    p->small_loop_cutoff = 5;
+    p->use_freq_filter = 1;
+    p->freq_to_cutoff = 4.0 / 5;
+    p->num_threads = 1;
+    p->pin_mode = OV_PINNED;
+}
+
+int ov_ctx_create(ov_ctx **out, int device)
+{
+    if (!out) return OV_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return OV_ERR_NODEVICE;
+    }
+    if (device < 0 || device >= n) return OV_ERR_ARG;
+    ov_ctx *c = new ov_ctx();
+    c->device = device;
+    ov_params_default(&c->params);
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+        delete c;
+        return OV_ERR_CUDA;
+    }
+    *out = c;
+    return OV_OK;
+}
+
+static void free_nodes(NodeArrays &a)
+{
+    double *ps[] = {a.x, a.y, a.z, a.tx, a.ty, a.tz, a.nx, a.ny, a.nz, a.vx, a.vy, a.vz, a.sx, a.sy, a.sz};
+    for (double *p : ps)
+        if (p) cudaFree(p);
+    a = NodeArrays{};
+}
+
+int ov_ctx_destroy(ov_ctx *c)
+{
+    if (!c) return OV_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    free_nodes(c->node);
+    for (auto &s : c->stage) free_nodes(s);
+    ov_tree_free(c->tree);
+    int *is[] = {c->fwd, c->rev, c->status, c->pin, c->dnodes};
+    for (int *p : is)
+        if (p) cudaFree(p);
+    if (c->dsum) cudaFree(c->dsum);
+    if (c->flush_buf) cudaFree(c->flush_buf);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->rk4_exec) cudaGraphExecDestroy(c->rk4_exec);
+    for (int i = 0; i < 4; ++i)
+        if (c->ph[i]) cudaEventDestroy(c->ph[i]);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return OV_OK;
+}
+
+const char *ov_last_error(const ov_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int ov_set_params(ov_ctx *c, const ov_params *p)
+{
+    if (!c || !p) return OV_ERR_ARG;
+    c->params = *p;
+    return OV_OK;
+}
+
+int ov_set_precision(ov_ctx *c, int precision)
+{
+    if (!c || (precision != OV_PREC_FP64 && precision != OV_PREC_MIXED)) return OV_ERR_ARG;
+    c->precision = precision;
+    return OV_OK;
+}
+
+void *ov_ctx_stream(ov_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int ov_capacity(const ov_ctx *c) { return c ? c->cap : 0; }
+
+}  // extern "C"
+
+static int alloc_nodes(ov_ctx *c, NodeArrays &a, int cap)
+{
+    size_t b = (size_t)cap * sizeof(double);
+    double **ps[] = {&a.x, &a.y, &a.z, &a.tx, &a.ty, &a.tz, &a.nx, &a.ny, &a.nz, &a.vx, &a.vy, &a.vz,
+                     &a.sx, &a.sy, &a.sz};
+    for (double **p : ps) {
+        OV_CUDA(c, cudaMalloc(p, b));
+        OV_CUDA(c, cudaMemsetAsync(*p, 0, b, c->stream));
+    }
+    return OV_OK;
+}
+
+static int ensure_capacity(ov_ctx *c, int cap)
+{
+    if (cap <= c->cap && c->node.x) return OV_OK;
+    cudaStreamSynchronize(c->stream);
+    free_nodes(c->node);
+    for (auto &s : c->stage) free_nodes(s);
+    int *is[] = {c->fwd, c->rev, c->status, c->pin};
+    for (int *p : is)
+        if (p) cudaFree(p);
+    if (c->rk4_exec) { cudaGraphExecDestroy(c->rk4_exec); c->rk4_exec = nullptr; }
+    int r;
+    if ((r = alloc_nodes(c, c->node, cap))) return r;
+    for (auto &s : c->stage)
+        if ((r = alloc_nodes(c, s, cap))) return r;
+    OV_CUDA(c, cudaMalloc(&c->fwd, (size_t)cap * 4));
+    OV_CUDA(c, cudaMalloc(&c->rev, (size_t)cap * 4));
+    OV_CUDA(c, cudaMalloc(&c->status, (size_t)cap * 4));
+    OV_CUDA(c, cudaMalloc(&c->pin, (size_t)cap * 4));
+    if ((r = ov_tree_reserve(c, cap))) return r;
+    c->cap = cap;
+    return OV_OK;
+}
+
+static int ensure_stage(ov_ctx *c, size_t bytes)
+{
+    if (c->h_stage_bytes >= bytes) return OV_OK;
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    c->h_stage = nullptr;
+    OV_CUDA(c, cudaMallocHost(&c->h_stage, bytes));
+    c->h_stage_bytes = bytes;
+    return OV_OK;
+}
+
+static void set_geometry(ov_ctx *c, const ov_domain_box &box, const ov_boundary_images &bimg)
+{
+    Geometry &g = c->geo;
+    memset(&g, 0, sizeof g);
+    for (int a = 0; a < 3; ++a) {
+        g.lo[a] = box.bottom_left_back.p[a];
+        g.hi[a] = box.top_right_front.p[a];
+        g.L[a] = g.hi[a] - g.lo[a];
+    }
+    for (int f = 0; f < 6; ++f) g.wall[f] = box.wall[f];
+    g.periodic[0] = box.wall[OV_LEFT] == OV_WALL_PERIODIC;
+    g.periodic[1] = box.wall[OV_BACK] == OV_WALL_PERIODIC;
+    g.periodic[2] = box.wall[OV_DOWN] == OV_WALL_PERIODIC;
+    g.n_img = std::min(bimg.n, OV_MAX_IMAGES);
+    for (int j = 0; j < g.n_img && bimg.images; ++j) {
+        for (int a = 0; a < 3; ++a) {
+            g.shift[j][a] = bimg.images[j].shift[a];
+            g.reflect[j][a] = bimg.images[j].reflect[a];
+        }
+        g.nreflect[j] = std::min(std::max(bimg.images[j].number_of_reflects, 0), 3);
+    }
+    // grid step of the mixed path: a power of two with every coordinate the
+    // traversal meets (box, one period either side) below 2^22 steps
+    double m = 0;
+    for (int a = 0; a < 3; ++a) m = std::max(m, std::max(fabs(g.lo[a]), fabs(g.hi[a])) + 2 * fabs(g.L[a]));
+    int e = (int)ceil(log2(m > 0 ? m : 1.0));
+    c->grid_h = ldexp(1.0, e - 22);
+}
+
+extern "C" {
+
+int ov_upload_tangle(ov_ctx *c, const ov_tangle_state *t) { return ov_upload_tangle_fields(c, t, OV_F_ALL); }
+
+int ov_upload_tangle_fields(ov_ctx *c, const ov_tangle_state *t, unsigned fields)
+{
+    if (!c || !t || t->N < 0) return OV_ERR_ARG;
+    cudaSetDevice(c->device);
+    int n = t->N;
+    int r;
+    int old_cap = c->cap;
+    if ((r = ensure_capacity(c, std::max(n, 1)))) return r;
+    if (!c->uploaded || c->cap != old_cap || c->n_live != n) fields |= OV_F_POS | OV_F_TOPOLOGY;
+    c->n_live = n;   // slots past t->N (a smaller tangle in a larger context) are EMPTY
+    set_geometry(c, t->box, t->bimg);
+    size_t cap = (size_t)c->cap;
+    if ((r = ensure_stage(c, cap * 3 * sizeof(double) * 5 + cap * 4 * sizeof(int)))) return r;
+    double *h = c->h_stage;
+    int *hi = (int *)(h + 15 * cap);
+    // positions, vels, vs, tangents, normals: AoS -> SoA
+    const ov_vec3 *src[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
+    const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
+    double *dd[15] = {c->node.x, c->node.y, c->node.z, c->node.vx, c->node.vy, c->node.vz,
+                      c->node.sx, c->node.sy, c->node.sz, c->node.tx, c->node.ty, c->node.tz,
+                      c->node.nx, c->node.ny, c->node.nz};
+    c->last_h2d = 0;
+    for (int f = 0; f < 5; ++f) {
+        if (!(fields & bits[f])) continue;
+        double *dst = h + 3 * cap * f;
+        for (int a = 0; a < 3; ++a)
+            for (size_t k = 0; k < cap; ++k) dst[a * cap + k] = (src[f] && (int)k < n) ? src[f][k].p[a] : 0.0;
+        for (int a = 0; a < 3; ++a)
+            OV_CUDA(c, cudaMemcpyAsync(dd[3 * f + a], dst + a * cap, cap * sizeof(double), cudaMemcpyHostToDevice,
+                                       c->stream));
+        c->last_h2d += 3 * cap * sizeof(double);
+    }
+    if (fields & OV_F_TOPOLOGY) {
+        for (int k = 0; k < n; ++k) {
+            int f = t->connections[k].forward, b = t->connections[k].reverse, st = t->status[k].status;
+            if (f < -1 || f >= n || b < -1 || b >= n || st < OV_EMPTY || st > OV_PINNED_SLIP)
+                return ov_fail(c, OV_ERR_TOPOLOGY, "node %d: connections (%d,%d) / status %d out of range", k, f, b, st);
+        }
+        for (size_t k = 0; k < cap; ++k) {
+            bool in = (int)k < n;
+            hi[k] = in ? t->connections[k].forward : -1;
+            hi[cap + k] = in ? t->connections[k].reverse : -1;
+            hi[2 * cap + k] = in ? t->status[k].status : OV_EMPTY;
+            hi[3 * cap + k] = in ? t->status[k].pin_wall : OV_NOT_A_FACE;
+        }
+        int *di[4] = {c->fwd, c->rev, c->status, c->pin};
+        for (int i = 0; i < 4; ++i)
+            OV_CUDA(c, cudaMemcpyAsync(di[i], hi + i * cap, cap * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        c->last_h2d += 4 * cap * sizeof(int);
+    }
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->uploaded = true;
+    return OV_OK;
+}
+
+int ov_download_tangle(ov_ctx *c, ov_tangle_state *t, unsigned fields)
+{
+    if (!c || !t) return OV_ERR_ARG;
+    if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
+    int n = std::min(t->N, c->cap);
+    size_t cap = (size_t)c->cap;
+    int r;
+    if ((r = ensure_stage(c, cap * 3 * sizeof(double) * 5 + cap * 4 * sizeof(int)))) return r;
+    double *h = c->h_stage;
+    int *hi = (int *)(h + 15 * cap);
+    const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
+    double *dd[15] = {c->node.x, c->node.y, c->node.z, c->node.vx, c->node.vy, c->node.vz,
+                      c->node.sx, c->node.sy, c->node.sz, c->node.tx, c->node.ty, c->node.tz,
+                      c->node.nx, c->node.ny, c->node.nz};
+    for (int f = 0; f < 5; ++f) {
+        if (!(fields & bits[f])) continue;
+        for (int a = 0; a < 3; ++a)
+            OV_CUDA(c, cudaMemcpyAsync(h + (3 * f + a) * cap, dd[3 * f + a], cap * sizeof(double),
+                                       cudaMemcpyDeviceToHost, c->stream));
+    }
+    int *di[4] = {c->fwd, c->rev, c->status, c->pin};
+    if (fields & OV_F_TOPOLOGY)
+        for (int i = 0; i < 4; ++i)
+            OV_CUDA(c, cudaMemcpyAsync(hi + i * cap, di[i], cap * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    ov_vec3 *dst[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
+    for (int f = 0; f < 5; ++f) {
+        if (!(fields & bits[f]) || !dst[f]) continue;
+        const double *s = h + 3 * cap * f;
+        for (int k = 0; k < n; ++k)
+            for (int a = 0; a < 3; ++a) dst[f][k].p[a] = s[a * cap + k];
+    }
+    if (fields & OV_F_TOPOLOGY) {
+        for (int k = 0; k < n; ++k) {
+            t->connections[k].forward = hi[k];
+            t->connections[k].reverse = hi[cap + k];
+            t->status[k].status = hi[2 * cap + k];
+            t->status[k].pin_wall = hi[3 * cap + k];
+        }
+    }
+    return OV_OK;
+}
+
+}  // extern "C"
+
+static int check_ready(ov_ctx *c)
+{
+    if (!c) return OV_ERR_ARG;
+    if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
+    cudaSetDevice(c->device);
+    return OV_OK;
+}
+
+// Read back the device counters of the last build/evaluation into ctx->stats.
+static int collect_stats(ov_ctx *c, bool sync)
+{
+    int host[TC_WORDS];
+    if (sync) OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    OV_CUDA(c, cudaMemcpy(host, c->tree.counters, sizeof host, cudaMemcpyDeviceToHost));
+    unsigned long long *s64 = (unsigned long long *)(host + TC_STAT64);
+    c->stats.node_evals = host[TC_NNE];
+    c->stats.cells = host[TC_NCELL];
+    c->stats.max_depth = host[TC_MAXDEPTH];
+    c->stats.out_of_root = host[TC_OUT];
+    c->stats.visits = (int64_t)s64[ST_VISITS];
+    c->stats.accepts = (int64_t)s64[ST_ACCEPTS];
+    c->stats.warp_steps = (int64_t)s64[ST_STEPS];
+    c->stats.fp64_fallbacks = (int64_t)s64[ST_FALLBACK];
+    c->stats.near_field_fp64 = (int64_t)s64[ST_NEAR64];
+    c->stats.error_word = host[TC_ERR];
+    return OV_OK;
+}
+
+static int error_from_word(ov_ctx *c)
+{
+    int w = (int)c->stats.error_word;
+    if (!w) return OV_OK;
+    if (w & OV_EW_NAN) return ov_fail(c, OV_ERR_NAN, "non-finite node position (error word 0x%x)", w);
+    if (w & OV_EW_WALK) return ov_fail(c, OV_ERR_TOPOLOGY, "filament walk reached an EMPTY slot (error word 0x%x)", w);
+    if (w & OV_EW_ITER) return ov_fail(c, OV_ERR_STACK, "traversal iteration bound exceeded (error word 0x%x)", w);
+    if (w & OV_EW_DEPTH)
+        return ov_fail(c, OV_ERR_DEPTH, "two nodes share a cell at tree level %d (error word 0x%x)", OV_MAX_LEVEL, w);
+    return OV_OK;   // sliver drops are counted, not fatal
+}
+
+// tangents + tree + traversal of one tangle on stream s (no host sync)
+static int eval_async(ov_ctx *c, NodeArrays &na, double t, bool tangents, cudaStream_t s)
+{
+    bool ph = c->phase_timing;
+    if (ph) OV_CUDA(c, cudaEventRecord(c->ph[0], s));
+    if (tangents) ov_launch_tangents(c, na, s);
+    if (ph) OV_CUDA(c, cudaEventRecord(c->ph[1], s));
+    int r = ov_tree_build(c, na, s);
+    if (r) return r;
+    if (ph) OV_CUDA(c, cudaEventRecord(c->ph[2], s));
+    ov_launch_velocities(c, na, t, c->precision, s);
+    if (ph) OV_CUDA(c, cudaEventRecord(c->ph[3], s));
+    OV_CUDA(c, cudaGetLastError());
+    return OV_OK;
+}
+
+extern "C" {
+
+int ov_update_tangents_normals(ov_ctx *c)
+{
+    int r = check_ready(c);
+    if (r) return r;
+    OV_CUDA(c, cudaMemsetAsync(c->tree.counters, 0, TC_WORDS * 4, c->stream));
+    ov_launch_tangents(c, c->node, c->stream);
+    OV_CUDA(c, cudaGetLastError());
+    if ((r = collect_stats(c, true))) return r;
+    return error_from_word(c);
+}
+
+// Evaluate, growing the cell storage and re-running when the tree did not fit.
+static int eval_sync(ov_ctx *c, NodeArrays &na, double t, bool tangents)
+{
+    int r;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        if ((r = eval_async(c, na, t, tangents, c->stream))) return r;
+        if ((r = collect_stats(c, true))) return r;
+        if (!(c->stats.error_word & OV_EW_CELLS)) return error_from_word(c);
+        int need = 0;
+        OV_CUDA(c, cudaMemcpy(&need, c->tree.counters + TC_NEED, 4, cudaMemcpyDeviceToHost));
+        if ((r = ov_tree_reserve_cells(c, need + need / 4 + 64))) return r;
+    }
+    return ov_fail(c, OV_ERR_ALLOC, "cell storage could not be sized");
+}
+
+int ov_update_velocities(ov_ctx *c, double t)
+{
+    int r = check_ready(c);
+    if (r) return r;
+    return eval_sync(c, c->node, t, false);
+}
+
+int ov_update_tangle(ov_ctx *c, double t)
+{
+    int r = check_ready(c);
+    if (r) return r;
+    return eval_sync(c, c->node, t, true);
+}
+
+// RK4 (vortex_dynamics.c:50-119) from k1 = the context's current vels.
+int ov_rk4_step(ov_ctx *c, double t, double dt)
+{
+    int r = check_ready(c);
+    if (r) return r;
+    cudaStream_t s = c->stream;
+    const double *vin[3][3] = {{c->node.vx, c->node.vy, c->node.vz},
+                               {c->stage[0].vx, c->stage[0].vy, c->stage[0].vz},
+                               {c->stage[1].vx, c->stage[1].vy, c->stage[1].vz}};
+    const double tt[3] = {t + dt / 2, t + dt / 2, t + dt};
+    int64_t err = 0;
+    for (int k = 0; k < 3; ++k) {
+        ov_launch_euler(c, c->node, vin[k][0], vin[k][1], vin[k][2], dt / 2, c->stage[k], s);
+        if ((r = eval_sync(c, c->stage[k], tt[k], true))) return r;
+        err |= c->stats.error_word;
+    }
+    ov_launch_rk4_combine(c, dt, s);
+    OV_CUDA(c, cudaGetLastError());
+    OV_CUDA(c, cudaStreamSynchronize(s));
+    c->stats.error_word = err;
+    return error_from_word(c);
+}
+
+int ov_direct_velocities(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out)
+{
+    int r = check_ready(c);
+    if (r) return r;
+    if (n < 0 || (n > 0 && !nodes)) return OV_ERR_ARG;
+    for (int i = 0; i < n; ++i)
+        if (nodes[i] < 0 || nodes[i] >= c->cap) return ov_fail(c, OV_ERR_ARG, "node %d out of range", nodes[i]);
+    return ov_direct_sum(c, nodes, n, t, vels_out, vs_out);
+}
+
+int ov_enforce_periodic_boundaries(ov_ctx *c)
+{
+    int r = check_ready(c);
+    if (r) return r;
+    ov_launch_periodic_wrap(c, c->stream);
+    OV_CUDA(c, cudaGetLastError());
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    return OV_OK;
+}
+
+int ov_get_stats(const ov_ctx *c, ov_stats *out)
+{
+    if (!c || !out) return OV_ERR_ARG;
+    *out = c->stats;
+    return OV_OK;
+}
+
+int ov_timer_start(ov_ctx *c)
+{
+    if (!c) return OV_ERR_ARG;
+    OV_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    return OV_OK;
+}
+
+int ov_timer_stop(ov_ctx *c, float *ms)
+{
+    if (!c || !ms) return OV_ERR_ARG;
+    OV_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    OV_CUDA(c, cudaEventSynchronize(c->ev1));
+    OV_CUDA(c, cudaEventElapsedTime(ms, c->ev0, c->ev1));
+    return OV_OK;
+}
+
+int ov_flush_l2(ov_ctx *c, size_t bytes)
+{
+    if (!c) return OV_ERR_ARG;
+    if (c->flush_bytes < bytes) {
+        if (c->flush_buf) cudaFree(c->flush_buf);
+        c->flush_buf = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->flush_buf, bytes));
+        c->flush_bytes = bytes;
+    }
+    static int v = 0;
+    OV_CUDA(c, cudaMemsetAsync(c->flush_buf, (++v) & 0xFF, bytes, c->stream));
+    return OV_OK;
+}
+
+int ov_synchronize(ov_ctx *c)
+{
+    if (!c) return OV_ERR_ARG;
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    return OV_OK;
+}
+
+int64_t ov_kernel_launches(const ov_ctx *c) { return c ? c->launches : 0; }
+
+int ov_set_phase_timing(ov_ctx *c, int on)
+{
+    if (!c) return OV_ERR_ARG;
+    if (on && !c->ph[0])
+        for (int i = 0; i < 4; ++i) OV_CUDA(c, cudaEventCreate(&c->ph[i]));
+    c->phase_timing = on != 0;
+    return OV_OK;
+}
+
+int ov_phase_times(ov_ctx *c, float ms[3])
+{
+    if (!c || !ms) return OV_ERR_ARG;
+    if (!c->phase_timing || !c->ph[0]) return ov_fail(c, OV_ERR_STATE, "phase timing is off");
+    OV_CUDA(c, cudaEventSynchronize(c->ph[3]));
+    for (int i = 0; i < 3; ++i) OV_CUDA(c, cudaEventElapsedTime(&ms[i], c->ph[i], c->ph[i + 1]));
+    return OV_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,275 @@
+// ov_internal.cuh - shared declarations of libovgpu (not part of the C ABI).
+//
+// Device data layout (HBM), per tangle of `cap` node slots:
+//   x,y,z            double[cap]  positions (SoA)
+//   fwd,rev          int[cap]     connections
+//   status,pin       int[cap]     node_status
+//   tx,ty,tz nx,...  double[cap]  tangents / normals (SoA)
+//   vx.. / sx..      double[cap]  vels / vs (SoA)
+// Linear octree (rebuilt per evaluation):
+//   keys,order       u64/int[cap] path keys and node ids, sorted by key
+//   cells            Cell64[ncell] pre-order cells: COM, circulation, Lm,
+//                                  subtree end (`next`) and node count
+//   cells32          Cell32[ncell] FP32 copy for the mixed traversal
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/openvort_gpu.h"
+
+#define OV_MAX_LEVEL 21                 // 3-bit digits below the root: 63 bits
+#define OV_KEY_OUT (0x8000000000000000ull) // node outside the root box (| node id)
+#define OV_KEY_EMPTY (0xFFFFFFFFFFFFFFFFull)
+#define OV_MAX_IMAGES 26
+
+// device error bits (ov_stats.error_word)
+enum {
+    OV_EW_DEPTH = 1,      // two nodes share the deepest cell
+    OV_EW_SLIVER = 2,     // a node fell in a rounding gap between child boxes
+    OV_EW_WALK = 4,       // step_node walked onto an EMPTY slot or looped
+    OV_EW_ITER = 8,       // traversal exceeded its iteration bound
+    OV_EW_NAN = 16,       // non-finite position
+    OV_EW_RUN = 32,       // sort fix-up met a run longer than its bound
+    OV_EW_CELLS = 64      // cell storage too small: host grows it and rebuilds
+};
+
+struct Cell64 {          // 64 bytes, one per cell, pre-order
+    double cx, cy, cz;   // centre of mass (mean position)
+    double qx, qy, qz;   // total circulation (sum of wrapped forward segments)
+    double lm;           // largest side of the cell box
+    int next;            // index of the first cell after this subtree
+    int count;           // nodes in the cell
+};
+
+struct Cell32 {          // 48 bytes: FP32 view for the mixed traversal
+    float gx, gy, gz;    // COM, grid part (multiple of the grid step h)
+    float fx, fy, fz;    // COM, fine part
+    float qx, qy, qz;    // circulation
+    float lm;            // Lm (rounded up)
+    int next;
+    int count;
+};
+
+struct TreeBuf {
+    int cap = 0;
+    uint64_t *keys = nullptr, *keys_alt = nullptr;
+    int *order = nullptr, *order_alt = nullptr;
+    int *cpl = nullptr;          // common prefix length with the next key
+    int *ncell_at = nullptr;     // cells starting at sorted position s
+    int *cell_off = nullptr;     // exclusive scan of ncell_at (+1 for the root)
+    int *scan_tmp = nullptr;
+    int *sort_hist = nullptr;
+    int cap_cells = 0;
+    Cell64 *cells = nullptr;
+    Cell32 *cells32 = nullptr;
+    int *parent = nullptr;
+    int *nchild = nullptr;
+    int *arrive = nullptr;
+    double *csum = nullptr;      // 6 doubles per cell: position sum, circulation sum
+    int *counters = nullptr;     // device scalars, see TreeCounters
+};
+
+// device-side scalars written by the build
+enum TreeCounters {
+    TC_M = 0,          // nodes inside the root box (sorted prefix)
+    TC_NNE,            // non-EMPTY nodes (targets)
+    TC_NCELL,          // cells
+    TC_MAXDEPTH,
+    TC_OUT,            // nodes outside the root box
+    TC_ERR,            // error bits
+    TC_MAXRUN,
+    TC_FALLBACK,       // mixed: guard-band FP64 decisions
+    TC_NEAR64,         // mixed: near-field FP64 interactions
+    TC_NEED,           // cells the tree needs (checked against the storage)
+    TC_COUNT,
+    TC_STAT64 = 16,    // int offset of the 64-bit counters: visits, accepts, warp steps, ...
+    TC_WORDS = 32      // ints allocated (and cleared per build)
+};
+enum { ST_VISITS = 0, ST_ACCEPTS, ST_STEPS, ST_FALLBACK, ST_NEAR64 };
+
+struct Geometry {
+    double lo[3], hi[3], L[3];
+    int periodic[3];             // low wall of the axis is periodic (seg_pwrap)
+    int wall[6];
+    int n_img;
+    int shift[OV_MAX_IMAGES][3];
+    int reflect[OV_MAX_IMAGES][3];
+    int nreflect[OV_MAX_IMAGES];
+};
+
+struct NodeArrays {              // one tangle (or one RK4 stage) in HBM
+    double *x = nullptr, *y = nullptr, *z = nullptr;
+    double *tx = nullptr, *ty = nullptr, *tz = nullptr;
+    double *nx = nullptr, *ny = nullptr, *nz = nullptr;
+    double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+    double *sx = nullptr, *sy = nullptr, *sz = nullptr;
+};
+
+struct DevParams {               // ov_params as the kernels need them
+    double kappa, a0, alpha, alpha_p, theta;
+    int friction, use_bh;
+    int vn_type, vs_type, vb_type;
+    double vn[3], vs[3], vb[3];          // direction * strength for SIMPLE
+    double vn_dir[3], vs_dir[3], vb_dir[3];   // normalised directions
+    double vn_s0, vn_s1, vn_tld, vs_s0, vs_s1, vs_tld, vb_s0, vb_s1, vb_tld;
+};
+
+struct ov_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    ov_params params{};
+    int precision = OV_PREC_FP64;
+    std::string err;
+    int cap = 0;                 // node slots
+    int n_live = 0;              // slots of the uploaded tangle (<= cap)
+    size_t last_h2d = 0;         // bytes of the last upload
+    bool uploaded = false;
+    Geometry geo{};
+    int *fwd = nullptr, *rev = nullptr, *status = nullptr, *pin = nullptr;
+    NodeArrays node;             // the tangle
+    NodeArrays stage[3];         // RK4 stage tangles (positions, tangents, vels)
+    TreeBuf tree;
+    int64_t launches = 0;
+    ov_stats stats{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    void *flush_buf = nullptr;
+    size_t flush_bytes = 0;
+    // host mirrors for the sequential topology passes
+    std::vector<double> h_pos;   // AoS xyz
+    std::vector<int> h_fwd, h_rev, h_status, h_pin;
+    // RK4 graph
+    cudaGraphExec_t rk4_exec = nullptr;
+    double rk4_dt = 0, rk4_t = 0;
+    int rk4_prec = -1;
+    // mixed-precision grid split
+    double grid_h = 0;
+    // direct-sum scratch
+    double *dsum = nullptr;
+    int dsum_cap = 0;
+    int *dnodes = nullptr;
+    // pinned host staging
+    double *h_stage = nullptr;
+    size_t h_stage_bytes = 0;
+    // per-phase timing of the last evaluation
+    bool phase_timing = false;
+    cudaEvent_t ph[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+// ------------------------------------------------------------ host helpers
+int ov_fail(ov_ctx *c, int code, const char *fmt, ...);
+#define OV_CUDA(ctx, call)                                                        \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess)                                                    \
+            return ov_fail((ctx), OV_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, \
+                           #call, cudaGetErrorString(e_));                        \
+    } while (0)
+#define OV_LAUNCHED(ctx) ((ctx)->launches++)
+
+DevParams ov_dev_params(const ov_params &p);
+
+inline unsigned long long *ov_stat_ptr(ov_ctx *c)
+{
+    return (unsigned long long *)(c->tree.counters + TC_STAT64);
+}
+
+// tree build (ov_tree.cu)
+int ov_tree_reserve(ov_ctx *c, int cap);
+int ov_tree_reserve_cells(ov_ctx *c, int cells);
+void ov_tree_free(TreeBuf &t);
+int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s);
+
+// sort / scan (ov_sort.cu)
+void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s);
+void ov_scan_exclusive(ov_ctx *c, const int *in, int *out, int n_max, const int *n_dev, int add,
+                       int *tmp, cudaStream_t s);
+
+// velocity path (ov_velocity.cu)
+void ov_launch_tangents(ov_ctx *c, const NodeArrays &na, cudaStream_t s);
+void ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s);
+int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out);
+void ov_launch_euler(ov_ctx *c, const NodeArrays &src, const double *vx, const double *vy,
+                     const double *vz, double dt, NodeArrays &dst, cudaStream_t s);
+void ov_launch_rk4_combine(ov_ctx *c, double dt, cudaStream_t s);
+void ov_launch_periodic_wrap(ov_ctx *c, cudaStream_t s);
+
+// ------------------------------------------------------------ device helpers
+#ifdef __CUDACC__
+// Explicitly rounded FP64 operations: never contracted into FMAs, so a
+// sequence written with them has exactly the reference's rounding.
+__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+
+// vec3_len / vec3_dot accumulation order: ((0 + a0 b0) + a1 b1) + a2 b2
+__device__ __forceinline__ double dot3_ref(double a0, double a1, double a2, double b0, double b1,
+                                           double b2)
+{
+    double o = rn_mul(a0, b0);
+    o = rn_add(o, rn_mul(a1, b1));
+    o = rn_add(o, rn_mul(a2, b2));
+    return o;
+}
+__device__ __forceinline__ double len3_ref(double a0, double a1, double a2)
+{
+    return __dsqrt_rn(dot3_ref(a0, a1, a2, a0, a1, a2));
+}
+
+// seg_pwrap (boundaries.c:54-83): r2 moved by periods toward r1.
+__device__ __forceinline__ void pwrap_dev(const Geometry &g, const double r1[3], double r2[3])
+{
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (!g.periodic[a]) continue;
+        double L = g.L[a], hL = g.L[a] * 0.5;
+        int guard = 0;
+        while (rn_sub(r2[a], r1[a]) > hL && guard++ < 64) r2[a] = rn_sub(r2[a], L);
+        while (rn_sub(r2[a], r1[a]) < -hL && guard++ < 128) r2[a] = rn_add(r2[a], L);
+    }
+}
+
+// make_child_box (octree.c:165-232) on one box (lo,hi): child `idx` in the
+// reference order BLF, BLB, BRF, BRB, TLF, TLB, TRF, TRB.
+__device__ __forceinline__ void child_box_dev(const double b[3], const double t[3], int idx,
+                                              double cb[3], double ct[3])
+{
+    double c[3], h[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        c[a] = rn_mul(rn_add(b[a], t[a]), 0.5);
+        h[a] = rn_mul(rn_sub(t[a], b[a]), 0.5);   // L/2, exact
+    }
+    switch (idx) {
+    case 0: cb[0] = rn_add(b[0], h[0]); cb[1] = b[1]; cb[2] = b[2];
+            ct[0] = rn_add(c[0], h[0]); ct[1] = c[1]; ct[2] = c[2]; break;
+    case 1: cb[0] = b[0]; cb[1] = b[1]; cb[2] = b[2]; ct[0] = c[0]; ct[1] = c[1]; ct[2] = c[2]; break;
+    case 2: cb[0] = c[0]; cb[1] = c[1]; cb[2] = rn_sub(c[2], h[2]);
+            ct[0] = t[0]; ct[1] = t[1]; ct[2] = rn_sub(t[2], h[2]); break;
+    case 3: cb[0] = b[0]; cb[1] = rn_add(b[1], h[1]); cb[2] = b[2];
+            ct[0] = c[0]; ct[1] = rn_add(c[1], h[1]); ct[2] = c[2]; break;
+    case 4: cb[0] = c[0]; cb[1] = rn_sub(c[1], h[1]); cb[2] = c[2];
+            ct[0] = t[0]; ct[1] = rn_sub(t[1], h[1]); ct[2] = t[2]; break;
+    case 5: cb[0] = b[0]; cb[1] = b[1]; cb[2] = rn_add(b[2], h[2]);
+            ct[0] = c[0]; ct[1] = c[1]; ct[2] = rn_add(c[2], h[2]); break;
+    case 6: cb[0] = c[0]; cb[1] = c[1]; cb[2] = c[2]; ct[0] = t[0]; ct[1] = t[1]; ct[2] = t[2]; break;
+    default: cb[0] = rn_sub(c[0], h[0]); cb[1] = c[1]; cb[2] = c[2];
+             ct[0] = rn_sub(t[0], h[0]); ct[1] = t[1]; ct[2] = t[2]; break;
+    }
+}
+
+__device__ __forceinline__ bool in_closed_box_dev(const double b[3], const double t[3], const double p[3])
+{
+    return p[0] >= b[0] && p[0] <= t[0] && p[1] >= b[1] && p[1] <= t[1] && p[2] >= b[2] && p[2] <= t[2];
+}
+
+// Largest side of a box, the reference's ternary (octree.c:302-306).
+__device__ __forceinline__ double box_lm(const double b[3], const double t[3])
+{
+    double Lx = rn_sub(t[0], b[0]), Ly = rn_sub(t[1], b[1]), Lz = rn_sub(t[2], b[2]);
+    return Lx > Ly ? (Lx > Lz ? Lx : Lz) : (Ly > Lz ? Ly : Lz);
+}
+#endif

@@ -1,0 +1,458 @@
+// ov_tree.cu - GPU linear octree with the reference's exact tree semantics.
+//
+// OpenVort's pointer octree (src/octree.c) splits the DOMAIN box until every
+// cell holds at most one node, assigning a node to the FIRST child (order
+// BLF, BLB, BRF, BRB, TLF, TLB, TRF, TRB) whose closed box holds it, with
+// child boxes computed by make_child_box's FP64 arithmetic (octree.c:165-232).
+// A node outside the root box belongs to the root only (octree.c:116-127).
+//
+// Here every node gets a 63-bit path key: 21 levels x 3-bit child index in
+// the reference order.  The child index at each level is read off a 62-bit
+// fixed-point image of the position when the node is at least 2^-40 box
+// lengths away from every face of every level (then the reference's
+// rounded boxes and tie order cannot change the answer); otherwise the
+// exact FP64 first-match descent of the reference is run for that node.
+// Sorting the keys puts the cells of each level in contiguous ranges and in
+// the reference's child order; cells are emitted in pre-order, so a cell's
+// subtree is [cell+1, cell.next) and a traversal needs no stack.
+#include "ov_internal.cuh"
+
+void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s);
+int ov_sort_hist_ints(int cap);
+int ov_scan_tmp_ints(int n_max);
+
+namespace {
+
+struct KeyGeom {
+    double lo[3], hi[3], L[3];
+    int fast;          // fixed-point digits allowed (rounding bound is small)
+};
+
+__device__ __forceinline__ uint64_t exact_key(const double p[3], const KeyGeom &g, int *err)
+{
+    double b[3] = {g.lo[0], g.lo[1], g.lo[2]}, t[3] = {g.hi[0], g.hi[1], g.hi[2]};
+    uint64_t key = 0;
+    for (int lev = 1; lev <= OV_MAX_LEVEL; ++lev) {
+        int pick = -1;
+        double cb[3], ct[3];
+        for (int idx = 0; idx < 8; ++idx) {
+            child_box_dev(b, t, idx, cb, ct);
+            if (in_closed_box_dev(cb, ct, p)) { pick = idx; break; }
+        }
+        if (pick < 0) {
+            // rounding gap between child boxes: the reference keeps the node
+            // only in this cell's ancestors; flagged, node kept in the octant
+            // its coordinates point to.
+            *err |= OV_EW_SLIVER;
+            double c[3];
+            for (int a = 0; a < 3; ++a) c[a] = rn_mul(rn_add(b[a], t[a]), 0.5);
+            pick = ((p[2] > c[2]) << 2) | ((p[1] > c[1]) << 1) | ((p[0] > c[0]) ? 0 : 1);
+            child_box_dev(b, t, pick, cb, ct);
+        }
+        key |= (uint64_t)pick << (63 - 3 * lev);
+        for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
+    }
+    return key;
+}
+
+__global__ void k_keys(const int *__restrict__ status, const double *__restrict__ x,
+                       const double *__restrict__ y, const double *__restrict__ z, int cap, KeyGeom g,
+                       uint64_t *__restrict__ keys, int *__restrict__ order, int *counters)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool live = i < cap && status[i] != OV_EMPTY;
+    double p[3] = {0, 0, 0};
+    if (live) { p[0] = x[i]; p[1] = y[i]; p[2] = z[i]; }
+    bool inside = live && in_closed_box_dev(g.lo, g.hi, p);
+    bool bad = live && !(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]));
+    // one atomic per warp for each counter
+    unsigned b_live = __ballot_sync(0xffffffffu, live), b_in = __ballot_sync(0xffffffffu, inside);
+    if (lane == 0 && b_live) {
+        atomicAdd(&counters[TC_NNE], __popc(b_live));
+        atomicAdd(&counters[TC_M], __popc(b_in));
+        atomicAdd(&counters[TC_OUT], __popc(b_live & ~b_in));
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&counters[TC_ERR], OV_EW_NAN);
+    if (i >= cap) return;
+    order[i] = i;
+    if (!live) { keys[i] = OV_KEY_EMPTY; return; }
+    if (!inside) { keys[i] = OV_KEY_OUT | (uint64_t)i; return; }
+    uint64_t U[3];
+    bool safe = g.fast != 0;
+    const uint64_t low = (1ull << 41) - 1, margin = 1ull << 22;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double u = rn_div(rn_sub(p[a], g.lo[a]), g.L[a]);
+        u = fmin(fmax(u, 0.0), 1.0);
+        U[a] = (uint64_t)(u * 4611686018427387904.0);   // u * 2^62
+        uint64_t r = U[a] & low;
+        safe = safe && r >= margin && r <= low + 1 - margin;
+    }
+    uint64_t key = 0;
+    if (safe) {
+#pragma unroll
+        for (int lev = 1; lev <= OV_MAX_LEVEL; ++lev) {
+            int sh = 62 - lev;
+            uint64_t xb = (U[0] >> sh) & 1, yb = (U[1] >> sh) & 1, zb = (U[2] >> sh) & 1;
+            key |= ((zb << 2) | (yb << 1) | (xb ^ 1)) << (63 - 3 * lev);
+        }
+    } else {
+        int err = 0;
+        key = exact_key(p, g, &err);
+        if (err) atomicOr(&counters[TC_ERR], err);
+    }
+    keys[i] = key;
+}
+
+__device__ __forceinline__ int cpl_of(uint64_t a, uint64_t b)
+{
+    uint64_t d = a ^ b;
+    if (d == 0) return OV_MAX_LEVEL;
+    return (__clzll(d) - 1) / 3;
+}
+
+// cpl[s] for s in [0, M-1), and the number of cells that start at s.
+__global__ void k_cpl(const uint64_t *__restrict__ keys, int cap, int *counters, int *__restrict__ cpl,
+                      int *__restrict__ ncell_at)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int M = counters[TC_M];
+    int nne = counters[TC_NNE];
+    int L = 0;
+    bool deep = false;
+    if (s < M) {
+        int cn = (s + 1 < M) ? cpl_of(keys[s], keys[s + 1]) : 0;
+        cpl[s] = cn;
+        int cp = (s > 0) ? cpl_of(keys[s - 1], keys[s]) : 0;
+        L = max(cp, cn) + 1;
+        if (L > OV_MAX_LEVEL) { deep = true; L = OV_MAX_LEVEL; }
+        ncell_at[s] = (nne >= 2) ? max(L - cp, 0) : 0;
+    }
+    int Lmax = (nne >= 2) ? L : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) Lmax = max(Lmax, __shfl_xor_sync(0xffffffffu, Lmax, o));
+    bool anydeep = __any_sync(0xffffffffu, deep);
+    if ((threadIdx.x & 31) == 0) {
+        if (Lmax > 0) atomicMax(&counters[TC_MAXDEPTH], Lmax);
+        if (anydeep) atomicOr(&counters[TC_ERR], OV_EW_DEPTH);
+    }
+}
+
+// first index j in [lo, hi) with (keys[j] >> sh) > P  (keys sorted)
+__device__ __forceinline__ int upper_prefix(const uint64_t *keys, int lo, int hi, int sh, uint64_t P)
+{
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if ((keys[mid] >> sh) > P) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+// first index j in [lo, hi) with (keys[j] >> sh) >= P
+__device__ __forceinline__ int lower_prefix(const uint64_t *keys, int lo, int hi, int sh, uint64_t P)
+{
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if ((keys[mid] >> sh) >= P) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+
+__global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict__ cpl,
+                        const int *__restrict__ cell_off, int *counters, KeyGeom g,
+                        Cell64 *__restrict__ cells, int *__restrict__ parent, int *__restrict__ nchild,
+                        int *__restrict__ arrive, int cap_cells)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int M = counters[TC_M];
+    int nne = counters[TC_NNE];
+    if (s >= M || nne < 2) return;
+    int ncell = cell_off[M];
+    if (ncell > cap_cells) {
+        if (s == 0) {
+            counters[TC_NEED] = ncell;
+            atomicOr(&counters[TC_ERR], OV_EW_CELLS);
+        }
+        return;
+    }
+    int cp = s > 0 ? cpl[s - 1] : 0;
+    int cn = s + 1 < M ? cpl[s] : 0;
+    int L = min(max(cp, cn) + 1, OV_MAX_LEVEL);
+    uint64_t key = keys[s];
+    // exact box of the first cell starting here, walked from the root
+    double b[3] = {g.lo[0], g.lo[1], g.lo[2]}, t[3] = {g.hi[0], g.hi[1], g.hi[2]};
+    for (int lev = 1; lev <= cp; ++lev) {
+        double cb[3], ct[3];
+        child_box_dev(b, t, (int)((key >> (63 - 3 * lev)) & 7), cb, ct);
+        for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
+    }
+    for (int lev = cp + 1; lev <= L; ++lev) {
+        int ci = cell_off[s] + (lev - cp - 1);
+        double cb[3], ct[3];
+        child_box_dev(b, t, (int)((key >> (63 - 3 * lev)) & 7), cb, ct);
+        for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
+        int sh = 63 - 3 * lev;
+        int e = (lev < L) ? upper_prefix(keys, s + 1, M, sh, key >> sh) - 1 : s;
+        if (lev == OV_MAX_LEVEL) e = upper_prefix(keys, s + 1, M, sh, key >> sh) - 1;
+        Cell64 cell;
+        cell.lm = box_lm(b, t);
+        cell.count = e - s + 1;
+        cell.next = (e + 1 < M) ? cell_off[e + 1] : ncell;
+        cell.cx = cell.cy = cell.cz = cell.qx = cell.qy = cell.qz = 0;
+        cells[ci] = cell;
+        int par;
+        if (lev == 1) par = 0;
+        else if (cp < lev - 1) par = ci - 1;
+        else {
+            int psh = 63 - 3 * (lev - 1);
+            int sp = lower_prefix(keys, 0, s, psh, key >> psh);
+            int cpp = sp > 0 ? cpl[sp - 1] : 0;
+            par = cell_off[sp] + (lev - 1 - cpp - 1);
+        }
+        parent[ci] = par;
+        arrive[ci] = 0;
+        atomicAdd(&nchild[par], 1);
+    }
+}
+
+__device__ __forceinline__ void node_moment(int id, const double *x, const double *y, const double *z,
+                                            const int *fwd, const Geometry &geo, double out[6])
+{
+    double p[3] = {x[id], y[id], z[id]};
+    out[0] = p[0]; out[1] = p[1]; out[2] = p[2];
+    int f = fwd[id];
+    if (f > -1) {
+        double r2[3] = {x[f], y[f], z[f]};
+        pwrap_dev(geo, p, r2);
+        out[3] = rn_sub(r2[0], p[0]); out[4] = rn_sub(r2[1], p[1]); out[5] = rn_sub(r2[2], p[2]);
+    } else {
+        out[3] = out[4] = out[5] = 0;
+    }
+}
+
+__device__ __forceinline__ void finalize_cell(Cell64 *cells, int ci, const double s[6], int count)
+{
+    double inv = 1.0 / (double)count;
+    cells[ci].cx = rn_mul(s[0], inv);
+    cells[ci].cy = rn_mul(s[1], inv);
+    cells[ci].cz = rn_mul(s[2], inv);
+    cells[ci].qx = s[3];
+    cells[ci].qy = s[4];
+    cells[ci].qz = s[5];
+}
+
+// Leaves from the nodes, then each parent from its children by the last
+// child to arrive (one atomic per edge, no waiting).
+__global__ void k_moments(const uint64_t *__restrict__ keys, const int *__restrict__ order,
+                          const int *__restrict__ cpl, const int *__restrict__ cell_off, int *counters,
+                          const double *__restrict__ x, const double *__restrict__ y,
+                          const double *__restrict__ z, const int *__restrict__ fwd, Geometry geo,
+                          Cell64 *cells, const int *__restrict__ parent, const int *__restrict__ nchild,
+                          int *arrive, double *csum, int cap_cells)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int M = counters[TC_M];
+    int nne = counters[TC_NNE];
+    if (s >= M || nne < 2 || cell_off[M] > cap_cells) return;
+    int cp = s > 0 ? cpl[s - 1] : 0;
+    int cn = s + 1 < M ? cpl[s] : 0;
+    int L = min(max(cp, cn) + 1, OV_MAX_LEVEL);
+    int leaf = cell_off[s] + (L - cp - 1);
+    int cnt = cells[leaf].count;
+    double acc[6];
+    if (cnt == 1) {
+        node_moment(order[s], x, y, z, fwd, geo, acc);
+    } else {
+        // deepest level still shared (depth overflow): sum its nodes
+        for (int k = 0; k < 6; ++k) acc[k] = 0;
+        for (int j = 0; j < cnt; ++j) {
+            double m[6];
+            node_moment(order[s + j], x, y, z, fwd, geo, m);
+            for (int k = 0; k < 6; ++k) acc[k] = rn_add(acc[k], m[k]);
+        }
+        if (s > 0 && cpl[s - 1] >= L) return;   // only the first node of the run
+    }
+    for (int k = 0; k < 6; ++k) csum[6 * (size_t)leaf + k] = acc[k];
+    finalize_cell(cells, leaf, acc, cnt);
+    int cur = leaf;
+    for (int guard = 0; guard < 64; ++guard) {
+        int p = parent[cur];
+        if (p <= 0) break;
+        __threadfence();
+        int old = atomicAdd(&arrive[p], 1);
+        if (old != nchild[p] - 1) break;
+        __threadfence();
+        double sum[6] = {0, 0, 0, 0, 0, 0};
+        int end = __ldcg(&cells[p].next);
+        for (int ch = p + 1; ch != end && ch > 0; ch = __ldcg(&cells[ch].next)) {
+            for (int k = 0; k < 6; ++k) sum[k] = rn_add(sum[k], __ldcg(&csum[6 * (size_t)ch + k]));
+        }
+        for (int k = 0; k < 6; ++k) csum[6 * (size_t)p + k] = sum[k];
+        finalize_cell(cells, p, sum, __ldcg(&cells[p].count));
+        cur = p;
+    }
+}
+
+// Root: level-1 children plus the nodes outside the root box; also the
+// one-node and empty tangles.
+__global__ void k_root(const int *__restrict__ order, const int *__restrict__ cell_off, int *counters,
+                       const double *__restrict__ x, const double *__restrict__ y,
+                       const double *__restrict__ z, const int *__restrict__ fwd, Geometry geo, KeyGeom g,
+                       Cell64 *cells, const double *csum, int cap_cells)
+{
+    __shared__ double red[6][256];
+    int M = counters[TC_M], nne = counters[TC_NNE], nout = counters[TC_OUT];
+    int ncell = nne == 0 ? 0 : (nne >= 2 ? cell_off[M] : 1);
+    if (ncell > cap_cells) ncell = 0;   // flagged by k_cells; the host grows the storage
+    if (threadIdx.x == 0) counters[TC_NCELL] = ncell;
+    if (ncell == 0) return;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int j = threadIdx.x; j < nout; j += blockDim.x) {
+        double m[6];
+        node_moment(order[M + j], x, y, z, fwd, geo, m);
+        for (int k = 0; k < 6; ++k) acc[k] = rn_add(acc[k], m[k]);
+    }
+    if (nne == 1 && M == 1 && threadIdx.x == 0) node_moment(order[0], x, y, z, fwd, geo, acc);
+    for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off)
+            for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = rn_add(red[k][threadIdx.x], red[k][threadIdx.x + off]);
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    double sum[6];
+    for (int k = 0; k < 6; ++k) sum[k] = 0;
+    if (nne >= 2) {
+        for (int ch = 1; ch < ncell && ch > 0; ch = cells[ch].next)
+            for (int k = 0; k < 6; ++k) sum[k] = rn_add(sum[k], csum[6 * (size_t)ch + k]);
+    }
+    for (int k = 0; k < 6; ++k) sum[k] = rn_add(sum[k], red[k][0]);
+    Cell64 r;
+    double inv = 1.0 / (double)nne;
+    r.cx = rn_mul(sum[0], inv); r.cy = rn_mul(sum[1], inv); r.cz = rn_mul(sum[2], inv);
+    r.qx = sum[3]; r.qy = sum[4]; r.qz = sum[5];
+    r.lm = box_lm(g.lo, g.hi);
+    r.next = ncell;
+    r.count = nne;
+    cells[0] = r;
+}
+
+// FP32 copy of every cell for the mixed traversal: COM split into a part on
+// the grid of step h (exact in FP32) and a small remainder.
+__global__ void k_cells32(const Cell64 *__restrict__ cells, const int *counters, double h, double inv_h,
+                          Cell32 *__restrict__ out)
+{
+    int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci >= counters[TC_NCELL]) return;
+    Cell64 c = cells[ci];
+    Cell32 o;
+    double cx = c.cx, cy = c.cy, cz = c.cz;
+    double gx = rint(cx * inv_h) * h, gy = rint(cy * inv_h) * h, gz = rint(cz * inv_h) * h;
+    o.gx = (float)gx; o.gy = (float)gy; o.gz = (float)gz;
+    o.fx = (float)(cx - gx); o.fy = (float)(cy - gy); o.fz = (float)(cz - gz);
+    o.qx = (float)c.qx; o.qy = (float)c.qy; o.qz = (float)c.qz;
+    o.lm = __double2float_ru(c.lm);
+    o.next = c.next;
+    o.count = c.count;
+    out[ci] = o;
+}
+
+}  // namespace
+
+int ov_tree_reserve_cells(ov_ctx *c, int cells)
+{
+    TreeBuf &t = c->tree;
+    if (t.cap_cells >= cells && t.cells) return OV_OK;
+    void *ptrs[] = {t.cells, t.cells32, t.parent, t.nchild, t.arrive, t.csum};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    t.cap_cells = cells;
+    OV_CUDA(c, cudaMalloc(&t.cells, (size_t)t.cap_cells * sizeof(Cell64)));
+    OV_CUDA(c, cudaMalloc(&t.cells32, (size_t)t.cap_cells * sizeof(Cell32)));
+    OV_CUDA(c, cudaMalloc(&t.parent, (size_t)t.cap_cells * 4));
+    OV_CUDA(c, cudaMalloc(&t.nchild, (size_t)t.cap_cells * 4));
+    OV_CUDA(c, cudaMalloc(&t.arrive, (size_t)t.cap_cells * 4));
+    OV_CUDA(c, cudaMalloc(&t.csum, (size_t)t.cap_cells * 6 * 8));
+    return OV_OK;
+}
+
+int ov_tree_reserve(ov_ctx *c, int cap)
+{
+    TreeBuf &t = c->tree;
+    if (t.cap >= cap && t.keys) return OV_OK;
+    ov_tree_free(t);
+    t.cap = cap;
+    size_t n = (size_t)cap;
+    OV_CUDA(c, cudaMalloc(&t.keys, n * 8));
+    OV_CUDA(c, cudaMalloc(&t.keys_alt, n * 8));
+    OV_CUDA(c, cudaMalloc(&t.order, n * 4));
+    OV_CUDA(c, cudaMalloc(&t.order_alt, n * 4));
+    OV_CUDA(c, cudaMalloc(&t.cpl, n * 4 + 4));
+    OV_CUDA(c, cudaMalloc(&t.ncell_at, n * 4 + 4));
+    OV_CUDA(c, cudaMalloc(&t.cell_off, n * 4 + 8));
+    OV_CUDA(c, cudaMalloc(&t.scan_tmp, (size_t)ov_scan_tmp_ints(cap) * 4));
+    OV_CUDA(c, cudaMalloc(&t.sort_hist, (size_t)ov_sort_hist_ints(cap) * 4));
+    OV_CUDA(c, cudaMalloc(&t.counters, TC_WORDS * 4));
+    // cells: about 1.3 per node for filament tangles; grown on demand
+    return ov_tree_reserve_cells(c, 2 * cap + 64);
+}
+
+void ov_tree_free(TreeBuf &t)
+{
+    void *ptrs[] = {t.keys, t.keys_alt, t.order, t.order_alt, t.cpl, t.ncell_at, t.cell_off, t.scan_tmp,
+                    t.sort_hist, t.cells, t.cells32, t.parent, t.nchild, t.arrive, t.csum, t.counters};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    t = TreeBuf{};
+}
+
+static KeyGeom key_geom(const Geometry &geo)
+{
+    KeyGeom g;
+    bool fast = true;
+    for (int a = 0; a < 3; ++a) {
+        g.lo[a] = geo.lo[a];
+        g.hi[a] = geo.hi[a];
+        g.L[a] = geo.L[a];
+        // bound on how far the reference's rounded faces (21 levels) and the
+        // fixed-point image may sit from the exact dyadic faces, in box units
+        double bound = (fabs(geo.lo[a]) + fabs(geo.hi[a])) / geo.L[a] * 64 * 2.220446049250313e-16 +
+                       4 * 2.220446049250313e-16;
+        if (!(bound < ldexp(1.0, -44))) fast = false;
+    }
+    g.fast = fast ? 1 : 0;
+    return g;
+}
+
+// Build the tree of `na` (positions of the context's topology) on stream s.
+// Everything stays on the device, so the sequence can be graph-captured.
+int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
+{
+    TreeBuf &t = c->tree;
+    int cap = c->cap;
+    KeyGeom g = key_geom(c->geo);
+    OV_CUDA(c, cudaMemsetAsync(t.counters, 0, TC_WORDS * 4, s));
+    OV_CUDA(c, cudaMemsetAsync(t.nchild, 0, (size_t)t.cap_cells * 4, s));
+    int nb = (cap + 255) / 256;
+    k_keys<<<nb, 256, 0, s>>>(c->status, na.x, na.y, na.z, cap, g, t.keys, t.order, t.counters);
+    c->launches++;
+    ov_sort_keys(c, t, cap, s);
+    k_cpl<<<nb, 256, 0, s>>>(t.keys, cap, t.counters, t.cpl, t.ncell_at);
+    c->launches++;
+    ov_scan_exclusive(c, t.ncell_at, t.cell_off, cap, t.counters + TC_M, 1, t.scan_tmp, s);
+    k_cells<<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, g, t.cells, t.parent, t.nchild, t.arrive,
+                               t.cap_cells);
+    k_moments<<<nb, 256, 0, s>>>(t.keys, t.order, t.cpl, t.cell_off, t.counters, na.x, na.y, na.z, c->fwd,
+                                 c->geo, t.cells, t.parent, t.nchild, t.arrive, t.csum, t.cap_cells);
+    k_root<<<1, 256, 0, s>>>(t.order, t.cell_off, t.counters, na.x, na.y, na.z, c->fwd, c->geo, g, t.cells,
+                             t.csum, t.cap_cells);
+    c->launches += 3;
+    if (c->precision == OV_PREC_MIXED) {
+        k_cells32<<<(t.cap_cells + 255) / 256, 256, 0, s>>>(t.cells, t.counters, c->grid_h, 1.0 / c->grid_h,
+                                                           t.cells32);
+        c->launches++;
+    }
+    OV_CUDA(c, cudaGetLastError());
+    return OV_OK;
+}

@@ -1,0 +1,595 @@
+// ov_velocity.cu - per-node velocity kernels.
+//
+//  k_tangents     update_tangent_normal (tangle.c:423-502), one node per thread
+//  k_vel_fp64     update_velocity (tangle.c:600-726) fused: LIA + external
+//                 v_s + Barnes-Hut over the primary and every image query
+//                 point + mutual friction, one warp per 32 Morton-ordered
+//                 targets sharing one cursor through the pre-order cells
+//  k_direct       the tree==NULL branch (tangle.c:652-687), one block per node
+//  k_euler / k_rk4_combine / k_wrap   RK4 stages and enforce_periodic_boundaries
+//
+// The FP64 traversal keeps the reference's decisions bit-for-bit given the
+// same cell data: Lm/d < theta, d < 1e-8 and ndot < 1e-8 are evaluated by a
+// cheap test with a 1e-12 relative guard band and, inside the band, by the
+// reference's own correctly rounded divisions.
+#include <math.h>
+
+#include "ov_internal.cuh"
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+#ifndef M_E
+#define M_E 2.7182818284590452354
+#endif
+
+namespace {
+
+struct VelArgs {
+    const int *order, *counters;
+    const Cell64 *cells;
+    const Cell32 *cells32;
+    const double *x, *y, *z, *tx, *ty, *tz, *nx, *ny, *nz;
+    double *vx, *vy, *vz, *sx, *sy, *sz;
+    const int *fwd, *rev, *status, *pin;
+    Geometry geo;
+    DevParams prm;
+    double t;
+    double f4pi;            // KAPPA/4/M_PI in the reference's rounding
+    double grid_h, inv_h;   // mixed path
+    double near2;           // mixed path: squared near-field radius
+    unsigned long long *stat;
+};
+
+// step_node (tangle.c:155-194) without recursion: a pinned end reverses the
+// walk and mirrors the result in its wall, innermost mirror applied first.
+__device__ bool step_node_dev(const VelArgs &a, int i, int where, double out[3])
+{
+    int walls[8];
+    int nw = 0, cur = i, w = where;
+    for (int guard = 0; w != 0; ++guard) {
+        if (guard > 16 || cur < 0) return false;
+        int st = a.status[cur];
+        if (st == OV_FREE) {
+            cur = w > 0 ? a.fwd[cur] : a.rev[cur];
+            w += w > 0 ? -1 : 1;
+        } else if (st == OV_PINNED || st == OV_PINNED_SLIP) {
+            int nb = w > 0 ? a.fwd[cur] : a.rev[cur];
+            if (nb >= 0) {
+                cur = nb;
+                w += w > 0 ? -1 : 1;
+            } else {
+                if (nw >= 8) return false;
+                walls[nw++] = a.pin[cur];
+                w = -w;
+            }
+        } else {
+            return false;
+        }
+    }
+    if (cur < 0 || a.status[cur] == OV_EMPTY) return false;
+    out[0] = a.x[cur]; out[1] = a.y[cur]; out[2] = a.z[cur];
+    for (int m = nw - 1; m >= 0; --m) {
+        int f = walls[m];
+        if (f < 0 || f > 5) continue;
+        int ax = f >> 1;
+        double wpos = (f & 1) ? a.geo.hi[ax] : a.geo.lo[ax];
+        out[ax] = rn_sub(rn_mul(2.0, wpos), out[ax]);
+    }
+    return true;
+}
+
+__device__ __forceinline__ double wrapped_len(const Geometry &g, const double r1[3], const double r2in[3])
+{
+    double r2[3] = {r2in[0], r2in[1], r2in[2]};
+    pwrap_dev(g, r1, r2);
+    return len3_ref(rn_sub(r1[0], r2[0]), rn_sub(r1[1], r2[1]), rn_sub(r1[2], r2[2]));
+}
+
+__global__ void k_tangents(VelArgs a, int cap, int *counters)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= cap || a.status[k] == OV_EMPTY) return;
+    const Geometry &g = a.geo;
+    double s0[3] = {a.x[k], a.y[k], a.z[k]}, s1[3], s2[3], sm1[3], sm2[3];
+    bool ok = step_node_dev(a, k, 1, s1) & step_node_dev(a, k, 2, s2) & step_node_dev(a, k, -1, sm1) &
+              step_node_dev(a, k, -2, sm2);
+    if (!ok) {
+        atomicOr(&counters[TC_ERR], OV_EW_WALK);
+        return;
+    }
+    double w2[3] = {s2[0], s2[1], s2[2]}, w1[3] = {s1[0], s1[1], s1[2]};
+    double wm1[3] = {sm1[0], sm1[1], sm1[2]}, wm2[3] = {sm2[0], sm2[1], sm2[2]};
+    pwrap_dev(g, s0, w2);
+    pwrap_dev(g, s0, w1);
+    pwrap_dev(g, s0, wm1);
+    pwrap_dev(g, s0, wm2);
+    double d1 = len3_ref(rn_sub(s0[0], w1[0]), rn_sub(s0[1], w1[1]), rn_sub(s0[2], w1[2]));
+    double d2 = rn_add(d1, wrapped_len(g, s1, s2));
+    double dm1 = len3_ref(rn_sub(s0[0], wm1[0]), rn_sub(s0[1], wm1[1]), rn_sub(s0[2], wm1[2]));
+    double dm2 = rn_add(dm1, wrapped_len(g, sm1, sm2));
+    double den[4] = {
+        rn_mul(rn_mul(rn_mul(d2, rn_sub(d2, d1)), rn_add(dm1, d2)), rn_add(dm2, d2)),
+        rn_mul(rn_mul(rn_mul(d1, rn_sub(d2, d1)), rn_add(dm1, d1)), rn_add(dm2, d1)),
+        rn_mul(rn_mul(rn_mul(dm1, rn_add(dm1, d1)), rn_add(dm1, d2)), rn_sub(dm2, dm1)),
+        rn_mul(rn_mul(rn_mul(dm2, rn_add(dm2, d1)), rn_add(dm2, d2)), rn_sub(dm2, dm1))};
+    double c1[4] = {rn_mul(rn_mul(-d1, dm1), dm2), rn_mul(rn_mul(d2, dm1), dm2), rn_mul(rn_mul(-d1, d2), dm2),
+                    rn_mul(rn_mul(d1, d2), dm1)};
+    double c2[4] = {
+        rn_mul(2.0, rn_sub(rn_mul(rn_sub(dm1, d1), dm2), rn_mul(d1, dm1))),
+        rn_mul(-2.0, rn_sub(rn_mul(rn_sub(dm1, d2), dm2), rn_mul(d2, dm1))),
+        rn_mul(2.0, rn_sub(rn_mul(rn_add(d2, d1), dm2), rn_mul(d1, d2))),
+        rn_mul(-2.0, rn_sub(rn_mul(rn_add(d2, d1), dm1), rn_mul(d1, d2)))};
+    double r1[4], r2[4];
+#pragma unroll
+    for (int z = 0; z < 4; ++z) { r1[z] = rn_div(c1[z], den[z]); r2[z] = rn_div(c2[z], den[z]); }
+    double ds[4][3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        ds[0][ax] = rn_sub(w2[ax], s0[ax]);
+        ds[1][ax] = rn_sub(w1[ax], s0[ax]);
+        ds[2][ax] = rn_sub(wm1[ax], s0[ax]);
+        ds[3][ax] = rn_sub(wm2[ax], s0[ax]);
+    }
+    double tg[3], nm[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        double tt = 0, nn = 0;
+#pragma unroll
+        for (int z = 0; z < 4; ++z) {
+            tt = rn_add(tt, rn_mul(r1[z], ds[z][ax]));
+            nn = rn_add(nn, rn_mul(r2[z], ds[z][ax]));
+        }
+        tg[ax] = tt; nm[ax] = nn;
+    }
+    double *T[3] = {(double *)a.tx, (double *)a.ty, (double *)a.tz};
+    double *Nn[3] = {(double *)a.nx, (double *)a.ny, (double *)a.nz};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) { T[ax][k] = tg[ax]; Nn[ax][k] = nm[ax]; }
+}
+
+// get_v (external_velocity.c:62-81)
+__device__ __forceinline__ void ext_vel(int type, const double dir[3], double s1, double s0, double tld,
+                                        double t, double out[3])
+{
+    if (type == OV_SIMPLE || type == OV_DECREASING) {
+        double s = s1;
+        if (type == OV_DECREASING && t < tld) s = rn_sub(s0, rn_div(rn_mul(t, rn_sub(s0, s1)), tld));
+        out[0] = rn_mul(dir[0], s); out[1] = rn_mul(dir[1], s); out[2] = rn_mul(dir[2], s);
+    } else {
+        out[0] = out[1] = out[2] = 0;
+    }
+}
+
+// shifted (tangle.c:370-414)
+__device__ __forceinline__ void image_point(const Geometry &g, int j, const double p[3], double q[3])
+{
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) q[ax] = rn_sub(p[ax], rn_mul(g.L[ax], (double)g.shift[j][ax]));
+    for (int m = 0; m < g.nreflect[j]; ++m) {
+        int f = g.reflect[j][m];
+        if (f < 0 || f > 5) continue;
+        int ax = f >> 1;
+        double w = (f & 1) ? g.hi[ax] : g.lo[ax];
+        q[ax] = rn_sub(rn_mul(2.0, w), p[ax]);
+    }
+}
+
+__device__ __forceinline__ void mirror_vec(int f, double v[3])
+{
+    // mirror_vector_reflect (boundaries.c:201-211): normal component flips
+    int ax = f >> 1;
+    v[ax] = -v[ax];
+}
+
+// The segment law (octree.c:321-342 / tangle.c:536-559) for R = COM - r
+// (or segment start - r) and Rp1 = R + q.  lR is |R| as the caller
+// computed it.  Returns false when a filter drops the segment.
+__device__ __forceinline__ bool segment_law64(const double R[3], const double Rp1[3], double lR, double f4pi,
+                                              double out[3])
+{
+    double lRp1 = len3_ref(Rp1[0], Rp1[1], Rp1[2]);
+    if (lR < 1e-8 || lRp1 < 1e-8) return false;
+    double dotv = dot3_ref(R[0], R[1], R[2], Rp1[0], Rp1[1], Rp1[2]);
+    double pr = rn_mul(lR, lRp1);
+    // ndot = dot/lR/lRp1 < 1e-8 ?
+    double thr = 1e-8 * pr;
+    bool drop;
+    if (dotv < thr * (1.0 - 1e-12)) drop = true;
+    else if (dotv > thr * (1.0 + 1e-12)) drop = false;
+    else drop = rn_div(rn_div(dotv, lR), lRp1) < 1e-8;
+    if (drop) return false;
+    double denom = pr * (pr + dotv);
+    double sc = f4pi * (lR + lRp1) / denom;
+    out[0] = (R[1] * Rp1[2] - R[2] * Rp1[1]) * sc;
+    out[1] = (R[2] * Rp1[0] - R[0] * Rp1[2]) * sc;
+    out[2] = (R[0] * Rp1[1] - R[1] * Rp1[0]) * sc;
+    return true;
+}
+
+// One Barnes-Hut query point for the 32 lanes of a warp.  `part` = lane
+// takes part; returns the lane's velocity in v.
+__device__ __forceinline__ void bh_query64(const VelArgs &a, const double q[3], bool part, int ncell,
+                                           double v[3], unsigned long long &visits,
+                                           unsigned long long &accepts, unsigned long long &steps,
+                                           bool &overflow)
+{
+    v[0] = v[1] = v[2] = 0;
+    const double theta = a.prm.theta;
+    int c = 0;
+    int resume = part ? 0 : 0x7fffffff;
+    int guard = 0;
+    while (c < ncell) {
+        const Cell64 *cp = a.cells + c;
+        double cx = __ldg(&cp->cx), cy = __ldg(&cp->cy), cz = __ldg(&cp->cz);
+        double lm = __ldg(&cp->lm);
+        int nxt = __ldg(&cp->next);
+        bool open = false;
+        if (c >= resume) {
+            ++visits;
+            double dx = rn_sub(q[0], cx), dy = rn_sub(q[1], cy), dz = rn_sub(q[2], cz);
+            double d = len3_ref(dx, dy, dz);
+            if (d < 1e-8) {
+                resume = nxt;
+            } else {
+                bool acc;
+                if (nxt == c + 1) {
+                    acc = true;   // leaf (or a cell at the deepest level)
+                } else {
+                    double td = theta * d;
+                    if (lm < td * (1.0 - 1e-12)) acc = true;
+                    else if (lm > td * (1.0 + 1e-12)) acc = false;
+                    else acc = rn_div(lm, d) < theta;
+                }
+                if (acc) {
+                    ++accepts;
+                    double R[3] = {-dx, -dy, -dz};
+                    double Rp1[3] = {rn_add(R[0], __ldg(&cp->qx)), rn_add(R[1], __ldg(&cp->qy)),
+                                     rn_add(R[2], __ldg(&cp->qz))};
+                    double w[3];
+                    if (segment_law64(R, Rp1, d, a.f4pi, w)) {
+                        v[0] += w[0]; v[1] += w[1]; v[2] += w[2];
+                    }
+                    resume = nxt;
+                } else {
+                    open = true;
+                }
+            }
+        }
+        ++steps;
+        c = __any_sync(0xffffffffu, open) ? c + 1 : nxt;
+        if (++guard > 4 * ncell + 64) { overflow = true; break; }
+    }
+}
+
+// LIA (tangle.c:568-592) + external v_s, given the BH sums; then vels with
+// mutual friction and PINNED_SLIP (tangle.c:689-725).
+__device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const double p[3], const double prim[3],
+                                            const double img[3], int *err, double vs_out[3], double vel_out[3])
+{
+    int st = a.status[id];
+    if (st == OV_PINNED) {
+        ext_vel(a.prm.vb_type, a.prm.vb_dir, a.prm.vb_s1, a.prm.vb_s0, a.prm.vb_tld, a.t, vel_out);
+        vs_out[0] = vs_out[1] = vs_out[2] = 0;
+        return true;
+    }
+    double nx_[3], pv[3];
+    if (!(step_node_dev(a, id, 1, nx_) && step_node_dev(a, id, -1, pv))) {
+        *err |= OV_EW_WALK;
+        return false;
+    }
+    double l_next = wrapped_len(a.geo, p, nx_);
+    double l_prev = wrapped_len(a.geo, pv, p);
+    double f = rn_div(rn_div(rn_mul(a.prm.kappa,
+                              log(rn_div(rn_div(rn_mul(2.0, sqrt(rn_mul(l_next, l_prev))), sqrt(M_E)), a.prm.a0))),
+                         4.0),
+                    M_PI);
+    double tg[3] = {a.tx[id], a.ty[id], a.tz[id]}, nm[3] = {a.nx[id], a.ny[id], a.nz[id]};
+    double vs[3] = {rn_mul(rn_sub(rn_mul(tg[1], nm[2]), rn_mul(tg[2], nm[1])), f),
+                    rn_mul(rn_sub(rn_mul(tg[2], nm[0]), rn_mul(tg[0], nm[2])), f),
+                    rn_mul(rn_sub(rn_mul(tg[0], nm[1]), rn_mul(tg[1], nm[0])), f)};
+    double ev[3];
+    ext_vel(a.prm.vs_type, a.prm.vs_dir, a.prm.vs_s1, a.prm.vs_s0, a.prm.vs_tld, a.t, ev);
+    for (int ax = 0; ax < 3; ++ax) vs[ax] = rn_add(rn_add(rn_add(vs[ax], ev[ax]), prim[ax]), img[ax]);
+    double vel[3] = {vs[0], vs[1], vs[2]};
+    if (a.prm.friction) {
+        double vn[3];
+        ext_vel(a.prm.vn_type, a.prm.vn_dir, a.prm.vn_s1, a.prm.vn_s0, a.prm.vn_tld, a.t, vn);
+        double dv[3] = {rn_sub(vn[0], vs[0]), rn_sub(vn[1], vs[1]), rn_sub(vn[2], vs[2])};
+        double c1[3] = {rn_sub(rn_mul(tg[1], dv[2]), rn_mul(tg[2], dv[1])), rn_sub(rn_mul(tg[2], dv[0]), rn_mul(tg[0], dv[2])),
+                        rn_sub(rn_mul(tg[0], dv[1]), rn_mul(tg[1], dv[0]))};
+        for (int ax = 0; ax < 3; ++ax) vel[ax] = rn_add(vel[ax], rn_mul(c1[ax], a.prm.alpha));
+        double c2[3] = {rn_sub(rn_mul(tg[1], c1[2]), rn_mul(tg[2], c1[1])), rn_sub(rn_mul(tg[2], c1[0]), rn_mul(tg[0], c1[2])),
+                        rn_sub(rn_mul(tg[0], c1[1]), rn_mul(tg[1], c1[0]))};
+        double m = -a.prm.alpha_p;
+        for (int ax = 0; ax < 3; ++ax) vel[ax] = rn_add(vel[ax], rn_mul(c2[ax], m));
+    }
+    if (st == OV_PINNED_SLIP) {
+        int f2 = a.pin[id];
+        if (f2 >= 0 && f2 < 6) {
+            int ax = f2 >> 1;
+            double n = (f2 & 1) ? -1.0 : 1.0;
+            double nv = rn_mul(n, vel[ax]);
+            vel[ax] = rn_sub(vel[ax], rn_mul(n, nv));
+        }
+    }
+    for (int ax = 0; ax < 3; ++ax) { vs_out[ax] = vs[ax]; vel_out[ax] = vel[ax]; }
+    return true;
+}
+
+__global__ void __launch_bounds__(128) k_vel_fp64(VelArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nne = a.counters[TC_NNE];
+    const int ncell = a.counters[TC_NCELL];
+    if (warp * 32 >= nne) return;   // warp-uniform
+    const int tix = warp * 32 + lane;
+    const bool valid = tix < nne;
+    const int id = valid ? a.order[tix] : 0;
+    const int st = valid ? a.status[id] : OV_EMPTY;
+    const bool part = valid && st != OV_PINNED && st != OV_EMPTY && a.prm.use_bh;
+    double p[3] = {0, 0, 0};
+    if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
+    double prim[3] = {0, 0, 0}, img[3] = {0, 0, 0};
+    unsigned long long visits = 0, accepts = 0, steps = 0;
+    bool overflow = false;
+    for (int j = -1; j < a.geo.n_img; ++j) {
+        double q[3], v[3];
+        if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+        else image_point(a.geo, j, p, q);
+        bh_query64(a, q, part, ncell, v, visits, accepts, steps, overflow);
+        if (j < 0) {
+            prim[0] = v[0]; prim[1] = v[1]; prim[2] = v[2];
+        } else {
+            for (int m = 0; m < a.geo.nreflect[j]; ++m) mirror_vec(a.geo.reflect[j][m], v);
+            img[0] = rn_add(img[0], v[0]); img[1] = rn_add(img[1], v[1]); img[2] = rn_add(img[2], v[2]);
+        }
+    }
+    int err = overflow ? OV_EW_ITER : 0;
+    if (valid && st != OV_EMPTY) {
+        double vs[3], vel[3];
+        if (finish_node(a, id, p, prim, img, &err, vs, vel)) {
+            a.sx[id] = vs[0]; a.sy[id] = vs[1]; a.sz[id] = vs[2];
+            a.vx[id] = vel[0]; a.vy[id] = vel[1]; a.vz[id] = vel[2];
+        }
+    }
+    // counters: one atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        visits += __shfl_xor_sync(0xffffffffu, visits, o);
+        accepts += __shfl_xor_sync(0xffffffffu, accepts, o);
+        err |= __shfl_xor_sync(0xffffffffu, err, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&a.stat[0], visits);
+        atomicAdd(&a.stat[1], accepts);
+        atomicAdd(&a.stat[2], steps);
+        if (err) atomicOr((int *)&a.counters[TC_ERR], err);
+    }
+}
+
+// ------------------------------------------------------------ direct sum
+// Velocity of node `nodes[b]` from every segment of the primary tangle
+// (skipping the two segments at the node) and of every image (skipping
+// nothing), as update_velocity with tree == NULL.
+__global__ void k_direct(VelArgs a, const int *__restrict__ nodes, int n, int cap, double *__restrict__ out)
+{
+    __shared__ double red[3][256];
+    int b = blockIdx.x;
+    if (b >= n) return;
+    int k = nodes[b];
+    double p[3] = {a.x[k], a.y[k], a.z[k]};
+    double acc[3] = {0, 0, 0};
+    for (int j = -1; j < a.geo.n_img; ++j) {
+        double q[3];
+        if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+        else image_point(a.geo, j, p, q);
+        for (int m = threadIdx.x; m < cap; m += blockDim.x) {
+            int f = a.fwd[m];
+            if (f == -1) continue;
+            if (j < 0 && (m == k || f == k)) continue;
+            double s1[3] = {a.x[m], a.y[m], a.z[m]};
+            double s2[3] = {a.x[f], a.y[f], a.z[f]};
+            pwrap_dev(a.geo, s1, s2);
+            double R[3] = {rn_sub(s1[0], q[0]), rn_sub(s1[1], q[1]), rn_sub(s1[2], q[2])};
+            double Rp1[3] = {rn_sub(s2[0], q[0]), rn_sub(s2[1], q[1]), rn_sub(s2[2], q[2])};
+            double lR = len3_ref(R[0], R[1], R[2]);
+            double w[3];
+            if (segment_law64(R, Rp1, lR, a.f4pi, w)) {
+                acc[0] += w[0]; acc[1] += w[1]; acc[2] += w[2];
+            }
+        }
+    }
+    for (int ax = 0; ax < 3; ++ax) red[ax][threadIdx.x] = acc[ax];
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off)
+            for (int ax = 0; ax < 3; ++ax) red[ax][threadIdx.x] += red[ax][threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        for (int ax = 0; ax < 3; ++ax) out[3 * (size_t)b + ax] = red[ax][0];
+    }
+}
+
+// Finish the direct-sum nodes (LIA, v_s, friction) into vels/vs scratch.
+__global__ void k_direct_finish(VelArgs a, const int *__restrict__ nodes, int n, const double *__restrict__ sums,
+                                double *__restrict__ vout, double *__restrict__ sout)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    int k = nodes[b];
+    double p[3] = {a.x[k], a.y[k], a.z[k]};
+    double prim[3] = {sums[3 * (size_t)b], sums[3 * (size_t)b + 1], sums[3 * (size_t)b + 2]};
+    double zero[3] = {0, 0, 0}, vs[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
+    int err = 0;
+    if (a.status[k] != OV_EMPTY) finish_node(a, k, p, prim, zero, &err, vs, vel);
+    for (int ax = 0; ax < 3; ++ax) {
+        vout[3 * (size_t)b + ax] = vel[ax];
+        sout[3 * (size_t)b + ax] = vs[ax];
+    }
+}
+
+// -------------------------------------------------------------- stepping
+// euler_step2 (vortex_dynamics.c:20-42): dst = src + v*dt on non-EMPTY nodes
+__global__ void k_euler(const int *__restrict__ status, const double *__restrict__ x, const double *__restrict__ y,
+                        const double *__restrict__ z, const double *__restrict__ vx, const double *__restrict__ vy,
+                        const double *__restrict__ vz, double dt, double *__restrict__ ox, double *__restrict__ oy,
+                        double *__restrict__ oz, int cap)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= cap || status[k] == OV_EMPTY) return;
+    ox[k] = rn_add(x[k], rn_mul(vx[k], dt));
+    oy[k] = rn_add(y[k], rn_mul(vy[k], dt));
+    oz[k] = rn_add(z[k], rn_mul(vz[k], dt));
+}
+
+struct Rk4Args {
+    const int *status;
+    double *x, *y, *z;
+    const double *v1x, *v1y, *v1z, *v2x, *v2y, *v2z, *v3x, *v3y, *v3z, *v4x, *v4y, *v4z;
+    double dt;
+    int cap;
+};
+
+// vortex_dynamics.c:95-115
+__global__ void k_rk4_combine(Rk4Args r)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= r.cap || r.status[k] == OV_EMPTY) return;
+    double d6 = r.dt / 6, d3 = r.dt / 3;
+    double *X[3] = {r.x, r.y, r.z};
+    const double *V1[3] = {r.v1x, r.v1y, r.v1z}, *V2[3] = {r.v2x, r.v2y, r.v2z};
+    const double *V3[3] = {r.v3x, r.v3y, r.v3z}, *V4[3] = {r.v4x, r.v4y, r.v4z};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        double mv = rn_mul(V1[ax][k], d6);
+        mv = rn_add(mv, rn_mul(V2[ax][k], d3));
+        mv = rn_add(mv, rn_mul(V3[ax][k], d3));
+        mv = rn_add(mv, rn_mul(V4[ax][k], d6));
+        X[ax][k] = rn_add(X[ax][k], mv);
+    }
+}
+
+// enforce_periodic_boundaries (tangle.c:793-814)
+__global__ void k_wrap(const int *__restrict__ status, double *x, double *y, double *z, Geometry g, int cap)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= cap || status[k] == OV_EMPTY) return;
+    double p[3] = {x[k], y[k], z[k]};
+    for (int guard = 0; guard < 64; ++guard) {
+        int face = -1;
+        if (p[0] < g.lo[0]) face = OV_LEFT;
+        if (p[0] > g.hi[0]) face = OV_RIGHT;
+        if (p[1] < g.lo[1]) face = OV_BACK;
+        if (p[1] > g.hi[1]) face = OV_FRONT;
+        if (p[2] < g.lo[2]) face = OV_DOWN;
+        if (p[2] > g.hi[2]) face = OV_UP;
+        if (face > -1 && g.wall[face] != OV_WALL_PERIODIC) face = -1;
+        if (face < 0) break;
+        int ax = face >> 1;
+        p[ax] = (face & 1) ? rn_sub(p[ax], g.L[ax]) : rn_add(p[ax], g.L[ax]);
+    }
+    x[k] = p[0]; y[k] = p[1]; z[k] = p[2];
+}
+
+VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long *stat)
+{
+    VelArgs a;
+    a.order = c->tree.order;
+    a.counters = c->tree.counters;
+    a.cells = c->tree.cells;
+    a.cells32 = c->tree.cells32;
+    a.x = na.x; a.y = na.y; a.z = na.z;
+    a.tx = na.tx; a.ty = na.ty; a.tz = na.tz;
+    a.nx = na.nx; a.ny = na.ny; a.nz = na.nz;
+    a.vx = na.vx; a.vy = na.vy; a.vz = na.vz;
+    a.sx = na.sx; a.sy = na.sy; a.sz = na.sz;
+    a.fwd = c->fwd; a.rev = c->rev; a.status = c->status; a.pin = c->pin;
+    a.geo = c->geo;
+    a.prm = ov_dev_params(c->params);
+    a.t = t;
+    a.f4pi = c->params.kappa / 4 / M_PI;
+    a.grid_h = c->grid_h;
+    a.inv_h = c->grid_h > 0 ? 1.0 / c->grid_h : 0;
+    double near = 2.0 * c->params.dl_max;
+    a.near2 = near * near;
+    a.stat = stat;
+    return a;
+}
+
+}  // namespace
+
+void ov_launch_tangents(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
+{
+    VelArgs a = make_args(c, na, 0.0, nullptr);
+    k_tangents<<<(c->cap + 255) / 256, 256, 0, s>>>(a, c->cap, c->tree.counters);
+    c->launches++;
+}
+
+void ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s)
+{
+    VelArgs a = make_args(c, na, t, ov_stat_ptr(c));
+    int warps = (c->cap + 31) / 32;
+    int threads = 128;
+    int blocks = (warps * 32 + threads - 1) / threads;
+    (void)precision;
+    k_vel_fp64<<<blocks, threads, 0, s>>>(a);
+    c->launches++;
+}
+
+int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out)
+{
+    if (n <= 0) return OV_OK;
+    if (c->dsum_cap < n) {
+        if (c->dsum) cudaFree(c->dsum);
+        if (c->dnodes) cudaFree(c->dnodes);
+        c->dsum = nullptr; c->dnodes = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->dsum, (size_t)n * 9 * sizeof(double)));
+        OV_CUDA(c, cudaMalloc(&c->dnodes, (size_t)n * sizeof(int)));
+        c->dsum_cap = n;
+    }
+    OV_CUDA(c, cudaMemcpyAsync(c->dnodes, nodes, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    VelArgs a = make_args(c, c->node, t, nullptr);
+    k_direct<<<n, 256, 0, c->stream>>>(a, c->dnodes, n, c->cap, c->dsum);
+    double *vo = c->dsum + 3 * (size_t)n, *so = c->dsum + 6 * (size_t)n;
+    k_direct_finish<<<(n + 127) / 128, 128, 0, c->stream>>>(a, c->dnodes, n, c->dsum, vo, so);
+    c->launches += 2;
+    OV_CUDA(c, cudaGetLastError());
+    if (vels_out)
+        OV_CUDA(c, cudaMemcpyAsync(vels_out, vo, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (vs_out)
+        OV_CUDA(c, cudaMemcpyAsync(vs_out, so, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    return OV_OK;
+}
+
+void ov_launch_euler(ov_ctx *c, const NodeArrays &src, const double *vx, const double *vy, const double *vz,
+                     double dt, NodeArrays &dst, cudaStream_t s)
+{
+    k_euler<<<(c->cap + 255) / 256, 256, 0, s>>>(c->status, src.x, src.y, src.z, vx, vy, vz, dt, dst.x, dst.y,
+                                                 dst.z, c->cap);
+    c->launches++;
+}
+
+void ov_launch_rk4_combine(ov_ctx *c, double dt, cudaStream_t s)
+{
+    Rk4Args r;
+    r.status = c->status;
+    r.x = c->node.x; r.y = c->node.y; r.z = c->node.z;
+    r.v1x = c->node.vx; r.v1y = c->node.vy; r.v1z = c->node.vz;
+    r.v2x = c->stage[0].vx; r.v2y = c->stage[0].vy; r.v2z = c->stage[0].vz;
+    r.v3x = c->stage[1].vx; r.v3y = c->stage[1].vy; r.v3z = c->stage[1].vz;
+    r.v4x = c->stage[2].vx; r.v4y = c->stage[2].vy; r.v4z = c->stage[2].vz;
+    r.dt = dt;
+    r.cap = c->cap;
+    k_rk4_combine<<<(c->cap + 255) / 256, 256, 0, s>>>(r);
+    c->launches++;
+}
+
+void ov_launch_periodic_wrap(ov_ctx *c, cudaStream_t s)
+{
+    k_wrap<<<(c->cap + 255) / 256, 256, 0, s>>>(c->status, c->node.x, c->node.y, c->node.z, c->geo, c->cap);
+    c->launches++;
+}

@@ -1,0 +1,248 @@
+"""Python host binding of libovgpu (ctypes over include/openvort_gpu.h).
+
+This mirrors the reference's own operations on a tangle:
+
+    ctx = Context()                      # one GPU context (stream, buffers)
+    ctx.set_params(params)               # the reference's globals, explicit
+    ctx.upload(host_tangle)              # struct tangle_state -> HBM
+    ctx.update_tangle(t)                 # update_tangle (tangle.h:114)
+    ctx.rk4_step(t, dt)                  # rk4_step (vortex_dynamics.c:50)
+    ctx.download(host_tangle)            # HBM -> struct tangle_state
+
+There is no CPU fallback: every call runs the CUDA library and raises
+OVError when it reports a failure, or RuntimeError when the library or a GPU
+is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_LIB = None
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libovgpu.so")
+
+
+class OVError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load(path: str | None = None):
+    """Load libovgpu.so (built by openvort_gb300.build); raise if absent."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"libovgpu.so not built ({path}); run `python -m openvort_gb300.build`")
+    L = C.CDLL(path)
+    P = C.c_void_p
+    TS = C.POINTER(abi.TangleState)
+    sig = {
+        "ov_ctx_create": (C.c_int, [C.POINTER(P), C.c_int]),
+        "ov_ctx_destroy": (C.c_int, [P]),
+        "ov_last_error": (C.c_char_p, [P]),
+        "ov_set_params": (C.c_int, [P, C.POINTER(abi.Params)]),
+        "ov_set_precision": (C.c_int, [P, C.c_int]),
+        "ov_ctx_stream": (P, [P]),
+        "ov_upload_tangle": (C.c_int, [P, TS]),
+        "ov_download_tangle": (C.c_int, [P, TS, C.c_uint]),
+        "ov_capacity": (C.c_int, [P]),
+        "ov_update_tangents_normals": (C.c_int, [P]),
+        "ov_update_velocities": (C.c_int, [P, C.c_double]),
+        "ov_update_tangle": (C.c_int, [P, C.c_double]),
+        "ov_rk4_step": (C.c_int, [P, C.c_double, C.c_double]),
+        "ov_direct_velocities": (C.c_int, [P, C.POINTER(C.c_int), C.c_int, C.c_double,
+                                           C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "ov_enforce_periodic_boundaries": (C.c_int, [P]),
+        "ov_eliminate_small_loops": (C.c_int, [P]),
+        "ov_reconnect": (C.c_int, [P, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), C.c_int]),
+        "ov_remesh": (C.c_int, [P, C.c_double, C.c_double, C.c_double]),
+        "ov_smooth": (C.c_int, [P]),
+        "ov_step": (C.c_int, [P, C.c_double, C.c_double]),
+        "ov_get_stats": (C.c_int, [P, C.POINTER(abi.Stats)]),
+        "ov_timer_start": (C.c_int, [P]),
+        "ov_timer_stop": (C.c_int, [P, C.POINTER(C.c_float)]),
+        "ov_flush_l2": (C.c_int, [P, C.c_size_t]),
+        "ov_synchronize": (C.c_int, [P]),
+        "ov_kernel_launches": (C.c_int64, [P]),
+        "ov_params_default": (None, [C.POINTER(abi.Params)]),
+        "ov_upload_tangle_fields": (C.c_int, [P, TS, C.c_uint]),
+        "ov_set_phase_timing": (C.c_int, [P, C.c_int]),
+        "ov_phase_times": (C.c_int, [P, C.POINTER(C.c_float)]),
+        "ov_measure_fma_peak": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = L
+    return L
+
+
+def declared_symbols() -> list[str]:
+    """Every function declared in include/*.h (for the export check)."""
+    import re
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    names = []
+    for f in sorted(os.listdir(inc)):
+        if not f.endswith(".h"):
+            continue
+        txt = open(os.path.join(inc, f)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b((?:ov|ovd)_\w+)\s*\(", txt, flags=re.M):
+            names.append(m.group(1))
+    return sorted(set(names))
+
+
+class Context:
+    """One libovgpu context on one GPU."""
+
+    def __init__(self, device: int = 0, params: abi.Params | None = None, precision: int = abi.OV_PREC_FP64):
+        self.lib = load()
+        self._h = C.c_void_p()
+        rc = self.lib.ov_ctx_create(C.byref(self._h), device)
+        if rc != 0:
+            raise OVError(rc, "ov_ctx_create failed (no usable CUDA device?)")
+        if params is not None:
+            self.set_params(params)
+        self.set_precision(precision)
+        self._host = None
+
+    # -------------------------------------------------------------- plumbing
+    def _check(self, rc: int):
+        if rc != 0:
+            raise OVError(rc, self.lib.ov_last_error(self._h).decode())
+
+    def close(self):
+        if self._h:
+            self.lib.ov_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_params(self, p: abi.Params):
+        self.params = p
+        self._check(self.lib.ov_set_params(self._h, C.byref(p)))
+
+    def set_precision(self, prec: int):
+        self._check(self.lib.ov_set_precision(self._h, prec))
+
+    # ----------------------------------------------------------------- data
+    def upload(self, host):
+        """host: workloads.HostTangle (or anything with .state())."""
+        self._host = host
+        self._state = host.state()
+        self._check(self.lib.ov_upload_tangle(self._h, C.byref(self._state)))
+
+    def upload_fields(self, host, fields: int):
+        self._host = host
+        self._state = host.state()
+        self._check(self.lib.ov_upload_tangle_fields(self._h, C.byref(self._state), fields))
+
+    def download(self, host=None, fields: int = abi.OV_F_ALL):
+        host = host or self._host
+        st = host.state()
+        self._check(self.lib.ov_download_tangle(self._h, C.byref(st), fields))
+        return host
+
+    # -------------------------------------------------------------- compute
+    def update_tangents_normals(self):
+        self._check(self.lib.ov_update_tangents_normals(self._h))
+
+    def update_velocities(self, t: float = 0.0):
+        self._check(self.lib.ov_update_velocities(self._h, t))
+
+    def update_tangle(self, t: float = 0.0):
+        self._check(self.lib.ov_update_tangle(self._h, t))
+
+    def rk4_step(self, t: float, dt: float):
+        self._check(self.lib.ov_rk4_step(self._h, t, dt))
+
+    def direct_velocities(self, nodes, t: float = 0.0):
+        nodes = np.ascontiguousarray(nodes, dtype=np.int32)
+        v = np.zeros((len(nodes), 3))
+        s = np.zeros((len(nodes), 3))
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        self._check(self.lib.ov_direct_velocities(self._h, nodes.ctypes.data_as(C.POINTER(C.c_int)),
+                                                  len(nodes), t, dp(v), dp(s)))
+        return v, s
+
+    def enforce_periodic(self):
+        self._check(self.lib.ov_enforce_periodic_boundaries(self._h))
+
+    def eliminate_small_loops(self):
+        self._check(self.lib.ov_eliminate_small_loops(self._h))
+
+    def reconnect(self, t: float = 0.0, log: bool = False):
+        n = C.c_int(0)
+        cap = max(16, self.capacity)
+        lk, ll = (C.c_int * cap)(), (C.c_int * cap)()
+        self._check(self.lib.ov_reconnect(self._h, t, C.byref(n), lk, ll, cap))
+        if log:
+            return n.value, list(zip(lk[:min(n.value, cap)], ll[:min(n.value, cap)]))
+        return n.value
+
+    def remesh(self, mn: float, mx: float, t: float = 0.0):
+        self._check(self.lib.ov_remesh(self._h, mn, mx, t))
+
+    def smooth(self):
+        self._check(self.lib.ov_smooth(self._h))
+
+    def step(self, t: float, dt: float):
+        self._check(self.lib.ov_step(self._h, t, dt))
+
+    @property
+    def capacity(self) -> int:
+        return self.lib.ov_capacity(self._h)
+
+    def stats(self) -> dict:
+        s = abi.Stats()
+        self._check(self.lib.ov_get_stats(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    # --------------------------------------------------------------- timing
+    def timer_start(self):
+        self._check(self.lib.ov_timer_start(self._h))
+
+    def timer_stop(self) -> float:
+        ms = C.c_float(0)
+        self._check(self.lib.ov_timer_stop(self._h, C.byref(ms)))
+        return ms.value
+
+    def flush_l2(self, nbytes: int = 256 << 20):
+        self._check(self.lib.ov_flush_l2(self._h, nbytes))
+
+    def synchronize(self):
+        self._check(self.lib.ov_synchronize(self._h))
+
+    def set_phase_timing(self, on: bool = True):
+        self._check(self.lib.ov_set_phase_timing(self._h, int(on)))
+
+    def phase_times(self) -> list[float]:
+        ms = (C.c_float * 3)()
+        self._check(self.lib.ov_phase_times(self._h, ms))
+        return list(ms)
+
+    def fma_peak_tflops(self, precision: int) -> float:
+        v = C.c_double(0)
+        self._check(self.lib.ov_measure_fma_peak(self._h, precision, C.byref(v)))
+        return v.value
+
+    @property
+    def kernel_launches(self) -> int:
+        return self.lib.ov_kernel_launches(self._h)
