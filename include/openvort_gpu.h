@@ -158,6 +158,51 @@ int ov_rk4_step(ov_ctx *ctx, double t, double dt);
 int ov_direct_velocities(ov_ctx *ctx, const int *nodes, int n, double t,
                          double *vels_out, double *vs_out);
 
+/* Largest node list one ov_direct_velocities_noalloc call accepts. */
+#define OV_NOALLOC_MAX_NODES 4096
+
+/*
+ * ov_direct_velocities_noalloc - the direct-sum velocities of
+ * ov_direct_velocities for callers that may not allocate GPU memory.
+ * This entry point has no counterpart in the reference.
+ *
+ * Who needs it: programs whose device memory is owned by someone else - a
+ * pool or arena allocator that has reserved the GPU, a host framework that
+ * hands the library its buffers once at start-up and forbids allocation
+ * afterwards - and latency-bound loops that must never reach cudaMalloc,
+ * which may synchronize the device.  The call takes no context, allocates
+ * nothing (no cudaMalloc, no cudaFree, no allocating library routine) and
+ * only launches two kernels on `stream`; the caller owns every buffer.
+ *
+ * Working space: the per-node partial sums live in one fixed array compiled
+ * into the library (3 doubles per node, OV_NOALLOC_MAX_NODES nodes, 96 KiB),
+ * which every GPU that loads the library keeps until the process exits.
+ * All calls on a device share that array: two calls whose kernels overlap on
+ * the GPU (different streams, no ordering between them) race and corrupt
+ * each other's results.  Calls ordered on one stream are safe; each call
+ * writes every partial sum it later reads, so nothing carries over.
+ * The first call on each device looks up the array's device address (with
+ * that device current); make that first call before any stream capture.
+ *
+ * Inputs (device pointers, n_slots node slots in the reference's indexing):
+ *   d_pos       x[n_slots], y[n_slots], z[n_slots]          (SoA doubles)
+ *   d_conn      forward[n_slots], reverse[n_slots]
+ *   d_status    status[n_slots], pin_wall[n_slots]
+ *   d_tangents  / d_normals  SoA like d_pos
+ *   d_nodes     n_nodes node ids, each in [0, n_slots)
+ * Outputs (device, AoS): d_vels, d_vs  n_nodes x 3 doubles (d_vs may be NULL).
+ * A node id out of range gives NaN outputs for that entry.
+ * Returns OV_ERR_ARG when n_nodes > OV_NOALLOC_MAX_NODES, n_nodes < 0 or a
+ * required pointer is NULL; OV_ERR_CUDA when the launch or the address
+ * look-up fails.  Asynchronous: synchronize `stream` before reading outputs.
+ */
+int ov_direct_velocities_noalloc(const ov_params *p, const ov_domain_box *box,
+                                 const ov_image_tangle *images, int n_images, int n_slots,
+                                 const double *d_pos, const int *d_conn, const int *d_status,
+                                 const double *d_tangents, const double *d_normals,
+                                 const int *d_nodes, int n_nodes, double t,
+                                 double *d_vels, double *d_vs, void *stream);
+
 /* ------------------------------------------------------ topology passes */
 int ov_enforce_periodic_boundaries(ov_ctx *ctx);
 int ov_eliminate_small_loops(ov_ctx *ctx);

@@ -593,3 +593,158 @@ void ov_launch_periodic_wrap(ov_ctx *c, cudaStream_t s)
     k_wrap<<<(c->cap + 255) / 256, 256, 0, s>>>(c->status, c->node.x, c->node.y, c->node.z, c->geo, c->cap);
     c->launches++;
 }
+
+// ----------------------------------------------------------------------------
+// Direct sum without allocation (ov_direct_velocities_noalloc).
+//
+// For callers that cannot allocate device memory: the partial sums that
+// ov_direct_velocities keeps in a context buffer live here in a fixed array
+// compiled into the library.  Host code never uses the array's name as a
+// pointer (on the host it is only a stand-in); the device address is looked
+// up once per device and passed to the kernels.
+// ----------------------------------------------------------------------------
+#include <mutex>
+
+static __device__ __align__(256) double g_noalloc_sums[3 * OV_NOALLOC_MAX_NODES];
+
+namespace {
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double *g_noalloc_addr[kNoallocMaxDevices] = {};
+
+// Sum pass: one block per listed node, every segment of the primary tangle
+// and of each image; writes the node's three partial sums into `sums`.
+__global__ void k_direct_noalloc(VelArgs a, const int *__restrict__ nodes, int n, int n_slots,
+                                 double *__restrict__ sums)
+{
+    __shared__ double red[3][256];
+    int b = blockIdx.x;
+    if (b >= n) return;
+    int k = nodes[b];
+    bool ok = k >= 0 && k < n_slots;
+    double acc[3] = {0, 0, 0};
+    if (ok) {
+        double p[3] = {a.x[k], a.y[k], a.z[k]};
+        for (int j = -1; j < a.geo.n_img; ++j) {
+            double q[3];
+            if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+            else image_point(a.geo, j, p, q);
+            for (int m = threadIdx.x; m < n_slots; m += blockDim.x) {
+                int f = a.fwd[m];
+                if (f < 0 || f >= n_slots) continue;
+                if (j < 0 && (m == k || f == k)) continue;
+                double s1[3] = {a.x[m], a.y[m], a.z[m]};
+                double s2[3] = {a.x[f], a.y[f], a.z[f]};
+                pwrap_dev(a.geo, s1, s2);
+                double R[3] = {rn_sub(s1[0], q[0]), rn_sub(s1[1], q[1]), rn_sub(s1[2], q[2])};
+                double Rp1[3] = {rn_sub(s2[0], q[0]), rn_sub(s2[1], q[1]), rn_sub(s2[2], q[2])};
+                double lR = len3_ref(R[0], R[1], R[2]);
+                double w[3];
+                if (segment_law64(R, Rp1, lR, a.f4pi, w)) {
+                    acc[0] += w[0]; acc[1] += w[1]; acc[2] += w[2];
+                }
+            }
+        }
+    }
+    for (int ax = 0; ax < 3; ++ax) red[ax][threadIdx.x] = acc[ax];
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off)
+            for (int ax = 0; ax < 3; ++ax) red[ax][threadIdx.x] += red[ax][threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int ax = 0; ax < 3; ++ax) sums[3 * (size_t)b + ax] = ok ? red[ax][0] : __longlong_as_double(0x7ff8000000000000ll);
+}
+
+// Finish pass: LIA, external v_s and mutual friction on top of the sums.
+__global__ void k_direct_noalloc_finish(VelArgs a, const int *__restrict__ nodes, int n, int n_slots,
+                                        const double *__restrict__ sums, double *__restrict__ vout,
+                                        double *__restrict__ sout)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    int k = nodes[b];
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    double vs[3] = {nan, nan, nan}, vel[3] = {nan, nan, nan};
+    if (k >= 0 && k < n_slots && a.status[k] != OV_EMPTY) {
+        double p[3] = {a.x[k], a.y[k], a.z[k]};
+        double prim[3] = {sums[3 * (size_t)b], sums[3 * (size_t)b + 1], sums[3 * (size_t)b + 2]};
+        double zero[3] = {0, 0, 0};
+        int err = 0;
+        if (!finish_node(a, k, p, prim, zero, &err, vs, vel))
+            for (int ax = 0; ax < 3; ++ax) vs[ax] = vel[ax] = nan;
+    }
+    for (int ax = 0; ax < 3; ++ax) {
+        vout[3 * (size_t)b + ax] = vel[ax];
+        if (sout) sout[3 * (size_t)b + ax] = vs[ax];
+    }
+}
+
+}  // namespace
+
+extern "C" int ov_direct_velocities_noalloc(const ov_params *p, const ov_domain_box *box,
+                                            const ov_image_tangle *images, int n_images, int n_slots,
+                                            const double *d_pos, const int *d_conn, const int *d_status,
+                                            const double *d_tangents, const double *d_normals,
+                                            const int *d_nodes, int n_nodes, double t, double *d_vels,
+                                            double *d_vs, void *stream)
+{
+    if (!p || !box || n_nodes < 0 || n_slots < 0 || n_images < 0 || n_images > OV_MAX_IMAGES ||
+        (n_images > 0 && !images))
+        return OV_ERR_ARG;
+    if (n_nodes > OV_NOALLOC_MAX_NODES) return OV_ERR_ARG;   // above the fixed working space
+    if (n_nodes == 0) return OV_OK;
+    if (!d_pos || !d_conn || !d_status || !d_tangents || !d_normals || !d_nodes || !d_vels) return OV_ERR_ARG;
+
+    // one-time look-up of the working array's device address on this device
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices) return OV_ERR_CUDA;
+    double *sums = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *addr = nullptr;
+            if (cudaGetSymbolAddress(&addr, g_noalloc_sums) != cudaSuccess || !addr) return OV_ERR_CUDA;
+            g_noalloc_addr[dev] = (double *)addr;
+        }
+        sums = g_noalloc_addr[dev];
+    }
+
+    VelArgs a;
+    memset(&a, 0, sizeof a);
+    size_t ns = (size_t)n_slots;
+    a.x = d_pos; a.y = d_pos + ns; a.z = d_pos + 2 * ns;
+    a.tx = d_tangents; a.ty = d_tangents + ns; a.tz = d_tangents + 2 * ns;
+    a.nx = d_normals; a.ny = d_normals + ns; a.nz = d_normals + 2 * ns;
+    a.fwd = d_conn; a.rev = d_conn + ns;
+    a.status = d_status; a.pin = d_status + ns;
+    Geometry &g = a.geo;
+    for (int ax = 0; ax < 3; ++ax) {
+        g.lo[ax] = box->bottom_left_back.p[ax];
+        g.hi[ax] = box->top_right_front.p[ax];
+        g.L[ax] = g.hi[ax] - g.lo[ax];
+    }
+    for (int f = 0; f < 6; ++f) g.wall[f] = box->wall[f];
+    g.periodic[0] = box->wall[OV_LEFT] == OV_WALL_PERIODIC;
+    g.periodic[1] = box->wall[OV_BACK] == OV_WALL_PERIODIC;
+    g.periodic[2] = box->wall[OV_DOWN] == OV_WALL_PERIODIC;
+    g.n_img = n_images;
+    for (int j = 0; j < n_images; ++j) {
+        for (int ax = 0; ax < 3; ++ax) {
+            g.shift[j][ax] = images[j].shift[ax];
+            g.reflect[j][ax] = images[j].reflect[ax];
+        }
+        int nr = images[j].number_of_reflects;
+        g.nreflect[j] = nr < 0 ? 0 : (nr > 3 ? 3 : nr);
+    }
+    a.prm = ov_dev_params(*p);
+    a.t = t;
+    a.f4pi = p->kappa / 4 / M_PI;
+
+    cudaStream_t s = (cudaStream_t)stream;
+    k_direct_noalloc<<<n_nodes, 256, 0, s>>>(a, d_nodes, n_nodes, n_slots, sums);
+    k_direct_noalloc_finish<<<(n_nodes + 127) / 128, 128, 0, s>>>(a, d_nodes, n_nodes, n_slots, sums, d_vels, d_vs);
+    return cudaGetLastError() == cudaSuccess ? OV_OK : OV_ERR_CUDA;
+}
