@@ -259,9 +259,14 @@ def run_ours(args):
             ctx.update_tangle(0.0)
             mt.append(ctx.timer_stop())
         ctx.download(ht, abi.OV_F_VELS)
+        mst = ctx.stats()
         err = float(np.linalg.norm(ht.vels - ref_v) / np.linalg.norm(ref_v))
         mixed = {"value": world * n / (statistics.mean(mt) * 1e-3), "unit": UNIT,
-                 "rel_l2_vs_fp64_tree": err, "ms_per_step": statistics.mean(mt)}
+                 "rel_l2_vs_fp64_tree": err, "ms_per_step": statistics.mean(mt),
+                 "speedup_vs_fp64": mean_ms / statistics.mean(mt),
+                 "same_decisions_as_fp64": bool(mst["accepts"] == acc and mst["visits"] == vis),
+                 "fp64_guard_band_decisions": mst["fp64_fallbacks"], "fp64_near_field": mst["near_field_fp64"],
+                 "warp_efficiency": mst["visits"] / max(1, 32 * mst["warp_steps"])}
         ctx.set_precision(abi.OV_PREC_FP64)
     except Exception as e:  # mixed path not built yet
         mixed = {"unavailable": str(e)[:200]}
@@ -289,7 +294,8 @@ def run_ours(args):
                      "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
                      "peak_source": "measured in this run (FP64 FMA chains, all SMs)",
                      "work": "42 flops per accepted interaction + 9 per visited cell",
-                     "accepts": acc, "visits": vis, "fp32_fma_peak_tflops": fp32_peak},
+                     "accepts": acc, "visits": vis, "fp32_fma_peak_tflops": fp32_peak,
+                     "warp_efficiency": vis / max(1, 32 * st["warp_steps"])},
         "cpu_baseline": cpu,
         "e2e": {"value": world * n / (e2e_mean * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},

@@ -135,6 +135,11 @@ int ov_upload_tangle(ov_ctx *ctx, const ov_tangle_state *t);
    host arrays must hold at least the context's node capacity (ov_capacity). */
 int ov_download_tangle(ov_ctx *ctx, ov_tangle_state *t, unsigned fields);
 int ov_capacity(const ov_ctx *ctx);
+/* Slot count of the tangle held by the context (tangle_state.N, which
+   remesh may double as expand_tangle does) and its next_empty /
+   total_empty bookkeeping.  A host tangle passed to ov_download_tangle must
+   have at least *n_slots slots. */
+int ov_tangle_info(const ov_ctx *ctx, int *n_slots, int *next_empty, int *total_empty);
 /* Upload only the OV_F_* fields selected (positions and topology are all
    update_tangle needs; update_velocities also reads tangents/normals).  The
    first upload into a context, or one that changes the node count, always
@@ -202,6 +207,13 @@ int ov_direct_velocities_noalloc(const ov_params *p, const ov_domain_box *box,
                                  const double *d_tangents, const double *d_normals,
                                  const int *d_nodes, int n_nodes, double t,
                                  double *d_vels, double *d_vs, void *stream);
+
+/* Barnes-Hut velocity sum of octree_get_vs (octree.c:296-356), FP64, at n
+   arbitrary points: the tree of the context's current positions is built
+   first when `rebuild` is non-zero (or none exists yet).  points and out are
+   host arrays of n vec3.  n = 0 with rebuild = 1 only builds the tree. */
+int ov_tree_velocity_at(ov_ctx *ctx, const double *points, int n, double resolution, int rebuild,
+                        double *out);
 
 /* ------------------------------------------------------ topology passes */
 int ov_enforce_periodic_boundaries(ov_ctx *ctx);

@@ -168,6 +168,15 @@ void *ov_ctx_stream(ov_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 int ov_capacity(const ov_ctx *c) { return c ? c->cap : 0; }
 
+int ov_tangle_info(const ov_ctx *c, int *n_slots, int *next_empty, int *total_empty)
+{
+    if (!c) return OV_ERR_ARG;
+    if (n_slots) *n_slots = c->n_live;
+    if (next_empty) *next_empty = c->next_empty;
+    if (total_empty) *total_empty = c->total_empty;
+    return OV_OK;
+}
+
 }  // extern "C"
 
 static int alloc_nodes(ov_ctx *c, NodeArrays &a, int cap)
@@ -200,6 +209,44 @@ static int ensure_capacity(ov_ctx *c, int cap)
     OV_CUDA(c, cudaMalloc(&c->rev, (size_t)cap * 4));
     OV_CUDA(c, cudaMalloc(&c->status, (size_t)cap * 4));
     OV_CUDA(c, cudaMalloc(&c->pin, (size_t)cap * 4));
+    if ((r = ov_tree_reserve(c, cap))) return r;
+    c->cap = cap;
+    return OV_OK;
+}
+
+int ov_grow_preserving(ov_ctx *c, int cap)
+{
+    if (cap <= c->cap) return OV_OK;
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    int old = c->cap;
+    size_t nb = (size_t)old * sizeof(double), nn = (size_t)cap * sizeof(double);
+    double **ps[] = {&c->node.x, &c->node.y, &c->node.z, &c->node.tx, &c->node.ty, &c->node.tz, &c->node.nx,
+                     &c->node.ny, &c->node.nz, &c->node.vx, &c->node.vy, &c->node.vz, &c->node.sx, &c->node.sy,
+                     &c->node.sz};
+    for (double **p : ps) {
+        double *q = nullptr;
+        OV_CUDA(c, cudaMalloc(&q, nn));
+        OV_CUDA(c, cudaMemsetAsync(q, 0, nn, c->stream));
+        OV_CUDA(c, cudaMemcpyAsync(q, *p, nb, cudaMemcpyDeviceToDevice, c->stream));
+        OV_CUDA(c, cudaStreamSynchronize(c->stream));
+        cudaFree(*p);
+        *p = q;
+    }
+    int **is[] = {&c->fwd, &c->rev, &c->status, &c->pin};
+    for (int **p : is) {
+        int *q = nullptr;
+        OV_CUDA(c, cudaMalloc(&q, (size_t)cap * 4));
+        OV_CUDA(c, cudaMemsetAsync(q, 0xFF, (size_t)cap * 4, c->stream));   // -1: EMPTY / no link
+        OV_CUDA(c, cudaMemcpyAsync(q, *p, (size_t)old * 4, cudaMemcpyDeviceToDevice, c->stream));
+        OV_CUDA(c, cudaStreamSynchronize(c->stream));
+        cudaFree(*p);
+        *p = q;
+    }
+    for (auto &s : c->stage) free_nodes(s);
+    int r;
+    for (auto &s : c->stage)
+        if ((r = alloc_nodes(c, s, cap))) return r;
+    if (c->rk4_exec) { cudaGraphExecDestroy(c->rk4_exec); c->rk4_exec = nullptr; }
     if ((r = ov_tree_reserve(c, cap))) return r;
     c->cap = cap;
     return OV_OK;
@@ -258,6 +305,9 @@ int ov_upload_tangle_fields(ov_ctx *c, const ov_tangle_state *t, unsigned fields
     if ((r = ensure_capacity(c, std::max(n, 1)))) return r;
     if (!c->uploaded || c->cap != old_cap || c->n_live != n) fields |= OV_F_POS | OV_F_TOPOLOGY;
     c->n_live = n;   // slots past t->N (a smaller tangle in a larger context) are EMPTY
+    c->tree_built = false;
+    c->next_empty = t->next_empty;
+    c->total_empty = t->total_empty;
     set_geometry(c, t->box, t->bimg);
     size_t cap = (size_t)c->cap;
     if ((r = ensure_stage(c, cap * 3 * sizeof(double) * 5 + cap * 4 * sizeof(int)))) return r;
@@ -307,6 +357,9 @@ int ov_download_tangle(ov_ctx *c, ov_tangle_state *t, unsigned fields)
 {
     if (!c || !t) return OV_ERR_ARG;
     if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
+    if (t->N < c->n_live)
+        return ov_fail(c, OV_ERR_ARG, "host tangle has %d slots, the context holds %d (expand it first)", t->N,
+                       c->n_live);
     int n = std::min(t->N, c->cap);
     size_t cap = (size_t)c->cap;
     int r;
@@ -336,6 +389,8 @@ int ov_download_tangle(ov_ctx *c, ov_tangle_state *t, unsigned fields)
             for (int a = 0; a < 3; ++a) dst[f][k].p[a] = s[a * cap + k];
     }
     if (fields & OV_F_TOPOLOGY) {
+        t->next_empty = c->next_empty;
+        t->total_empty = c->total_empty + (t->N - c->n_live);
         for (int k = 0; k < n; ++k) {
             t->connections[k].forward = hi[k];
             t->connections[k].reverse = hi[cap + k];
@@ -383,6 +438,12 @@ static int error_from_word(ov_ctx *c)
     if (w & OV_EW_NAN) return ov_fail(c, OV_ERR_NAN, "non-finite node position (error word 0x%x)", w);
     if (w & OV_EW_WALK) return ov_fail(c, OV_ERR_TOPOLOGY, "filament walk reached an EMPTY slot (error word 0x%x)", w);
     if (w & OV_EW_ITER) return ov_fail(c, OV_ERR_STACK, "traversal iteration bound exceeded (error word 0x%x)", w);
+    if (w & OV_EW_BOUNDS) {
+        int bad = 0;
+        cudaMemcpy(&bad, c->tree.counters + TC_BAD, 4, cudaMemcpyDeviceToHost);
+        return ov_fail(c, OV_ERR_STATE, "device bounds check failed: code %d index %d (error word 0x%x)",
+                       (bad >> 24) & 0x3F, bad & 0xFFFFFF, w);
+    }
     if (w & OV_EW_DEPTH)
         return ov_fail(c, OV_ERR_DEPTH, "two nodes share a cell at tree level %d (error word 0x%x)", OV_MAX_LEVEL, w);
     return OV_OK;   // sliver drops are counted, not fatal
@@ -404,21 +465,8 @@ static int eval_async(ov_ctx *c, NodeArrays &na, double t, bool tangents, cudaSt
     return OV_OK;
 }
 
-extern "C" {
-
-int ov_update_tangents_normals(ov_ctx *c)
-{
-    int r = check_ready(c);
-    if (r) return r;
-    OV_CUDA(c, cudaMemsetAsync(c->tree.counters, 0, TC_WORDS * 4, c->stream));
-    ov_launch_tangents(c, c->node, c->stream);
-    OV_CUDA(c, cudaGetLastError());
-    if ((r = collect_stats(c, true))) return r;
-    return error_from_word(c);
-}
-
 // Evaluate, growing the cell storage and re-running when the tree did not fit.
-static int eval_sync(ov_ctx *c, NodeArrays &na, double t, bool tangents)
+int ov_eval_sync(ov_ctx *c, NodeArrays &na, double t, bool tangents)
 {
     int r;
     for (int attempt = 0; attempt < 3; ++attempt) {
@@ -432,18 +480,31 @@ static int eval_sync(ov_ctx *c, NodeArrays &na, double t, bool tangents)
     return ov_fail(c, OV_ERR_ALLOC, "cell storage could not be sized");
 }
 
+extern "C" {
+
+int ov_update_tangents_normals(ov_ctx *c)
+{
+    int r = check_ready(c);
+    if (r) return r;
+    OV_CUDA(c, cudaMemsetAsync(c->tree.counters, 0, TC_WORDS * 4, c->stream));
+    ov_launch_tangents(c, c->node, c->stream);
+    OV_CUDA(c, cudaGetLastError());
+    if ((r = collect_stats(c, true))) return r;
+    return error_from_word(c);
+}
+
 int ov_update_velocities(ov_ctx *c, double t)
 {
     int r = check_ready(c);
     if (r) return r;
-    return eval_sync(c, c->node, t, false);
+    return ov_eval_sync(c, c->node, t, false);
 }
 
 int ov_update_tangle(ov_ctx *c, double t)
 {
     int r = check_ready(c);
     if (r) return r;
-    return eval_sync(c, c->node, t, true);
+    return ov_eval_sync(c, c->node, t, true);
 }
 
 // RK4 (vortex_dynamics.c:50-119) from k1 = the context's current vels.
@@ -459,7 +520,7 @@ int ov_rk4_step(ov_ctx *c, double t, double dt)
     int64_t err = 0;
     for (int k = 0; k < 3; ++k) {
         ov_launch_euler(c, c->node, vin[k][0], vin[k][1], vin[k][2], dt / 2, c->stage[k], s);
-        if ((r = eval_sync(c, c->stage[k], tt[k], true))) return r;
+        if ((r = ov_eval_sync(c, c->stage[k], tt[k], true))) return r;
         err |= c->stats.error_word;
     }
     ov_launch_rk4_combine(c, dt, s);
@@ -483,6 +544,7 @@ int ov_enforce_periodic_boundaries(ov_ctx *c)
 {
     int r = check_ready(c);
     if (r) return r;
+    c->tree_built = false;
     ov_launch_periodic_wrap(c, c->stream);
     OV_CUDA(c, cudaGetLastError());
     OV_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -33,7 +33,8 @@ enum {
     OV_EW_ITER = 8,       // traversal exceeded its iteration bound
     OV_EW_NAN = 16,       // non-finite position
     OV_EW_RUN = 32,       // sort fix-up met a run longer than its bound
-    OV_EW_CELLS = 64      // cell storage too small: host grows it and rebuilds
+    OV_EW_CELLS = 64,     // cell storage too small: host grows it and rebuilds
+    OV_EW_BOUNDS = 128    // an index failed a bounds check (access skipped)
 };
 
 struct Cell64 {          // 64 bytes, one per cell, pre-order
@@ -84,6 +85,7 @@ enum TreeCounters {
     TC_FALLBACK,       // mixed: guard-band FP64 decisions
     TC_NEAR64,         // mixed: near-field FP64 interactions
     TC_NEED,           // cells the tree needs (checked against the storage)
+    TC_BAD,            // first failed bounds check: code << 24 | low bits of the index
     TC_COUNT,
     TC_STAT64 = 16,    // int offset of the 64-bit counters: visits, accepts, warp steps, ...
     TC_WORDS = 32      // ints allocated (and cleared per build)
@@ -122,6 +124,7 @@ struct ov_ctx {
     cudaStream_t stream = nullptr;
     ov_params params{};
     int precision = OV_PREC_FP64;
+    bool tree_built = false;     // the tree matches node positions (tree queries)
     std::string err;
     int cap = 0;                 // node slots
     int n_live = 0;              // slots of the uploaded tangle (<= cap)
@@ -137,9 +140,20 @@ struct ov_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     void *flush_buf = nullptr;
     size_t flush_bytes = 0;
-    // host mirrors for the sequential topology passes
-    std::vector<double> h_pos;   // AoS xyz
-    std::vector<int> h_fwd, h_rev, h_status, h_pin;
+    // host mirrors for the sequential topology passes (valid between
+    // ov_pull_host and ov_push_device)
+    std::vector<double> h_x, h_y, h_z;
+    std::vector<int> h_fwd, h_rev, h_status, h_pin, h_recalc;
+    int next_empty = -1, total_empty = 0;   // tangle_state bookkeeping (tangle.h:63-64)
+    // reconnect / smoothing scratch
+    uint64_t *d_gkeys = nullptr, *d_gkeys_alt = nullptr;
+    int *d_gidx = nullptr, *d_gidx_alt = nullptr;
+    int *d_pairs = nullptr, *d_npairs = nullptr;
+    int pair_cap = 0;
+    int *d_loop_nodes = nullptr, *d_loop_off = nullptr;
+    double *d_loop_buf = nullptr;
+    int loop_cap = 0, loop_nodes_cap = 0;
+    size_t loop_buf_cap = 0;
     // RK4 graph
     cudaGraphExec_t rk4_exec = nullptr;
     double rk4_dt = 0, rk4_t = 0;
@@ -178,6 +192,11 @@ inline unsigned long long *ov_stat_ptr(ov_ctx *c)
 
 // tree build (ov_tree.cu)
 int ov_tree_reserve(ov_ctx *c, int cap);
+// grow the node arrays to `cap` slots keeping their contents (topology passes)
+int ov_grow_preserving(ov_ctx *c, int cap);
+int ov_pull_host(ov_ctx *c);     // positions + topology -> host mirrors
+int ov_push_device(ov_ctx *c, int first_new_slot);  // host mirrors -> device
+int ov_eval_sync(ov_ctx *c, NodeArrays &na, double t, bool tangents);
 int ov_tree_reserve_cells(ov_ctx *c, int cells);
 void ov_tree_free(TreeBuf &t);
 int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s);

@@ -1,10 +1,1091 @@
-// ov_topology.cu - topology passes (reconnect, remesh, small loops, smoothing).
+// ov_topology.cu - topology passes of the time step.
+//
+//  ov_reconnect           reconnect (vortex_dynamics.c:186-288)
+//  ov_remesh              remesh + add_point + remove_point + slot allocation
+//                         (tangle.c:1018-1061, 261-355, 201-253, 68-101)
+//  ov_eliminate_small_loops (tangle.c:1063-1128)
+//  ov_smooth              smooth / high_freq_cutoff / low_pass_filter
+//                         (vortex_smooth.c:134-175, 183-453, 459-462)
+//  ov_step                one main-loop body (main.c:125-141)
+//
+// The reference's passes are sequential: a reconnection rewires connections
+// that later candidates see, and remesh walks the slots in index order,
+// visiting nodes it inserted in the same pass.  Those decisions are taken
+// here on the host, in the reference's order and FP64 rounding, on host
+// mirrors of positions and topology; the GPU does the parallel parts:
+//   * reconnect: candidate pairs within rec_dist from a uniform grid over a
+//     key sort of the nodes (cell side >= 2 rec_dist, so 27 neighbour cells
+//     are enough even for nodes within rounding of a cell face), and the
+//     O(N (1+n_img)) direct-sum velocities of every candidate node in one
+//     batch; rewiring changes four segments, whose contributions the host
+//     subtracts/adds for later candidates, and a decision whose dx.dv sits
+//     within 1e-9 of zero is recomputed in the reference's summation order;
+//   * smoothing: one block per closed loop (the loop decomposition is host
+//     work): unwrap, optional detrend / odd extension, low-pass DFT on the
+//     kept bins only, write back.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
 #include "ov_internal.cuh"
 
-extern "C" {
-int ov_eliminate_small_loops(ov_ctx *c) { return ov_fail(c, OV_ERR_STATE, "not built yet"); }
-int ov_reconnect(ov_ctx *c, double, int *, int *, int *, int) { return ov_fail(c, OV_ERR_STATE, "not built yet"); }
-int ov_remesh(ov_ctx *c, double, double, double) { return ov_fail(c, OV_ERR_STATE, "not built yet"); }
-int ov_smooth(ov_ctx *c) { return ov_fail(c, OV_ERR_STATE, "not built yet"); }
-int ov_step(ov_ctx *c, double, double) { return ov_fail(c, OV_ERR_STATE, "not built yet"); }
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+#ifndef M_E
+#define M_E 2.7182818284590452354
+#endif
+
+int ov_direct_raw(ov_ctx *c, const int *nodes, int n, double *sums_out);
+
+namespace {
+
+// ------------------------------------------------------------ host math
+// vec3_math.c operation order; this file's host code is compiled with
+// -ffp-contract=off.
+inline double hdot(const double a[3], const double b[3])
+{
+    double o = 0;
+    o += a[0] * b[0];
+    o += a[1] * b[1];
+    o += a[2] * b[2];
+    return o;
 }
+inline double hlen(const double a[3]) { return sqrt(hdot(a, a)); }
+inline void hsub(double r[3], const double a[3], const double b[3])
+{
+    for (int i = 0; i < 3; ++i) r[i] = a[i] - b[i];
+}
+inline void hcross(double r[3], const double u[3], const double v[3])
+{
+    double a0 = u[1] * v[2] - u[2] * v[1], a1 = u[2] * v[0] - u[0] * v[2], a2 = u[0] * v[1] - u[1] * v[0];
+    r[0] = a0; r[1] = a1; r[2] = a2;
+}
+
+// seg_pwrap (boundaries.c:54-83)
+inline void hpwrap(const Geometry &g, const double r1[3], double r2[3])
+{
+    for (int a = 0; a < 3; ++a) {
+        if (!g.periodic[a]) continue;
+        double L = g.L[a];
+        int guard = 0;
+        while ((r2[a] - r1[a]) > L / 2 && guard++ < 1000) r2[a] -= L;
+        while ((r2[a] - r1[a]) < -L / 2 && guard++ < 2000) r2[a] += L;
+    }
+}
+// segment_len of seg_pwrap(r1, r2): |r1 - r2'|
+inline double hpwrap_len(const Geometry &g, const double r1[3], const double r2in[3])
+{
+    double r2[3] = {r2in[0], r2in[1], r2in[2]};
+    hpwrap(g, r1, r2);
+    double d[3];
+    hsub(d, r1, r2);
+    return hlen(d);
+}
+
+struct Host {
+    ov_ctx *c;
+    int N() const { return c->n_live; }
+    void pos(int i, double p[3]) const { p[0] = c->h_x[i]; p[1] = c->h_y[i]; p[2] = c->h_z[i]; }
+    int &fwd(int i) { return c->h_fwd[i]; }
+    int &rev(int i) { return c->h_rev[i]; }
+    int &st(int i) { return c->h_status[i]; }
+    int &pin(int i) { return c->h_pin[i]; }
+};
+
+inline bool pinned(int s) { return s == OV_PINNED || s == OV_PINNED_SLIP; }
+
+// step_node (tangle.c:155-194)
+bool hstep(Host &h, int i, int where, double out[3])
+{
+    int walls[8], nw = 0, cur = i, w = where;
+    for (int guard = 0; w != 0; ++guard) {
+        if (guard > 16 || cur < 0 || cur >= h.N()) return false;
+        int s = h.st(cur);
+        if (s == OV_FREE) {
+            cur = w > 0 ? h.fwd(cur) : h.rev(cur);
+            w += w > 0 ? -1 : 1;
+        } else if (pinned(s)) {
+            int nb = w > 0 ? h.fwd(cur) : h.rev(cur);
+            if (nb >= 0) { cur = nb; w += w > 0 ? -1 : 1; }
+            else {
+                if (nw >= 8) return false;
+                walls[nw++] = h.pin(cur);
+                w = -w;
+            }
+        } else {
+            return false;
+        }
+    }
+    if (cur < 0 || cur >= h.N() || h.st(cur) == OV_EMPTY) return false;
+    h.pos(cur, out);
+    const Geometry &g = h.c->geo;
+    for (int m = nw - 1; m >= 0; --m) {
+        int f = walls[m];
+        if (f < 0 || f > 5) continue;
+        int ax = f >> 1;
+        double wp = (f & 1) ? g.hi[ax] : g.lo[ax];
+        out[ax] = 2 * wp - out[ax];
+    }
+    return true;
+}
+
+// update_tangent_normal (tangle.c:423-502)
+bool htangent(Host &h, int k, double tg[3], double nm[3])
+{
+    const Geometry &g = h.c->geo;
+    double s0[3], s1[3], s2[3], sm1[3], sm2[3];
+    h.pos(k, s0);
+    if (!(hstep(h, k, 1, s1) && hstep(h, k, 2, s2) && hstep(h, k, -1, sm1) && hstep(h, k, -2, sm2))) return false;
+    double w2[3] = {s2[0], s2[1], s2[2]}, w1[3] = {s1[0], s1[1], s1[2]};
+    double wm1[3] = {sm1[0], sm1[1], sm1[2]}, wm2[3] = {sm2[0], sm2[1], sm2[2]};
+    hpwrap(g, s0, w2); hpwrap(g, s0, w1); hpwrap(g, s0, wm1); hpwrap(g, s0, wm2);
+    double ds[4][3];
+    hsub(ds[0], w2, s0); hsub(ds[1], w1, s0); hsub(ds[2], wm1, s0); hsub(ds[3], wm2, s0);
+    double t1[3], t2[3];
+    hsub(t1, s0, w1);
+    double d1 = hlen(t1);
+    double d2 = d1 + hpwrap_len(g, s1, s2);
+    hsub(t2, s0, wm1);
+    double dm1 = hlen(t2);
+    double dm2 = dm1 + hpwrap_len(g, sm1, sm2);
+    double den[4] = {d2 * (d2 - d1) * (dm1 + d2) * (dm2 + d2), d1 * (d2 - d1) * (dm1 + d1) * (dm2 + d1),
+                     dm1 * (dm1 + d1) * (dm1 + d2) * (dm2 - dm1), dm2 * (dm2 + d1) * (dm2 + d2) * (dm2 - dm1)};
+    double c1[4] = {-d1 * dm1 * dm2, d2 * dm1 * dm2, -d1 * d2 * dm2, d1 * d2 * dm1};
+    double c2[4] = {2 * ((dm1 - d1) * dm2 - d1 * dm1), -2 * ((dm1 - d2) * dm2 - d2 * dm1),
+                    2 * ((d2 + d1) * dm2 - d1 * d2), -2 * ((d2 + d1) * dm1 - d1 * d2)};
+    for (int a = 0; a < 3; ++a) {
+        double tt = 0, nn = 0;
+        for (int z = 0; z < 4; ++z) {
+            tt += c1[z] / den[z] * ds[z][a];
+            nn += c2[z] / den[z] * ds[z][a];
+        }
+        tg[a] = tt;
+        nm[a] = nn;
+    }
+    return true;
+}
+
+// get_v (external_velocity.c:62-81)
+void hext(const ov_ext_vel &e, double t, double out[3])
+{
+    out[0] = out[1] = out[2] = 0;
+    if (e.type != OV_SIMPLE && e.type != OV_DECREASING) return;
+    double d[3] = {e.direction.p[0], e.direction.p[1], e.direction.p[2]};
+    if (!(d[0] == 0 && d[1] == 0 && d[2] == 0)) {
+        double inv = 1 / hlen(d);
+        for (int a = 0; a < 3; ++a) d[a] = d[a] * inv;
+    }
+    double s = e.strength;
+    if (e.type == OV_DECREASING && t < e.time_of_linear_decrease)
+        s = e.starting_strength - t * (e.starting_strength - e.strength) / e.time_of_linear_decrease;
+    for (int a = 0; a < 3; ++a) out[a] = d[a] * s;
+}
+
+// the segment law of segment_field (tangle.c:536-559)
+bool hlaw(const double R[3], const double Rp1[3], double kappa, double out[3])
+{
+    double lR = hlen(R), lRp1 = hlen(Rp1);
+    double denom = lR * lRp1 * (lR * lRp1 + hdot(R, Rp1));
+    double f = kappa / 4 / M_PI;
+    if (lR < 1e-8 || lRp1 < 1e-8) return false;
+    if (hdot(R, Rp1) / hlen(R) / hlen(Rp1) < 1e-8) return false;
+    double cr[3];
+    hcross(cr, R, Rp1);
+    double m = f * (lR + lRp1) / denom;
+    for (int a = 0; a < 3; ++a) out[a] = cr[a] * m;
+    return true;
+}
+
+// shifted (tangle.c:370-414)
+void himage(const Geometry &g, int j, const double p[3], double q[3])
+{
+    for (int a = 0; a < 3; ++a) q[a] = p[a] - g.L[a] * g.shift[j][a];
+    for (int m = 0; m < g.nreflect[j]; ++m) {
+        int f = g.reflect[j][m];
+        if (f < 0 || f > 5) continue;
+        int ax = f >> 1;
+        double w = (f & 1) ? g.hi[ax] : g.lo[ax];
+        q[ax] = 2 * w - p[ax];
+    }
+}
+
+// contribution of segment m -> f at point r (segment_field)
+bool hsegment(Host &h, int m, int f, const double r[3], double out[3])
+{
+    double a[3], b[3];
+    h.pos(m, a);
+    h.pos(f, b);
+    hpwrap(h.c->geo, a, b);
+    double R[3], Rp1[3];
+    hsub(R, a, r);
+    hsub(Rp1, b, r);
+    return hlaw(R, Rp1, h.c->params.kappa, out);
+}
+
+// lia_velocity (tangle.c:568-592) + external v_s, given tangent/normal
+bool hlia(Host &h, int i, const double tg[3], const double nm[3], double t, double vs[3])
+{
+    double p[3], nx[3], pv[3];
+    h.pos(i, p);
+    if (!(hstep(h, i, 1, nx) && hstep(h, i, -1, pv))) return false;
+    const ov_params &P = h.c->params;
+    double l_next = hpwrap_len(h.c->geo, p, nx);
+    double l_prev = hpwrap_len(h.c->geo, pv, p);
+    double f = P.kappa * log(2 * sqrt(l_next * l_prev) / sqrt(M_E) / P.vortex_width) / 4 / M_PI;
+    double cr[3];
+    hcross(cr, tg, nm);
+    double ev[3];
+    hext(P.vs, t, ev);
+    for (int a = 0; a < 3; ++a) vs[a] = cr[a] * f + ev[a];
+    return true;
+}
+
+// vels from vs: mutual friction and PINNED_SLIP (tangle.c:694-725)
+void hfriction(Host &h, int k, const double tg[3], const double vs[3], double t, double vel[3])
+{
+    const ov_params &P = h.c->params;
+    for (int a = 0; a < 3; ++a) vel[a] = vs[a];
+    if (P.use_mutual_friction) {
+        double vn[3], dv[3], c1[3], c2[3];
+        hext(P.vn, t, vn);
+        hsub(dv, vn, vs);
+        hcross(c1, tg, dv);
+        for (int a = 0; a < 3; ++a) vel[a] = vel[a] + c1[a] * P.alpha;
+        hcross(c2, tg, c1);
+        for (int a = 0; a < 3; ++a) vel[a] = vel[a] + c2[a] * -P.alpha_p;
+    }
+    if (h.st(k) == OV_PINNED_SLIP) {
+        int f = h.pin(k);
+        if (f >= 0 && f < 6) {
+            int ax = f >> 1;
+            double n = (f & 1) ? -1.0 : 1.0;
+            double nv = n * vel[ax];
+            vel[ax] = vel[ax] - n * nv;
+        }
+    }
+}
+
+// update_velocity(k, tree=NULL) exactly as the reference sums it: into vs in
+// segment-index order, primary then images.
+bool hdirect_exact(Host &h, int k, const double tg[3], const double nm[3], double t, double vel[3])
+{
+    double vs[3];
+    if (!hlia(h, k, tg, nm, t, vs)) return false;
+    double x[3];
+    h.pos(k, x);
+    const Geometry &g = h.c->geo;
+    int N = h.N();
+    for (int m = 0; m < N; ++m) {
+        int f = h.fwd(m);
+        if (f == -1 || k == m || k == f) continue;
+        double w[3];
+        if (hsegment(h, m, f, x, w))
+            for (int a = 0; a < 3; ++a) vs[a] = vs[a] + w[a];
+    }
+    for (int j = 0; j < g.n_img; ++j) {
+        double q[3];
+        himage(g, j, x, q);
+        for (int m = 0; m < N; ++m) {
+            int f = h.fwd(m);
+            if (f == -1) continue;
+            double w[3];
+            if (hsegment(h, m, f, q, w))
+                for (int a = 0; a < 3; ++a) vs[a] = vs[a] + w[a];
+        }
+    }
+    hfriction(h, k, tg, vs, t, vel);
+    return true;
+}
+
+// ------------------------------------------------------------- GPU parts
+struct GridGeom {
+    double lo[3], L[3];
+    int n[3];
+    int periodic[3];
+};
+
+__global__ void k_grid_keys(const int *__restrict__ status, const double *__restrict__ x,
+                            const double *__restrict__ y, const double *__restrict__ z, int n_live, int cap,
+                            GridGeom gg, uint64_t *__restrict__ keys, int *__restrict__ idx)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    idx[i] = i;
+    int s = i < n_live ? status[i] : OV_EMPTY;
+    if (s != OV_FREE) { keys[i] = ~0ull; return; }
+    double p[3] = {x[i], y[i], z[i]};
+    unsigned cell[3];
+    for (int a = 0; a < 3; ++a) {
+        double u = (p[a] - gg.lo[a]) / gg.L[a];
+        u -= floor(u);
+        int ci = (int)(u * gg.n[a]);
+        cell[a] = (unsigned)min(max(ci, 0), gg.n[a] - 1);
+    }
+    uint64_t cid = ((uint64_t)cell[2] * gg.n[1] + cell[1]) * gg.n[0] + cell[0];
+    keys[i] = (cid << 32) | (uint64_t)i;
+}
+
+__device__ __forceinline__ int lower_key(const uint64_t *keys, int n, uint64_t v)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (keys[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_pairs(const uint64_t *__restrict__ keys, const int *__restrict__ idx, int cap,
+                        const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+                        GridGeom gg, Geometry geo, double rec_dist, int *__restrict__ pairs, int *npairs,
+                        int pair_cap)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    uint64_t key = keys[i];
+    if (key == ~0ull) return;
+    int k = idx[i];
+    uint64_t cid = key >> 32;
+    int c[3] = {(int)(cid % gg.n[0]), (int)((cid / gg.n[0]) % gg.n[1]), (int)(cid / ((uint64_t)gg.n[0] * gg.n[1]))};
+    double pk[3] = {x[k], y[k], z[k]};
+    int lo3[3], hi3[3];
+    for (int a = 0; a < 3; ++a) {
+        if (gg.n[a] >= 3) { lo3[a] = -1; hi3[a] = 1; }
+        else if (gg.n[a] == 2) { lo3[a] = 0; hi3[a] = 1; }
+        else { lo3[a] = 0; hi3[a] = 0; }
+    }
+    for (int dz = lo3[2]; dz <= hi3[2]; ++dz)
+        for (int dy = lo3[1]; dy <= hi3[1]; ++dy)
+            for (int dx = lo3[0]; dx <= hi3[0]; ++dx) {
+                int nc[3] = {c[0] + dx, c[1] + dy, c[2] + dz};
+                bool skip = false;
+                for (int a = 0; a < 3; ++a) {
+                    if (gg.n[a] <= 2) { nc[a] = ((nc[a] % gg.n[a]) + gg.n[a]) % gg.n[a]; continue; }
+                    if (nc[a] < 0 || nc[a] >= gg.n[a]) {
+                        if (!gg.periodic[a]) skip = true;
+                        nc[a] = (nc[a] + gg.n[a]) % gg.n[a];
+                    }
+                }
+                if (skip) continue;
+                uint64_t ncid = ((uint64_t)nc[2] * gg.n[1] + nc[1]) * gg.n[0] + nc[0];
+                int b = lower_key(keys, cap, ncid << 32), e = lower_key(keys, cap, (ncid + 1) << 32);
+                for (int j = b; j < e; ++j) {
+                    int l = idx[j];
+                    if (l <= k) continue;
+                    double v2[3] = {x[l], y[l], z[l]};
+                    pwrap_dev(geo, pk, v2);
+                    double d = len3_ref(rn_sub(pk[0], v2[0]), rn_sub(pk[1], v2[1]), rn_sub(pk[2], v2[2]));
+                    if (d > rec_dist) continue;
+                    int slot = atomicAdd(npairs, 1);
+                    if (slot < pair_cap) { pairs[2 * slot] = k; pairs[2 * slot + 1] = l; }
+                }
+            }
+}
+
+__global__ void k_zero_vel(const int *__restrict__ ids, int n, double *vx, double *vy, double *vz, double *sx,
+                           double *sy, double *sz)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int k = ids[i];
+    vx[k] = vy[k] = vz[k] = 0;
+    sx[k] = sy[k] = sz[k] = 0;
+}
+
+// ---- smoothing: one block per closed loop
+struct SmoothArgs {
+    const int *loop_off, *loop_nodes;
+    double *x, *y, *z;
+    double *buf;               // 3 * 2 * total nodes
+    Geometry geo;
+    double freq_to_cutoff;
+};
+
+__global__ void __launch_bounds__(256) k_smooth(SmoothArgs a)
+{
+    const int lp = blockIdx.x;
+    const int b0 = a.loop_off[lp], len = a.loop_off[lp + 1] - b0;
+    const int *nodes = a.loop_nodes + b0;
+    double *X[3];
+    for (int ax = 0; ax < 3; ++ax) X[ax] = a.buf + (size_t)(2 * b0) * 3 + (size_t)ax * 2 * len;
+    __shared__ int s_detrend, s_n;
+    __shared__ double s_coef[3], s_c0[3];
+    if (threadIdx.x == 0) {
+        // unwrap along the loop (vortex_smooth.c:218-242)
+        int k = nodes[0];
+        double prev[3] = {a.x[k], a.y[k], a.z[k]};
+        for (int ax = 0; ax < 3; ++ax) X[ax][0] = prev[ax];
+        for (int j = 1; j < len; ++j) {
+            int m = nodes[j];
+            double r2[3] = {a.x[m], a.y[m], a.z[m]};
+            double r1[3] = {X[0][j - 1], X[1][j - 1], X[2][j - 1]};
+            pwrap_dev(a.geo, r1, r2);
+            for (int ax = 0; ax < 3; ++ax) X[ax][j] = r2[ax];
+        }
+        double gx = X[0][0] - X[0][len - 1], gy = X[1][0] - X[1][len - 1], gz = X[2][0] - X[2][len - 1];
+        double gap = sqrt(gx * gx + gy * gy + gz * gz);
+        s_detrend = (gap > a.geo.L[0] / 2 && len > 2) ? 1 : 0;
+        s_n = s_detrend ? 2 * len - 2 : len;
+        if (s_detrend) {
+            for (int ax = 0; ax < 3; ++ax) {
+                s_coef[ax] = (X[ax][len - 1] - X[ax][0]) / (len - 1);
+                s_c0[ax] = X[ax][0];
+            }
+        }
+    }
+    __syncthreads();
+    const int N = s_n;
+    if (s_detrend) {
+        // vortex_smooth.c:252-279: subtract the chord, odd extension
+        for (int j = threadIdx.x; j < len; j += blockDim.x)
+            for (int ax = 0; ax < 3; ++ax)
+                X[ax][j] = (j == 0 || j == len - 1) ? 0.0 : X[ax][j] - s_coef[ax] * j - s_c0[ax];
+        __syncthreads();
+        for (int j = threadIdx.x; j < len - 2; j += blockDim.x)
+            for (int ax = 0; ax < 3; ++ax) X[ax][len + j] = -X[ax][len - 2 - j];
+        __syncthreads();
+    }
+    // low_pass_filter (vortex_smooth.c:134-175) on the kept half-complex bins
+    int cut = (int)(a.freq_to_cutoff * N / 2);
+    int zlo = 0, zhi = 0;
+    if (N > 2 * cut + 1) {
+        zlo = N / 2 - cut;
+        zhi = (N % 2 == 0) ? N / 2 + 1 + cut : N / 2 + cut;
+    }
+    // dynamic shared memory: twiddles cos/sin(2 pi m / N) for m in [0, N),
+    // cosine bins [0, N/2] and sine bins [1, (N-1)/2] per coordinate
+    extern __shared__ double sh[];
+    const int ncos = N / 2 + 1, nsin = (N - 1) / 2;
+    double *TC = sh, *TS = sh + N;
+    double *RC = sh + 2 * N, *IS = RC + 3 * ncos;   // [ax][k]
+    for (int m = threadIdx.x; m < N; m += blockDim.x) sincospi(2.0 * (double)m / N, &TS[m], &TC[m]);
+    __syncthreads();
+    for (int kk = threadIdx.x; kk < ncos + nsin; kk += blockDim.x) {
+        bool is_cos = kk < ncos;
+        int k = is_cos ? kk : kk - ncos + 1;
+        int hcidx = is_cos ? k : N - k;
+        bool kept = !(hcidx >= zlo && hcidx < zhi);
+        double acc[3] = {0, 0, 0};
+        if (kept) {
+            int m = 0;
+            for (int j = 0; j < N; ++j) {
+                double tw = is_cos ? TC[m] : -TS[m];
+                for (int ax = 0; ax < 3; ++ax) acc[ax] += X[ax][j] * tw;
+                m += k;
+                if (m >= N) m -= N;
+            }
+        }
+        for (int ax = 0; ax < 3; ++ax) {
+            if (is_cos) RC[ax * ncos + k] = acc[ax];
+            else IS[ax * nsin + (k - 1)] = acc[ax];
+        }
+    }
+    __syncthreads();
+    // highest bin that survived the cut (bins above it are all zero)
+    int kmax = (zhi > zlo) ? max(zlo - 1, N - zhi) : N / 2;
+    for (int j = threadIdx.x; j < len; j += blockDim.x) {
+        double s[3] = {RC[0], RC[ncos], RC[2 * ncos]};
+        int m = 0;
+        for (int k = 1; k < N - k && k <= kmax; ++k) {
+            m += j;
+            if (m >= N) m -= N * (m / N);
+            double cv = TC[m], sv = TS[m];
+            for (int ax = 0; ax < 3; ++ax) s[ax] += 2 * (RC[ax * ncos + k] * cv - IS[ax * nsin + (k - 1)] * sv);
+        }
+        if (N % 2 == 0)
+            for (int ax = 0; ax < 3; ++ax) s[ax] += RC[ax * ncos + N / 2] * ((j % 2) ? -1.0 : 1.0);
+        double out[3];
+        for (int ax = 0; ax < 3; ++ax) {
+            out[ax] = s[ax] / N;
+            if (s_detrend) out[ax] = out[ax] + s_coef[ax] * j + s_c0[ax];
+        }
+        int node = nodes[j];
+        a.x[node] = out[0]; a.y[node] = out[1]; a.z[node] = out[2];
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ host mirror
+int ov_pull_host(ov_ctx *c)
+{
+    int n = c->n_live;
+    c->h_x.resize(n); c->h_y.resize(n); c->h_z.resize(n);
+    c->h_fwd.resize(n); c->h_rev.resize(n); c->h_status.resize(n); c->h_pin.resize(n);
+    c->h_recalc.assign(n, 0);
+    if (n == 0) return OV_OK;
+    double *dd[3] = {c->node.x, c->node.y, c->node.z};
+    double *hd[3] = {c->h_x.data(), c->h_y.data(), c->h_z.data()};
+    for (int a = 0; a < 3; ++a)
+        OV_CUDA(c, cudaMemcpyAsync(hd[a], dd[a], (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+    int *di[4] = {c->fwd, c->rev, c->status, c->pin};
+    int *hi[4] = {c->h_fwd.data(), c->h_rev.data(), c->h_status.data(), c->h_pin.data()};
+    for (int a = 0; a < 4; ++a)
+        OV_CUDA(c, cudaMemcpyAsync(hi[a], di[a], (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    return OV_OK;
+}
+
+int ov_push_device(ov_ctx *c, int pos_too)
+{
+    int n = c->n_live;
+    c->tree_built = false;
+    if (n > c->cap) {
+        int r = ov_grow_preserving(c, n);
+        if (r) return r;
+    }
+    if (n == 0) return OV_OK;
+    if (pos_too) {
+        double *dd[3] = {c->node.x, c->node.y, c->node.z};
+        double *hd[3] = {c->h_x.data(), c->h_y.data(), c->h_z.data()};
+        for (int a = 0; a < 3; ++a)
+            OV_CUDA(c, cudaMemcpyAsync(dd[a], hd[a], (size_t)n * 8, cudaMemcpyHostToDevice, c->stream));
+    }
+    int *di[4] = {c->fwd, c->rev, c->status, c->pin};
+    int *hi[4] = {c->h_fwd.data(), c->h_rev.data(), c->h_status.data(), c->h_pin.data()};
+    for (int a = 0; a < 4; ++a)
+        OV_CUDA(c, cudaMemcpyAsync(di[a], hi[a], (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    return OV_OK;
+}
+
+namespace {
+
+int ready(ov_ctx *c)
+{
+    if (!c) return OV_ERR_ARG;
+    if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
+    cudaSetDevice(c->device);
+    return OV_OK;
+}
+
+// ------------------------------------------------------- slot allocation
+// expand_tangle (tangle.c:68-101): the pool doubles, new slots EMPTY
+void hexpand(ov_ctx *c, int n);
+
+// search_next_empty_node (tangle.c:201-234); a slot past the end counts as
+// not empty where the reference reads status[k+1] out of bounds.
+int hsearch_empty(ov_ctx *c)
+{
+    Host h{c};
+    int N = h.N();
+    if (c->next_empty > 0) {
+        if (c->next_empty < N && h.st(c->next_empty) == OV_EMPTY) {
+            int id = c->next_empty;
+            if (c->next_empty + 1 < N && h.st(c->next_empty + 1) == OV_EMPTY) ++c->next_empty;
+            else c->next_empty = -1;
+            return id;
+        }
+    }
+    for (int k = 0; k < N; ++k) {
+        if (h.st(k) == OV_EMPTY) {
+            c->next_empty = (k + 1 < N && h.st(k + 1) == OV_EMPTY) ? k + 1 : -1;
+            return k;
+        }
+    }
+    return -1;
+}
+
+// get_next_empty_node (tangle.c:241-253)
+int hget_empty(ov_ctx *c)
+{
+    int id = hsearch_empty(c);
+    while (id < 0 || c->h_status[id] != OV_EMPTY) {
+        hexpand(c, 2 * c->n_live > 0 ? 2 * c->n_live : 1);
+        id = hsearch_empty(c);
+    }
+    return id;
+}
+
+void hexpand(ov_ctx *c, int n)
+{
+    int old = c->n_live;
+    c->h_x.resize(n, 0.0); c->h_y.resize(n, 0.0); c->h_z.resize(n, 0.0);
+    c->h_fwd.resize(n, -1); c->h_rev.resize(n, -1);
+    c->h_status.resize(n, OV_EMPTY); c->h_pin.resize(n, OV_NOT_A_FACE);
+    c->h_recalc.resize(n, 0);
+    for (int k = old; k < n; ++k) {
+        c->h_status[k] = OV_EMPTY; c->h_pin[k] = OV_NOT_A_FACE;
+        c->h_fwd[k] = -1; c->h_rev[k] = -1;
+    }
+    c->n_live = n;
+    c->total_empty += n - old;
+    c->next_empty = hget_empty(c);
+}
+
+// out_of_box + periodic_shift (tangle.c:761-814, boundaries.c:113-150)
+void hperiodic(ov_ctx *c)
+{
+    Host h{c};
+    const Geometry &g = c->geo;
+    for (int k = 0; k < h.N(); ++k) {
+        if (h.st(k) == OV_EMPTY) continue;
+        double p[3];
+        h.pos(k, p);
+        for (int guard = 0; guard < 1000; ++guard) {
+            int face = -1;
+            if (p[0] < g.lo[0]) face = OV_LEFT;
+            if (p[0] > g.hi[0]) face = OV_RIGHT;
+            if (p[1] < g.lo[1]) face = OV_BACK;
+            if (p[1] > g.hi[1]) face = OV_FRONT;
+            if (p[2] < g.lo[2]) face = OV_DOWN;
+            if (p[2] > g.hi[2]) face = OV_UP;
+            if (face > -1 && g.wall[face] != OV_WALL_PERIODIC) face = -1;
+            if (face < 0) break;
+            int ax = face >> 1;
+            if (face % 2 == 0) p[ax] += g.L[ax];
+            else p[ax] -= g.L[ax];
+        }
+        c->h_x[k] = p[0]; c->h_y[k] = p[1]; c->h_z[k] = p[2];
+    }
+}
+
+// eliminate_small_loops (tangle.c:1063-1128); returns nodes removed
+int hsmall_loops(ov_ctx *c)
+{
+    Host h{c};
+    int N = h.N(), removed = 0;
+    std::vector<char> seen(N > 0 ? N : 1, 0);
+    for (int k = 0; k < N; ++k) {
+        if (h.st(k) == OV_EMPTY || seen[k]) continue;
+        seen[k] = 1;
+        int steps = 0, here = k, nx = h.fwd(here);
+        while (nx != k) {
+            if (pinned(h.st(here)) && nx < 0) {
+                here = k;
+                nx = h.rev(here);
+                while (nx >= 0) {
+                    seen[here] = 1;
+                    here = nx;
+                    nx = h.rev(here);
+                    steps++;
+                }
+                break;
+            }
+            if (nx < 0 || nx >= N) break;
+            seen[here] = 1;
+            here = nx;
+            nx = h.fwd(here);
+            steps++;
+            if (steps > N) break;
+        }
+        if (steps < c->params.small_loop_cutoff) {
+            nx = here;
+            for (int guard = 0; guard <= N; ++guard) {
+                int cur = nx;
+                nx = h.fwd(nx);
+                h.fwd(cur) = -1;
+                h.rev(cur) = -1;
+                h.st(cur) = OV_EMPTY;
+                removed++;
+                if (nx == here || nx < 0) break;
+            }
+        }
+    }
+    return removed;
+}
+
+// add_point (tangle.c:261-335)
+int hadd_point(ov_ctx *c, int p, std::vector<int> &new_nodes)
+{
+    int np = hget_empty(c);
+    Host h{c};
+    h.st(np) = OV_FREE;
+    h.pin(np) = OV_NOT_A_FACE;
+    int nx = h.fwd(p);
+    double tg[3], n0[3], n1[3];
+    htangent(h, p, tg, n0);
+    htangent(h, nx, tg, n1);
+    double s0[3], s1[3];
+    h.pos(p, s0);
+    h.pos(nx, s1);
+    hpwrap(c->geo, s0, s1);
+    double dd[3];
+    hsub(dd, s0, s1);
+    double l = hlen(dd);
+    double n[3], pos[3];
+    for (int a = 0; a < 3; ++a) n[a] = (n0[a] + n1[a]) * 0.5;
+    if (hlen(n) > 1e-5) {
+        double R = 1 / hlen(n);
+        double dR = R * R - l * l / 4;
+        double delta = dR > 0 ? R - sqrt(dR) : R;
+        if (!(n[0] == 0 && n[1] == 0 && n[2] == 0)) {
+            double inv = 1 / hlen(n);
+            for (int a = 0; a < 3; ++a) n[a] = n[a] * inv;
+        }
+        for (int a = 0; a < 3; ++a) n[a] = n[a] * -1;
+        for (int a = 0; a < 3; ++a) pos[a] = (s0[a] + s1[a]) * 0.5 + n[a] * delta;
+    } else {
+        for (int a = 0; a < 3; ++a) pos[a] = (s0[a] + s1[a]) * 0.5;
+    }
+    c->h_x[np] = pos[0]; c->h_y[np] = pos[1]; c->h_z[np] = pos[2];
+    h.rev(np) = p;
+    h.fwd(np) = nx;
+    h.fwd(p) = np;
+    h.rev(nx) = np;
+    new_nodes.push_back(np);
+    return np;
+}
+
+// remove_point (tangle.c:342-355)
+void hremove(ov_ctx *c, int i)
+{
+    Host h{c};
+    int pv = h.rev(i), nx = h.fwd(i);
+    if (pv >= 0) h.fwd(pv) = nx;
+    if (nx >= 0) h.rev(nx) = pv;
+    h.rev(i) = h.fwd(i) = -1;
+    h.st(i) = OV_EMPTY;
+}
+
+void hremesh(ov_ctx *c, double min_dist, double max_dist, int *added_out, int *removed_out,
+             std::vector<int> &new_nodes)
+{
+    int added = 0, removed = 0;
+    for (int k = 0; k < c->n_live; ++k) {
+        Host h{c};
+        if (h.st(k) == OV_EMPTY) continue;
+        int nx = h.fwd(k), pv = h.rev(k);
+        double lf = 0, lr = 0, pk[3];
+        h.pos(k, pk);
+        if (nx >= 0) { double q[3]; h.pos(nx, q); lf = hpwrap_len(c->geo, pk, q); }
+        if (pv >= 0) { double q[3]; h.pos(pv, q); lr = hpwrap_len(c->geo, pk, q); }
+        if (nx >= 0 && pv >= 0 && ((lf < min_dist || lr < min_dist) && (lf + lr) < max_dist)) {
+            hremove(c, k);
+            removed++;
+        }
+        if (nx >= 0 && lf > max_dist) {
+            added++;
+            hadd_point(c, k, new_nodes);
+        }
+    }
+    if (added) {
+        hperiodic(c);
+        std::fill(c->h_recalc.begin(), c->h_recalc.end(), 0);
+    }
+    *added_out = added;
+    *removed_out = removed;
+}
+
+int ensure_pairs(ov_ctx *c, int need)
+{
+    if (c->pair_cap >= need && c->d_pairs) return OV_OK;
+    if (c->d_pairs) cudaFree(c->d_pairs);
+    c->d_pairs = nullptr;
+    OV_CUDA(c, cudaMalloc(&c->d_pairs, (size_t)need * 2 * sizeof(int)));
+    if (!c->d_npairs) OV_CUDA(c, cudaMalloc(&c->d_npairs, sizeof(int)));
+    c->pair_cap = need;
+    return OV_OK;
+}
+
+// candidate pairs (k < l, both FREE) with |seg_pwrap(x_k, x_l)| <= rec_dist
+int find_pairs(ov_ctx *c, std::vector<std::pair<int, int>> &out)
+{
+    out.clear();
+    int cap = c->cap;
+    double rd = c->params.rec_dist;
+    GridGeom gg;
+    for (int a = 0; a < 3; ++a) {
+        gg.lo[a] = c->geo.lo[a];
+        gg.L[a] = c->geo.L[a];
+        double cells = floor(c->geo.L[a] / (2.0 * rd));
+        gg.n[a] = (int)std::max(1.0, std::min(cells, 1024.0));
+        gg.periodic[a] = c->geo.periodic[a];
+    }
+    int r = ensure_pairs(c, std::max(c->pair_cap, 4 * std::max(c->n_live, 16)));
+    if (r) return r;
+    TreeBuf &t = c->tree;
+    int nb = (cap + 255) / 256;
+    k_grid_keys<<<nb, 256, 0, c->stream>>>(c->status, c->node.x, c->node.y, c->node.z, c->n_live, cap, gg, t.keys,
+                                           t.order);
+    c->launches++;
+    ov_sort_keys(c, t, cap, c->stream);
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        OV_CUDA(c, cudaMemsetAsync(c->d_npairs, 0, sizeof(int), c->stream));
+        k_pairs<<<nb, 256, 0, c->stream>>>(t.keys, t.order, cap, c->node.x, c->node.y, c->node.z, gg, c->geo, rd,
+                                           c->d_pairs, c->d_npairs, c->pair_cap);
+        c->launches++;
+        OV_CUDA(c, cudaGetLastError());
+        int np = 0;
+        OV_CUDA(c, cudaMemcpyAsync(&np, c->d_npairs, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        OV_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (np > c->pair_cap) {
+            if ((r = ensure_pairs(c, np + np / 2))) return r;
+            continue;
+        }
+        std::vector<int> buf(2 * (size_t)np);
+        if (np)
+            OV_CUDA(c, cudaMemcpy(buf.data(), c->d_pairs, (size_t)np * 2 * sizeof(int), cudaMemcpyDeviceToHost));
+        out.resize(np);
+        for (int i = 0; i < np; ++i) out[i] = {buf[2 * i], buf[2 * i + 1]};
+        std::sort(out.begin(), out.end());
+        out.erase(std::unique(out.begin(), out.end()), out.end());
+        return OV_OK;
+    }
+    return ov_fail(c, OV_ERR_ALLOC, "candidate pair buffer could not be sized");
+}
+
+struct SegChange {
+    int m, f;
+    double sign;   // +1 added, -1 removed
+};
+
+}  // namespace
+
+extern "C" {
+
+int ov_eliminate_small_loops(ov_ctx *c)
+{
+    int r = ready(c);
+    if (r) return r;
+    if ((r = ov_pull_host(c))) return r;
+    int removed = hsmall_loops(c);
+    c->stats.small_loops_removed = removed;
+    if (removed) return ov_push_device(c, 0);
+    return OV_OK;
+}
+
+int ov_remesh(ov_ctx *c, double min_dist, double max_dist, double t)
+{
+    (void)t;
+    int r = ready(c);
+    if (r) return r;
+    if ((r = ov_pull_host(c))) return r;
+    int added = 0, removed = 0;
+    std::vector<int> new_nodes;
+    hremesh(c, min_dist, max_dist, &added, &removed, new_nodes);
+    c->stats.remesh_added = added;
+    c->stats.remesh_removed = removed;
+    if (!added && !removed) return OV_OK;
+    if ((r = ov_push_device(c, 1))) return r;
+    if (!new_nodes.empty()) {
+        int *d = nullptr;
+        OV_CUDA(c, cudaMalloc(&d, new_nodes.size() * sizeof(int)));
+        OV_CUDA(c, cudaMemcpy(d, new_nodes.data(), new_nodes.size() * sizeof(int), cudaMemcpyHostToDevice));
+        k_zero_vel<<<((int)new_nodes.size() + 255) / 256, 256, 0, c->stream>>>(
+            d, (int)new_nodes.size(), c->node.vx, c->node.vy, c->node.vz, c->node.sx, c->node.sy, c->node.sz);
+        c->launches++;
+        OV_CUDA(c, cudaStreamSynchronize(c->stream));
+        cudaFree(d);
+    }
+    return OV_OK;
+}
+
+int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int log_cap)
+{
+    int r = ready(c);
+    if (r) return r;
+    if ((r = ov_pull_host(c))) return r;
+    std::vector<std::pair<int, int>> pairs;
+    if ((r = find_pairs(c, pairs))) return r;
+    Host h{c};
+    int N = h.N();
+    // direct sums of every candidate node on the pass's starting topology
+    std::vector<int> cand;
+    cand.reserve(2 * pairs.size());
+    for (auto &pr : pairs) { cand.push_back(pr.first); cand.push_back(pr.second); }
+    std::sort(cand.begin(), cand.end());
+    cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+    std::vector<double> sums(3 * cand.size());
+    if (!cand.empty() && (r = ov_direct_raw(c, cand.data(), (int)cand.size(), sums.data()))) return r;
+    auto cand_index = [&](int k) {
+        return (int)(std::lower_bound(cand.begin(), cand.end(), k) - cand.begin());
+    };
+    std::vector<SegChange> changes;
+    std::vector<int> &recalc = c->h_recalc;
+    recalc.assign(N, 0);
+    const double cos_cut = cos(c->params.reconnection_angle_cutoff);
+    const Geometry &g = c->geo;
+    int nrec = 0;
+
+    // velocity of an unflagged candidate node on the current topology
+    auto velocity = [&](int k, const double tg[3], const double nm[3], double vel[3]) -> bool {
+        double vs[3];
+        if (!hlia(h, k, tg, nm, t, vs)) return false;
+        int ci = cand_index(k);
+        double nl[3] = {sums[3 * ci], sums[3 * ci + 1], sums[3 * ci + 2]};
+        if (!changes.empty()) {
+            double x[3];
+            h.pos(k, x);
+            for (const SegChange &sc : changes) {
+                for (int j = -1; j < g.n_img; ++j) {
+                    double q[3];
+                    if (j < 0) { q[0] = x[0]; q[1] = x[1]; q[2] = x[2]; }
+                    else himage(g, j, x, q);
+                    double w[3];
+                    if (hsegment(h, sc.m, sc.f, q, w))
+                        for (int a = 0; a < 3; ++a) nl[a] += sc.sign * w[a];
+                }
+            }
+        }
+        for (int a = 0; a < 3; ++a) vs[a] = vs[a] + nl[a];
+        hfriction(h, k, tg, vs, t, vel);
+        return true;
+    };
+
+    size_t i = 0;
+    while (i < pairs.size()) {
+        int k = pairs[i].first;
+        size_t e = i;
+        while (e < pairs.size() && pairs[e].first == k) ++e;
+        int sk = h.st(k);
+        if (sk == OV_EMPTY || pinned(sk) || recalc[k]) { i = e; continue; }
+        for (size_t q = i; q < e; ++q) {
+            int l = pairs[q].second;
+            int sl = h.st(l);
+            if (sl == OV_EMPTY || pinned(sl) || h.fwd(k) == l || h.rev(k) == l || recalc[l]) continue;
+            double tk[3], nk[3], tl[3], nl_[3];
+            if (!htangent(h, k, tk, nk) || !htangent(h, l, tl, nl_))
+                return ov_fail(c, OV_ERR_TOPOLOGY, "reconnect: filament walk from %d or %d failed", k, l);
+            if (hlen(tk) < 0.5 || hlen(tl) < 0.5) continue;
+            if (hdot(tk, tl) / hlen(tk) / hlen(tl) > cos_cut) continue;
+            double vk[3], vl[3];
+            if (!velocity(k, tk, nk, vk) || !velocity(l, tl, nl_, vl))
+                return ov_fail(c, OV_ERR_TOPOLOGY, "reconnect: velocity of %d or %d failed", k, l);
+            double v1[3], v2[3], dx[3], dv[3];
+            h.pos(k, v1);
+            h.pos(l, v2);
+            hpwrap(g, v1, v2);
+            hsub(dx, v1, v2);
+            hsub(dv, vk, vl);
+            double proj = hdot(dx, dv);
+            if (fabs(proj) <= 1e-9 * hlen(dx) * hlen(dv)) {
+                // too close to call after a different summation order: redo
+                // both velocities exactly as the reference sums them
+                hdirect_exact(h, k, tk, nk, t, vk);
+                hdirect_exact(h, l, tl, nl_, t, vl);
+                hsub(dv, vk, vl);
+                proj = hdot(dx, dv);
+            }
+            if (proj > 0) continue;
+            int kn = h.fwd(k), kp = h.rev(k), ln = h.fwd(l), lp = h.rev(l);
+            // do_reconnection (vortex_dynamics.c:128-175)
+            auto slen = [&](int a, int b) {
+                double pa[3], pb[3];
+                h.pos(a, pa);
+                h.pos(b, pb);
+                return hpwrap_len(g, pa, pb);
+            };
+            double cf1 = slen(k, l) + slen(kn, lp) - slen(k, kn) - slen(l, lp);
+            double cf2 = slen(k, l) + slen(kp, ln) - slen(k, kp) - slen(l, ln);
+            if (cf1 > 0 && cf2 > 0) continue;
+            if (cf1 < cf2) {
+                changes.push_back({k, kn, -1.0});
+                changes.push_back({lp, l, -1.0});
+                h.fwd(k) = l; h.rev(l) = k;
+                h.rev(kn) = lp; h.fwd(lp) = kn;
+                changes.push_back({k, l, 1.0});
+                changes.push_back({lp, kn, 1.0});
+            } else {
+                changes.push_back({l, ln, -1.0});
+                changes.push_back({kp, k, -1.0});
+                h.fwd(l) = k; h.rev(k) = l;
+                h.rev(ln) = kp; h.fwd(kp) = ln;
+                changes.push_back({l, k, 1.0});
+                changes.push_back({kp, ln, 1.0});
+            }
+            recalc[k]++; recalc[h.fwd(k)]++; recalc[h.rev(k)]++; recalc[kn]++; recalc[kp]++;
+            recalc[l]++; recalc[h.fwd(l)]++; recalc[h.rev(l)]++; recalc[ln]++; recalc[lp]++;
+            if (log_k && log_l && nrec < log_cap) { log_k[nrec] = k; log_l[nrec] = l; }
+            nrec++;
+            break;
+        }
+        i = e;
+    }
+    c->stats.reconnections = nrec;
+    if (nrecs) *nrecs = nrec;
+    if (nrec) return ov_push_device(c, 0);
+    return OV_OK;
+}
+
+int ov_smooth(ov_ctx *c)
+{
+    int r = ready(c);
+    if (r) return r;
+    if (!c->params.use_freq_filter) return OV_OK;
+    if ((r = ov_pull_host(c))) return r;
+    Host h{c};
+    int N = h.N();
+    // closed loops in the reference's discovery order (vortex_smooth.c:192-210)
+    std::vector<char> seen(N > 0 ? N : 1, 0);
+    std::vector<int> off{0}, nodes;
+    int maxlen = 0;
+    for (int i = 0; i < N; ++i) {
+        if (seen[i]) continue;
+        if (h.st(i) == OV_EMPTY) { seen[i] = 1; continue; }
+        int j = i, guard = 0;
+        while (h.rev(j) != i && h.rev(j) != -1 && guard++ <= N) j = h.rev(j);
+        if (h.rev(j) == -1 || guard > N) { seen[i] = 1; continue; }   // open line: not smoothed
+        int len = 0;
+        int m = i;
+        do {
+            nodes.push_back(m);
+            seen[m] = 1;
+            m = h.fwd(m);
+            ++len;
+        } while (m != i && m >= 0 && len <= N);
+        off.push_back((int)nodes.size());
+        maxlen = std::max(maxlen, len);
+    }
+    int nloops = (int)off.size() - 1;
+    if (nloops == 0) return OV_OK;
+    size_t total = nodes.size();
+    if (c->loop_cap < nloops + 1 || c->loop_nodes_cap < (int)total) {
+        if (c->d_loop_off) cudaFree(c->d_loop_off);
+        if (c->d_loop_nodes) cudaFree(c->d_loop_nodes);
+        OV_CUDA(c, cudaMalloc(&c->d_loop_off, (size_t)(nloops + 1) * 4));
+        OV_CUDA(c, cudaMalloc(&c->d_loop_nodes, total * 4));
+        c->loop_cap = nloops + 1;
+        c->loop_nodes_cap = (int)total;
+    }
+    size_t need = total * 2 * 3 * sizeof(double);
+    if (c->loop_buf_cap < need) {
+        if (c->d_loop_buf) cudaFree(c->d_loop_buf);
+        OV_CUDA(c, cudaMalloc(&c->d_loop_buf, need));
+        c->loop_buf_cap = need;
+    }
+    OV_CUDA(c, cudaMemcpyAsync(c->d_loop_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    OV_CUDA(c, cudaMemcpyAsync(c->d_loop_nodes, nodes.data(), total * 4, cudaMemcpyHostToDevice, c->stream));
+    SmoothArgs a;
+    a.loop_off = c->d_loop_off;
+    a.loop_nodes = c->d_loop_nodes;
+    a.x = c->node.x; a.y = c->node.y; a.z = c->node.z;
+    a.buf = c->d_loop_buf;
+    a.geo = c->geo;
+    a.freq_to_cutoff = c->params.freq_to_cutoff;
+    int Nmax = 2 * maxlen;
+    size_t shbytes = (size_t)(2 * Nmax + 3 * (Nmax / 2 + 1 + Nmax)) * sizeof(double);
+    if (shbytes > 200 * 1024) return ov_fail(c, OV_ERR_ARG, "loop of %d nodes too long to smooth", maxlen);
+    if (shbytes > 48 * 1024)
+        OV_CUDA(c, cudaFuncSetAttribute(k_smooth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes));
+    c->tree_built = false;
+    k_smooth<<<nloops, 256, shbytes, c->stream>>>(a);
+    c->launches++;
+    OV_CUDA(c, cudaGetLastError());
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    return OV_OK;
+}
+
+int ov_step(ov_ctx *c, double t, double dt)
+{
+    int r = ready(c);
+    if (r) return r;
+    int nrec = 0;
+    if ((r = ov_eliminate_small_loops(c))) return r;
+    if ((r = ov_reconnect(c, 0.0, &nrec, nullptr, nullptr, 0))) return r;
+    if ((r = ov_eliminate_small_loops(c))) return r;
+    if ((r = ov_smooth(c))) return r;
+    if ((r = ov_enforce_periodic_boundaries(c))) return r;
+    if ((r = ov_remesh(c, c->params.dl_min, c->params.dl_max, 0.0))) return r;
+    if ((r = ov_eliminate_small_loops(c))) return r;
+    if ((r = ov_update_tangle(c, t))) return r;
+    if ((r = ov_rk4_step(c, t, dt))) return r;
+    if ((r = ov_enforce_periodic_boundaries(c))) return r;
+    c->stats.reconnections = nrec;
+    return OV_OK;
+}
+
+}  // extern "C"

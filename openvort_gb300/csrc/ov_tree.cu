@@ -431,6 +431,7 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
 {
     TreeBuf &t = c->tree;
     int cap = c->cap;
+    c->tree_built = false;   // a query tree is only current until the next build
     KeyGeom g = key_geom(c->geo);
     OV_CUDA(c, cudaMemsetAsync(t.counters, 0, TC_WORDS * 4, s));
     OV_CUDA(c, cudaMemsetAsync(t.nchild, 0, (size_t)t.cap_cells * 4, s));

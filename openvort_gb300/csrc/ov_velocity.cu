@@ -37,9 +37,18 @@ struct VelArgs {
     double t;
     double f4pi;            // KAPPA/4/M_PI in the reference's rounding
     double grid_h, inv_h;   // mixed path
+    float shift_g[OV_MAX_IMAGES][3], shift_f[OV_MAX_IMAGES][3];   // L*shift split on the grid
+    int cap;                // node slots (bounds checks)
     double near2;           // mixed path: squared near-field radius
     unsigned long long *stat;
 };
+
+// Record the first failed bounds check (code, index) and raise the error bit.
+__device__ __forceinline__ void bad_index(const VelArgs &a, int code, int idx)
+{
+    atomicCAS((int *)&a.counters[TC_BAD], 0, (code << 24) | (idx & 0xFFFFFF) | (1 << 30));
+    atomicOr((int *)&a.counters[TC_ERR], OV_EW_BOUNDS);
+}
 
 // step_node (tangle.c:155-194) without recursion: a pinned end reverses the
 // walk and mirrors the result in its wall, innermost mirror applied first.
@@ -48,7 +57,7 @@ __device__ bool step_node_dev(const VelArgs &a, int i, int where, double out[3])
     int walls[8];
     int nw = 0, cur = i, w = where;
     for (int guard = 0; w != 0; ++guard) {
-        if (guard > 16 || cur < 0) return false;
+        if (guard > 16 || cur < 0 || cur >= a.cap) return false;
         int st = a.status[cur];
         if (st == OV_FREE) {
             cur = w > 0 ? a.fwd[cur] : a.rev[cur];
@@ -67,7 +76,7 @@ __device__ bool step_node_dev(const VelArgs &a, int i, int where, double out[3])
             return false;
         }
     }
-    if (cur < 0 || a.status[cur] == OV_EMPTY) return false;
+    if (cur < 0 || cur >= a.cap || a.status[cur] == OV_EMPTY) return false;
     out[0] = a.x[cur]; out[1] = a.y[cur]; out[2] = a.z[cur];
     for (int m = nw - 1; m >= 0; --m) {
         int f = walls[m];
@@ -220,10 +229,12 @@ __device__ __forceinline__ void bh_query64(const VelArgs &a, const double q[3], 
     int resume = part ? 0 : 0x7fffffff;
     int guard = 0;
     while (c < ncell) {
+        if (c < 0) { bad_index(a, 5, c); break; }
         const Cell64 *cp = a.cells + c;
         double cx = __ldg(&cp->cx), cy = __ldg(&cp->cy), cz = __ldg(&cp->cz);
         double lm = __ldg(&cp->lm);
         int nxt = __ldg(&cp->next);
+        if (nxt <= c || nxt > ncell) { bad_index(a, 6, c); nxt = ncell; }
         bool open = false;
         if (c >= resume) {
             ++visits;
@@ -494,6 +505,253 @@ __global__ void k_wrap(const int *__restrict__ status, double *x, double *y, dou
     x[k] = p[0]; y[k] = p[1]; z[k] = p[2];
 }
 
+// ----------------------------------------------------------- mixed precision
+//
+// Positions and centres of mass are split as p = g + f: g on a grid of step
+// h = 2^k (every coordinate below 2^22 steps, so g is exact in FP32 and a
+// difference of two g's is exact), f the FP32 remainder (|f| <= h/2).  A
+// separation is (g_r - g_c) + (f_r - f_c): relative error ~1e-7 even for the
+// nearest cells, where a plain FP32 difference of absolute positions would
+// lose 4-5 digits.  Decisions (d < 1e-8, Lm/d < theta, |Rp1| < 1e-8,
+// ndot < 1e-8) are taken in FP32 only outside a guard band around the
+// threshold and redone exactly in FP64 inside it, so they are the FP64
+// path's decisions.  Leaf interactions closer than the near-field radius
+// are done in FP64.  Per-query sums use Kahan compensation.
+
+// decision of the FP64 path for cell c: 1 skip (d < 1e-8), 2 accept, 0 open
+__device__ __forceinline__ int decide64(const Cell64 *cp, const double q[3], double theta, bool leaf, double dxyz[3],
+                                        double *dout)
+{
+    double dx = rn_sub(q[0], __ldg(&cp->cx)), dy = rn_sub(q[1], __ldg(&cp->cy)), dz = rn_sub(q[2], __ldg(&cp->cz));
+    double d = len3_ref(dx, dy, dz);
+    dxyz[0] = dx; dxyz[1] = dy; dxyz[2] = dz;
+    *dout = d;
+    if (d < 1e-8) return 1;
+    if (leaf) return 2;
+    double lm = __ldg(&cp->lm);
+    double td = theta * d;
+    if (lm < td * (1.0 - 1e-12)) return 2;
+    if (lm > td * (1.0 + 1e-12)) return 0;
+    return rn_div(lm, d) < theta ? 2 : 0;
+}
+
+__device__ __forceinline__ bool interact64(const Cell64 *cp, const double dxyz[3], double d, double f4pi, double w[3])
+{
+    double R[3] = {-dxyz[0], -dxyz[1], -dxyz[2]};
+    double Rp1[3] = {rn_add(R[0], __ldg(&cp->qx)), rn_add(R[1], __ldg(&cp->qy)), rn_add(R[2], __ldg(&cp->qz))};
+    return segment_law64(R, Rp1, d, f4pi, w);
+}
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float v)
+{
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+constexpr int kNearCap = 24;   // deferred near-field leaves per lane
+
+
+struct MixedAcc {
+    float s0, s1, s2, c0, c1, c2;   // Kahan sums over every query point
+    unsigned nvis, nacc, nstep, nfb, nnear;
+};
+
+// One query point (g + f split, image j; j < 0 the node itself) for the 32
+// lanes of a warp.  Near-field leaves are appended to the lane's list
+// (cell, image) and evaluated in FP64 after all query points.
+__device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], const float f[3], const double p[3],
+                                           int j, bool part, int ncell, MixedAcc &m, int *near_list, int &nnear,
+                                           double w64[3], bool &overflow)
+// near_list: this lane's column of a shared [kNearCap][32] array, stride 32
+{
+    const float th2 = (float)(a.prm.theta * a.prm.theta);
+    const float near2 = (float)a.near2;
+    const float f4pi = (float)a.f4pi;
+    int c = 0;
+    int resume = part ? 0 : 0x7fffffff;
+    const int guard_max = 4 * ncell + 64;
+    int steps = 0;
+    while (c < ncell) {
+        if (c < 0) { bad_index(a, 1, c); break; }
+        const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
+        float4 A = __ldg(cp4), B = __ldg(cp4 + 1), Cc = __ldg(cp4 + 2);
+        // A = (gx, gy, gz, fx)  B = (fy, fz, qx, qy)  Cc = (qz, lm, next, count)
+        int nxt = __float_as_int(Cc.z);
+        if (nxt <= c || nxt > ncell) { bad_index(a, 2, c); nxt = ncell; }
+        bool open = false;
+        if (c >= resume) {
+            ++m.nvis;
+            float dx = (g[0] - A.x) + (f[0] - A.w);
+            float dy = (g[1] - A.y) + (f[1] - B.x);
+            float dz = (g[2] - A.z) + (f[2] - B.y);
+            float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const bool leaf = (nxt == c + 1);
+            // 1 skip, 2 accept, 0 open, -1 decide in FP64
+            int dec;
+            if (d2 < 1e-16f * (1.0f - 1e-5f)) dec = 1;
+            else if (d2 <= 1e-16f * (1.0f + 1e-5f)) dec = -1;
+            else if (leaf) dec = 2;
+            else {
+                float lm2 = Cc.y * Cc.y, b = th2 * d2;
+                dec = lm2 < b * (1.0f - 2e-5f) ? 2 : (lm2 > b * (1.0f + 2e-5f) ? 0 : -1);
+            }
+            bool use64 = dec < 0;
+            if (use64) {
+                // rare: inside a guard band, decided exactly as the FP64 path
+                ++m.nfb;
+                double q[3], dxyz[3], d64;
+                if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+                else image_point(a.geo, j, p, q);
+                dec = decide64(a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
+            }
+            if (dec == 2) {
+                ++m.nacc;
+                float R0 = -dx, R1 = -dy, R2 = -dz;
+                float qx = B.z, qy = B.w, qz = Cc.x;
+                float P0 = R0 + qx, P1 = R1 + qy, P2 = R2 + qz;
+                float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
+                float dot = fmaf(R0, P0, fmaf(R1, P1, R2 * P2));
+                float ra = rsqrtf(d2), rb = rsqrtf(lp2);
+                float ab = ra * rb;
+                float nd = dot * ab;
+                use64 = use64 || (leaf && d2 < near2) || fabsf(lp2 - 1e-16f) <= 1e-16f * 1e-5f ||
+                        fabsf(nd - 1e-8f) < 4e-6f;
+                if (use64) {
+                    // near field, or a filter inside its guard band: FP64, deferred
+                    ++m.nnear;
+                    if (nnear < kNearCap) {
+                        near_list[32 * nnear] = (c << 5) | (j + 1);
+                        ++nnear;
+                    } else {
+                        double q[3], dxyz[3], d64, w[3];
+                        if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+                        else image_point(a.geo, j, p, q);
+                        decide64(a.cells + c, q, a.prm.theta, true, dxyz, &d64);
+                        if (interact64(a.cells + c, dxyz, d64, a.f4pi, w)) {
+                            w64[0] += w[0]; w64[1] += w[1]; w64[2] += w[2];
+                        }
+                    }
+                } else if (lp2 >= 1e-16f && nd >= 1e-8f) {
+                    float den = fmaf(dot, ab, 1.0f);
+                    float sc = __fdividef(f4pi * (ra + rb) * ab, den);
+                    // R x Rp1 = R x q
+                    kahan_add(m.s0, m.c0, (R1 * qz - R2 * qy) * sc);
+                    kahan_add(m.s1, m.c1, (R2 * qx - R0 * qz) * sc);
+                    kahan_add(m.s2, m.c2, (R0 * qy - R1 * qx) * sc);
+                }
+                resume = nxt;
+            } else if (dec == 1) {
+                resume = nxt;
+            } else {
+                open = true;
+            }
+        }
+        ++steps;
+        c = __any_sync(0xffffffffu, open) ? c + 1 : nxt;
+        if (steps > guard_max) { overflow = true; break; }
+    }
+    m.nstep += steps;
+}
+
+__global__ void __launch_bounds__(128) k_vel_mixed(VelArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nne = a.counters[TC_NNE];
+    const int ncell = a.counters[TC_NCELL];
+    if (warp * 32 >= nne) return;
+    const int tix = warp * 32 + lane;
+    bool valid = tix < nne && tix < a.cap;
+    int id = valid ? a.order[tix] : 0;
+    if (valid && (id < 0 || id >= a.cap)) { bad_index(a, 4, id); valid = false; id = 0; }
+    const int st = valid ? a.status[id] : OV_EMPTY;
+    const bool part = valid && st != OV_PINNED && st != OV_EMPTY && a.prm.use_bh;
+    double p[3] = {0, 0, 0};
+    if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
+    float g0[3], f0[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        double G = rint(p[ax] * a.inv_h) * a.grid_h;
+        g0[ax] = (float)G;
+        f0[ax] = (float)(p[ax] - G);
+    }
+    MixedAcc m = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
+    double w64[3] = {0, 0, 0};        // FP64 sums: near field and list overflow
+    double img64[3] = {0, 0, 0};      // images with mirror reflections
+    __shared__ int s_near[4][kNearCap * 32];   // per warp: [entry][lane]
+    int *near_list = &s_near[(threadIdx.x >> 5) & 3][lane];
+    int nnear = 0;
+    bool overflow = false;
+    for (int j = -1; j < a.geo.n_img; ++j) {
+        float g[3], f[3];
+        if (j < 0) {
+            for (int ax = 0; ax < 3; ++ax) { g[ax] = g0[ax]; f[ax] = f0[ax]; }
+        } else {
+            // image query p - L*shift: grid parts subtract exactly
+            for (int ax = 0; ax < 3; ++ax) {
+                g[ax] = g0[ax] - a.shift_g[j][ax];
+                f[ax] = f0[ax] - a.shift_f[j][ax];
+            }
+        }
+        if (j >= 0 && a.geo.nreflect[j] > 0) {
+            // mirror images (wall geometries) keep their own FP64 sum
+            double q[3], v[3];
+            image_point(a.geo, j, p, q);
+            unsigned long long vi = 0, ac = 0, sp = 0;
+            bh_query64(a, q, part, ncell, v, vi, ac, sp, overflow);
+            for (int r = 0; r < a.geo.nreflect[j]; ++r) mirror_vec(a.geo.reflect[j][r], v);
+            img64[0] += v[0]; img64[1] += v[1]; img64[2] += v[2];
+            m.nvis += (unsigned)vi; m.nacc += (unsigned)ac; m.nstep += (unsigned)sp;
+            continue;
+        }
+        bh_query32(a, g, f, p, j, part, ncell, m, near_list, nnear, w64, overflow);
+    }
+    // deferred near-field interactions, all lanes together
+    for (int i = 0; i < nnear && i < kNearCap; ++i) {
+        int e = near_list[32 * i];
+        int c = e >> 5, j = (e & 31) - 1;
+        if (c < 0 || c >= ncell || j < -1 || j >= a.geo.n_img) { bad_index(a, 3, e); continue; }
+        double q[3], dxyz[3], d64, w[3];
+        if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+        else image_point(a.geo, j, p, q);
+        decide64(a.cells + c, q, a.prm.theta, true, dxyz, &d64);
+        if (interact64(a.cells + c, dxyz, d64, a.f4pi, w)) {
+            w64[0] += w[0]; w64[1] += w[1]; w64[2] += w[2];
+        }
+    }
+    double bh[3] = {((double)m.s0 - (double)m.c0) + w64[0] + img64[0],
+                    ((double)m.s1 - (double)m.c1) + w64[1] + img64[1],
+                    ((double)m.s2 - (double)m.c2) + w64[2] + img64[2]};
+    double zero[3] = {0, 0, 0};
+    int err = overflow ? OV_EW_ITER : 0;
+    if (valid && st != OV_EMPTY) {
+        double vs[3], vel[3];
+        if (finish_node(a, id, p, bh, zero, &err, vs, vel)) {
+            a.sx[id] = vs[0]; a.sy[id] = vs[1]; a.sz[id] = vs[2];
+            a.vx[id] = vel[0]; a.vy[id] = vel[1]; a.vz[id] = vel[2];
+        }
+    }
+    unsigned long long visits = m.nvis, accepts = m.nacc, fallback = m.nfb, near64 = m.nnear;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        visits += __shfl_xor_sync(0xffffffffu, visits, o);
+        accepts += __shfl_xor_sync(0xffffffffu, accepts, o);
+        fallback += __shfl_xor_sync(0xffffffffu, fallback, o);
+        near64 += __shfl_xor_sync(0xffffffffu, near64, o);
+        err |= __shfl_xor_sync(0xffffffffu, err, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&a.stat[ST_VISITS], visits);
+        atomicAdd(&a.stat[ST_ACCEPTS], accepts);
+        atomicAdd(&a.stat[ST_STEPS], (unsigned long long)m.nstep);
+        atomicAdd(&a.stat[ST_FALLBACK], fallback);
+        atomicAdd(&a.stat[ST_NEAR64], near64);
+        if (err) atomicOr((int *)&a.counters[TC_ERR], err);
+    }
+}
+
 VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long *stat)
 {
     VelArgs a;
@@ -515,7 +773,15 @@ VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long 
     a.inv_h = c->grid_h > 0 ? 1.0 / c->grid_h : 0;
     double near = 2.0 * c->params.dl_max;
     a.near2 = near * near;
+    for (int j = 0; j < c->geo.n_img; ++j)
+        for (int ax = 0; ax < 3; ++ax) {
+            double sh = c->geo.L[ax] * (double)c->geo.shift[j][ax];
+            double G = c->grid_h > 0 ? rint(sh / c->grid_h) * c->grid_h : 0.0;
+            a.shift_g[j][ax] = (float)G;
+            a.shift_f[j][ax] = (float)(sh - G);
+        }
     a.stat = stat;
+    a.cap = c->cap;
     return a;
 }
 
@@ -534,8 +800,10 @@ void ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precisi
     int warps = (c->cap + 31) / 32;
     int threads = 128;
     int blocks = (warps * 32 + threads - 1) / threads;
-    (void)precision;
-    k_vel_fp64<<<blocks, threads, 0, s>>>(a);
+    if (precision == OV_PREC_MIXED)
+        k_vel_mixed<<<blocks, threads, 0, s>>>(a);
+    else
+        k_vel_fp64<<<blocks, threads, 0, s>>>(a);
     c->launches++;
 }
 
@@ -561,6 +829,89 @@ int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out
         OV_CUDA(c, cudaMemcpyAsync(vels_out, vo, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if (vs_out)
         OV_CUDA(c, cudaMemcpyAsync(vs_out, so, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    return OV_OK;
+}
+
+__global__ void __launch_bounds__(128) k_query64(VelArgs a, const double *__restrict__ pts, int n,
+                                                 double *__restrict__ out)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp * 32 >= n) return;
+    const int i = warp * 32 + lane;
+    const bool valid = i < n;
+    double q[3] = {0, 0, 0};
+    if (valid) { q[0] = pts[3 * i]; q[1] = pts[3 * i + 1]; q[2] = pts[3 * i + 2]; }
+    unsigned long long visits = 0, accepts = 0, steps = 0;
+    bool overflow = false;
+    double v[3];
+    bh_query64(a, q, valid, a.counters[TC_NCELL], v, visits, accepts, steps, overflow);
+    if (valid) { out[3 * i] = v[0]; out[3 * i + 1] = v[1]; out[3 * i + 2] = v[2]; }
+    if (overflow && lane == 0) atomicOr((int *)&a.counters[TC_ERR], OV_EW_ITER);
+}
+
+extern "C" int ov_tree_velocity_at(ov_ctx *c, const double *points, int n, double resolution, int rebuild,
+                                   double *out)
+{
+    if (!c || n < 0 || (n > 0 && (!points || !out))) return OV_ERR_ARG;
+    if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
+    cudaSetDevice(c->device);
+    if (rebuild || !c->tree_built) {
+        int r = ov_tree_build(c, c->node, c->stream);
+        if (r) return r;
+        OV_CUDA(c, cudaStreamSynchronize(c->stream));
+        int need = 0;
+        OV_CUDA(c, cudaMemcpy(&need, c->tree.counters + TC_NEED, 4, cudaMemcpyDeviceToHost));
+        int err = 0;
+        OV_CUDA(c, cudaMemcpy(&err, c->tree.counters + TC_ERR, 4, cudaMemcpyDeviceToHost));
+        if (err & OV_EW_CELLS) {
+            if ((r = ov_tree_reserve_cells(c, need + need / 4 + 64))) return r;
+            if ((r = ov_tree_build(c, c->node, c->stream))) return r;
+        }
+        c->tree_built = true;
+    }
+    if (n == 0) return OV_OK;
+    if (c->dsum_cap < n) {
+        if (c->dsum) cudaFree(c->dsum);
+        if (c->dnodes) cudaFree(c->dnodes);
+        c->dsum = nullptr; c->dnodes = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->dsum, (size_t)n * 9 * sizeof(double)));
+        OV_CUDA(c, cudaMalloc(&c->dnodes, (size_t)n * sizeof(int)));
+        c->dsum_cap = n;
+    }
+    double *dp = c->dsum, *dout = c->dsum + 3 * (size_t)n;
+    OV_CUDA(c, cudaMemcpyAsync(dp, points, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    VelArgs a = make_args(c, c->node, 0.0, nullptr);
+    a.prm.theta = resolution;
+    int warps = (n + 31) / 32;
+    k_query64<<<(warps * 32 + 127) / 128, 128, 0, c->stream>>>(a, dp, n, dout);
+    c->launches++;
+    OV_CUDA(c, cudaGetLastError());
+    OV_CUDA(c, cudaMemcpyAsync(out, dout, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    return OV_OK;
+}
+
+// Raw direct sums (no LIA / friction) of the listed nodes on the current
+// device state: the nonlocal velocities reconnect needs.
+int ov_direct_raw(ov_ctx *c, const int *nodes, int n, double *sums_out)
+{
+    if (n <= 0) return OV_OK;
+    if (c->dsum_cap < n) {
+        if (c->dsum) cudaFree(c->dsum);
+        if (c->dnodes) cudaFree(c->dnodes);
+        c->dsum = nullptr; c->dnodes = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->dsum, (size_t)n * 9 * sizeof(double)));
+        OV_CUDA(c, cudaMalloc(&c->dnodes, (size_t)n * sizeof(int)));
+        c->dsum_cap = n;
+    }
+    OV_CUDA(c, cudaMemcpyAsync(c->dnodes, nodes, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    VelArgs a = make_args(c, c->node, 0.0, nullptr);
+    k_direct<<<n, 256, 0, c->stream>>>(a, c->dnodes, n, c->n_live, c->dsum);
+    c->launches++;
+    OV_CUDA(c, cudaGetLastError());
+    OV_CUDA(c, cudaMemcpyAsync(sums_out, c->dsum, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     OV_CUDA(c, cudaStreamSynchronize(c->stream));
     return OV_OK;
 }
@@ -720,6 +1071,7 @@ extern "C" int ov_direct_velocities_noalloc(const ov_params *p, const ov_domain_
     a.nx = d_normals; a.ny = d_normals + ns; a.nz = d_normals + 2 * ns;
     a.fwd = d_conn; a.rev = d_conn + ns;
     a.status = d_status; a.pin = d_status + ns;
+    a.cap = n_slots;
     Geometry &g = a.geo;
     for (int ax = 0; ax < 3; ++ax) {
         g.lo[ax] = box->bottom_left_back.p[ax];

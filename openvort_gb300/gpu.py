@@ -77,6 +77,7 @@ def load(path: str | None = None):
         "ov_set_phase_timing": (C.c_int, [P, C.c_int]),
         "ov_phase_times": (C.c_int, [P, C.POINTER(C.c_float)]),
         "ov_measure_fma_peak": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
+        "ov_tangle_info": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -153,6 +154,25 @@ class Context:
         self._host = host
         self._state = host.state()
         self._check(self.lib.ov_upload_tangle_fields(self._h, C.byref(self._state), fields))
+
+    def tangle_info(self) -> tuple[int, int, int]:
+        n, ne, te = C.c_int(0), C.c_int(0), C.c_int(0)
+        self._check(self.lib.ov_tangle_info(self._h, C.byref(n), C.byref(ne), C.byref(te)))
+        return n.value, ne.value, te.value
+
+    def download_resized(self, host):
+        """Download into a copy of `host` grown to the context's slot count."""
+        from .workloads import HostTangle
+        n, _, _ = self.tangle_info()
+        if n > host.n:
+            pos = np.zeros((n, 3))
+            pos[:host.n] = host.pos
+            fwd = np.full(n, -1)
+            rev = np.full(n, -1)
+            st = np.full(n, abi.OV_EMPTY)
+            fwd[:host.n], rev[:host.n], st[:host.n] = host.conn[:, 0], host.conn[:, 1], host.stat[:, 0]
+            host = HostTangle(pos, fwd, rev, host.box_lo, host.box_hi, n_images=host.n_images, status=st)
+        return self.download(host)
 
     def download(self, host=None, fields: int = abi.OV_F_ALL):
         host = host or self._host

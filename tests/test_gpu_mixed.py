@@ -1,0 +1,62 @@
+"""Mixed-precision traversal against the FP64 tree (needs a GB300).
+
+The mixed path takes the same accept/open decisions as the FP64 path (FP32
+outside a guard band, FP64 inside it), so visit and accept counts must be
+equal, and velocities must agree within 1e-6 relative L2 (the stated gate).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from openvort_gb300 import abi, gpu, workloads as W
+from tests._util import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 1e-6
+
+
+def _eval(ht, p, prec):
+    ctx = gpu.Context(0, params=p, precision=prec)
+    ctx.upload(ht)
+    ctx.update_tangle(0.0)
+    ctx.download(ht, abi.OV_F_VELS | abi.OV_F_VS)
+    st = ctx.stats()
+    ctx.close()
+    return np.array(ht.vels), np.array(ht.vs), st
+
+
+@pytest.mark.parametrize("n_loops,theta", [(256, 0.4), (1024, 0.3), (1024, 0.5)])
+def test_mixed_vs_fp64_tree(n_loops, theta):
+    ht = W.random_walk_tangle(n_loops, 256, D=0.1, seed=1)
+    p = W.config_params("rw", bh_resolution=theta)
+    v64, s64, st64 = _eval(ht, p, abi.OV_PREC_FP64)
+    v32, s32, st32 = _eval(ht, p, abi.OV_PREC_MIXED)
+    assert st32["error_word"] == 0
+    assert st32["accepts"] == st64["accepts"] and st32["visits"] == st64["visits"]
+    assert rel_l2(v32, v64) < MIXED_TOL
+    assert rel_l2(s32, s64) < MIXED_TOL
+
+
+def test_mixed_rk4_and_edge_cases():
+    ht = W.random_walk_tangle(10, 48, D=0.1, seed=24)
+    ht.pos[::5] += 0.004
+    p = W.config_params("rw")
+    v64, _, _ = _eval(ht, p, abi.OV_PREC_FP64)
+    v32, _, st = _eval(ht, p, abi.OV_PREC_MIXED)
+    assert st["error_word"] == 0
+    assert rel_l2(v32, v64) < MIXED_TOL
+    # an RK4 step in mixed precision stays within the gate of the FP64 step
+    out = []
+    for prec in (abi.OV_PREC_FP64, abi.OV_PREC_MIXED):
+        h = W.random_walk_tangle(16, 64, D=0.1, seed=50)
+        ctx = gpu.Context(0, params=p, precision=prec)
+        ctx.upload(h)
+        ctx.update_tangle(0.0)
+        ctx.rk4_step(0.0, 5e-5)
+        ctx.download(h, abi.OV_F_POS)
+        ctx.close()
+        out.append(np.array(h.pos))
+    start = W.random_walk_tangle(16, 64, D=0.1, seed=50).pos
+    assert rel_l2(out[1] - start, out[0] - start) < MIXED_TOL

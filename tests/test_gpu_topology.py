@@ -1,0 +1,125 @@
+"""Topology passes and full time steps on the GPU against OpenVort's own
+outputs (golden vectors) and the C oracle (needs a GB300).
+
+Gates: reconnection counts, connections and status identical; positions
+within 1e-10 of the reference (FP64 path; only summation order differs).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from openvort_gb300 import abi, gpu, workloads as W
+from oracle.pyoracle import Checker
+from tests._util import host_from_arrays, rel_err, used
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name,cfg", [("dense_steps.npz", "rw"), ("rings8_steps.npz", "rings8")])
+def test_full_steps_match_reference(golden, name, cfg):
+    g = golden(name)
+    ht = host_from_arrays(g)
+    p = W.config_params(cfg)
+    ctx = gpu.Context(0, params=p)
+    ctx.upload(ht)
+    dt = float(g["dt"])
+    recs = []
+    steps = g["traj_steps"] if "traj_steps" in g else np.arange(len(g["recs"]))
+    for s in range(len(g["recs"])):
+        ctx.step(s * dt, dt)
+        recs.append(ctx.stats()["reconnections"])
+        if name.startswith("dense"):
+            out = ctx.download_resized(ht)
+            np.testing.assert_array_equal(out.conn, g["conn_steps"][s])
+            np.testing.assert_array_equal(out.stat, g["status_steps"][s])
+            m = used(g["status_steps"][s])
+            assert rel_err(out.pos[m], g["traj"][s][m]) < 1e-10
+        elif s in steps:
+            out = ctx.download_resized(ht)
+            i = list(steps).index(s)
+            m = used(out.stat)
+            assert rel_err(out.pos[m], g["traj"][i][m]) < 1e-10
+    assert recs == list(g["recs"])
+    if "conn_final" in g:
+        out = ctx.download_resized(ht)
+        np.testing.assert_array_equal(out.conn, g["conn_final"])
+    ctx.close()
+
+
+@pytest.mark.parametrize("tag", ["coarse", "fine"])
+def test_remesh_matches_reference(golden, tag):
+    g = golden("remesh.npz")
+    ht = host_from_arrays(g, prefix=f"{tag}_in_")
+    ctx = gpu.Context(0, params=W.config_params("rw"))
+    ctx.upload(ht)
+    ctx.remesh(5e-4, 1.5e-3, 0.0)
+    n, _, _ = ctx.tangle_info()
+    assert n == int(g[f"{tag}_N"])
+    out = ctx.download_resized(ht)
+    ctx.close()
+    np.testing.assert_array_equal(out.conn, g[f"{tag}_conn"])
+    np.testing.assert_array_equal(out.stat, g[f"{tag}_status"])
+    m = used(g[f"{tag}_status"])
+    assert rel_err(out.pos[m], g[f"{tag}_pos"][m]) < 1e-12
+
+
+def test_reconnect_log_and_small_loops_vs_oracle():
+    port = Checker("port")
+    ht = W.random_walk_tangle(40, 48, D=0.03, seed=61)
+    p = W.config_params("rw")
+    port.set_params(p)
+    t = port.tangle(ht)
+    n_ref, log_ref = port.reconnect(t, 0.0, log=True)
+    removed_ref = port.eliminate_small_loops(t)
+    ctx = gpu.Context(0, params=p)
+    ctx.upload(ht)
+    n_gpu, log_gpu = ctx.reconnect(0.0, log=True)
+    ctx.eliminate_small_loops()
+    st = ctx.stats()
+    out = ctx.download_resized(ht)
+    ctx.close()
+    assert n_ref > 0 and n_gpu == n_ref and log_gpu == log_ref
+    assert st["small_loops_removed"] == removed_ref
+    np.testing.assert_array_equal(out.conn, t.copy("conn"))
+    np.testing.assert_array_equal(out.stat, t.copy("status"))
+
+
+def test_smoothing_vs_oracle():
+    port = Checker("port")
+    ht = W.random_walk_tangle(12, 64, D=0.1, seed=62)
+    # one loop spans more than half the box so the detrended branch runs too
+    k = np.arange(64)
+    ht.pos[:64] = np.stack([np.mod(0.01 + k * 0.1 / 64 * 1.0, 0.1), 0.05 + 0.002 * np.sin(k), 0.05 + 0 * k], 1)
+    p = W.config_params("rw", use_freq_filter=1, freq_to_cutoff=0.8)
+    port.set_params(p)
+    t = port.tangle(ht)
+    port.smooth(t)
+    ctx = gpu.Context(0, params=p)
+    ctx.upload(ht)
+    ctx.smooth()
+    out = ctx.download(ht, abi.OV_F_POS)
+    ctx.close()
+    ref = t.copy("pos")
+    assert np.abs(out.pos - ref).max() < 1e-12
+    assert np.abs(ref - W.random_walk_tangle(12, 64, D=0.1, seed=62).pos[:]).max() > 0  # it smoothed
+
+
+def test_remesh_grows_pool_like_expand_tangle():
+    # every segment longer than dl_max: the pool must double, as expand_tangle does
+    ht = W.random_walk_tangle(2, 20, D=0.1, delta=4e-3, seed=63)
+    port = Checker("port")
+    p = W.config_params("rw")
+    port.set_params(p)
+    t = port.tangle(ht)
+    port.remesh(t, p.dl_min, p.dl_max, 0.0)
+    ctx = gpu.Context(0, params=p)
+    ctx.upload(ht)
+    ctx.remesh(p.dl_min, p.dl_max, 0.0)
+    out = ctx.download_resized(ht)
+    n, ne, te = ctx.tangle_info()
+    ctx.close()
+    assert n == t.n and n > ht.n
+    np.testing.assert_array_equal(out.conn, t.copy("conn"))
+    m = used(out.stat)
+    assert rel_err(out.pos[m], t.copy("pos")[m]) < 1e-12
