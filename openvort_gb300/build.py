@@ -20,6 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "lib")
 OBJ = os.path.join(LIB, "_obj")
 SO = os.path.join(LIB, "libovgpu.so")
+DROPIN = os.path.join(LIB, "libovdropin.a")
 
 CU_SOURCES = ["ov_sort.cu", "ov_tree.cu", "ov_velocity.cu", "ov_mixed.cu", "ov_capi.cu", "ov_topology.cu", "ov_peak.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -62,7 +63,20 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if p.returncode != 0:
         raise RuntimeError(f"link failed:\n{p.stderr}")
     os.replace(tmp, SO)
+    build_dropin()
     return SO
+
+
+def build_dropin() -> str:
+    """ov_dropin.c -> libovdropin.a (with the __wrap_ aliases) for linking into the reference."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    obj = os.path.join(OBJ, "ov_dropin.o")
+    subprocess.run([cc, "-O2", "-fPIC", "-ffp-contract=off", "-DOV_DROPIN_WRAP", "-c",
+                    os.path.join(CSRC, "ov_dropin.c"), "-o", obj], check=True)
+    if os.path.exists(DROPIN):
+        os.remove(DROPIN)
+    subprocess.run(["ar", "rcs", DROPIN, obj], check=True)
+    return DROPIN
 
 
 if __name__ == "__main__":

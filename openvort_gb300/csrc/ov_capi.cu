@@ -136,6 +136,7 @@ int ov_ctx_destroy(ov_ctx *c)
     for (int *p : is)
         if (p) cudaFree(p);
     if (c->dsum) cudaFree(c->dsum);
+    if (c->part) cudaFree(c->part);
     if (c->flush_buf) cudaFree(c->flush_buf);
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->rk4_exec) cudaGraphExecDestroy(c->rk4_exec);
@@ -459,7 +460,7 @@ static int eval_async(ov_ctx *c, NodeArrays &na, double t, bool tangents, cudaSt
     int r = ov_tree_build(c, na, s);
     if (r) return r;
     if (ph) OV_CUDA(c, cudaEventRecord(c->ph[2], s));
-    ov_launch_velocities(c, na, t, c->precision, s);
+    if ((r = ov_launch_velocities(c, na, t, c->precision, s))) return r;
     if (ph) OV_CUDA(c, cudaEventRecord(c->ph[3], s));
     OV_CUDA(c, cudaGetLastError());
     return OV_OK;

@@ -160,6 +160,9 @@ struct ov_ctx {
     int rk4_prec = -1;
     // mixed-precision grid split
     double grid_h = 0;
+    // per-group partial velocity sums of the traversal (6 doubles x groups x cap)
+    double *part = nullptr;
+    size_t part_cap = 0;
     // direct-sum scratch
     double *dsum = nullptr;
     int dsum_cap = 0;
@@ -208,7 +211,7 @@ void ov_scan_exclusive(ov_ctx *c, const int *in, int *out, int n_max, const int 
 
 // velocity path (ov_velocity.cu)
 void ov_launch_tangents(ov_ctx *c, const NodeArrays &na, cudaStream_t s);
-void ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s);
+int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s);
 int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out);
 void ov_launch_euler(ov_ctx *c, const NodeArrays &src, const double *vx, const double *vy,
                      const double *vz, double dt, NodeArrays &dst, cudaStream_t s);

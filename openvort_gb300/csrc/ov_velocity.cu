@@ -39,6 +39,7 @@ struct VelArgs {
     double grid_h, inv_h;   // mixed path
     float shift_g[OV_MAX_IMAGES][3], shift_f[OV_MAX_IMAGES][3];   // L*shift split on the grid
     int cap;                // node slots (bounds checks)
+    float th2f, near2f, f4pif;   // theta^2, near-field radius^2, KAPPA/4/pi in FP32
     double near2;           // mixed path: squared near-field radius
     unsigned long long *stat;
 };
@@ -328,16 +329,23 @@ __device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const doub
     return true;
 }
 
-__global__ void __launch_bounds__(128) k_vel_fp64(VelArgs a)
+// The 1 + n_img query points of every node (qi = 0 the node itself, qi >= 1
+// image qi-1) are split over G warp groups (blockIdx.y = g takes qi = g,
+// g+G, ...) so that small tangles still fill the GPU; each group writes its
+// partial sums (own point, images) per sorted target and k_vel_finish adds
+// them in group order.
+__global__ void __launch_bounds__(128) k_vel_fp64(VelArgs a, int G, double *__restrict__ part_out)
 {
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int g = blockIdx.y;
     const int nne = a.counters[TC_NNE];
     const int ncell = a.counters[TC_NCELL];
     if (warp * 32 >= nne) return;   // warp-uniform
     const int tix = warp * 32 + lane;
-    const bool valid = tix < nne;
-    const int id = valid ? a.order[tix] : 0;
+    bool valid = tix < nne && tix < a.cap;
+    int id = valid ? a.order[tix] : 0;
+    if (valid && (id < 0 || id >= a.cap)) { bad_index(a, 4, id); valid = false; id = 0; }
     const int st = valid ? a.status[id] : OV_EMPTY;
     const bool part = valid && st != OV_PINNED && st != OV_EMPTY && a.prm.use_bh;
     double p[3] = {0, 0, 0};
@@ -345,7 +353,8 @@ __global__ void __launch_bounds__(128) k_vel_fp64(VelArgs a)
     double prim[3] = {0, 0, 0}, img[3] = {0, 0, 0};
     unsigned long long visits = 0, accepts = 0, steps = 0;
     bool overflow = false;
-    for (int j = -1; j < a.geo.n_img; ++j) {
+    for (int qi = g; qi <= a.geo.n_img; qi += G) {
+        const int j = qi - 1;
         double q[3], v[3];
         if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
         else image_point(a.geo, j, p, q);
@@ -357,15 +366,14 @@ __global__ void __launch_bounds__(128) k_vel_fp64(VelArgs a)
             img[0] = rn_add(img[0], v[0]); img[1] = rn_add(img[1], v[1]); img[2] = rn_add(img[2], v[2]);
         }
     }
-    int err = overflow ? OV_EW_ITER : 0;
-    if (valid && st != OV_EMPTY) {
-        double vs[3], vel[3];
-        if (finish_node(a, id, p, prim, img, &err, vs, vel)) {
-            a.sx[id] = vs[0]; a.sy[id] = vs[1]; a.sz[id] = vs[2];
-            a.vx[id] = vel[0]; a.vy[id] = vel[1]; a.vz[id] = vel[2];
+    if (valid) {
+        const size_t cap = (size_t)a.cap;
+        for (int ax = 0; ax < 3; ++ax) {
+            part_out[((size_t)(2 * g) * 3 + ax) * cap + tix] = prim[ax];
+            part_out[((size_t)(2 * g + 1) * 3 + ax) * cap + tix] = img[ax];
         }
     }
-    // counters: one atomic per warp
+    int err = overflow ? OV_EW_ITER : 0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         visits += __shfl_xor_sync(0xffffffffu, visits, o);
@@ -373,11 +381,38 @@ __global__ void __launch_bounds__(128) k_vel_fp64(VelArgs a)
         err |= __shfl_xor_sync(0xffffffffu, err, o);
     }
     if (lane == 0) {
-        atomicAdd(&a.stat[0], visits);
-        atomicAdd(&a.stat[1], accepts);
-        atomicAdd(&a.stat[2], steps);
+        atomicAdd(&a.stat[ST_VISITS], visits);
+        atomicAdd(&a.stat[ST_ACCEPTS], accepts);
+        atomicAdd(&a.stat[ST_STEPS], steps);
         if (err) atomicOr((int *)&a.counters[TC_ERR], err);
     }
+}
+
+// Sum the group partials in group order, then LIA, v_s and mutual friction.
+__global__ void k_vel_finish(VelArgs a, int G, const double *__restrict__ part_in)
+{
+    const int tix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nne = a.counters[TC_NNE];
+    if (tix >= nne || tix >= a.cap) return;
+    int id = a.order[tix];
+    if (id < 0 || id >= a.cap) { bad_index(a, 7, id); return; }
+    const int st = a.status[id];
+    if (st == OV_EMPTY) return;
+    const size_t cap = (size_t)a.cap;
+    double prim[3] = {0, 0, 0}, img[3] = {0, 0, 0};
+    for (int g = 0; g < G; ++g)
+        for (int ax = 0; ax < 3; ++ax) {
+            prim[ax] = rn_add(prim[ax], part_in[((size_t)(2 * g) * 3 + ax) * cap + tix]);
+            img[ax] = rn_add(img[ax], part_in[((size_t)(2 * g + 1) * 3 + ax) * cap + tix]);
+        }
+    double p[3] = {a.x[id], a.y[id], a.z[id]};
+    double vs[3], vel[3];
+    int err = 0;
+    if (finish_node(a, id, p, prim, img, &err, vs, vel)) {
+        a.sx[id] = vs[0]; a.sy[id] = vs[1]; a.sz[id] = vs[2];
+        a.vx[id] = vel[0]; a.vy[id] = vel[1]; a.vz[id] = vel[2];
+    }
+    if (err) atomicOr((int *)&a.counters[TC_ERR], err);
 }
 
 // ------------------------------------------------------------ direct sum
@@ -566,9 +601,9 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
                                            double w64[3], bool &overflow)
 // near_list: this lane's column of a shared [kNearCap][32] array, stride 32
 {
-    const float th2 = (float)(a.prm.theta * a.prm.theta);
-    const float near2 = (float)a.near2;
-    const float f4pi = (float)a.f4pi;
+    const float th2 = a.th2f;
+    const float near2 = a.near2f;
+    const float f4pi = a.f4pif;
     int c = 0;
     int resume = part ? 0 : 0x7fffffff;
     const int guard_max = 4 * ncell + 64;
@@ -655,10 +690,11 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
     m.nstep += steps;
 }
 
-__global__ void __launch_bounds__(128) k_vel_mixed(VelArgs a)
+__global__ void __launch_bounds__(128) k_vel_mixed(VelArgs a, int G, double *__restrict__ part_out)
 {
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int grp = blockIdx.y;
     const int nne = a.counters[TC_NNE];
     const int ncell = a.counters[TC_NCELL];
     if (warp * 32 >= nne) return;
@@ -684,7 +720,8 @@ __global__ void __launch_bounds__(128) k_vel_mixed(VelArgs a)
     int *near_list = &s_near[(threadIdx.x >> 5) & 3][lane];
     int nnear = 0;
     bool overflow = false;
-    for (int j = -1; j < a.geo.n_img; ++j) {
+    for (int qi = grp; qi <= a.geo.n_img; qi += G) {
+        const int j = qi - 1;
         float g[3], f[3];
         if (j < 0) {
             for (int ax = 0; ax < 3; ++ax) { g[ax] = g0[ax]; f[ax] = f0[ax]; }
@@ -724,15 +761,14 @@ __global__ void __launch_bounds__(128) k_vel_mixed(VelArgs a)
     double bh[3] = {((double)m.s0 - (double)m.c0) + w64[0] + img64[0],
                     ((double)m.s1 - (double)m.c1) + w64[1] + img64[1],
                     ((double)m.s2 - (double)m.c2) + w64[2] + img64[2]};
-    double zero[3] = {0, 0, 0};
-    int err = overflow ? OV_EW_ITER : 0;
-    if (valid && st != OV_EMPTY) {
-        double vs[3], vel[3];
-        if (finish_node(a, id, p, bh, zero, &err, vs, vel)) {
-            a.sx[id] = vs[0]; a.sy[id] = vs[1]; a.sz[id] = vs[2];
-            a.vx[id] = vel[0]; a.vy[id] = vel[1]; a.vz[id] = vel[2];
+    if (valid) {
+        const size_t cap = (size_t)a.cap;
+        for (int ax = 0; ax < 3; ++ax) {
+            part_out[((size_t)(2 * grp) * 3 + ax) * cap + tix] = bh[ax];
+            part_out[((size_t)(2 * grp + 1) * 3 + ax) * cap + tix] = 0.0;
         }
     }
+    int err = overflow ? OV_EW_ITER : 0;
     unsigned long long visits = m.nvis, accepts = m.nacc, fallback = m.nfb, near64 = m.nnear;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -782,6 +818,9 @@ VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long 
         }
     a.stat = stat;
     a.cap = c->cap;
+    a.th2f = (float)(a.prm.theta * a.prm.theta);
+    a.near2f = (float)a.near2;
+    a.f4pif = (float)a.f4pi;
     return a;
 }
 
@@ -794,17 +833,37 @@ void ov_launch_tangents(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     c->launches++;
 }
 
-void ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s)
+// Query groups per node: enough warps for ~32 per SM on small tangles.
+int ov_query_groups(ov_ctx *c)
+{
+    int warps = (c->cap + 31) / 32;
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    int G = (32 * sms + warps - 1) / warps;
+    return G < 1 ? 1 : (G > 8 ? 8 : G);
+}
+
+int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s)
 {
     VelArgs a = make_args(c, na, t, ov_stat_ptr(c));
+    int G = ov_query_groups(c);
+    size_t need = (size_t)G * 6 * (size_t)c->cap;
+    if (c->part_cap < need) {
+        if (c->part) cudaFree(c->part);
+        c->part = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->part, need * sizeof(double)));
+        c->part_cap = need;
+    }
     int warps = (c->cap + 31) / 32;
     int threads = 128;
-    int blocks = (warps * 32 + threads - 1) / threads;
+    dim3 grid((warps * 32 + threads - 1) / threads, G);
     if (precision == OV_PREC_MIXED)
-        k_vel_mixed<<<blocks, threads, 0, s>>>(a);
+        k_vel_mixed<<<grid, threads, 0, s>>>(a, G, c->part);
     else
-        k_vel_fp64<<<blocks, threads, 0, s>>>(a);
-    c->launches++;
+        k_vel_fp64<<<grid, threads, 0, s>>>(a, G, c->part);
+    k_vel_finish<<<(c->cap + 127) / 128, 128, 0, s>>>(a, G, c->part);
+    c->launches += 2;
+    return OV_OK;
 }
 
 int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out)

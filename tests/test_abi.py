@@ -18,10 +18,18 @@ def lib():
 
 
 def test_every_declared_symbol_is_exported(lib):
+    """ov_* from libovgpu.so, ovd_* (the drop-in layer) from libovdropin.a."""
+    import subprocess
+    from openvort_gb300 import build
     names = gpu.declared_symbols()
-    assert "ov_update_velocities" in names and "ov_rk4_step" in names
-    missing = [n for n in names if not hasattr(lib, n)]
+    assert "ov_update_velocities" in names and "ov_rk4_step" in names and "ovd_update_velocities" in names
+    missing = [n for n in names if n.startswith("ov_") and not hasattr(lib, n)]
     assert not missing, missing
+    syms = subprocess.run(["nm", build.DROPIN], capture_output=True, text=True).stdout
+    defined = {ln.split()[-1] for ln in syms.splitlines() if " T " in ln}
+    missing = [n for n in names if n.startswith("ovd_") and n not in defined]
+    assert not missing, missing
+    assert "__wrap_update_velocities" in defined
 
 
 def test_defaults_are_the_reference_defaults(lib):
