@@ -78,7 +78,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -208,14 +208,14 @@ def run_ours(args):
     l0 = ctx.kernel_launches
     barrier(dist)
     ctx.synchronize()
-    with ClockSampler(device) as clk:
-        for _ in range(args.steps):
-            ctx.flush_l2(256 << 20)
-            ctx.timer_start()
-            ctx.update_tangle(0.0)
-            step_ms.append(ctx.timer_stop())
-            trav_ms.append(ctx.phase_times())
-        ctx.synchronize()
+    clk = ClockSampler(device).__enter__()
+    for _ in range(args.steps):
+        ctx.flush_l2(256 << 20)
+        ctx.timer_start()
+        ctx.update_tangle(0.0)
+        step_ms.append(ctx.timer_stop())
+        trav_ms.append(ctx.phase_times())
+    ctx.synchronize()
     launches = ctx.kernel_launches - l0 - args.steps     # minus the flush memsets (not kernels of ours)
     barrier(dist)
     st = ctx.stats()
@@ -271,6 +271,27 @@ def run_ours(args):
     except Exception as e:  # mixed path not built yet
         mixed = {"unavailable": str(e)[:200]}
 
+    # ---- RK4 steps/s: update_tangle (k1) + rk4_step (three stages + combine, one CUDA graph)
+    rk4 = {}
+    for name, prec in (("fp64", abi.OV_PREC_FP64), ("mixed", abi.OV_PREC_MIXED)):
+        ctx.set_precision(prec)
+        ctx.upload(ht)
+        dt = 5e-5
+        for w in range(2):
+            ctx.update_tangle(w * dt)
+            ctx.rk4_step(w * dt, dt)
+        ts = []
+        for k in range(max(2, args.steps // 2)):
+            ctx.flush_l2(256 << 20)
+            ctx.timer_start()
+            ctx.update_tangle(k * dt)
+            ctx.rk4_step(k * dt, dt)
+            ts.append(ctx.timer_stop())
+        rk4[name] = {"steps_per_s": 1e3 / statistics.mean(ts), "ms_per_step": statistics.mean(ts),
+                     "node_evals_per_s": 4 * n / (statistics.mean(ts) * 1e-3)}
+    ctx.set_precision(abi.OV_PREC_FP64)
+    clk.__exit__(None, None, None)
+
     # ---- CPU baseline (rank 0 only, bounded sample)
     cpu = None
     if rank == 0 and world == 1:
@@ -300,6 +321,7 @@ def run_ours(args):
         "e2e": {"value": world * n / (e2e_mean * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "mixed": mixed,
+        "rk4": rk4,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "peaks_source": peak_src,

@@ -124,6 +124,9 @@ int ov_ctx_destroy(ov_ctx *ctx);
 const char *ov_last_error(const ov_ctx *ctx);
 int ov_set_params(ov_ctx *ctx, const ov_params *p);
 int ov_set_precision(ov_ctx *ctx, int precision);
+/* RK4 steps run as one captured CUDA graph (default on); off launches the
+   same kernels one by one (identical results). */
+int ov_set_rk4_graph(ov_ctx *ctx, int on);
 /* cudaStream_t the context launches on, as an opaque pointer (for callers that
    time or order their own work against it). */
 void *ov_ctx_stream(ov_ctx *ctx);

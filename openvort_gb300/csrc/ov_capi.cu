@@ -106,6 +106,7 @@ int ov_ctx_create(ov_ctx **out, int device)
     if (device < 0 || device >= n) return OV_ERR_ARG;
     ov_ctx *c = new ov_ctx();
     c->device = device;
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     ov_params_default(&c->params);
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
@@ -142,6 +143,8 @@ int ov_ctx_destroy(ov_ctx *c)
     if (c->rk4_exec) cudaGraphExecDestroy(c->rk4_exec);
     for (int i = 0; i < 4; ++i)
         if (c->ph[i]) cudaEventDestroy(c->ph[i]);
+    if (c->d_time) cudaFree(c->d_time);
+    if (c->h_time) cudaFreeHost(c->h_time);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -155,6 +158,13 @@ int ov_set_params(ov_ctx *c, const ov_params *p)
 {
     if (!c || !p) return OV_ERR_ARG;
     c->params = *p;
+    return OV_OK;
+}
+
+int ov_set_rk4_graph(ov_ctx *c, int on)
+{
+    if (!c) return OV_ERR_ARG;
+    c->use_graph = on != 0;
     return OV_OK;
 }
 
@@ -451,9 +461,16 @@ static int error_from_word(ov_ctx *c)
 }
 
 // tangents + tree + traversal of one tangle on stream s (no host sync)
+// Clear the error words that accumulate over one API call.
+static int clear_call_words(ov_ctx *c)
+{
+    OV_CUDA(c, cudaMemsetAsync(c->tree.counters + TC_ERR, 0, (TC_COUNT - TC_ERR) * 4, c->stream));
+    return OV_OK;
+}
+
 static int eval_async(ov_ctx *c, NodeArrays &na, double t, bool tangents, cudaStream_t s)
 {
-    bool ph = c->phase_timing;
+    bool ph = c->phase_timing && c->time_dev_index < 0;
     if (ph) OV_CUDA(c, cudaEventRecord(c->ph[0], s));
     if (tangents) ov_launch_tangents(c, na, s);
     if (ph) OV_CUDA(c, cudaEventRecord(c->ph[1], s));
@@ -471,6 +488,7 @@ int ov_eval_sync(ov_ctx *c, NodeArrays &na, double t, bool tangents)
 {
     int r;
     for (int attempt = 0; attempt < 3; ++attempt) {
+        if ((r = clear_call_words(c))) return r;
         if ((r = eval_async(c, na, t, tangents, c->stream))) return r;
         if ((r = collect_stats(c, true))) return r;
         if (!(c->stats.error_word & OV_EW_CELLS)) return error_from_word(c);
@@ -488,7 +506,7 @@ int ov_update_tangents_normals(ov_ctx *c)
     int r = check_ready(c);
     if (r) return r;
     OV_CUDA(c, cudaMemsetAsync(c->tree.counters, 0, TC_WORDS * 4, c->stream));
-    ov_launch_tangents(c, c->node, c->stream);
+    ov_launch_tangents(c, c->node, c->stream);   // (all counter words cleared: a new call)
     OV_CUDA(c, cudaGetLastError());
     if ((r = collect_stats(c, true))) return r;
     return error_from_word(c);
@@ -509,26 +527,102 @@ int ov_update_tangle(ov_ctx *c, double t)
 }
 
 // RK4 (vortex_dynamics.c:50-119) from k1 = the context's current vels.
+// The RK4 sequence (vortex_dynamics.c:75-115) as launched on stream s:
+// three Euler stages from the start positions, each followed by tangents,
+// tree and velocities, then the combine.  Times come from d_time when
+// time_dev_index >= 0 (graph capture).
+static int rk4_sequence(ov_ctx *c, double t, double dt, cudaStream_t s)
+{
+    const double *vin[3][3] = {{c->node.vx, c->node.vy, c->node.vz},
+                               {c->stage[0].vx, c->stage[0].vy, c->stage[0].vz},
+                               {c->stage[1].vx, c->stage[1].vy, c->stage[1].vz}};
+    const double tt[3] = {t + dt / 2, t + dt / 2, t + dt};
+    int r;
+    for (int k = 0; k < 3; ++k) {
+        if (c->time_dev_index >= 0) c->time_dev_index = k;
+        ov_launch_euler(c, c->node, vin[k][0], vin[k][1], vin[k][2], dt / 2, c->stage[k], s);
+        if ((r = eval_async(c, c->stage[k], tt[k], true, s))) return r;
+    }
+    ov_launch_rk4_combine(c, dt, s);
+    OV_CUDA(c, cudaGetLastError());
+    return OV_OK;
+}
+
+static unsigned long long mix64(unsigned long long h, const void *p, size_t n)
+{
+    const unsigned char *b = (const unsigned char *)p;
+    for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    return h;
+}
+
+// Identity of everything the captured graph bakes in: buffers, sizes,
+// parameters, geometry, precision.
+static unsigned long long graph_key(ov_ctx *c)
+{
+    unsigned long long h = 1469598103934665603ull;
+    h = mix64(h, &c->params, sizeof c->params);
+    h = mix64(h, &c->geo, sizeof c->geo);
+    int ints[4] = {c->cap, c->tree.cap_cells, c->precision, 0};
+    h = mix64(h, ints, sizeof ints);
+    const void *ptrs[4] = {c->node.x, c->tree.cells, c->part, c->d_time};
+    h = mix64(h, ptrs, sizeof ptrs);
+    return h;
+}
+
 int ov_rk4_step(ov_ctx *c, double t, double dt)
 {
     int r = check_ready(c);
     if (r) return r;
     cudaStream_t s = c->stream;
-    const double *vin[3][3] = {{c->node.vx, c->node.vy, c->node.vz},
-                               {c->stage[0].vx, c->stage[0].vy, c->stage[0].vz},
-                               {c->stage[1].vx, c->stage[1].vy, c->stage[1].vz}};
-    const double tt[3] = {t + dt / 2, t + dt / 2, t + dt};
-    int64_t err = 0;
-    for (int k = 0; k < 3; ++k) {
-        ov_launch_euler(c, c->node, vin[k][0], vin[k][1], vin[k][2], dt / 2, c->stage[k], s);
-        if ((r = ov_eval_sync(c, c->stage[k], tt[k], true))) return r;
-        err |= c->stats.error_word;
+    if (!c->d_time) {
+        OV_CUDA(c, cudaMalloc(&c->d_time, 8 * sizeof(double)));
+        OV_CUDA(c, cudaMallocHost(&c->h_time, 8 * sizeof(double)));
     }
-    ov_launch_rk4_combine(c, dt, s);
-    OV_CUDA(c, cudaGetLastError());
-    OV_CUDA(c, cudaStreamSynchronize(s));
-    c->stats.error_word = err;
-    return error_from_word(c);
+    if ((r = ov_reserve_velocity_scratch(c))) return r;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        if ((r = clear_call_words(c))) return r;
+        c->h_time[0] = t + dt / 2;
+        c->h_time[1] = t + dt / 2;
+        c->h_time[2] = t + dt;
+        c->h_time[3] = dt / 2;
+        c->h_time[4] = dt;
+        OV_CUDA(c, cudaMemcpyAsync(c->d_time, c->h_time, 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (c->use_graph) {
+            unsigned long long key = graph_key(c);
+            if (!c->rk4_exec || key != c->rk4_key) {
+                if (c->rk4_exec) { cudaGraphExecDestroy(c->rk4_exec); c->rk4_exec = nullptr; }
+                cudaGraph_t g = nullptr;
+                OV_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                c->time_dev_index = 0;
+                int64_t l0 = c->launches;
+                r = rk4_sequence(c, t, dt, s);
+                c->rk4_kernels = c->launches - l0;
+                c->launches = l0;
+                c->time_dev_index = -1;
+                cudaError_t e = cudaStreamEndCapture(s, &g);
+                if (r) { if (g) cudaGraphDestroy(g); return r; }
+                if (e != cudaSuccess) return ov_fail(c, OV_ERR_CUDA, "RK4 graph capture: %s", cudaGetErrorString(e));
+                e = cudaGraphInstantiate(&c->rk4_exec, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) return ov_fail(c, OV_ERR_CUDA, "RK4 graph instantiate: %s", cudaGetErrorString(e));
+                c->rk4_key = key;
+            }
+            OV_CUDA(c, cudaGraphLaunch(c->rk4_exec, s));
+            c->launches += c->rk4_kernels;
+        } else {
+            c->time_dev_index = 0;
+            r = rk4_sequence(c, t, dt, s);
+            c->time_dev_index = -1;
+            if (r) return r;
+        }
+        if ((r = collect_stats(c, true))) return r;
+        if (!(c->stats.error_word & OV_EW_CELLS)) return error_from_word(c);
+        // a stage tree did not fit: the combine did not run; grow and redo
+        int need = 0;
+        OV_CUDA(c, cudaMemcpy(&need, c->tree.counters + TC_NEED, 4, cudaMemcpyDeviceToHost));
+        if ((r = ov_tree_reserve_cells(c, need + need / 4 + 64))) return r;
+    }
+    return ov_fail(c, OV_ERR_ALLOC, "cell storage could not be sized");
 }
 
 int ov_direct_velocities(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out)

@@ -21,7 +21,7 @@
 #include "../../include/openvort_gpu.h"
 
 #define OV_MAX_LEVEL 21                 // 3-bit digits below the root: 63 bits
-#define OV_KEY_OUT (0x8000000000000000ull) // node outside the root box (| node id)
+#define OV_KEY_OUT (0x8000000000000000ull) // node outside the root box (| wrapped path >> 1)
 #define OV_KEY_EMPTY (0xFFFFFFFFFFFFFFFFull)
 #define OV_MAX_IMAGES 26
 
@@ -58,6 +58,7 @@ struct TreeBuf {
     int cap = 0;
     uint64_t *keys = nullptr, *keys_alt = nullptr;
     int *order = nullptr, *order_alt = nullptr;
+    int *torder = nullptr;       // traversal order of the targets (spatial, all non-EMPTY)
     int *cpl = nullptr;          // common prefix length with the next key
     int *ncell_at = nullptr;     // cells starting at sorted position s
     int *cell_off = nullptr;     // exclusive scan of ncell_at (+1 for the root)
@@ -75,20 +76,23 @@ struct TreeBuf {
 
 // device-side scalars written by the build
 enum TreeCounters {
+    // cleared by every tree build
     TC_M = 0,          // nodes inside the root box (sorted prefix)
     TC_NNE,            // non-EMPTY nodes (targets)
     TC_NCELL,          // cells
     TC_MAXDEPTH,
     TC_OUT,            // nodes outside the root box
-    TC_ERR,            // error bits
     TC_MAXRUN,
     TC_FALLBACK,       // mixed: guard-band FP64 decisions
     TC_NEAR64,         // mixed: near-field FP64 interactions
-    TC_NEED,           // cells the tree needs (checked against the storage)
+    TC_BUILD_CLEAR,    // = 8: words [0, 8) are per build
+    // cleared once per API call (they accumulate over the stages of an RK4 step)
+    TC_ERR = 8,        // error bits
     TC_BAD,            // first failed bounds check: code << 24 | low bits of the index
+    TC_NEED,           // most cells any build needed (checked against the storage)
     TC_COUNT,
-    TC_STAT64 = 16,    // int offset of the 64-bit counters: visits, accepts, warp steps, ...
-    TC_WORDS = 32      // ints allocated (and cleared per build)
+    TC_STAT64 = 16,    // int offset of the 64-bit counters (per build): visits, accepts, warp steps, ...
+    TC_WORDS = 32      // ints allocated
 };
 enum { ST_VISITS = 0, ST_ACCEPTS, ST_STEPS, ST_FALLBACK, ST_NEAR64 };
 
@@ -121,6 +125,7 @@ struct DevParams {               // ov_params as the kernels need them
 
 struct ov_ctx {
     int device = 0;
+    int sm_count = 152;
     cudaStream_t stream = nullptr;
     ov_params params{};
     int precision = OV_PREC_FP64;
@@ -154,10 +159,15 @@ struct ov_ctx {
     double *d_loop_buf = nullptr;
     int loop_cap = 0, loop_nodes_cap = 0;
     size_t loop_buf_cap = 0;
-    // RK4 graph
+    // RK4 graph: stage times and steps live in d_time = {t+dt/2, t+dt/2,
+    // t+dt, dt/2, dt}; kernels read them when time_dev_index >= 0
     cudaGraphExec_t rk4_exec = nullptr;
-    double rk4_dt = 0, rk4_t = 0;
-    int rk4_prec = -1;
+    unsigned long long rk4_key = 0;
+    double *d_time = nullptr;
+    double *h_time = nullptr;
+    int time_dev_index = -1;
+    bool use_graph = true;
+    int64_t rk4_kernels = 0;     // kernels in the captured RK4 graph
     // mixed-precision grid split
     double grid_h = 0;
     // per-group partial velocity sums of the traversal (6 doubles x groups x cap)
@@ -212,6 +222,7 @@ void ov_scan_exclusive(ov_ctx *c, const int *in, int *out, int n_max, const int 
 // velocity path (ov_velocity.cu)
 void ov_launch_tangents(ov_ctx *c, const NodeArrays &na, cudaStream_t s);
 int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s);
+int ov_reserve_velocity_scratch(ov_ctx *c);
 int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out);
 void ov_launch_euler(ov_ctx *c, const NodeArrays &src, const double *vx, const double *vy,
                      const double *vz, double dt, NodeArrays &dst, cudaStream_t s);

@@ -77,7 +77,29 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
     if (i >= cap) return;
     order[i] = i;
     if (!live) { keys[i] = OV_KEY_EMPTY; return; }
-    if (!inside) { keys[i] = OV_KEY_OUT | (uint64_t)i; return; }
+    if (!inside) {
+        // root-only member (octree.c:116-127).  The rest of the key orders
+        // it among the other root-only nodes by the cell path of its
+        // position clamped to the box, so it can be merged into the
+        // traversal order beside its spatial neighbours (k_target_order).
+        uint64_t k2 = 0;
+        uint64_t W[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            double u = (p[a] - g.lo[a]) / g.L[a];
+            u = fmin(fmax(u, 0.0), 1.0);
+            if (!(u >= 0.0 && u <= 1.0)) u = 0.0;   // non-finite input
+            W[a] = (uint64_t)(u * 4611686018427387904.0);
+        }
+#pragma unroll
+        for (int lev = 1; lev <= OV_MAX_LEVEL; ++lev) {
+            int sh = 62 - lev;
+            uint64_t xb = (W[0] >> sh) & 1, yb = (W[1] >> sh) & 1, zb = (W[2] >> sh) & 1;
+            k2 |= ((zb << 2) | (yb << 1) | (xb ^ 1)) << (63 - 3 * lev);
+        }
+        keys[i] = OV_KEY_OUT | (k2 >> 1);
+        return;
+    }
     uint64_t U[3];
     bool safe = g.fast != 0;
     const uint64_t low = (1ull << 41) - 1, margin = 1ull << 22;
@@ -103,6 +125,40 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
         if (err) atomicOr(&counters[TC_ERR], err);
     }
     keys[i] = key;
+}
+
+// Traversal order: the in-box nodes in path order merged with the root-only
+// nodes at the position of their clamped path (merge by rank; in-box first on
+// ties).  Out-of-box targets then share warps with their spatial neighbours
+// instead of forming a few warps that span the whole box surface.
+__global__ void k_target_order(const uint64_t *__restrict__ keys, const int *__restrict__ order, int cap,
+                               const int *counters, int *__restrict__ torder)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int M = counters[TC_M], nne = counters[TC_NNE];
+    if (s >= nne || s >= cap) return;
+    int nout = nne - M;
+    int pos;
+    if (s < M) {
+        // in-box: its rank plus the root-only nodes whose clamped path is smaller
+        uint64_t k = keys[s];
+        int lo = 0, hi = nout;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (((keys[M + mid] & ~OV_KEY_OUT) << 1) < k) lo = mid + 1; else hi = mid;
+        }
+        pos = s + lo;
+    } else {
+        int j = s - M;
+        uint64_t k = (keys[s] & ~OV_KEY_OUT) << 1;
+        int lo = 0, hi = M;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (keys[mid] <= k) lo = mid + 1; else hi = mid;
+        }
+        pos = j + lo;
+    }
+    torder[pos] = order[s];
 }
 
 __device__ __forceinline__ int cpl_of(uint64_t a, uint64_t b)
@@ -170,7 +226,7 @@ __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict
     int ncell = cell_off[M];
     if (ncell > cap_cells) {
         if (s == 0) {
-            counters[TC_NEED] = ncell;
+            atomicMax(&counters[TC_NEED], ncell);
             atomicOr(&counters[TC_ERR], OV_EW_CELLS);
         }
         return;
@@ -388,19 +444,21 @@ int ov_tree_reserve(ov_ctx *c, int cap)
     OV_CUDA(c, cudaMalloc(&t.keys_alt, n * 8));
     OV_CUDA(c, cudaMalloc(&t.order, n * 4));
     OV_CUDA(c, cudaMalloc(&t.order_alt, n * 4));
+    OV_CUDA(c, cudaMalloc(&t.torder, n * 4));
     OV_CUDA(c, cudaMalloc(&t.cpl, n * 4 + 4));
     OV_CUDA(c, cudaMalloc(&t.ncell_at, n * 4 + 4));
     OV_CUDA(c, cudaMalloc(&t.cell_off, n * 4 + 8));
     OV_CUDA(c, cudaMalloc(&t.scan_tmp, (size_t)ov_scan_tmp_ints(cap) * 4));
     OV_CUDA(c, cudaMalloc(&t.sort_hist, (size_t)ov_sort_hist_ints(cap) * 4));
     OV_CUDA(c, cudaMalloc(&t.counters, TC_WORDS * 4));
+    OV_CUDA(c, cudaMemset(t.counters, 0, TC_WORDS * 4));
     // cells: about 1.3 per node for filament tangles; grown on demand
     return ov_tree_reserve_cells(c, 2 * cap + 64);
 }
 
 void ov_tree_free(TreeBuf &t)
 {
-    void *ptrs[] = {t.keys, t.keys_alt, t.order, t.order_alt, t.cpl, t.ncell_at, t.cell_off, t.scan_tmp,
+    void *ptrs[] = {t.keys, t.keys_alt, t.order, t.order_alt, t.torder, t.cpl, t.ncell_at, t.cell_off, t.scan_tmp,
                     t.sort_hist, t.cells, t.cells32, t.parent, t.nchild, t.arrive, t.csum, t.counters};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -433,14 +491,16 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     int cap = c->cap;
     c->tree_built = false;   // a query tree is only current until the next build
     KeyGeom g = key_geom(c->geo);
-    OV_CUDA(c, cudaMemsetAsync(t.counters, 0, TC_WORDS * 4, s));
+    OV_CUDA(c, cudaMemsetAsync(t.counters, 0, TC_BUILD_CLEAR * 4, s));
+    OV_CUDA(c, cudaMemsetAsync(t.counters + TC_STAT64, 0, (TC_WORDS - TC_STAT64) * 4, s));
     OV_CUDA(c, cudaMemsetAsync(t.nchild, 0, (size_t)t.cap_cells * 4, s));
     int nb = (cap + 255) / 256;
     k_keys<<<nb, 256, 0, s>>>(c->status, na.x, na.y, na.z, cap, g, t.keys, t.order, t.counters);
     c->launches++;
     ov_sort_keys(c, t, cap, s);
     k_cpl<<<nb, 256, 0, s>>>(t.keys, cap, t.counters, t.cpl, t.ncell_at);
-    c->launches++;
+    k_target_order<<<nb, 256, 0, s>>>(t.keys, t.order, cap, t.counters, t.torder);
+    c->launches += 2;
     ov_scan_exclusive(c, t.ncell_at, t.cell_off, cap, t.counters + TC_M, 1, t.scan_tmp, s);
     k_cells<<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, g, t.cells, t.parent, t.nchild, t.arrive,
                                t.cap_cells);

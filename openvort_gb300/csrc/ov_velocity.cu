@@ -35,6 +35,8 @@ struct VelArgs {
     Geometry geo;
     DevParams prm;
     double t;
+    const double *t_dev;    // when set, the time is t_dev[t_index] (graph-captured RK4)
+    int t_index;
     double f4pi;            // KAPPA/4/M_PI in the reference's rounding
     double grid_h, inv_h;   // mixed path
     float shift_g[OV_MAX_IMAGES][3], shift_f[OV_MAX_IMAGES][3];   // L*shift split on the grid
@@ -157,6 +159,8 @@ __global__ void k_tangents(VelArgs a, int cap, int *counters)
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) { T[ax][k] = tg[ax]; Nn[ax][k] = nm[ax]; }
 }
+
+__device__ __forceinline__ double now(const VelArgs &a) { return a.t_dev ? a.t_dev[a.t_index] : a.t; }
 
 // get_v (external_velocity.c:62-81)
 __device__ __forceinline__ void ext_vel(int type, const double dir[3], double s1, double s0, double tld,
@@ -281,7 +285,7 @@ __device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const doub
 {
     int st = a.status[id];
     if (st == OV_PINNED) {
-        ext_vel(a.prm.vb_type, a.prm.vb_dir, a.prm.vb_s1, a.prm.vb_s0, a.prm.vb_tld, a.t, vel_out);
+        ext_vel(a.prm.vb_type, a.prm.vb_dir, a.prm.vb_s1, a.prm.vb_s0, a.prm.vb_tld, now(a), vel_out);
         vs_out[0] = vs_out[1] = vs_out[2] = 0;
         return true;
     }
@@ -301,12 +305,12 @@ __device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const doub
                     rn_mul(rn_sub(rn_mul(tg[2], nm[0]), rn_mul(tg[0], nm[2])), f),
                     rn_mul(rn_sub(rn_mul(tg[0], nm[1]), rn_mul(tg[1], nm[0])), f)};
     double ev[3];
-    ext_vel(a.prm.vs_type, a.prm.vs_dir, a.prm.vs_s1, a.prm.vs_s0, a.prm.vs_tld, a.t, ev);
+    ext_vel(a.prm.vs_type, a.prm.vs_dir, a.prm.vs_s1, a.prm.vs_s0, a.prm.vs_tld, now(a), ev);
     for (int ax = 0; ax < 3; ++ax) vs[ax] = rn_add(rn_add(rn_add(vs[ax], ev[ax]), prim[ax]), img[ax]);
     double vel[3] = {vs[0], vs[1], vs[2]};
     if (a.prm.friction) {
         double vn[3];
-        ext_vel(a.prm.vn_type, a.prm.vn_dir, a.prm.vn_s1, a.prm.vn_s0, a.prm.vn_tld, a.t, vn);
+        ext_vel(a.prm.vn_type, a.prm.vn_dir, a.prm.vn_s1, a.prm.vn_s0, a.prm.vn_tld, now(a), vn);
         double dv[3] = {rn_sub(vn[0], vs[0]), rn_sub(vn[1], vs[1]), rn_sub(vn[2], vs[2])};
         double c1[3] = {rn_sub(rn_mul(tg[1], dv[2]), rn_mul(tg[2], dv[1])), rn_sub(rn_mul(tg[2], dv[0]), rn_mul(tg[0], dv[2])),
                         rn_sub(rn_mul(tg[0], dv[1]), rn_mul(tg[1], dv[0]))};
@@ -482,16 +486,19 @@ __global__ void k_direct_finish(VelArgs a, const int *__restrict__ nodes, int n,
 __global__ void k_euler(const int *__restrict__ status, const double *__restrict__ x, const double *__restrict__ y,
                         const double *__restrict__ z, const double *__restrict__ vx, const double *__restrict__ vy,
                         const double *__restrict__ vz, double dt, double *__restrict__ ox, double *__restrict__ oy,
-                        double *__restrict__ oz, int cap)
+                        double *__restrict__ oz, int cap, const double *dt_dev)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= cap || status[k] == OV_EMPTY) return;
+    if (dt_dev) dt = *dt_dev;
     ox[k] = rn_add(x[k], rn_mul(vx[k], dt));
     oy[k] = rn_add(y[k], rn_mul(vy[k], dt));
     oz[k] = rn_add(z[k], rn_mul(vz[k], dt));
 }
 
 struct Rk4Args {
+    const double *dt_dev;   // when set: the step, and the error word that vetoes the update
+    const int *err;
     const int *status;
     double *x, *y, *z;
     const double *v1x, *v1y, *v1z, *v2x, *v2y, *v2z, *v3x, *v3y, *v3z, *v4x, *v4y, *v4z;
@@ -504,7 +511,10 @@ __global__ void k_rk4_combine(Rk4Args r)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= r.cap || r.status[k] == OV_EMPTY) return;
-    double d6 = r.dt / 6, d3 = r.dt / 3;
+    // a stage whose tree did not fit its storage leaves the step undone
+    if (r.err && (*r.err & OV_EW_CELLS)) return;
+    double dt = r.dt_dev ? *r.dt_dev : r.dt;
+    double d6 = dt / 6, d3 = dt / 3;
     double *X[3] = {r.x, r.y, r.z};
     const double *V1[3] = {r.v1x, r.v1y, r.v1z}, *V2[3] = {r.v2x, r.v2y, r.v2z};
     const double *V3[3] = {r.v3x, r.v3y, r.v3z}, *V4[3] = {r.v4x, r.v4y, r.v4z};
@@ -604,10 +614,13 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
     const float th2 = a.th2f;
     const float near2 = a.near2f;
     const float f4pi = a.f4pif;
+    const float d2lo = 1e-16f * (1.0f - 1e-5f), d2hi = 1e-16f * (1.0f + 1e-5f);
     int c = 0;
     int resume = part ? 0 : 0x7fffffff;
     const int guard_max = 4 * ncell + 64;
     int steps = 0;
+    // plain FP32 sub-sums, folded into the Kahan sums every 16 warp steps
+    float p0 = 0, p1 = 0, p2 = 0;
     while (c < ncell) {
         if (c < 0) { bad_index(a, 1, c); break; }
         const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
@@ -618,43 +631,40 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
         bool open = false;
         if (c >= resume) {
             ++m.nvis;
-            float dx = (g[0] - A.x) + (f[0] - A.w);
-            float dy = (g[1] - A.y) + (f[1] - B.x);
-            float dz = (g[2] - A.z) + (f[2] - B.y);
-            float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float dx = (g[0] - A.x) + (f[0] - A.w);
+            const float dy = (g[1] - A.y) + (f[1] - B.x);
+            const float dz = (g[2] - A.z) + (f[2] - B.y);
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             const bool leaf = (nxt == c + 1);
-            // 1 skip, 2 accept, 0 open, -1 decide in FP64
-            int dec;
-            if (d2 < 1e-16f * (1.0f - 1e-5f)) dec = 1;
-            else if (d2 <= 1e-16f * (1.0f + 1e-5f)) dec = -1;
-            else if (leaf) dec = 2;
-            else {
-                float lm2 = Cc.y * Cc.y, b = th2 * d2;
-                dec = lm2 < b * (1.0f - 2e-5f) ? 2 : (lm2 > b * (1.0f + 2e-5f) ? 0 : -1);
-            }
-            bool use64 = dec < 0;
-            if (use64) {
+            const float lm2 = Cc.y * Cc.y, b = th2 * d2;
+            // decisions taken in FP32 only when clear of their thresholds
+            bool skip = d2 < d2lo;
+            bool acc = !skip && (leaf || lm2 < b * (1.0f - 2e-5f));
+            bool opn = !skip && !leaf && lm2 > b * (1.0f + 2e-5f);
+            bool exact = (!skip && d2 <= d2hi) || (!skip && !acc && !opn);
+            if (exact) {
                 // rare: inside a guard band, decided exactly as the FP64 path
                 ++m.nfb;
                 double q[3], dxyz[3], d64;
                 if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
                 else image_point(a.geo, j, p, q);
-                dec = decide64(a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
+                int dec = decide64(a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
+                skip = dec == 1;
+                acc = dec == 2;
             }
-            if (dec == 2) {
+            if (acc) {
                 ++m.nacc;
-                float R0 = -dx, R1 = -dy, R2 = -dz;
-                float qx = B.z, qy = B.w, qz = Cc.x;
-                float P0 = R0 + qx, P1 = R1 + qy, P2 = R2 + qz;
-                float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
-                float dot = fmaf(R0, P0, fmaf(R1, P1, R2 * P2));
-                float ra = rsqrtf(d2), rb = rsqrtf(lp2);
-                float ab = ra * rb;
-                float nd = dot * ab;
-                use64 = use64 || (leaf && d2 < near2) || fabsf(lp2 - 1e-16f) <= 1e-16f * 1e-5f ||
-                        fabsf(nd - 1e-8f) < 4e-6f;
-                if (use64) {
-                    // near field, or a filter inside its guard band: FP64, deferred
+                const float R0 = -dx, R1 = -dy, R2 = -dz;
+                const float qx = B.z, qy = B.w, qz = Cc.x;
+                const float P0 = R0 + qx, P1 = R1 + qy, P2 = R2 + qz;
+                const float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
+                const float dot = fmaf(R0, P0, fmaf(R1, P1, R2 * P2));
+                const float ra = rsqrtf(d2), rb = rsqrtf(lp2);
+                const float ab = ra * rb;
+                const float nd = dot * ab;
+                const bool defer = exact || (leaf && d2 < near2) || lp2 < d2hi || fabsf(nd - 1e-8f) < 4e-6f;
+                if (defer) {
+                    // near field, or a filter inside its guard band: FP64, after the traversal
                     ++m.nnear;
                     if (nnear < kNearCap) {
                         near_list[32 * nnear] = (c << 5) | (j + 1);
@@ -668,25 +678,33 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
                             w64[0] += w[0]; w64[1] += w[1]; w64[2] += w[2];
                         }
                     }
-                } else if (lp2 >= 1e-16f && nd >= 1e-8f) {
-                    float den = fmaf(dot, ab, 1.0f);
-                    float sc = __fdividef(f4pi * (ra + rb) * ab, den);
+                } else if (nd >= 1e-8f) {
+                    const float sc = __fdividef(f4pi * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
                     // R x Rp1 = R x q
-                    kahan_add(m.s0, m.c0, (R1 * qz - R2 * qy) * sc);
-                    kahan_add(m.s1, m.c1, (R2 * qx - R0 * qz) * sc);
-                    kahan_add(m.s2, m.c2, (R0 * qy - R1 * qx) * sc);
+                    p0 = fmaf(fmaf(R1, qz, -R2 * qy), sc, p0);
+                    p1 = fmaf(fmaf(R2, qx, -R0 * qz), sc, p1);
+                    p2 = fmaf(fmaf(R0, qy, -R1 * qx), sc, p2);
                 }
                 resume = nxt;
-            } else if (dec == 1) {
+            } else if (skip) {
                 resume = nxt;
             } else {
                 open = true;
             }
         }
         ++steps;
+        if ((steps & 15) == 0) {   // warp-uniform
+            kahan_add(m.s0, m.c0, p0);
+            kahan_add(m.s1, m.c1, p1);
+            kahan_add(m.s2, m.c2, p2);
+            p0 = p1 = p2 = 0;
+        }
         c = __any_sync(0xffffffffu, open) ? c + 1 : nxt;
         if (steps > guard_max) { overflow = true; break; }
     }
+    kahan_add(m.s0, m.c0, p0);
+    kahan_add(m.s1, m.c1, p1);
+    kahan_add(m.s2, m.c2, p2);
     m.nstep += steps;
 }
 
@@ -791,7 +809,7 @@ __global__ void __launch_bounds__(128) k_vel_mixed(VelArgs a, int G, double *__r
 VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long *stat)
 {
     VelArgs a;
-    a.order = c->tree.order;
+    a.order = c->tree.torder;
     a.counters = c->tree.counters;
     a.cells = c->tree.cells;
     a.cells32 = c->tree.cells32;
@@ -804,6 +822,8 @@ VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long 
     a.geo = c->geo;
     a.prm = ov_dev_params(c->params);
     a.t = t;
+    a.t_dev = nullptr;
+    a.t_index = 0;
     a.f4pi = c->params.kappa / 4 / M_PI;
     a.grid_h = c->grid_h;
     a.inv_h = c->grid_h > 0 ? 1.0 / c->grid_h : 0;
@@ -837,15 +857,12 @@ void ov_launch_tangents(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
 int ov_query_groups(ov_ctx *c)
 {
     int warps = (c->cap + 31) / 32;
-    int sms = 152;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    int G = (32 * sms + warps - 1) / warps;
+    int G = (32 * c->sm_count + warps - 1) / warps;
     return G < 1 ? 1 : (G > 8 ? 8 : G);
 }
 
-int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s)
+int ov_reserve_velocity_scratch(ov_ctx *c)
 {
-    VelArgs a = make_args(c, na, t, ov_stat_ptr(c));
     int G = ov_query_groups(c);
     size_t need = (size_t)G * 6 * (size_t)c->cap;
     if (c->part_cap < need) {
@@ -854,6 +871,19 @@ int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precisio
         OV_CUDA(c, cudaMalloc(&c->part, need * sizeof(double)));
         c->part_cap = need;
     }
+    return OV_OK;
+}
+
+int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s)
+{
+    VelArgs a = make_args(c, na, t, ov_stat_ptr(c));
+    if (c->time_dev_index >= 0) {
+        a.t_dev = c->d_time;
+        a.t_index = c->time_dev_index;
+    }
+    int G = ov_query_groups(c);
+    int r = ov_reserve_velocity_scratch(c);
+    if (r) return r;
     int warps = (c->cap + 31) / 32;
     int threads = 128;
     dim3 grid((warps * 32 + threads - 1) / threads, G);
@@ -917,6 +947,7 @@ extern "C" int ov_tree_velocity_at(ov_ctx *c, const double *points, int n, doubl
     if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
     cudaSetDevice(c->device);
     if (rebuild || !c->tree_built) {
+        OV_CUDA(c, cudaMemsetAsync(c->tree.counters + TC_ERR, 0, (TC_COUNT - TC_ERR) * 4, c->stream));
         int r = ov_tree_build(c, c->node, c->stream);
         if (r) return r;
         OV_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -978,14 +1009,17 @@ int ov_direct_raw(ov_ctx *c, const int *nodes, int n, double *sums_out)
 void ov_launch_euler(ov_ctx *c, const NodeArrays &src, const double *vx, const double *vy, const double *vz,
                      double dt, NodeArrays &dst, cudaStream_t s)
 {
+    const double *dt_dev = c->time_dev_index >= 0 ? c->d_time + 3 : nullptr;   // d_time[3] = dt/2
     k_euler<<<(c->cap + 255) / 256, 256, 0, s>>>(c->status, src.x, src.y, src.z, vx, vy, vz, dt, dst.x, dst.y,
-                                                 dst.z, c->cap);
+                                                 dst.z, c->cap, dt_dev);
     c->launches++;
 }
 
 void ov_launch_rk4_combine(ov_ctx *c, double dt, cudaStream_t s)
 {
     Rk4Args r;
+    r.dt_dev = c->time_dev_index >= 0 ? c->d_time + 4 : nullptr;   // d_time[4] = dt
+    r.err = c->tree.counters + TC_ERR;
     r.status = c->status;
     r.x = c->node.x; r.y = c->node.y; r.z = c->node.z;
     r.v1x = c->node.vx; r.v1y = c->node.vy; r.v1z = c->node.vz;

@@ -77,6 +77,7 @@ def load(path: str | None = None):
         "ov_set_phase_timing": (C.c_int, [P, C.c_int]),
         "ov_phase_times": (C.c_int, [P, C.POINTER(C.c_float)]),
         "ov_measure_fma_peak": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
+        "ov_set_rk4_graph": (C.c_int, [P, C.c_int]),
         "ov_tangle_info": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     }
     for name, (res, args) in sig.items():
@@ -139,6 +140,9 @@ class Context:
     def set_params(self, p: abi.Params):
         self.params = p
         self._check(self.lib.ov_set_params(self._h, C.byref(p)))
+
+    def set_rk4_graph(self, on: bool):
+        self._check(self.lib.ov_set_rk4_graph(self._h, int(on)))
 
     def set_precision(self, prec: int):
         self._check(self.lib.ov_set_precision(self._h, prec))

@@ -181,3 +181,22 @@ def test_all_empty_and_tiny_tangles():
     ht.stat[:, 0] = abi.OV_EMPTY
     st = _gpu_eval(ht, W.config_params("rw"))
     assert st["node_evals"] == 0 and st["cells"] == 0
+
+
+@pytest.mark.parametrize("prec", [abi.OV_PREC_FP64, abi.OV_PREC_MIXED])
+def test_rk4_graph_equals_stream_launches(prec):
+    """The captured RK4 graph gives bit-identical positions to launching the
+    same kernels one by one, over several steps (graph reused, times updated)."""
+    outs = []
+    for graph in (True, False):
+        ht = W.random_walk_tangle(12, 64, D=0.1, seed=34)
+        ctx = gpu.Context(0, params=W.config_params("rw"), precision=prec)
+        ctx.set_rk4_graph(graph)
+        ctx.upload(ht)
+        for s in range(3):
+            ctx.update_tangle(s * 5e-5)
+            ctx.rk4_step(s * 5e-5, 5e-5)
+        ctx.download(ht, abi.OV_F_POS)
+        ctx.close()
+        outs.append(np.array(ht.pos))
+    np.testing.assert_array_equal(outs[0], outs[1])
