@@ -189,6 +189,100 @@ def run_reference(args):
     return 0
 
 
+ENSEMBLE = dict(workload="ensemble of 48 independent random-walk tangles, 256-node loops, node counts "
+                         "log-uniform in [2048, 131072], D=0.1 cm, periodic_26, theta=0.4; per-member "
+                         "alpha~U(0.03,0.3), alpha'~U(0,0.02), v_n~U(0.2,2) x (seeded)",
+                n_tangles=48, min_nodes=2048, max_nodes=131072, per_loop=256, D=0.1, seed=11, dt=5e-5)
+
+
+def run_ensemble(args, device=0):
+    """The batching form: every member in one context, one persistent
+    traversal launch per evaluation, RK4 as one graph, topology passes per
+    member; mixed precision after the autotuner picked the launch shape."""
+    from openvort_gb300 import abi, gpu, workloads as W
+    E = ENSEMBLE
+    ms = W.ensemble(E["n_tangles"], E["min_nodes"], E["max_nodes"], E["per_loop"], D=E["D"], seed=E["seed"])
+    hosts = [m.tangle for m in ms]
+    params = [W.member_params(m) for m in ms]
+    n = sum(h.n for h in hosts)
+    ctx = gpu.Context(device, params=params[0], precision=abi.OV_PREC_FP64)
+    ctx.upload_ensemble(hosts, params, headroom=2.0)
+
+    def timed_evals(reps):
+        ts = []
+        for _ in range(reps):
+            ctx.flush_l2(256 << 20)
+            ctx.timer_start()
+            ctx.update_tangle(0.0)
+            ts.append(ctx.timer_stop())
+        return statistics.mean(ts)
+
+    # FP64 reference evaluation (same launch shape rules, untuned)
+    ctx.update_tangle(0.0)
+    fp64_ms = timed_evals(2)
+    ref = [ctx.download_member(i, W.HostTangle(h.pos.copy(), h.conn[:, 0].copy(), h.conn[:, 1].copy(),
+                                               h.box_lo, h.box_hi, n_images=h.n_images)).vels.copy()
+           for i, h in enumerate(hosts)]
+    # mixed precision, autotuned
+    ctx.set_precision(abi.OV_PREC_MIXED)
+    tune, tune_ms = ctx.autotune(0.0)
+    for _ in range(max(1, args.warmup)):
+        ctx.update_tangle(0.0)
+    l0 = ctx.kernel_launches
+    mixed_ms = timed_evals(max(3, args.steps))
+    launches_per_eval = (ctx.kernel_launches - l0 - max(3, args.steps)) / max(3, args.steps)
+    st = ctx.stats()
+    num = den = 0.0
+    for i, h in enumerate(hosts):
+        v = ctx.download_member(i, W.HostTangle(h.pos.copy(), h.conn[:, 0].copy(), h.conn[:, 1].copy(),
+                                                h.box_lo, h.box_hi, n_images=h.n_images)).vels
+        num += float(np.sum((v[:len(ref[i])] - ref[i]) ** 2))
+        den += float(np.sum(ref[i] ** 2))
+    # RK4 steps/s (update_tangle + rk4_step, all members in one graph)
+    dt = E["dt"]
+    for w in range(2):
+        ctx.update_tangle(w * dt)
+        ctx.rk4_step(w * dt, dt)
+    ts = []
+    for k in range(max(2, args.steps // 2)):
+        ctx.timer_start()
+        ctx.update_tangle(k * dt)
+        ctx.rk4_step(k * dt, dt)
+        ts.append(ctx.timer_stop())
+    rk4_ms = statistics.mean(ts)
+    # full time steps with reconnection and remeshing (host wall clock)
+    ctx.upload_ensemble(hosts, params, headroom=2.0)
+    K = args.ensemble_steps
+    recs = added = 0
+    t0 = time.perf_counter()
+    for k in range(K):
+        ctx.step(k * dt, dt)
+        s2 = ctx.stats()
+        recs += s2["reconnections"]
+        added += s2["remesh_added"]
+    ctx.synchronize()
+    full_ms = (time.perf_counter() - t0) * 1e3 / max(1, K)
+    n_end = sum(ctx.member_info(i)[0] - ctx.member_info(i)[2] for i in range(len(hosts)))
+    ctx.close()
+    return {
+        "config": E, "members": len(hosts), "nodes": n, "nodes_per_member_min_max": [min(h.n for h in hosts),
+                                                                                  max(h.n for h in hosts)],
+        "tuning": tune, "tuned_eval_ms": tune_ms,
+        "mixed": {"value": n / (mixed_ms * 1e-3), "unit": UNIT, "ms_per_eval": mixed_ms,
+                  "rel_l2_vs_fp64_tree": (num / den) ** 0.5 if den > 0 else None,
+                  "fp64_guard_band_decisions": st["fp64_fallbacks"], "fp64_near_field": st["near_field_fp64"],
+                  "kernel_launches_per_eval": launches_per_eval},
+        "fp64": {"value": n / (fp64_ms * 1e-3), "unit": UNIT, "ms_per_eval": fp64_ms},
+        "mixed_speedup_vs_fp64": fp64_ms / mixed_ms,
+        "rk4_mixed": {"steps_per_s": 1e3 / rk4_ms, "ms_per_step": rk4_ms,
+                      "node_evals_per_s": 4 * n / (rk4_ms * 1e-3)},
+        "full_steps_mixed": {"steps": K, "ms_per_step_wall": full_ms, "steps_per_s": 1e3 / full_ms,
+                             "reconnections": recs, "remesh_added": added, "live_nodes_end": n_end,
+                             "includes": "small loops x3, reconnect, periodic wrap, remesh, update_tangle, "
+                                         "rk4_step (graph), per step; host wall clock"},
+    }
+
+
 def run_ours(args):
     from openvort_gb300 import abi, gpu
     world, rank, local, dist = dist_setup()
@@ -290,6 +384,12 @@ def run_ours(args):
         rk4[name] = {"steps_per_s": 1e3 / statistics.mean(ts), "ms_per_step": statistics.mean(ts),
                      "node_evals_per_s": 4 * n / (statistics.mean(ts) * 1e-3)}
     ctx.set_precision(abi.OV_PREC_FP64)
+    ensemble = None
+    if world == 1 and args.ensemble_steps >= 0:
+        try:
+            ensemble = run_ensemble(args, device)
+        except Exception as e:
+            ensemble = {"error": str(e)[:300]}
     clk.__exit__(None, None, None)
 
     # ---- CPU baseline (rank 0 only, bounded sample)
@@ -322,6 +422,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h},
         "mixed": mixed,
         "rk4": rk4,
+        "ensemble": ensemble,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "peaks_source": peak_src,
@@ -336,6 +437,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ensemble-steps", type=int, default=10,
+                    help="full time steps of the 48-tangle ensemble (-1: skip the ensemble section)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

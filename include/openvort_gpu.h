@@ -149,6 +149,46 @@ int ov_tangle_info(const ov_ctx *ctx, int *n_slots, int *next_empty, int *total_
    transfers positions and topology as well. */
 int ov_upload_tangle_fields(ov_ctx *ctx, const ov_tangle_state *t, unsigned fields);
 
+/* ----------------------------------------------------------- ensembles */
+/* An ensemble of independent tangles held by one context.  Every entry
+   point of this header then acts on all members at once: one tree per
+   member built in the same launches, one persistent traversal launch over a
+   (member, node tile) work queue, RK4 as one graph for all members, and the
+   topology passes member by member in the reference's order.  Members share
+   the box and image set and KAPPA, BH_resolution and use_BH (OV_ERR_ARG
+   otherwise); every other parameter is per member.  Member i keeps its own
+   slot range of ceil(N_i * headroom) slots (headroom >= 1; 2 leaves room
+   for one doubling by expand_tangle without moving the other members), so
+   its slot indices, next_empty and total_empty are those of the member's
+   own tangle_state.  ov_upload_tangle makes a one-member context. */
+int ov_upload_ensemble(ov_ctx *ctx, const ov_tangle_state *const *tangles, const ov_params *params, int n,
+                       double headroom);
+int ov_ensemble_size(const ov_ctx *ctx);
+/* tangle_state N / next_empty / total_empty of member i */
+int ov_member_info(const ov_ctx *ctx, int i, int *n_slots, int *next_empty, int *total_empty);
+/* ov_download_tangle for member i (t->N must be >= the member's N) */
+int ov_download_member(ov_ctx *ctx, int i, ov_tangle_state *t, unsigned fields);
+/* per-member parameters (the shared ones must keep their values) */
+int ov_set_member_params(ov_ctx *ctx, int i, const ov_params *p);
+
+/* Launch shape of the traversal: warps per block (2, 4 or 8), query groups
+   per node (1-27; 0 = from the node count), persistent blocks per SM (0 =
+   the occupancy limit) and the order of the work queue (largest member
+   first or member order).  Results do not depend on it. */
+typedef struct ov_tuning {
+    int warps_per_block;
+    int query_groups;
+    int blocks_per_sm;
+    int largest_first;
+} ov_tuning;
+int ov_get_tuning(const ov_ctx *ctx, ov_tuning *out);
+int ov_set_tuning(ov_ctx *ctx, const ov_tuning *tu);
+/* Time the velocity evaluation of the resident tangle(s) at time t over
+   candidate launch shapes (context precision), keep the fastest, and return
+   it in *best with its time in *ms_best (either may be NULL).  The
+   context's velocities are overwritten. */
+int ov_autotune(ov_ctx *ctx, double t, ov_tuning *best, float *ms_best);
+
 /* ------------------------------------------------------- velocity path */
 /* Tangents and normals of every node: update_tangents_normals (tangle.c:509). */
 int ov_update_tangents_normals(ov_ctx *ctx);

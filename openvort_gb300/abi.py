@@ -82,6 +82,12 @@ class Stats(C.Structure):
         "small_loops_removed", "error_word")]
 
 
+class Tuning(C.Structure):
+    """ov_tuning: launch shape of the traversal."""
+    _fields_ = [("warps_per_block", C.c_int), ("query_groups", C.c_int), ("blocks_per_sm", C.c_int),
+                ("largest_first", C.c_int)]
+
+
 assert C.sizeof(TangleState) == 168 and C.sizeof(DomainBox) == 72 and C.sizeof(ExtVel) == 56
 
 

@@ -49,6 +49,7 @@ DevParams ov_dev_params(const ov_params &p)
     d.theta = p.bh_resolution;
     d.friction = p.use_mutual_friction;
     d.use_bh = p.use_bh;
+    d.rec_dist = p.rec_dist;
     const ov_ext_vel *src[3] = {&p.vn, &p.vs, &p.vb};
     int *types[3] = {&d.vn_type, &d.vs_type, &d.vb_type};
     double *dirs[3] = {d.vn_dir, d.vs_dir, d.vb_dir};
@@ -133,8 +134,13 @@ int ov_ctx_destroy(ov_ctx *c)
     free_nodes(c->node);
     for (auto &s : c->stage) free_nodes(s);
     ov_tree_free(c->tree);
-    int *is[] = {c->fwd, c->rev, c->status, c->pin, c->dnodes};
+    int *is[] = {c->fwd, c->rev, c->status, c->pin, c->dnodes, c->d_tid, c->d_qorder};
     for (int *p : is)
+        if (p) cudaFree(p);
+    if (c->d_tprm) cudaFree(c->d_tprm);
+    if (c->d_mrange) cudaFree(c->d_mrange);
+    void *scratch[] = {c->d_pairs, c->d_npairs, c->d_loop_off, c->d_loop_nodes, c->d_loop_buf, c->d_loop_cut};
+    for (void *p : scratch)
         if (p) cudaFree(p);
     if (c->dsum) cudaFree(c->dsum);
     if (c->part) cudaFree(c->part);
@@ -158,6 +164,8 @@ int ov_set_params(ov_ctx *c, const ov_params *p)
 {
     if (!c || !p) return OV_ERR_ARG;
     c->params = *p;
+    for (Member &m : c->mem) m.params = *p;   // an ensemble: every member
+    if (c->mem.size() > 1 && c->d_tprm) return ov_upload_member_tables(c);
     return OV_OK;
 }
 
@@ -182,9 +190,49 @@ int ov_capacity(const ov_ctx *c) { return c ? c->cap : 0; }
 int ov_tangle_info(const ov_ctx *c, int *n_slots, int *next_empty, int *total_empty)
 {
     if (!c) return OV_ERR_ARG;
+    if (c->mem.size() == 1) return ov_member_info(c, 0, n_slots, next_empty, total_empty);
+    // an ensemble: the whole pool
+    int te = 0;
+    for (const Member &m : c->mem) te += m.total_empty + (m.cap - m.n);
     if (n_slots) *n_slots = c->n_live;
-    if (next_empty) *next_empty = c->next_empty;
-    if (total_empty) *total_empty = c->total_empty;
+    if (next_empty) *next_empty = -1;
+    if (total_empty) *total_empty = te;
+    return OV_OK;
+}
+
+int ov_member_info(const ov_ctx *c, int i, int *n_slots, int *next_empty, int *total_empty)
+{
+    if (!c || i < 0 || i >= (int)c->mem.size()) return OV_ERR_ARG;
+    const Member &m = c->mem[i];
+    if (n_slots) *n_slots = m.n;
+    if (next_empty) *next_empty = m.next_empty;
+    if (total_empty) *total_empty = m.total_empty;
+    return OV_OK;
+}
+
+int ov_ensemble_size(const ov_ctx *c) { return c ? (int)c->mem.size() : 0; }
+
+int ov_get_tuning(const ov_ctx *c, ov_tuning *out)
+{
+    if (!c || !out) return OV_ERR_ARG;
+    out->warps_per_block = c->tune.warps;
+    out->query_groups = c->tune.groups;
+    out->blocks_per_sm = c->tune.blocks_per_sm;
+    out->largest_first = c->tune.largest_first;
+    return OV_OK;
+}
+
+int ov_set_tuning(ov_ctx *c, const ov_tuning *tu)
+{
+    if (!c || !tu) return OV_ERR_ARG;
+    if ((tu->warps_per_block != 2 && tu->warps_per_block != 4 && tu->warps_per_block != 8) ||
+        tu->query_groups < 0 || tu->query_groups > 27 || tu->blocks_per_sm < 0 || tu->blocks_per_sm > 64)
+        return ov_fail(c, OV_ERR_ARG, "tuning out of range");
+    c->tune.warps = tu->warps_per_block;
+    c->tune.groups = tu->query_groups;
+    c->tune.blocks_per_sm = tu->blocks_per_sm;
+    c->tune.largest_first = tu->largest_first != 0;
+    if (c->uploaded && c->mem.size() > 1) return ov_upload_member_tables(c);
     return OV_OK;
 }
 
@@ -302,7 +350,192 @@ static void set_geometry(ov_ctx *c, const ov_domain_box &box, const ov_boundary_
     c->grid_h = ldexp(1.0, e - 22);
 }
 
+// Per-member device tables: build table, parameters, queue order, slot
+// ranges, and (ensembles) the member of every slot.
+int ov_reserve_members(ov_ctx *c, int nt)
+{
+    nt = std::max(nt, 1);
+    if (c->tree.tt && c->tcap >= nt) return OV_OK;
+    if (c->tree.tt) cudaFree(c->tree.tt);
+    if (c->d_tprm) cudaFree(c->d_tprm);
+    if (c->d_qorder) cudaFree(c->d_qorder);
+    if (c->d_mrange) cudaFree(c->d_mrange);
+    c->tree.tt = nullptr; c->d_tprm = nullptr; c->d_qorder = nullptr; c->d_mrange = nullptr;
+    c->tcap = 0;
+    OV_CUDA(c, cudaMalloc(&c->tree.tt, (size_t)nt * TT_WORDS * 4));
+    OV_CUDA(c, cudaMemset(c->tree.tt, 0, (size_t)nt * TT_WORDS * 4));
+    OV_CUDA(c, cudaMalloc(&c->d_tprm, (size_t)nt * sizeof(DevParams)));
+    OV_CUDA(c, cudaMalloc(&c->d_qorder, (size_t)nt * 4));
+    OV_CUDA(c, cudaMalloc(&c->d_mrange, (size_t)nt * sizeof(int2)));
+    c->tcap = nt;
+    return OV_OK;
+}
+
+int ov_upload_member_tables(ov_ctx *c)
+{
+    const int nt = (int)c->mem.size();
+    int r;
+    if ((r = ov_reserve_members(c, nt))) return r;
+    c->key_tbits = 0;
+    while ((1 << c->key_tbits) < nt) ++c->key_tbits;
+    c->key_levels = std::min(OV_MAX_LEVEL, (63 - c->key_tbits) / 3);
+    c->rk4_key = 0;   // the graph bakes the layout in
+    std::vector<DevParams> prm(nt);
+    std::vector<int> q(nt);
+    std::vector<int2> rng(nt);
+    for (int i = 0; i < nt; ++i) {
+        prm[i] = ov_dev_params(c->mem[i].params);
+        q[i] = i;
+        rng[i] = make_int2(c->mem[i].lo, c->mem[i].lo + c->mem[i].cap);
+    }
+    if (c->tune.largest_first)
+        std::stable_sort(q.begin(), q.end(), [&](int a, int b) { return c->mem[a].n > c->mem[b].n; });
+    OV_CUDA(c, cudaMemcpy(c->d_tprm, prm.data(), nt * sizeof(DevParams), cudaMemcpyHostToDevice));
+    OV_CUDA(c, cudaMemcpy(c->d_qorder, q.data(), nt * 4, cudaMemcpyHostToDevice));
+    OV_CUDA(c, cudaMemcpy(c->d_mrange, rng.data(), nt * sizeof(int2), cudaMemcpyHostToDevice));
+    if (nt > 1) {
+        if (c->d_tid) cudaFree(c->d_tid);
+        c->d_tid = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->d_tid, (size_t)std::max(c->cap, 1) * 4));
+        std::vector<int> tid(std::max(c->cap, 1), 0);
+        for (int i = 0; i < nt; ++i)
+            for (int k = 0; k < c->mem[i].cap; ++k) tid[c->mem[i].lo + k] = i;
+        OV_CUDA(c, cudaMemcpy(c->d_tid, tid.data(), tid.size() * 4, cudaMemcpyHostToDevice));
+    }
+    return OV_OK;
+}
+
+// Move the per-slot device arrays that have no host mirror (tangents,
+// normals, vels, vs) from the member layout `old` to the context's current
+// one (the context already holds enough slots).
+int ov_move_device_slots(ov_ctx *c, const std::vector<Member> &old)
+{
+    size_t n = (size_t)std::max(c->n_live, 1);
+    double *tmp = nullptr;
+    OV_CUDA(c, cudaMalloc(&tmp, n * sizeof(double)));
+    double *arrs[12] = {c->node.tx, c->node.ty, c->node.tz, c->node.nx, c->node.ny, c->node.nz,
+                        c->node.vx, c->node.vy, c->node.vz, c->node.sx, c->node.sy, c->node.sz};
+    int r = OV_OK;
+    for (double *arr : arrs) {
+        if (cudaMemsetAsync(tmp, 0, n * sizeof(double), c->stream) != cudaSuccess) { r = OV_ERR_CUDA; break; }
+        for (size_t i = 0; i < old.size() && i < c->mem.size(); ++i) {
+            size_t len = (size_t)std::min(old[i].cap, c->mem[i].cap);
+            if (len && cudaMemcpyAsync(tmp + c->mem[i].lo, arr + old[i].lo, len * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+                r = OV_ERR_CUDA;
+        }
+        if (cudaMemcpyAsync(arr, tmp, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+            r = OV_ERR_CUDA;
+    }
+    cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    if (r) return ov_fail(c, r, "moving member slots failed");
+    return OV_OK;
+}
+
 extern "C" {
+
+int ov_upload_ensemble(ov_ctx *c, const ov_tangle_state *const *ts, const ov_params *params, int n,
+                       double headroom)
+{
+    if (!c || !ts || !params || n < 1 || !(headroom >= 1.0 && headroom <= 64.0)) return OV_ERR_ARG;
+    cudaSetDevice(c->device);
+    for (int i = 0; i < n; ++i) {
+        const ov_tangle_state *t = ts[i];
+        if (!t || t->N < 0) return ov_fail(c, OV_ERR_ARG, "member %d: no tangle", i);
+        if (memcmp(&t->box, &ts[0]->box, sizeof t->box) != 0 || t->bimg.n != ts[0]->bimg.n)
+            return ov_fail(c, OV_ERR_ARG, "member %d: box or image set differs from member 0", i);
+        for (int j = 0; j < t->bimg.n; ++j)
+            if (!t->bimg.images || !ts[0]->bimg.images ||
+                memcmp(&t->bimg.images[j], &ts[0]->bimg.images[j], sizeof(ov_image_tangle)) != 0)
+                return ov_fail(c, OV_ERR_ARG, "member %d: image %d differs from member 0", i, j);
+        const ov_params &p = params[i], &p0 = params[0];
+        if (p.kappa != p0.kappa || p.bh_resolution != p0.bh_resolution || p.use_bh != p0.use_bh)
+            return ov_fail(c, OV_ERR_ARG, "member %d: KAPPA, BH_resolution and use_BH must be shared", i);
+    }
+    std::vector<Member> mem(n);
+    long long lo = 0;
+    for (int i = 0; i < n; ++i) {
+        Member &m = mem[i];
+        m.lo = (int)lo;
+        m.n = ts[i]->N;
+        m.cap = std::max(m.n, (int)std::min(ceil((double)m.n * headroom), 1e9));
+        m.next_empty = ts[i]->next_empty;
+        m.total_empty = ts[i]->total_empty;
+        m.params = params[i];
+        lo += m.cap;
+        if (lo > (1LL << 30)) return ov_fail(c, OV_ERR_ARG, "ensemble of more than 2^30 slots");
+    }
+    int r;
+    for (int i = 0; i < n; ++i) {
+        const ov_tangle_state *t = ts[i];
+        for (int k = 0; k < t->N; ++k) {
+            int f = t->connections[k].forward, b = t->connections[k].reverse, st = t->status[k].status;
+            if (f < -1 || f >= t->N || b < -1 || b >= t->N || st < OV_EMPTY || st > OV_PINNED_SLIP)
+                return ov_fail(c, OV_ERR_TOPOLOGY, "member %d node %d: connections (%d,%d) / status %d out of range",
+                               i, k, f, b, st);
+        }
+    }
+    const int total = (int)lo;
+    if ((r = ensure_capacity(c, std::max(total, 1)))) return r;
+    c->mem = mem;
+    c->n_live = total;
+    c->params = params[0];
+    c->tree_built = false;
+    c->host_valid = false;
+    set_geometry(c, ts[0]->box, ts[0]->bimg);
+    if ((r = ov_upload_member_tables(c))) return r;
+    size_t cap = (size_t)c->cap;
+    if ((r = ensure_stage(c, cap * 3 * sizeof(double) * 5 + cap * 4 * sizeof(int)))) return r;
+    double *h = c->h_stage;
+    int *hi = (int *)(h + 15 * cap);
+    std::fill(h, h + 15 * cap, 0.0);
+    std::fill(hi, hi + 2 * cap, -1);
+    std::fill(hi + 2 * cap, hi + 3 * cap, (int)OV_EMPTY);
+    std::fill(hi + 3 * cap, hi + 4 * cap, (int)OV_NOT_A_FACE);
+    for (int i = 0; i < n; ++i) {
+        const ov_tangle_state *t = ts[i];
+        const size_t o = (size_t)mem[i].lo;
+        const ov_vec3 *src[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
+        for (int f = 0; f < 5; ++f) {
+            if (!src[f]) continue;
+            double *dst = h + 3 * cap * f;
+            for (int a = 0; a < 3; ++a)
+                for (int k = 0; k < t->N; ++k) dst[a * cap + o + k] = src[f][k].p[a];
+        }
+        for (int k = 0; k < t->N; ++k) {
+            int f = t->connections[k].forward, b = t->connections[k].reverse;
+            hi[o + k] = f >= 0 ? f + (int)o : -1;
+            hi[cap + o + k] = b >= 0 ? b + (int)o : -1;
+            hi[2 * cap + o + k] = t->status[k].status;
+            hi[3 * cap + o + k] = t->status[k].pin_wall;
+        }
+    }
+    double *dd[15] = {c->node.x, c->node.y, c->node.z, c->node.vx, c->node.vy, c->node.vz,
+                      c->node.sx, c->node.sy, c->node.sz, c->node.tx, c->node.ty, c->node.tz,
+                      c->node.nx, c->node.ny, c->node.nz};
+    for (int k = 0; k < 15; ++k)
+        OV_CUDA(c, cudaMemcpyAsync(dd[k], h + k * cap, cap * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    int *di[4] = {c->fwd, c->rev, c->status, c->pin};
+    for (int i = 0; i < 4; ++i)
+        OV_CUDA(c, cudaMemcpyAsync(di[i], hi + i * cap, cap * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    c->last_h2d = cap * (15 * sizeof(double) + 4 * sizeof(int));
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->uploaded = true;
+    return OV_OK;
+}
+
+int ov_set_member_params(ov_ctx *c, int i, const ov_params *p)
+{
+    if (!c || !p || i < 0 || i >= (int)c->mem.size()) return OV_ERR_ARG;
+    const ov_params &p0 = c->params;
+    if (c->mem.size() > 1 && (p->kappa != p0.kappa || p->bh_resolution != p0.bh_resolution || p->use_bh != p0.use_bh))
+        return ov_fail(c, OV_ERR_ARG, "KAPPA, BH_resolution and use_BH are shared by the members");
+    c->mem[i].params = *p;
+    if (c->mem.size() == 1) c->params = *p;
+    if (c->uploaded && c->mem.size() > 1) return ov_upload_member_tables(c);
+    return OV_OK;
+}
 
 int ov_upload_tangle(ov_ctx *c, const ov_tangle_state *t) { return ov_upload_tangle_fields(c, t, OV_F_ALL); }
 
@@ -314,12 +547,21 @@ int ov_upload_tangle_fields(ov_ctx *c, const ov_tangle_state *t, unsigned fields
     int r;
     int old_cap = c->cap;
     if ((r = ensure_capacity(c, std::max(n, 1)))) return r;
-    if (!c->uploaded || c->cap != old_cap || c->n_live != n) fields |= OV_F_POS | OV_F_TOPOLOGY;
+    if (!c->uploaded || c->cap != old_cap || c->n_live != n || c->mem.size() != 1)
+        fields |= OV_F_POS | OV_F_TOPOLOGY;
     c->n_live = n;   // slots past t->N (a smaller tangle in a larger context) are EMPTY
     c->tree_built = false;
-    c->next_empty = t->next_empty;
-    c->total_empty = t->total_empty;
+    c->host_valid = false;
+    if (c->mem.size() != 1) c->mem.assign(1, Member{});
+    Member &m0 = c->mem[0];
+    m0.lo = 0;
+    m0.n = n;
+    m0.cap = n;
+    m0.next_empty = t->next_empty;
+    m0.total_empty = t->total_empty;
+    m0.params = c->params;
     set_geometry(c, t->box, t->bimg);
+    if ((r = ov_upload_member_tables(c))) return r;
     size_t cap = (size_t)c->cap;
     if ((r = ensure_stage(c, cap * 3 * sizeof(double) * 5 + cap * 4 * sizeof(int)))) return r;
     double *h = c->h_stage;
@@ -364,52 +606,83 @@ int ov_upload_tangle_fields(ov_ctx *c, const ov_tangle_state *t, unsigned fields
     return OV_OK;
 }
 
-int ov_download_tangle(ov_ctx *c, ov_tangle_state *t, unsigned fields)
+// Copy slots [lo, lo + span) of the device pool into host tangle slots
+// [0, min(span, t->N)), connections shifted by -lo; host slots past span
+// become EMPTY.
+static int download_range(ov_ctx *c, ov_tangle_state *t, unsigned fields, int lo, int span, int next_empty,
+                          int total_empty)
 {
-    if (!c || !t) return OV_ERR_ARG;
-    if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
-    if (t->N < c->n_live)
-        return ov_fail(c, OV_ERR_ARG, "host tangle has %d slots, the context holds %d (expand it first)", t->N,
-                       c->n_live);
-    int n = std::min(t->N, c->cap);
-    size_t cap = (size_t)c->cap;
+    const int n = std::min(t->N, span);
+    const size_t m = (size_t)std::max(n, 1);
     int r;
-    if ((r = ensure_stage(c, cap * 3 * sizeof(double) * 5 + cap * 4 * sizeof(int)))) return r;
+    if ((r = ensure_stage(c, m * 3 * sizeof(double) * 5 + m * 4 * sizeof(int)))) return r;
     double *h = c->h_stage;
-    int *hi = (int *)(h + 15 * cap);
+    int *hi = (int *)(h + 15 * m);
     const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
     double *dd[15] = {c->node.x, c->node.y, c->node.z, c->node.vx, c->node.vy, c->node.vz,
                       c->node.sx, c->node.sy, c->node.sz, c->node.tx, c->node.ty, c->node.tz,
                       c->node.nx, c->node.ny, c->node.nz};
-    for (int f = 0; f < 5; ++f) {
-        if (!(fields & bits[f])) continue;
-        for (int a = 0; a < 3; ++a)
-            OV_CUDA(c, cudaMemcpyAsync(h + (3 * f + a) * cap, dd[3 * f + a], cap * sizeof(double),
-                                       cudaMemcpyDeviceToHost, c->stream));
+    if (n > 0) {
+        for (int f = 0; f < 5; ++f) {
+            if (!(fields & bits[f])) continue;
+            for (int a = 0; a < 3; ++a)
+                OV_CUDA(c, cudaMemcpyAsync(h + (3 * f + a) * m, dd[3 * f + a] + lo, (size_t)n * sizeof(double),
+                                           cudaMemcpyDeviceToHost, c->stream));
+        }
+        int *di[4] = {c->fwd, c->rev, c->status, c->pin};
+        if (fields & OV_F_TOPOLOGY)
+            for (int i = 0; i < 4; ++i)
+                OV_CUDA(c, cudaMemcpyAsync(hi + i * m, di[i] + lo, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost,
+                                           c->stream));
+        OV_CUDA(c, cudaStreamSynchronize(c->stream));
     }
-    int *di[4] = {c->fwd, c->rev, c->status, c->pin};
-    if (fields & OV_F_TOPOLOGY)
-        for (int i = 0; i < 4; ++i)
-            OV_CUDA(c, cudaMemcpyAsync(hi + i * cap, di[i], cap * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    OV_CUDA(c, cudaStreamSynchronize(c->stream));
     ov_vec3 *dst[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
     for (int f = 0; f < 5; ++f) {
         if (!(fields & bits[f]) || !dst[f]) continue;
-        const double *s = h + 3 * cap * f;
+        const double *s = h + 3 * m * f;
         for (int k = 0; k < n; ++k)
-            for (int a = 0; a < 3; ++a) dst[f][k].p[a] = s[a * cap + k];
+            for (int a = 0; a < 3; ++a) dst[f][k].p[a] = s[a * m + k];
+        for (int k = n; k < t->N; ++k)
+            for (int a = 0; a < 3; ++a) dst[f][k].p[a] = 0.0;
     }
     if (fields & OV_F_TOPOLOGY) {
-        t->next_empty = c->next_empty;
-        t->total_empty = c->total_empty + (t->N - c->n_live);
+        t->next_empty = next_empty;
+        t->total_empty = total_empty;
         for (int k = 0; k < n; ++k) {
-            t->connections[k].forward = hi[k];
-            t->connections[k].reverse = hi[cap + k];
-            t->status[k].status = hi[2 * cap + k];
-            t->status[k].pin_wall = hi[3 * cap + k];
+            int f = hi[k], b = hi[m + k];
+            t->connections[k].forward = f >= 0 ? f - lo : -1;
+            t->connections[k].reverse = b >= 0 ? b - lo : -1;
+            t->status[k].status = hi[2 * m + k];
+            t->status[k].pin_wall = hi[3 * m + k];
+        }
+        for (int k = n; k < t->N; ++k) {
+            t->connections[k].forward = t->connections[k].reverse = -1;
+            t->status[k].status = OV_EMPTY;
+            t->status[k].pin_wall = OV_NOT_A_FACE;
         }
     }
     return OV_OK;
+}
+
+int ov_download_member(ov_ctx *c, int i, ov_tangle_state *t, unsigned fields)
+{
+    if (!c || !t || i < 0 || i >= (int)c->mem.size()) return OV_ERR_ARG;
+    if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
+    cudaSetDevice(c->device);
+    const Member &m = c->mem[i];
+    if (t->N < m.n)
+        return ov_fail(c, OV_ERR_ARG, "host tangle has %d slots, member %d holds %d (expand it first)", t->N, i, m.n);
+    // slots of the host tangle past the member's N are EMPTY
+    const int span = c->mem.size() == 1 ? c->cap : m.cap;
+    return download_range(c, t, fields, m.lo, span, m.next_empty, m.total_empty + (t->N - m.n));
+}
+
+int ov_download_tangle(ov_ctx *c, ov_tangle_state *t, unsigned fields)
+{
+    if (!c || !t) return OV_ERR_ARG;
+    if (c->mem.size() > 1)
+        return ov_fail(c, OV_ERR_STATE, "the context holds an ensemble: use ov_download_member");
+    return ov_download_member(c, 0, t, fields);
 }
 
 }  // extern "C"
@@ -562,8 +835,14 @@ static unsigned long long graph_key(ov_ctx *c)
     unsigned long long h = 1469598103934665603ull;
     h = mix64(h, &c->params, sizeof c->params);
     h = mix64(h, &c->geo, sizeof c->geo);
-    int ints[4] = {c->cap, c->tree.cap_cells, c->precision, 0};
+    int ints[8] = {c->cap, c->tree.cap_cells, c->precision, (int)c->mem.size(), c->tune.warps, c->tune.groups,
+                   c->tune.blocks_per_sm, c->tune.largest_first};
     h = mix64(h, ints, sizeof ints);
+    for (const Member &m : c->mem) {
+        int lay[3] = {m.lo, m.n, m.cap};
+        h = mix64(h, lay, sizeof lay);
+        h = mix64(h, &m.params, sizeof m.params);
+    }
     const void *ptrs[4] = {c->node.x, c->tree.cells, c->part, c->d_time};
     h = mix64(h, ptrs, sizeof ptrs);
     return h;
@@ -573,6 +852,7 @@ int ov_rk4_step(ov_ctx *c, double t, double dt)
 {
     int r = check_ready(c);
     if (r) return r;
+    c->host_valid = false;
     cudaStream_t s = c->stream;
     if (!c->d_time) {
         OV_CUDA(c, cudaMalloc(&c->d_time, 8 * sizeof(double)));
@@ -625,6 +905,81 @@ int ov_rk4_step(ov_ctx *c, double t, double dt)
     return ov_fail(c, OV_ERR_ALLOC, "cell storage could not be sized");
 }
 
+// Device time of one velocity evaluation (tree + traversal) with the
+// context's current tuning: best of `reps` after one warm-up.
+static int time_eval(ov_ctx *c, double t, int reps, float *ms)
+{
+    int r;
+    if ((r = ov_reserve_velocity_scratch(c))) return r;
+    if ((r = ov_eval_sync(c, c->node, t, false))) return r;
+    float best = 1e30f;
+    for (int i = 0; i < reps; ++i) {
+        if ((r = clear_call_words(c))) return r;
+        OV_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+        if ((r = eval_async(c, c->node, t, false, c->stream))) return r;
+        OV_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+        OV_CUDA(c, cudaEventSynchronize(c->ev1));
+        float m = 0;
+        OV_CUDA(c, cudaEventElapsedTime(&m, c->ev0, c->ev1));
+        best = std::min(best, m);
+        if ((r = collect_stats(c, false))) return r;
+        if ((r = error_from_word(c))) return r;
+    }
+    *ms = best;
+    return OV_OK;
+}
+
+int ov_autotune(ov_ctx *c, double t, ov_tuning *best_out, float *ms_best)
+{
+    int r = check_ready(c);
+    if (r) return r;
+    const Tuning saved = c->tune;
+    Tuning best = c->tune;
+    best.groups = ov_query_groups(c);   // resolve the default
+    float best_ms = 1e30f;
+    auto trial = [&](const Tuning &tu, float *ms) -> int {
+        c->tune = tu;
+        int rr;
+        if (c->mem.size() > 1 && (rr = ov_upload_member_tables(c))) return rr;
+        return time_eval(c, t, 3, ms);
+    };
+    if ((r = trial(best, &best_ms))) { c->tune = saved; return r; }
+    // coordinate descent: block shape, query groups, blocks per SM, queue order
+    const int maxg = std::min(c->geo.n_img + 1, 27);
+    const int warps[3] = {2, 4, 8};
+    const int groups[8] = {1, 2, 3, 4, 6, 9, 14, 27};
+    for (int stage = 0; stage < 4; ++stage) {
+        std::vector<Tuning> cand;
+        if (stage == 0)
+            for (int w : warps) { Tuning tu = best; tu.warps = w; cand.push_back(tu); }
+        if (stage == 1)
+            for (int g : groups)
+                if (g <= maxg) { Tuning tu = best; tu.groups = g; cand.push_back(tu); }
+        if (stage == 2) {
+            int occ = 0;
+            ov_traversal_blocks(c, c->precision, best.warps, &occ);
+            for (int b : {0, occ - 1, (occ + 1) / 2})
+                if (b >= 0) { Tuning tu = best; tu.blocks_per_sm = b; cand.push_back(tu); }
+        }
+        if (stage == 3 && c->mem.size() > 1)
+            for (int lf : {1, 0}) { Tuning tu = best; tu.largest_first = lf; cand.push_back(tu); }
+        for (const Tuning &tu : cand) {
+            if (tu.warps == best.warps && tu.groups == best.groups && tu.blocks_per_sm == best.blocks_per_sm &&
+                tu.largest_first == best.largest_first)
+                continue;
+            float ms = 0;
+            if ((r = trial(tu, &ms))) { c->tune = saved; if (c->mem.size() > 1) ov_upload_member_tables(c); return r; }
+            if (ms < best_ms * 0.99f) { best_ms = ms; best = tu; }
+        }
+    }
+    c->tune = best;
+    if (c->mem.size() > 1 && (r = ov_upload_member_tables(c))) return r;
+    if ((r = ov_reserve_velocity_scratch(c))) return r;
+    if (best_out) ov_get_tuning(c, best_out);
+    if (ms_best) *ms_best = best_ms;
+    return OV_OK;
+}
+
 int ov_direct_velocities(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out)
 {
     int r = check_ready(c);
@@ -640,6 +995,7 @@ int ov_enforce_periodic_boundaries(ov_ctx *c)
     int r = check_ready(c);
     if (r) return r;
     c->tree_built = false;
+    c->host_valid = false;
     ov_launch_periodic_wrap(c, c->stream);
     OV_CUDA(c, cudaGetLastError());
     OV_CUDA(c, cudaStreamSynchronize(c->stream));

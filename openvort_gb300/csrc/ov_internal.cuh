@@ -54,8 +54,20 @@ struct Cell32 {          // 48 bytes: FP32 view for the mixed traversal
     int count;
 };
 
+// Per-member results of a forest build (tree.tt, TT_WORDS ints a member).
+enum MemberWords {
+    TT_NNE = 0,   // non-EMPTY nodes
+    TT_M,         // nodes inside the box
+    TT_START,     // first sorted position of the member
+    TT_ROOT,      // root cell
+    TT_END,       // one past the member's last cell
+    TT_ITEM0,     // first work item of the member in the traversal queue
+    TT_WORDS = 8
+};
+
 struct TreeBuf {
     int cap = 0;
+    int *tt = nullptr;           // TT_WORDS ints per member
     uint64_t *keys = nullptr, *keys_alt = nullptr;
     int *order = nullptr, *order_alt = nullptr;
     int *torder = nullptr;       // traversal order of the targets (spatial, all non-EMPTY)
@@ -90,6 +102,8 @@ enum TreeCounters {
     TC_ERR = 8,        // error bits
     TC_BAD,            // first failed bounds check: code << 24 | low bits of the index
     TC_NEED,           // most cells any build needed (checked against the storage)
+    TC_WORK,           // work-queue counter of the traversal (reset per launch)
+    TC_ITEMS,          // work items of the traversal (written by the build)
     TC_COUNT,
     TC_STAT64 = 16,    // int offset of the 64-bit counters (per build): visits, accepts, warp steps, ...
     TC_WORDS = 32      // ints allocated
@@ -121,11 +135,42 @@ struct DevParams {               // ov_params as the kernels need them
     double vn[3], vs[3], vb[3];          // direction * strength for SIMPLE
     double vn_dir[3], vs_dir[3], vb_dir[3];   // normalised directions
     double vn_s0, vn_s1, vn_tld, vs_s0, vs_s1, vs_tld, vb_s0, vb_s1, vb_tld;
+    double rec_dist;                     // reconnection candidate radius
+};
+
+// One tangle of the pool.  A single uploaded tangle is member 0 of 1; an
+// ensemble keeps each member in its own contiguous slot range, so local
+// index = slot - lo and the reference's slot arithmetic (next_empty, the
+// doubling of expand_tangle) holds per member.
+struct Member {
+    int lo = 0;            // first slot
+    int n = 0;             // the member's tangle_state N (its visible slots)
+    int cap = 0;           // slots reserved for it (>= n; [lo+n, lo+cap) EMPTY)
+    int next_empty = -1;   // tangle.h:63, local index
+    int total_empty = 0;   // tangle.h:64
+    ov_params params{};
+};
+
+// Launch shape of the traversal, chosen by ov_autotune or set by the caller.
+struct Tuning {
+    int warps = 4;         // warps per block (2, 4 or 8)
+    int groups = 0;        // query groups per node (0: from the node count)
+    int blocks_per_sm = 0; // persistent blocks per SM (0: occupancy limit)
+    int largest_first = 1; // work queue visits the largest member first
 };
 
 struct ov_ctx {
     int device = 0;
     int sm_count = 152;
+    std::vector<Member> mem{Member{}};
+    int key_tbits = 0;                     // member-id bits on top of the path keys
+    int key_levels = OV_MAX_LEVEL;         // tree levels below each root
+    int *d_tid = nullptr;                  // member of each slot (ensembles only)
+    DevParams *d_tprm = nullptr;           // per-member parameters (ensembles only)
+    int *d_qorder = nullptr;               // members in work-queue order
+    int2 *d_mrange = nullptr;              // per-member slot range [lo, lo + cap)
+    int tcap = 0;                          // members the per-member device arrays hold
+    Tuning tune;
     cudaStream_t stream = nullptr;
     ov_params params{};
     int precision = OV_PREC_FP64;
@@ -149,7 +194,7 @@ struct ov_ctx {
     // ov_pull_host and ov_push_device)
     std::vector<double> h_x, h_y, h_z;
     std::vector<int> h_fwd, h_rev, h_status, h_pin, h_recalc;
-    int next_empty = -1, total_empty = 0;   // tangle_state bookkeeping (tangle.h:63-64)
+    bool host_valid = false;     // the mirrors equal the device positions and topology
     // reconnect / smoothing scratch
     uint64_t *d_gkeys = nullptr, *d_gkeys_alt = nullptr;
     int *d_gidx = nullptr, *d_gidx_alt = nullptr;
@@ -157,6 +202,7 @@ struct ov_ctx {
     int pair_cap = 0;
     int *d_loop_nodes = nullptr, *d_loop_off = nullptr;
     double *d_loop_buf = nullptr;
+    double *d_loop_cut = nullptr;
     int loop_cap = 0, loop_nodes_cap = 0;
     size_t loop_buf_cap = 0;
     // RK4 graph: stage times and steps live in d_time = {t+dt/2, t+dt/2,
@@ -211,6 +257,9 @@ int ov_pull_host(ov_ctx *c);     // positions + topology -> host mirrors
 int ov_push_device(ov_ctx *c, int first_new_slot);  // host mirrors -> device
 int ov_eval_sync(ov_ctx *c, NodeArrays &na, double t, bool tangents);
 int ov_tree_reserve_cells(ov_ctx *c, int cells);
+int ov_reserve_members(ov_ctx *c, int nt);   // per-member device tables (ov_capi.cu)
+int ov_upload_member_tables(ov_ctx *c);
+int ov_move_device_slots(ov_ctx *c, const std::vector<Member> &old);
 void ov_tree_free(TreeBuf &t);
 int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s);
 
@@ -223,6 +272,8 @@ void ov_scan_exclusive(ov_ctx *c, const int *in, int *out, int n_max, const int 
 void ov_launch_tangents(ov_ctx *c, const NodeArrays &na, cudaStream_t s);
 int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s);
 int ov_reserve_velocity_scratch(ov_ctx *c);
+int ov_query_groups(ov_ctx *c);
+int ov_traversal_blocks(ov_ctx *c, int precision, int warps, int *per_sm);
 int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out);
 void ov_launch_euler(ov_ctx *c, const NodeArrays &src, const double *vx, const double *vy,
                      const double *vz, double dt, NodeArrays &dst, cudaStream_t s);

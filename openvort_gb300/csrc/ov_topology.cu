@@ -85,8 +85,12 @@ inline double hpwrap_len(const Geometry &g, const double r1[3], const double r2i
     return hlen(d);
 }
 
+// Host mirror of the pool, seen from one member: its visible slots
+// [lo, hi) and its parameters.  Indices stay pool slots.
 struct Host {
     ov_ctx *c;
+    int lo, hi;
+    const ov_params *P;
     int N() const { return c->n_live; }
     void pos(int i, double p[3]) const { p[0] = c->h_x[i]; p[1] = c->h_y[i]; p[2] = c->h_z[i]; }
     int &fwd(int i) { return c->h_fwd[i]; }
@@ -96,6 +100,12 @@ struct Host {
 };
 
 inline bool pinned(int s) { return s == OV_PINNED || s == OV_PINNED_SLIP; }
+
+inline Host host_of(ov_ctx *c, int mi)
+{
+    const Member &m = c->mem[mi];
+    return Host{c, m.lo, m.lo + m.n, &m.params};
+}
 
 // step_node (tangle.c:155-194)
 bool hstep(Host &h, int i, int where, double out[3])
@@ -222,7 +232,7 @@ bool hsegment(Host &h, int m, int f, const double r[3], double out[3])
     double R[3], Rp1[3];
     hsub(R, a, r);
     hsub(Rp1, b, r);
-    return hlaw(R, Rp1, h.c->params.kappa, out);
+    return hlaw(R, Rp1, h.P->kappa, out);
 }
 
 // lia_velocity (tangle.c:568-592) + external v_s, given tangent/normal
@@ -231,7 +241,7 @@ bool hlia(Host &h, int i, const double tg[3], const double nm[3], double t, doub
     double p[3], nx[3], pv[3];
     h.pos(i, p);
     if (!(hstep(h, i, 1, nx) && hstep(h, i, -1, pv))) return false;
-    const ov_params &P = h.c->params;
+    const ov_params &P = *h.P;
     double l_next = hpwrap_len(h.c->geo, p, nx);
     double l_prev = hpwrap_len(h.c->geo, pv, p);
     double f = P.kappa * log(2 * sqrt(l_next * l_prev) / sqrt(M_E) / P.vortex_width) / 4 / M_PI;
@@ -246,7 +256,7 @@ bool hlia(Host &h, int i, const double tg[3], const double nm[3], double t, doub
 // vels from vs: mutual friction and PINNED_SLIP (tangle.c:694-725)
 void hfriction(Host &h, int k, const double tg[3], const double vs[3], double t, double vel[3])
 {
-    const ov_params &P = h.c->params;
+    const ov_params &P = *h.P;
     for (int a = 0; a < 3; ++a) vel[a] = vs[a];
     if (P.use_mutual_friction) {
         double vn[3], dv[3], c1[3], c2[3];
@@ -277,8 +287,7 @@ bool hdirect_exact(Host &h, int k, const double tg[3], const double nm[3], doubl
     double x[3];
     h.pos(k, x);
     const Geometry &g = h.c->geo;
-    int N = h.N();
-    for (int m = 0; m < N; ++m) {
+    for (int m = h.lo; m < h.hi; ++m) {
         int f = h.fwd(m);
         if (f == -1 || k == m || k == f) continue;
         double w[3];
@@ -288,7 +297,7 @@ bool hdirect_exact(Host &h, int k, const double tg[3], const double nm[3], doubl
     for (int j = 0; j < g.n_img; ++j) {
         double q[3];
         himage(g, j, x, q);
-        for (int m = 0; m < N; ++m) {
+        for (int m = h.lo; m < h.hi; ++m) {
             int f = h.fwd(m);
             if (f == -1) continue;
             double w[3];
@@ -340,14 +349,16 @@ __device__ __forceinline__ int lower_key(const uint64_t *keys, int n, uint64_t v
 
 __global__ void k_pairs(const uint64_t *__restrict__ keys, const int *__restrict__ idx, int cap,
                         const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
-                        GridGeom gg, Geometry geo, double rec_dist, int *__restrict__ pairs, int *npairs,
-                        int pair_cap)
+                        GridGeom gg, Geometry geo, double rec_dist, const int *__restrict__ tid,
+                        const DevParams *__restrict__ tprm, int *__restrict__ pairs, int *npairs, int pair_cap)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap) return;
     uint64_t key = keys[i];
     if (key == ~0ull) return;
     int k = idx[i];
+    const int mk = tid ? tid[k] : 0;   // pairs within one member, at its rec_dist
+    if (tid) rec_dist = tprm[mk].rec_dist;
     uint64_t cid = key >> 32;
     int c[3] = {(int)(cid % gg.n[0]), (int)((cid / gg.n[0]) % gg.n[1]), (int)(cid / ((uint64_t)gg.n[0] * gg.n[1]))};
     double pk[3] = {x[k], y[k], z[k]};
@@ -375,6 +386,7 @@ __global__ void k_pairs(const uint64_t *__restrict__ keys, const int *__restrict
                 for (int j = b; j < e; ++j) {
                     int l = idx[j];
                     if (l <= k) continue;
+                    if (tid && tid[l] != mk) continue;
                     double v2[3] = {x[l], y[l], z[l]};
                     pwrap_dev(geo, pk, v2);
                     double d = len3_ref(rn_sub(pk[0], v2[0]), rn_sub(pk[1], v2[1]), rn_sub(pk[2], v2[2]));
@@ -401,7 +413,7 @@ struct SmoothArgs {
     double *x, *y, *z;
     double *buf;               // 3 * 2 * total nodes
     Geometry geo;
-    double freq_to_cutoff;
+    const double *cutoff;      // freq_to_cutoff of each loop's member
 };
 
 __global__ void __launch_bounds__(256) k_smooth(SmoothArgs a)
@@ -449,7 +461,7 @@ __global__ void __launch_bounds__(256) k_smooth(SmoothArgs a)
         __syncthreads();
     }
     // low_pass_filter (vortex_smooth.c:134-175) on the kept half-complex bins
-    int cut = (int)(a.freq_to_cutoff * N / 2);
+    int cut = (int)(a.cutoff[lp] * N / 2);
     int zlo = 0, zhi = 0;
     if (N > 2 * cut + 1) {
         zlo = N / 2 - cut;
@@ -513,6 +525,11 @@ __global__ void __launch_bounds__(256) k_smooth(SmoothArgs a)
 int ov_pull_host(ov_ctx *c)
 {
     int n = c->n_live;
+    if (c->host_valid && (int)c->h_x.size() == n && (int)c->h_status.size() == n) {
+        c->h_recalc.assign(n, 0);
+        return OV_OK;   // nothing changed positions or topology since the last pull / push
+    }
+    c->host_valid = false;
     c->h_x.resize(n); c->h_y.resize(n); c->h_z.resize(n);
     c->h_fwd.resize(n); c->h_rev.resize(n); c->h_status.resize(n); c->h_pin.resize(n);
     c->h_recalc.assign(n, 0);
@@ -526,6 +543,7 @@ int ov_pull_host(ov_ctx *c)
     for (int a = 0; a < 4; ++a)
         OV_CUDA(c, cudaMemcpyAsync(hi[a], di[a], (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
     OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->host_valid = true;
     return OV_OK;
 }
 
@@ -533,6 +551,7 @@ int ov_push_device(ov_ctx *c, int pos_too)
 {
     int n = c->n_live;
     c->tree_built = false;
+    c->host_valid = false;
     if (n > c->cap) {
         int r = ov_grow_preserving(c, n);
         if (r) return r;
@@ -549,6 +568,7 @@ int ov_push_device(ov_ctx *c, int pos_too)
     for (int a = 0; a < 4; ++a)
         OV_CUDA(c, cudaMemcpyAsync(di[a], hi[a], (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
     OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->host_valid = true;   // positions were pushed, or are unchanged since the pull
     return OV_OK;
 }
 
@@ -563,68 +583,106 @@ int ready(ov_ctx *c)
 }
 
 // ------------------------------------------------------- slot allocation
-// expand_tangle (tangle.c:68-101): the pool doubles, new slots EMPTY
-void hexpand(ov_ctx *c, int n);
+// expand_tangle (tangle.c:68-101) of member mi to n slots
+int hexpand(ov_ctx *c, int mi, int n);
 
-// search_next_empty_node (tangle.c:201-234); a slot past the end counts as
-// not empty where the reference reads status[k+1] out of bounds.
-int hsearch_empty(ov_ctx *c)
+// Give member mi room for n visible slots: a single tangle grows its host
+// arrays; an ensemble member past its reserved range gets a range of 2n
+// slots and the members after it move up (host mirror now, device slots
+// without a mirror right away; positions and topology follow on the push).
+int hrelayout(ov_ctx *c, int mi, int n)
 {
-    Host h{c};
-    int N = h.N();
-    if (c->next_empty > 0) {
-        if (c->next_empty < N && h.st(c->next_empty) == OV_EMPTY) {
-            int id = c->next_empty;
-            if (c->next_empty + 1 < N && h.st(c->next_empty + 1) == OV_EMPTY) ++c->next_empty;
-            else c->next_empty = -1;
-            return id;
+    Member &m = c->mem[mi];
+    if (n <= m.cap) return OV_OK;
+    const int newcap = c->mem.size() == 1 ? n : 2 * n;
+    const int delta = newcap - m.cap;
+    const int at = m.lo + m.cap;   // first slot after the member
+    const int old_total = c->n_live;
+    std::vector<Member> old = c->mem;
+    auto grow_d = [&](std::vector<double> &v) { v.insert(v.begin() + at, (size_t)delta, 0.0); };
+    auto grow_i = [&](std::vector<int> &v, int fill) { v.insert(v.begin() + at, (size_t)delta, fill); };
+    grow_d(c->h_x); grow_d(c->h_y); grow_d(c->h_z);
+    grow_i(c->h_fwd, -1); grow_i(c->h_rev, -1);
+    grow_i(c->h_status, OV_EMPTY); grow_i(c->h_pin, OV_NOT_A_FACE);
+    grow_i(c->h_recalc, 0);
+    const int total = old_total + delta;
+    for (int k = 0; k < total; ++k) {
+        if (c->h_fwd[k] >= at) c->h_fwd[k] += delta;
+        if (c->h_rev[k] >= at) c->h_rev[k] += delta;
+    }
+    m.cap = newcap;
+    for (size_t j = mi + 1; j < c->mem.size(); ++j) c->mem[j].lo += delta;
+    c->n_live = total;
+    if (c->mem.size() == 1) return OV_OK;   // a single tangle grows on the push
+    int r;
+    if (total > c->cap && (r = ov_grow_preserving(c, total))) return r;
+    if ((r = ov_move_device_slots(c, old))) return r;
+    return ov_upload_member_tables(c);
+}
+
+// search_next_empty_node (tangle.c:201-234) in member mi (returns a pool
+// slot); a slot past the member's end counts as not empty where the
+// reference reads status[k+1] out of bounds.
+int hsearch_empty(ov_ctx *c, int mi)
+{
+    Member &m = c->mem[mi];
+    Host h = host_of(c, mi);
+    const int N = m.n, lo = m.lo;
+    if (m.next_empty > 0) {
+        if (m.next_empty < N && h.st(lo + m.next_empty) == OV_EMPTY) {
+            int id = m.next_empty;
+            if (m.next_empty + 1 < N && h.st(lo + m.next_empty + 1) == OV_EMPTY) ++m.next_empty;
+            else m.next_empty = -1;
+            return lo + id;
         }
     }
     for (int k = 0; k < N; ++k) {
-        if (h.st(k) == OV_EMPTY) {
-            c->next_empty = (k + 1 < N && h.st(k + 1) == OV_EMPTY) ? k + 1 : -1;
-            return k;
+        if (h.st(lo + k) == OV_EMPTY) {
+            m.next_empty = (k + 1 < N && h.st(lo + k + 1) == OV_EMPTY) ? k + 1 : -1;
+            return lo + k;
         }
     }
     return -1;
 }
 
-// get_next_empty_node (tangle.c:241-253)
-int hget_empty(ov_ctx *c)
+// get_next_empty_node (tangle.c:241-253); -1 when the pool cannot grow
+int hget_empty(ov_ctx *c, int mi)
 {
-    int id = hsearch_empty(c);
-    while (id < 0 || c->h_status[id] != OV_EMPTY) {
-        hexpand(c, 2 * c->n_live > 0 ? 2 * c->n_live : 1);
-        id = hsearch_empty(c);
+    int id = hsearch_empty(c, mi);
+    for (int guard = 0; id < 0 || c->h_status[id] != OV_EMPTY; ++guard) {
+        int n = c->mem[mi].n;
+        if (guard > 40 || hexpand(c, mi, 2 * n > 0 ? 2 * n : 1)) return -1;
+        id = hsearch_empty(c, mi);
     }
     return id;
 }
 
-void hexpand(ov_ctx *c, int n)
+int hexpand(ov_ctx *c, int mi, int n)
 {
-    int old = c->n_live;
-    c->h_x.resize(n, 0.0); c->h_y.resize(n, 0.0); c->h_z.resize(n, 0.0);
-    c->h_fwd.resize(n, -1); c->h_rev.resize(n, -1);
-    c->h_status.resize(n, OV_EMPTY); c->h_pin.resize(n, OV_NOT_A_FACE);
-    c->h_recalc.resize(n, 0);
-    for (int k = old; k < n; ++k) {
+    int r = hrelayout(c, mi, n);
+    if (r) return r;
+    Member &m = c->mem[mi];
+    const int old = m.n;
+    for (int k = m.lo + old; k < m.lo + n; ++k) {
         c->h_status[k] = OV_EMPTY; c->h_pin[k] = OV_NOT_A_FACE;
         c->h_fwd[k] = -1; c->h_rev[k] = -1;
     }
-    c->n_live = n;
-    c->total_empty += n - old;
-    c->next_empty = hget_empty(c);
+    m.n = n;
+    m.total_empty += n - old;
+    int id = hget_empty(c, mi);
+    if (id < 0) return ov_fail(c, OV_ERR_ALLOC, "member %d could not grow", mi);
+    c->mem[mi].next_empty = id - c->mem[mi].lo;
+    return OV_OK;
 }
 
-// out_of_box + periodic_shift (tangle.c:761-814, boundaries.c:113-150)
-void hperiodic(ov_ctx *c)
+// out_of_box + periodic_shift (tangle.c:761-814, boundaries.c:113-150) on
+// slots [lo, hi)
+void hperiodic(ov_ctx *c, int lo, int hi)
 {
-    Host h{c};
     const Geometry &g = c->geo;
-    for (int k = 0; k < h.N(); ++k) {
-        if (h.st(k) == OV_EMPTY) continue;
-        double p[3];
-        h.pos(k, p);
+    for (int k = lo; k < hi; ++k) {
+        if (c->h_status[k] == OV_EMPTY) continue;
+        double p[3] = {c->h_x[k], c->h_y[k], c->h_z[k]};
         for (int guard = 0; guard < 1000; ++guard) {
             int face = -1;
             if (p[0] < g.lo[0]) face = OV_LEFT;
@@ -643,36 +701,38 @@ void hperiodic(ov_ctx *c)
     }
 }
 
-// eliminate_small_loops (tangle.c:1063-1128); returns nodes removed
-int hsmall_loops(ov_ctx *c)
+// eliminate_small_loops (tangle.c:1063-1128) in member mi; returns nodes removed
+int hsmall_loops(ov_ctx *c, int mi)
 {
-    Host h{c};
-    int N = h.N(), removed = 0;
+    Host h = host_of(c, mi);
+    const int lo = h.lo, hi = h.hi, N = hi - lo;
+    int removed = 0;
     std::vector<char> seen(N > 0 ? N : 1, 0);
-    for (int k = 0; k < N; ++k) {
-        if (h.st(k) == OV_EMPTY || seen[k]) continue;
-        seen[k] = 1;
+    auto mark = [&](int slot) { if (slot >= lo && slot < hi) seen[slot - lo] = 1; };
+    for (int k = lo; k < hi; ++k) {
+        if (h.st(k) == OV_EMPTY || seen[k - lo]) continue;
+        seen[k - lo] = 1;
         int steps = 0, here = k, nx = h.fwd(here);
         while (nx != k) {
             if (pinned(h.st(here)) && nx < 0) {
                 here = k;
                 nx = h.rev(here);
                 while (nx >= 0) {
-                    seen[here] = 1;
+                    mark(here);
                     here = nx;
                     nx = h.rev(here);
                     steps++;
                 }
                 break;
             }
-            if (nx < 0 || nx >= N) break;
-            seen[here] = 1;
+            if (nx < lo || nx >= hi) break;
+            mark(here);
             here = nx;
             nx = h.fwd(here);
             steps++;
             if (steps > N) break;
         }
-        if (steps < c->params.small_loop_cutoff) {
+        if (steps < h.P->small_loop_cutoff) {
             nx = here;
             for (int guard = 0; guard <= N; ++guard) {
                 int cur = nx;
@@ -688,11 +748,12 @@ int hsmall_loops(ov_ctx *c)
     return removed;
 }
 
-// add_point (tangle.c:261-335)
-int hadd_point(ov_ctx *c, int p, std::vector<int> &new_nodes)
+// add_point (tangle.c:261-335) in member mi; -1 when no slot could be had
+int hadd_point(ov_ctx *c, int mi, int p, std::vector<int> &new_nodes)
 {
-    int np = hget_empty(c);
-    Host h{c};
+    int np = hget_empty(c, mi);
+    if (np < 0) return -1;
+    Host h = host_of(c, mi);
     h.st(np) = OV_FREE;
     h.pin(np) = OV_NOT_A_FACE;
     int nx = h.fwd(p);
@@ -733,7 +794,7 @@ int hadd_point(ov_ctx *c, int p, std::vector<int> &new_nodes)
 // remove_point (tangle.c:342-355)
 void hremove(ov_ctx *c, int i)
 {
-    Host h{c};
+    Host h{c, 0, c->n_live, &c->params};
     int pv = h.rev(i), nx = h.fwd(i);
     if (pv >= 0) h.fwd(pv) = nx;
     if (nx >= 0) h.rev(nx) = pv;
@@ -741,33 +802,39 @@ void hremove(ov_ctx *c, int i)
     h.st(i) = OV_EMPTY;
 }
 
-void hremesh(ov_ctx *c, double min_dist, double max_dist, int *added_out, int *removed_out,
-             std::vector<int> &new_nodes)
+// remesh (tangle.c:1018-1061) of member mi: slots in index order, including
+// the ones it inserts (and the range it grows into)
+int hremesh(ov_ctx *c, int mi, double min_dist, double max_dist, int *added_out, int *removed_out,
+            std::vector<int> &new_nodes)
 {
     int added = 0, removed = 0;
-    for (int k = 0; k < c->n_live; ++k) {
-        Host h{c};
-        if (h.st(k) == OV_EMPTY) continue;
-        int nx = h.fwd(k), pv = h.rev(k);
+    for (int k = 0; k < c->mem[mi].n; ++k) {
+        Host h = host_of(c, mi);
+        const int s = h.lo + k;
+        if (h.st(s) == OV_EMPTY) continue;
+        int nx = h.fwd(s), pv = h.rev(s);
         double lf = 0, lr = 0, pk[3];
-        h.pos(k, pk);
+        h.pos(s, pk);
         if (nx >= 0) { double q[3]; h.pos(nx, q); lf = hpwrap_len(c->geo, pk, q); }
         if (pv >= 0) { double q[3]; h.pos(pv, q); lr = hpwrap_len(c->geo, pk, q); }
         if (nx >= 0 && pv >= 0 && ((lf < min_dist || lr < min_dist) && (lf + lr) < max_dist)) {
-            hremove(c, k);
+            hremove(c, s);
             removed++;
         }
         if (nx >= 0 && lf > max_dist) {
             added++;
-            hadd_point(c, k, new_nodes);
+            if (hadd_point(c, mi, s, new_nodes) < 0) return OV_ERR_ALLOC;
         }
     }
     if (added) {
-        hperiodic(c);
-        std::fill(c->h_recalc.begin(), c->h_recalc.end(), 0);
+        // points added outside the domain (tangle.c:1056-1060)
+        const Member &m = c->mem[mi];
+        hperiodic(c, m.lo, m.lo + m.n);
+        std::fill(c->h_recalc.begin() + m.lo, c->h_recalc.begin() + m.lo + m.n, 0);
     }
     *added_out = added;
     *removed_out = removed;
+    return OV_OK;
 }
 
 int ensure_pairs(ov_ctx *c, int need)
@@ -786,7 +853,8 @@ int find_pairs(ov_ctx *c, std::vector<std::pair<int, int>> &out)
 {
     out.clear();
     int cap = c->cap;
-    double rd = c->params.rec_dist;
+    double rd = 0;
+    for (const Member &m : c->mem) rd = std::max(rd, m.params.rec_dist);   // grid for the largest
     GridGeom gg;
     for (int a = 0; a < 3; ++a) {
         gg.lo[a] = c->geo.lo[a];
@@ -805,8 +873,10 @@ int find_pairs(ov_ctx *c, std::vector<std::pair<int, int>> &out)
     ov_sort_keys(c, t, cap, c->stream);
     for (int attempt = 0; attempt < 2; ++attempt) {
         OV_CUDA(c, cudaMemsetAsync(c->d_npairs, 0, sizeof(int), c->stream));
+        const bool ens = c->mem.size() > 1;
         k_pairs<<<nb, 256, 0, c->stream>>>(t.keys, t.order, cap, c->node.x, c->node.y, c->node.z, gg, c->geo, rd,
-                                           c->d_pairs, c->d_npairs, c->pair_cap);
+                                           ens ? c->d_tid : nullptr, ens ? c->d_tprm : nullptr, c->d_pairs,
+                                           c->d_npairs, c->pair_cap);
         c->launches++;
         OV_CUDA(c, cudaGetLastError());
         int np = 0;
@@ -842,9 +912,12 @@ int ov_eliminate_small_loops(ov_ctx *c)
     int r = ready(c);
     if (r) return r;
     if ((r = ov_pull_host(c))) return r;
-    int removed = hsmall_loops(c);
+    c->host_valid = false;   // until the mirror is pushed (or found unchanged)
+    int removed = 0;
+    for (int mi = 0; mi < (int)c->mem.size(); ++mi) removed += hsmall_loops(c, mi);
     c->stats.small_loops_removed = removed;
     if (removed) return ov_push_device(c, 0);
+    c->host_valid = true;
     return OV_OK;
 }
 
@@ -854,12 +927,28 @@ int ov_remesh(ov_ctx *c, double min_dist, double max_dist, double t)
     int r = ready(c);
     if (r) return r;
     if ((r = ov_pull_host(c))) return r;
+    c->host_valid = false;
     int added = 0, removed = 0;
     std::vector<int> new_nodes;
-    hremesh(c, min_dist, max_dist, &added, &removed, new_nodes);
+    for (int mi = 0; mi < (int)c->mem.size(); ++mi) {
+        // a single tangle takes the arguments; ensemble members their own dl_min / dl_max
+        double lo = c->mem.size() == 1 ? min_dist : c->mem[mi].params.dl_min;
+        double hi = c->mem.size() == 1 ? max_dist : c->mem[mi].params.dl_max;
+        int a = 0, d = 0;
+        if ((r = hremesh(c, mi, lo, hi, &a, &d, new_nodes))) {
+            // keep host and device consistent before reporting
+            ov_push_device(c, 1);
+            return r == OV_ERR_ALLOC ? ov_fail(c, r, "remesh: no empty slot could be had") : r;
+        }
+        added += a;
+        removed += d;
+    }
     c->stats.remesh_added = added;
     c->stats.remesh_removed = removed;
-    if (!added && !removed) return OV_OK;
+    if (!added && !removed) {
+        c->host_valid = true;
+        return OV_OK;
+    }
     if ((r = ov_push_device(c, 1))) return r;
     if (!new_nodes.empty()) {
         int *d = nullptr;
@@ -879,10 +968,10 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     int r = ready(c);
     if (r) return r;
     if ((r = ov_pull_host(c))) return r;
+    c->host_valid = false;
     std::vector<std::pair<int, int>> pairs;
     if ((r = find_pairs(c, pairs))) return r;
-    Host h{c};
-    int N = h.N();
+    const int N = c->n_live;
     // direct sums of every candidate node on the pass's starting topology
     std::vector<int> cand;
     cand.reserve(2 * pairs.size());
@@ -894,12 +983,24 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     auto cand_index = [&](int k) {
         return (int)(std::lower_bound(cand.begin(), cand.end(), k) - cand.begin());
     };
-    std::vector<SegChange> changes;
+    std::vector<SegChange> changes;   // of the member being processed
     std::vector<int> &recalc = c->h_recalc;
     recalc.assign(N, 0);
-    const double cos_cut = cos(c->params.reconnection_angle_cutoff);
     const Geometry &g = c->geo;
     int nrec = 0;
+    // members own contiguous slot ranges and pairs are sorted by k: each
+    // member's pairs form one run, processed in the reference's order
+    auto member_of = [&](int k) {
+        int lo = 0, hi = (int)c->mem.size() - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (c->mem[mid].lo <= k) lo = mid; else hi = mid - 1;
+        }
+        return lo;
+    };
+    int cur_member = -1;
+    Host h = host_of(c, 0);
+    double cos_cut = 0;
 
     // velocity of an unflagged candidate node on the current topology
     auto velocity = [&](int k, const double tg[3], const double nm[3], double vel[3]) -> bool {
@@ -931,6 +1032,13 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         int k = pairs[i].first;
         size_t e = i;
         while (e < pairs.size() && pairs[e].first == k) ++e;
+        int mk = member_of(k);
+        if (mk != cur_member) {
+            cur_member = mk;
+            h = host_of(c, mk);
+            changes.clear();
+            cos_cut = cos(h.P->reconnection_angle_cutoff);
+        }
         int sk = h.st(k);
         if (sk == OV_EMPTY || pinned(sk) || recalc[k]) { i = e; continue; }
         for (size_t q = i; q < e; ++q) {
@@ -998,6 +1106,7 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     c->stats.reconnections = nrec;
     if (nrecs) *nrecs = nrec;
     if (nrec) return ov_push_device(c, 0);
+    c->host_valid = true;
     return OV_OK;
 }
 
@@ -1005,30 +1114,38 @@ int ov_smooth(ov_ctx *c)
 {
     int r = ready(c);
     if (r) return r;
-    if (!c->params.use_freq_filter) return OV_OK;
+    bool any = false;
+    for (const Member &m : c->mem) any = any || m.params.use_freq_filter;
+    if (!any) return OV_OK;
     if ((r = ov_pull_host(c))) return r;
-    Host h{c};
-    int N = h.N();
-    // closed loops in the reference's discovery order (vortex_smooth.c:192-210)
-    std::vector<char> seen(N > 0 ? N : 1, 0);
+    // closed loops of each filtering member in the reference's discovery
+    // order (vortex_smooth.c:192-210)
     std::vector<int> off{0}, nodes;
+    std::vector<double> cut;
     int maxlen = 0;
-    for (int i = 0; i < N; ++i) {
-        if (seen[i]) continue;
-        if (h.st(i) == OV_EMPTY) { seen[i] = 1; continue; }
-        int j = i, guard = 0;
-        while (h.rev(j) != i && h.rev(j) != -1 && guard++ <= N) j = h.rev(j);
-        if (h.rev(j) == -1 || guard > N) { seen[i] = 1; continue; }   // open line: not smoothed
-        int len = 0;
-        int m = i;
-        do {
-            nodes.push_back(m);
-            seen[m] = 1;
-            m = h.fwd(m);
-            ++len;
-        } while (m != i && m >= 0 && len <= N);
-        off.push_back((int)nodes.size());
-        maxlen = std::max(maxlen, len);
+    for (int mi = 0; mi < (int)c->mem.size(); ++mi) {
+        if (!c->mem[mi].params.use_freq_filter) continue;
+        Host h = host_of(c, mi);
+        const int lo = h.lo, N = h.hi - h.lo;
+        std::vector<char> seen(N > 0 ? N : 1, 0);
+        for (int i = lo; i < h.hi; ++i) {
+            if (seen[i - lo]) continue;
+            if (h.st(i) == OV_EMPTY) { seen[i - lo] = 1; continue; }
+            int j = i, guard = 0;
+            while (h.rev(j) != i && h.rev(j) != -1 && guard++ <= N) j = h.rev(j);
+            if (h.rev(j) == -1 || guard > N) { seen[i - lo] = 1; continue; }   // open line: not smoothed
+            int len = 0;
+            int m = i;
+            do {
+                nodes.push_back(m);
+                if (m >= lo && m < h.hi) seen[m - lo] = 1;
+                m = h.fwd(m);
+                ++len;
+            } while (m != i && m >= 0 && len <= N);
+            off.push_back((int)nodes.size());
+            cut.push_back(h.P->freq_to_cutoff);
+            maxlen = std::max(maxlen, len);
+        }
     }
     int nloops = (int)off.size() - 1;
     if (nloops == 0) return OV_OK;
@@ -1036,8 +1153,11 @@ int ov_smooth(ov_ctx *c)
     if (c->loop_cap < nloops + 1 || c->loop_nodes_cap < (int)total) {
         if (c->d_loop_off) cudaFree(c->d_loop_off);
         if (c->d_loop_nodes) cudaFree(c->d_loop_nodes);
+        if (c->d_loop_cut) cudaFree(c->d_loop_cut);
+        c->d_loop_off = nullptr; c->d_loop_nodes = nullptr; c->d_loop_cut = nullptr;
         OV_CUDA(c, cudaMalloc(&c->d_loop_off, (size_t)(nloops + 1) * 4));
-        OV_CUDA(c, cudaMalloc(&c->d_loop_nodes, total * 4));
+        OV_CUDA(c, cudaMalloc(&c->d_loop_cut, (size_t)(nloops + 1) * sizeof(double)));
+        OV_CUDA(c, cudaMalloc(&c->d_loop_nodes, std::max(total, (size_t)1) * 4));
         c->loop_cap = nloops + 1;
         c->loop_nodes_cap = (int)total;
     }
@@ -1048,6 +1168,8 @@ int ov_smooth(ov_ctx *c)
         c->loop_buf_cap = need;
     }
     OV_CUDA(c, cudaMemcpyAsync(c->d_loop_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    OV_CUDA(c, cudaMemcpyAsync(c->d_loop_cut, cut.data(), cut.size() * sizeof(double), cudaMemcpyHostToDevice,
+                               c->stream));
     OV_CUDA(c, cudaMemcpyAsync(c->d_loop_nodes, nodes.data(), total * 4, cudaMemcpyHostToDevice, c->stream));
     SmoothArgs a;
     a.loop_off = c->d_loop_off;
@@ -1055,13 +1177,14 @@ int ov_smooth(ov_ctx *c)
     a.x = c->node.x; a.y = c->node.y; a.z = c->node.z;
     a.buf = c->d_loop_buf;
     a.geo = c->geo;
-    a.freq_to_cutoff = c->params.freq_to_cutoff;
+    a.cutoff = c->d_loop_cut;
     int Nmax = 2 * maxlen;
     size_t shbytes = (size_t)(2 * Nmax + 3 * (Nmax / 2 + 1 + Nmax)) * sizeof(double);
     if (shbytes > 200 * 1024) return ov_fail(c, OV_ERR_ARG, "loop of %d nodes too long to smooth", maxlen);
     if (shbytes > 48 * 1024)
         OV_CUDA(c, cudaFuncSetAttribute(k_smooth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes));
     c->tree_built = false;
+    c->host_valid = false;
     k_smooth<<<nloops, 256, shbytes, c->stream>>>(a);
     c->launches++;
     OV_CUDA(c, cudaGetLastError());

@@ -15,6 +15,13 @@
 // Sorting the keys puts the cells of each level in contiguous ranges and in
 // the reference's child order; cells are emitted in pre-order, so a cell's
 // subtree is [cell+1, cell.next) and a traversal needs no stack.
+//
+// An ensemble builds one such tree per member in the same launches (a
+// forest): the member id sits above the out-of-box bit of the key, so the
+// sort groups members, and each member's sorted range gets its own root
+// cell followed by its pre-order cells.  With a single member the id field
+// is empty and the keys hold 21 levels; with T members it takes
+// ceil(log2 T) bits and the keys hold floor((63 - bits) / 3) levels.
 #include "ov_internal.cuh"
 
 void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s);
@@ -26,13 +33,27 @@ namespace {
 struct KeyGeom {
     double lo[3], hi[3], L[3];
     int fast;          // fixed-point digits allowed (rounding bound is small)
+    int tb;            // member-id bits on top of the key
+    int levels;        // levels the key holds
+    uint64_t lvmask;   // the levels' bits in the path field
+    int nt;            // members
 };
 
+// bit offset of the level-`lev` digit
+__device__ __forceinline__ int dsh(const KeyGeom &g, int lev) { return 63 - g.tb - 3 * lev; }
+// member of a non-EMPTY key (clamped: ids come from the slot table)
+__device__ __forceinline__ int key_member(const KeyGeom &g, uint64_t key)
+{
+    int m = g.tb ? (int)(key >> (64 - g.tb)) : 0;
+    return m < g.nt ? m : g.nt - 1;
+}
+
+// 63-bit path (digit of level lev at bit 63 - 3 lev) by the reference's descent
 __device__ __forceinline__ uint64_t exact_key(const double p[3], const KeyGeom &g, int *err)
 {
     double b[3] = {g.lo[0], g.lo[1], g.lo[2]}, t[3] = {g.hi[0], g.hi[1], g.hi[2]};
     uint64_t key = 0;
-    for (int lev = 1; lev <= OV_MAX_LEVEL; ++lev) {
+    for (int lev = 1; lev <= g.levels; ++lev) {
         int pick = -1;
         double cb[3], ct[3];
         for (int idx = 0; idx < 8; ++idx) {
@@ -56,27 +77,35 @@ __device__ __forceinline__ uint64_t exact_key(const double p[3], const KeyGeom &
 }
 
 __global__ void k_keys(const int *__restrict__ status, const double *__restrict__ x,
-                       const double *__restrict__ y, const double *__restrict__ z, int cap, KeyGeom g,
-                       uint64_t *__restrict__ keys, int *__restrict__ order, int *counters)
+                       const double *__restrict__ y, const double *__restrict__ z, const int *__restrict__ tid,
+                       int cap, KeyGeom g, uint64_t *__restrict__ keys, int *__restrict__ order,
+                       int *counters, int *tt)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     bool live = i < cap && status[i] != OV_EMPTY;
     double p[3] = {0, 0, 0};
     if (live) { p[0] = x[i]; p[1] = y[i]; p[2] = z[i]; }
+    int m = (live && tid) ? tid[i] : 0;
     bool inside = live && in_closed_box_dev(g.lo, g.hi, p);
     bool bad = live && !(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]));
-    // one atomic per warp for each counter
+    // one atomic per warp for each counter, one per member present in the warp
     unsigned b_live = __ballot_sync(0xffffffffu, live), b_in = __ballot_sync(0xffffffffu, inside);
+    unsigned peers = __match_any_sync(0xffffffffu, live ? m : -1) & b_live;
     if (lane == 0 && b_live) {
         atomicAdd(&counters[TC_NNE], __popc(b_live));
         atomicAdd(&counters[TC_M], __popc(b_in));
         atomicAdd(&counters[TC_OUT], __popc(b_live & ~b_in));
     }
+    if (live && lane == __ffs(peers) - 1) {
+        atomicAdd(&tt[m * TT_WORDS + TT_NNE], __popc(peers));
+        atomicAdd(&tt[m * TT_WORDS + TT_M], __popc(peers & b_in));
+    }
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&counters[TC_ERR], OV_EW_NAN);
     if (i >= cap) return;
     order[i] = i;
     if (!live) { keys[i] = OV_KEY_EMPTY; return; }
+    const uint64_t prefix = g.tb ? (uint64_t)m << (64 - g.tb) : 0;
     if (!inside) {
         // root-only member (octree.c:116-127).  The rest of the key orders
         // it among the other root-only nodes by the cell path of its
@@ -97,7 +126,7 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
             uint64_t xb = (W[0] >> sh) & 1, yb = (W[1] >> sh) & 1, zb = (W[2] >> sh) & 1;
             k2 |= ((zb << 2) | (yb << 1) | (xb ^ 1)) << (63 - 3 * lev);
         }
-        keys[i] = OV_KEY_OUT | (k2 >> 1);
+        keys[i] = prefix | (1ull << (63 - g.tb)) | (k2 >> (g.tb + 1));
         return;
     }
     uint64_t U[3];
@@ -124,66 +153,117 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
         key = exact_key(p, g, &err);
         if (err) atomicOr(&counters[TC_ERR], err);
     }
-    keys[i] = key;
+    keys[i] = prefix | ((key >> g.tb) & g.lvmask);
+}
+
+// Member layout: first sorted position of each member (members in id order)
+// and the first work tile of each in the traversal queue (queue order).
+__global__ void k_layout(int *tt, int nt, const int *__restrict__ qorder, int *counters)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int acc = 0;
+    for (int m = 0; m < nt; ++m) {
+        tt[m * TT_WORDS + TT_START] = acc;
+        acc += tt[m * TT_WORDS + TT_NNE];
+    }
+    int tiles = 0;
+    for (int k = 0; k < nt; ++k) {
+        int m = qorder ? qorder[k] : k;
+        if (m < 0 || m >= nt) { atomicOr(&counters[TC_ERR], OV_EW_BOUNDS); continue; }
+        tt[m * TT_WORDS + TT_ITEM0] = tiles;
+        tiles += (tt[m * TT_WORDS + TT_NNE] + 31) / 32;
+    }
+    counters[TC_ITEMS] = tiles;
+}
+
+// path bits of a key without member id (in-box keys) / of the clamped path
+// (out-of-box keys), comparable with each other
+__device__ __forceinline__ uint64_t inbox_path(const KeyGeom &g, uint64_t k)
+{
+    return k & ((1ull << (63 - g.tb)) - 1);
+}
+__device__ __forceinline__ uint64_t out_path(const KeyGeom &g, uint64_t k)
+{
+    return (k & ((1ull << (63 - g.tb)) - 1)) << 1;
 }
 
 // Traversal order: the in-box nodes in path order merged with the root-only
 // nodes at the position of their clamped path (merge by rank; in-box first on
-// ties).  Out-of-box targets then share warps with their spatial neighbours
-// instead of forming a few warps that span the whole box surface.
+// ties), per member.  Out-of-box targets then share warps with their spatial
+// neighbours instead of forming a few warps that span the whole box surface.
 __global__ void k_target_order(const uint64_t *__restrict__ keys, const int *__restrict__ order, int cap,
-                               const int *counters, int *__restrict__ torder)
+                               const int *counters, const int *__restrict__ tt, KeyGeom g,
+                               int *__restrict__ torder)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
-    int M = counters[TC_M], nne = counters[TC_NNE];
-    if (s >= nne || s >= cap) return;
+    int nne_all = counters[TC_NNE];
+    if (s >= nne_all || s >= cap) return;
+    const int *w = tt + key_member(g, keys[s]) * TT_WORDS;
+    const int st = w[TT_START], M = w[TT_M], nne = w[TT_NNE];
+    const int loc = s - st;
+    if (loc < 0 || loc >= nne) return;   // cannot happen for a consistent build
     int nout = nne - M;
     int pos;
-    if (s < M) {
+    if (loc < M) {
         // in-box: its rank plus the root-only nodes whose clamped path is smaller
-        uint64_t k = keys[s];
+        uint64_t k = inbox_path(g, keys[s]);
         int lo = 0, hi = nout;
         while (lo < hi) {
             int mid = (lo + hi) >> 1;
-            if (((keys[M + mid] & ~OV_KEY_OUT) << 1) < k) lo = mid + 1; else hi = mid;
+            if (out_path(g, keys[st + M + mid]) < k) lo = mid + 1; else hi = mid;
         }
-        pos = s + lo;
+        pos = loc + lo;
     } else {
-        int j = s - M;
-        uint64_t k = (keys[s] & ~OV_KEY_OUT) << 1;
+        int j = loc - M;
+        uint64_t k = out_path(g, keys[s]);
         int lo = 0, hi = M;
         while (lo < hi) {
             int mid = (lo + hi) >> 1;
-            if (keys[mid] <= k) lo = mid + 1; else hi = mid;
+            if (inbox_path(g, keys[st + mid]) <= k) lo = mid + 1; else hi = mid;
         }
         pos = j + lo;
     }
-    torder[pos] = order[s];
+    torder[st + pos] = order[s];
 }
 
-__device__ __forceinline__ int cpl_of(uint64_t a, uint64_t b)
+__device__ __forceinline__ int cpl_of(const KeyGeom &g, uint64_t a, uint64_t b)
 {
     uint64_t d = a ^ b;
-    if (d == 0) return OV_MAX_LEVEL;
-    return (__clzll(d) - 1) / 3;
+    if (d == 0) return g.levels;
+    return min((__clzll(d) - 1 - g.tb) / 3, g.levels);
 }
 
-// cpl[s] for s in [0, M-1), and the number of cells that start at s.
-__global__ void k_cpl(const uint64_t *__restrict__ keys, int cap, int *counters, int *__restrict__ cpl,
-                      int *__restrict__ ncell_at)
+// cpl[s] (common levels with the next in-box key of the member) and the
+// number of cells that start at sorted position s: the member's root at its
+// first position, then the cells of the levels the node starts.
+__global__ void k_cpl(const uint64_t *__restrict__ keys, int cap, int *counters, const int *__restrict__ tt,
+                      KeyGeom g, int *__restrict__ cpl, int *__restrict__ ncell_at)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
-    int M = counters[TC_M];
-    int nne = counters[TC_NNE];
-    int L = 0;
+    int nne_all = counters[TC_NNE];
+    int L = 0, nne = 0;
     bool deep = false;
-    if (s < M) {
-        int cn = (s + 1 < M) ? cpl_of(keys[s], keys[s + 1]) : 0;
-        cpl[s] = cn;
-        int cp = (s > 0) ? cpl_of(keys[s - 1], keys[s]) : 0;
-        L = max(cp, cn) + 1;
-        if (L > OV_MAX_LEVEL) { deep = true; L = OV_MAX_LEVEL; }
-        ncell_at[s] = (nne >= 2) ? max(L - cp, 0) : 0;
+    if (s < nne_all && s < cap) {
+        uint64_t key = keys[s];
+        const int *w = tt + key_member(g, key) * TT_WORDS;
+        const int st = w[TT_START], M = w[TT_M];
+        nne = w[TT_NNE];
+        const int loc = s - st;
+        if (loc < 0 || loc >= nne) {   // cannot happen for a consistent build
+            cpl[s] = 0;
+            ncell_at[s] = 0;
+            nne = 0;
+        } else if (loc < M) {
+            int cn = (loc + 1 < M) ? cpl_of(g, key, keys[s + 1]) : 0;
+            cpl[s] = cn;
+            int cp = (loc > 0) ? cpl_of(g, keys[s - 1], key) : 0;
+            L = max(cp, cn) + 1;
+            if (L > g.levels) { deep = true; L = g.levels; }
+            ncell_at[s] = ((nne >= 2) ? max(L - cp, 0) : 0) + (loc == 0);
+        } else {
+            cpl[s] = 0;
+            ncell_at[s] = (loc == 0);
+        }
     }
     int Lmax = (nne >= 2) ? L : 0;
 #pragma unroll
@@ -215,15 +295,14 @@ __device__ __forceinline__ int lower_prefix(const uint64_t *keys, int lo, int hi
 }
 
 __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict__ cpl,
-                        const int *__restrict__ cell_off, int *counters, KeyGeom g,
-                        Cell64 *__restrict__ cells, int *__restrict__ parent, int *__restrict__ nchild,
+                        const int *__restrict__ cell_off, int *counters, const int *__restrict__ tt, KeyGeom g,
+                        int cap, Cell64 *__restrict__ cells, int *__restrict__ parent, int *__restrict__ nchild,
                         int *__restrict__ arrive, int cap_cells)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
-    int M = counters[TC_M];
-    int nne = counters[TC_NNE];
-    if (s >= M || nne < 2) return;
-    int ncell = cell_off[M];
+    int nne_all = counters[TC_NNE];
+    if (s >= nne_all || s >= cap) return;
+    int ncell = cell_off[nne_all];
     if (ncell > cap_cells) {
         if (s == 0) {
             atomicMax(&counters[TC_NEED], ncell);
@@ -231,39 +310,46 @@ __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict
         }
         return;
     }
-    int cp = s > 0 ? cpl[s - 1] : 0;
-    int cn = s + 1 < M ? cpl[s] : 0;
-    int L = min(max(cp, cn) + 1, OV_MAX_LEVEL);
     uint64_t key = keys[s];
+    const int *w = tt + key_member(g, key) * TT_WORDS;
+    const int st = w[TT_START], M = w[TT_M], nne = w[TT_NNE];
+    const int loc = s - st;
+    if (loc < 0 || loc >= M || nne < 2) return;
+    const int end = st + M;   // the member's in-box positions are [st, end)
+    const int root = cell_off[st];
+    int cp = loc > 0 ? cpl[s - 1] : 0;
+    int cn = loc + 1 < M ? cpl[s] : 0;
+    int L = min(max(cp, cn) + 1, g.levels);
+    const int base = cell_off[s] + (loc == 0);
     // exact box of the first cell starting here, walked from the root
     double b[3] = {g.lo[0], g.lo[1], g.lo[2]}, t[3] = {g.hi[0], g.hi[1], g.hi[2]};
     for (int lev = 1; lev <= cp; ++lev) {
         double cb[3], ct[3];
-        child_box_dev(b, t, (int)((key >> (63 - 3 * lev)) & 7), cb, ct);
+        child_box_dev(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
         for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
     }
     for (int lev = cp + 1; lev <= L; ++lev) {
-        int ci = cell_off[s] + (lev - cp - 1);
+        int ci = base + (lev - cp - 1);
         double cb[3], ct[3];
-        child_box_dev(b, t, (int)((key >> (63 - 3 * lev)) & 7), cb, ct);
+        child_box_dev(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
         for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
-        int sh = 63 - 3 * lev;
-        int e = (lev < L) ? upper_prefix(keys, s + 1, M, sh, key >> sh) - 1 : s;
-        if (lev == OV_MAX_LEVEL) e = upper_prefix(keys, s + 1, M, sh, key >> sh) - 1;
+        int sh = dsh(g, lev);
+        int e = (lev < L) ? upper_prefix(keys, s + 1, end, sh, key >> sh) - 1 : s;
+        if (lev == g.levels) e = upper_prefix(keys, s + 1, end, sh, key >> sh) - 1;
         Cell64 cell;
         cell.lm = box_lm(b, t);
         cell.count = e - s + 1;
-        cell.next = (e + 1 < M) ? cell_off[e + 1] : ncell;
+        cell.next = cell_off[e + 1];   // the member's end of cells when e + 1 == end
         cell.cx = cell.cy = cell.cz = cell.qx = cell.qy = cell.qz = 0;
         cells[ci] = cell;
         int par;
-        if (lev == 1) par = 0;
+        if (lev == 1) par = root;
         else if (cp < lev - 1) par = ci - 1;
         else {
-            int psh = 63 - 3 * (lev - 1);
-            int sp = lower_prefix(keys, 0, s, psh, key >> psh);
-            int cpp = sp > 0 ? cpl[sp - 1] : 0;
-            par = cell_off[sp] + (lev - 1 - cpp - 1);
+            int psh = dsh(g, lev - 1);
+            int sp = lower_prefix(keys, st, s, psh, key >> psh);
+            int cpp = sp > st ? cpl[sp - 1] : 0;
+            par = cell_off[sp] + (sp == st) + (lev - 1 - cpp - 1);
         }
         parent[ci] = par;
         arrive[ci] = 0;
@@ -301,19 +387,24 @@ __device__ __forceinline__ void finalize_cell(Cell64 *cells, int ci, const doubl
 // child to arrive (one atomic per edge, no waiting).
 __global__ void k_moments(const uint64_t *__restrict__ keys, const int *__restrict__ order,
                           const int *__restrict__ cpl, const int *__restrict__ cell_off, int *counters,
+                          const int *__restrict__ tt, KeyGeom g, int cap,
                           const double *__restrict__ x, const double *__restrict__ y,
                           const double *__restrict__ z, const int *__restrict__ fwd, Geometry geo,
                           Cell64 *cells, const int *__restrict__ parent, const int *__restrict__ nchild,
                           int *arrive, double *csum, int cap_cells)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
-    int M = counters[TC_M];
-    int nne = counters[TC_NNE];
-    if (s >= M || nne < 2 || cell_off[M] > cap_cells) return;
-    int cp = s > 0 ? cpl[s - 1] : 0;
-    int cn = s + 1 < M ? cpl[s] : 0;
-    int L = min(max(cp, cn) + 1, OV_MAX_LEVEL);
-    int leaf = cell_off[s] + (L - cp - 1);
+    int nne_all = counters[TC_NNE];
+    if (s >= nne_all || s >= cap || cell_off[nne_all] > cap_cells) return;
+    const int *w = tt + key_member(g, keys[s]) * TT_WORDS;
+    const int st = w[TT_START], M = w[TT_M], nne = w[TT_NNE];
+    const int loc = s - st;
+    if (loc < 0 || loc >= M || nne < 2) return;
+    const int root = cell_off[st];
+    int cp = loc > 0 ? cpl[s - 1] : 0;
+    int cn = loc + 1 < M ? cpl[s] : 0;
+    int L = min(max(cp, cn) + 1, g.levels);
+    int leaf = cell_off[s] + (loc == 0) + (L - cp - 1);
     int cnt = cells[leaf].count;
     double acc[6];
     if (cnt == 1) {
@@ -326,14 +417,14 @@ __global__ void k_moments(const uint64_t *__restrict__ keys, const int *__restri
             node_moment(order[s + j], x, y, z, fwd, geo, m);
             for (int k = 0; k < 6; ++k) acc[k] = rn_add(acc[k], m[k]);
         }
-        if (s > 0 && cpl[s - 1] >= L) return;   // only the first node of the run
+        if (loc > 0 && cpl[s - 1] >= L) return;   // only the first node of the run
     }
     for (int k = 0; k < 6; ++k) csum[6 * (size_t)leaf + k] = acc[k];
     finalize_cell(cells, leaf, acc, cnt);
     int cur = leaf;
     for (int guard = 0; guard < 64; ++guard) {
         int p = parent[cur];
-        if (p <= 0) break;
+        if (p <= root) break;
         __threadfence();
         int old = atomicAdd(&arrive[p], 1);
         if (old != nchild[p] - 1) break;
@@ -349,26 +440,32 @@ __global__ void k_moments(const uint64_t *__restrict__ keys, const int *__restri
     }
 }
 
-// Root: level-1 children plus the nodes outside the root box; also the
-// one-node and empty tangles.
+// Roots, one block per member: level-1 children plus the nodes outside the
+// root box; also the one-node and empty members.
 __global__ void k_root(const int *__restrict__ order, const int *__restrict__ cell_off, int *counters,
-                       const double *__restrict__ x, const double *__restrict__ y,
+                       int *tt, const double *__restrict__ x, const double *__restrict__ y,
                        const double *__restrict__ z, const int *__restrict__ fwd, Geometry geo, KeyGeom g,
                        Cell64 *cells, const double *csum, int cap_cells)
 {
     __shared__ double red[6][256];
-    int M = counters[TC_M], nne = counters[TC_NNE], nout = counters[TC_OUT];
-    int ncell = nne == 0 ? 0 : (nne >= 2 ? cell_off[M] : 1);
-    if (ncell > cap_cells) ncell = 0;   // flagged by k_cells; the host grows the storage
-    if (threadIdx.x == 0) counters[TC_NCELL] = ncell;
-    if (ncell == 0) return;
+    int *w = tt + blockIdx.x * TT_WORDS;
+    const int M = w[TT_M], nne = w[TT_NNE], st = w[TT_START], nout = nne - M;
+    const int total = cell_off[counters[TC_NNE]];
+    const bool fits = total <= cap_cells;   // else flagged by k_cells; the host grows the storage
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters[TC_NCELL] = fits ? total : 0;
+    const int root = cell_off[st], end = cell_off[st + nne];
+    if (threadIdx.x == 0) {
+        w[TT_ROOT] = (fits && nne > 0) ? root : 0;
+        w[TT_END] = (fits && nne > 0) ? end : 0;
+    }
+    if (!fits || nne == 0) return;
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int j = threadIdx.x; j < nout; j += blockDim.x) {
         double m[6];
-        node_moment(order[M + j], x, y, z, fwd, geo, m);
+        node_moment(order[st + M + j], x, y, z, fwd, geo, m);
         for (int k = 0; k < 6; ++k) acc[k] = rn_add(acc[k], m[k]);
     }
-    if (nne == 1 && M == 1 && threadIdx.x == 0) node_moment(order[0], x, y, z, fwd, geo, acc);
+    if (nne == 1 && M == 1 && threadIdx.x == 0) node_moment(order[st], x, y, z, fwd, geo, acc);
     for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = acc[k];
     __syncthreads();
     for (int off = blockDim.x / 2; off > 0; off >>= 1) {
@@ -380,7 +477,7 @@ __global__ void k_root(const int *__restrict__ order, const int *__restrict__ ce
     double sum[6];
     for (int k = 0; k < 6; ++k) sum[k] = 0;
     if (nne >= 2) {
-        for (int ch = 1; ch < ncell && ch > 0; ch = cells[ch].next)
+        for (int ch = root + 1; ch < end && ch > root; ch = cells[ch].next)
             for (int k = 0; k < 6; ++k) sum[k] = rn_add(sum[k], csum[6 * (size_t)ch + k]);
     }
     for (int k = 0; k < 6; ++k) sum[k] = rn_add(sum[k], red[k][0]);
@@ -389,9 +486,9 @@ __global__ void k_root(const int *__restrict__ order, const int *__restrict__ ce
     r.cx = rn_mul(sum[0], inv); r.cy = rn_mul(sum[1], inv); r.cz = rn_mul(sum[2], inv);
     r.qx = sum[3]; r.qy = sum[4]; r.qz = sum[5];
     r.lm = box_lm(g.lo, g.hi);
-    r.next = ncell;
+    r.next = end;
     r.count = nne;
-    cells[0] = r;
+    cells[root] = r;
 }
 
 // FP32 copy of every cell for the mixed traversal: COM split into a part on
@@ -437,7 +534,10 @@ int ov_tree_reserve(ov_ctx *c, int cap)
 {
     TreeBuf &t = c->tree;
     if (t.cap >= cap && t.keys) return OV_OK;
+    int *tt = t.tt;
+    t.tt = nullptr;
     ov_tree_free(t);
+    t.tt = tt;
     t.cap = cap;
     size_t n = (size_t)cap;
     OV_CUDA(c, cudaMalloc(&t.keys, n * 8));
@@ -452,21 +552,23 @@ int ov_tree_reserve(ov_ctx *c, int cap)
     OV_CUDA(c, cudaMalloc(&t.sort_hist, (size_t)ov_sort_hist_ints(cap) * 4));
     OV_CUDA(c, cudaMalloc(&t.counters, TC_WORDS * 4));
     OV_CUDA(c, cudaMemset(t.counters, 0, TC_WORDS * 4));
-    // cells: about 1.3 per node for filament tangles; grown on demand
-    return ov_tree_reserve_cells(c, 2 * cap + 64);
+    // cells: about 1.3 per node for filament tangles (plus a root per
+    // member); grown on demand
+    return ov_tree_reserve_cells(c, 2 * cap + 64 + (int)c->mem.size());
 }
 
 void ov_tree_free(TreeBuf &t)
 {
     void *ptrs[] = {t.keys, t.keys_alt, t.order, t.order_alt, t.torder, t.cpl, t.ncell_at, t.cell_off, t.scan_tmp,
-                    t.sort_hist, t.cells, t.cells32, t.parent, t.nchild, t.arrive, t.csum, t.counters};
+                    t.sort_hist, t.cells, t.cells32, t.parent, t.nchild, t.arrive, t.csum, t.counters, t.tt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     t = TreeBuf{};
 }
 
-static KeyGeom key_geom(const Geometry &geo)
+static KeyGeom key_geom(const ov_ctx *c)
 {
+    const Geometry &geo = c->geo;
     KeyGeom g;
     bool fast = true;
     for (int a = 0; a < 3; ++a) {
@@ -480,34 +582,44 @@ static KeyGeom key_geom(const Geometry &geo)
         if (!(bound < ldexp(1.0, -44))) fast = false;
     }
     g.fast = fast ? 1 : 0;
+    g.tb = c->key_tbits;
+    g.levels = c->key_levels;
+    g.lvmask = ((g.levels >= 21 ? ~0ull >> 1 : (1ull << (3 * g.levels)) - 1)) << (63 - g.tb - 3 * g.levels);
+    g.nt = (int)c->mem.size();
     return g;
 }
 
-// Build the tree of `na` (positions of the context's topology) on stream s.
-// Everything stays on the device, so the sequence can be graph-captured.
+// Build the tree (a forest for ensembles) of `na` with the context's
+// topology on stream s.  Everything stays on the device, so the sequence
+// can be graph-captured.
 int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
 {
     TreeBuf &t = c->tree;
     int cap = c->cap;
+    const int nt = (int)c->mem.size();
     c->tree_built = false;   // a query tree is only current until the next build
-    KeyGeom g = key_geom(c->geo);
+    if (!t.tt) return ov_fail(c, OV_ERR_STATE, "member table not allocated");
+    KeyGeom g = key_geom(c);
     OV_CUDA(c, cudaMemsetAsync(t.counters, 0, TC_BUILD_CLEAR * 4, s));
     OV_CUDA(c, cudaMemsetAsync(t.counters + TC_STAT64, 0, (TC_WORDS - TC_STAT64) * 4, s));
+    OV_CUDA(c, cudaMemsetAsync(t.tt, 0, (size_t)nt * TT_WORDS * 4, s));
     OV_CUDA(c, cudaMemsetAsync(t.nchild, 0, (size_t)t.cap_cells * 4, s));
     int nb = (cap + 255) / 256;
-    k_keys<<<nb, 256, 0, s>>>(c->status, na.x, na.y, na.z, cap, g, t.keys, t.order, t.counters);
-    c->launches++;
-    ov_sort_keys(c, t, cap, s);
-    k_cpl<<<nb, 256, 0, s>>>(t.keys, cap, t.counters, t.cpl, t.ncell_at);
-    k_target_order<<<nb, 256, 0, s>>>(t.keys, t.order, cap, t.counters, t.torder);
+    k_keys<<<nb, 256, 0, s>>>(c->status, na.x, na.y, na.z, nt > 1 ? c->d_tid : nullptr, cap, g, t.keys, t.order,
+                              t.counters, t.tt);
+    k_layout<<<1, 32, 0, s>>>(t.tt, nt, c->d_qorder, t.counters);
     c->launches += 2;
-    ov_scan_exclusive(c, t.ncell_at, t.cell_off, cap, t.counters + TC_M, 1, t.scan_tmp, s);
-    k_cells<<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, g, t.cells, t.parent, t.nchild, t.arrive,
-                               t.cap_cells);
-    k_moments<<<nb, 256, 0, s>>>(t.keys, t.order, t.cpl, t.cell_off, t.counters, na.x, na.y, na.z, c->fwd,
-                                 c->geo, t.cells, t.parent, t.nchild, t.arrive, t.csum, t.cap_cells);
-    k_root<<<1, 256, 0, s>>>(t.order, t.cell_off, t.counters, na.x, na.y, na.z, c->fwd, c->geo, g, t.cells,
-                             t.csum, t.cap_cells);
+    ov_sort_keys(c, t, cap, s);
+    k_cpl<<<nb, 256, 0, s>>>(t.keys, cap, t.counters, t.tt, g, t.cpl, t.ncell_at);
+    k_target_order<<<nb, 256, 0, s>>>(t.keys, t.order, cap, t.counters, t.tt, g, t.torder);
+    c->launches += 2;
+    ov_scan_exclusive(c, t.ncell_at, t.cell_off, cap, t.counters + TC_NNE, 0, t.scan_tmp, s);
+    k_cells<<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.parent, t.nchild,
+                               t.arrive, t.cap_cells);
+    k_moments<<<nb, 256, 0, s>>>(t.keys, t.order, t.cpl, t.cell_off, t.counters, t.tt, g, cap, na.x, na.y, na.z,
+                                 c->fwd, c->geo, t.cells, t.parent, t.nchild, t.arrive, t.csum, t.cap_cells);
+    k_root<<<nt, 256, 0, s>>>(t.order, t.cell_off, t.counters, t.tt, na.x, na.y, na.z, c->fwd, c->geo, g, t.cells,
+                              t.csum, t.cap_cells);
     c->launches += 3;
     if (c->precision == OV_PREC_MIXED) {
         k_cells32<<<(t.cap_cells + 255) / 256, 256, 0, s>>>(t.cells, t.counters, c->grid_h, 1.0 / c->grid_h,

@@ -14,6 +14,8 @@
 // reference's own correctly rounded divisions.
 #include <math.h>
 
+#include <algorithm>
+
 #include "ov_internal.cuh"
 
 #ifndef M_PI
@@ -27,6 +29,14 @@ namespace {
 
 struct VelArgs {
     const int *order, *counters;
+    const int *tt;          // per-member build table (TT_WORDS ints a member)
+    const int *qorder;      // members in work-queue order (null: id order)
+    const int *tid;         // member of each slot (null: a single tangle)
+    const DevParams *tprm;  // per-member parameters (null: prm)
+    const int2 *mrange;     // per-member slot range [x, y) (null: [0, cap))
+    int *work;              // work-queue counter
+    int nt;                 // members
+    int G;                  // query groups per node
     const Cell64 *cells;
     const Cell32 *cells32;
     const double *x, *y, *z, *tx, *ty, *tz, *nx, *ny, *nz;
@@ -223,18 +233,20 @@ __device__ __forceinline__ bool segment_law64(const double R[3], const double Rp
 
 // One Barnes-Hut query point for the 32 lanes of a warp.  `part` = lane
 // takes part; returns the lane's velocity in v.
-__device__ __forceinline__ void bh_query64(const VelArgs &a, const double q[3], bool part, int ncell,
+__device__ __forceinline__ void bh_query64(const VelArgs &a, const double q[3], bool part, int root, int ncell,
                                            double v[3], unsigned long long &visits,
                                            unsigned long long &accepts, unsigned long long &steps,
                                            bool &overflow)
+// cells of the tree: [root, ncell)
 {
     v[0] = v[1] = v[2] = 0;
     const double theta = a.prm.theta;
-    int c = 0;
+    int c = root;
     int resume = part ? 0 : 0x7fffffff;
     int guard = 0;
+    const int guard_max = 4 * (ncell - root) + 64;
     while (c < ncell) {
-        if (c < 0) { bad_index(a, 5, c); break; }
+        if (c < root) { bad_index(a, 5, c); break; }
         const Cell64 *cp = a.cells + c;
         double cx = __ldg(&cp->cx), cy = __ldg(&cp->cy), cz = __ldg(&cp->cz);
         double lm = __ldg(&cp->lm);
@@ -274,18 +286,19 @@ __device__ __forceinline__ void bh_query64(const VelArgs &a, const double q[3], 
         }
         ++steps;
         c = __any_sync(0xffffffffu, open) ? c + 1 : nxt;
-        if (++guard > 4 * ncell + 64) { overflow = true; break; }
+        if (++guard > guard_max) { overflow = true; break; }
     }
 }
 
 // LIA (tangle.c:568-592) + external v_s, given the BH sums; then vels with
 // mutual friction and PINNED_SLIP (tangle.c:689-725).
-__device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const double p[3], const double prim[3],
-                                            const double img[3], int *err, double vs_out[3], double vel_out[3])
+__device__ __forceinline__ bool finish_impl(const VelArgs &a, const DevParams &P, int id, const double p[3],
+                                            const double prim[3], const double img[3], int *err, double vs_out[3],
+                                            double vel_out[3])
 {
     int st = a.status[id];
     if (st == OV_PINNED) {
-        ext_vel(a.prm.vb_type, a.prm.vb_dir, a.prm.vb_s1, a.prm.vb_s0, a.prm.vb_tld, now(a), vel_out);
+        ext_vel(P.vb_type, P.vb_dir, P.vb_s1, P.vb_s0, P.vb_tld, now(a), vel_out);
         vs_out[0] = vs_out[1] = vs_out[2] = 0;
         return true;
     }
@@ -296,8 +309,8 @@ __device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const doub
     }
     double l_next = wrapped_len(a.geo, p, nx_);
     double l_prev = wrapped_len(a.geo, pv, p);
-    double f = rn_div(rn_div(rn_mul(a.prm.kappa,
-                              log(rn_div(rn_div(rn_mul(2.0, sqrt(rn_mul(l_next, l_prev))), sqrt(M_E)), a.prm.a0))),
+    double f = rn_div(rn_div(rn_mul(P.kappa,
+                              log(rn_div(rn_div(rn_mul(2.0, sqrt(rn_mul(l_next, l_prev))), sqrt(M_E)), P.a0))),
                          4.0),
                     M_PI);
     double tg[3] = {a.tx[id], a.ty[id], a.tz[id]}, nm[3] = {a.nx[id], a.ny[id], a.nz[id]};
@@ -305,19 +318,19 @@ __device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const doub
                     rn_mul(rn_sub(rn_mul(tg[2], nm[0]), rn_mul(tg[0], nm[2])), f),
                     rn_mul(rn_sub(rn_mul(tg[0], nm[1]), rn_mul(tg[1], nm[0])), f)};
     double ev[3];
-    ext_vel(a.prm.vs_type, a.prm.vs_dir, a.prm.vs_s1, a.prm.vs_s0, a.prm.vs_tld, now(a), ev);
+    ext_vel(P.vs_type, P.vs_dir, P.vs_s1, P.vs_s0, P.vs_tld, now(a), ev);
     for (int ax = 0; ax < 3; ++ax) vs[ax] = rn_add(rn_add(rn_add(vs[ax], ev[ax]), prim[ax]), img[ax]);
     double vel[3] = {vs[0], vs[1], vs[2]};
-    if (a.prm.friction) {
+    if (P.friction) {
         double vn[3];
-        ext_vel(a.prm.vn_type, a.prm.vn_dir, a.prm.vn_s1, a.prm.vn_s0, a.prm.vn_tld, now(a), vn);
+        ext_vel(P.vn_type, P.vn_dir, P.vn_s1, P.vn_s0, P.vn_tld, now(a), vn);
         double dv[3] = {rn_sub(vn[0], vs[0]), rn_sub(vn[1], vs[1]), rn_sub(vn[2], vs[2])};
         double c1[3] = {rn_sub(rn_mul(tg[1], dv[2]), rn_mul(tg[2], dv[1])), rn_sub(rn_mul(tg[2], dv[0]), rn_mul(tg[0], dv[2])),
                         rn_sub(rn_mul(tg[0], dv[1]), rn_mul(tg[1], dv[0]))};
-        for (int ax = 0; ax < 3; ++ax) vel[ax] = rn_add(vel[ax], rn_mul(c1[ax], a.prm.alpha));
+        for (int ax = 0; ax < 3; ++ax) vel[ax] = rn_add(vel[ax], rn_mul(c1[ax], P.alpha));
         double c2[3] = {rn_sub(rn_mul(tg[1], c1[2]), rn_mul(tg[2], c1[1])), rn_sub(rn_mul(tg[2], c1[0]), rn_mul(tg[0], c1[2])),
                         rn_sub(rn_mul(tg[0], c1[1]), rn_mul(tg[1], c1[0]))};
-        double m = -a.prm.alpha_p;
+        double m = -P.alpha_p;
         for (int ax = 0; ax < 3; ++ax) vel[ax] = rn_add(vel[ax], rn_mul(c2[ax], m));
     }
     if (st == OV_PINNED_SLIP) {
@@ -333,48 +346,109 @@ __device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const doub
     return true;
 }
 
+// finish_impl with the parameters of the node's member
+__device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const double p[3], const double prim[3],
+                                            const double img[3], int *err, double vs_out[3], double vel_out[3])
+{
+    if (a.tprm) {
+        int m = a.tid[id];
+        if (m < 0 || m >= a.nt) { bad_index(a, 8, id); return false; }
+        const DevParams P = a.tprm[m];
+        return finish_impl(a, P, id, p, prim, img, err, vs_out, vel_out);
+    }
+    return finish_impl(a, a.prm, id, p, prim, img, err, vs_out, vel_out);
+}
+
+// Work item `it` of the traversal queue: member m, its first sorted
+// position st, its node count nne, its cells [root, end), and the tile and
+// query group.  Items are (tile, group) pairs, tiles of 32 sorted targets
+// never crossing a member; members come in queue order.
+struct WorkItem {
+    int m, st, nne, root, end, tile, grp;
+};
+
+__device__ __forceinline__ WorkItem decode_item(const VelArgs &a, int it)
+{
+    WorkItem w;
+    int tile = it / a.G;
+    w.grp = it - tile * a.G;
+    int k = 0;
+    if (a.nt > 1) {
+        // last member (in queue order) whose first tile is <= tile
+        int lo = 0, hi = a.nt - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            int mm = a.qorder ? a.qorder[mid] : mid;
+            if (a.tt[mm * TT_WORDS + TT_ITEM0] <= tile) lo = mid; else hi = mid - 1;
+        }
+        k = lo;
+    }
+    w.m = a.qorder ? a.qorder[k] : k;
+    const int *t = a.tt + w.m * TT_WORDS;
+    w.st = t[TT_START];
+    w.nne = t[TT_NNE];
+    w.root = t[TT_ROOT];
+    w.end = t[TT_END];
+    w.tile = tile - t[TT_ITEM0];
+    return w;
+}
+
+// next work item of the warp (lane 0 takes it, all lanes get it)
+__device__ __forceinline__ int next_item(const VelArgs &a)
+{
+    int it = 0;
+    if ((threadIdx.x & 31) == 0) it = atomicAdd(a.work, 1);
+    return __shfl_sync(0xffffffffu, it, 0);
+}
+
 // The 1 + n_img query points of every node (qi = 0 the node itself, qi >= 1
-// image qi-1) are split over G warp groups (blockIdx.y = g takes qi = g,
-// g+G, ...) so that small tangles still fill the GPU; each group writes its
-// partial sums (own point, images) per sorted target and k_vel_finish adds
-// them in group order.
-__global__ void __launch_bounds__(128) k_vel_fp64(VelArgs a, int G, double *__restrict__ part_out)
+// image qi-1) are split over G query groups (group g takes qi = g, g+G,
+// ...) so that small tangles still fill the GPU.  Persistent warps pull
+// (tile, group) items from the work queue; each writes its partial sums
+// (own point, images) per sorted target and k_vel_finish adds them in group
+// order, so the result does not depend on which warp took which item.
+// Resident blocks per SM the register budget is sized for (about 24 warps).
+template <int W> constexpr int min_blocks() { return W == 2 ? 12 : (W == 4 ? 6 : 3); }
+template <int W> constexpr int min_blocks_mixed() { return W == 2 ? 10 : (W == 4 ? 5 : 2); }
+
+template <int W>
+__global__ void __launch_bounds__(32 * W, min_blocks<W>()) k_vel_fp64(VelArgs a, double *__restrict__ part_out)
 {
     const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int g = blockIdx.y;
-    const int nne = a.counters[TC_NNE];
-    const int ncell = a.counters[TC_NCELL];
-    if (warp * 32 >= nne) return;   // warp-uniform
-    const int tix = warp * 32 + lane;
-    bool valid = tix < nne && tix < a.cap;
-    int id = valid ? a.order[tix] : 0;
-    if (valid && (id < 0 || id >= a.cap)) { bad_index(a, 4, id); valid = false; id = 0; }
-    const int st = valid ? a.status[id] : OV_EMPTY;
-    const bool part = valid && st != OV_PINNED && st != OV_EMPTY && a.prm.use_bh;
-    double p[3] = {0, 0, 0};
-    if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
-    double prim[3] = {0, 0, 0}, img[3] = {0, 0, 0};
+    const int items = a.counters[TC_ITEMS] * a.G;
     unsigned long long visits = 0, accepts = 0, steps = 0;
     bool overflow = false;
-    for (int qi = g; qi <= a.geo.n_img; qi += G) {
-        const int j = qi - 1;
-        double q[3], v[3];
-        if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
-        else image_point(a.geo, j, p, q);
-        bh_query64(a, q, part, ncell, v, visits, accepts, steps, overflow);
-        if (j < 0) {
-            prim[0] = v[0]; prim[1] = v[1]; prim[2] = v[2];
-        } else {
-            for (int m = 0; m < a.geo.nreflect[j]; ++m) mirror_vec(a.geo.reflect[j][m], v);
-            img[0] = rn_add(img[0], v[0]); img[1] = rn_add(img[1], v[1]); img[2] = rn_add(img[2], v[2]);
+    for (int it = next_item(a); it < items; it = next_item(a)) {
+        const WorkItem w = decode_item(a, it);
+        const int loc = 32 * w.tile + lane;
+        const int tix = w.st + loc;
+        bool valid = loc < w.nne && tix < a.cap;
+        int id = valid ? a.order[tix] : 0;
+        if (valid && (id < 0 || id >= a.cap)) { bad_index(a, 4, id); valid = false; id = 0; }
+        const int st = valid ? a.status[id] : OV_EMPTY;
+        const bool part = valid && st != OV_PINNED && st != OV_EMPTY && a.prm.use_bh;
+        double p[3] = {0, 0, 0};
+        if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
+        double prim[3] = {0, 0, 0}, img[3] = {0, 0, 0};
+        for (int qi = w.grp; qi <= a.geo.n_img; qi += a.G) {
+            const int j = qi - 1;
+            double q[3], v[3];
+            if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+            else image_point(a.geo, j, p, q);
+            bh_query64(a, q, part, w.root, w.end, v, visits, accepts, steps, overflow);
+            if (j < 0) {
+                prim[0] = v[0]; prim[1] = v[1]; prim[2] = v[2];
+            } else {
+                for (int m = 0; m < a.geo.nreflect[j]; ++m) mirror_vec(a.geo.reflect[j][m], v);
+                img[0] = rn_add(img[0], v[0]); img[1] = rn_add(img[1], v[1]); img[2] = rn_add(img[2], v[2]);
+            }
         }
-    }
-    if (valid) {
-        const size_t cap = (size_t)a.cap;
-        for (int ax = 0; ax < 3; ++ax) {
-            part_out[((size_t)(2 * g) * 3 + ax) * cap + tix] = prim[ax];
-            part_out[((size_t)(2 * g + 1) * 3 + ax) * cap + tix] = img[ax];
+        if (valid) {
+            const size_t cap = (size_t)a.cap;
+            for (int ax = 0; ax < 3; ++ax) {
+                part_out[((size_t)(2 * w.grp) * 3 + ax) * cap + tix] = prim[ax];
+                part_out[((size_t)(2 * w.grp + 1) * 3 + ax) * cap + tix] = img[ax];
+            }
         }
     }
     int err = overflow ? OV_EW_ITER : 0;
@@ -393,7 +467,7 @@ __global__ void __launch_bounds__(128) k_vel_fp64(VelArgs a, int G, double *__re
 }
 
 // Sum the group partials in group order, then LIA, v_s and mutual friction.
-__global__ void k_vel_finish(VelArgs a, int G, const double *__restrict__ part_in)
+__global__ void k_vel_finish(VelArgs a, const double *__restrict__ part_in)
 {
     const int tix = blockIdx.x * blockDim.x + threadIdx.x;
     const int nne = a.counters[TC_NNE];
@@ -404,7 +478,7 @@ __global__ void k_vel_finish(VelArgs a, int G, const double *__restrict__ part_i
     if (st == OV_EMPTY) return;
     const size_t cap = (size_t)a.cap;
     double prim[3] = {0, 0, 0}, img[3] = {0, 0, 0};
-    for (int g = 0; g < G; ++g)
+    for (int g = 0; g < a.G; ++g)
         for (int ax = 0; ax < 3; ++ax) {
             prim[ax] = rn_add(prim[ax], part_in[((size_t)(2 * g) * 3 + ax) * cap + tix]);
             img[ax] = rn_add(img[ax], part_in[((size_t)(2 * g + 1) * 3 + ax) * cap + tix]);
@@ -431,11 +505,18 @@ __global__ void k_direct(VelArgs a, const int *__restrict__ nodes, int n, int ca
     int k = nodes[b];
     double p[3] = {a.x[k], a.y[k], a.z[k]};
     double acc[3] = {0, 0, 0};
+    // segments of the node's own member only
+    int lo = 0, hi = cap;
+    if (a.tid && a.mrange) {
+        int mm = a.tid[k];
+        if (mm >= 0 && mm < a.nt) { lo = a.mrange[mm].x; hi = min(a.mrange[mm].y, cap); }
+        else { bad_index(a, 9, k); hi = 0; }
+    }
     for (int j = -1; j < a.geo.n_img; ++j) {
         double q[3];
         if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
         else image_point(a.geo, j, p, q);
-        for (int m = threadIdx.x; m < cap; m += blockDim.x) {
+        for (int m = lo + threadIdx.x; m < hi; m += blockDim.x) {
             int f = a.fwd[m];
             if (f == -1) continue;
             if (j < 0 && (m == k || f == k)) continue;
@@ -607,7 +688,8 @@ struct MixedAcc {
 // lanes of a warp.  Near-field leaves are appended to the lane's list
 // (cell, image) and evaluated in FP64 after all query points.
 __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], const float f[3], const double p[3],
-                                           int j, bool part, int ncell, MixedAcc &m, int *near_list, int &nnear,
+                                           int j, bool part, int root, int ncell, MixedAcc &m, int *near_list,
+                                           int &nnear,
                                            double w64[3], bool &overflow)
 // near_list: this lane's column of a shared [kNearCap][32] array, stride 32
 {
@@ -615,14 +697,14 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
     const float near2 = a.near2f;
     const float f4pi = a.f4pif;
     const float d2lo = 1e-16f * (1.0f - 1e-5f), d2hi = 1e-16f * (1.0f + 1e-5f);
-    int c = 0;
+    int c = root;
     int resume = part ? 0 : 0x7fffffff;
-    const int guard_max = 4 * ncell + 64;
+    const int guard_max = 4 * (ncell - root) + 64;
     int steps = 0;
     // plain FP32 sub-sums, folded into the Kahan sums every 16 warp steps
     float p0 = 0, p1 = 0, p2 = 0;
     while (c < ncell) {
-        if (c < 0) { bad_index(a, 1, c); break; }
+        if (c < root) { bad_index(a, 1, c); break; }
         const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
         float4 A = __ldg(cp4), B = __ldg(cp4 + 1), Cc = __ldg(cp4 + 2);
         // A = (gx, gy, gz, fx)  B = (fy, fz, qx, qy)  Cc = (qz, lm, next, count)
@@ -708,103 +790,127 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
     m.nstep += steps;
 }
 
-__global__ void __launch_bounds__(128) k_vel_mixed(VelArgs a, int G, double *__restrict__ part_out)
+template <int W>
+__global__ void __launch_bounds__(32 * W, min_blocks_mixed<W>()) k_vel_mixed(VelArgs a, double *__restrict__ part_out)
 {
     const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int grp = blockIdx.y;
-    const int nne = a.counters[TC_NNE];
-    const int ncell = a.counters[TC_NCELL];
-    if (warp * 32 >= nne) return;
-    const int tix = warp * 32 + lane;
-    bool valid = tix < nne && tix < a.cap;
-    int id = valid ? a.order[tix] : 0;
-    if (valid && (id < 0 || id >= a.cap)) { bad_index(a, 4, id); valid = false; id = 0; }
-    const int st = valid ? a.status[id] : OV_EMPTY;
-    const bool part = valid && st != OV_PINNED && st != OV_EMPTY && a.prm.use_bh;
-    double p[3] = {0, 0, 0};
-    if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
-    float g0[3], f0[3];
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-        double G = rint(p[ax] * a.inv_h) * a.grid_h;
-        g0[ax] = (float)G;
-        f0[ax] = (float)(p[ax] - G);
-    }
-    MixedAcc m = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
-    double w64[3] = {0, 0, 0};        // FP64 sums: near field and list overflow
-    double img64[3] = {0, 0, 0};      // images with mirror reflections
-    __shared__ int s_near[4][kNearCap * 32];   // per warp: [entry][lane]
-    int *near_list = &s_near[(threadIdx.x >> 5) & 3][lane];
-    int nnear = 0;
+    const int items = a.counters[TC_ITEMS] * a.G;
+    __shared__ int s_near[W][kNearCap * 32];   // per warp: [entry][lane]
+    int *near_list = &s_near[threadIdx.x >> 5][lane];
+    unsigned visits = 0, accepts = 0, steps = 0, fallback = 0, near64 = 0;   // per lane
     bool overflow = false;
-    for (int qi = grp; qi <= a.geo.n_img; qi += G) {
-        const int j = qi - 1;
-        float g[3], f[3];
-        if (j < 0) {
-            for (int ax = 0; ax < 3; ++ax) { g[ax] = g0[ax]; f[ax] = f0[ax]; }
-        } else {
-            // image query p - L*shift: grid parts subtract exactly
-            for (int ax = 0; ax < 3; ++ax) {
-                g[ax] = g0[ax] - a.shift_g[j][ax];
-                f[ax] = f0[ax] - a.shift_f[j][ax];
+    for (int it = next_item(a); it < items; it = next_item(a)) {
+        const WorkItem w = decode_item(a, it);
+        const int loc = 32 * w.tile + lane;
+        const int tix = w.st + loc;
+        bool valid = loc < w.nne && tix < a.cap;
+        int id = valid ? a.order[tix] : 0;
+        if (valid && (id < 0 || id >= a.cap)) { bad_index(a, 4, id); valid = false; id = 0; }
+        const int st = valid ? a.status[id] : OV_EMPTY;
+        const bool part = valid && st != OV_PINNED && st != OV_EMPTY && a.prm.use_bh;
+        double p[3] = {0, 0, 0};
+        if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
+        float g0[3], f0[3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            double G = rint(p[ax] * a.inv_h) * a.grid_h;
+            g0[ax] = (float)G;
+            f0[ax] = (float)(p[ax] - G);
+        }
+        MixedAcc m = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
+        double w64[3] = {0, 0, 0};        // FP64 sums: near field and list overflow
+        double img64[3] = {0, 0, 0};      // images with mirror reflections
+        int nnear = 0;
+        for (int qi = w.grp; qi <= a.geo.n_img; qi += a.G) {
+            const int j = qi - 1;
+            float g[3], f[3];
+            if (j < 0) {
+                for (int ax = 0; ax < 3; ++ax) { g[ax] = g0[ax]; f[ax] = f0[ax]; }
+            } else {
+                // image query p - L*shift: grid parts subtract exactly
+                for (int ax = 0; ax < 3; ++ax) {
+                    g[ax] = g0[ax] - a.shift_g[j][ax];
+                    f[ax] = f0[ax] - a.shift_f[j][ax];
+                }
+            }
+            if (j >= 0 && a.geo.nreflect[j] > 0) {
+                // mirror images (wall geometries) keep their own FP64 sum
+                double q[3], v[3];
+                image_point(a.geo, j, p, q);
+                unsigned long long vi = 0, ac = 0, sp = 0;
+                bh_query64(a, q, part, w.root, w.end, v, vi, ac, sp, overflow);
+                for (int r = 0; r < a.geo.nreflect[j]; ++r) mirror_vec(a.geo.reflect[j][r], v);
+                img64[0] += v[0]; img64[1] += v[1]; img64[2] += v[2];
+                m.nvis += (unsigned)vi; m.nacc += (unsigned)ac; m.nstep += (unsigned)sp;
+                continue;
+            }
+            bh_query32(a, g, f, p, j, part, w.root, w.end, m, near_list, nnear, w64, overflow);
+        }
+        // deferred near-field interactions, all lanes together
+        for (int i = 0; i < nnear && i < kNearCap; ++i) {
+            int e = near_list[32 * i];
+            int c = e >> 5, j = (e & 31) - 1;
+            if (c < w.root || c >= w.end || j < -1 || j >= a.geo.n_img) { bad_index(a, 3, e); continue; }
+            double q[3], dxyz[3], d64, wv[3];
+            if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+            else image_point(a.geo, j, p, q);
+            decide64(a.cells + c, q, a.prm.theta, true, dxyz, &d64);
+            if (interact64(a.cells + c, dxyz, d64, a.f4pi, wv)) {
+                w64[0] += wv[0]; w64[1] += wv[1]; w64[2] += wv[2];
             }
         }
-        if (j >= 0 && a.geo.nreflect[j] > 0) {
-            // mirror images (wall geometries) keep their own FP64 sum
-            double q[3], v[3];
-            image_point(a.geo, j, p, q);
-            unsigned long long vi = 0, ac = 0, sp = 0;
-            bh_query64(a, q, part, ncell, v, vi, ac, sp, overflow);
-            for (int r = 0; r < a.geo.nreflect[j]; ++r) mirror_vec(a.geo.reflect[j][r], v);
-            img64[0] += v[0]; img64[1] += v[1]; img64[2] += v[2];
-            m.nvis += (unsigned)vi; m.nacc += (unsigned)ac; m.nstep += (unsigned)sp;
-            continue;
+        __syncwarp();   // the list is rewritten by the next item
+        double bh[3] = {((double)m.s0 - (double)m.c0) + w64[0] + img64[0],
+                        ((double)m.s1 - (double)m.c1) + w64[1] + img64[1],
+                        ((double)m.s2 - (double)m.c2) + w64[2] + img64[2]};
+        if (valid) {
+            const size_t cap = (size_t)a.cap;
+            for (int ax = 0; ax < 3; ++ax) {
+                part_out[((size_t)(2 * w.grp) * 3 + ax) * cap + tix] = bh[ax];
+                part_out[((size_t)(2 * w.grp + 1) * 3 + ax) * cap + tix] = 0.0;
+            }
         }
-        bh_query32(a, g, f, p, j, part, ncell, m, near_list, nnear, w64, overflow);
-    }
-    // deferred near-field interactions, all lanes together
-    for (int i = 0; i < nnear && i < kNearCap; ++i) {
-        int e = near_list[32 * i];
-        int c = e >> 5, j = (e & 31) - 1;
-        if (c < 0 || c >= ncell || j < -1 || j >= a.geo.n_img) { bad_index(a, 3, e); continue; }
-        double q[3], dxyz[3], d64, w[3];
-        if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
-        else image_point(a.geo, j, p, q);
-        decide64(a.cells + c, q, a.prm.theta, true, dxyz, &d64);
-        if (interact64(a.cells + c, dxyz, d64, a.f4pi, w)) {
-            w64[0] += w[0]; w64[1] += w[1]; w64[2] += w[2];
-        }
-    }
-    double bh[3] = {((double)m.s0 - (double)m.c0) + w64[0] + img64[0],
-                    ((double)m.s1 - (double)m.c1) + w64[1] + img64[1],
-                    ((double)m.s2 - (double)m.c2) + w64[2] + img64[2]};
-    if (valid) {
-        const size_t cap = (size_t)a.cap;
-        for (int ax = 0; ax < 3; ++ax) {
-            part_out[((size_t)(2 * grp) * 3 + ax) * cap + tix] = bh[ax];
-            part_out[((size_t)(2 * grp + 1) * 3 + ax) * cap + tix] = 0.0;
-        }
+        visits += m.nvis;
+        accepts += m.nacc;
+        steps += m.nstep;
+        fallback += m.nfb;
+        near64 += m.nnear;
     }
     int err = overflow ? OV_EW_ITER : 0;
-    unsigned long long visits = m.nvis, accepts = m.nacc, fallback = m.nfb, near64 = m.nnear;
+    unsigned long long v64 = visits, a64 = accepts, f64 = fallback, n64 = near64;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        visits += __shfl_xor_sync(0xffffffffu, visits, o);
-        accepts += __shfl_xor_sync(0xffffffffu, accepts, o);
-        fallback += __shfl_xor_sync(0xffffffffu, fallback, o);
-        near64 += __shfl_xor_sync(0xffffffffu, near64, o);
+        v64 += __shfl_xor_sync(0xffffffffu, v64, o);
+        a64 += __shfl_xor_sync(0xffffffffu, a64, o);
+        f64 += __shfl_xor_sync(0xffffffffu, f64, o);
+        n64 += __shfl_xor_sync(0xffffffffu, n64, o);
         err |= __shfl_xor_sync(0xffffffffu, err, o);
     }
     if (lane == 0) {
-        atomicAdd(&a.stat[ST_VISITS], visits);
-        atomicAdd(&a.stat[ST_ACCEPTS], accepts);
-        atomicAdd(&a.stat[ST_STEPS], (unsigned long long)m.nstep);
-        atomicAdd(&a.stat[ST_FALLBACK], fallback);
-        atomicAdd(&a.stat[ST_NEAR64], near64);
+        atomicAdd(&a.stat[ST_VISITS], v64);
+        atomicAdd(&a.stat[ST_ACCEPTS], a64);
+        atomicAdd(&a.stat[ST_STEPS], (unsigned long long)steps);
+        atomicAdd(&a.stat[ST_FALLBACK], f64);
+        atomicAdd(&a.stat[ST_NEAR64], n64);
         if (err) atomicOr((int *)&a.counters[TC_ERR], err);
     }
 }
+
+}  // namespace
+
+// Query groups per node: the tuned value, else enough warps for ~32 per SM
+// on small tangles.
+int ov_query_groups(ov_ctx *c)
+{
+    int maxg = c->geo.n_img + 1;
+    if (c->tune.groups > 0) return std::min(c->tune.groups, std::min(maxg, 27));
+    int warps = (c->cap + 31) / 32;
+    int G = (32 * c->sm_count + warps - 1) / warps;
+    G = G < 1 ? 1 : (G > 8 ? 8 : G);
+    return std::min(G, maxg);
+}
+
+namespace {
 
 VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long *stat)
 {
@@ -838,6 +944,15 @@ VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long 
         }
     a.stat = stat;
     a.cap = c->cap;
+    const bool ens = c->mem.size() > 1;
+    a.tt = c->tree.tt;
+    a.qorder = ens ? c->d_qorder : nullptr;
+    a.tid = ens ? c->d_tid : nullptr;
+    a.tprm = ens ? c->d_tprm : nullptr;
+    a.mrange = ens ? c->d_mrange : nullptr;
+    a.work = c->tree.counters + TC_WORK;
+    a.nt = (int)c->mem.size();
+    a.G = ov_query_groups(c);
     a.th2f = (float)(a.prm.theta * a.prm.theta);
     a.near2f = (float)a.near2;
     a.f4pif = (float)a.f4pi;
@@ -853,14 +968,6 @@ void ov_launch_tangents(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     c->launches++;
 }
 
-// Query groups per node: enough warps for ~32 per SM on small tangles.
-int ov_query_groups(ov_ctx *c)
-{
-    int warps = (c->cap + 31) / 32;
-    int G = (32 * c->sm_count + warps - 1) / warps;
-    return G < 1 ? 1 : (G > 8 ? 8 : G);
-}
-
 int ov_reserve_velocity_scratch(ov_ctx *c)
 {
     int G = ov_query_groups(c);
@@ -874,6 +981,38 @@ int ov_reserve_velocity_scratch(ov_ctx *c)
     return OV_OK;
 }
 
+// Traversal kernel for a precision and block shape.
+typedef void (*VelKernel)(VelArgs, double *);
+static VelKernel vel_kernel(int precision, int warps)
+{
+    if (precision == OV_PREC_MIXED) {
+        if (warps == 2) return k_vel_mixed<2>;
+        if (warps == 8) return k_vel_mixed<8>;
+        return k_vel_mixed<4>;
+    }
+    if (warps == 2) return k_vel_fp64<2>;
+    if (warps == 8) return k_vel_fp64<8>;
+    return k_vel_fp64<4>;
+}
+
+// Persistent grid: resident blocks per SM (tuned or the occupancy limit) on
+// every SM, but no more blocks than there can be work items.
+int ov_traversal_blocks(ov_ctx *c, int precision, int warps, int *per_sm)
+{
+    VelKernel k = vel_kernel(precision, warps);
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * warps, 0) != cudaSuccess || occ < 1) {
+        cudaGetLastError();
+        occ = 1;
+    }
+    int bps = c->tune.blocks_per_sm > 0 ? std::min(c->tune.blocks_per_sm, occ) : occ;
+    if (per_sm) *per_sm = occ;
+    long long items = ((long long)(c->cap + 31) / 32 + (long long)c->mem.size()) * ov_query_groups(c);
+    long long need = (items + warps - 1) / warps;
+    long long blocks = std::min((long long)bps * c->sm_count, need);
+    return (int)std::max(1LL, blocks);
+}
+
 int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s)
 {
     VelArgs a = make_args(c, na, t, ov_stat_ptr(c));
@@ -881,17 +1020,14 @@ int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precisio
         a.t_dev = c->d_time;
         a.t_index = c->time_dev_index;
     }
-    int G = ov_query_groups(c);
     int r = ov_reserve_velocity_scratch(c);
     if (r) return r;
-    int warps = (c->cap + 31) / 32;
-    int threads = 128;
-    dim3 grid((warps * 32 + threads - 1) / threads, G);
-    if (precision == OV_PREC_MIXED)
-        k_vel_mixed<<<grid, threads, 0, s>>>(a, G, c->part);
-    else
-        k_vel_fp64<<<grid, threads, 0, s>>>(a, G, c->part);
-    k_vel_finish<<<(c->cap + 127) / 128, 128, 0, s>>>(a, G, c->part);
+    int warps = c->tune.warps;
+    if (warps != 2 && warps != 8) warps = 4;
+    int blocks = ov_traversal_blocks(c, precision, warps, nullptr);
+    OV_CUDA(c, cudaMemsetAsync(a.work, 0, sizeof(int), s));
+    vel_kernel(precision, warps)<<<blocks, 32 * warps, 0, s>>>(a, c->part);
+    k_vel_finish<<<(c->cap + 127) / 128, 128, 0, s>>>(a, c->part);
     c->launches += 2;
     return OV_OK;
 }
@@ -935,7 +1071,7 @@ __global__ void __launch_bounds__(128) k_query64(VelArgs a, const double *__rest
     unsigned long long visits = 0, accepts = 0, steps = 0;
     bool overflow = false;
     double v[3];
-    bh_query64(a, q, valid, a.counters[TC_NCELL], v, visits, accepts, steps, overflow);
+    bh_query64(a, q, valid, 0, a.counters[TC_NCELL], v, visits, accepts, steps, overflow);
     if (valid) { out[3 * i] = v[0]; out[3 * i + 1] = v[1]; out[3 * i + 2] = v[2]; }
     if (overflow && lane == 0) atomicOr((int *)&a.counters[TC_ERR], OV_EW_ITER);
 }
@@ -945,6 +1081,7 @@ extern "C" int ov_tree_velocity_at(ov_ctx *c, const double *points, int n, doubl
 {
     if (!c || n < 0 || (n > 0 && (!points || !out))) return OV_ERR_ARG;
     if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
+    if (c->mem.size() > 1) return ov_fail(c, OV_ERR_STATE, "tree queries need a single tangle, not an ensemble");
     cudaSetDevice(c->device);
     if (rebuild || !c->tree_built) {
         OV_CUDA(c, cudaMemsetAsync(c->tree.counters + TC_ERR, 0, (TC_COUNT - TC_ERR) * 4, c->stream));

@@ -79,6 +79,14 @@ def load(path: str | None = None):
         "ov_measure_fma_peak": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
         "ov_set_rk4_graph": (C.c_int, [P, C.c_int]),
         "ov_tangle_info": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "ov_upload_ensemble": (C.c_int, [P, C.POINTER(TS), C.POINTER(abi.Params), C.c_int, C.c_double]),
+        "ov_ensemble_size": (C.c_int, [P]),
+        "ov_member_info": (C.c_int, [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "ov_download_member": (C.c_int, [P, C.c_int, TS, C.c_uint]),
+        "ov_set_member_params": (C.c_int, [P, C.c_int, C.POINTER(abi.Params)]),
+        "ov_get_tuning": (C.c_int, [P, C.POINTER(abi.Tuning)]),
+        "ov_set_tuning": (C.c_int, [P, C.POINTER(abi.Tuning)]),
+        "ov_autotune": (C.c_int, [P, C.c_double, C.POINTER(abi.Tuning), C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -101,6 +109,20 @@ def declared_symbols() -> list[str]:
         for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b((?:ov|ovd)_\w+)\s*\(", txt, flags=re.M):
             names.append(m.group(1))
     return sorted(set(names))
+
+
+def _grown(host, n: int):
+    """`host`, or a copy of it grown to n slots (new slots EMPTY)."""
+    from .workloads import HostTangle
+    if n <= host.n:
+        return host
+    pos = np.zeros((n, 3))
+    pos[:host.n] = host.pos
+    fwd = np.full(n, -1)
+    rev = np.full(n, -1)
+    st = np.full(n, abi.OV_EMPTY)
+    fwd[:host.n], rev[:host.n], st[:host.n] = host.conn[:, 0], host.conn[:, 1], host.stat[:, 0]
+    return HostTangle(pos, fwd, rev, host.box_lo, host.box_hi, n_images=host.n_images, status=st)
 
 
 class Context:
@@ -159,6 +181,52 @@ class Context:
         self._state = host.state()
         self._check(self.lib.ov_upload_tangle_fields(self._h, C.byref(self._state), fields))
 
+    def upload_ensemble(self, hosts, params, headroom: float = 2.0):
+        """hosts: HostTangles; params: one abi.Params per member."""
+        self._members = list(hosts)
+        self._mstates = [h.state() for h in self._members]
+        arr = (C.POINTER(abi.TangleState) * len(hosts))(*[C.pointer(st) for st in self._mstates])
+        parr = (abi.Params * len(params))(*params)
+        self._check(self.lib.ov_upload_ensemble(self._h, arr, parr, len(hosts), headroom))
+        self._host = None
+
+    @property
+    def ensemble_size(self) -> int:
+        return self.lib.ov_ensemble_size(self._h)
+
+    def member_info(self, i: int) -> tuple[int, int, int]:
+        n, ne, te = C.c_int(0), C.c_int(0), C.c_int(0)
+        self._check(self.lib.ov_member_info(self._h, i, C.byref(n), C.byref(ne), C.byref(te)))
+        return n.value, ne.value, te.value
+
+    def download_member(self, i: int, host=None, fields: int = abi.OV_F_ALL):
+        """Download member i into `host` (default: the uploaded one), grown
+        to the member's slot count when remesh has expanded it."""
+        host = host if host is not None else self._members[i]
+        n, _, _ = self.member_info(i)
+        host = _grown(host, n)
+        st = host.state()
+        self._check(self.lib.ov_download_member(self._h, i, C.byref(st), fields))
+        return host
+
+    def set_member_params(self, i: int, p: abi.Params):
+        self._check(self.lib.ov_set_member_params(self._h, i, C.byref(p)))
+
+    def get_tuning(self) -> abi.Tuning:
+        tu = abi.Tuning()
+        self._check(self.lib.ov_get_tuning(self._h, C.byref(tu)))
+        return tu
+
+    def set_tuning(self, warps_per_block: int = 4, query_groups: int = 0, blocks_per_sm: int = 0,
+                   largest_first: int = 1):
+        tu = abi.Tuning(warps_per_block, query_groups, blocks_per_sm, largest_first)
+        self._check(self.lib.ov_set_tuning(self._h, C.byref(tu)))
+
+    def autotune(self, t: float = 0.0) -> tuple[dict, float]:
+        tu, ms = abi.Tuning(), C.c_float(0)
+        self._check(self.lib.ov_autotune(self._h, t, C.byref(tu), C.byref(ms)))
+        return {f: getattr(tu, f) for f, _ in tu._fields_}, ms.value
+
     def tangle_info(self) -> tuple[int, int, int]:
         n, ne, te = C.c_int(0), C.c_int(0), C.c_int(0)
         self._check(self.lib.ov_tangle_info(self._h, C.byref(n), C.byref(ne), C.byref(te)))
@@ -166,17 +234,8 @@ class Context:
 
     def download_resized(self, host):
         """Download into a copy of `host` grown to the context's slot count."""
-        from .workloads import HostTangle
         n, _, _ = self.tangle_info()
-        if n > host.n:
-            pos = np.zeros((n, 3))
-            pos[:host.n] = host.pos
-            fwd = np.full(n, -1)
-            rev = np.full(n, -1)
-            st = np.full(n, abi.OV_EMPTY)
-            fwd[:host.n], rev[:host.n], st[:host.n] = host.conn[:, 0], host.conn[:, 1], host.stat[:, 0]
-            host = HostTangle(pos, fwd, rev, host.box_lo, host.box_hi, n_images=host.n_images, status=st)
-        return self.download(host)
+        return self.download(_grown(host, n))
 
     def download(self, host=None, fields: int = abi.OV_F_ALL):
         host = host or self._host

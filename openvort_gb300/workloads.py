@@ -252,6 +252,12 @@ def ensemble(n_tangles: int = 48, min_nodes: int = 2048, max_nodes: int = 131072
     return out
 
 
+def member_params(m: EnsembleMember, **over) -> abi.Params:
+    """Run parameters of one ensemble member: the random-walk set with the
+    member's alpha, alpha' and v_n (along x)."""
+    return config_params("rw", alpha=m.alpha, alpha_p=m.alpha_p, vn=(abi.OV_SIMPLE, m.vn, (1, 0, 0)), **over)
+
+
 def config_params(name: str, **over) -> abi.Params:
     """Run parameters of the named benchmark configuration."""
     base = dict(kappa=9.97e-4, vortex_width=1.3e-8, alpha=0.098, alpha_p=0.016, use_bh=1,
