@@ -254,12 +254,15 @@ def run_ensemble(args, device=0):
     ctx.upload_ensemble(hosts, params, headroom=2.0)
     K = args.ensemble_steps
     recs = added = 0
+    passes = {}
     t0 = time.perf_counter()
     for k in range(K):
         ctx.step(k * dt, dt)
         s2 = ctx.stats()
         recs += s2["reconnections"]
         added += s2["remesh_added"]
+        for name, v in ctx.step_times().items():
+            passes[name] = passes.get(name, 0.0) + v / K
     ctx.synchronize()
     full_ms = (time.perf_counter() - t0) * 1e3 / max(1, K)
     n_end = sum(ctx.member_info(i)[0] - ctx.member_info(i)[2] for i in range(len(hosts)))
@@ -278,6 +281,7 @@ def run_ensemble(args, device=0):
                       "node_evals_per_s": 4 * n / (rk4_ms * 1e-3)},
         "full_steps_mixed": {"steps": K, "ms_per_step_wall": full_ms, "steps_per_s": 1e3 / full_ms,
                              "reconnections": recs, "remesh_added": added, "live_nodes_end": n_end,
+                             "pass_ms": passes,
                              "includes": "small loops x3, reconnect, periodic wrap, remesh, update_tangle, "
                                          "rk4_step (graph), per step; host wall clock"},
     }

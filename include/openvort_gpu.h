@@ -274,6 +274,12 @@ int ov_smooth(ov_ctx *ctx);
    loops, smooth, periodic wrap, remesh, small loops, update_tangle, rk4_step,
    periodic wrap. */
 int ov_step(ov_ctx *ctx, double t, double dt);
+/* Host wall-clock milliseconds of the last ov_step, per pass: [0] small
+   loops (three calls), [1] reconnect, [2] smooth, [3] periodic wrap (two
+   calls), [4] remesh, [5] update_tangle, [6] rk4_step, [7] the whole step;
+   reconnect's parts: [8] mirror + candidate pairs, [9] direct sums,
+   [10] sequential decisions, [11] push.  Writes min(n, 12) values. */
+int ov_step_times(const ov_ctx *ctx, double *ms, int n);
 
 int ov_get_stats(const ov_ctx *ctx, ov_stats *out);
 

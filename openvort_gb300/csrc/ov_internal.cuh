@@ -195,6 +195,7 @@ struct ov_ctx {
     std::vector<double> h_x, h_y, h_z;
     std::vector<int> h_fwd, h_rev, h_status, h_pin, h_recalc;
     bool host_valid = false;     // the mirrors equal the device positions and topology
+    double step_ms[12] = {};     // host wall time of the last ov_step's passes (+ reconnect parts)
     // reconnect / smoothing scratch
     uint64_t *d_gkeys = nullptr, *d_gkeys_alt = nullptr;
     int *d_gidx = nullptr, *d_gidx_alt = nullptr;

@@ -27,6 +27,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <vector>
 
 #include "ov_internal.cuh"
@@ -967,10 +968,17 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
 {
     int r = ready(c);
     if (r) return r;
+    auto clk = [] { return std::chrono::steady_clock::now(); };
+    auto ms_since = [&](std::chrono::steady_clock::time_point t0) {
+        return std::chrono::duration<double, std::milli>(clk() - t0).count();
+    };
+    auto tr = clk();
     if ((r = ov_pull_host(c))) return r;
     c->host_valid = false;
     std::vector<std::pair<int, int>> pairs;
     if ((r = find_pairs(c, pairs))) return r;
+    c->step_ms[8] = ms_since(tr);
+    tr = clk();
     const int N = c->n_live;
     // direct sums of every candidate node on the pass's starting topology
     std::vector<int> cand;
@@ -980,6 +988,8 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
     std::vector<double> sums(3 * cand.size());
     if (!cand.empty() && (r = ov_direct_raw(c, cand.data(), (int)cand.size(), sums.data()))) return r;
+    c->step_ms[9] = ms_since(tr);
+    tr = clk();
     auto cand_index = [&](int k) {
         return (int)(std::lower_bound(cand.begin(), cand.end(), k) - cand.begin());
     };
@@ -1105,7 +1115,13 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     }
     c->stats.reconnections = nrec;
     if (nrecs) *nrecs = nrec;
-    if (nrec) return ov_push_device(c, 0);
+    c->step_ms[10] = ms_since(tr);
+    tr = clk();
+    if (nrec) {
+        r = ov_push_device(c, 0);
+        c->step_ms[11] = ms_since(tr);
+        return r;
+    }
     c->host_valid = true;
     return OV_OK;
 }
@@ -1197,17 +1213,45 @@ int ov_step(ov_ctx *c, double t, double dt)
     int r = ready(c);
     if (r) return r;
     int nrec = 0;
+    // host wall time of each pass: small loops, reconnect, smooth, periodic,
+    // remesh, update_tangle, rk4_step, total
+    double *ms = c->step_ms;
+    for (int i = 0; i < 12; ++i) ms[i] = 0;
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    auto since = [&](std::chrono::steady_clock::time_point t0) {
+        return std::chrono::duration<double, std::milli>(now() - t0).count();
+    };
+    const auto t_all = now();
+    auto t0 = now();
     if ((r = ov_eliminate_small_loops(c))) return r;
+    ms[0] += since(t0); t0 = now();
     if ((r = ov_reconnect(c, 0.0, &nrec, nullptr, nullptr, 0))) return r;
+    ms[1] += since(t0); t0 = now();
     if ((r = ov_eliminate_small_loops(c))) return r;
+    ms[0] += since(t0); t0 = now();
     if ((r = ov_smooth(c))) return r;
+    ms[2] += since(t0); t0 = now();
     if ((r = ov_enforce_periodic_boundaries(c))) return r;
+    ms[3] += since(t0); t0 = now();
     if ((r = ov_remesh(c, c->params.dl_min, c->params.dl_max, 0.0))) return r;
+    ms[4] += since(t0); t0 = now();
     if ((r = ov_eliminate_small_loops(c))) return r;
+    ms[0] += since(t0); t0 = now();
     if ((r = ov_update_tangle(c, t))) return r;
+    ms[5] += since(t0); t0 = now();
     if ((r = ov_rk4_step(c, t, dt))) return r;
+    ms[6] += since(t0); t0 = now();
     if ((r = ov_enforce_periodic_boundaries(c))) return r;
+    ms[3] += since(t0);
+    ms[7] = since(t_all);
     c->stats.reconnections = nrec;
+    return OV_OK;
+}
+
+int ov_step_times(const ov_ctx *c, double *ms, int n)
+{
+    if (!c || !ms || n < 0) return OV_ERR_ARG;
+    for (int i = 0; i < n && i < 12; ++i) ms[i] = c->step_ms[i];
     return OV_OK;
 }
 

@@ -361,17 +361,19 @@ __device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const doub
 
 // Work item `it` of the traversal queue: member m, its first sorted
 // position st, its node count nne, its cells [root, end), and the tile and
-// query group.  Items are (tile, group) pairs, tiles of 32 sorted targets
-// never crossing a member; members come in queue order.
+// query group.  Items are (group, tile) pairs, group-major: warps running at
+// the same time share the query points' image set and walk nearby targets,
+// so they touch the same cells.  Tiles of 32 sorted targets never cross a
+// member; members come in queue order.
 struct WorkItem {
     int m, st, nne, root, end, tile, grp;
 };
 
-__device__ __forceinline__ WorkItem decode_item(const VelArgs &a, int it)
+__device__ __forceinline__ WorkItem decode_item(const VelArgs &a, int it, int tiles)
 {
     WorkItem w;
-    int tile = it / a.G;
-    w.grp = it - tile * a.G;
+    w.grp = it / tiles;
+    int tile = it - w.grp * tiles;
     int k = 0;
     if (a.nt > 1) {
         // last member (in queue order) whose first tile is <= tile
@@ -415,11 +417,12 @@ template <int W>
 __global__ void __launch_bounds__(32 * W, min_blocks<W>()) k_vel_fp64(VelArgs a, double *__restrict__ part_out)
 {
     const int lane = threadIdx.x & 31;
-    const int items = a.counters[TC_ITEMS] * a.G;
+    const int tiles = a.counters[TC_ITEMS];
+    const int items = tiles * a.G;
     unsigned long long visits = 0, accepts = 0, steps = 0;
     bool overflow = false;
     for (int it = next_item(a); it < items; it = next_item(a)) {
-        const WorkItem w = decode_item(a, it);
+        const WorkItem w = decode_item(a, it, tiles);
         const int loc = 32 * w.tile + lane;
         const int tix = w.st + loc;
         bool valid = loc < w.nne && tix < a.cap;
@@ -794,13 +797,14 @@ template <int W>
 __global__ void __launch_bounds__(32 * W, min_blocks_mixed<W>()) k_vel_mixed(VelArgs a, double *__restrict__ part_out)
 {
     const int lane = threadIdx.x & 31;
-    const int items = a.counters[TC_ITEMS] * a.G;
+    const int tiles = a.counters[TC_ITEMS];
+    const int items = tiles * a.G;
     __shared__ int s_near[W][kNearCap * 32];   // per warp: [entry][lane]
     int *near_list = &s_near[threadIdx.x >> 5][lane];
     unsigned visits = 0, accepts = 0, steps = 0, fallback = 0, near64 = 0;   // per lane
     bool overflow = false;
     for (int it = next_item(a); it < items; it = next_item(a)) {
-        const WorkItem w = decode_item(a, it);
+        const WorkItem w = decode_item(a, it, tiles);
         const int loc = 32 * w.tile + lane;
         const int tix = w.st + loc;
         bool valid = loc < w.nne && tix < a.cap;

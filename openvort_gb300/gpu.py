@@ -87,6 +87,7 @@ def load(path: str | None = None):
         "ov_get_tuning": (C.c_int, [P, C.POINTER(abi.Tuning)]),
         "ov_set_tuning": (C.c_int, [P, C.POINTER(abi.Tuning)]),
         "ov_autotune": (C.c_int, [P, C.c_double, C.POINTER(abi.Tuning), C.POINTER(C.c_float)]),
+        "ov_step_times": (C.c_int, [P, C.POINTER(C.c_double), C.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -288,6 +289,15 @@ class Context:
 
     def step(self, t: float, dt: float):
         self._check(self.lib.ov_step(self._h, t, dt))
+
+    STEP_PASSES = ("small_loops", "reconnect", "smooth", "periodic", "remesh", "update_tangle", "rk4_step",
+                   "total", "reconnect_pairs", "reconnect_direct_sums", "reconnect_decisions", "reconnect_push")
+
+    def step_times(self) -> dict:
+        """Host wall ms of the last step(), per pass."""
+        ms = (C.c_double * 12)()
+        self._check(self.lib.ov_step_times(self._h, ms, 12))
+        return dict(zip(self.STEP_PASSES, list(ms)))
 
     @property
     def capacity(self) -> int:
