@@ -206,6 +206,14 @@ int ov_rk4_step(ov_ctx *ctx, double t, double dt);
 int ov_direct_velocities(ov_ctx *ctx, const int *nodes, int n, double t,
                          double *vels_out, double *vs_out);
 
+/* The nonlocal part of the direct sum (segments of the node's own tangle and
+   every image, without LIA or external/friction terms) for n nodes, as
+   reconnect uses it.  precision OV_PREC_MIXED: far segments in FP32 on
+   grid-split positions, near ones in FP64; OV_PREC_FP64: all in FP64.
+   out (host, 5 doubles per node): the three components, a bound on each
+   component's error, and the sum of the terms' magnitudes. */
+int ov_direct_sums_bounded(ov_ctx *ctx, const int *nodes, int n, int precision, double *out);
+
 /* Largest node list one ov_direct_velocities_noalloc call accepts. */
 #define OV_NOALLOC_MAX_NODES 4096
 

@@ -220,6 +220,13 @@ struct ov_ctx {
     // per-group partial velocity sums of the traversal (6 doubles x groups x cap)
     double *part = nullptr;
     size_t part_cap = 0;
+    // reconnection velocities: candidate list, sums + bounds, corrections,
+    // split positions, per-block partials
+    int *rec_nodes = nullptr, *rec_pair = nullptr;
+    double *rec_out = nullptr, *rec_corr = nullptr, *rec_part = nullptr;
+    float *rec_split = nullptr;
+    int rec_cap = 0, rec_split_cap = 0;
+    size_t rec_part_cap = 0;
     // direct-sum scratch
     double *dsum = nullptr;
     int dsum_cap = 0;
@@ -276,6 +283,11 @@ int ov_reserve_velocity_scratch(ov_ctx *c);
 int ov_query_groups(ov_ctx *c);
 int ov_traversal_blocks(ov_ctx *c, int precision, int warps, int *per_sm);
 int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out);
+// reconnection velocities (ov_velocity.cu)
+int ov_rec_begin(ov_ctx *c, const int *cand, int n, double *out);
+int ov_rec_exact(ov_ctx *c, int k, int l, double out[10]);
+int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const double *sign, int nch,
+                   double *corr_out);
 void ov_launch_euler(ov_ctx *c, const NodeArrays &src, const double *vx, const double *vy,
                      const double *vz, double dt, NodeArrays &dst, cudaStream_t s);
 void ov_launch_rk4_combine(ov_ctx *c, double dt, cudaStream_t s);

@@ -17,9 +17,12 @@
 //     key sort of the nodes (cell side >= 2 rec_dist, so 27 neighbour cells
 //     are enough even for nodes within rounding of a cell face), and the
 //     O(N (1+n_img)) direct-sum velocities of every candidate node in one
-//     batch; rewiring changes four segments, whose contributions the host
-//     subtracts/adds for later candidates, and a decision whose dx.dv sits
-//     within 1e-9 of zero is recomputed in the reference's summation order;
+//     batch, in mixed precision with a rigorous error bound; rewiring
+//     changes four segments, whose contributions are added to every
+//     remaining candidate of the member on the device; a decision the bound
+//     cannot settle gets FP64 sums, and one whose dx.dv is still within the
+//     error of the reference's own summation is recomputed in the
+//     reference's summation order;
 //   * smoothing: one block per closed loop (the loop decomposition is host
 //     work): unwrap, optional detrend / odd extension, low-pass DFT on the
 //     kept bins only, write back.
@@ -899,11 +902,6 @@ int find_pairs(ov_ctx *c, std::vector<std::pair<int, int>> &out)
     return ov_fail(c, OV_ERR_ALLOC, "candidate pair buffer could not be sized");
 }
 
-struct SegChange {
-    int m, f;
-    double sign;   // +1 added, -1 removed
-};
-
 }  // namespace
 
 extern "C" {
@@ -980,20 +978,22 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     c->step_ms[8] = ms_since(tr);
     tr = clk();
     const int N = c->n_live;
-    // direct sums of every candidate node on the pass's starting topology
+    // direct sums of every candidate node on the pass's starting topology:
+    // mixed precision with an error bound (rec[4 i + 3]), FP64 on demand
     std::vector<int> cand;
     cand.reserve(2 * pairs.size());
     for (auto &pr : pairs) { cand.push_back(pr.first); cand.push_back(pr.second); }
     std::sort(cand.begin(), cand.end());
     cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
-    std::vector<double> sums(3 * cand.size());
-    if (!cand.empty() && (r = ov_direct_raw(c, cand.data(), (int)cand.size(), sums.data()))) return r;
+    const int C = (int)cand.size();
+    std::vector<double> rec(5 * (size_t)C), corr(3 * (size_t)C, 0.0);
+    std::vector<char> exact(C, 0);
+    if (C && (r = ov_rec_begin(c, cand.data(), C, rec.data()))) return r;
     c->step_ms[9] = ms_since(tr);
     tr = clk();
     auto cand_index = [&](int k) {
         return (int)(std::lower_bound(cand.begin(), cand.end(), k) - cand.begin());
     };
-    std::vector<SegChange> changes;   // of the member being processed
     std::vector<int> &recalc = c->h_recalc;
     recalc.assign(N, 0);
     const Geometry &g = c->geo;
@@ -1008,32 +1008,26 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         }
         return lo;
     };
-    int cur_member = -1;
+    int cur_member = -1, cb = 0, ce = 0;   // the member's candidates [cb, ce)
     Host h = host_of(c, 0);
     double cos_cut = 0;
 
-    // velocity of an unflagged candidate node on the current topology
-    auto velocity = [&](int k, const double tg[3], const double nm[3], double vel[3]) -> bool {
+    // velocity of an unflagged candidate node on the current topology, and a
+    // bound on how far it may sit from the reference's update_velocity: the
+    // error of our sum plus the rounding of the reference's own sequential
+    // sum of 27 N terms (at most (27 N - 1) eps64 times their magnitudes)
+    auto velocity = [&](int k, const double tg[3], const double nm[3], double vel[3], double *bound) -> bool {
         double vs[3];
         if (!hlia(h, k, tg, nm, t, vs)) return false;
         int ci = cand_index(k);
-        double nl[3] = {sums[3 * ci], sums[3 * ci + 1], sums[3 * ci + 2]};
-        if (!changes.empty()) {
-            double x[3];
-            h.pos(k, x);
-            for (const SegChange &sc : changes) {
-                for (int j = -1; j < g.n_img; ++j) {
-                    double q[3];
-                    if (j < 0) { q[0] = x[0]; q[1] = x[1]; q[2] = x[2]; }
-                    else himage(g, j, x, q);
-                    double w[3];
-                    if (hsegment(h, sc.m, sc.f, q, w))
-                        for (int a = 0; a < 3; ++a) nl[a] += sc.sign * w[a];
-                }
-            }
-        }
-        for (int a = 0; a < 3; ++a) vs[a] = vs[a] + nl[a];
+        const double *rc = &rec[5 * (size_t)ci];
+        for (int a = 0; a < 3; ++a) vs[a] = vs[a] + (rc[a] + corr[3 * (size_t)ci + a]);
         hfriction(h, k, tg, vs, t, vel);
+        const double tl = hlen(tg);
+        const double n_terms = (double)(h.hi - h.lo) * (g.n_img + 1);
+        const double comp = rc[3] + n_terms * 1.1102230246251565e-16 * rc[4];
+        // the friction terms are linear in vs: |d vel| <= |d vs| (1 + alpha |t| + alpha' |t|^2)
+        *bound = comp * 1.7320508075688772 * 1.01 * (1.0 + fabs(h.P->alpha) * tl + fabs(h.P->alpha_p) * tl * tl);
         return true;
     };
 
@@ -1046,8 +1040,10 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         if (mk != cur_member) {
             cur_member = mk;
             h = host_of(c, mk);
-            changes.clear();
             cos_cut = cos(h.P->reconnection_angle_cutoff);
+            const Member &M = c->mem[mk];
+            cb = cand_index(M.lo);
+            ce = cand_index(M.lo + M.cap);
         }
         int sk = h.st(k);
         if (sk == OV_EMPTY || pinned(sk) || recalc[k]) { i = e; continue; }
@@ -1060,8 +1056,8 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
                 return ov_fail(c, OV_ERR_TOPOLOGY, "reconnect: filament walk from %d or %d failed", k, l);
             if (hlen(tk) < 0.5 || hlen(tl) < 0.5) continue;
             if (hdot(tk, tl) / hlen(tk) / hlen(tl) > cos_cut) continue;
-            double vk[3], vl[3];
-            if (!velocity(k, tk, nk, vk) || !velocity(l, tl, nl_, vl))
+            double vk[3], vl[3], bk = 0, bl = 0;
+            if (!velocity(k, tk, nk, vk, &bk) || !velocity(l, tl, nl_, vl, &bl))
                 return ov_fail(c, OV_ERR_TOPOLOGY, "reconnect: velocity of %d or %d failed", k, l);
             double v1[3], v2[3], dx[3], dv[3];
             h.pos(k, v1);
@@ -1070,7 +1066,24 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
             hsub(dx, v1, v2);
             hsub(dv, vk, vl);
             double proj = hdot(dx, dv);
-            if (fabs(proj) <= 1e-9 * hlen(dx) * hlen(dv)) {
+            if (fabs(proj) <= hlen(dx) * (bk + bl) + 1e-9 * hlen(dx) * hlen(dv)) {
+                // the mixed-precision sums cannot decide: FP64 sums of both
+                int ck = cand_index(k), cl = cand_index(l);
+                if (!exact[ck] || !exact[cl]) {
+                    double ex[10];
+                    if ((r = ov_rec_exact(c, k, l, ex))) return r;
+                    for (int a = 0; a < 5; ++a) {
+                        rec[5 * (size_t)ck + a] = ex[a];
+                        rec[5 * (size_t)cl + a] = ex[5 + a];
+                    }
+                    exact[ck] = exact[cl] = 1;
+                    velocity(k, tk, nk, vk, &bk);
+                    velocity(l, tl, nl_, vl, &bl);
+                    hsub(dv, vk, vl);
+                    proj = hdot(dx, dv);
+                }
+            }
+            if (fabs(proj) <= hlen(dx) * (bk + bl) + 1e-9 * hlen(dx) * hlen(dv)) {
                 // too close to call after a different summation order: redo
                 // both velocities exactly as the reference sums them
                 hdirect_exact(h, k, tk, nk, t, vk);
@@ -1090,21 +1103,22 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
             double cf1 = slen(k, l) + slen(kn, lp) - slen(k, kn) - slen(l, lp);
             double cf2 = slen(k, l) + slen(kp, ln) - slen(k, kp) - slen(l, ln);
             if (cf1 > 0 && cf2 > 0) continue;
+            int cm[4], cfw[4];
+            double csg[4] = {-1.0, -1.0, 1.0, 1.0};
             if (cf1 < cf2) {
-                changes.push_back({k, kn, -1.0});
-                changes.push_back({lp, l, -1.0});
+                cm[0] = k; cfw[0] = kn; cm[1] = lp; cfw[1] = l;     // removed
                 h.fwd(k) = l; h.rev(l) = k;
                 h.rev(kn) = lp; h.fwd(lp) = kn;
-                changes.push_back({k, l, 1.0});
-                changes.push_back({lp, kn, 1.0});
+                cm[2] = k; cfw[2] = l; cm[3] = lp; cfw[3] = kn;     // added
             } else {
-                changes.push_back({l, ln, -1.0});
-                changes.push_back({kp, k, -1.0});
+                cm[0] = l; cfw[0] = ln; cm[1] = kp; cfw[1] = k;
                 h.fwd(l) = k; h.rev(k) = l;
                 h.rev(ln) = kp; h.fwd(kp) = ln;
-                changes.push_back({l, k, 1.0});
-                changes.push_back({kp, ln, 1.0});
+                cm[2] = l; cfw[2] = k; cm[3] = kp; cfw[3] = ln;
             }
+            // the four changed segments' contributions to the member's candidates
+            if (ce > cb && (r = ov_rec_correct(c, cb, ce - cb, cm, cfw, csg, 4, corr.data() + 3 * (size_t)cb)))
+                return r;
             recalc[k]++; recalc[h.fwd(k)]++; recalc[h.rev(k)]++; recalc[kn]++; recalc[kp]++;
             recalc[l]++; recalc[h.fwd(l)]++; recalc[h.rev(l)]++; recalc[ln]++; recalc[lp]++;
             if (log_k && log_l && nrec < log_cap) { log_k[nrec] = k; log_l[nrec] = l; }

@@ -13,6 +13,7 @@
 // cheap test with a 1e-12 relative guard band and, inside the band, by the
 // reference's own correctly rounded divisions.
 #include <math.h>
+#include <string.h>
 
 #include <algorithm>
 
@@ -1143,6 +1144,401 @@ int ov_direct_raw(ov_ctx *c, const int *nodes, int n, double *sums_out)
     c->launches++;
     OV_CUDA(c, cudaGetLastError());
     OV_CUDA(c, cudaMemcpyAsync(sums_out, c->dsum, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    return OV_OK;
+}
+
+// ---------------------------------------- reconnection velocities (reconnect)
+//
+// reconnect (vortex_dynamics.c:186-288) needs, for every candidate node, the
+// direct-sum velocity of update_velocity(k, t, NULL) on the pass's current
+// topology.  The sums over the pass's starting topology are computed here in
+// one batch, split into (candidate, chunk of segments) blocks:
+//   * mixed: segments farther than r_near from the query point in FP32 on
+//     the grid-split positions (separations exact to ~1e-7 relative),
+//     Kahan-summed per thread, with a rigorous bound on their error; closer
+//     segments, and any whose wrap or filter sits near its threshold, in FP64;
+//   * FP64: every term in FP64 (for the rare pairs the bound cannot decide).
+// Rewiring changes four segments at a time; their contributions to every
+// remaining candidate are added on the device after each reconnection.
+
+namespace {
+
+struct RecArgs {
+    const double *x, *y, *z;
+    const int *fwd;
+    const float *sp;          // split positions: gx, gy, gz, fx, fy, fz, each [cap]
+    Geometry geo;
+    float shift_g[OV_MAX_IMAGES][3], shift_f[OV_MAX_IMAGES][3];
+    float Lg[3], Lf[3], hL[3];   // period split on the grid, half period
+    double f4pi;
+    float f4pif;
+    float rnear2;             // squared FP64 radius
+    const int *tid;
+    const int2 *mrange;
+    int nt, cap;
+};
+
+// grid split of every position (the mixed traversal's split, step h)
+__global__ void k_split(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+                        int cap, double h, double inv_h, float *__restrict__ sp)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    const double p[3] = {x[i], y[i], z[i]};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double G = rint(p[a] * inv_h) * h;
+        sp[(size_t)a * cap + i] = (float)G;
+        sp[(size_t)(3 + a) * cap + i] = (float)(p[a] - G);
+    }
+}
+
+__device__ __forceinline__ void member_range(const RecArgs &r, int k, int &lo, int &hi)
+{
+    lo = 0;
+    hi = r.cap;
+    if (r.tid && r.mrange) {
+        int m = r.tid[k];
+        if (m >= 0 && m < r.nt) { lo = r.mrange[m].x; hi = min(r.mrange[m].y, r.cap); }
+        else hi = 0;
+    }
+}
+
+// FP64 term: segment m -> f at image j of node position p (as k_direct)
+__device__ __forceinline__ bool rec_term64(const RecArgs &r, int m, int f, int j, const double p[3], double w[3])
+{
+    double q[3];
+    if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+    else image_point(r.geo, j, p, q);
+    double s1[3] = {r.x[m], r.y[m], r.z[m]};
+    double s2[3] = {r.x[f], r.y[f], r.z[f]};
+    pwrap_dev(r.geo, s1, s2);
+    double R[3] = {rn_sub(s1[0], q[0]), rn_sub(s1[1], q[1]), rn_sub(s1[2], q[2])};
+    double Rp1[3] = {rn_sub(s2[0], q[0]), rn_sub(s2[1], q[1]), rn_sub(s2[2], q[2])};
+    return segment_law64(R, Rp1, len3_ref(R[0], R[1], R[2]), r.f4pi, w);
+}
+
+constexpr int kRecThreads = 256;
+constexpr int kRecVals = 7;   // 3 sums, FP32 magnitude, 3 spare (|FP64 terms|)
+
+__global__ void __launch_bounds__(kRecThreads) k_rec_sums(RecArgs r, const int *__restrict__ nodes, int n,
+                                                          int span, int max_chunks, int force64,
+                                                          double *__restrict__ part)
+{
+    __shared__ float s_q[OV_MAX_IMAGES + 1][6];   // split query points: self, then images
+    __shared__ double red[kRecVals][kRecThreads];
+    const int b = blockIdx.x, chunk = blockIdx.y;
+    if (b >= n) return;
+    const int k = nodes[b];
+    int lo, hi;
+    member_range(r, k, lo, hi);
+    const int m0 = lo + chunk * span, m1 = min(hi, m0 + span);
+    double *out = part + ((size_t)b * max_chunks + chunk) * kRecVals;
+    if (m0 >= m1 || k < 0 || k >= r.cap) {
+        if (threadIdx.x < kRecVals) out[threadIdx.x] = 0.0;
+        return;
+    }
+    const double p[3] = {r.x[k], r.y[k], r.z[k]};
+    const int nq = r.geo.n_img + 1;
+    if (threadIdx.x < nq) {
+        const int j = (int)threadIdx.x - 1;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            float g = r.sp[(size_t)a * r.cap + k], f = r.sp[(size_t)(3 + a) * r.cap + k];
+            if (j >= 0) { g -= r.shift_g[j][a]; f -= r.shift_f[j][a]; }
+            s_q[threadIdx.x][a] = g;
+            s_q[threadIdx.x][3 + a] = f;
+        }
+    }
+    __syncthreads();
+    float s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0, mag = 0;
+    double d0 = 0, d1 = 0, d2 = 0, dabs = 0;
+    const float eps_band = 1e-3f;
+    for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+        const int f = r.fwd[m];
+        if (f < 0 || f >= r.cap) continue;
+        float ag[3], af[3], sv[3];
+        bool seg64 = force64 != 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            ag[a] = r.sp[(size_t)a * r.cap + m];
+            af[a] = r.sp[(size_t)(3 + a) * r.cap + m];
+            float bg = r.sp[(size_t)a * r.cap + f], bf = r.sp[(size_t)(3 + a) * r.cap + f];
+            float d = (bg - ag[a]) + (bf - af[a]);
+            if (r.geo.periodic[a]) {
+                // seg_pwrap: the end moved by a period toward the start
+                if (fabsf(fabsf(d) - r.hL[a]) < eps_band * r.hL[a]) seg64 = true;
+                if (d > r.hL[a]) { bg -= r.Lg[a]; bf -= r.Lf[a]; }
+                else if (d < -r.hL[a]) { bg += r.Lg[a]; bf += r.Lf[a]; }
+                if (fabsf(d) > 3.0f * r.hL[a]) seg64 = true;   // more than one period: FP64 loop
+            }
+            sv[a] = (bg - ag[a]) + (bf - af[a]);
+        }
+        const float slen = sqrtf(fmaf(sv[0], sv[0], fmaf(sv[1], sv[1], sv[2] * sv[2])));
+        for (int qi = 0; qi < nq; ++qi) {
+            const int j = qi - 1;
+            if (j < 0 && (m == k || f == k)) continue;   // the node's own segments (primary only)
+            float R[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) R[a] = (ag[a] - s_q[qi][a]) + (af[a] - s_q[qi][3 + a]);
+            const float lR2 = fmaf(R[0], R[0], fmaf(R[1], R[1], R[2] * R[2]));
+            const float P0 = R[0] + sv[0], P1 = R[1] + sv[1], P2 = R[2] + sv[2];
+            const float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
+            bool use64 = seg64 || lR2 < r.rnear2 || lp2 < r.rnear2;
+            float ra = 0, rb = 0, ab = 0, dot = 0, nd = 0;
+            if (!use64) {
+                ra = rsqrtf(lR2);
+                rb = rsqrtf(lp2);
+                ab = ra * rb;
+                dot = fmaf(R[0], P0, fmaf(R[1], P1, R[2] * P2));
+                nd = dot * ab;
+                if (fabsf(nd - 1e-8f) < 1e-4f) use64 = true;   // filter near its threshold
+            }
+            if (use64) {
+                double w[3];
+                if (rec_term64(r, m, f, j, p, w)) {
+                    d0 += w[0]; d1 += w[1]; d2 += w[2];
+                    dabs += fabs(w[0]) + fabs(w[1]) + fabs(w[2]);
+                }
+                continue;
+            }
+            if (nd < 1e-8f) continue;   // ndot filter (far from its threshold here)
+            const float sc = __fdividef(r.f4pif * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
+            // R x Rp1 = R x s
+            kahan_add(s0, c0, fmaf(R[1], sv[2], -R[2] * sv[1]) * sc);
+            kahan_add(s1, c1, fmaf(R[2], sv[0], -R[0] * sv[2]) * sc);
+            kahan_add(s2, c2, fmaf(R[0], sv[1], -R[1] * sv[0]) * sc);
+            mag += sc * slen * lR2 * ra;   // sc |R| |s| >= |w| (per component)
+        }
+    }
+    red[0][threadIdx.x] = ((double)s0 - (double)c0) + d0;
+    red[1][threadIdx.x] = ((double)s1 - (double)c1) + d1;
+    red[2][threadIdx.x] = ((double)s2 - (double)c2) + d2;
+    red[3][threadIdx.x] = (double)mag;
+    red[4][threadIdx.x] = dabs;
+    red[5][threadIdx.x] = fabs((double)s0) + fabs((double)s1) + fabs((double)s2);
+    red[6][threadIdx.x] = 0.0;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off)
+            for (int v = 0; v < kRecVals; ++v) red[v][threadIdx.x] += red[v][threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x < kRecVals) out[threadIdx.x] = red[threadIdx.x][0];
+}
+
+// out[5 b + {0,1,2}] = sums over the chunks in order, out[5 b + 3] = bound on
+// each component's error: FP32 terms (per-term rounding, Kahan), FP64 terms
+// and the FP64 reductions; out[5 b + 4] = sum of the terms' magnitudes.
+__global__ void k_rec_finish(const double *__restrict__ part, int n, int max_chunks, double *__restrict__ out)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    double acc[kRecVals] = {0, 0, 0, 0, 0, 0, 0};
+    for (int ch = 0; ch < max_chunks; ++ch)
+        for (int v = 0; v < kRecVals; ++v) acc[v] += part[((size_t)b * max_chunks + ch) * kRecVals + v];
+    const double eps32 = 5.9604644775390625e-8;
+    for (int a = 0; a < 3; ++a) out[5 * (size_t)b + a] = acc[a];
+    out[5 * (size_t)b + 3] = 1.01 * (64.0 * eps32 * acc[3] + 4.0 * eps32 * acc[5]) + 1e-12 * (acc[4] + acc[3]);
+    out[5 * (size_t)b + 4] = 1.01 * (acc[3] + acc[4]);
+}
+
+struct RecChange {
+    int m[8], f[8];
+    double sign[8];
+    int n;
+};
+
+// Contribution of the changed segments to candidates [c0, c0 + nc) of the
+// sorted candidate list, one thread per (candidate, query point).
+__global__ void k_corr(RecArgs r, const int *__restrict__ cand, int c0, int nc, RecChange ch,
+                       double *__restrict__ part)
+{
+    const int nq = r.geo.n_img + 1;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nc * nq) return;
+    int ci = idx / nq, qi = idx - ci * nq;
+    int k = cand[c0 + ci];
+    double acc[3] = {0, 0, 0};
+    if (k >= 0 && k < r.cap) {
+        const double p[3] = {r.x[k], r.y[k], r.z[k]};
+        for (int i = 0; i < ch.n && i < 8; ++i) {
+            int m = ch.m[i], f = ch.f[i];
+            if (m < 0 || m >= r.cap || f < 0 || f >= r.cap) continue;
+            double w[3];
+            if (rec_term64(r, m, f, qi - 1, p, w))
+                for (int a = 0; a < 3; ++a) acc[a] += ch.sign[i] * w[a];
+        }
+    }
+    for (int a = 0; a < 3; ++a) part[(size_t)idx * 3 + a] = acc[a];
+}
+
+__global__ void k_corr_finish(const double *__restrict__ part, int nc, int nq, double *__restrict__ corr)
+{
+    int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci >= nc) return;
+    double acc[3] = {0, 0, 0};
+    for (int q = 0; q < nq; ++q)
+        for (int a = 0; a < 3; ++a) acc[a] += part[((size_t)ci * nq + q) * 3 + a];
+    for (int a = 0; a < 3; ++a) corr[3 * (size_t)ci + a] += acc[a];
+}
+
+RecArgs make_rec_args(ov_ctx *c)
+{
+    RecArgs r;
+    memset(&r, 0, sizeof r);
+    r.x = c->node.x; r.y = c->node.y; r.z = c->node.z;
+    r.fwd = c->fwd;
+    r.sp = c->rec_split;
+    r.geo = c->geo;
+    const double h = c->grid_h;
+    for (int j = 0; j < c->geo.n_img; ++j)
+        for (int a = 0; a < 3; ++a) {
+            double sh = c->geo.L[a] * (double)c->geo.shift[j][a];
+            double G = rint(sh / h) * h;
+            r.shift_g[j][a] = (float)G;
+            r.shift_f[j][a] = (float)(sh - G);
+        }
+    for (int a = 0; a < 3; ++a) {
+        double G = rint(c->geo.L[a] / h) * h;
+        r.Lg[a] = (float)G;
+        r.Lf[a] = (float)(c->geo.L[a] - G);
+        r.hL[a] = (float)(c->geo.L[a] * 0.5);
+    }
+    r.f4pi = c->params.kappa / 4 / M_PI;
+    r.f4pif = (float)r.f4pi;
+    // FP64 within 4 dl_max (segments are shorter than 2 dl_max after remesh)
+    double dl = 0;
+    for (const Member &m : c->mem) dl = std::max(dl, m.params.dl_max);
+    double rn = 4.0 * std::max(dl, c->params.rec_dist);
+    r.rnear2 = (float)(rn * rn);
+    const bool ens = c->mem.size() > 1;
+    r.tid = ens ? c->d_tid : nullptr;
+    r.mrange = ens ? c->d_mrange : nullptr;
+    r.nt = (int)c->mem.size();
+    r.cap = c->cap;
+    return r;
+}
+
+int rec_reserve(ov_ctx *c, int n, int max_chunks)
+{
+    size_t need_part = (size_t)std::max(n, 1) * max_chunks * kRecVals;
+    const int nq = c->geo.n_img + 1;
+    need_part = std::max(need_part, (size_t)std::max(n, 1) * nq * 3);
+    if (c->rec_part_cap < need_part) {
+        if (c->rec_part) cudaFree(c->rec_part);
+        c->rec_part = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->rec_part, need_part * sizeof(double)));
+        c->rec_part_cap = need_part;
+    }
+    if (c->rec_cap < n) {
+        if (c->rec_nodes) cudaFree(c->rec_nodes);
+        if (c->rec_out) cudaFree(c->rec_out);
+        if (c->rec_corr) cudaFree(c->rec_corr);
+        c->rec_nodes = nullptr; c->rec_out = nullptr; c->rec_corr = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->rec_nodes, (size_t)n * sizeof(int)));
+        OV_CUDA(c, cudaMalloc(&c->rec_out, (size_t)n * 5 * sizeof(double)));
+        OV_CUDA(c, cudaMalloc(&c->rec_corr, (size_t)n * 3 * sizeof(double)));
+        c->rec_cap = n;
+    }
+    if (c->rec_split_cap < c->cap) {
+        if (c->rec_split) cudaFree(c->rec_split);
+        c->rec_split = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->rec_split, (size_t)c->cap * 6 * sizeof(float)));
+        c->rec_split_cap = c->cap;
+    }
+    return OV_OK;
+}
+
+int rec_launch_sums(ov_ctx *c, const int *d_nodes, int n, bool force64, double *out_host)
+{
+    int maxcap = 0;
+    for (const Member &m : c->mem) maxcap = std::max(maxcap, c->mem.size() == 1 ? c->cap : m.cap);
+    const int span = 8192;
+    const int max_chunks = std::max(1, (maxcap + span - 1) / span);
+    int r = rec_reserve(c, n, max_chunks);
+    if (r) return r;
+    RecArgs ra = make_rec_args(c);
+    dim3 grid(n, max_chunks);
+    k_rec_sums<<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, force64 ? 1 : 0, c->rec_part);
+    k_rec_finish<<<(n + 127) / 128, 128, 0, c->stream>>>(c->rec_part, n, max_chunks, c->rec_out);
+    c->launches += 2;
+    OV_CUDA(c, cudaGetLastError());
+    OV_CUDA(c, cudaMemcpyAsync(out_host, c->rec_out, (size_t)n * 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    return OV_OK;
+}
+
+}  // namespace
+
+// Mixed-precision sums of the candidate list (kept on the device for the
+// corrections): out[5 i + {0,1,2}] the sum, out[5 i + 3] a bound on each
+// component's error, out[5 i + 4] the sum of the terms' magnitudes.
+int ov_rec_begin(ov_ctx *c, const int *cand, int n, double *out)
+{
+    if (n <= 0) return OV_OK;
+    int maxcap = 0;
+    for (const Member &m : c->mem) maxcap = std::max(maxcap, c->mem.size() == 1 ? c->cap : m.cap);
+    int r = rec_reserve(c, n, std::max(1, (maxcap + 8191) / 8192));
+    if (r) return r;
+    OV_CUDA(c, cudaMemcpyAsync(c->rec_nodes, cand, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    OV_CUDA(c, cudaMemsetAsync(c->rec_corr, 0, (size_t)n * 3 * sizeof(double), c->stream));
+    k_split<<<(c->cap + 255) / 256, 256, 0, c->stream>>>(c->node.x, c->node.y, c->node.z, c->cap, c->grid_h,
+                                                        1.0 / c->grid_h, c->rec_split);
+    c->launches++;
+    return rec_launch_sums(c, c->rec_nodes, n, false, out);
+}
+
+// FP64 sums (every term in FP64) of nodes k and l, laid out as ov_rec_begin's.
+int ov_rec_exact(ov_ctx *c, int k, int l, double out[10])
+{
+    int nodes[2] = {k, l};
+    if (!c->rec_pair) OV_CUDA(c, cudaMalloc(&c->rec_pair, 2 * sizeof(int)));
+    OV_CUDA(c, cudaMemcpyAsync(c->rec_pair, nodes, 2 * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    return rec_launch_sums(c, c->rec_pair, 2, true, out);
+}
+
+extern "C" int ov_direct_sums_bounded(ov_ctx *c, const int *nodes, int n, int precision, double *out)
+{
+    if (!c || n < 0 || (n > 0 && (!nodes || !out))) return OV_ERR_ARG;
+    if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
+    if (precision != OV_PREC_FP64 && precision != OV_PREC_MIXED) return OV_ERR_ARG;
+    cudaSetDevice(c->device);
+    for (int i = 0; i < n; ++i)
+        if (nodes[i] < 0 || nodes[i] >= c->cap) return ov_fail(c, OV_ERR_ARG, "node %d out of range", nodes[i]);
+    if (n == 0) return OV_OK;
+    int maxcap = 0;
+    for (const Member &m : c->mem) maxcap = std::max(maxcap, c->mem.size() == 1 ? c->cap : m.cap);
+    int r = rec_reserve(c, n, std::max(1, (maxcap + 8191) / 8192));
+    if (r) return r;
+    OV_CUDA(c, cudaMemcpyAsync(c->rec_nodes, nodes, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    k_split<<<(c->cap + 255) / 256, 256, 0, c->stream>>>(c->node.x, c->node.y, c->node.z, c->cap, c->grid_h,
+                                                        1.0 / c->grid_h, c->rec_split);
+    c->launches++;
+    return rec_launch_sums(c, c->rec_nodes, n, precision == OV_PREC_FP64, out);
+}
+
+// Add the changed segments' contributions to candidates [c0, c0 + nc) and
+// copy their corrections to corr_out (nc x 3).
+int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const double *sign, int nch,
+                   double *corr_out)
+{
+    if (nc <= 0) return OV_OK;
+    RecChange ch;
+    memset(&ch, 0, sizeof ch);
+    ch.n = std::min(nch, 8);
+    for (int i = 0; i < ch.n; ++i) { ch.m[i] = m[i]; ch.f[i] = f[i]; ch.sign[i] = sign[i]; }
+    RecArgs ra = make_rec_args(c);
+    const int nq = c->geo.n_img + 1;
+    const int threads = nc * nq;
+    k_corr<<<(threads + 127) / 128, 128, 0, c->stream>>>(ra, c->rec_nodes, c0, nc, ch, c->rec_part);
+    k_corr_finish<<<(nc + 127) / 128, 128, 0, c->stream>>>(c->rec_part, nc, nq, c->rec_corr + 3 * (size_t)c0);
+    c->launches += 2;
+    OV_CUDA(c, cudaGetLastError());
+    OV_CUDA(c, cudaMemcpyAsync(corr_out, c->rec_corr + 3 * (size_t)c0, (size_t)nc * 3 * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
     OV_CUDA(c, cudaStreamSynchronize(c->stream));
     return OV_OK;
 }

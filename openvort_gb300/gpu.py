@@ -88,6 +88,7 @@ def load(path: str | None = None):
         "ov_set_tuning": (C.c_int, [P, C.POINTER(abi.Tuning)]),
         "ov_autotune": (C.c_int, [P, C.c_double, C.POINTER(abi.Tuning), C.POINTER(C.c_float)]),
         "ov_step_times": (C.c_int, [P, C.POINTER(C.c_double), C.c_int]),
+        "ov_direct_sums_bounded": (C.c_int, [P, C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -265,6 +266,14 @@ class Context:
         self._check(self.lib.ov_direct_velocities(self._h, nodes.ctypes.data_as(C.POINTER(C.c_int)),
                                                   len(nodes), t, dp(v), dp(s)))
         return v, s
+
+    def direct_sums_bounded(self, nodes, precision: int = abi.OV_PREC_MIXED):
+        """Nonlocal direct sums of `nodes`: (sums[n,3], bound[n], magnitude[n])."""
+        nodes = np.ascontiguousarray(nodes, dtype=np.int32)
+        out = np.zeros((len(nodes), 5))
+        self._check(self.lib.ov_direct_sums_bounded(self._h, nodes.ctypes.data_as(C.POINTER(C.c_int)), len(nodes),
+                                                    precision, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out[:, :3].copy(), out[:, 3].copy(), out[:, 4].copy()
 
     def enforce_periodic(self):
         self._check(self.lib.ov_enforce_periodic_boundaries(self._h))

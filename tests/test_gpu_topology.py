@@ -123,3 +123,28 @@ def test_remesh_grows_pool_like_expand_tangle():
     np.testing.assert_array_equal(out.conn, t.copy("conn"))
     m = used(out.stat)
     assert rel_err(out.pos[m], t.copy("pos")[m]) < 1e-12
+
+
+@pytest.mark.parametrize("n_loops,D", [(64, 0.1), (40, 0.03)])
+def test_reconnect_sums_within_their_bound(n_loops, D):
+    """The mixed-precision direct sums reconnect decides with stay within
+    their own error bound of the FP64 sums, and the FP64 sums match the
+    oracle's direct sums (nonlocal part) to 1e-12 relative."""
+    ht = W.random_walk_tangle(n_loops, 64 if D == 0.1 else 48, D=D, seed=77)
+    ctx = gpu.Context(0, params=W.config_params("rw"))
+    ctx.upload(ht)
+    nodes = np.arange(0, ht.n, max(1, ht.n // 300))
+    s32, b32, mag = ctx.direct_sums_bounded(nodes, abi.OV_PREC_MIXED)
+    s64, b64, _ = ctx.direct_sums_bounded(nodes, abi.OV_PREC_FP64)
+    ctx.close()
+    err = np.abs(s32 - s64).max(axis=1)
+    assert np.all(err <= b32 + b64), (err / b32).max()
+    assert np.all(b32 > 0) and np.all(b32 < 1e-4 * mag + 1e-300)
+    # with zero tangents/normals (as uploaded) and no v_s, the oracle's
+    # update_velocity(k, NULL) is the nonlocal sum alone
+    assert not ht.tangents.any() and not ht.normals.any()
+    port = Checker("port")
+    port.set_params(W.config_params("rw"))
+    t = port.tangle(ht)
+    _, vs_ref = port.direct_velocities(t, nodes)
+    assert rel_err(s64, vs_ref) < 1e-12
