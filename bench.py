@@ -255,12 +255,16 @@ def run_ensemble(args, device=0):
     K = args.ensemble_steps
     recs = added = 0
     passes = {}
+    rstat = {"reconnect_candidates": 0, "reconnect_evaluated": 0, "reconnect_fp64_pairs": 0,
+             "reconnect_exact_pairs": 0}
     t0 = time.perf_counter()
     for k in range(K):
         ctx.step(k * dt, dt)
         s2 = ctx.stats()
         recs += s2["reconnections"]
         added += s2["remesh_added"]
+        for key in rstat:
+            rstat[key] += s2[key]
         for name, v in ctx.step_times().items():
             passes[name] = passes.get(name, 0.0) + v / K
     ctx.synchronize()
@@ -281,9 +285,136 @@ def run_ensemble(args, device=0):
                       "node_evals_per_s": 4 * n / (rk4_ms * 1e-3)},
         "full_steps_mixed": {"steps": K, "ms_per_step_wall": full_ms, "steps_per_s": 1e3 / full_ms,
                              "reconnections": recs, "remesh_added": added, "live_nodes_end": n_end,
-                             "pass_ms": passes,
+                             "pass_ms": passes, "reconnect_counts": rstat,
                              "includes": "small loops x3, reconnect, periodic wrap, remesh, update_tangle, "
                                          "rk4_step (graph), per step; host wall clock"},
+    }
+
+
+PRECISION_FORM = dict(workload="random-walk tangle, 1,024 loops x 256 nodes (262,144), D=0.1 cm, periodic_26, "
+                               "theta in {0.3, 0.5}", n_loops=1024, per_loop=256, D=0.1, seed=3, thetas=[0.3, 0.5],
+                      direct_subsample=8192)
+LARGE = dict(workload="random-walk tangle, 4,096 loops x 256 nodes (1,048,576), D=0.2 cm, periodic_26, theta=0.4, "
+                      "alpha=0.098, alpha'=0.016, v_n=1.0 x, dt=2e-5, reconnect + remesh + smoothing (cutoff 0.8)",
+             n_loops=4096, per_loop=256, D=0.2, seed=5, theta=0.4, dt=2e-5)
+
+
+def direct_subsample(n, count, seed=0):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, size=min(count, n), replace=False))
+
+
+def eval_ms(ctx, reps):
+    ts = []
+    for _ in range(reps):
+        ctx.flush_l2(256 << 20)
+        ctx.timer_start()
+        ctx.update_tangle(0.0)
+        ts.append(ctx.timer_stop())
+    return statistics.mean(ts)
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def run_precision_form(args, device=0):
+    """262,144 nodes at theta 0.3 and 0.5: mixed vs FP64 tree, both against
+    FP64 direct sums on a node subsample."""
+    from openvort_gb300 import abi, gpu, workloads as W
+    P = PRECISION_FORM
+    ht = W.random_walk_tangle(P["n_loops"], P["per_loop"], D=P["D"], seed=P["seed"])
+    n = ht.n
+    sub = direct_subsample(n, P["direct_subsample"], 1)
+    out = {"config": P, "nodes": n, "by_theta": {}}
+    direct = None
+    for theta in P["thetas"]:
+        ctx = gpu.Context(device, params=W.config_params("rw", bh_resolution=theta), precision=abi.OV_PREC_FP64)
+        ctx.upload(ht)
+        ctx.update_tangle(0.0)
+        if direct is None:
+            direct, _ = ctx.direct_velocities(sub)   # FP64 direct sums (tree == NULL branch), tangents current
+        fp64_ms = eval_ms(ctx, 2)
+        v64 = ctx.download(ht, abi.OV_F_VELS).vels.copy()
+        st64 = ctx.stats()
+        ctx.set_precision(abi.OV_PREC_MIXED)
+        ctx.update_tangle(0.0)
+        mixed_ms = eval_ms(ctx, max(3, args.steps))
+        v32 = ctx.download(ht, abi.OV_F_VELS).vels.copy()
+        st32 = ctx.stats()
+        ctx.close()
+        out["by_theta"][str(theta)] = {
+            "fp64": {"value": n / (fp64_ms * 1e-3), "unit": UNIT, "ms_per_eval": fp64_ms,
+                     "rel_l2_vs_direct_subsample": rel_l2(v64[sub], direct)},
+            "mixed": {"value": n / (mixed_ms * 1e-3), "unit": UNIT, "ms_per_eval": mixed_ms,
+                      "rel_l2_vs_fp64_tree": rel_l2(v32, v64),
+                      "rel_l2_vs_direct_subsample": rel_l2(v32[sub], direct),
+                      "same_decisions_as_fp64": bool(st32["accepts"] == st64["accepts"]
+                                                     and st32["visits"] == st64["visits"])},
+            "mixed_speedup_vs_fp64": fp64_ms / mixed_ms,
+        }
+    return out
+
+
+def run_large(args, device=0):
+    """1,048,576 nodes: mixed-precision RK4 and full time steps with
+    reconnection, remeshing and smoothing; FP64 evaluation beside it."""
+    from openvort_gb300 import abi, gpu, workloads as W
+    E = LARGE
+    ht = W.random_walk_tangle(E["n_loops"], E["per_loop"], D=E["D"], seed=E["seed"])
+    n = ht.n
+    p = W.config_params("large", bh_resolution=E["theta"])
+    ctx = gpu.Context(device, params=p, precision=abi.OV_PREC_FP64)
+    ctx.upload(ht)
+    ctx.update_tangle(0.0)
+    fp64_ms = eval_ms(ctx, 1)
+    v64 = ctx.download(ht, abi.OV_F_VELS).vels.copy()
+    ctx.set_precision(abi.OV_PREC_MIXED)
+    ctx.upload(ht)
+    tune, _ = ctx.autotune(0.0)
+    ctx.update_tangle(0.0)
+    mixed_ms = eval_ms(ctx, max(3, args.steps))
+    v32 = ctx.download(ht, abi.OV_F_VELS).vels.copy()
+    dt = E["dt"]
+    ctx.upload(ht)
+    for w in range(2):
+        ctx.update_tangle(w * dt)
+        ctx.rk4_step(w * dt, dt)
+    ts = []
+    for k in range(max(2, args.steps // 2)):
+        ctx.timer_start()
+        ctx.update_tangle(k * dt)
+        ctx.rk4_step(k * dt, dt)
+        ts.append(ctx.timer_stop())
+    rk4_ms = statistics.mean(ts)
+    ctx.upload(ht)
+    K = args.large_steps
+    passes, recs, added = {}, 0, 0
+    rstat = {"reconnect_candidates": 0, "reconnect_evaluated": 0, "reconnect_fp64_pairs": 0,
+             "reconnect_exact_pairs": 0}
+    t0 = time.perf_counter()
+    for k in range(K):
+        ctx.step(k * dt, dt)
+        s2 = ctx.stats()
+        recs += s2["reconnections"]
+        added += s2["remesh_added"]
+        for key in rstat:
+            rstat[key] += s2[key]
+        for name, v in ctx.step_times().items():
+            passes[name] = passes.get(name, 0.0) + v / max(1, K)
+    ctx.synchronize()
+    full_ms = (time.perf_counter() - t0) * 1e3 / max(1, K)
+    ctx.close()
+    return {
+        "config": E, "nodes": n, "tuning": tune,
+        "fp64": {"value": n / (fp64_ms * 1e-3), "unit": UNIT, "ms_per_eval": fp64_ms},
+        "mixed": {"value": n / (mixed_ms * 1e-3), "unit": UNIT, "ms_per_eval": mixed_ms,
+                  "rel_l2_vs_fp64_tree": rel_l2(v32, v64)},
+        "mixed_speedup_vs_fp64": fp64_ms / mixed_ms,
+        "rk4_mixed": {"steps_per_s": 1e3 / rk4_ms, "ms_per_step": rk4_ms, "node_evals_per_s": 4 * n / (rk4_ms * 1e-3)},
+        "full_steps_mixed": {"steps": K, "ms_per_step_wall": full_ms, "steps_per_s": 1e3 / full_ms if K else None,
+                             "reconnections": recs, "remesh_added": added, "pass_ms": passes,
+                             "reconnect_counts": rstat},
     }
 
 
@@ -342,6 +473,11 @@ def run_ours(args):
     h2d = n * (3 * 8 + 4 * 4)
     d2h = n * 3 * 8
 
+    # ---- accuracy of the FP64 tree against FP64 direct sums on a 4,096-node subsample
+    sub = direct_subsample(n, 4096, 1)
+    direct_v, _ = ctx.direct_velocities(sub)
+    fp64_vs_direct = rel_l2(np.array(ht.vels)[sub], direct_v)
+
     # ---- mixed precision on the same workload (reported beside FP64)
     mixed = None
     try:
@@ -360,7 +496,8 @@ def run_ours(args):
         mst = ctx.stats()
         err = float(np.linalg.norm(ht.vels - ref_v) / np.linalg.norm(ref_v))
         mixed = {"value": world * n / (statistics.mean(mt) * 1e-3), "unit": UNIT,
-                 "rel_l2_vs_fp64_tree": err, "ms_per_step": statistics.mean(mt),
+                 "rel_l2_vs_fp64_tree": err, "rel_l2_vs_direct_subsample": rel_l2(ht.vels[sub], direct_v),
+                 "ms_per_step": statistics.mean(mt),
                  "speedup_vs_fp64": mean_ms / statistics.mean(mt),
                  "same_decisions_as_fp64": bool(mst["accepts"] == acc and mst["visits"] == vis),
                  "fp64_guard_band_decisions": mst["fp64_fallbacks"], "fp64_near_field": mst["near_field_fp64"],
@@ -388,12 +525,22 @@ def run_ours(args):
         rk4[name] = {"steps_per_s": 1e3 / statistics.mean(ts), "ms_per_step": statistics.mean(ts),
                      "node_evals_per_s": 4 * n / (statistics.mean(ts) * 1e-3)}
     ctx.set_precision(abi.OV_PREC_FP64)
-    ensemble = None
+    ensemble = precision_form = large = None
     if world == 1 and args.ensemble_steps >= 0:
         try:
             ensemble = run_ensemble(args, device)
         except Exception as e:
             ensemble = {"error": str(e)[:300]}
+    if world == 1 and args.precision_form:
+        try:
+            precision_form = run_precision_form(args, device)
+        except Exception as e:
+            precision_form = {"error": str(e)[:300]}
+    if world == 1 and args.large_steps >= 0:
+        try:
+            large = run_large(args, device)
+        except Exception as e:
+            large = {"error": str(e)[:300]}
     clk.__exit__(None, None, None)
 
     # ---- CPU baseline (rank 0 only, bounded sample)
@@ -421,12 +568,16 @@ def run_ours(args):
                      "work": "42 flops per accepted interaction + 9 per visited cell",
                      "accepts": acc, "visits": vis, "fp32_fma_peak_tflops": fp32_peak,
                      "warp_efficiency": vis / max(1, 32 * st["warp_steps"])},
+        "accuracy": {"fp64_tree_rel_l2_vs_direct_subsample": fp64_vs_direct,
+                     "subsample": "4,096 nodes, FP64 direct sums (tree == NULL branch) on the GPU"},
         "cpu_baseline": cpu,
         "e2e": {"value": world * n / (e2e_mean * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "mixed": mixed,
         "rk4": rk4,
         "ensemble": ensemble,
+        "precision_form": precision_form,
+        "large": large,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "peaks_source": peak_src,
@@ -443,6 +594,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ensemble-steps", type=int, default=10,
                     help="full time steps of the 48-tangle ensemble (-1: skip the ensemble section)")
+    ap.add_argument("--large-steps", type=int, default=5,
+                    help="full time steps of the 1,048,576-node tangle (-1: skip that section)")
+    ap.add_argument("--precision-form", type=int, default=1, help="262,144-node theta 0.3/0.5 section (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

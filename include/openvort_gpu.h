@@ -114,6 +114,10 @@ typedef struct ov_stats {
     int64_t remesh_removed;    /* last remesh pass */
     int64_t small_loops_removed;
     int64_t error_word;        /* device error flags, 0 when clean */
+    int64_t reconnect_candidates;   /* last reconnect pass: nodes in candidate pairs */
+    int64_t reconnect_fp64_pairs;   /* pairs the mixed-precision bound left undecided (FP64 sums) */
+    int64_t reconnect_exact_pairs;  /* pairs recomputed in the reference's summation order */
+    int64_t reconnect_evaluated;    /* candidate velocities the decisions used */
 } ov_stats;
 
 typedef struct ov_ctx ov_ctx;
@@ -173,13 +177,16 @@ int ov_set_member_params(ov_ctx *ctx, int i, const ov_params *p);
 
 /* Launch shape of the traversal: warps per block (2, 4 or 8), query groups
    per node (1-27; 0 = from the node count), persistent blocks per SM (0 =
-   the occupancy limit) and the order of the work queue (largest member
-   first or member order).  Results do not depend on it. */
+   the occupancy limit), the order of the work queue (largest member first
+   or member order) and, for the mixed traversal, the register budget
+   (0: the default; 1: fewer registers for one more resident block).
+   Results do not depend on it. */
 typedef struct ov_tuning {
     int warps_per_block;
     int query_groups;
     int blocks_per_sm;
     int largest_first;
+    int high_occupancy;
 } ov_tuning;
 int ov_get_tuning(const ov_ctx *ctx, ov_tuning *out);
 int ov_set_tuning(ov_ctx *ctx, const ov_tuning *tu);
@@ -286,7 +293,10 @@ int ov_step(ov_ctx *ctx, double t, double dt);
    loops (three calls), [1] reconnect, [2] smooth, [3] periodic wrap (two
    calls), [4] remesh, [5] update_tangle, [6] rk4_step, [7] the whole step;
    reconnect's parts: [8] mirror + candidate pairs, [9] direct sums,
-   [10] sequential decisions, [11] push.  Writes min(n, 12) values. */
+   [10] sequential decisions, [11] push; inside [10]: [12] reading
+   corrections back, [13] launching corrections, [14] FP64 sums of
+   undecided pairs, [15] reference-order recomputes.  Writes min(n, 16)
+   values. */
 int ov_step_times(const ov_ctx *ctx, double *ms, int n);
 
 int ov_get_stats(const ov_ctx *ctx, ov_stats *out);

@@ -79,13 +79,14 @@ class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "node_evals", "cells", "max_depth", "visits", "accepts", "warp_steps", "fp64_fallbacks",
         "near_field_fp64", "out_of_root", "reconnections", "remesh_added", "remesh_removed",
-        "small_loops_removed", "error_word")]
+        "small_loops_removed", "error_word", "reconnect_candidates", "reconnect_fp64_pairs",
+        "reconnect_exact_pairs", "reconnect_evaluated")]
 
 
 class Tuning(C.Structure):
     """ov_tuning: launch shape of the traversal."""
     _fields_ = [("warps_per_block", C.c_int), ("query_groups", C.c_int), ("blocks_per_sm", C.c_int),
-                ("largest_first", C.c_int)]
+                ("largest_first", C.c_int), ("high_occupancy", C.c_int)]
 
 
 assert C.sizeof(TangleState) == 168 and C.sizeof(DomainBox) == 72 and C.sizeof(ExtVel) == 56

@@ -140,13 +140,15 @@ int ov_ctx_destroy(ov_ctx *c)
     if (c->d_tprm) cudaFree(c->d_tprm);
     if (c->d_mrange) cudaFree(c->d_mrange);
     void *scratch[] = {c->d_pairs, c->d_npairs, c->d_loop_off, c->d_loop_nodes, c->d_loop_buf, c->d_loop_cut,
-                       c->rec_nodes, c->rec_pair, c->rec_out, c->rec_corr, c->rec_part, c->rec_split};
+                       c->rec_nodes, c->rec_pair, c->rec_out, c->rec_corr, c->rec_part, c->rec_split,
+                       c->fft_buf, c->fft_tw, c->long_buf};
     for (void *p : scratch)
         if (p) cudaFree(p);
     if (c->dsum) cudaFree(c->dsum);
     if (c->part) cudaFree(c->part);
     if (c->flush_buf) cudaFree(c->flush_buf);
     if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->h_corr) cudaFreeHost(c->h_corr);
     if (c->rk4_exec) cudaGraphExecDestroy(c->rk4_exec);
     for (int i = 0; i < 4; ++i)
         if (c->ph[i]) cudaEventDestroy(c->ph[i]);
@@ -220,6 +222,7 @@ int ov_get_tuning(const ov_ctx *c, ov_tuning *out)
     out->query_groups = c->tune.groups;
     out->blocks_per_sm = c->tune.blocks_per_sm;
     out->largest_first = c->tune.largest_first;
+    out->high_occupancy = c->tune.hi_occ;
     return OV_OK;
 }
 
@@ -227,12 +230,14 @@ int ov_set_tuning(ov_ctx *c, const ov_tuning *tu)
 {
     if (!c || !tu) return OV_ERR_ARG;
     if ((tu->warps_per_block != 2 && tu->warps_per_block != 4 && tu->warps_per_block != 8) ||
-        tu->query_groups < 0 || tu->query_groups > 27 || tu->blocks_per_sm < 0 || tu->blocks_per_sm > 64)
+        tu->query_groups < 0 || tu->query_groups > 27 || tu->blocks_per_sm < 0 || tu->blocks_per_sm > 64 ||
+        (tu->high_occupancy != 0 && tu->high_occupancy != 1))
         return ov_fail(c, OV_ERR_ARG, "tuning out of range");
     c->tune.warps = tu->warps_per_block;
     c->tune.groups = tu->query_groups;
     c->tune.blocks_per_sm = tu->blocks_per_sm;
     c->tune.largest_first = tu->largest_first != 0;
+    c->tune.hi_occ = tu->high_occupancy;
     if (c->uploaded && c->mem.size() > 1) return ov_upload_member_tables(c);
     return OV_OK;
 }
@@ -316,6 +321,7 @@ static int ensure_stage(ov_ctx *c, size_t bytes)
 {
     if (c->h_stage_bytes >= bytes) return OV_OK;
     if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->h_corr) cudaFreeHost(c->h_corr);
     c->h_stage = nullptr;
     OV_CUDA(c, cudaMallocHost(&c->h_stage, bytes));
     c->h_stage_bytes = bytes;
@@ -836,8 +842,8 @@ static unsigned long long graph_key(ov_ctx *c)
     unsigned long long h = 1469598103934665603ull;
     h = mix64(h, &c->params, sizeof c->params);
     h = mix64(h, &c->geo, sizeof c->geo);
-    int ints[8] = {c->cap, c->tree.cap_cells, c->precision, (int)c->mem.size(), c->tune.warps, c->tune.groups,
-                   c->tune.blocks_per_sm, c->tune.largest_first};
+    int ints[9] = {c->cap, c->tree.cap_cells, c->precision, (int)c->mem.size(), c->tune.warps, c->tune.groups,
+                   c->tune.blocks_per_sm, c->tune.largest_first, c->tune.hi_occ};
     h = mix64(h, ints, sizeof ints);
     for (const Member &m : c->mem) {
         int lay[3] = {m.lo, m.n, m.cap};
@@ -949,10 +955,16 @@ int ov_autotune(ov_ctx *c, double t, ov_tuning *best_out, float *ms_best)
     const int maxg = std::min(c->geo.n_img + 1, 27);
     const int warps[3] = {2, 4, 8};
     const int groups[8] = {1, 2, 3, 4, 6, 9, 14, 27};
-    for (int stage = 0; stage < 4; ++stage) {
+    for (int stage = 0; stage < 5; ++stage) {
         std::vector<Tuning> cand;
         if (stage == 0)
-            for (int w : warps) { Tuning tu = best; tu.warps = w; cand.push_back(tu); }
+            for (int w : warps)
+                for (int ho = 0; ho <= (c->precision == OV_PREC_MIXED ? 1 : 0); ++ho) {
+                    Tuning tu = best;
+                    tu.warps = w;
+                    tu.hi_occ = ho;
+                    cand.push_back(tu);
+                }
         if (stage == 1)
             for (int g : groups)
                 if (g <= maxg) { Tuning tu = best; tu.groups = g; cand.push_back(tu); }
@@ -964,9 +976,12 @@ int ov_autotune(ov_ctx *c, double t, ov_tuning *best_out, float *ms_best)
         }
         if (stage == 3 && c->mem.size() > 1)
             for (int lf : {1, 0}) { Tuning tu = best; tu.largest_first = lf; cand.push_back(tu); }
+        if (stage == 4) {   // the block shape again, given the groups and grid picked
+            for (int w : warps) { Tuning tu = best; tu.warps = w; cand.push_back(tu); }
+        }
         for (const Tuning &tu : cand) {
             if (tu.warps == best.warps && tu.groups == best.groups && tu.blocks_per_sm == best.blocks_per_sm &&
-                tu.largest_first == best.largest_first)
+                tu.largest_first == best.largest_first && tu.hi_occ == best.hi_occ)
                 continue;
             float ms = 0;
             if ((r = trial(tu, &ms))) { c->tune = saved; if (c->mem.size() > 1) ov_upload_member_tables(c); return r; }

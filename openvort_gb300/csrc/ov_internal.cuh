@@ -157,6 +157,7 @@ struct Tuning {
     int groups = 0;        // query groups per node (0: from the node count)
     int blocks_per_sm = 0; // persistent blocks per SM (0: occupancy limit)
     int largest_first = 1; // work queue visits the largest member first
+    int hi_occ = 0;        // mixed traversal: the tighter register budget variant
 };
 
 struct ov_ctx {
@@ -195,7 +196,7 @@ struct ov_ctx {
     std::vector<double> h_x, h_y, h_z;
     std::vector<int> h_fwd, h_rev, h_status, h_pin, h_recalc;
     bool host_valid = false;     // the mirrors equal the device positions and topology
-    double step_ms[12] = {};     // host wall time of the last ov_step's passes (+ reconnect parts)
+    double step_ms[16] = {};     // host wall time of the last ov_step's passes (+ reconnect parts)
     // reconnect / smoothing scratch
     uint64_t *d_gkeys = nullptr, *d_gkeys_alt = nullptr;
     int *d_gidx = nullptr, *d_gidx_alt = nullptr;
@@ -204,6 +205,12 @@ struct ov_ctx {
     int *d_loop_nodes = nullptr, *d_loop_off = nullptr;
     double *d_loop_buf = nullptr;
     double *d_loop_cut = nullptr;
+    // long-loop smoothing (Bluestein FFT): work buffers, twiddles of size fft_M
+    double2 *fft_buf = nullptr, *fft_tw = nullptr;
+    size_t fft_cap = 0;
+    int fft_M = 0;
+    void *long_buf = nullptr;
+    size_t long_cap = 0;
     int loop_cap = 0, loop_nodes_cap = 0;
     size_t loop_buf_cap = 0;
     // RK4 graph: stage times and steps live in d_time = {t+dt/2, t+dt/2,
@@ -225,6 +232,8 @@ struct ov_ctx {
     int *rec_nodes = nullptr, *rec_pair = nullptr;
     double *rec_out = nullptr, *rec_corr = nullptr, *rec_part = nullptr;
     float *rec_split = nullptr;
+    double *h_corr = nullptr;    // pinned host copy of the corrections
+    size_t h_corr_cap = 0;
     int rec_cap = 0, rec_split_cap = 0;
     size_t rec_part_cap = 0;
     // direct-sum scratch
@@ -286,8 +295,8 @@ int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out
 // reconnection velocities (ov_velocity.cu)
 int ov_rec_begin(ov_ctx *c, const int *cand, int n, double *out);
 int ov_rec_exact(ov_ctx *c, int k, int l, double out[10]);
-int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const double *sign, int nch,
-                   double *corr_out);
+int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const double *sign, int nch);
+int ov_rec_fetch(ov_ctx *c, int c0, int n, double *out);
 void ov_launch_euler(ov_ctx *c, const NodeArrays &src, const double *vx, const double *vy,
                      const double *vz, double dt, NodeArrays &dst, cudaStream_t s);
 void ov_launch_rk4_combine(ov_ctx *c, double dt, cudaStream_t s);

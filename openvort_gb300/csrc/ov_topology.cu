@@ -523,6 +523,145 @@ __global__ void __launch_bounds__(256) k_smooth(SmoothArgs a)
     }
 }
 
+// ---- smoothing of long loops: Bluestein DFT on an FP64 Stockham FFT
+//
+// A loop too long for one block's shared memory is low-pass filtered with
+// the same half-complex bin mask through an exact DFT of its (arbitrary)
+// length N written as a convolution of length M = 2^p >= 2N - 1 (Bluestein):
+//   X_k = conj(w_k) sum_n (x_n conj(w_n)) w_(k-n),  w_n = exp(i pi n^2 / N),
+// the convolution done by radix-2 Stockham FFTs (ping-pong buffers, twiddle
+// table exp(-2 pi i t / M) computed once per M), the inverse by conjugation.
+// Three coordinates go through each pass as a batch.
+
+// exp(i pi n^2 / N) with n^2 reduced mod 2N exactly
+__device__ __forceinline__ double2 chirp(long long n, long long N)
+{
+    long long r = (n * n) % (2 * N);
+    double s, c;
+    sincospi((double)r / (double)N, &s, &c);
+    return make_double2(c, s);
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__global__ void k_twiddles(double2 *tw, int M)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= M / 2) return;
+    double s, c;
+    sincospi(-2.0 * (double)t / (double)M, &s, &c);
+    tw[t] = make_double2(c, s);
+}
+
+// b_n = w_n for |n| < N (wrapped into [0, M)), else 0
+__global__ void k_chirp_filter(double2 *b, int N, int M)
+{
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= M) return;
+    double2 v = make_double2(0, 0);
+    if (n < N) v = chirp(n, N);
+    else if (n > M - N) v = chirp(M - n, N);
+    b[n] = v;
+}
+
+// a[c][n] = in[c][n] conj(w_n) (n < N), zero padded to M; in is complex
+// (stride N per coordinate) or, when re != nullptr, real
+__global__ void k_chirp_in(const double *re, const double2 *in, int N, int M, double2 *a)
+{
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = blockIdx.y;
+    if (n >= M) return;
+    double2 v = make_double2(0, 0);
+    if (n < N) {
+        double2 x = re ? make_double2(re[(size_t)c * N + n], 0.0) : in[(size_t)c * N + n];
+        double2 w = chirp(n, N);
+        v = cmul(x, make_double2(w.x, -w.y));
+    }
+    a[(size_t)c * M + n] = v;
+}
+
+// one radix-2 Stockham pass over `batch` sequences of length M
+__global__ void k_fft_pass(const double2 *__restrict__ in, double2 *__restrict__ out, const double2 *__restrict__ tw,
+                           int M, int Ns)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = blockIdx.y;
+    if (j >= M / 2) return;
+    const double2 *x = in + (size_t)c * M;
+    double2 *y = out + (size_t)c * M;
+    int k = j & (Ns - 1);
+    double2 w = tw[(size_t)k * (M / (2 * Ns))];
+    double2 v0 = x[j], v1 = cmul(x[j + M / 2], w);
+    int d = ((j - k) << 1) + k;
+    y[d] = make_double2(v0.x + v1.x, v0.y + v1.y);
+    y[d + Ns] = make_double2(v0.x - v1.x, v0.y - v1.y);
+}
+
+// A[c] <- conj(A[c] * B) (the inverse transform runs as a forward one on
+// the conjugate)
+__global__ void k_conv_mul(double2 *A, const double2 *__restrict__ B, int M)
+{
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = blockIdx.y;
+    if (n >= M) return;
+    double2 v = cmul(A[(size_t)c * M + n], B[n]);
+    A[(size_t)c * M + n] = make_double2(v.x, -v.y);
+}
+
+// X_k = conj(w_k) conj(c_k) / M for k < N (c = FFT of the conjugated product)
+__global__ void k_chirp_out(const double2 *cbuf, int N, int M, double2 *X)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = blockIdx.y;
+    if (k >= N) return;
+    double2 v = cbuf[(size_t)c * M + k];
+    v = make_double2(v.x / M, -v.y / M);
+    double2 w = chirp(k, N);
+    X[(size_t)c * N + k] = cmul(v, make_double2(w.x, -w.y));
+}
+
+// The reference's half-complex mask (vortex_smooth.c:146-160): element h of
+// the R2HC array (real part of bin h for h <= N/2, imaginary part of bin
+// N - h above) is zeroed for h in [zlo, zhi); the spectrum stays Hermitian.
+// Writes conj(X') for the inverse transform.
+__global__ void k_lowpass_mask(double2 *X, int N, int zlo, int zhi)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = blockIdx.y;
+    if (k >= N) return;
+    int kk = k <= N / 2 ? k : N - k;   // bin of the half-complex pair
+    double2 v = X[(size_t)c * N + k];
+    bool keep_re = !(kk >= zlo && kk < zhi);
+    bool keep_im = kk == 0 || (2 * kk == N) || !((N - kk) >= zlo && (N - kk) < zhi);
+    if (kk == 0 || 2 * kk == N) v.y = 0;
+    if (!keep_re) v.x = 0;
+    if (!keep_im) v.y = 0;
+    X[(size_t)c * N + k] = make_double2(v.x, -v.y);
+}
+
+// positions of the loop from the filtered sequence: out = Re(y)/N (+ the
+// chord of a detrended loop)
+__global__ void k_long_writeback(const double2 *__restrict__ Y, int N, int len, const int *__restrict__ nodes,
+                                 int detrend, double cx, double cy, double cz, double ox, double oy, double oz,
+                                 double *x, double *y, double *z, int cap)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= len) return;
+    int node = nodes[j];
+    if (node < 0 || node >= cap) return;
+    // Y = FFT(conj X') conjugated and / N on read: x_j = Re(conj(Y_j)) / N
+    double o[3];
+    const double co[3] = {cx, cy, cz}, c0[3] = {ox, oy, oz};
+    for (int a = 0; a < 3; ++a) {
+        o[a] = Y[(size_t)a * N + j].x / N;
+        if (detrend) o[a] = o[a] + co[a] * j + c0[a];
+    }
+    x[node] = o[0]; y[node] = o[1]; z[node] = o[2];
+}
+
 }  // namespace
 
 // ------------------------------------------------------------ host mirror
@@ -904,6 +1043,136 @@ int find_pairs(ov_ctx *c, std::vector<std::pair<int, int>> &out)
 
 }  // namespace
 
+namespace {
+
+// Forward DFT of 3 sequences of length N (real `re` or complex `cin`, N per
+// coordinate) into X (3N complex), by Bluestein over radix-2 FFTs.
+int bluestein3(ov_ctx *c, const double *re, const double2 *cin, int N, double2 *X)
+{
+    int M = 1;
+    while (M < 2 * N - 1) M <<= 1;
+    if (M < 2) M = 2;
+    cudaStream_t st = c->stream;
+    // buffers: A, T (3M each), B, TB (M each), twiddles (M/2)
+    size_t need = (size_t)8 * M;
+    if (c->fft_cap < need) {
+        if (c->fft_buf) cudaFree(c->fft_buf);
+        c->fft_buf = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->fft_buf, need * sizeof(double2)));
+        c->fft_cap = need;
+        c->fft_M = 0;
+    }
+    double2 *A = c->fft_buf, *T = A + 3 * (size_t)M, *B = T + 3 * (size_t)M, *TB = B + M;
+    double2 *tw = c->fft_tw;
+    if (c->fft_M != M) {
+        if (c->fft_tw) cudaFree(c->fft_tw);
+        c->fft_tw = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->fft_tw, (size_t)std::max(M / 2, 1) * sizeof(double2)));
+        tw = c->fft_tw;
+        k_twiddles<<<(M / 2 + 255) / 256, 256, 0, st>>>(tw, M);
+        c->fft_M = M;
+        c->launches++;
+    }
+    auto fft = [&](double2 *x, double2 *y, int batch) -> double2 * {
+        for (int Ns = 1; Ns < M; Ns <<= 1) {
+            k_fft_pass<<<dim3((M / 2 + 255) / 256, batch), 256, 0, st>>>(x, y, tw, M, Ns);
+            c->launches++;
+            std::swap(x, y);
+        }
+        return x;   // holds the result
+    };
+    const dim3 gM((M + 255) / 256, 3), gN((N + 255) / 256, 3);
+    k_chirp_filter<<<(M + 255) / 256, 256, 0, st>>>(B, N, M);
+    k_chirp_in<<<gM, 256, 0, st>>>(re, cin, N, M, A);
+    c->launches += 2;
+    double2 *Bf = fft(B, TB, 1);
+    double2 *Af = fft(A, T, 3);
+    k_conv_mul<<<gM, 256, 0, st>>>(Af, Bf, M);
+    c->launches++;
+    double2 *Cf = fft(Af, Af == A ? T : A, 3);
+    k_chirp_out<<<gN, 256, 0, st>>>(Cf, N, M, X);
+    c->launches++;
+    OV_CUDA(c, cudaGetLastError());
+    return OV_OK;
+}
+
+// Loops of more than this many nodes are smoothed through the FFT path.
+constexpr int kLongLoop = 1024;
+
+// smooth one long closed loop (nodes in loop order), as k_smooth does for
+// short ones: unwrap and detrend on the host mirror, filter on the GPU,
+// write the positions back on the GPU
+int smooth_long_loop(ov_ctx *c, const int *nodes, int len, double freq_to_cutoff)
+{
+    Host h{c, 0, c->n_live, &c->params};
+    const Geometry &g = c->geo;
+    std::vector<double> X[3];
+    for (auto &v : X) v.assign((size_t)2 * len, 0.0);
+    double prev[3];
+    h.pos(nodes[0], prev);
+    for (int a = 0; a < 3; ++a) X[a][0] = prev[a];
+    for (int j = 1; j < len; ++j) {
+        double r2[3], r1[3] = {X[0][j - 1], X[1][j - 1], X[2][j - 1]};
+        h.pos(nodes[j], r2);
+        hpwrap(g, r1, r2);
+        for (int a = 0; a < 3; ++a) X[a][j] = r2[a];
+    }
+    double gx = X[0][0] - X[0][len - 1], gy = X[1][0] - X[1][len - 1], gz = X[2][0] - X[2][len - 1];
+    double gap = sqrt(gx * gx + gy * gy + gz * gz);
+    const int detrend = (gap > g.L[0] / 2 && len > 2) ? 1 : 0;
+    const int N = detrend ? 2 * len - 2 : len;
+    double coef[3] = {0, 0, 0}, c0[3] = {0, 0, 0};
+    if (detrend) {
+        for (int a = 0; a < 3; ++a) {
+            coef[a] = (X[a][len - 1] - X[a][0]) / (len - 1);
+            c0[a] = X[a][0];
+        }
+        for (int a = 0; a < 3; ++a) {
+            for (int j = 0; j < len; ++j)
+                X[a][j] = (j == 0 || j == len - 1) ? 0.0 : X[a][j] - coef[a] * j - c0[a];
+            for (int j = 0; j < len - 2; ++j) X[a][len + j] = -X[a][len - 2 - j];
+        }
+    }
+    std::vector<double> flat((size_t)3 * N);
+    for (int a = 0; a < 3; ++a) std::copy(X[a].begin(), X[a].begin() + N, flat.begin() + (size_t)a * N);
+    size_t need = (size_t)3 * N * sizeof(double) + (size_t)2 * 3 * N * sizeof(double2) + (size_t)len * sizeof(int);
+    if (c->long_cap < need) {
+        if (c->long_buf) cudaFree(c->long_buf);
+        c->long_buf = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->long_buf, need));
+        c->long_cap = need;
+    }
+    // complex arrays first: every double2 stays 16-byte aligned
+    double2 *d_X = (double2 *)c->long_buf;
+    double2 *d_Z = d_X + 3 * (size_t)N;
+    double *d_re = (double *)(d_Z + 3 * (size_t)N);
+    int *d_nodes = (int *)(d_re + 3 * (size_t)N);
+    OV_CUDA(c, cudaMemcpyAsync(d_re, flat.data(), flat.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    OV_CUDA(c, cudaMemcpyAsync(d_nodes, nodes, (size_t)len * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    int r;
+    if ((r = bluestein3(c, d_re, nullptr, N, d_X))) return r;
+    // low_pass_filter's zeroed range (vortex_smooth.c:146-160)
+    int cut = (int)(freq_to_cutoff * N / 2);
+    int zlo = 0, zhi = 0;
+    if (N > 2 * cut + 1) {
+        zlo = N / 2 - cut;
+        zhi = (N % 2 == 0) ? N / 2 + 1 + cut : N / 2 + cut;
+    }
+    const dim3 gN((N + 255) / 256, 3);
+    k_lowpass_mask<<<gN, 256, 0, c->stream>>>(d_X, N, zlo, zhi);
+    c->launches++;
+    if ((r = bluestein3(c, nullptr, d_X, N, d_Z))) return r;
+    k_long_writeback<<<(len + 255) / 256, 256, 0, c->stream>>>(d_Z, N, len, d_nodes, detrend, coef[0], coef[1],
+                                                               coef[2], c0[0], c0[1], c0[2], c->node.x, c->node.y,
+                                                               c->node.z, c->cap);
+    c->launches++;
+    OV_CUDA(c, cudaGetLastError());
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));   // the host buffers above go out of scope
+    return OV_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int ov_eliminate_small_loops(ov_ctx *c)
@@ -971,6 +1240,7 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         return std::chrono::duration<double, std::milli>(clk() - t0).count();
     };
     auto tr = clk();
+    for (int i = 8; i < 16; ++i) c->step_ms[i] = 0;
     if ((r = ov_pull_host(c))) return r;
     c->host_valid = false;
     std::vector<std::pair<int, int>> pairs;
@@ -986,8 +1256,26 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     std::sort(cand.begin(), cand.end());
     cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
     const int C = (int)cand.size();
-    std::vector<double> rec(5 * (size_t)C), corr(3 * (size_t)C, 0.0);
+    std::vector<double> rec(5 * (size_t)C);
+    // corrections read back from the device (pinned: many small copies)
+    if (c->h_corr_cap < 4 * (size_t)std::max(C, 1)) {
+        if (c->h_corr) cudaFreeHost(c->h_corr);
+        c->h_corr = nullptr;
+        OV_CUDA(c, cudaMallocHost(&c->h_corr, 4 * (size_t)std::max(C, 1) * sizeof(double)));
+        c->h_corr_cap = 4 * (size_t)std::max(C, 1);
+    }
+    double *corr = c->h_corr;
+    std::fill(corr, corr + 4 * (size_t)C, 0.0);
     std::vector<char> exact(C, 0);
+    // corrections on the host are read back lazily, a window at a time:
+    // corr_gen[i] < gen means candidate i's copy predates the last rewiring
+    std::vector<int> corr_gen(C, 0);
+    int gen = 0;
+    const int kFetch = 2048;
+    int64_t evaluated = 0;
+    c->stats.reconnect_candidates = C;
+    c->stats.reconnect_fp64_pairs = 0;
+    c->stats.reconnect_exact_pairs = 0;
     if (C && (r = ov_rec_begin(c, cand.data(), C, rec.data()))) return r;
     c->step_ms[9] = ms_since(tr);
     tr = clk();
@@ -1020,12 +1308,20 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         double vs[3];
         if (!hlia(h, k, tg, nm, t, vs)) return false;
         int ci = cand_index(k);
-        const double *rc = &rec[5 * (size_t)ci];
-        for (int a = 0; a < 3; ++a) vs[a] = vs[a] + (rc[a] + corr[3 * (size_t)ci + a]);
+        if (corr_gen[ci] < gen) {
+            const auto tf = clk();
+            const int n = std::min(ce, ci + kFetch) - ci;
+            if (ov_rec_fetch(c, ci, n, corr + 4 * (size_t)ci)) return false;
+            std::fill(corr_gen.begin() + ci, corr_gen.begin() + ci + n, gen);
+            c->step_ms[12] += ms_since(tf);
+        }
+        ++evaluated;
+        const double *rc = &rec[5 * (size_t)ci], *cc = &corr[4 * (size_t)ci];
+        for (int a = 0; a < 3; ++a) vs[a] = vs[a] + (rc[a] + cc[a]);
         hfriction(h, k, tg, vs, t, vel);
         const double tl = hlen(tg);
         const double n_terms = (double)(h.hi - h.lo) * (g.n_img + 1);
-        const double comp = rc[3] + n_terms * 1.1102230246251565e-16 * rc[4];
+        const double comp = rc[3] + cc[3] + n_terms * 1.1102230246251565e-16 * rc[4];
         // the friction terms are linear in vs: |d vel| <= |d vs| (1 + alpha |t| + alpha' |t|^2)
         *bound = comp * 1.7320508075688772 * 1.01 * (1.0 + fabs(h.P->alpha) * tl + fabs(h.P->alpha_p) * tl * tl);
         return true;
@@ -1070,8 +1366,11 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
                 // the mixed-precision sums cannot decide: FP64 sums of both
                 int ck = cand_index(k), cl = cand_index(l);
                 if (!exact[ck] || !exact[cl]) {
+                    ++c->stats.reconnect_fp64_pairs;
                     double ex[10];
+                    const auto te = clk();
                     if ((r = ov_rec_exact(c, k, l, ex))) return r;
+                    c->step_ms[14] += ms_since(te);
                     for (int a = 0; a < 5; ++a) {
                         rec[5 * (size_t)ck + a] = ex[a];
                         rec[5 * (size_t)cl + a] = ex[5 + a];
@@ -1086,8 +1385,11 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
             if (fabs(proj) <= hlen(dx) * (bk + bl) + 1e-9 * hlen(dx) * hlen(dv)) {
                 // too close to call after a different summation order: redo
                 // both velocities exactly as the reference sums them
+                ++c->stats.reconnect_exact_pairs;
+                const auto tx = clk();
                 hdirect_exact(h, k, tk, nk, t, vk);
                 hdirect_exact(h, l, tl, nl_, t, vl);
+                c->step_ms[15] += ms_since(tx);
                 hsub(dv, vk, vl);
                 proj = hdot(dx, dv);
             }
@@ -1116,9 +1418,13 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
                 h.rev(ln) = kp; h.fwd(kp) = ln;
                 cm[2] = l; cfw[2] = k; cm[3] = kp; cfw[3] = ln;
             }
-            // the four changed segments' contributions to the member's candidates
-            if (ce > cb && (r = ov_rec_correct(c, cb, ce - cb, cm, cfw, csg, 4, corr.data() + 3 * (size_t)cb)))
-                return r;
+            // the four changed segments' contributions to the member's
+            // candidates still to come (pairs are (k, l > k), sorted by k)
+            const int cfrom = cand_index(k) + 1;
+            const auto tc = clk();
+            if (ce > cfrom && (r = ov_rec_correct(c, cfrom, ce - cfrom, cm, cfw, csg, 4))) return r;
+            c->step_ms[13] += ms_since(tc);
+            ++gen;
             recalc[k]++; recalc[h.fwd(k)]++; recalc[h.rev(k)]++; recalc[kn]++; recalc[kp]++;
             recalc[l]++; recalc[h.fwd(l)]++; recalc[h.rev(l)]++; recalc[ln]++; recalc[lp]++;
             if (log_k && log_l && nrec < log_cap) { log_k[nrec] = k; log_l[nrec] = l; }
@@ -1128,6 +1434,7 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         i = e;
     }
     c->stats.reconnections = nrec;
+    c->stats.reconnect_evaluated = evaluated;
     if (nrecs) *nrecs = nrec;
     c->step_ms[10] = ms_since(tr);
     tr = clk();
@@ -1150,8 +1457,8 @@ int ov_smooth(ov_ctx *c)
     if ((r = ov_pull_host(c))) return r;
     // closed loops of each filtering member in the reference's discovery
     // order (vortex_smooth.c:192-210)
-    std::vector<int> off{0}, nodes;
-    std::vector<double> cut;
+    std::vector<int> off{0}, nodes, long_off, long_nodes;
+    std::vector<double> cut, long_cut;
     int maxlen = 0;
     for (int mi = 0; mi < (int)c->mem.size(); ++mi) {
         if (!c->mem[mi].params.use_freq_filter) continue;
@@ -1166,16 +1473,33 @@ int ov_smooth(ov_ctx *c)
             if (h.rev(j) == -1 || guard > N) { seen[i - lo] = 1; continue; }   // open line: not smoothed
             int len = 0;
             int m = i;
+            const size_t start = nodes.size();
             do {
                 nodes.push_back(m);
                 if (m >= lo && m < h.hi) seen[m - lo] = 1;
                 m = h.fwd(m);
                 ++len;
             } while (m != i && m >= 0 && len <= N);
+            if (len > kLongLoop) {
+                // long loop: the FFT path, after the short ones
+                long_off.push_back((int)long_nodes.size());
+                long_nodes.insert(long_nodes.end(), nodes.begin() + start, nodes.end());
+                long_cut.push_back(h.P->freq_to_cutoff);
+                nodes.resize(start);
+                continue;
+            }
             off.push_back((int)nodes.size());
             cut.push_back(h.P->freq_to_cutoff);
             maxlen = std::max(maxlen, len);
         }
+    }
+    long_off.push_back((int)long_nodes.size());
+    // long loops first (they read the host mirror, which the short-loop
+    // kernel does not touch; loops share no nodes)
+    for (size_t q = 0; q + 1 < long_off.size(); ++q) {
+        if ((r = smooth_long_loop(c, long_nodes.data() + long_off[q], long_off[q + 1] - long_off[q], long_cut[q])))
+            return r;
+        c->host_valid = false;
     }
     int nloops = (int)off.size() - 1;
     if (nloops == 0) return OV_OK;
@@ -1230,7 +1554,7 @@ int ov_step(ov_ctx *c, double t, double dt)
     // host wall time of each pass: small loops, reconnect, smooth, periodic,
     // remesh, update_tangle, rk4_step, total
     double *ms = c->step_ms;
-    for (int i = 0; i < 12; ++i) ms[i] = 0;
+    for (int i = 0; i < 16; ++i) ms[i] = 0;
     auto now = [] { return std::chrono::steady_clock::now(); };
     auto since = [&](std::chrono::steady_clock::time_point t0) {
         return std::chrono::duration<double, std::milli>(now() - t0).count();
@@ -1265,7 +1589,7 @@ int ov_step(ov_ctx *c, double t, double dt)
 int ov_step_times(const ov_ctx *c, double *ms, int n)
 {
     if (!c || !ms || n < 0) return OV_ERR_ARG;
-    for (int i = 0; i < n && i < 12; ++i) ms[i] = c->step_ms[i];
+    for (int i = 0; i < n && i < 16; ++i) ms[i] = c->step_ms[i];
     return OV_OK;
 }
 

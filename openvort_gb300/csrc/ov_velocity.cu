@@ -412,7 +412,11 @@ __device__ __forceinline__ int next_item(const VelArgs &a)
 // order, so the result does not depend on which warp took which item.
 // Resident blocks per SM the register budget is sized for (about 24 warps).
 template <int W> constexpr int min_blocks() { return W == 2 ? 12 : (W == 4 ? 6 : 3); }
-template <int W> constexpr int min_blocks_mixed() { return W == 2 ? 10 : (W == 4 ? 5 : 2); }
+// (HI: a tighter register budget for one more block per SM, paid in spills)
+template <int W, int HI> constexpr int min_blocks_mixed()
+{
+    return W == 2 ? (HI ? 12 : 10) : (W == 4 ? (HI ? 6 : 5) : (HI ? 3 : 2));
+}
 
 template <int W>
 __global__ void __launch_bounds__(32 * W, min_blocks<W>()) k_vel_fp64(VelArgs a, double *__restrict__ part_out)
@@ -794,8 +798,9 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
     m.nstep += steps;
 }
 
-template <int W>
-__global__ void __launch_bounds__(32 * W, min_blocks_mixed<W>()) k_vel_mixed(VelArgs a, double *__restrict__ part_out)
+template <int W, int HI>
+__global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mixed(VelArgs a,
+                                                                                  double *__restrict__ part_out)
 {
     const int lane = threadIdx.x & 31;
     const int tiles = a.counters[TC_ITEMS];
@@ -988,12 +993,17 @@ int ov_reserve_velocity_scratch(ov_ctx *c)
 
 // Traversal kernel for a precision and block shape.
 typedef void (*VelKernel)(VelArgs, double *);
-static VelKernel vel_kernel(int precision, int warps)
+static VelKernel vel_kernel(int precision, int warps, int hi_occ)
 {
     if (precision == OV_PREC_MIXED) {
-        if (warps == 2) return k_vel_mixed<2>;
-        if (warps == 8) return k_vel_mixed<8>;
-        return k_vel_mixed<4>;
+        if (hi_occ) {
+            if (warps == 2) return k_vel_mixed<2, 1>;
+            if (warps == 8) return k_vel_mixed<8, 1>;
+            return k_vel_mixed<4, 1>;
+        }
+        if (warps == 2) return k_vel_mixed<2, 0>;
+        if (warps == 8) return k_vel_mixed<8, 0>;
+        return k_vel_mixed<4, 0>;
     }
     if (warps == 2) return k_vel_fp64<2>;
     if (warps == 8) return k_vel_fp64<8>;
@@ -1004,7 +1014,7 @@ static VelKernel vel_kernel(int precision, int warps)
 // every SM, but no more blocks than there can be work items.
 int ov_traversal_blocks(ov_ctx *c, int precision, int warps, int *per_sm)
 {
-    VelKernel k = vel_kernel(precision, warps);
+    VelKernel k = vel_kernel(precision, warps, c->tune.hi_occ);
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * warps, 0) != cudaSuccess || occ < 1) {
         cudaGetLastError();
@@ -1031,7 +1041,7 @@ int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precisio
     if (warps != 2 && warps != 8) warps = 4;
     int blocks = ov_traversal_blocks(c, precision, warps, nullptr);
     OV_CUDA(c, cudaMemsetAsync(a.work, 0, sizeof(int), s));
-    vel_kernel(precision, warps)<<<blocks, 32 * warps, 0, s>>>(a, c->part);
+    vel_kernel(precision, warps, c->tune.hi_occ)<<<blocks, 32 * warps, 0, s>>>(a, c->part);
     k_vel_finish<<<(c->cap + 127) / 128, 128, 0, s>>>(a, c->part);
     c->launches += 2;
     return OV_OK;
@@ -1276,6 +1286,7 @@ __global__ void __launch_bounds__(kRecThreads) k_rec_sums(RecArgs r, const int *
             sv[a] = (bg - ag[a]) + (bf - af[a]);
         }
         const float slen = sqrtf(fmaf(sv[0], sv[0], fmaf(sv[1], sv[1], sv[2] * sv[2])));
+        float t0 = 0, t1 = 0, t2 = 0;   // this segment's terms over the query points
         for (int qi = 0; qi < nq; ++qi) {
             const int j = qi - 1;
             if (j < 0 && (m == k || f == k)) continue;   // the node's own segments (primary only)
@@ -1306,11 +1317,14 @@ __global__ void __launch_bounds__(kRecThreads) k_rec_sums(RecArgs r, const int *
             if (nd < 1e-8f) continue;   // ndot filter (far from its threshold here)
             const float sc = __fdividef(r.f4pif * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
             // R x Rp1 = R x s
-            kahan_add(s0, c0, fmaf(R[1], sv[2], -R[2] * sv[1]) * sc);
-            kahan_add(s1, c1, fmaf(R[2], sv[0], -R[0] * sv[2]) * sc);
-            kahan_add(s2, c2, fmaf(R[0], sv[1], -R[1] * sv[0]) * sc);
+            t0 = fmaf(fmaf(R[1], sv[2], -R[2] * sv[1]), sc, t0);
+            t1 = fmaf(fmaf(R[2], sv[0], -R[0] * sv[2]), sc, t1);
+            t2 = fmaf(fmaf(R[0], sv[1], -R[1] * sv[0]), sc, t2);
             mag += sc * slen * lR2 * ra;   // sc |R| |s| >= |w| (per component)
         }
+        kahan_add(s0, c0, t0);
+        kahan_add(s1, c1, t1);
+        kahan_add(s2, c2, t2);
     }
     red[0][threadIdx.x] = ((double)s0 - (double)c0) + d0;
     red[1][threadIdx.x] = ((double)s1 - (double)c1) + d1;
@@ -1340,7 +1354,7 @@ __global__ void k_rec_finish(const double *__restrict__ part, int n, int max_chu
         for (int v = 0; v < kRecVals; ++v) acc[v] += part[((size_t)b * max_chunks + ch) * kRecVals + v];
     const double eps32 = 5.9604644775390625e-8;
     for (int a = 0; a < 3; ++a) out[5 * (size_t)b + a] = acc[a];
-    out[5 * (size_t)b + 3] = 1.01 * (64.0 * eps32 * acc[3] + 4.0 * eps32 * acc[5]) + 1e-12 * (acc[4] + acc[3]);
+    out[5 * (size_t)b + 3] = 1.01 * ((64.0 + 28.0) * eps32 * acc[3] + 4.0 * eps32 * acc[5]) + 1e-12 * (acc[4] + acc[3]);
     out[5 * (size_t)b + 4] = 1.01 * (acc[3] + acc[4]);
 }
 
@@ -1351,7 +1365,9 @@ struct RecChange {
 };
 
 // Contribution of the changed segments to candidates [c0, c0 + nc) of the
-// sorted candidate list, one thread per (candidate, query point).
+// sorted candidate list, one thread per (candidate, query point): FP32 on
+// the split positions with the error bound of k_rec_sums, FP64 near the
+// query point.  part: 4 doubles per thread (3 sums, bound).
 __global__ void k_corr(RecArgs r, const int *__restrict__ cand, int c0, int nc, RecChange ch,
                        double *__restrict__ part)
 {
@@ -1359,29 +1375,81 @@ __global__ void k_corr(RecArgs r, const int *__restrict__ cand, int c0, int nc, 
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= nc * nq) return;
     int ci = idx / nq, qi = idx - ci * nq;
+    const int j = qi - 1;
     int k = cand[c0 + ci];
     double acc[3] = {0, 0, 0};
+    double bound = 0;
     if (k >= 0 && k < r.cap) {
         const double p[3] = {r.x[k], r.y[k], r.z[k]};
+        float qg[3], qf[3];
+        for (int a = 0; a < 3; ++a) {
+            qg[a] = r.sp[(size_t)a * r.cap + k];
+            qf[a] = r.sp[(size_t)(3 + a) * r.cap + k];
+            if (j >= 0) { qg[a] -= r.shift_g[j][a]; qf[a] -= r.shift_f[j][a]; }
+        }
         for (int i = 0; i < ch.n && i < 8; ++i) {
             int m = ch.m[i], f = ch.f[i];
             if (m < 0 || m >= r.cap || f < 0 || f >= r.cap) continue;
-            double w[3];
-            if (rec_term64(r, m, f, qi - 1, p, w))
-                for (int a = 0; a < 3; ++a) acc[a] += ch.sign[i] * w[a];
+            float ag[3], af[3], sv[3];
+            bool use64 = false;
+            for (int a = 0; a < 3; ++a) {
+                ag[a] = r.sp[(size_t)a * r.cap + m];
+                af[a] = r.sp[(size_t)(3 + a) * r.cap + m];
+                float bg = r.sp[(size_t)a * r.cap + f], bf = r.sp[(size_t)(3 + a) * r.cap + f];
+                float d = (bg - ag[a]) + (bf - af[a]);
+                if (r.geo.periodic[a]) {
+                    if (fabsf(fabsf(d) - r.hL[a]) < 1e-3f * r.hL[a] || fabsf(d) > 3.0f * r.hL[a]) use64 = true;
+                    if (d > r.hL[a]) { bg -= r.Lg[a]; bf -= r.Lf[a]; }
+                    else if (d < -r.hL[a]) { bg += r.Lg[a]; bf += r.Lf[a]; }
+                }
+                sv[a] = (bg - ag[a]) + (bf - af[a]);
+            }
+            float R[3];
+            for (int a = 0; a < 3; ++a) R[a] = (ag[a] - qg[a]) + (af[a] - qf[a]);
+            const float lR2 = fmaf(R[0], R[0], fmaf(R[1], R[1], R[2] * R[2]));
+            const float P0 = R[0] + sv[0], P1 = R[1] + sv[1], P2 = R[2] + sv[2];
+            const float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
+            use64 = use64 || lR2 < r.rnear2 || lp2 < r.rnear2;
+            float ra = 0, rb = 0, ab = 0, dot = 0, nd = 0;
+            if (!use64) {
+                ra = rsqrtf(lR2);
+                rb = rsqrtf(lp2);
+                ab = ra * rb;
+                dot = fmaf(R[0], P0, fmaf(R[1], P1, R[2] * P2));
+                nd = dot * ab;
+                if (fabsf(nd - 1e-8f) < 1e-4f) use64 = true;
+            }
+            if (use64) {
+                double w[3];
+                if (rec_term64(r, m, f, j, p, w)) {
+                    for (int a = 0; a < 3; ++a) acc[a] += ch.sign[i] * w[a];
+                    bound += 1e-12 * (fabs(w[0]) + fabs(w[1]) + fabs(w[2]));
+                }
+                continue;
+            }
+            if (nd < 1e-8f) continue;
+            const float sc = __fdividef(r.f4pif * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
+            const float slen = sqrtf(fmaf(sv[0], sv[0], fmaf(sv[1], sv[1], sv[2] * sv[2])));
+            acc[0] += ch.sign[i] * (double)(fmaf(R[1], sv[2], -R[2] * sv[1]) * sc);
+            acc[1] += ch.sign[i] * (double)(fmaf(R[2], sv[0], -R[0] * sv[2]) * sc);
+            acc[2] += ch.sign[i] * (double)(fmaf(R[0], sv[1], -R[1] * sv[0]) * sc);
+            bound += 1.01 * 64.0 * 5.9604644775390625e-8 * (double)(sc * slen * lR2 * ra);
         }
     }
-    for (int a = 0; a < 3; ++a) part[(size_t)idx * 3 + a] = acc[a];
+    for (int a = 0; a < 3; ++a) part[(size_t)idx * 4 + a] = acc[a];
+    part[(size_t)idx * 4 + 3] = bound;
 }
 
+// corr[4 c + {0,1,2}] += the query points' sums in order, corr[4 c + 3] += bound
 __global__ void k_corr_finish(const double *__restrict__ part, int nc, int nq, double *__restrict__ corr)
 {
     int ci = blockIdx.x * blockDim.x + threadIdx.x;
     if (ci >= nc) return;
-    double acc[3] = {0, 0, 0};
+    double acc[4] = {0, 0, 0, 0};
     for (int q = 0; q < nq; ++q)
-        for (int a = 0; a < 3; ++a) acc[a] += part[((size_t)ci * nq + q) * 3 + a];
-    for (int a = 0; a < 3; ++a) corr[3 * (size_t)ci + a] += acc[a];
+        for (int a = 0; a < 4; ++a) acc[a] += part[((size_t)ci * nq + q) * 4 + a];
+    for (int a = 0; a < 3; ++a) corr[4 * (size_t)ci + a] += acc[a];
+    corr[4 * (size_t)ci + 3] += acc[3] * (1.0 + 1e-9) + 1e-15 * (fabs(acc[0]) + fabs(acc[1]) + fabs(acc[2]));
 }
 
 RecArgs make_rec_args(ov_ctx *c)
@@ -1425,7 +1493,7 @@ int rec_reserve(ov_ctx *c, int n, int max_chunks)
 {
     size_t need_part = (size_t)std::max(n, 1) * max_chunks * kRecVals;
     const int nq = c->geo.n_img + 1;
-    need_part = std::max(need_part, (size_t)std::max(n, 1) * nq * 3);
+    need_part = std::max(need_part, (size_t)std::max(n, 1) * nq * 4);
     if (c->rec_part_cap < need_part) {
         if (c->rec_part) cudaFree(c->rec_part);
         c->rec_part = nullptr;
@@ -1439,7 +1507,7 @@ int rec_reserve(ov_ctx *c, int n, int max_chunks)
         c->rec_nodes = nullptr; c->rec_out = nullptr; c->rec_corr = nullptr;
         OV_CUDA(c, cudaMalloc(&c->rec_nodes, (size_t)n * sizeof(int)));
         OV_CUDA(c, cudaMalloc(&c->rec_out, (size_t)n * 5 * sizeof(double)));
-        OV_CUDA(c, cudaMalloc(&c->rec_corr, (size_t)n * 3 * sizeof(double)));
+        OV_CUDA(c, cudaMalloc(&c->rec_corr, (size_t)n * 4 * sizeof(double)));
         c->rec_cap = n;
     }
     if (c->rec_split_cap < c->cap) {
@@ -1484,7 +1552,7 @@ int ov_rec_begin(ov_ctx *c, const int *cand, int n, double *out)
     int r = rec_reserve(c, n, std::max(1, (maxcap + 8191) / 8192));
     if (r) return r;
     OV_CUDA(c, cudaMemcpyAsync(c->rec_nodes, cand, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    OV_CUDA(c, cudaMemsetAsync(c->rec_corr, 0, (size_t)n * 3 * sizeof(double), c->stream));
+    OV_CUDA(c, cudaMemsetAsync(c->rec_corr, 0, (size_t)n * 4 * sizeof(double), c->stream));
     k_split<<<(c->cap + 255) / 256, 256, 0, c->stream>>>(c->node.x, c->node.y, c->node.z, c->cap, c->grid_h,
                                                         1.0 / c->grid_h, c->rec_split);
     c->launches++;
@@ -1520,10 +1588,10 @@ extern "C" int ov_direct_sums_bounded(ov_ctx *c, const int *nodes, int n, int pr
     return rec_launch_sums(c, c->rec_nodes, n, precision == OV_PREC_FP64, out);
 }
 
-// Add the changed segments' contributions to candidates [c0, c0 + nc) and
-// copy their corrections to corr_out (nc x 3).
-int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const double *sign, int nch,
-                   double *corr_out)
+// Add the changed segments' contributions (and their error bounds) to
+// candidates [c0, c0 + nc) on the device (asynchronous; ov_rec_fetch reads
+// them back).
+int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const double *sign, int nch)
 {
     if (nc <= 0) return OV_OK;
     RecChange ch;
@@ -1534,10 +1602,17 @@ int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const 
     const int nq = c->geo.n_img + 1;
     const int threads = nc * nq;
     k_corr<<<(threads + 127) / 128, 128, 0, c->stream>>>(ra, c->rec_nodes, c0, nc, ch, c->rec_part);
-    k_corr_finish<<<(nc + 127) / 128, 128, 0, c->stream>>>(c->rec_part, nc, nq, c->rec_corr + 3 * (size_t)c0);
+    k_corr_finish<<<(nc + 127) / 128, 128, 0, c->stream>>>(c->rec_part, nc, nq, c->rec_corr + 4 * (size_t)c0);
     c->launches += 2;
     OV_CUDA(c, cudaGetLastError());
-    OV_CUDA(c, cudaMemcpyAsync(corr_out, c->rec_corr + 3 * (size_t)c0, (size_t)nc * 3 * sizeof(double),
+    return OV_OK;
+}
+
+// Corrections of candidates [c0, c0 + n) (4 doubles each) into out.
+int ov_rec_fetch(ov_ctx *c, int c0, int n, double *out)
+{
+    if (n <= 0) return OV_OK;
+    OV_CUDA(c, cudaMemcpyAsync(out, c->rec_corr + 4 * (size_t)c0, (size_t)n * 4 * sizeof(double),
                                cudaMemcpyDeviceToHost, c->stream));
     OV_CUDA(c, cudaStreamSynchronize(c->stream));
     return OV_OK;

@@ -220,8 +220,8 @@ class Context:
         return tu
 
     def set_tuning(self, warps_per_block: int = 4, query_groups: int = 0, blocks_per_sm: int = 0,
-                   largest_first: int = 1):
-        tu = abi.Tuning(warps_per_block, query_groups, blocks_per_sm, largest_first)
+                   largest_first: int = 1, high_occupancy: int = 0):
+        tu = abi.Tuning(warps_per_block, query_groups, blocks_per_sm, largest_first, high_occupancy)
         self._check(self.lib.ov_set_tuning(self._h, C.byref(tu)))
 
     def autotune(self, t: float = 0.0) -> tuple[dict, float]:
@@ -300,12 +300,13 @@ class Context:
         self._check(self.lib.ov_step(self._h, t, dt))
 
     STEP_PASSES = ("small_loops", "reconnect", "smooth", "periodic", "remesh", "update_tangle", "rk4_step",
-                   "total", "reconnect_pairs", "reconnect_direct_sums", "reconnect_decisions", "reconnect_push")
+                   "total", "reconnect_pairs", "reconnect_direct_sums", "reconnect_decisions", "reconnect_push",
+                   "reconnect_fetch", "reconnect_correct", "reconnect_fp64", "reconnect_exact")
 
     def step_times(self) -> dict:
         """Host wall ms of the last step(), per pass."""
-        ms = (C.c_double * 12)()
-        self._check(self.lib.ov_step_times(self._h, ms, 12))
+        ms = (C.c_double * 16)()
+        self._check(self.lib.ov_step_times(self._h, ms, 16))
         return dict(zip(self.STEP_PASSES, list(ms)))
 
     @property

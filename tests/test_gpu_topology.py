@@ -148,3 +148,35 @@ def test_reconnect_sums_within_their_bound(n_loops, D):
     t = port.tangle(ht)
     _, vs_ref = port.direct_velocities(t, nodes)
     assert rel_err(s64, vs_ref) < 1e-12
+
+
+@pytest.mark.parametrize("detrend", [False, True])
+def test_long_loop_smoothing_vs_oracle(detrend):
+    """Loops longer than one block's shared memory go through the Bluestein
+    FFT path; the result equals the restatement's direct DFT low-pass."""
+    n = 3000
+    k = np.arange(n)
+    rng = np.random.default_rng(5)
+    if detrend:
+        # a loop that winds once around the periodic box in x (gap > L/2 after unwrapping)
+        pos = np.stack([np.mod(k * 0.1 / n, 0.1), 0.05 + 0.003 * np.sin(2 * np.pi * 7 * k / n),
+                        0.05 + 0.002 * rng.standard_normal(n) * 0.1], 1)
+    else:
+        th = 2 * np.pi * k / n
+        pos = np.stack([0.05 + 0.03 * np.cos(th), 0.05 + 0.03 * np.sin(th),
+                        0.05 + 0.0005 * rng.standard_normal(n)], 1)
+    pos0 = pos.copy()   # the host tangle holds `pos` itself, which the download overwrites
+    ht = W.HostTangle(pos, (k + 1) % n, (k - 1) % n, np.zeros(3), np.full(3, 0.1), n_images=26)
+    p = W.config_params("rw", use_freq_filter=1, freq_to_cutoff=0.8)
+    port = Checker("port")
+    port.set_params(p)
+    t = port.tangle(ht)
+    port.smooth(t)
+    ctx = gpu.Context(0, params=p)
+    ctx.upload(ht)
+    ctx.smooth()
+    out = ctx.download(ht, abi.OV_F_POS)
+    ctx.close()
+    ref = t.copy("pos")
+    assert np.abs(out.pos - ref).max() < 1e-12
+    assert np.abs(ref - pos0).max() > 1e-6   # it smoothed
