@@ -178,9 +178,9 @@ int ov_set_member_params(ov_ctx *ctx, int i, const ov_params *p);
 /* Launch shape of the traversal: warps per block (2, 4 or 8), query groups
    per node (1-27; 0 = from the node count), persistent blocks per SM (0 =
    the occupancy limit), the order of the work queue (largest member first
-   or member order) and, for the mixed traversal, the register budget
-   (0: the default; 1: fewer registers for one more resident block).
-   Results do not depend on it. */
+   or member order), and for the mixed traversal the register budget (0:
+   the default; 1: fewer registers for one more resident block).  Results
+   do not depend on it. */
 typedef struct ov_tuning {
     int warps_per_block;
     int query_groups;

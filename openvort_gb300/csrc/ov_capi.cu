@@ -141,7 +141,7 @@ int ov_ctx_destroy(ov_ctx *c)
     if (c->d_mrange) cudaFree(c->d_mrange);
     void *scratch[] = {c->d_pairs, c->d_npairs, c->d_loop_off, c->d_loop_nodes, c->d_loop_buf, c->d_loop_cut,
                        c->rec_nodes, c->rec_pair, c->rec_out, c->rec_corr, c->rec_part, c->rec_split,
-                       c->fft_buf, c->fft_tw, c->long_buf};
+                       c->fft_buf, c->fft_tw, c->long_buf, c->rec_pf, c->rec_pf_idx};
     for (void *p : scratch)
         if (p) cudaFree(p);
     if (c->dsum) cudaFree(c->dsum);
@@ -149,6 +149,8 @@ int ov_ctx_destroy(ov_ctx *c)
     if (c->flush_buf) cudaFree(c->flush_buf);
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->h_corr) cudaFreeHost(c->h_corr);
+    if (c->h_pf) cudaFreeHost(c->h_pf);
+    if (c->rec_ev) cudaEventDestroy(c->rec_ev);
     if (c->rk4_exec) cudaGraphExecDestroy(c->rk4_exec);
     for (int i = 0; i < 4; ++i)
         if (c->ph[i]) cudaEventDestroy(c->ph[i]);
@@ -322,6 +324,8 @@ static int ensure_stage(ov_ctx *c, size_t bytes)
     if (c->h_stage_bytes >= bytes) return OV_OK;
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->h_corr) cudaFreeHost(c->h_corr);
+    if (c->h_pf) cudaFreeHost(c->h_pf);
+    if (c->rec_ev) cudaEventDestroy(c->rec_ev);
     c->h_stage = nullptr;
     OV_CUDA(c, cudaMallocHost(&c->h_stage, bytes));
     c->h_stage_bytes = bytes;

@@ -1266,12 +1266,19 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     }
     double *corr = c->h_corr;
     std::fill(corr, corr + 4 * (size_t)C, 0.0);
-    std::vector<char> exact(C, 0);
-    // corrections on the host are read back lazily, a window at a time:
-    // corr_gen[i] < gen means candidate i's copy predates the last rewiring
-    std::vector<int> corr_gen(C, 0);
+    // FP64 sums on the current topology (refinements), valid while
+    // ex_gen[i] == gen
+    std::vector<double> ex(5 * (size_t)C);
+    std::vector<int> ex_gen(C, -1);
+    int pushed_gen = 0;   // generation of the device's connections
+    // corrections on the host are read back lazily: corr_gen[i] < gen means
+    // candidate i's copy predates the last rewiring.  After each rewiring
+    // the corrections of the next pairs' candidates are read back ahead
+    // (pf_gen[i] == gen: waiting in the pinned prefetch buffer at pf_pos[i]).
+    std::vector<int> corr_gen(C, 0), pf_gen(C, -1), pf_pos(C, 0);
     int gen = 0;
-    const int kFetch = 2048;
+    bool pf_waited = true;
+    const int kFetch = 256, kAhead = 48;
     int64_t evaluated = 0;
     c->stats.reconnect_candidates = C;
     c->stats.reconnect_fp64_pairs = 0;
@@ -1308,15 +1315,33 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         double vs[3];
         if (!hlia(h, k, tg, nm, t, vs)) return false;
         int ci = cand_index(k);
-        if (corr_gen[ci] < gen) {
-            const auto tf = clk();
-            const int n = std::min(ce, ci + kFetch) - ci;
-            if (ov_rec_fetch(c, ci, n, corr + 4 * (size_t)ci)) return false;
-            std::fill(corr_gen.begin() + ci, corr_gen.begin() + ci + n, gen);
-            c->step_ms[12] += ms_since(tf);
+        static const double zero4[4] = {0, 0, 0, 0};
+        const double *rc, *cc;
+        if (ex_gen[ci] == gen) {
+            rc = &ex[5 * (size_t)ci];   // FP64 on the current topology: no corrections
+            cc = zero4;
+        } else {
+            if (corr_gen[ci] < gen) {
+                const auto tf = clk();
+                if (pf_gen[ci] == gen) {
+                    if (!pf_waited) {
+                        if (ov_rec_wait(c)) return false;
+                        pf_waited = true;
+                    }
+                    for (int a = 0; a < 4; ++a) corr[4 * (size_t)ci + a] = c->h_pf[4 * (size_t)pf_pos[ci] + a];
+                    corr_gen[ci] = gen;
+                } else {
+                    const int n = std::min(ce, ci + kFetch) - ci;
+                    if (ov_rec_fetch(c, ci, n, corr + 4 * (size_t)ci)) return false;
+                    std::fill(corr_gen.begin() + ci, corr_gen.begin() + ci + n, gen);
+                    pf_waited = true;   // the stream is idle now
+                }
+                c->step_ms[12] += ms_since(tf);
+            }
+            rc = &rec[5 * (size_t)ci];
+            cc = &corr[4 * (size_t)ci];
         }
         ++evaluated;
-        const double *rc = &rec[5 * (size_t)ci], *cc = &corr[4 * (size_t)ci];
         for (int a = 0; a < 3; ++a) vs[a] = vs[a] + (rc[a] + cc[a]);
         hfriction(h, k, tg, vs, t, vel);
         const double tl = hlen(tg);
@@ -1364,18 +1389,26 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
             double proj = hdot(dx, dv);
             if (fabs(proj) <= hlen(dx) * (bk + bl) + 1e-9 * hlen(dx) * hlen(dv)) {
                 // the mixed-precision sums cannot decide: FP64 sums of both
+                // on the current topology (the device's connections are
+                // brought up to date first)
                 int ck = cand_index(k), cl = cand_index(l);
-                if (!exact[ck] || !exact[cl]) {
+                if (ex_gen[ck] != gen || ex_gen[cl] != gen) {
                     ++c->stats.reconnect_fp64_pairs;
-                    double ex[10];
+                    double exv[10];
                     const auto te = clk();
-                    if ((r = ov_rec_exact(c, k, l, ex))) return r;
+                    if (pushed_gen != gen) {
+                        OV_CUDA(c, cudaMemcpyAsync(c->fwd, c->h_fwd.data(), (size_t)c->n_live * sizeof(int),
+                                                   cudaMemcpyHostToDevice, c->stream));
+                        pushed_gen = gen;
+                    }
+                    if ((r = ov_rec_exact(c, k, l, exv))) return r;
+                    pf_waited = true;
                     c->step_ms[14] += ms_since(te);
                     for (int a = 0; a < 5; ++a) {
-                        rec[5 * (size_t)ck + a] = ex[a];
-                        rec[5 * (size_t)cl + a] = ex[5 + a];
+                        ex[5 * (size_t)ck + a] = exv[a];
+                        ex[5 * (size_t)cl + a] = exv[5 + a];
                     }
-                    exact[ck] = exact[cl] = 1;
+                    ex_gen[ck] = ex_gen[cl] = gen;
                     velocity(k, tk, nk, vk, &bk);
                     velocity(l, tl, nl_, vl, &bl);
                     hsub(dv, vk, vl);
@@ -1423,8 +1456,26 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
             const int cfrom = cand_index(k) + 1;
             const auto tc = clk();
             if (ce > cfrom && (r = ov_rec_correct(c, cfrom, ce - cfrom, cm, cfw, csg, 4))) return r;
-            c->step_ms[13] += ms_since(tc);
             ++gen;
+            {
+                // read back ahead the corrections of the next pairs' candidates
+                std::vector<int> ahead;
+                ahead.reserve(2 * kAhead);
+                for (size_t qq = e; qq < pairs.size() && qq < e + kAhead; ++qq) {
+                    for (int node : {pairs[qq].first, pairs[qq].second}) {
+                        int cj = cand_index(node);
+                        if (cj < cfrom || cj >= ce || pf_gen[cj] == gen) continue;
+                        pf_gen[cj] = gen;
+                        pf_pos[cj] = (int)ahead.size();
+                        ahead.push_back(cj);
+                    }
+                }
+                if (!ahead.empty()) {
+                    if ((r = ov_rec_prefetch(c, ahead.data(), (int)ahead.size()))) return r;
+                    pf_waited = false;
+                }
+            }
+            c->step_ms[13] += ms_since(tc);
             recalc[k]++; recalc[h.fwd(k)]++; recalc[h.rev(k)]++; recalc[kn]++; recalc[kp]++;
             recalc[l]++; recalc[h.fwd(l)]++; recalc[h.rev(l)]++; recalc[ln]++; recalc[lp]++;
             if (log_k && log_l && nrec < log_cap) { log_k[nrec] = k; log_l[nrec] = l; }

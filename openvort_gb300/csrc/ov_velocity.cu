@@ -232,6 +232,41 @@ __device__ __forceinline__ bool segment_law64(const double R[3], const double Rp
     return true;
 }
 
+// FP64 hardware approximations (PTX rcp.approx / rsqrt.approx, about 20
+// correct bits) refined by two Newton-Raphson steps each (20 -> 40 -> 80
+// bits): full double precision without the correctly rounded sequences.
+__device__ __forceinline__ double rcp_seed(double x)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return y;
+}
+__device__ __forceinline__ double rsqrt_seed(double x)
+{
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return y;
+}
+
+// 1/x (x normal and positive)
+__device__ __forceinline__ double recip_1_2(double x)
+{
+    double y = rcp_seed(x);
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
+// 1/sqrt(x) (x normal and positive): y <- y (3/2 - x/2 y^2)
+__device__ __forceinline__ double rsqrt_nr(double x)
+{
+    double y = rsqrt_seed(x);
+    const double h = 0.5 * x;
+    y = y * fma(-h * y, y, 1.5);
+    return y * fma(-h * y, y, 1.5);
+}
+
 // One Barnes-Hut query point for the 32 lanes of a warp.  `part` = lane
 // takes part; returns the lane's velocity in v.
 __device__ __forceinline__ void bh_query64(const VelArgs &a, const double q[3], bool part, int root, int ncell,
@@ -1229,6 +1264,36 @@ __device__ __forceinline__ bool rec_term64(const RecArgs &r, int m, int f, int j
     return segment_law64(R, Rp1, len3_ref(R[0], R[1], R[2]), r.f4pi, w);
 }
 
+// FP64 term without the reference's correctly rounded square roots and
+// divisions (for whole-sum FP64 refinements): the filters are decided the
+// reference's way when their test values lie near the thresholds.
+__device__ __forceinline__ bool rec_term64_fast(const RecArgs &r, int m, int f, int j, const double p[3],
+                                                double w[3])
+{
+    double q[3];
+    if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+    else image_point(r.geo, j, p, q);
+    double s1[3] = {r.x[m], r.y[m], r.z[m]};
+    double s2[3] = {r.x[f], r.y[f], r.z[f]};
+    pwrap_dev(r.geo, s1, s2);
+    const double R[3] = {s1[0] - q[0], s1[1] - q[1], s1[2] - q[2]};
+    const double P[3] = {s2[0] - q[0], s2[1] - q[1], s2[2] - q[2]};
+    const double lR2 = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+    const double lp2 = P[0] * P[0] + P[1] * P[1] + P[2] * P[2];
+    if (lR2 < 1.001e-16 || lp2 < 1.001e-16) return rec_term64(r, m, f, j, p, w);   // |R| < 1e-8 filter
+    if (lR2 > 1e30 || lp2 > 1e30) return rec_term64(r, m, f, j, p, w);
+    const double ra = rsqrt_nr(lR2), rb = rsqrt_nr(lp2), ab = ra * rb;
+    const double dotv = R[0] * P[0] + R[1] * P[1] + R[2] * P[2];
+    const double nd = dotv * ab;
+    if (fabs(nd - 1e-8) < 1e-6) return rec_term64(r, m, f, j, p, w);   // ndot filter near its threshold
+    if (nd < 1e-8) return false;
+    const double sc = r.f4pi * (ra + rb) * ab * recip_1_2(1.0 + nd);
+    w[0] = (R[1] * P[2] - R[2] * P[1]) * sc;
+    w[1] = (R[2] * P[0] - R[0] * P[2]) * sc;
+    w[2] = (R[0] * P[1] - R[1] * P[0]) * sc;
+    return true;
+}
+
 constexpr int kRecThreads = 256;
 constexpr int kRecVals = 7;   // 3 sums, FP32 magnitude, 3 spare (|FP64 terms|)
 
@@ -1308,7 +1373,7 @@ __global__ void __launch_bounds__(kRecThreads) k_rec_sums(RecArgs r, const int *
             }
             if (use64) {
                 double w[3];
-                if (rec_term64(r, m, f, j, p, w)) {
+                if (force64 ? rec_term64_fast(r, m, f, j, p, w) : rec_term64(r, m, f, j, p, w)) {
                     d0 += w[0]; d1 += w[1]; d2 += w[2];
                     dabs += fabs(w[0]) + fabs(w[1]) + fabs(w[2]);
                 }
@@ -1605,6 +1670,50 @@ int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const 
     k_corr_finish<<<(nc + 127) / 128, 128, 0, c->stream>>>(c->rec_part, nc, nq, c->rec_corr + 4 * (size_t)c0);
     c->launches += 2;
     OV_CUDA(c, cudaGetLastError());
+    return OV_OK;
+}
+
+namespace {
+__global__ void k_corr_gather(const double *__restrict__ corr, const int *__restrict__ idx, int n,
+                              double *__restrict__ out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 4 * n) return;
+    out[i] = corr[4 * (size_t)idx[i >> 2] + (i & 3)];
+}
+}  // namespace
+
+// Start reading back the corrections of candidates idx[0..n) (after every
+// correction launched so far) into the pinned buffer c->h_pf; ov_rec_wait
+// waits for it.
+int ov_rec_prefetch(ov_ctx *c, const int *idx, int n)
+{
+    if (n <= 0) return OV_OK;
+    if (c->rec_pf_cap < n) {
+        if (c->rec_pf) cudaFree(c->rec_pf);
+        if (c->rec_pf_idx) cudaFree(c->rec_pf_idx);
+        if (c->h_pf) cudaFreeHost(c->h_pf);
+        c->rec_pf = nullptr; c->rec_pf_idx = nullptr; c->h_pf = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->rec_pf, (size_t)n * 4 * sizeof(double)));
+        OV_CUDA(c, cudaMalloc(&c->rec_pf_idx, (size_t)n * sizeof(int)));
+        OV_CUDA(c, cudaMallocHost(&c->h_pf, (size_t)n * (4 * sizeof(double) + sizeof(int))));
+        c->rec_pf_cap = n;
+    }
+    if (!c->rec_ev) OV_CUDA(c, cudaEventCreateWithFlags(&c->rec_ev, cudaEventDisableTiming));
+    int *h_idx = (int *)(c->h_pf + 4 * (size_t)c->rec_pf_cap);
+    memcpy(h_idx, idx, (size_t)n * sizeof(int));
+    OV_CUDA(c, cudaMemcpyAsync(c->rec_pf_idx, h_idx, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    k_corr_gather<<<(4 * n + 127) / 128, 128, 0, c->stream>>>(c->rec_corr, c->rec_pf_idx, n, c->rec_pf);
+    c->launches++;
+    OV_CUDA(c, cudaMemcpyAsync(c->h_pf, c->rec_pf, (size_t)n * 4 * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+    OV_CUDA(c, cudaEventRecord(c->rec_ev, c->stream));
+    return OV_OK;
+}
+
+int ov_rec_wait(ov_ctx *c)
+{
+    OV_CUDA(c, cudaEventSynchronize(c->rec_ev));
     return OV_OK;
 }
 

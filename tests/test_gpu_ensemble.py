@@ -85,7 +85,7 @@ def test_queue_order_and_block_shape_do_not_change_results():
     ms = members(sizes=(6, 2, 9))
     outs = []
     for tune in (TUNE, dict(TUNE, largest_first=0, warps_per_block=2),
-                 dict(TUNE, warps_per_block=8, blocks_per_sm=1)):
+                 dict(TUNE, warps_per_block=8, blocks_per_sm=1), dict(TUNE, high_occupancy=1)):
         ens = ensemble(ms, abi.OV_PREC_FP64, tune=tune)
         ens.update_tangle(0.0)
         outs.append([ens.download_member(i, clone(ms[i][0])).vels for i in range(len(ms))])
