@@ -143,11 +143,14 @@ def barrier(dist):
         dist.barrier()
 
 
-def cpu_eval_time(kind: str, threads: int, reps: int, tangle=None):
+def cpu_eval_time(kind: str, threads: int, reps: int, tangle=None, params=None):
     """Seconds per full update_tangle of the workload in the CPU checker."""
     from oracle.pyoracle import Checker
     c = Checker(kind, fast=(kind == "port"))
-    c.set_params(make_params(threads))
+    if params is None:
+        params = make_params(threads)
+    params.num_threads = threads
+    c.set_params(params)
     ht = tangle or make_tangle()
     times = []
     for _ in range(reps):
@@ -271,7 +274,14 @@ def run_ensemble(args, device=0):
     full_ms = (time.perf_counter() - t0) * 1e3 / max(1, K)
     n_end = sum(ctx.member_info(i)[0] - ctx.member_info(i)[2] for i in range(len(hosts)))
     ctx.close()
+    cpu = None
+    if args.cpu_sections:
+        threads = os.cpu_count() or 1
+        cpu_s = sum(min(cpu_eval_time(cpu_kind(), threads, 1, h, p)) for h, p in zip(hosts, params))
+        cpu = {"value": n / cpu_s, "unit": UNIT, "cores": threads, "kind": cpu_kind(),
+               "sample": "one full update_tangle of every member, members one after another"}
     return {
+        "cpu_baseline": cpu,
         "config": E, "members": len(hosts), "nodes": n, "nodes_per_member_min_max": [min(h.n for h in hosts),
                                                                                   max(h.n for h in hosts)],
         "tuning": tune, "tuned_eval_ms": tune_ms,
@@ -343,7 +353,14 @@ def run_precision_form(args, device=0):
         v32 = ctx.download(ht, abi.OV_F_VELS).vels.copy()
         st32 = ctx.stats()
         ctx.close()
+        cpu_s = None
+        if args.cpu_sections:
+            threads = os.cpu_count() or 1
+            cpu_s = min(cpu_eval_time(cpu_kind(), threads, 1, ht, W.config_params("rw", bh_resolution=theta)))
         out["by_theta"][str(theta)] = {
+            "cpu_baseline": None if cpu_s is None else {
+                "value": n / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": cpu_kind(),
+                "sample": "one full update_tangle of the 262,144-node tangle"},
             "fp64": {"value": n / (fp64_ms * 1e-3), "unit": UNIT, "ms_per_eval": fp64_ms,
                      "rel_l2_vs_direct_subsample": rel_l2(v64[sub], direct)},
             "mixed": {"value": n / (mixed_ms * 1e-3), "unit": UNIT, "ms_per_eval": mixed_ms,
@@ -405,8 +422,15 @@ def run_large(args, device=0):
     ctx.synchronize()
     full_ms = (time.perf_counter() - t0) * 1e3 / max(1, K)
     ctx.close()
+    cpu = None
+    if args.cpu_sections:
+        threads = os.cpu_count() or 1
+        cpu_s = min(cpu_eval_time(cpu_kind(), threads, 1, ht, W.config_params("large", bh_resolution=E["theta"])))
+        cpu = {"value": n / cpu_s, "unit": UNIT, "cores": threads, "kind": cpu_kind(),
+               "sample": "one full update_tangle of the 1,048,576-node tangle (a full step is reconnect-dominated "
+                         "and not run on the CPU)"}
     return {
-        "config": E, "nodes": n, "tuning": tune,
+        "config": E, "nodes": n, "tuning": tune, "cpu_baseline": cpu,
         "fp64": {"value": n / (fp64_ms * 1e-3), "unit": UNIT, "ms_per_eval": fp64_ms},
         "mixed": {"value": n / (mixed_ms * 1e-3), "unit": UNIT, "ms_per_eval": mixed_ms,
                   "rel_l2_vs_fp64_tree": rel_l2(v32, v64)},
@@ -473,10 +497,7 @@ def run_ours(args):
     h2d = n * (3 * 8 + 4 * 4)
     d2h = n * 3 * 8
 
-    # ---- accuracy of the FP64 tree against FP64 direct sums on a 4,096-node subsample
-    sub = direct_subsample(n, 4096, 1)
-    direct_v, _ = ctx.direct_velocities(sub)
-    fp64_vs_direct = rel_l2(np.array(ht.vels)[sub], direct_v)
+    fp64_vels = np.array(ht.vels)   # the FP64 tree's velocities (accuracy check at the end)
 
     # ---- mixed precision on the same workload (reported beside FP64)
     mixed = None
@@ -495,9 +516,9 @@ def run_ours(args):
         ctx.download(ht, abi.OV_F_VELS)
         mst = ctx.stats()
         err = float(np.linalg.norm(ht.vels - ref_v) / np.linalg.norm(ref_v))
+        mixed_vels = np.array(ht.vels)
         mixed = {"value": world * n / (statistics.mean(mt) * 1e-3), "unit": UNIT,
-                 "rel_l2_vs_fp64_tree": err, "rel_l2_vs_direct_subsample": rel_l2(ht.vels[sub], direct_v),
-                 "ms_per_step": statistics.mean(mt),
+                 "rel_l2_vs_fp64_tree": err, "ms_per_step": statistics.mean(mt),
                  "speedup_vs_fp64": mean_ms / statistics.mean(mt),
                  "same_decisions_as_fp64": bool(mst["accepts"] == acc and mst["visits"] == vis),
                  "fp64_guard_band_decisions": mst["fp64_fallbacks"], "fp64_near_field": mst["near_field_fp64"],
@@ -525,6 +546,16 @@ def run_ours(args):
         rk4[name] = {"steps_per_s": 1e3 / statistics.mean(ts), "ms_per_step": statistics.mean(ts),
                      "node_evals_per_s": 4 * n / (statistics.mean(ts) * 1e-3)}
     ctx.set_precision(abi.OV_PREC_FP64)
+    # ---- accuracy against FP64 direct sums on a 4,096-node subsample (after the
+    # timed sections: the direct sums are O(N) per node)
+    ctx.upload(ht)
+    ctx.update_tangle(0.0)
+    sub = direct_subsample(n, 4096, 1)
+    direct_v, _ = ctx.direct_velocities(sub)
+    fp64_vs_direct = rel_l2(fp64_vels[sub], direct_v)
+    if isinstance(mixed, dict) and "value" in mixed:
+        mixed["rel_l2_vs_direct_subsample"] = rel_l2(mixed_vels[sub], direct_v)
+
     ensemble = precision_form = large = None
     if world == 1 and args.ensemble_steps >= 0:
         try:
@@ -597,6 +628,8 @@ def main():
     ap.add_argument("--large-steps", type=int, default=5,
                     help="full time steps of the 1,048,576-node tangle (-1: skip that section)")
     ap.add_argument("--precision-form", type=int, default=1, help="262,144-node theta 0.3/0.5 section (0: skip)")
+    ap.add_argument("--cpu-sections", type=int, default=1,
+                    help="time the CPU baseline of the ensemble, precision-form and large sections too (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -42,7 +42,6 @@
 #define M_E 2.7182818284590452354
 #endif
 
-int ov_direct_raw(ov_ctx *c, const int *nodes, int n, double *sums_out);
 
 namespace {
 

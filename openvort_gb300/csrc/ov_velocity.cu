@@ -5,7 +5,8 @@
 //                 v_s + Barnes-Hut over the primary and every image query
 //                 point + mutual friction, one warp per 32 Morton-ordered
 //                 targets sharing one cursor through the pre-order cells
-//  k_direct       the tree==NULL branch (tangle.c:652-687), one block per node
+//  k_rec_sums     direct sums, the tree==NULL branch (tangle.c:652-687), in
+//                 (node, segment chunk) blocks; k_direct_finish adds LIA etc.
 //  k_euler / k_rk4_combine / k_wrap   RK4 stages and enforce_periodic_boundaries
 //
 // The FP64 traversal keeps the reference's decisions bit-for-bit given the
@@ -537,65 +538,16 @@ __global__ void k_vel_finish(VelArgs a, const double *__restrict__ part_in)
 }
 
 // ------------------------------------------------------------ direct sum
-// Velocity of node `nodes[b]` from every segment of the primary tangle
-// (skipping the two segments at the node) and of every image (skipping
-// nothing), as update_velocity with tree == NULL.
-__global__ void k_direct(VelArgs a, const int *__restrict__ nodes, int n, int cap, double *__restrict__ out)
-{
-    __shared__ double red[3][256];
-    int b = blockIdx.x;
-    if (b >= n) return;
-    int k = nodes[b];
-    double p[3] = {a.x[k], a.y[k], a.z[k]};
-    double acc[3] = {0, 0, 0};
-    // segments of the node's own member only
-    int lo = 0, hi = cap;
-    if (a.tid && a.mrange) {
-        int mm = a.tid[k];
-        if (mm >= 0 && mm < a.nt) { lo = a.mrange[mm].x; hi = min(a.mrange[mm].y, cap); }
-        else { bad_index(a, 9, k); hi = 0; }
-    }
-    for (int j = -1; j < a.geo.n_img; ++j) {
-        double q[3];
-        if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
-        else image_point(a.geo, j, p, q);
-        for (int m = lo + threadIdx.x; m < hi; m += blockDim.x) {
-            int f = a.fwd[m];
-            if (f == -1) continue;
-            if (j < 0 && (m == k || f == k)) continue;
-            double s1[3] = {a.x[m], a.y[m], a.z[m]};
-            double s2[3] = {a.x[f], a.y[f], a.z[f]};
-            pwrap_dev(a.geo, s1, s2);
-            double R[3] = {rn_sub(s1[0], q[0]), rn_sub(s1[1], q[1]), rn_sub(s1[2], q[2])};
-            double Rp1[3] = {rn_sub(s2[0], q[0]), rn_sub(s2[1], q[1]), rn_sub(s2[2], q[2])};
-            double lR = len3_ref(R[0], R[1], R[2]);
-            double w[3];
-            if (segment_law64(R, Rp1, lR, a.f4pi, w)) {
-                acc[0] += w[0]; acc[1] += w[1]; acc[2] += w[2];
-            }
-        }
-    }
-    for (int ax = 0; ax < 3; ++ax) red[ax][threadIdx.x] = acc[ax];
-    __syncthreads();
-    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < off)
-            for (int ax = 0; ax < 3; ++ax) red[ax][threadIdx.x] += red[ax][threadIdx.x + off];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        for (int ax = 0; ax < 3; ++ax) out[3 * (size_t)b + ax] = red[ax][0];
-    }
-}
-
 // Finish the direct-sum nodes (LIA, v_s, friction) into vels/vs scratch.
 __global__ void k_direct_finish(VelArgs a, const int *__restrict__ nodes, int n, const double *__restrict__ sums,
-                                double *__restrict__ vout, double *__restrict__ sout)
+                                int stride, double *__restrict__ vout, double *__restrict__ sout)
 {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     int k = nodes[b];
     double p[3] = {a.x[k], a.y[k], a.z[k]};
-    double prim[3] = {sums[3 * (size_t)b], sums[3 * (size_t)b + 1], sums[3 * (size_t)b + 2]};
+    const double *sb = sums + (size_t)stride * b;
+    double prim[3] = {sb[0], sb[1], sb[2]};
     double zero[3] = {0, 0, 0}, vs[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
     int err = 0;
     if (a.status[k] != OV_EMPTY) finish_node(a, k, p, prim, zero, &err, vs, vel);
@@ -1082,6 +1034,8 @@ int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precisio
     return OV_OK;
 }
 
+int ov_direct_sum_chunked(ov_ctx *c, const int *nodes, int n, double *d_out_vel, double *d_out_vs, double t);
+
 int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out, double *vs_out)
 {
     if (n <= 0) return OV_OK;
@@ -1093,13 +1047,9 @@ int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out
         OV_CUDA(c, cudaMalloc(&c->dnodes, (size_t)n * sizeof(int)));
         c->dsum_cap = n;
     }
-    OV_CUDA(c, cudaMemcpyAsync(c->dnodes, nodes, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    VelArgs a = make_args(c, c->node, t, nullptr);
-    k_direct<<<n, 256, 0, c->stream>>>(a, c->dnodes, n, c->cap, c->dsum);
     double *vo = c->dsum + 3 * (size_t)n, *so = c->dsum + 6 * (size_t)n;
-    k_direct_finish<<<(n + 127) / 128, 128, 0, c->stream>>>(a, c->dnodes, n, c->dsum, vo, so);
-    c->launches += 2;
-    OV_CUDA(c, cudaGetLastError());
+    int r = ov_direct_sum_chunked(c, nodes, n, vo, so, t);
+    if (r) return r;
     if (vels_out)
         OV_CUDA(c, cudaMemcpyAsync(vels_out, vo, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if (vs_out)
@@ -1166,29 +1116,6 @@ extern "C" int ov_tree_velocity_at(ov_ctx *c, const double *points, int n, doubl
     c->launches++;
     OV_CUDA(c, cudaGetLastError());
     OV_CUDA(c, cudaMemcpyAsync(out, dout, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    OV_CUDA(c, cudaStreamSynchronize(c->stream));
-    return OV_OK;
-}
-
-// Raw direct sums (no LIA / friction) of the listed nodes on the current
-// device state: the nonlocal velocities reconnect needs.
-int ov_direct_raw(ov_ctx *c, const int *nodes, int n, double *sums_out)
-{
-    if (n <= 0) return OV_OK;
-    if (c->dsum_cap < n) {
-        if (c->dsum) cudaFree(c->dsum);
-        if (c->dnodes) cudaFree(c->dnodes);
-        c->dsum = nullptr; c->dnodes = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->dsum, (size_t)n * 9 * sizeof(double)));
-        OV_CUDA(c, cudaMalloc(&c->dnodes, (size_t)n * sizeof(int)));
-        c->dsum_cap = n;
-    }
-    OV_CUDA(c, cudaMemcpyAsync(c->dnodes, nodes, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    VelArgs a = make_args(c, c->node, 0.0, nullptr);
-    k_direct<<<n, 256, 0, c->stream>>>(a, c->dnodes, n, c->n_live, c->dsum);
-    c->launches++;
-    OV_CUDA(c, cudaGetLastError());
-    OV_CUDA(c, cudaMemcpyAsync(sums_out, c->dsum, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     OV_CUDA(c, cudaStreamSynchronize(c->stream));
     return OV_OK;
 }
@@ -1651,6 +1578,29 @@ extern "C" int ov_direct_sums_bounded(ov_ctx *c, const int *nodes, int n, int pr
                                                         1.0 / c->grid_h, c->rec_split);
     c->launches++;
     return rec_launch_sums(c, c->rec_nodes, n, precision == OV_PREC_FP64, out);
+}
+
+// ov_direct_velocities: FP64 direct sums in (node, segment chunk) blocks,
+// then LIA, v_s and friction (k_direct_finish) into device arrays.
+int ov_direct_sum_chunked(ov_ctx *c, const int *nodes, int n, double *d_out_vel, double *d_out_vs, double t)
+{
+    int maxcap = 0;
+    for (const Member &m : c->mem) maxcap = std::max(maxcap, c->mem.size() == 1 ? c->cap : m.cap);
+    const int span = 8192, max_chunks = std::max(1, (maxcap + span - 1) / span);
+    int r = rec_reserve(c, n, max_chunks);
+    if (r) return r;
+    OV_CUDA(c, cudaMemcpyAsync(c->rec_nodes, nodes, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    k_split<<<(c->cap + 255) / 256, 256, 0, c->stream>>>(c->node.x, c->node.y, c->node.z, c->cap, c->grid_h,
+                                                        1.0 / c->grid_h, c->rec_split);
+    RecArgs ra = make_rec_args(c);
+    k_rec_sums<<<dim3(n, max_chunks), kRecThreads, 0, c->stream>>>(ra, c->rec_nodes, n, span, max_chunks, 1,
+                                                                   c->rec_part);
+    k_rec_finish<<<(n + 127) / 128, 128, 0, c->stream>>>(c->rec_part, n, max_chunks, c->rec_out);
+    VelArgs a = make_args(c, c->node, t, nullptr);
+    k_direct_finish<<<(n + 127) / 128, 128, 0, c->stream>>>(a, c->rec_nodes, n, c->rec_out, 5, d_out_vel, d_out_vs);
+    c->launches += 4;
+    OV_CUDA(c, cudaGetLastError());
+    return OV_OK;
 }
 
 // Add the changed segments' contributions (and their error bounds) to
