@@ -118,6 +118,8 @@ typedef struct ov_stats {
     int64_t reconnect_fp64_pairs;   /* pairs the mixed-precision bound left undecided (FP64 sums) */
     int64_t reconnect_exact_pairs;  /* pairs recomputed in the reference's summation order */
     int64_t reconnect_evaluated;    /* candidate velocities the decisions used */
+    int64_t wall_clipped;           /* last wall pass: nodes connected to a wall */
+    int64_t wall_removed;           /* last wall pass: nodes removed behind a wall */
 } ov_stats;
 
 typedef struct ov_ctx ov_ctx;
@@ -280,14 +282,18 @@ int ov_eliminate_small_loops(ov_ctx *ctx);
    log_l are non-NULL the (k,l) of each reconnection is written, in order,
    up to log_cap entries. */
 int ov_reconnect(ov_ctx *ctx, double t, int *nrecs, int *log_k, int *log_l, int log_cap);
+/* enforce_wall_boundaries (tangle.c:966): connect nodes within rec_dist of a
+   mirror wall to it (connect_to_wall, tangle.c:877) and remove nodes behind
+   one.  Nothing to do when every wall is periodic or open. */
+int ov_enforce_wall_boundaries(ov_ctx *ctx, double t);
 /* remesh (tangle.c:1018). */
 int ov_remesh(ov_ctx *ctx, double min_dist, double max_dist, double t);
 /* smooth (vortex_smooth.c:459): per-loop low-pass filter when use_freq_filter. */
 int ov_smooth(ov_ctx *ctx);
 /* One iteration of the reference's main loop body (main.c:125-141), without
-   injection, frame output and wall clipping: small loops, reconnect, small
-   loops, smooth, periodic wrap, remesh, small loops, update_tangle, rk4_step,
-   periodic wrap. */
+   injection and frame output: wall boundaries, small loops, reconnect, small
+   loops, smooth, periodic wrap, remesh (with wall boundaries after
+   insertions), small loops, update_tangle, rk4_step, periodic wrap. */
 int ov_step(ov_ctx *ctx, double t, double dt);
 /* Host wall-clock milliseconds of the last ov_step, per pass: [0] small
    loops (three calls), [1] reconnect, [2] smooth, [3] periodic wrap (two

@@ -80,7 +80,7 @@ class Stats(C.Structure):
         "node_evals", "cells", "max_depth", "visits", "accepts", "warp_steps", "fp64_fallbacks",
         "near_field_fp64", "out_of_root", "reconnections", "remesh_added", "remesh_removed",
         "small_loops_removed", "error_word", "reconnect_candidates", "reconnect_fp64_pairs",
-        "reconnect_exact_pairs", "reconnect_evaluated")]
+        "reconnect_exact_pairs", "reconnect_evaluated", "wall_clipped", "wall_removed")]
 
 
 class Tuning(C.Structure):
@@ -103,6 +103,87 @@ def image_shifts(n_images: int) -> list[tuple[int, int, int]]:
     out = [s for s in itertools.product((-1, 0, 1), repeat=3) if 0 < sum(map(abs, s)) <= maxnz]
     assert len(out) == n_images
     return out
+
+
+# Faces (boundaries.h): LEFT, RIGHT, BACK, FRONT, DOWN, UP.
+_L, _R, _B, _F, _D, _U = 0, 1, 2, 3, 4, 5
+_P, _M, _O = OV_WALL_PERIODIC, OV_WALL_MIRROR, OV_WALL_OPEN
+
+
+def image_set(name: str):
+    """(images, walls) of one of the reference's named boundary configurations
+    (src/boundary_images.c): images is a list of (shift, reflect faces), in
+    the reference's table order, walls the six wall types of the box.
+
+    The wall tables are data the drop-in must reproduce as the reference
+    defines them, including two entries that look unintended: in
+    wall_1_18 (boundary_images.c:193) the image (1, -1, 0) carries one
+    reflection through LEFT (its count is written `01` with no face given),
+    and wall_parallel_planes (:121-131) lists (-1, 1, -1) and (-1, 1, 1)
+    twice while (1, -1, -1) and (1, -1, 1) are missing.
+    """
+    def lex(maxnz, reflect_down=False):
+        out = []
+        for sh in image_shifts({1: 6, 2: 18, 3: 26}[maxnz]):
+            out.append((sh, (_D,) if reflect_down and sh[2] == -1 else ()))
+        return out
+    if name in ("periodic_6", "periodic_18", "periodic_26"):
+        n = int(name.split("_")[1])
+        return [(sh, ()) for sh in image_shifts(n)], (_P,) * 6
+    if name == "open":
+        return [], (_O,) * 6
+    if name == "wall_1_open":
+        return [((0, 0, -1), (_D,))], (_O, _O, _O, _O, _M, _O)
+    walls_1 = (_P, _P, _P, _P, _M, _P)
+    if name == "wall_1_6":
+        return [(sh, r) for sh, r in lex(1, True) if sh != (0, 0, 1)], walls_1
+    if name == "wall_1_18":
+        out = lex(2, True)
+        out = [(sh, (_L,) if sh == (1, -1, 0) else r) for sh, r in out]
+        return out, walls_1
+    if name == "wall_1_26":
+        return lex(3, True), walls_1
+    if name == "wall_2_4":
+        return [((-1, 0, 0), ()), ((1, 0, 0), ()), ((0, -1, 0), ()), ((0, 1, 0), ()),
+                ((0, 0, -1), (_D,)), ((0, 0, 1), (_U,))], (_P, _P, _P, _P, _M, _M)
+    if name == "wall_2_2":
+        return [((-1, 0, 0), ()), ((1, 0, 0), ()), ((0, -1, 0), (_B,)), ((0, 1, 0), (_F,)),
+                ((0, 0, -1), (_D,)), ((0, 0, 1), (_U,))], (_P, _P, _M, _M, _M, _M)
+    if name == "wall_parallel_planes":
+        out = [((-1, 0, 0), ()), ((1, 0, 0), ()), ((0, -1, 0), ()), ((0, 1, 0), ()),
+               ((0, 0, -1), (_D,)), ((0, 0, 1), (_U,))]
+        out += [((-1, -1, 0), ()), ((1, -1, 0), ()), ((-1, 1, 0), ()), ((1, 1, 0), ())]
+        for z, face in ((-1, _D), (1, _U)):
+            out += [((1, 0, z), (face,)), ((-1, 0, z), (face,)), ((0, 1, z), (face,)), ((0, -1, z), (face,))]
+        for z, face in ((-1, _D), (1, _U)):
+            out += [((1, 1, z), (face,)), ((-1, 1, z), (face,)), ((-1, 1, z), (face,)), ((-1, -1, z), (face,))]
+        return out, (_P, _P, _P, _P, _M, _M)
+    if name == "wall_canal":
+        def refl(sh):
+            r = []
+            if sh[1] == -1: r.append(_B)
+            if sh[1] == 1: r.append(_F)
+            if sh[2] == -1: r.append(_D)
+            if sh[2] == 1: r.append(_U)
+            return tuple(r)
+        order = [(-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1),
+                 (0, -1, -1), (0, -1, 1), (0, 1, -1), (0, 1, 1)]
+        for x in (-1, 1):
+            order += [(x, -1, 0), (x, 1, 0), (x, 0, -1), (x, 0, 1),
+                      (x, -1, -1), (x, -1, 1), (x, 1, -1), (x, 1, 1)]
+        return [(sh, refl(sh)) for sh in order], (_P, _P, _M, _M, _M, _M)
+    raise ValueError(f"unknown boundary configuration {name!r}")
+
+
+def image_table_of(images):
+    """ctypes array of ImageTangle for a list of (shift, reflect faces)."""
+    arr = (ImageTangle * max(len(images), 1))()
+    for i, (sh, refl) in enumerate(images):
+        arr[i].shift[:] = sh
+        r = list(refl) + [0] * (3 - len(refl))
+        arr[i].reflect[:] = r
+        arr[i].number_of_reflects = len(refl)
+    return arr
 
 
 def image_table(n_images: int):

@@ -6,6 +6,8 @@
 //  ov_eliminate_small_loops (tangle.c:1063-1128)
 //  ov_smooth              smooth / high_freq_cutoff / low_pass_filter
 //                         (vortex_smooth.c:134-175, 183-453, 459-462)
+//  ov_enforce_wall_boundaries  enforce_wall_boundaries + connect_to_wall
+//                         (tangle.c:822-1016)
 //  ov_step                one main-loop body (main.c:125-141)
 //
 // The reference's passes are sequential: a reconnection rewires connections
@@ -944,9 +946,192 @@ void hremove(ov_ctx *c, int i)
     h.st(i) = OV_EMPTY;
 }
 
+// ------------------------------------------------------------ walls
+// boundary_normals (boundaries.c:11-18): inward unit normals of the faces
+const double kWallNormal[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+
+inline bool solid_wall(const Geometry &g, int wall)
+{
+    return g.wall[wall] != OV_WALL_OPEN && g.wall[wall] != OV_WALL_PERIODIC;
+}
+
+// check_wall (tangle.c:822-838)
+bool hcheck_wall(Host &h, int k, int wall)
+{
+    const Geometry &g = h.c->geo;
+    const int ax = wall >> 1;
+    double p[3];
+    h.pos(k, p);
+    if ((wall & 1) == 0) return p[ax] < (h.P->rec_dist + g.lo[ax]);
+    return p[ax] > (g.hi[ax] - h.P->rec_dist);
+}
+
+// wall_dist (tangle.c:847-867)
+double hwall_dist(Host &h, int k, int wall)
+{
+    const Geometry &g = h.c->geo;
+    const int ax = wall >> 1;
+    double p[3];
+    h.pos(k, p);
+    return (wall & 1) == 0 ? p[ax] - g.lo[ax] : g.hi[ax] - p[ax];
+}
+
+// The device's positions and connections brought up to the host mirror's
+// (for direct sums on the current topology in the middle of a host pass).
+int sync_device_geometry(ov_ctx *c)
+{
+    const size_t n = (size_t)c->n_live;
+    if (n > (size_t)c->cap) {
+        int r = ov_grow_preserving(c, (int)n);
+        if (r) return r;
+    }
+    double *dd[3] = {c->node.x, c->node.y, c->node.z};
+    const double *hd[3] = {c->h_x.data(), c->h_y.data(), c->h_z.data()};
+    for (int a = 0; a < 3; ++a)
+        OV_CUDA(c, cudaMemcpyAsync(dd[a], hd[a], n * 8, cudaMemcpyHostToDevice, c->stream));
+    OV_CUDA(c, cudaMemcpyAsync(c->fwd, c->h_fwd.data(), n * 4, cudaMemcpyHostToDevice, c->stream));
+    return OV_OK;
+}
+
+// update_velocity(k, t, NULL) on the current topology, for a sign decision
+// dot(vel, n) > 0: FP64 direct sums on the GPU, and the reference's own
+// summation order on the host when the sum's error could flip the sign.
+int hdirect_sign(ov_ctx *c, Host &h, int k, const double tg[3], const double nm[3], double t, const double n[3],
+                 double *dotv)
+{
+    int r;
+    if ((r = sync_device_geometry(c))) return r;
+    double ex[10];
+    if ((r = ov_rec_exact(c, k, k, ex))) return r;
+    double vs[3], vel[3];
+    if (!hlia(h, k, tg, nm, t, vs)) return ov_fail(c, OV_ERR_TOPOLOGY, "walls: filament walk from %d failed", k);
+    for (int a = 0; a < 3; ++a) vs[a] = vs[a] + ex[a];
+    hfriction(h, k, tg, vs, t, vel);
+    const double tl = hlen(tg);
+    const double n_terms = (double)(h.hi - h.lo) * (h.c->geo.n_img + 1);
+    const double bound = (ex[3] + n_terms * 1.1102230246251565e-16 * ex[4]) * 1.7320508075688772 * 1.01 *
+                         (1.0 + fabs(h.P->alpha) * tl + fabs(h.P->alpha_p) * tl * tl);
+    double d = hdot(vel, n);
+    if (fabs(d) <= bound) {
+        hdirect_exact(h, k, tg, nm, t, vel);
+        d = hdot(vel, n);
+    }
+    *dotv = d;
+    return OV_OK;
+}
+
+// connect_to_wall (tangle.c:877-958) in member mi; *done = 1 when clipped
+int hconnect_to_wall(ov_ctx *c, int mi, int k, int wall, double t, std::vector<int> &new_nodes, int *done)
+{
+    *done = 0;
+    Host h = host_of(c, mi);
+    double tg[3], nm[3];
+    if (!htangent(h, k, tg, nm)) return ov_fail(c, OV_ERR_TOPOLOGY, "walls: filament walk from %d failed", k);
+    const double *n = kWallNormal[wall];
+    const double d0 = hwall_dist(h, k, wall);
+    // only a node in front of the wall and moving away from it is left alone
+    if (d0 > 0) {
+        double dv = 0;
+        int r = hdirect_sign(c, h, k, tg, nm, t, n, &dv);
+        if (r) return r;
+        if (dv > 0) return OV_OK;
+    }
+    // the reference applies the integer abs() to the normalised dot product,
+    // so this test only fires for a tangent exactly along the normal
+    const double nd = hdot(tg, n) / hlen(tg) / hlen(n);
+    if (abs((int)nd) > cos(h.P->reconnection_angle_cutoff)) return OV_OK;
+    const int next = h.fwd(k), prev = h.rev(k);
+    if (next < 0 || prev < 0) return OV_OK;
+    const double d1 = hwall_dist(h, next, wall), dm1 = hwall_dist(h, prev, wall);
+    double pk[3], pn[3], pp[3];
+    h.pos(k, pk);
+    h.pos(next, pn);
+    h.pos(prev, pp);
+    const double vd1 = hpwrap_len(c->geo, pk, pn), vdm1 = hpwrap_len(c->geo, pk, pp);
+    if (vd1 < d0 + d1 && vdm1 < d0 + dm1) return OV_OK;   // the length would grow
+    const int np1 = hget_empty(c, mi);
+    if (np1 < 0) return OV_ERR_ALLOC;
+    c->h_status[np1] = h.P->pin_mode;
+    c->h_pin[np1] = wall;
+    const int np2 = hget_empty(c, mi);
+    if (np2 < 0) return OV_ERR_ALLOC;
+    c->h_status[np2] = h.P->pin_mode;
+    c->h_pin[np2] = wall;
+    auto clip = [&](int dst, const double src[3], double dist) {
+        double tmp[3] = {n[0] * -dist, n[1] * -dist, n[2] * -dist};
+        c->h_x[dst] = src[0] + tmp[0];
+        c->h_y[dst] = src[1] + tmp[1];
+        c->h_z[dst] = src[2] + tmp[2];
+    };
+    clip(np1, pk, d0);
+    std::vector<int> &rc = c->h_recalc;
+    rc[k]++; rc[np1]++; rc[np2]++; rc[next]++; rc[prev]++;
+    if (d1 < dm1) {
+        clip(np2, pn, d1);
+        c->h_fwd[k] = np1;
+        c->h_fwd[np1] = -1; c->h_rev[np1] = k;
+        c->h_fwd[np2] = next; c->h_rev[np2] = -1;
+        c->h_rev[next] = np2;
+    } else {
+        clip(np2, pp, dm1);
+        c->h_rev[k] = np1;
+        c->h_fwd[np1] = k; c->h_rev[np1] = -1;
+        c->h_fwd[np2] = -1; c->h_rev[np2] = prev;
+        c->h_fwd[prev] = np2;
+    }
+    new_nodes.push_back(np1);
+    new_nodes.push_back(np2);
+    *done = 1;
+    return OV_OK;
+}
+
+// enforce_wall_boundaries (tangle.c:966-1016) on member mi
+int hwalls(ov_ctx *c, int mi, double t, std::vector<int> &new_nodes, int *clipped, int *removed)
+{
+    const Geometry &g = c->geo;
+    {
+        const Member &m = c->mem[mi];
+        std::fill(c->h_recalc.begin() + m.lo, c->h_recalc.begin() + m.lo + m.n, 0);
+    }
+    for (int wall = 0; wall < 6; ++wall) {
+        if (!solid_wall(g, wall)) continue;
+        for (int j = 0; j < c->mem[mi].n; ++j) {   // N may grow while clipping
+            Host h = host_of(c, mi);
+            const int k = h.lo + j;
+            const int st = h.st(k);
+            if (pinned(st) || st == OV_EMPTY || c->h_recalc[k]) continue;
+            if (!hcheck_wall(h, k, wall)) continue;
+            int done = 0, r = hconnect_to_wall(c, mi, k, wall, t, new_nodes, &done);
+            if (r) return r;
+            *clipped += done;
+        }
+    }
+    for (int wall = 0; wall < 6; ++wall) {
+        if (!solid_wall(g, wall)) continue;
+        for (int j = 0; j < c->mem[mi].n; ++j) {
+            Host h = host_of(c, mi);
+            const int k = h.lo + j;
+            const int st = h.st(k);
+            if (pinned(st) || st == OV_EMPTY) continue;
+            if (hwall_dist(h, k, wall) < 0) {
+                hremove(c, k);
+                ++*removed;
+            }
+        }
+    }
+    return OV_OK;
+}
+
+inline bool any_solid_wall(const Geometry &g)
+{
+    for (int w = 0; w < 6; ++w)
+        if (solid_wall(g, w)) return true;
+    return false;
+}
+
 // remesh (tangle.c:1018-1061) of member mi: slots in index order, including
 // the ones it inserts (and the range it grows into)
-int hremesh(ov_ctx *c, int mi, double min_dist, double max_dist, int *added_out, int *removed_out,
+int hremesh(ov_ctx *c, int mi, double min_dist, double max_dist, double time, int *added_out, int *removed_out,
             std::vector<int> &new_nodes)
 {
     int added = 0, removed = 0;
@@ -973,6 +1158,10 @@ int hremesh(ov_ctx *c, int mi, double min_dist, double max_dist, int *added_out,
         const Member &m = c->mem[mi];
         hperiodic(c, m.lo, m.lo + m.n);
         std::fill(c->h_recalc.begin() + m.lo, c->h_recalc.begin() + m.lo + m.n, 0);
+        if (any_solid_wall(c->geo)) {
+            int clipped = 0, gone = 0, r = hwalls(c, mi, time, new_nodes, &clipped, &gone);
+            if (r) return r;
+        }
     }
     *added_out = added;
     *removed_out = removed;
@@ -1190,7 +1379,6 @@ int ov_eliminate_small_loops(ov_ctx *c)
 
 int ov_remesh(ov_ctx *c, double min_dist, double max_dist, double t)
 {
-    (void)t;
     int r = ready(c);
     if (r) return r;
     if ((r = ov_pull_host(c))) return r;
@@ -1202,7 +1390,7 @@ int ov_remesh(ov_ctx *c, double min_dist, double max_dist, double t)
         double lo = c->mem.size() == 1 ? min_dist : c->mem[mi].params.dl_min;
         double hi = c->mem.size() == 1 ? max_dist : c->mem[mi].params.dl_max;
         int a = 0, d = 0;
-        if ((r = hremesh(c, mi, lo, hi, &a, &d, new_nodes))) {
+        if ((r = hremesh(c, mi, lo, hi, t, &a, &d, new_nodes))) {
             // keep host and device consistent before reporting
             ov_push_device(c, 1);
             return r == OV_ERR_ALLOC ? ov_fail(c, r, "remesh: no empty slot could be had") : r;
@@ -1596,6 +1784,41 @@ int ov_smooth(ov_ctx *c)
     return OV_OK;
 }
 
+int ov_enforce_wall_boundaries(ov_ctx *c, double t)
+{
+    int r = ready(c);
+    if (r) return r;
+    c->stats.wall_clipped = c->stats.wall_removed = 0;
+    if (!any_solid_wall(c->geo)) return OV_OK;
+    if ((r = ov_pull_host(c))) return r;
+    c->host_valid = false;
+    std::vector<int> new_nodes;
+    int clipped = 0, removed = 0;
+    for (int mi = 0; mi < (int)c->mem.size(); ++mi)
+        if ((r = hwalls(c, mi, t, new_nodes, &clipped, &removed))) {
+            ov_push_device(c, 1);
+            return r;
+        }
+    c->stats.wall_clipped = clipped;
+    c->stats.wall_removed = removed;
+    if (!clipped && !removed) {
+        c->host_valid = true;   // nothing changed (direct sums synced the device to the same state)
+        return OV_OK;
+    }
+    if ((r = ov_push_device(c, 1))) return r;
+    if (!new_nodes.empty()) {
+        int *d = nullptr;
+        OV_CUDA(c, cudaMalloc(&d, new_nodes.size() * sizeof(int)));
+        OV_CUDA(c, cudaMemcpy(d, new_nodes.data(), new_nodes.size() * sizeof(int), cudaMemcpyHostToDevice));
+        k_zero_vel<<<((int)new_nodes.size() + 255) / 256, 256, 0, c->stream>>>(
+            d, (int)new_nodes.size(), c->node.vx, c->node.vy, c->node.vz, c->node.sx, c->node.sy, c->node.sz);
+        c->launches++;
+        OV_CUDA(c, cudaStreamSynchronize(c->stream));
+        cudaFree(d);
+    }
+    return OV_OK;
+}
+
 int ov_step(ov_ctx *c, double t, double dt)
 {
     int r = ready(c);
@@ -1611,6 +1834,7 @@ int ov_step(ov_ctx *c, double t, double dt)
     };
     const auto t_all = now();
     auto t0 = now();
+    if ((r = ov_enforce_wall_boundaries(c, 0.0))) return r;   // main.c:125 (nothing to do in a periodic box)
     if ((r = ov_eliminate_small_loops(c))) return r;
     ms[0] += since(t0); t0 = now();
     if ((r = ov_reconnect(c, 0.0, &nrec, nullptr, nullptr, 0))) return r;

@@ -1288,7 +1288,8 @@ __global__ void __launch_bounds__(kRecThreads) k_rec_sums(RecArgs r, const int *
             const float lR2 = fmaf(R[0], R[0], fmaf(R[1], R[1], R[2] * R[2]));
             const float P0 = R[0] + sv[0], P1 = R[1] + sv[1], P2 = R[2] + sv[2];
             const float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
-            bool use64 = seg64 || lR2 < r.rnear2 || lp2 < r.rnear2;
+            // mirror images (reflected query points): FP64, as the split shift tables hold translations only
+            bool use64 = seg64 || lR2 < r.rnear2 || lp2 < r.rnear2 || (j >= 0 && r.geo.nreflect[j] > 0);
             float ra = 0, rb = 0, ab = 0, dot = 0, nd = 0;
             if (!use64) {
                 ra = rsqrtf(lR2);
@@ -1401,7 +1402,7 @@ __global__ void k_corr(RecArgs r, const int *__restrict__ cand, int c0, int nc, 
             const float lR2 = fmaf(R[0], R[0], fmaf(R[1], R[1], R[2] * R[2]));
             const float P0 = R[0] + sv[0], P1 = R[1] + sv[1], P2 = R[2] + sv[2];
             const float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
-            use64 = use64 || lR2 < r.rnear2 || lp2 < r.rnear2;
+            use64 = use64 || lR2 < r.rnear2 || lp2 < r.rnear2 || (j >= 0 && r.geo.nreflect[j] > 0);
             float ra = 0, rb = 0, ab = 0, dot = 0, nd = 0;
             if (!use64) {
                 ra = rsqrtf(lR2);

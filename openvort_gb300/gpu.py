@@ -88,6 +88,7 @@ def load(path: str | None = None):
         "ov_set_tuning": (C.c_int, [P, C.POINTER(abi.Tuning)]),
         "ov_autotune": (C.c_int, [P, C.c_double, C.POINTER(abi.Tuning), C.POINTER(C.c_float)]),
         "ov_step_times": (C.c_int, [P, C.POINTER(C.c_double), C.c_int]),
+        "ov_enforce_wall_boundaries": (C.c_int, [P, C.c_double]),
         "ov_direct_sums_bounded": (C.c_int, [P, C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
@@ -277,6 +278,9 @@ class Context:
 
     def enforce_periodic(self):
         self._check(self.lib.ov_enforce_periodic_boundaries(self._h))
+
+    def enforce_walls(self, t: float = 0.0):
+        self._check(self.lib.ov_enforce_wall_boundaries(self._h, t))
 
     def eliminate_small_loops(self):
         self._check(self.lib.ov_eliminate_small_loops(self._h))

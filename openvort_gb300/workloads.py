@@ -99,6 +99,7 @@ class HostTangle:
     status: np.ndarray | None = None
     walls: tuple = (1, 1, 1, 1, 1, 1)
     meta: dict = field(default_factory=dict)
+    image_set: str = ""   # a named boundary configuration (sets images and walls)
 
     def __post_init__(self):
         n = len(self.pos)
@@ -115,7 +116,12 @@ class HostTangle:
         else:
             st[:, 0] = self.status
         self.stat = st
-        self._images = abi.image_table(self.n_images)
+        if self.image_set:
+            imgs, self.walls = abi.image_set(self.image_set)
+            self.n_images = len(imgs)
+            self._images = abi.image_table_of(imgs)
+        else:
+            self._images = abi.image_table(self.n_images)
         self._state = None
 
     @property

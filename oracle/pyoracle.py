@@ -57,7 +57,8 @@ class CTangle:
             self.ts.bimg.images = C.cast(host._images, C.POINTER(abi.ImageTangle))
             self.ts.bimg.n = host.n_images
         else:
-            self.ts.bimg = lib.reference_images(host.n_images)
+            # the reference's own table: by name, or the periodic set of that size
+            self.ts.bimg = lib.reference_images(getattr(host, "image_set", "") or host.n_images)
         self.ts.next_empty = -1
         self.ts.total_empty = int((host.stat[:, 0] == abi.OV_EMPTY).sum())
 
@@ -147,8 +148,10 @@ class Checker:
             raise ValueError(kind)
 
     # ---------------------------------------------------------------- setup
-    def reference_images(self, n_images):
-        name = {6: "periodic_6", 18: "periodic_18", 26: "periodic_26", 0: "open_boundaries"}[n_images]
+    def reference_images(self, n_images_or_name):
+        key = n_images_or_name
+        name = {6: "periodic_6", 18: "periodic_18", 26: "periodic_26", 0: "open_boundaries",
+                "open": "open_boundaries"}.get(key, key)
         return abi.BoundaryImages.in_dll(self.lib, name)
 
     def set_params(self, p: abi.Params):

@@ -6,7 +6,7 @@ and stores inputs and outputs as small .npz files.  The GPU machine has no
 reference checkout; there the tests compare against these files and against
 the C restatement (oracle/ov_oracle.c), which these files also pin.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [walls]
 """
 from __future__ import annotations
 
@@ -55,9 +55,39 @@ def ref_step(c, t, time, dt):
     return n
 
 
+WALL_SETS = ("wall_1_open", "wall_1_18", "wall_1_26", "wall_2_4", "wall_2_2", "wall_parallel_planes",
+             "wall_canal", "open", "periodic_6")
+
+
+def walls(ref):
+    """Velocities under the reference's wall (mirror-image) and open boundary
+    configurations: one random-walk tangle, BH at theta 0.4 and direct sums."""
+    base = W.random_walk_tangle(8, 48, D=0.1, seed=17)
+    p = W.config_params("rw")
+    p.num_threads = 8
+    ref.set_params(p)
+    out = dict(pos=base.pos, conn=base.conn, status=base.stat, box_lo=base.box_lo, box_hi=base.box_hi,
+               sets=np.array(WALL_SETS))
+    nodes = np.arange(0, base.n, 13, dtype=np.int32)
+    out["direct_nodes"] = nodes
+    for name in WALL_SETS:
+        ht = W.HostTangle(base.pos.copy(), base.conn[:, 0].copy(), base.conn[:, 1].copy(), base.box_lo,
+                          base.box_hi, image_set=name)
+        t = ref.tangle(ht)
+        ref.update_tangle(t, 0.0)
+        out[f"{name}_vels"], out[f"{name}_vs"] = t.copy("vels"), t.copy("vs")
+        dv, dvs = ref.direct_velocities(t, nodes, 0.0)
+        out[f"{name}_direct_vels"], out[f"{name}_direct_vs"] = dv, dvs
+        t.free()
+    save("walls.npz", **out)
+
+
 def main():
     build(ref=True)
     ref = Checker("reference")
+    if len(sys.argv) > 1 and sys.argv[1] == "walls":
+        walls(ref)
+        return
 
     # 1. BH velocities (theta 0.4, 0.3 and 0.5) and direct sums on a small random-walk tangle
     ht = W.random_walk_tangle(16, 64, D=0.1, seed=3)
@@ -143,6 +173,9 @@ def main():
     save("rw256x256_sub.npz", nodes=sub, pos_sub=ht.pos[sub], vels=t.copy("vels")[sub], vs=t.copy("vs")[sub],
          pos_checksum=np.array([ht.pos.sum(), (ht.pos ** 2).sum()]))
     t.free()
+
+    # 6. Wall (mirror-image) and open boundary configurations
+    walls(ref)
 
 
 if __name__ == "__main__":

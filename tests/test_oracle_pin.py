@@ -172,3 +172,41 @@ def test_ring_velocity_known_answer(port):
     v = np.linalg.norm(t.copy("vels"), axis=1).mean()
     v_exact = 9.97e-4 / (4 * np.pi * R) * (np.log(8 * R / 1.3e-8) - 0.5)
     assert abs(v / v_exact - 1) < 0.05
+
+
+@pytest.mark.skipif(not reference_available(), reason="OpenVort checkout not built here")
+@pytest.mark.parametrize("name", ["periodic_6", "periodic_18", "periodic_26", "wall_1_open", "wall_1_18",
+                                  "wall_1_26", "wall_2_4", "wall_2_2", "wall_parallel_planes", "wall_canal"])
+def test_boundary_tables_match_reference(name):
+    """The named boundary configurations equal the reference's own tables
+    (read from the compiled reference), entry by entry."""
+    import ctypes as C
+    import os
+    from openvort_gb300 import abi
+    lib = C.CDLL(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref",
+                              "libovref.so"))
+    bimg = abi.BoundaryImages.in_dll(lib, name)
+    ours, _ = abi.image_set(name)
+    assert bimg.n == len(ours)
+    for j, (sh, refl) in enumerate(ours):
+        e = bimg.images[j]
+        assert tuple(e.shift) == tuple(sh), j
+        assert e.number_of_reflects == len(refl), j
+        assert tuple(e.reflect[:len(refl)]) == tuple(refl), j
+
+
+@pytest.mark.parametrize("name", ["wall_1_open", "wall_1_18", "wall_1_26", "wall_2_4", "wall_2_2",
+                                  "wall_parallel_planes", "wall_canal", "open", "periodic_6"])
+def test_wall_configurations_match_golden(port, golden, name):
+    """Mirror-image and open boundaries: the restatement's BH and direct-sum
+    velocities equal the reference's (golden vectors from the reference)."""
+    g = golden("walls.npz")
+    ht = W.HostTangle(g["pos"].copy(), g["conn"][:, 0].copy(), g["conn"][:, 1].copy(), g["box_lo"], g["box_hi"],
+                      image_set=name)
+    port.set_params(W.config_params("rw"))
+    t = port.tangle(ht)
+    port.update_tangle(t, 0.0)
+    assert node_rel_err(t.copy("vels"), g[f"{name}_vels"]) < 1e-12
+    dv, _ = port.direct_velocities(t, g["direct_nodes"], 0.0)
+    assert node_rel_err(dv, g[f"{name}_direct_vels"]) < 1e-12
+    t.free()
