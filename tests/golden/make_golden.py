@@ -82,11 +82,69 @@ def walls(ref):
     save("walls.npz", **out)
 
 
+def wall_rings(n_rings=6, radius=0.012, npts=40, seed=23):
+    """Rings in a box with mirror walls in z (wall_2_4), placed so that some
+    dip through the bottom or top wall and some pass within rec_dist of it."""
+    rng = np.random.default_rng(seed)
+    pos, fwd, rev = [], [], []
+    for r in range(n_rings):
+        cx, cy = rng.uniform(0.02, 0.08, 2)
+        top = r % 2 == 1
+        gap = [-0.004, 0.0002, 0.0, -0.001, 0.00035, 0.003][r % 6]
+        cz = (0.1 - radius - gap) if top else (radius + gap)
+        phi = 2 * np.pi * np.arange(npts) / npts
+        tilt = rng.uniform(-0.3, 0.3)
+        x = cx + radius * np.cos(phi) * np.cos(tilt)
+        y = cy + radius * np.cos(phi) * np.sin(tilt)
+        z = cz + radius * np.sin(phi)
+        base = r * npts
+        k = np.arange(npts)
+        pos.append(np.stack([x, y, z], 1))
+        fwd.append(base + (k + 1) % npts)
+        rev.append(base + (k - 1) % npts)
+    return W.HostTangle(np.concatenate(pos), np.concatenate(fwd), np.concatenate(rev), np.zeros(3),
+                        np.full(3, 0.1), image_set="wall_2_4")
+
+
+def wall_steps(ref):
+    """enforce_wall_boundaries on its own, then three main-loop steps
+    (main.c:125-141 without injection and smoothing) under mirror walls."""
+    import ctypes as C
+    ht = wall_rings()
+    p = W.config_params("rings8", rec_dist=8e-4)
+    p.num_threads = 8
+    ref.set_params(p)
+    t = ref.tangle(ht)
+    ref.lib.enforce_wall_boundaries.argtypes = [C.c_void_p, C.c_double]
+    ref.lib.enforce_wall_boundaries(C.addressof(t.ts), 0.0)
+    out = dict(pos=ht.pos, conn=ht.conn, status=ht.stat, box_lo=ht.box_lo, box_hi=ht.box_hi)
+    out["enf_N"], out["enf_pos"], out["enf_conn"], out["enf_status"] = t.n, t.copy("pos"), t.copy("conn"), \
+        t.copy("status")
+    dt = 5e-5
+    recs, conns, stats, poss, ns = [], [], [], [], []
+    for s_ in range(3):
+        ref.lib.enforce_wall_boundaries(C.addressof(t.ts), 0.0)
+        recs.append(ref_step(ref, t, s_ * dt, dt))
+        conns.append(t.copy("conn"))
+        stats.append(t.copy("status"))
+        poss.append(t.copy("pos"))
+        ns.append(t.n)
+    nmax = max(ns)
+    pad = lambda a, fill: np.concatenate([a, np.full((nmax - len(a),) + a.shape[1:], fill, a.dtype)])  # noqa: E731
+    out["recs"], out["dt"], out["steps_N"] = np.array(recs), dt, np.array(ns)
+    out["steps_conn"] = np.stack([pad(a, -1) for a in conns])
+    out["steps_status"] = np.stack([pad(a, -1) for a in stats])
+    out["steps_pos"] = np.stack([pad(a, 0.0) for a in poss])
+    t.free()
+    save("wall_steps.npz", **out)
+
+
 def main():
     build(ref=True)
     ref = Checker("reference")
     if len(sys.argv) > 1 and sys.argv[1] == "walls":
         walls(ref)
+        wall_steps(ref)
         return
 
     # 1. BH velocities (theta 0.4, 0.3 and 0.5) and direct sums on a small random-walk tangle
@@ -176,6 +234,7 @@ def main():
 
     # 6. Wall (mirror-image) and open boundary configurations
     walls(ref)
+    wall_steps(ref)
 
 
 if __name__ == "__main__":

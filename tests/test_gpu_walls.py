@@ -72,3 +72,37 @@ def test_bounded_sums_with_mirror_images(golden):
     s64, b64, _ = ctx.direct_sums_bounded(nodes, abi.OV_PREC_FP64)
     ctx.close()
     assert np.all(np.abs(s32 - s64).max(axis=1) <= b32 + b64)
+
+
+def test_wall_clipping_and_steps_match_reference(golden):
+    """enforce_wall_boundaries (connect_to_wall, removal behind walls) and three
+    full steps under mirror walls in z, against the reference's own run."""
+    g = golden("wall_steps.npz")
+    ht = W.HostTangle(g["pos"].copy(), g["conn"][:, 0].copy(), g["conn"][:, 1].copy(), g["box_lo"], g["box_hi"],
+                      image_set="wall_2_4")
+    p = W.config_params("rings8", rec_dist=8e-4)
+    ctx = gpu.Context(0, params=p)
+    ctx.upload(ht)
+    ctx.enforce_walls(0.0)
+    st = ctx.stats()
+    n, _, _ = ctx.tangle_info()
+    assert n == int(g["enf_N"])
+    out = ctx.download_resized(ht)
+    np.testing.assert_array_equal(out.conn, g["enf_conn"])
+    np.testing.assert_array_equal(out.stat, g["enf_status"])
+    used = g["enf_status"][:, 0] != abi.OV_EMPTY
+    assert np.abs(out.pos[used] - g["enf_pos"][used]).max() < 1e-14
+    assert st["wall_clipped"] > 0 and st["wall_removed"] > 0
+    dt = float(g["dt"])
+    for s in range(3):
+        ctx.step(s * dt, dt)
+        assert ctx.stats()["reconnections"] == int(g["recs"][s])
+        n, _, _ = ctx.tangle_info()
+        assert n == int(g["steps_N"][s])
+        out = ctx.download_resized(ht)
+        np.testing.assert_array_equal(out.conn, g["steps_conn"][s][:n])
+        np.testing.assert_array_equal(out.stat, g["steps_status"][s][:n])
+        used = g["steps_status"][s][:n, 0] != abi.OV_EMPTY
+        ref = g["steps_pos"][s][:n]
+        assert np.abs(out.pos[used] - ref[used]).max() / np.abs(ref[used]).max() < 1e-10
+    ctx.close()
