@@ -307,6 +307,20 @@ int ov_step_times(const ov_ctx *ctx, double *ms, int n);
 
 int ov_get_stats(const ov_ctx *ctx, ov_stats *out);
 
+/* --------------------------------------------------------------- frames */
+/* Frame files in the reference's text format (utils.c:68-199).  Host-only
+   calls except ov_save_frame.
+   ov_write_frame: save_tangle of a host tangle, loops in its order; digits
+     15 writes the reference's files exactly, 17 an exact round trip.
+   ov_frame_slots: the N, next_empty and total_empty that load_tangle
+     leaves in a tangle made by create_tangle(n0) (any may be NULL).
+   ov_read_frame: load_tangle into `t`, which must have at least that N.
+   ov_save_frame: the context's tangle (member 0) or an ensemble member. */
+int ov_write_frame(const ov_tangle_state *t, const char *path, int digits);
+int ov_frame_slots(const char *path, int n0, int *n_slots, int *next_empty, int *total_empty);
+int ov_read_frame(const char *path, int n0, ov_tangle_state *t);
+int ov_save_frame(ov_ctx *ctx, int member, const char *path, int digits);
+
 /* -------------------------------------------------------------- timing */
 /* CUDA-event timing on the context's stream (for benchmarks). */
 int ov_timer_start(ov_ctx *ctx);

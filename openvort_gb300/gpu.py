@@ -89,6 +89,11 @@ def load(path: str | None = None):
         "ov_autotune": (C.c_int, [P, C.c_double, C.POINTER(abi.Tuning), C.POINTER(C.c_float)]),
         "ov_step_times": (C.c_int, [P, C.POINTER(C.c_double), C.c_int]),
         "ov_enforce_wall_boundaries": (C.c_int, [P, C.c_double]),
+        "ov_write_frame": (C.c_int, [TS, C.c_char_p, C.c_int]),
+        "ov_frame_slots": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int)]),
+        "ov_read_frame": (C.c_int, [C.c_char_p, C.c_int, TS]),
+        "ov_save_frame": (C.c_int, [P, C.c_int, C.c_char_p, C.c_int]),
         "ov_direct_sums_bounded": (C.c_int, [P, C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
@@ -112,6 +117,33 @@ def declared_symbols() -> list[str]:
         for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b((?:ov|ovd)_\w+)\s*\(", txt, flags=re.M):
             names.append(m.group(1))
     return sorted(set(names))
+
+
+def write_frame(host, path: str, digits: int = 15):
+    """save_tangle of a host tangle (no GPU needed)."""
+    st = host.state()
+    rc = load().ov_write_frame(C.byref(st), path.encode(), digits)
+    if rc:
+        raise OVError(rc, f"writing {path}")
+
+
+def read_frame(path: str, n0: int = 1):
+    """load_tangle into a fresh host tangle made as create_tangle(n0) would
+    be, grown as the file needs (no GPU needed); returns the HostTangle and
+    its (next_empty, total_empty)."""
+    from .workloads import HostTangle
+    L = load()
+    n, ne, te = C.c_int(0), C.c_int(0), C.c_int(0)
+    rc = L.ov_frame_slots(path.encode(), n0, C.byref(n), C.byref(ne), C.byref(te))
+    if rc:
+        raise OVError(rc, f"reading {path}")
+    ht = HostTangle(np.zeros((n.value, 3)), np.full(n.value, -1), np.full(n.value, -1), np.zeros(3), np.ones(3),
+                    n_images=0, status=np.full(n.value, abi.OV_EMPTY))
+    st = ht.state()
+    rc = L.ov_read_frame(path.encode(), n0, C.byref(st))
+    if rc:
+        raise OVError(rc, f"reading {path}")
+    return ht, (st.next_empty, st.total_empty)   # the call filled ht's arrays in place
 
 
 def _grown(host, n: int):
@@ -278,6 +310,9 @@ class Context:
 
     def enforce_periodic(self):
         self._check(self.lib.ov_enforce_periodic_boundaries(self._h))
+
+    def save_frame(self, path: str, member: int = 0, digits: int = 15):
+        self._check(self.lib.ov_save_frame(self._h, member, path.encode(), digits))
 
     def enforce_walls(self, t: float = 0.0):
         self._check(self.lib.ov_enforce_wall_boundaries(self._h, t))

@@ -120,6 +120,11 @@ def wall_steps(ref):
     out = dict(pos=ht.pos, conn=ht.conn, status=ht.stat, box_lo=ht.box_lo, box_hi=ht.box_hi)
     out["enf_N"], out["enf_pos"], out["enf_conn"], out["enf_status"] = t.n, t.copy("pos"), t.copy("conn"), \
         t.copy("status")
+    # the reference's frame file of this state
+    out["enf_vels"], out["enf_tangents"], out["enf_normals"] = t.copy("vels"), t.copy("tangents"), \
+        t.copy("normals")
+    ref.lib.save_tangle.argtypes = [C.c_char_p, C.c_void_p]
+    ref.lib.save_tangle(os.path.join(OUT, "frame_walls.txt").encode(), C.addressof(t.ts))
     dt = 5e-5
     recs, conns, stats, poss, ns = [], [], [], [], []
     for s_ in range(3):
@@ -135,6 +140,10 @@ def wall_steps(ref):
     out["steps_conn"] = np.stack([pad(a, -1) for a in conns])
     out["steps_status"] = np.stack([pad(a, -1) for a in stats])
     out["steps_pos"] = np.stack([pad(a, 0.0) for a in poss])
+    # EMPTY slots hold whatever realloc left there: store zeros
+    out["enf_pos"][out["enf_status"][:, 0] == -1] = 0.0
+    for s_ in range(3):
+        out["steps_pos"][s_][out["steps_status"][s_][:, 0] == -1] = 0.0
     t.free()
     save("wall_steps.npz", **out)
 
