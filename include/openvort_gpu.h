@@ -120,6 +120,7 @@ typedef struct ov_stats {
     int64_t reconnect_evaluated;    /* candidate velocities the decisions used */
     int64_t wall_clipped;           /* last wall pass: nodes connected to a wall */
     int64_t wall_removed;           /* last wall pass: nodes removed behind a wall */
+    int64_t injected_nodes;         /* last injection pass: nodes added */
 } ov_stats;
 
 typedef struct ov_ctx ov_ctx;
@@ -290,10 +291,11 @@ int ov_enforce_wall_boundaries(ov_ctx *ctx, double t);
 int ov_remesh(ov_ctx *ctx, double min_dist, double max_dist, double t);
 /* smooth (vortex_smooth.c:459): per-loop low-pass filter when use_freq_filter. */
 int ov_smooth(ov_ctx *ctx);
-/* One iteration of the reference's main loop body (main.c:125-141), without
-   injection and frame output: wall boundaries, small loops, reconnect, small
-   loops, smooth, periodic wrap, remesh (with wall boundaries after
-   insertions), small loops, update_tangle, rk4_step, periodic wrap. */
+/* One iteration of the reference's main loop body (main.c:123-141), without
+   frame output: injection (when set with ov_set_injection), wall
+   boundaries, small loops, reconnect, small loops, smooth, periodic wrap,
+   remesh (with wall boundaries after insertions), small loops,
+   update_tangle, rk4_step, periodic wrap. */
 int ov_step(ov_ctx *ctx, double t, double dt);
 /* Host wall-clock milliseconds of the last ov_step, per pass: [0] small
    loops (three calls), [1] reconnect, [2] smooth, [3] periodic wrap (two
@@ -307,6 +309,44 @@ int ov_step_times(const ov_ctx *ctx, double *ms, int n);
 
 int ov_get_stats(const ov_ctx *ctx, ov_stats *out);
 
+/* ------------------------------------------------------------ injection */
+/* The reference's injection settings (vortex_constants.h:48-56,
+   initial_conditions.c:61-68) for one tangle, with the state of its random
+   stream: drand48's 48-bit state X as erand48 holds it, rand48[0] the low
+   16 bits (srand48(s) leaves {0x330E, s & 0xFFFF, (s >> 16) & 0xFFFF}). */
+typedef struct ov_injection {
+    int loop_injection;        /* loop_injection: inject_loop on */
+    double loop_frequency;     /* loop_injection_frequency: loops per unit time */
+    int line_injection;        /* line_injection: inject_line_pairs on */
+    int line_n;                /* line_injection_n: pairs per injection */
+    double line_frequency;     /* line_injection_frequency */
+    int line_polarized;        /* line_injection_polarized */
+    unsigned short rand48[3];  /* the stream inject_loop / inject_line_pairs draw from */
+} ov_injection;
+
+/* add_loop (vortex_injection.c:49): a ring of (int)(4 pi r / (dl_max +
+   dl_min)) FREE nodes around `center` in the plane normal to `dir`, slots
+   from get_next_empty_node after doubling the member until it has that
+   many EMPTY slots.  member: 0 for a single tangle. */
+int ov_add_loop(ov_ctx *ctx, int member, const double center[3], const double dir[3], double r);
+/* add_line_in_zdir (vortex_injection.c:267): a line along z through
+   (x, y) from wall to wall, pinned (params pin_mode) at both ends;
+   direction +1 runs up, -1 down. */
+int ov_add_line_in_zdir(ov_ctx *ctx, int member, double x, double y, int direction);
+/* Injection settings of one member (all members when member < 0); resets
+   the last-injection times of inject_loop and inject_line_pairs to 0, as a
+   new process starts them.  ov_get_injection returns the settings with the
+   stream's current state. */
+int ov_set_injection(ov_ctx *ctx, int member, const ov_injection *inj);
+int ov_get_injection(const ov_ctx *ctx, int member, ov_injection *out);
+/* inject_vortices (vortex_injection.c:702) for every member, in member
+   order.  ov_step runs it first (main.c:123) when a member has injection
+   on. */
+int ov_inject_vortices(ov_ctx *ctx, double t);
+/* One draw of the injection stream (drand48's recurrence on the state x,
+   as erand48 draws); host only. */
+double ov_erand48(unsigned short x[3]);
+
 /* --------------------------------------------------------------- frames */
 /* Frame files in the reference's text format (utils.c:68-199).  Host-only
    calls except ov_save_frame.
@@ -314,7 +354,10 @@ int ov_get_stats(const ov_ctx *ctx, ov_stats *out);
      15 writes the reference's files exactly, 17 an exact round trip.
    ov_frame_slots: the N, next_empty and total_empty that load_tangle
      leaves in a tangle made by create_tangle(n0) (any may be NULL).
-   ov_read_frame: load_tangle into `t`, which must have at least that N.
+   ov_read_frame: load_tangle into `t`, which must have at least that N
+     slots; n0 is the slot count before the load and t->next_empty,
+     t->total_empty on entry the bookkeeping before it (create_tangle(n0)
+     leaves 0 and n0).
    ov_save_frame: the context's tangle (member 0) or an ensemble member. */
 int ov_write_frame(const ov_tangle_state *t, const char *path, int digits);
 int ov_frame_slots(const char *path, int n0, int *n_slots, int *next_empty, int *total_empty);

@@ -51,6 +51,20 @@ void *ovd_octree_build(const ov_tangle_state *tangle);
 void ovd_octree_get_vs(const ov_tangle_state *tangle, const void *tree, const ov_vec3 *r,
                        double resolution, ov_vec3 *res);
 void ovd_octree_destroy(void *tree);
+/* enforce_wall_boundaries   include/tangle.h:100, src/tangle.c:966 (may grow the arrays) */
+void ovd_enforce_wall_boundaries(ov_tangle_state *tangle, double time);
+/* save_tangle / load_tangle include/utils.h:17-18, src/utils.c:132-199 (no GPU;
+   load_tangle grows the arrays with realloc as expand_tangle does) */
+void ovd_save_tangle(const char *filename, ov_tangle_state *tangle);
+int ovd_load_tangle(const char *filename, ov_tangle_state *tangle);
+/* add_loop / add_line_in_zdir  include/vortex_injection.h:13, 23,
+   src/vortex_injection.c:49, 267 (may grow the arrays) */
+void ovd_add_loop(ov_tangle_state *tangle, ov_vec3 *center, ov_vec3 *dir, double r);
+void ovd_add_line_in_zdir(ov_tangle_state *tangle, double x, double y, int direction);
+/* inject_vortices           include/vortex_injection.h:35, src/vortex_injection.c:702
+   (settings from the reference's loop_injection / line_injection globals,
+   draws from the process's drand48 stream) */
+void ovd_inject_vortices(ov_tangle_state *tangle, double t);
 /* status of the last ovd_* call (an ov_status value) */
 int ovd_last_status(void);
 

@@ -80,7 +80,36 @@ class Stats(C.Structure):
         "node_evals", "cells", "max_depth", "visits", "accepts", "warp_steps", "fp64_fallbacks",
         "near_field_fp64", "out_of_root", "reconnections", "remesh_added", "remesh_removed",
         "small_loops_removed", "error_word", "reconnect_candidates", "reconnect_fp64_pairs",
-        "reconnect_exact_pairs", "reconnect_evaluated", "wall_clipped", "wall_removed")]
+        "reconnect_exact_pairs", "reconnect_evaluated", "wall_clipped", "wall_removed", "injected_nodes")]
+
+
+class Injection(C.Structure):
+    """ov_injection: the reference's injection settings (vortex_constants.h:48-56)
+    and the state of the drand48 stream they draw from (rand48[0] = low 16 bits)."""
+    _fields_ = [("loop_injection", C.c_int), ("loop_frequency", C.c_double), ("line_injection", C.c_int),
+                ("line_n", C.c_int), ("line_frequency", C.c_double), ("line_polarized", C.c_int),
+                ("rand48", C.c_ushort * 3)]
+
+
+def srand48_state(seed: int) -> tuple[int, int, int]:
+    """The drand48 state srand48(seed) leaves: the high 32 bits from the seed,
+    the low 16 bits 0x330E (POSIX)."""
+    seed &= 0xFFFFFFFF
+    return (0x330E, seed & 0xFFFF, seed >> 16)
+
+
+def make_injection(seed: int = 0, loop_frequency: float = 0.0, line_n: int = 0, line_frequency: float = 0.0,
+                   line_polarized: bool = False) -> Injection:
+    """Injection settings; a frequency of 0 leaves that kind off."""
+    inj = Injection()
+    inj.loop_injection = int(loop_frequency > 0)
+    inj.loop_frequency = loop_frequency if loop_frequency > 0 else 1.0
+    inj.line_injection = int(line_frequency > 0 and line_n > 0)
+    inj.line_n = line_n
+    inj.line_frequency = line_frequency if line_frequency > 0 else 1.0
+    inj.line_polarized = int(line_polarized)
+    inj.rand48[:] = srand48_state(seed)
+    return inj
 
 
 class Tuning(C.Structure):

@@ -323,9 +323,6 @@ static int ensure_stage(ov_ctx *c, size_t bytes)
 {
     if (c->h_stage_bytes >= bytes) return OV_OK;
     if (c->h_stage) cudaFreeHost(c->h_stage);
-    if (c->h_corr) cudaFreeHost(c->h_corr);
-    if (c->h_pf) cudaFreeHost(c->h_pf);
-    if (c->rec_ev) cudaEventDestroy(c->rec_ev);
     c->h_stage = nullptr;
     OV_CUDA(c, cudaMallocHost(&c->h_stage, bytes));
     c->h_stage_bytes = bytes;

@@ -6,6 +6,7 @@
  * the reference reads them; the caller's tangle_state is uploaded, the GPU
  * computes, and the fields the reference function writes are copied back.
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -19,6 +20,9 @@ extern double VORTEX_WIDTH, KAPPA, alpha, alpha_p, global_dl_min, global_dl_max,
 extern double reconnection_angle_cutoff, freq_to_cutoff, BH_resolution;
 extern int use_mutual_friction, use_BH, small_loop_cutoff, use_freq_filter, global_num_threads, pin_mode;
 extern ov_ext_vel vn_conf, vs_conf, vb_conf;
+/* injection settings (include/vortex_constants.h:48-56) */
+extern int loop_injection, line_injection, line_injection_n, line_injection_polarized;
+extern double loop_injection_frequency, line_injection_frequency;
 
 static ov_ctx *g_ctx = NULL;
 static int g_status = OV_OK;
@@ -233,6 +237,118 @@ void ovd_smooth(ov_tangle_state *t)
     g_status = OV_OK;
 }
 
+void ovd_enforce_wall_boundaries(ov_tangle_state *t, double time)
+{
+    ov_ctx *c = context();
+    if (!c) return;
+    TRY(ov_upload_tangle_fields(c, t, OV_F_POS | OV_F_TOPOLOGY), "enforce_wall_boundaries");
+    TRY(ov_enforce_wall_boundaries(c, time), "enforce_wall_boundaries");
+    TRY(sync_back(t, OV_F_POS | OV_F_TOPOLOGY), "enforce_wall_boundaries");
+    g_status = OV_OK;
+}
+
+/* Frame files need no GPU. */
+void ovd_save_tangle(const char *filename, ov_tangle_state *t)
+{
+    report(ov_write_frame(t, filename, 15), "save_tangle");
+}
+
+int ovd_load_tangle(const char *filename, ov_tangle_state *t)
+{
+    int n = 0;
+    TRYV(ov_frame_slots(filename, t->N, &n, NULL, NULL), "load_tangle", -1);
+    const int n0 = t->N;
+    if (n > t->N) TRYV(grow_host(t, n), "load_tangle", -1);
+    TRYV(ov_read_frame(filename, n0, t), "load_tangle", -1);
+    g_status = OV_OK;
+    return 0;
+}
+
+void ovd_add_loop(ov_tangle_state *t, ov_vec3 *center, ov_vec3 *dir, double r)
+{
+    ov_ctx *c = context();
+    if (!c) return;
+    TRY(ov_upload_tangle_fields(c, t, OV_F_POS | OV_F_TOPOLOGY), "add_loop");
+    TRY(ov_add_loop(c, 0, center->p, dir->p, r), "add_loop");
+    TRY(sync_back(t, OV_F_POS | OV_F_TOPOLOGY), "add_loop");
+    g_status = OV_OK;
+}
+
+void ovd_add_line_in_zdir(ov_tangle_state *t, double x, double y, int direction)
+{
+    ov_ctx *c = context();
+    if (!c) return;
+    TRY(ov_upload_tangle_fields(c, t, OV_F_POS | OV_F_TOPOLOGY), "add_line_in_zdir");
+    TRY(ov_add_line_in_zdir(c, 0, x, y, direction), "add_line_in_zdir");
+    TRY(sync_back(t, OV_F_POS | OV_F_TOPOLOGY), "add_line_in_zdir");
+    g_status = OV_OK;
+}
+
+/* vec3_normalize (vec3_math.c:208) */
+static void normalize3(double v[3])
+{
+    if (v[0] == 0 && v[1] == 0 && v[2] == 0) return;
+    double d = 0;
+    for (int k = 0; k < 3; ++k) d += v[k] * v[k];
+    const double m = 1 / sqrt(d);
+    for (int k = 0; k < 3; ++k) v[k] = v[k] * m;
+}
+
+/* inject_vortices (vortex_injection.c:702-800) drawing from the process's
+   own drand48 stream, so the draws interleave with the rest of the
+   program's as they do in the reference.  The direction's three draws are
+   taken last component first, the order in which the reference build
+   (gcc, x86-64) evaluates vec3()'s arguments. */
+void ovd_inject_vortices(ov_tangle_state *t, double time)
+{
+    static double last_loop = 0, last_line = 0;
+    ov_ctx *c = NULL;
+    const double left = t->box.bottom_left_back.p[0], right = t->box.top_right_front.p[0];
+    const double back = t->box.bottom_left_back.p[1], front = t->box.top_right_front.p[1];
+    g_status = OV_OK;
+    if (loop_injection) {
+        double dir[3];
+        dir[2] = -drand48();
+        dir[1] = 2 * (drand48() - 0.5);
+        dir[0] = 2 * (drand48() - 0.5);
+        normalize3(dir);
+        if (!(time - last_loop < 1 / loop_injection_frequency)) {
+            last_loop = time;
+            double cent[3];
+            cent[2] = t->box.top_right_front.p[2];
+            cent[0] = left + (right - left) * drand48();
+            cent[1] = back + (front - back) * drand48();
+            const double D = fabs(right - left), rmin = 0.05 * D, rmax = 0.25 * D;
+            const double r = rmin + (rmax - rmin) * drand48();
+            if (!(c = context())) return;
+            TRY(ov_upload_tangle_fields(c, t, OV_F_POS | OV_F_TOPOLOGY), "inject_vortices");
+            TRY(ov_add_loop(c, 0, cent, dir, r), "inject_vortices");
+        }
+    }
+    if (line_injection && !(time - last_line < 1 / line_injection_frequency)) {
+        last_line = time;
+        for (int k = 0; k < line_injection_n; ++k) {
+            const double x1 = left + drand48() * (right - left);
+            const double x2 = left + drand48() * (right - left);
+            double y1, y2;
+            if (line_injection_polarized) {
+                y1 = back + (1 + drand48()) * (front - back) / 2;
+                y2 = back + drand48() * (front - back) / 2;
+            } else {
+                y1 = back + drand48() * (front - back);
+                y2 = back + drand48() * (front - back);
+            }
+            if (!c) {
+                if (!(c = context())) return;
+                TRY(ov_upload_tangle_fields(c, t, OV_F_POS | OV_F_TOPOLOGY), "inject_vortices");
+            }
+            TRY(ov_add_line_in_zdir(c, 0, x1, y1, +1), "inject_vortices");
+            TRY(ov_add_line_in_zdir(c, 0, x2, y2, -1), "inject_vortices");
+        }
+    }
+    if (c) TRY(sync_back(t, OV_F_POS | OV_F_TOPOLOGY), "inject_vortices");
+}
+
 /* The octree API: the tree lives in the context; the handle only marks
    that ovd_octree_build ran for this tangle. */
 typedef struct ovd_tree { const ov_tangle_state *tangle; } ovd_tree;
@@ -280,4 +396,10 @@ void __wrap_octree_get_vs(const ov_tangle_state *t, const void *tree, const ov_v
     ovd_octree_get_vs(t, tree, r, res_, res);
 }
 void __wrap_octree_destroy(void *tree) { ovd_octree_destroy(tree); }
+void __wrap_enforce_wall_boundaries(ov_tangle_state *t, double time) { ovd_enforce_wall_boundaries(t, time); }
+void __wrap_save_tangle(const char *f, ov_tangle_state *t) { ovd_save_tangle(f, t); }
+int __wrap_load_tangle(const char *f, ov_tangle_state *t) { return ovd_load_tangle(f, t); }
+void __wrap_add_loop(ov_tangle_state *t, ov_vec3 *c, ov_vec3 *d, double r) { ovd_add_loop(t, c, d, r); }
+void __wrap_add_line_in_zdir(ov_tangle_state *t, double x, double y, int d) { ovd_add_line_in_zdir(t, x, y, d); }
+void __wrap_inject_vortices(ov_tangle_state *t, double time) { ovd_inject_vortices(t, time); }
 #endif

@@ -4,6 +4,8 @@
 //  ov_frame_slots   the slot count and empty-slot bookkeeping load_tangle
 //                   leaves (utils.c:92-130, 185-199, with expand_tangle)
 //  ov_read_frame    load_tangle into a caller tangle of that many slots
+//                   (its next_empty / total_empty on entry are those of
+//                   the tangle before the load)
 //  ov_save_frame    a context's tangle (or ensemble member) to a frame file
 //
 // A frame line: loop index, position, velocity, tangent, normal (each three
@@ -65,17 +67,19 @@ int parse_frame(const char *path, std::vector<FrameLine> &out)
 }
 
 // The slot count, next_empty and total_empty after load_tangle into a
-// tangle made by create_tangle(n0): statuses reset for the n0 slots, then
+// tangle of n0 slots whose bookkeeping was (next_empty0, total_empty0)
+// (create_tangle leaves 0 and n0): statuses reset for the n0 slots, then
 // each line grows the tangle by doubling while its id does not fit
 // (expand_tangle, tangle.c:68-101, which also runs get_next_empty_node on
-// the statuses loaded so far).
+// the statuses loaded so far).  Without growth the bookkeeping is left as
+// it was, as load_point leaves it.
 struct LoadBook {
     int n, next_empty, total_empty;
 };
 
-LoadBook simulate_load(const std::vector<FrameLine> &lines, int n0)
+LoadBook simulate_load(const std::vector<FrameLine> &lines, int n0, int next_empty0, int total_empty0)
 {
-    LoadBook b{n0, 0, n0};
+    LoadBook b{n0, next_empty0, total_empty0};
     std::vector<int> st(n0 > 0 ? n0 : 0, OV_EMPTY);
     auto search = [&]() -> int {   // search_next_empty_node (tangle.c:201-234)
         const int N = b.n;
@@ -166,7 +170,7 @@ int ov_frame_slots(const char *path, int n0, int *n_slots, int *next_empty, int 
     std::vector<FrameLine> lines;
     int r = parse_frame(path, lines);
     if (r) return r;
-    LoadBook b = simulate_load(lines, n0);
+    LoadBook b = simulate_load(lines, n0, 0, n0);
     if (n_slots) *n_slots = b.n;
     if (next_empty) *next_empty = b.next_empty;
     if (total_empty) *total_empty = b.total_empty;
@@ -179,7 +183,7 @@ int ov_read_frame(const char *path, int n0, ov_tangle_state *t)
     std::vector<FrameLine> lines;
     int r = parse_frame(path, lines);
     if (r) return r;
-    LoadBook b = simulate_load(lines, n0);
+    LoadBook b = simulate_load(lines, n0, t->next_empty, t->total_empty);
     if (t->N < b.n) return OV_ERR_ARG;   // size the tangle with ov_frame_slots first
     if (t->N > 0 && (!t->vnodes || !t->vels || !t->tangents || !t->normals || !t->connections || !t->status))
         return OV_ERR_ARG;

@@ -149,6 +149,9 @@ struct Member {
     int next_empty = -1;   // tangle.h:63, local index
     int total_empty = 0;   // tangle.h:64
     ov_params params{};
+    ov_injection inj{};        // injection settings and random stream
+    double last_loop = 0;      // inject_loop's last injection time
+    double last_line = 0;      // inject_line_pairs' last injection time
 };
 
 // Launch shape of the traversal, chosen by ov_autotune or set by the caller.

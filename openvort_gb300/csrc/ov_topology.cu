@@ -8,6 +8,9 @@
 //                         (vortex_smooth.c:134-175, 183-453, 459-462)
 //  ov_enforce_wall_boundaries  enforce_wall_boundaries + connect_to_wall
 //                         (tangle.c:822-1016)
+//  ov_add_loop, ov_add_line_in_zdir, ov_inject_vortices
+//                         add_loop, add_line_in_zdir, inject_vortices
+//                         (vortex_injection.c:18-100, 267-319, 702-800)
 //  ov_step                one main-loop body (main.c:125-141)
 //
 // The reference's passes are sequential: a reconnection rewires connections
@@ -1361,6 +1364,247 @@ int smooth_long_loop(ov_ctx *c, const int *nodes, int len, double freq_to_cutoff
 
 }  // namespace
 
+namespace {
+
+// ------------------------------------------------------------- injection
+// drand48 as POSIX defines it: X <- (0x5DEECE66D X + 0xB) mod 2^48, the
+// result X / 2^48; x[0] holds the low 16 bits of X.
+double hrand48(unsigned short x[3])
+{
+    uint64_t X = (uint64_t)x[0] | (uint64_t)x[1] << 16 | (uint64_t)x[2] << 32;
+    X = (0x5DEECE66DULL * X + 0xBULL) & 0xFFFFFFFFFFFFULL;
+    x[0] = (unsigned short)(X & 0xFFFF);
+    x[1] = (unsigned short)((X >> 16) & 0xFFFF);
+    x[2] = (unsigned short)((X >> 32) & 0xFFFF);
+    return ldexp((double)X, -48);
+}
+
+// vec3_normalize (vec3_math.c:208): times the reciprocal of the length
+void hnormalize(double v[3])
+{
+    if (v[0] == 0 && v[1] == 0 && v[2] == 0) return;
+    const double m = 1 / hlen(v);
+    for (int i = 0; i < 3; ++i) v[i] = v[i] * m;
+}
+
+// number_of_empty_nodes (tangle.c:128) of member mi
+int hcount_empty(ov_ctx *c, int mi)
+{
+    const Member &m = c->mem[mi];
+    int n = 0;
+    for (int k = m.lo; k < m.lo + m.n; ++k) n += c->h_status[k] == OV_EMPTY;
+    return n;
+}
+
+// the doubling loop before add_loop / add_line_in_zdir place their nodes
+int hreserve_empty(ov_ctx *c, int mi, int need)
+{
+    for (int guard = 0; hcount_empty(c, mi) < need; ++guard) {
+        const int n = c->mem[mi].n;
+        if (guard > 40) return OV_ERR_ALLOC;
+        int r = hexpand(c, mi, n > 0 ? 2 * n : 1);
+        if (r) return r;
+    }
+    return OV_OK;
+}
+
+// perpendicular (vortex_injection.c:18-40): dir's component-free part of
+// (1,0,0), or of (0,1,0) when dir is along x, normalised
+void hperpendicular(const double dir[3], double out[3])
+{
+    const double ax[2][3] = {{1, 0, 0}, {0, 1, 0}};
+    for (int q = 0; q < 2; ++q) {
+        const double m = -hdot(ax[q], dir);
+        for (int i = 0; i < 3; ++i) out[i] = dir[i] * m;
+        for (int i = 0; i < 3; ++i) out[i] = out[i] + ax[q][i];
+        if (q == 0 && !(hlen(out) > 1e-8)) continue;
+        hnormalize(out);
+        return;
+    }
+}
+
+void hset_node(ov_ctx *c, int i, const double p[3], int status)
+{
+    c->h_x[i] = p[0]; c->h_y[i] = p[1]; c->h_z[i] = p[2];
+    c->h_status[i] = status;
+}
+
+// add_loop (vortex_injection.c:49-100) in member mi; the new slots are
+// appended to `added`
+int hadd_loop(ov_ctx *c, int mi, const double center[3], const double dir[3], double r, std::vector<int> &added)
+{
+    const ov_params &P = c->mem[mi].params;
+    const int npts = (int)(4 * M_PI * r / (P.dl_max + P.dl_min));
+    if (npts <= 0) return OV_OK;   // the reference would write connections[-1]
+    int rc = hreserve_empty(c, mi, npts);
+    if (rc) return rc;
+    double zdir[3], u[3], v[3];
+    hperpendicular(dir, zdir);
+    hcross(u, zdir, dir);
+    hcross(v, dir, u);
+    hnormalize(u);
+    hnormalize(v);
+    int first = -1, curr = -1, last = -1;
+    for (int k = 0; k < npts; ++k) {
+        const double phi = 2 * M_PI / npts * k;
+        const double cs = cos(phi), sn = sin(phi);
+        double p[3], q[3];
+        for (int i = 0; i < 3; ++i) p[i] = u[i] * (r * cs);
+        for (int i = 0; i < 3; ++i) q[i] = v[i] * (r * sn);
+        for (int i = 0; i < 3; ++i) p[i] = p[i] + q[i];
+        for (int i = 0; i < 3; ++i) p[i] = p[i] + center[i];
+        curr = hget_empty(c, mi);
+        if (curr < 0) return OV_ERR_ALLOC;
+        if (first < 0) first = curr;
+        hset_node(c, curr, p, OV_FREE);
+        if (curr != first) {
+            c->h_rev[curr] = last;
+            c->h_fwd[last] = curr;
+        }
+        last = curr;
+        added.push_back(curr);
+    }
+    c->h_fwd[curr] = first;
+    c->h_rev[first] = curr;
+    return OV_OK;
+}
+
+// add_line_in_zdir (vortex_injection.c:267-319) in member mi
+int hadd_line_z(ov_ctx *c, int mi, double x, double y, int direction, std::vector<int> &added)
+{
+    const ov_params &P = c->mem[mi].params;
+    const double zmin = c->geo.lo[2], zmax = c->geo.hi[2];
+    const int points = (int)(2 * (zmax - zmin) / (P.dl_max - P.dl_min));
+    if (points <= 0) return OV_ERR_ARG;   // the reference divides by it
+    int rc = hreserve_empty(c, mi, points);
+    if (rc) return rc;
+    const double dz = (zmax - zmin) / points;
+    const double zstart = direction > 0 ? zmin : zmax;
+    const double zend = direction > 0 ? zmax : zmin;
+    double s[3] = {x, y, zstart};
+    int pt = hget_empty(c, mi);
+    if (pt < 0) return OV_ERR_ALLOC;
+    hset_node(c, pt, s, P.pin_mode);
+    c->h_pin[pt] = direction > 0 ? OV_DOWN : OV_UP;
+    c->h_rev[pt] = -1;
+    added.push_back(pt);
+    for (int k = 1; k < points - 1; ++k) {
+        const int last = pt;
+        if ((pt = hget_empty(c, mi)) < 0) return OV_ERR_ALLOC;
+        s[2] = zstart + direction * k * dz;
+        hset_node(c, pt, s, OV_FREE);
+        c->h_pin[pt] = OV_NOT_A_FACE;
+        c->h_rev[pt] = last;
+        c->h_fwd[last] = pt;
+        added.push_back(pt);
+    }
+    s[2] = zend;
+    const int last = pt;
+    if ((pt = hget_empty(c, mi)) < 0) return OV_ERR_ALLOC;
+    hset_node(c, pt, s, P.pin_mode);
+    c->h_pin[pt] = direction > 0 ? OV_UP : OV_DOWN;
+    c->h_rev[pt] = last;
+    c->h_fwd[pt] = -1;
+    c->h_fwd[last] = pt;
+    added.push_back(pt);
+    return OV_OK;
+}
+
+// Host mirror for a pass that may change nothing: pulled on first use.
+struct LazyMirror {
+    ov_ctx *c;
+    bool pulled = false;
+    int get()
+    {
+        if (pulled) return OV_OK;
+        int r = ov_pull_host(c);
+        if (r) return r;
+        c->host_valid = false;
+        pulled = true;
+        return OV_OK;
+    }
+};
+
+// inject_loop (vortex_injection.c:715-752) for member mi.  Three draws for
+// the direction come first, whether or not it is time to inject; the build
+// of the reference this follows evaluates vec3()'s three arguments from
+// the last to the first.
+int hinject_loop(ov_ctx *c, int mi, double t, LazyMirror &mir, std::vector<int> &added)
+{
+    Member &m = c->mem[mi];
+    unsigned short *x = m.inj.rand48;
+    double dir[3];
+    dir[2] = -hrand48(x);
+    dir[1] = 2 * (hrand48(x) - 0.5);
+    dir[0] = 2 * (hrand48(x) - 0.5);
+    hnormalize(dir);
+    if (t - m.last_loop < 1 / m.inj.loop_frequency) return OV_OK;
+    m.last_loop = t;
+    const double left = c->geo.lo[0], right = c->geo.hi[0], back = c->geo.lo[1], front = c->geo.hi[1];
+    double cent[3];
+    cent[2] = c->geo.hi[2];
+    cent[0] = left + (right - left) * hrand48(x);
+    cent[1] = back + (front - back) * hrand48(x);
+    const double D = fabs(right - left), rmin = 0.05 * D, rmax = 0.25 * D;
+    const double r = rmin + (rmax - rmin) * hrand48(x);
+    int rc = mir.get();
+    if (rc) return rc;
+    return hadd_loop(c, mi, cent, dir, r, added);
+}
+
+// inject_line_pairs (vortex_injection.c:760-800) for member mi
+int hinject_lines(ov_ctx *c, int mi, double t, LazyMirror &mir, std::vector<int> &added)
+{
+    Member &m = c->mem[mi];
+    unsigned short *x = m.inj.rand48;
+    if (t - m.last_line < 1 / m.inj.line_frequency) return OV_OK;
+    m.last_line = t;
+    for (int k = 0; k < m.inj.line_n; ++k) {
+        const double left = c->geo.lo[0], right = c->geo.hi[0], back = c->geo.lo[1], front = c->geo.hi[1];
+        const double x1 = left + hrand48(x) * (right - left);
+        const double x2 = left + hrand48(x) * (right - left);
+        double y1, y2;
+        if (m.inj.line_polarized) {
+            y1 = back + (1 + hrand48(x)) * (front - back) / 2;
+            y2 = back + hrand48(x) * (front - back) / 2;
+        } else {
+            y1 = back + hrand48(x) * (front - back);
+            y2 = back + hrand48(x) * (front - back);
+        }
+        int rc = mir.get();
+        if (rc) return rc;
+        if ((rc = hadd_line_z(c, mi, x1, y1, +1, added))) return rc;
+        if ((rc = hadd_line_z(c, mi, x2, y2, -1, added))) return rc;
+    }
+    return OV_OK;
+}
+
+// host mirror -> device after nodes were added; their velocities start at 0
+int push_added(ov_ctx *c, const std::vector<int> &added)
+{
+    int r = ov_push_device(c, 1);
+    if (r || added.empty()) return r;
+    int *d = nullptr;
+    OV_CUDA(c, cudaMalloc(&d, added.size() * sizeof(int)));
+    OV_CUDA(c, cudaMemcpy(d, added.data(), added.size() * sizeof(int), cudaMemcpyHostToDevice));
+    k_zero_vel<<<((int)added.size() + 255) / 256, 256, 0, c->stream>>>(
+        d, (int)added.size(), c->node.vx, c->node.vy, c->node.vz, c->node.sx, c->node.sy, c->node.sz);
+    c->launches++;
+    OV_CUDA(c, cudaGetLastError());
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(d);
+    return OV_OK;
+}
+
+bool any_injection(const ov_ctx *c)
+{
+    for (const Member &m : c->mem)
+        if (m.inj.loop_injection || m.inj.line_injection) return true;
+    return false;
+}
+
+}  // namespace
+
 extern "C" {
 
 int ov_eliminate_small_loops(ov_ctx *c)
@@ -1819,6 +2063,74 @@ int ov_enforce_wall_boundaries(ov_ctx *c, double t)
     return OV_OK;
 }
 
+int ov_add_loop(ov_ctx *c, int member, const double center[3], const double dir[3], double r)
+{
+    int rc = ready(c);
+    if (rc) return rc;
+    if (!center || !dir || member < 0 || member >= (int)c->mem.size() || !(r >= 0)) return OV_ERR_ARG;
+    if ((rc = ov_pull_host(c))) return rc;
+    c->host_valid = false;
+    std::vector<int> added;
+    rc = hadd_loop(c, member, center, dir, r, added);
+    c->stats.injected_nodes = (int64_t)added.size();
+    int rp = push_added(c, added);
+    if (rc) return ov_fail(c, rc, "add_loop: no empty slot could be had");
+    return rp;
+}
+
+int ov_add_line_in_zdir(ov_ctx *c, int member, double x, double y, int direction)
+{
+    int rc = ready(c);
+    if (rc) return rc;
+    if (member < 0 || member >= (int)c->mem.size()) return OV_ERR_ARG;
+    if ((rc = ov_pull_host(c))) return rc;
+    c->host_valid = false;
+    std::vector<int> added;
+    rc = hadd_line_z(c, member, x, y, direction, added);
+    c->stats.injected_nodes = (int64_t)added.size();
+    int rp = push_added(c, added);
+    if (rc) return ov_fail(c, rc, "add_line_in_zdir: %s", rc == OV_ERR_ARG ? "no nodes fit the box" : "no empty slot");
+    return rp;
+}
+
+int ov_set_injection(ov_ctx *c, int member, const ov_injection *inj)
+{
+    if (!c || !inj || member >= (int)c->mem.size() || c->mem.empty()) return OV_ERR_ARG;
+    if (inj->line_n < 0) return OV_ERR_ARG;
+    for (int mi = member < 0 ? 0 : member; mi < (member < 0 ? (int)c->mem.size() : member + 1); ++mi) {
+        c->mem[mi].inj = *inj;
+        c->mem[mi].last_loop = c->mem[mi].last_line = 0;
+    }
+    return OV_OK;
+}
+
+int ov_get_injection(const ov_ctx *c, int member, ov_injection *out)
+{
+    if (!c || !out || member < 0 || member >= (int)c->mem.size()) return OV_ERR_ARG;
+    *out = c->mem[member].inj;
+    return OV_OK;
+}
+
+int ov_inject_vortices(ov_ctx *c, double t)
+{
+    int rc = ready(c);
+    if (rc) return rc;
+    c->stats.injected_nodes = 0;
+    if (!any_injection(c)) return OV_OK;
+    LazyMirror mir{c};
+    std::vector<int> added;
+    for (int mi = 0; mi < (int)c->mem.size() && !rc; ++mi) {
+        if (c->mem[mi].inj.loop_injection) rc = hinject_loop(c, mi, t, mir, added);
+        if (!rc && c->mem[mi].inj.line_injection) rc = hinject_lines(c, mi, t, mir, added);
+    }
+    c->stats.injected_nodes = (int64_t)added.size();
+    int rp = mir.pulled ? push_added(c, added) : OV_OK;
+    if (rc) return ov_fail(c, rc, "inject_vortices: %s", rc == OV_ERR_ARG ? "no nodes fit the box" : "no empty slot");
+    return rp;
+}
+
+double ov_erand48(unsigned short x[3]) { return x ? hrand48(x) : -1.0; }
+
 int ov_step(ov_ctx *c, double t, double dt)
 {
     int r = ready(c);
@@ -1834,6 +2146,7 @@ int ov_step(ov_ctx *c, double t, double dt)
     };
     const auto t_all = now();
     auto t0 = now();
+    if (any_injection(c) && (r = ov_inject_vortices(c, t))) return r;   // main.c:123
     if ((r = ov_enforce_wall_boundaries(c, 0.0))) return r;   // main.c:125 (nothing to do in a periodic box)
     if ((r = ov_eliminate_small_loops(c))) return r;
     ms[0] += since(t0); t0 = now();

@@ -95,6 +95,12 @@ def load(path: str | None = None):
         "ov_read_frame": (C.c_int, [C.c_char_p, C.c_int, TS]),
         "ov_save_frame": (C.c_int, [P, C.c_int, C.c_char_p, C.c_int]),
         "ov_direct_sums_bounded": (C.c_int, [P, C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(C.c_double)]),
+        "ov_add_loop": (C.c_int, [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double]),
+        "ov_add_line_in_zdir": (C.c_int, [P, C.c_int, C.c_double, C.c_double, C.c_int]),
+        "ov_set_injection": (C.c_int, [P, C.c_int, C.POINTER(abi.Injection)]),
+        "ov_get_injection": (C.c_int, [P, C.c_int, C.POINTER(abi.Injection)]),
+        "ov_inject_vortices": (C.c_int, [P, C.c_double]),
+        "ov_erand48": (C.c_double, [C.POINTER(C.c_ushort)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -119,6 +125,12 @@ def declared_symbols() -> list[str]:
     return sorted(set(names))
 
 
+def erand48(state) -> float:
+    """One draw of the injection stream from `state` (a ctypes c_ushort * 3,
+    advanced in place); host only."""
+    return load().ov_erand48(state)
+
+
 def write_frame(host, path: str, digits: int = 15):
     """save_tangle of a host tangle (no GPU needed)."""
     st = host.state()
@@ -140,6 +152,7 @@ def read_frame(path: str, n0: int = 1):
     ht = HostTangle(np.zeros((n.value, 3)), np.full(n.value, -1), np.full(n.value, -1), np.zeros(3), np.ones(3),
                     n_images=0, status=np.full(n.value, abi.OV_EMPTY))
     st = ht.state()
+    st.next_empty, st.total_empty = 0, n0   # as create_tangle(n0) leaves them
     rc = L.ov_read_frame(path.encode(), n0, C.byref(st))
     if rc:
         raise OVError(rc, f"reading {path}")
@@ -313,6 +326,27 @@ class Context:
 
     def save_frame(self, path: str, member: int = 0, digits: int = 15):
         self._check(self.lib.ov_save_frame(self._h, member, path.encode(), digits))
+
+    def add_loop(self, center, direction, radius: float, member: int = 0):
+        """add_loop (vortex_injection.c:49): a ring of FREE nodes."""
+        c3 = (C.c_double * 3)(*map(float, center))
+        d3 = (C.c_double * 3)(*map(float, direction))
+        self._check(self.lib.ov_add_loop(self._h, member, c3, d3, float(radius)))
+
+    def add_line_in_zdir(self, x: float, y: float, direction: int, member: int = 0):
+        """add_line_in_zdir (vortex_injection.c:267): a pinned line along z."""
+        self._check(self.lib.ov_add_line_in_zdir(self._h, member, float(x), float(y), int(direction)))
+
+    def set_injection(self, inj: abi.Injection, member: int = -1):
+        self._check(self.lib.ov_set_injection(self._h, member, C.byref(inj)))
+
+    def get_injection(self, member: int = 0) -> abi.Injection:
+        out = abi.Injection()
+        self._check(self.lib.ov_get_injection(self._h, member, C.byref(out)))
+        return out
+
+    def inject_vortices(self, t: float):
+        self._check(self.lib.ov_inject_vortices(self._h, float(t)))
 
     def enforce_walls(self, t: float = 0.0):
         self._check(self.lib.ov_enforce_wall_boundaries(self._h, t))

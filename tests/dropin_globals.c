@@ -26,3 +26,9 @@ double BH_resolution = 0.4;
 ov_ext_vel vn_conf = {OV_SIMPLE, 10.493799, 0, 0, {{1.0, 0, 0}}};
 ov_ext_vel vb_conf = {OV_NO_FLOW, 0, 0, 0, {{0, 0, 0}}};
 ov_ext_vel vs_conf = {OV_SIMPLE, 0.493799, 0, 0, {{-1.0, 0, 0}}};
+int loop_injection = 0;
+double loop_injection_frequency = 1;
+int line_injection = 0;
+int line_injection_n = 1;
+double line_injection_frequency = 1;
+int line_injection_polarized = 0;

@@ -6,7 +6,7 @@ and stores inputs and outputs as small .npz files.  The GPU machine has no
 reference checkout; there the tests compare against these files and against
 the C restatement (oracle/ov_oracle.c), which these files also pin.
 
-Usage:  python tests/golden/make_golden.py [walls]
+Usage:  python tests/golden/make_golden.py [walls | injection]
 """
 from __future__ import annotations
 
@@ -148,12 +148,117 @@ def wall_steps(ref):
     save("wall_steps.npz", **out)
 
 
+def _libc():
+    import ctypes as C
+    libc = C.CDLL("libc.so.6")
+    libc.drand48.restype = C.c_double
+    libc.srand48.argtypes = [C.c_long]
+    return libc
+
+
+def _set_injection(ref, inj):
+    import ctypes as C
+    L = ref.lib
+    C.c_int.in_dll(L, "loop_injection").value = inj["loop_injection"]
+    C.c_double.in_dll(L, "loop_injection_frequency").value = inj["loop_frequency"]
+    C.c_int.in_dll(L, "line_injection").value = inj["line_injection"]
+    C.c_int.in_dll(L, "line_injection_n").value = inj["line_n"]
+    C.c_double.in_dll(L, "line_injection_frequency").value = inj["line_frequency"]
+    C.c_int.in_dll(L, "line_injection_polarized").value = inj["line_polarized"]
+
+
+def _state(t):
+    return dict(N=t.n, pos=t.copy("pos"), conn=t.copy("conn"), status=t.copy("status"),
+                next_empty=t.ts.next_empty, total_empty=t.ts.total_empty)
+
+
+def injection(ref):
+    """add_loop / add_line_in_zdir on a wall tangle with a freed ring (slot
+    reuse, pool doubling, both branches of perpendicular), and the drand48
+    stream the injection draws from."""
+    import ctypes as C
+    ht = wall_rings()
+    ring = slice(2 * 40, 3 * 40)   # free the third ring's slots
+    ht.stat[ring, 0] = -1
+    ht.conn[ring] = -1
+    p = W.config_params("rings8", rec_dist=8e-4)
+    out = dict(pos=ht.pos, conn=ht.conn, status=ht.stat, box_lo=ht.box_lo, box_hi=ht.box_hi)
+    V = C.c_double * 3
+    calls = [("loop", (0.05, 0.05, 0.05), (1.0, 0.0, 0.0), 0.004), ("loop", (0.03, 0.06, 0.02), (0.3, -0.5, 0.8), 0.02),
+             ("line", 0.031, 0.077, +1), ("line", 0.062, 0.018, -1), ("loop", (0.07, 0.02, 0.09), (0, 0, -1), 0.009)]
+    ref.lib.add_loop.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+    ref.lib.add_line_in_zdir.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int]
+    for k, call in enumerate(calls):
+        p.pin_mode = 1 if k < 3 else 2   # PINNED, then PINNED_SLIP for the second line
+        ref.set_params(p)
+        if k == 0:
+            t = ref.tangle(ht)
+        if call[0] == "loop":
+            ref.lib.add_loop(C.addressof(t.ts), C.byref(V(*call[1])), C.byref(V(*call[2])), call[3])
+        else:
+            ref.lib.add_line_in_zdir(C.addressof(t.ts), call[1], call[2], call[3])
+        for key, v in _state(t).items():
+            out[f"c{k}_{key}"] = v
+        # EMPTY slots hold whatever realloc left there
+        out[f"c{k}_pos"][out[f"c{k}_status"][:, 0] == -1] = 0.0
+    t.free()
+    libc = _libc()
+    libc.srand48(20240607)
+    out["rand_seed"] = 20240607
+    out["rand_draws"] = np.array([libc.drand48() for _ in range(64)])
+    save("inject.npz", **out)
+
+
+INJECT_CONF = dict(loop_injection=1, loop_frequency=2e4, line_injection=1, line_n=1, line_frequency=1e4,
+                   line_polarized=1, seed=777)
+
+
+def inject_steps(ref):
+    """inject_vortices then the main-loop body (main.c:123-141 without
+    smoothing) for three steps under mirror walls in z."""
+    import ctypes as C
+    ht = wall_rings()
+    p = W.config_params("rings8", rec_dist=8e-4)
+    p.num_threads = 8
+    ref.set_params(p)
+    _set_injection(ref, INJECT_CONF)
+    libc = _libc()
+    libc.srand48(INJECT_CONF["seed"])
+    t = ref.tangle(ht)
+    ref.lib.enforce_wall_boundaries.argtypes = [C.c_void_p, C.c_double]
+    ref.lib.inject_vortices.argtypes = [C.c_void_p, C.c_double]
+    dt = 5e-5
+    out = dict(pos=ht.pos, conn=ht.conn, status=ht.stat, box_lo=ht.box_lo, box_hi=ht.box_hi, dt=dt,
+               **{f"inj_{k}": v for k, v in INJECT_CONF.items()})
+    recs, states = [], []
+    for s_ in range(3):
+        ref.lib.inject_vortices(C.addressof(t.ts), s_ * dt)
+        ref.lib.enforce_wall_boundaries(C.addressof(t.ts), 0.0)
+        recs.append(ref_step(ref, t, s_ * dt, dt))
+        states.append(_state(t))
+    out["next_draw"] = libc.drand48()
+    nmax = max(st["N"] for st in states)
+    pad = lambda a, fill: np.concatenate([a, np.full((nmax - len(a),) + a.shape[1:], fill, a.dtype)])  # noqa: E731
+    out["recs"], out["steps_N"] = np.array(recs), np.array([st["N"] for st in states])
+    out["steps_conn"] = np.stack([pad(st["conn"], -1) for st in states])
+    out["steps_status"] = np.stack([pad(st["status"], -1) for st in states])
+    out["steps_pos"] = np.stack([pad(st["pos"], 0.0) for st in states])
+    for s_ in range(3):
+        out["steps_pos"][s_][out["steps_status"][s_][:, 0] == -1] = 0.0
+    t.free()
+    save("inject_steps.npz", **out)
+
+
 def main():
     build(ref=True)
     ref = Checker("reference")
     if len(sys.argv) > 1 and sys.argv[1] == "walls":
         walls(ref)
         wall_steps(ref)
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "injection":
+        injection(ref)
+        inject_steps(ref)
         return
 
     # 1. BH velocities (theta 0.4, 0.3 and 0.5) and direct sums on a small random-walk tangle
@@ -244,6 +349,10 @@ def main():
     # 6. Wall (mirror-image) and open boundary configurations
     walls(ref)
     wall_steps(ref)
+
+    # 7. Injection (add_loop, add_line_in_zdir, inject_vortices in the main loop)
+    injection(ref)
+    inject_steps(ref)
 
 
 if __name__ == "__main__":

@@ -19,7 +19,8 @@ REF_INC = "/root/reference/include"
 OBJ = os.path.join(ROOT, "oracle", "_ref", "obj")
 WRAPPED = ["update_tangents_normals", "update_velocities", "update_velocity", "rk4_step", "reconnect", "remesh",
            "eliminate_small_loops", "enforce_periodic_boundaries", "smooth", "octree_build", "octree_get_vs",
-           "octree_destroy"]
+           "octree_destroy", "enforce_wall_boundaries", "save_tangle", "load_tangle", "add_loop", "add_line_in_zdir",
+           "inject_vortices"]
 
 
 @pytest.mark.skipif(not (os.path.isdir(REF_INC) and glob.glob(os.path.join(OBJ, "*.o"))),

@@ -31,7 +31,7 @@ def dropin(tmp_path_factory):
     subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-o", str(out),
                     os.path.join(ROOT, "openvort_gb300", "csrc", "ov_dropin.c"),
                     os.path.join(ROOT, "tests", "dropin_globals.c"),
-                    "-L" + libdir, "-lovgpu", "-Wl,-rpath," + libdir], check=True)
+                    "-L" + libdir, "-lovgpu", "-Wl,-rpath," + libdir, "-lm"], check=True)
     L = C.CDLL(str(out))
     for name, args, res in [
         ("ovd_update_tangents_normals", [TS], None), ("ovd_update_velocities", [TS, C.c_double], None),
@@ -41,7 +41,12 @@ def dropin(tmp_path_factory):
         ("ovd_eliminate_small_loops", [TS], None), ("ovd_enforce_periodic_boundaries", [TS], None),
         ("ovd_smooth", [TS], None), ("ovd_octree_build", [TS], C.c_void_p),
         ("ovd_octree_get_vs", [TS, C.c_void_p, C.POINTER(abi.Vec3), C.c_double, C.POINTER(abi.Vec3)], None),
-        ("ovd_octree_destroy", [C.c_void_p], None), ("ovd_last_status", [], C.c_int)]:
+        ("ovd_octree_destroy", [C.c_void_p], None), ("ovd_last_status", [], C.c_int),
+        ("ovd_enforce_wall_boundaries", [TS, C.c_double], None),
+        ("ovd_save_tangle", [C.c_char_p, TS], None), ("ovd_load_tangle", [C.c_char_p, TS], C.c_int),
+        ("ovd_add_loop", [TS, C.POINTER(abi.Vec3), C.POINTER(abi.Vec3), C.c_double], None),
+        ("ovd_add_line_in_zdir", [TS, C.c_double, C.c_double, C.c_int], None),
+        ("ovd_inject_vortices", [TS, C.c_double], None)]:
         fn = getattr(L, name)
         fn.argtypes = args
         fn.restype = res
@@ -56,6 +61,7 @@ def set_globals(L, p):
     dbl("global_dl_min", p.dl_min); dbl("global_dl_max", p.dl_max); dbl("rec_dist", p.rec_dist)
     dbl("reconnection_angle_cutoff", p.reconnection_angle_cutoff); i32("small_loop_cutoff", p.small_loop_cutoff)
     i32("use_freq_filter", p.use_freq_filter); dbl("freq_to_cutoff", p.freq_to_cutoff)
+    i32("pin_mode", p.pin_mode)
     for name, src in (("vn_conf", p.vn), ("vs_conf", p.vs), ("vb_conf", p.vb)):
         dst = abi.ExtVel.in_dll(L, name)
         C.memmove(C.addressof(dst), C.addressof(src), C.sizeof(abi.ExtVel))
@@ -129,3 +135,83 @@ def test_octree_api(dropin):
         np.testing.assert_allclose(list(got.p), list(ref.p), rtol=1e-10, atol=1e-14)
     dropin.ovd_octree_destroy(tree)
     port.lib.orc_octree_destroy(otree)
+
+
+def vec3(v):
+    out = abi.Vec3()
+    out.p[:] = list(map(float, v))
+    return out
+
+
+def test_injection_walls_and_frames_in_place(dropin, golden, tmp_path):
+    """add_loop / add_line_in_zdir, then inject_vortices + enforce_wall_boundaries
+    + the rest of the main loop through the drop-in, against the reference's
+    run; save_tangle / load_tangle round trip of the result."""
+    from tests.test_gpu_inject import CALLS, wall_tangle
+    port = Checker("port")
+    g = golden("inject.npz")
+    p = W.config_params("rings8", rec_dist=8e-4)
+    t = port.tangle(wall_tangle(g))
+    for k, call in enumerate(CALLS):
+        p.pin_mode = abi.OV_PINNED if k < 3 else abi.OV_PINNED_SLIP
+        set_globals(dropin, p)
+        if call[0] == "loop":
+            dropin.ovd_add_loop(C.byref(t.ts), C.byref(vec3(call[1])), C.byref(vec3(call[2])), call[3])
+        else:
+            dropin.ovd_add_line_in_zdir(C.byref(t.ts), call[1], call[2], call[3])
+        assert dropin.ovd_last_status() == 0
+        assert t.n == int(g[f"c{k}_N"])
+        assert (t.ts.next_empty, t.ts.total_empty) == (int(g[f"c{k}_next_empty"]), int(g[f"c{k}_total_empty"]))
+        np.testing.assert_array_equal(t.copy("conn"), g[f"c{k}_conn"])
+        np.testing.assert_array_equal(t.copy("status"), g[f"c{k}_status"])
+
+    g = golden("inject_steps.npz")
+    p = W.config_params("rings8", rec_dist=8e-4)
+    set_globals(dropin, p)
+    i32 = lambda n, v: setattr(C.c_int.in_dll(dropin, n), "value", int(v))  # noqa: E731
+    dbl = lambda n, v: setattr(C.c_double.in_dll(dropin, n), "value", float(v))  # noqa: E731
+    i32("loop_injection", g["inj_loop_injection"]); dbl("loop_injection_frequency", g["inj_loop_frequency"])
+    i32("line_injection", g["inj_line_injection"]); i32("line_injection_n", g["inj_line_n"])
+    dbl("line_injection_frequency", g["inj_line_frequency"]); i32("line_injection_polarized", g["inj_line_polarized"])
+    libc = C.CDLL("libc.so.6")
+    libc.srand48.argtypes = [C.c_long]
+    libc.drand48.restype = C.c_double
+    libc.srand48(int(g["inj_seed"]))
+    t = port.tangle(wall_tangle(g))
+    ts = C.byref(t.ts)
+    dt = float(g["dt"])
+    for s_ in range(3):
+        dropin.ovd_inject_vortices(ts, s_ * dt)
+        dropin.ovd_enforce_wall_boundaries(ts, 0.0)
+        dropin.ovd_eliminate_small_loops(ts)
+        assert dropin.ovd_reconnect(ts, 0.0) == int(g["recs"][s_])
+        dropin.ovd_eliminate_small_loops(ts)
+        dropin.ovd_enforce_periodic_boundaries(ts)
+        dropin.ovd_remesh(ts, p.dl_min, p.dl_max, 0.0)
+        dropin.ovd_eliminate_small_loops(ts)
+        dropin.ovd_update_tangents_normals(ts)
+        dropin.ovd_update_velocities(ts, s_ * dt)
+        dropin.ovd_rk4_step(ts, s_ * dt, dt)
+        dropin.ovd_enforce_periodic_boundaries(ts)
+        assert dropin.ovd_last_status() == 0
+        n = t.n
+        assert n == int(g["steps_N"][s_])
+        np.testing.assert_array_equal(t.copy("conn"), g["steps_conn"][s_][:n])
+        np.testing.assert_array_equal(t.copy("status"), g["steps_status"][s_][:n])
+        live = g["steps_status"][s_][:n, 0] != abi.OV_EMPTY
+        ref = g["steps_pos"][s_][:n][live]
+        assert np.abs(t.copy("pos")[live] - ref).max() / np.abs(ref).max() < 1e-10
+    assert libc.drand48() == float(g["next_draw"])
+    i32("loop_injection", 0); i32("line_injection", 0)
+
+    path = str(tmp_path / "frame.txt").encode()
+    dropin.ovd_save_tangle(path, ts)
+    back = port.tangle(W.HostTangle(np.zeros((1, 3)), np.full(1, -1), np.full(1, -1), np.zeros(3), np.full(3, 0.1),
+                                    status=np.full(1, abi.OV_EMPTY)))
+    back.ts.next_empty, back.ts.total_empty = 0, 1
+    assert dropin.ovd_load_tangle(path, C.byref(back.ts)) == 0
+    assert back.n >= t.n
+    live = t.copy("status")[:, 0] != abi.OV_EMPTY
+    np.testing.assert_array_equal(back.copy("conn")[:t.n][live], t.copy("conn")[live])
+    np.testing.assert_array_equal(back.copy("status")[:t.n][live], t.copy("status")[live])
+    assert np.abs(back.copy("pos")[:t.n][live] - t.copy("pos")[live]).max() < 1e-15
