@@ -58,6 +58,34 @@ class TangleState(C.Structure):
     ]
 
 
+class SphDomain(C.Structure):
+    """ov_sph_domain: the spherical fork's section (radii, angular half widths)."""
+    _fields_ = [("inner_radius", C.c_double), ("outer_radius", C.c_double), ("azimut_angle", C.c_double),
+                ("polar_angle", C.c_double)]
+
+
+class SphTangleState(C.Structure):
+    """ov_sph_tangle_state: the spherical fork's tangle_state (status.pin_wall = pin_surface)."""
+    _fields_ = [
+        ("vnodes", C.POINTER(Vec3)), ("vels", C.POINTER(Vec3)), ("vs", C.POINTER(Vec3)),
+        ("tangents", C.POINTER(Vec3)), ("normals", C.POINTER(Vec3)),
+        ("recalculate", C.POINTER(C.c_int)), ("connections", C.POINTER(Neighbour)),
+        ("status", C.POINTER(NodeStatus)), ("domain_section", SphDomain),
+        ("N", C.c_int), ("next_empty", C.c_int), ("total_empty", C.c_int),
+    ]
+
+
+class SphParams(C.Structure):
+    """ov_sph_params: the spherical fork's globals on its velocity path."""
+    _fields_ = [("kappa", C.c_double), ("vortex_width", C.c_double), ("alpha", C.c_double), ("alpha_p", C.c_double),
+                ("use_mutual_friction", C.c_int), ("bh_resolution", C.c_double), ("dl_min", C.c_double),
+                ("dl_max", C.c_double), ("q_dot", C.c_double), ("temp_bath", C.c_double),
+                ("use_temperature", C.c_int), ("outer_surface", C.c_int)]
+
+
+OV_INNER, OV_OUTER = 0, 1
+
+
 class ExtVel(C.Structure):
     _fields_ = [("type", C.c_int), ("strength", C.c_double), ("time_of_linear_decrease", C.c_double),
                 ("starting_strength", C.c_double), ("direction", Vec3)]
@@ -119,6 +147,7 @@ class Tuning(C.Structure):
 
 
 assert C.sizeof(TangleState) == 168 and C.sizeof(DomainBox) == 72 and C.sizeof(ExtVel) == 56
+assert C.sizeof(SphTangleState) == 112 and SphTangleState.N.offset == 96
 
 
 def image_shifts(n_images: int) -> list[tuple[int, int, int]]:

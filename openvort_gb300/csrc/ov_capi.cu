@@ -7,6 +7,7 @@
 #include <algorithm>
 
 #include "ov_internal.cuh"
+#include "ov_helium.cuh"
 
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
@@ -738,6 +739,10 @@ static int error_from_word(ov_ctx *c)
     }
     if (w & OV_EW_DEPTH)
         return ov_fail(c, OV_ERR_DEPTH, "two nodes share a cell at tree level %d (error word 0x%x)", OV_MAX_LEVEL, w);
+    if (w & OV_EW_TEMP)
+        return ov_fail(c, OV_ERR_ARG, "a node's temperature is outside the He II model's range (error word 0x%x)", w);
+    if (w & OV_EW_INVERT)
+        return ov_fail(c, OV_ERR_ARG, "spherical inversion of a node at the origin (error word 0x%x)", w);
     return OV_OK;   // sliver drops are counted, not fatal
 }
 
@@ -1081,6 +1086,204 @@ int ov_phase_times(ov_ctx *c, float ms[3])
     OV_CUDA(c, cudaEventSynchronize(c->ph[3]));
     for (int i = 0; i < 3; ++i) OV_CUDA(c, cudaEventElapsedTime(&ms[i], c->ph[i], c->ph[i + 1]));
     return OV_OK;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------- spherical fork
+// The tangle in slots [0, N) (member 0) and its inner image in [N, 2N)
+// (member 1, connections shifted by N): one forest build gives both trees.
+static int sph_run(ov_ctx *c, ov_sph_tangle_state *t, const ov_sph_params *p, double time, bool tangents,
+                   bool vels)
+{
+    (void)time;   // the fork's velocities do not depend on time
+    if (!c || !t || !p || t->N < 0) return OV_ERR_ARG;
+    cudaSetDevice(c->device);
+    if (p->outer_surface)
+        return ov_fail(c, OV_ERR_ARG,
+                       "outer_surface = 1 is not supported (the reference's branch uses a null image tree)");
+    const ov_sph_domain &dom = t->domain_section;
+    if (!(dom.inner_radius > 0 && dom.outer_radius > dom.inner_radius && dom.azimut_angle > 0 &&
+          dom.polar_angle > 0))
+        return ov_fail(c, OV_ERR_ARG, "spherical section: need 0 < inner < outer radius and positive angles");
+    const int N = t->N;
+    if (N > 0 && (!t->vnodes || !t->vels || !t->vs || !t->tangents || !t->normals || !t->connections || !t->status))
+        return OV_ERR_ARG;
+    SphSettings ss;
+    ss.kappa = p->kappa; ss.a0 = p->vortex_width; ss.alpha = p->alpha; ss.alpha_p = p->alpha_p;
+    ss.dl_min = p->dl_min; ss.dl_max = p->dl_max; ss.theta = p->bh_resolution;
+    ss.friction = p->use_mutual_friction; ss.use_temperature = p->use_temperature;
+    ss.q_dot = p->q_dot; ss.t_bath = p->temp_bath; ss.prof_a = 0;
+    if (p->use_temperature) {
+        int terr = 0;
+        ss.prof_a = helium::profile_A(p->q_dot, p->temp_bath, p->kappa, &terr);
+        if (terr) return ov_fail(c, OV_ERR_ARG, "bath temperature %g K outside the He II model's range", p->temp_bath);
+    }
+    SphDomain sd{N, dom.inner_radius, dom.outer_radius, dom.azimut_angle, dom.polar_angle};
+    if (N == 0) return OV_OK;
+    int r;
+    const int slots = 2 * N;
+    if ((r = ensure_capacity(c, slots))) return r;
+    c->uploaded = false;   // the context holds no regular tangle after this call
+    c->tree_built = false;
+    c->host_valid = false;
+    c->n_live = slots;
+    ov_params op;
+    ov_params_default(&op);
+    op.kappa = p->kappa; op.vortex_width = p->vortex_width; op.alpha = p->alpha; op.alpha_p = p->alpha_p;
+    op.use_mutual_friction = p->use_mutual_friction; op.bh_resolution = p->bh_resolution; op.use_bh = 1;
+    op.dl_min = p->dl_min; op.dl_max = p->dl_max;
+    c->params = op;
+    c->mem.assign(2, Member{});
+    for (int m = 0; m < 2; ++m) {
+        c->mem[m].lo = m * N;
+        c->mem[m].n = N;
+        c->mem[m].cap = N;
+        c->mem[m].params = op;
+    }
+    Geometry &g = c->geo;
+    memset(&g, 0, sizeof g);
+    for (int a = 0; a < 3; ++a) { g.lo[a] = 0; g.hi[a] = 1; g.L[a] = 1; }
+    g.sph = 1;
+    g.sph_az = dom.azimut_angle;
+    g.sph_pl = dom.polar_angle;
+    g.sph_seg_max = 5 * p->dl_max;
+    const double A = dom.azimut_angle, P = dom.polar_angle;
+    const double ri = dom.inner_radius, ro = dom.outer_radius;
+    const double lo0[3] = {ri, -A, -P}, hi0[3] = {ro, A, P};
+    const double lo1[3] = {ri * ri / ro, -A, -P}, hi1[3] = {ri, A, P};   // the inner image's section
+    for (int a = 0; a < 3; ++a) {
+        c->sph_lo[0][a] = lo0[a]; c->sph_hi[0][a] = hi0[a];
+        c->sph_lo[1][a] = lo1[a]; c->sph_hi[1][a] = hi1[a];
+    }
+    if ((r = ov_upload_member_tables(c))) return r;
+    // upload: positions, vels, vs, tangents, normals of the tangle (SoA), topology of both members
+    const size_t cap = (size_t)c->cap;
+    if ((r = ensure_stage(c, cap * 3 * sizeof(double) * 5 + cap * 4 * sizeof(int)))) return r;
+    double *h = c->h_stage;
+    int *hi_ = (int *)(h + 15 * cap);
+    const ov_vec3 *src[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
+    double *dd[15] = {c->node.x, c->node.y, c->node.z, c->node.vx, c->node.vy, c->node.vz,
+                      c->node.sx, c->node.sy, c->node.sz, c->node.tx, c->node.ty, c->node.tz,
+                      c->node.nx, c->node.ny, c->node.nz};
+    for (int f = 0; f < 5; ++f) {
+        double *dst = h + 3 * cap * f;
+        for (int a = 0; a < 3; ++a)
+            for (int k = 0; k < N; ++k) dst[a * cap + k] = src[f][k].p[a];
+        for (int a = 0; a < 3; ++a)
+            OV_CUDA(c, cudaMemcpyAsync(dd[3 * f + a], dst + a * cap, (size_t)N * sizeof(double),
+                                       cudaMemcpyHostToDevice, c->stream));
+    }
+    int *hf = hi_, *hr = hi_ + cap, *hs = hi_ + 2 * cap, *hp = hi_ + 3 * cap;
+    for (int k = 0; k < N; ++k) {
+        const int f = t->connections[k].forward, b = t->connections[k].reverse, st = t->status[k].status;
+        if (f < -1 || f >= N || b < -1 || b >= N || st < OV_EMPTY || st > OV_PINNED_SLIP)
+            return ov_fail(c, OV_ERR_TOPOLOGY, "node %d: bad connection or status", k);
+        hf[k] = f; hr[k] = b; hs[k] = st; hp[k] = t->status[k].pin_wall;
+        hf[N + k] = f < 0 ? -1 : f + N;
+        hr[N + k] = b < 0 ? -1 : b + N;
+        hs[N + k] = st;
+        hp[N + k] = t->status[k].pin_wall;
+    }
+    for (size_t k = (size_t)slots; k < cap; ++k) {   // slots past the two members are EMPTY
+        hf[k] = hr[k] = -1;
+        hs[k] = OV_EMPTY;
+        hp[k] = OV_NOT_A_FACE;
+    }
+    int *di[4] = {c->fwd, c->rev, c->status, c->pin};
+    int *hsrc[4] = {hf, hr, hs, hp};
+    for (int a = 0; a < 4; ++a)
+        OV_CUDA(c, cudaMemcpyAsync(di[a], hsrc[a], cap * 4, cudaMemcpyHostToDevice, c->stream));
+    c->last_h2d = (size_t)N * (15 * sizeof(double)) + cap * 16;
+    OV_CUDA(c, cudaMemsetAsync(c->tree.counters, 0, TC_WORDS * 4, c->stream));
+    if (tangents) ov_launch_sph_tangents(c, sd, ss);
+    if (vels) {
+        ov_launch_sph_images(c, sd, ss);
+        for (int attempt = 0;; ++attempt) {
+            if ((r = ov_tree_build(c, c->node, c->stream))) return r;
+            ov_launch_sph_velocities(c, sd, ss);
+            OV_CUDA(c, cudaGetLastError());
+            if ((r = collect_stats(c, true))) return r;
+            if (!(c->stats.error_word & OV_EW_CELLS)) break;
+            if (attempt == 2) return ov_fail(c, OV_ERR_ALLOC, "cell storage could not be sized");
+            int need = 0;
+            OV_CUDA(c, cudaMemcpy(&need, c->tree.counters + TC_NEED, 4, cudaMemcpyDeviceToHost));
+            if ((r = ov_tree_reserve_cells(c, need + need / 4 + 64))) return r;
+            OV_CUDA(c, cudaMemsetAsync(c->tree.counters + TC_ERR, 0, (TC_COUNT - TC_ERR) * 4, c->stream));
+        }
+    } else {
+        OV_CUDA(c, cudaGetLastError());
+        if ((r = collect_stats(c, true))) return r;
+    }
+    if ((r = error_from_word(c))) return r;
+    // download what the reference writes: tangents, normals; vels, vs
+    const int fsel[4] = {tangents ? 3 : -1, tangents ? 4 : -1, vels ? 1 : -1, vels ? 2 : -1};
+    ov_vec3 *out[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
+    for (int q = 0; q < 4; ++q) {
+        const int f = fsel[q];
+        if (f < 0) continue;
+        double *dst = h + 3 * cap * f;
+        for (int a = 0; a < 3; ++a)
+            OV_CUDA(c, cudaMemcpyAsync(dst + a * cap, dd[3 * f + a], (size_t)N * sizeof(double),
+                                       cudaMemcpyDeviceToHost, c->stream));
+    }
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int q = 0; q < 4; ++q) {
+        const int f = fsel[q];
+        if (f < 0) continue;
+        const double *dsrc = h + 3 * cap * f;
+        for (int k = 0; k < N; ++k)
+            for (int a = 0; a < 3; ++a) out[f][k].p[a] = dsrc[a * cap + k];
+    }
+    return OV_OK;
+}
+
+extern "C" {
+
+void ov_sph_params_default(ov_sph_params *p)
+{
+    if (!p) return;
+    memset(p, 0, sizeof *p);
+    p->kappa = 9.97e-4;
+    p->vortex_width = 1e-8;
+    p->alpha = 0.034;
+    p->alpha_p = 1.383e-2;
+    p->use_mutual_friction = 1;
+    p->bh_resolution = 0.4;
+    p->dl_min = 0.5e-3;
+    p->dl_max = 1.5e-3;
+    p->q_dot = 0.03;
+    p->temp_bath = 1.65;
+    p->use_temperature = 1;
+    p->outer_surface = 0;
+}
+
+int ov_sph_update_tangents_normals(ov_ctx *c, ov_sph_tangle_state *t, const ov_sph_params *p)
+{
+    return sph_run(c, t, p, 0.0, true, false);
+}
+
+int ov_sph_update_velocities(ov_ctx *c, ov_sph_tangle_state *t, const ov_sph_params *p, double time)
+{
+    return sph_run(c, t, p, time, false, true);
+}
+
+int ov_sph_update_tangle(ov_ctx *c, ov_sph_tangle_state *t, const ov_sph_params *p, double time)
+{
+    return sph_run(c, t, p, time, true, true);
+}
+
+int ov_sph_helium(double T, double out[6])
+{
+    if (!out) return OV_ERR_ARG;
+    int err = 0;
+    out[0] = helium::superfluid_density(T, &err);
+    out[1] = helium::total_density(T, &err);
+    out[2] = helium::normal_density(T, &err);
+    out[3] = helium::entropy(T, &err);
+    out[4] = helium::friction_alpha(T, &err);
+    out[5] = helium::friction_alpha_p(T, &err);
+    return err ? OV_ERR_ARG : OV_OK;
 }
 
 }  // extern "C"

@@ -19,11 +19,13 @@
 #include <vector>
 
 #include "../../include/openvort_gpu.h"
+#include "../../include/ov_spherical.h"
 
 #define OV_MAX_LEVEL 21                 // 3-bit digits below the root: 63 bits
 #define OV_KEY_OUT (0x8000000000000000ull) // node outside the root box (| wrapped path >> 1)
 #define OV_KEY_EMPTY (0xFFFFFFFFFFFFFFFFull)
 #define OV_MAX_IMAGES 26
+#define OV_SPH_MEMBERS 2                // spherical section: the tangle and its inner image
 
 // device error bits (ov_stats.error_word)
 enum {
@@ -34,7 +36,9 @@ enum {
     OV_EW_NAN = 16,       // non-finite position
     OV_EW_RUN = 32,       // sort fix-up met a run longer than its bound
     OV_EW_CELLS = 64,     // cell storage too small: host grows it and rebuilds
-    OV_EW_BOUNDS = 128    // an index failed a bounds check (access skipped)
+    OV_EW_BOUNDS = 128,   // an index failed a bounds check (access skipped)
+    OV_EW_TEMP = 256,     // spherical fork: a temperature outside the He II model's range
+    OV_EW_INVERT = 512    // spherical fork: inversion of a node at the origin
 };
 
 struct Cell64 {          // 64 bytes, one per cell, pre-order
@@ -118,6 +122,10 @@ struct Geometry {
     int shift[OV_MAX_IMAGES][3];
     int reflect[OV_MAX_IMAGES][3];
     int nreflect[OV_MAX_IMAGES];
+    // spherical section domains (the spherical fork): seg_pwrap by angles
+    int sph;                     // 1: this geometry is a spherical section
+    double sph_az, sph_pl;       // half widths of the azimuth and polar ranges
+    double sph_seg_max;          // 5 dl_max: longer wrapped segments stay out of the moments
 };
 
 struct NodeArrays {              // one tangle (or one RK4 stage) in HBM
@@ -250,6 +258,8 @@ struct ov_ctx {
     // pinned host staging
     double *h_stage = nullptr;
     size_t h_stage_bytes = 0;
+    // spherical sections: (r, az, pl) bounds of each tree member's root cell
+    double sph_lo[OV_SPH_MEMBERS][3] = {}, sph_hi[OV_SPH_MEMBERS][3] = {};
     // per-phase timing of the last evaluation
     bool phase_timing = false;
     cudaEvent_t ph[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -309,6 +319,20 @@ int ov_rec_wait(ov_ctx *c);
 void ov_launch_euler(ov_ctx *c, const NodeArrays &src, const double *vx, const double *vy,
                      const double *vz, double dt, NodeArrays &dst, cudaStream_t s);
 void ov_launch_rk4_combine(ov_ctx *c, double dt, cudaStream_t s);
+// spherical fork (ov_velocity.cu): the tangle in slots [0, n), its inner
+// image in [n, 2n)
+struct SphDomain {
+    int n;
+    double ri, ro, az, pl;       // radii, angular half widths
+};
+struct SphSettings {
+    double kappa, a0, alpha, alpha_p, dl_min, dl_max, theta;
+    int friction, use_temperature;
+    double q_dot, t_bath, prof_a;
+};
+void ov_launch_sph_tangents(ov_ctx *c, const SphDomain &d, const SphSettings &p);
+void ov_launch_sph_images(ov_ctx *c, const SphDomain &d, const SphSettings &p);
+void ov_launch_sph_velocities(ov_ctx *c, const SphDomain &d, const SphSettings &p);
 void ov_launch_periodic_wrap(ov_ctx *c, cudaStream_t s);
 
 // ------------------------------------------------------------ device helpers
@@ -379,6 +403,81 @@ __device__ __forceinline__ void child_box_dev(const double b[3], const double t[
 __device__ __forceinline__ bool in_closed_box_dev(const double b[3], const double t[3], const double p[3])
 {
     return p[0] >= b[0] && p[0] <= t[0] && p[1] >= b[1] && p[1] <= t[1] && p[2] >= b[2] && p[2] <= t[2];
+}
+
+// ------------------------------------------- spherical section helpers
+// vec3_math.c of the spherical fork (240-282): radius, azimuth (elevation
+// from the x-y plane), polar angle (in the x-y plane), and back.
+__device__ __forceinline__ double sph_radius(const double v[3])
+{
+    return __dsqrt_rn(rn_add(rn_add(rn_mul(v[0], v[0]), rn_mul(v[1], v[1])), rn_mul(v[2], v[2])));
+}
+__device__ __forceinline__ double sph_azimut(const double v[3])
+{
+    return atan2(v[2], __dsqrt_rn(rn_add(rn_mul(v[1], v[1]), rn_mul(v[0], v[0]))));
+}
+__device__ __forceinline__ double sph_polar(const double v[3])
+{
+    if (v[0] == 0 && v[1] == 0) return 0.0;
+    return atan2(v[1], v[0]);
+}
+__device__ __forceinline__ void sph_to_vec(double rad, double az, double pl, double out[3])
+{
+    const double ca = cos(az);
+    out[0] = rn_mul(rn_mul(rad, ca), cos(pl));
+    out[1] = rn_mul(rn_mul(rad, ca), sin(pl));
+    out[2] = rn_mul(rad, sin(az));
+}
+// spherical_inversion: radius R^2 / r at the same angles (false for r == 0)
+__device__ __forceinline__ bool sph_invert(const double v[3], double R, double out[3])
+{
+    const double r = sph_radius(v);
+    if (r == 0) return false;
+    sph_to_vec(rn_div(rn_mul(R, R), r), sph_azimut(v), sph_polar(v), out);
+    return true;
+}
+// shifted(r, d_az, d_pl) of the spherical fork (tangle.c:622-629)
+__device__ __forceinline__ void sph_rotate(const double v[3], double d_az, double d_pl, double out[3])
+{
+    sph_to_vec(sph_radius(v), rn_add(sph_azimut(v), d_az), rn_add(sph_polar(v), d_pl), out);
+}
+// seg_pwrap of the spherical fork (boundaries.c:36-72): r2's angles moved
+// by whole periods (twice the half widths) toward r1's, then r2 rebuilt
+// from its radius and those angles.
+__device__ __forceinline__ void sph_pwrap(const Geometry &g, const double r1[3], double r2[3])
+{
+    const double A = g.sph_az, P = g.sph_pl;
+    const double a1 = sph_azimut(r1), p1 = sph_polar(r1);
+    double a2 = sph_azimut(r2), p2 = sph_polar(r2);
+    const double A2 = rn_mul(2.0, A), P2 = rn_mul(2.0, P);
+    int guard = 0;
+    while (rn_sub(a2, a1) > A && guard++ < 64) a2 = rn_sub(a2, A2);
+    while (rn_sub(a2, a1) < -A && guard++ < 128) a2 = rn_add(a2, A2);
+    guard = 0;
+    while (rn_sub(p2, p1) > P && guard++ < 64) p2 = rn_sub(p2, P2);
+    while (rn_sub(p2, p1) < -P && guard++ < 128) p2 = rn_add(p2, P2);
+    sph_to_vec(sph_radius(r2), a2, p2, r2);
+}
+// make_child_box of the spherical fork (octree.c:183-262) on (r, az, pl)
+// bounds: child idx = 4 (upper azimuth) + 2 (upper polar) + (lower radius).
+__device__ __forceinline__ void sph_child_box(const double b[3], const double t[3], int idx, double cb[3],
+                                              double ct[3])
+{
+    const double mr = rn_div(rn_add(t[0], b[0]), 2.0), ma = rn_div(rn_add(t[1], b[1]), 2.0),
+                 mp = rn_div(rn_add(t[2], b[2]), 2.0);
+    if (idx & 1) { cb[0] = b[0]; ct[0] = mr; } else { cb[0] = mr; ct[0] = t[0]; }
+    if (idx & 4) { cb[1] = ma; ct[1] = t[1]; } else { cb[1] = b[1]; ct[1] = ma; }
+    if (idx & 2) { cb[2] = mp; ct[2] = t[2]; } else { cb[2] = b[2]; ct[2] = mp; }
+}
+// Lm of a spherical cell (octree.c:344-348 of the fork): the largest of the
+// radial depth and the two chords at the outer radius.
+__device__ __forceinline__ double sph_box_lm(const double b[3], const double t[3])
+{
+    const double rd = rn_sub(t[0], b[0]);
+    const double az = rn_mul(rn_mul(t[0], 2.0), fabs(sin(rn_div(rn_sub(t[1], b[1]), 2.0))));
+    const double pl = rn_mul(rn_mul(rn_mul(t[0], 2.0), fabs(sin(rn_div(rn_sub(t[2], b[2]), 2.0)))),
+                             fabs(cos(rn_div(rn_add(t[1], b[1]), 2.0))));
+    return rd > az ? (rd > pl ? rd : pl) : (az > pl ? az : pl);
 }
 
 // Largest side of a box, the reference's ternary (octree.c:302-306).

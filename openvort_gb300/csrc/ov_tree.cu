@@ -37,6 +37,9 @@ struct KeyGeom {
     int levels;        // levels the key holds
     uint64_t lvmask;   // the levels' bits in the path field
     int nt;            // members
+    // spherical sections: per member (r, az, pl) bounds of the root cell
+    double sb[OV_SPH_MEMBERS][3], st[OV_SPH_MEMBERS][3];
+    int sph_root;      // the root cells' Lm from those bounds
 };
 
 // bit offset of the level-`lev` digit
@@ -76,6 +79,27 @@ __device__ __forceinline__ uint64_t exact_key(const double p[3], const KeyGeom &
     return key;
 }
 
+// Path of a point u = (r, az, pl) inside member m's spherical root cell, by
+// the fork's first-match descent (octree.c:126-137 with its make_child_box):
+// ties go to the outer radial half and the lower angular halves.
+__device__ __forceinline__ uint64_t sph_key(const double u[3], const KeyGeom &g, int m)
+{
+    double b[3] = {g.sb[m][0], g.sb[m][1], g.sb[m][2]}, t[3] = {g.st[m][0], g.st[m][1], g.st[m][2]};
+    uint64_t key = 0;
+    for (int lev = 1; lev <= g.levels; ++lev) {
+        const double mr = rn_div(rn_add(t[0], b[0]), 2.0), ma = rn_div(rn_add(t[1], b[1]), 2.0),
+                     mp = rn_div(rn_add(t[2], b[2]), 2.0);
+        const int rl = u[0] >= mr ? 0 : 1, au = u[1] <= ma ? 0 : 1, pu = u[2] <= mp ? 0 : 1;
+        const int idx = 4 * au + 2 * pu + rl;
+        double cb[3], ct[3];
+        sph_child_box(b, t, idx, cb, ct);
+        for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
+        key |= (uint64_t)idx << (63 - 3 * lev);
+    }
+    return key;
+}
+
+template <bool SPH>
 __global__ void k_keys(const int *__restrict__ status, const double *__restrict__ x,
                        const double *__restrict__ y, const double *__restrict__ z, const int *__restrict__ tid,
                        int cap, KeyGeom g, uint64_t *__restrict__ keys, int *__restrict__ order,
@@ -87,7 +111,15 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
     double p[3] = {0, 0, 0};
     if (live) { p[0] = x[i]; p[1] = y[i]; p[2] = z[i]; }
     int m = (live && tid) ? tid[i] : 0;
-    bool inside = live && in_closed_box_dev(g.lo, g.hi, p);
+    double u[3] = {0, 0, 0};   // spherical sections: (r, az, pl)
+    bool inside;
+    if (SPH) {
+        if (m < 0 || m >= OV_SPH_MEMBERS) m = 0;
+        if (live) { u[0] = sph_radius(p); u[1] = sph_azimut(p); u[2] = sph_polar(p); }
+        inside = live && in_closed_box_dev(g.sb[m], g.st[m], u);
+    } else {
+        inside = live && in_closed_box_dev(g.lo, g.hi, p);
+    }
     bool bad = live && !(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]));
     // one atomic per warp for each counter, one per member present in the warp
     unsigned b_live = __ballot_sync(0xffffffffu, live), b_in = __ballot_sync(0xffffffffu, inside);
@@ -106,6 +138,19 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
     order[i] = i;
     if (!live) { keys[i] = OV_KEY_EMPTY; return; }
     const uint64_t prefix = g.tb ? (uint64_t)m << (64 - g.tb) : 0;
+    if (SPH) {
+        // outside the member's section: root only, ordered by the path of
+        // its angles and radius clamped into the section
+        double v[3];
+        for (int a = 0; a < 3; ++a) {
+            v[a] = fmin(fmax(u[a], g.sb[m][a]), g.st[m][a]);
+            if (!(v[a] >= g.sb[m][a])) v[a] = g.sb[m][a];   // non-finite input
+        }
+        const uint64_t path = sph_key(v, g, m);
+        if (!inside) keys[i] = prefix | (1ull << (63 - g.tb)) | (path >> (g.tb + 1));
+        else keys[i] = prefix | ((path >> g.tb) & g.lvmask);
+        return;
+    }
     if (!inside) {
         // root-only member (octree.c:116-127).  The rest of the key orders
         // it among the other root-only nodes by the cell path of its
@@ -294,6 +339,7 @@ __device__ __forceinline__ int lower_prefix(const uint64_t *keys, int lo, int hi
     return lo;
 }
 
+template <bool SPH>
 __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict__ cpl,
                         const int *__restrict__ cell_off, int *counters, const int *__restrict__ tt, KeyGeom g,
                         int cap, Cell64 *__restrict__ cells, int *__restrict__ parent, int *__restrict__ nchild,
@@ -322,22 +368,29 @@ __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict
     int L = min(max(cp, cn) + 1, g.levels);
     const int base = cell_off[s] + (loc == 0);
     // exact box of the first cell starting here, walked from the root
-    double b[3] = {g.lo[0], g.lo[1], g.lo[2]}, t[3] = {g.hi[0], g.hi[1], g.hi[2]};
+    double b[3], t[3];
+    const int mem = key_member(g, key) < OV_SPH_MEMBERS ? key_member(g, key) : 0;
+    for (int a = 0; a < 3; ++a) {
+        b[a] = SPH ? g.sb[mem][a] : g.lo[a];
+        t[a] = SPH ? g.st[mem][a] : g.hi[a];
+    }
     for (int lev = 1; lev <= cp; ++lev) {
         double cb[3], ct[3];
-        child_box_dev(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
+        if (SPH) sph_child_box(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
+        else child_box_dev(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
         for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
     }
     for (int lev = cp + 1; lev <= L; ++lev) {
         int ci = base + (lev - cp - 1);
         double cb[3], ct[3];
-        child_box_dev(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
+        if (SPH) sph_child_box(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
+        else child_box_dev(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
         for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
         int sh = dsh(g, lev);
         int e = (lev < L) ? upper_prefix(keys, s + 1, end, sh, key >> sh) - 1 : s;
         if (lev == g.levels) e = upper_prefix(keys, s + 1, end, sh, key >> sh) - 1;
         Cell64 cell;
-        cell.lm = box_lm(b, t);
+        cell.lm = SPH ? sph_box_lm(b, t) : box_lm(b, t);
         cell.count = e - s + 1;
         cell.next = cell_off[e + 1];   // the member's end of cells when e + 1 == end
         cell.cx = cell.cy = cell.cz = cell.qx = cell.qy = cell.qz = 0;
@@ -365,8 +418,11 @@ __device__ __forceinline__ void node_moment(int id, const double *x, const doubl
     int f = fwd[id];
     if (f > -1) {
         double r2[3] = {x[f], y[f], z[f]};
-        pwrap_dev(geo, p, r2);
+        if (geo.sph) sph_pwrap(geo, p, r2);
+        else pwrap_dev(geo, p, r2);
         out[3] = rn_sub(r2[0], p[0]); out[4] = rn_sub(r2[1], p[1]); out[5] = rn_sub(r2[2], p[2]);
+        // the spherical fork leaves segments longer than 5 dl_max out (octree.c:316-322)
+        if (geo.sph && len3_ref(out[3], out[4], out[5]) > geo.sph_seg_max) out[3] = out[4] = out[5] = 0;
     } else {
         out[3] = out[4] = out[5] = 0;
     }
@@ -485,7 +541,8 @@ __global__ void k_root(const int *__restrict__ order, const int *__restrict__ ce
     double inv = 1.0 / (double)nne;
     r.cx = rn_mul(sum[0], inv); r.cy = rn_mul(sum[1], inv); r.cz = rn_mul(sum[2], inv);
     r.qx = sum[3]; r.qy = sum[4]; r.qz = sum[5];
-    r.lm = box_lm(g.lo, g.hi);
+    const int mem = blockIdx.x < OV_SPH_MEMBERS ? blockIdx.x : 0;
+    r.lm = g.sph_root ? sph_box_lm(g.sb[mem], g.st[mem]) : box_lm(g.lo, g.hi);
     r.next = end;
     r.count = nne;
     cells[root] = r;
@@ -586,6 +643,12 @@ static KeyGeom key_geom(const ov_ctx *c)
     g.levels = c->key_levels;
     g.lvmask = ((g.levels >= 21 ? ~0ull >> 1 : (1ull << (3 * g.levels)) - 1)) << (63 - g.tb - 3 * g.levels);
     g.nt = (int)c->mem.size();
+    g.sph_root = c->geo.sph;
+    for (int m = 0; m < OV_SPH_MEMBERS; ++m)
+        for (int a = 0; a < 3; ++a) {
+            g.sb[m][a] = c->sph_lo[m][a];
+            g.st[m][a] = c->sph_hi[m][a];
+        }
     return g;
 }
 
@@ -605,8 +668,12 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     OV_CUDA(c, cudaMemsetAsync(t.tt, 0, (size_t)nt * TT_WORDS * 4, s));
     OV_CUDA(c, cudaMemsetAsync(t.nchild, 0, (size_t)t.cap_cells * 4, s));
     int nb = (cap + 255) / 256;
-    k_keys<<<nb, 256, 0, s>>>(c->status, na.x, na.y, na.z, nt > 1 ? c->d_tid : nullptr, cap, g, t.keys, t.order,
-                              t.counters, t.tt);
+    if (c->geo.sph)
+        k_keys<true><<<nb, 256, 0, s>>>(c->status, na.x, na.y, na.z, nt > 1 ? c->d_tid : nullptr, cap, g, t.keys,
+                                        t.order, t.counters, t.tt);
+    else
+        k_keys<false><<<nb, 256, 0, s>>>(c->status, na.x, na.y, na.z, nt > 1 ? c->d_tid : nullptr, cap, g, t.keys,
+                                         t.order, t.counters, t.tt);
     k_layout<<<1, 32, 0, s>>>(t.tt, nt, c->d_qorder, t.counters);
     c->launches += 2;
     ov_sort_keys(c, t, cap, s);
@@ -614,8 +681,12 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     k_target_order<<<nb, 256, 0, s>>>(t.keys, t.order, cap, t.counters, t.tt, g, t.torder);
     c->launches += 2;
     ov_scan_exclusive(c, t.ncell_at, t.cell_off, cap, t.counters + TC_NNE, 0, t.scan_tmp, s);
-    k_cells<<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.parent, t.nchild,
-                               t.arrive, t.cap_cells);
+    if (c->geo.sph)
+        k_cells<true><<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.parent,
+                                         t.nchild, t.arrive, t.cap_cells);
+    else
+        k_cells<false><<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.parent,
+                                          t.nchild, t.arrive, t.cap_cells);
     k_moments<<<nb, 256, 0, s>>>(t.keys, t.order, t.cpl, t.cell_off, t.counters, t.tt, g, cap, na.x, na.y, na.z,
                                  c->fwd, c->geo, t.cells, t.parent, t.nchild, t.arrive, t.csum, t.cap_cells);
     k_root<<<nt, 256, 0, s>>>(t.order, t.cell_off, t.counters, t.tt, na.x, na.y, na.z, c->fwd, c->geo, g, t.cells,

@@ -1865,3 +1865,314 @@ extern "C" int ov_direct_velocities_noalloc(const ov_params *p, const ov_domain_
     k_direct_noalloc_finish<<<(n_nodes + 127) / 128, 128, 0, s>>>(a, d_nodes, n_nodes, n_slots, sums, d_vels, d_vs);
     return cudaGetLastError() == cudaSuccess ? OV_OK : OV_ERR_CUDA;
 }
+
+// ------------------------------------------------ spherical section domains
+//
+// The spherical fork (src_spherical/ of OpenVort): the domain is a section of
+// a spherical shell, inner radius ri, outer ro, azimuth and polar angle in
+// (-A, A) and (-P, P); the section repeats by rotations of 2A and 2P, and the
+// inner surface is a wall made by the spherical inversion of the tangle
+// through ri (its own tree, subtracted).  The slot pool holds the tangle in
+// member 0 and its inner image in member 1, and one forest build gives both
+// trees.  Every node walks the tangle's tree at its position and at its 8
+// rotated copies (results rotated back), then the image's tree at the same 9
+// points, all in FP64 on the reference's decisions.  The angles go through
+// the device's atan2 / sin / cos, whose last bit may differ from the host
+// libm's: velocities agree to rounding, a decision exactly on a threshold
+// could go the other way.
+#include "ov_helium.cuh"
+
+namespace {
+
+struct SphArgs {
+    VelArgs v;                 // tree, positions, topology (slots [0, n) the tangle)
+    int n;                     // slots of the tangle
+    double ri, ro;             // shell radii
+    double d_az, d_pl;         // the section's full angular widths (rotation steps)
+    double kappa, a0, alpha, alpha_p, dl_min, dl_max;
+    int friction, use_temperature;
+    double q_dot, t_bath, prof_a;   // temperature profile (use_temperature)
+};
+
+// step_node of the fork (tangle.c:155-201): a pinned end reverses the walk
+// and inverts the result through its surface, innermost first.
+__device__ bool sph_step_node(const SphArgs &s, int i, int where, double out[3])
+{
+    const VelArgs &a = s.v;
+    int surf[8];
+    int nw = 0, cur = i, w = where;
+    for (int guard = 0; w != 0; ++guard) {
+        if (guard > 16 || cur < 0 || cur >= s.n) return false;
+        const int st = a.status[cur];
+        if (st == OV_FREE) {
+            cur = w > 0 ? a.fwd[cur] : a.rev[cur];
+            w += w > 0 ? -1 : 1;
+        } else if (st == OV_PINNED || st == OV_PINNED_SLIP) {
+            const int nb = w > 0 ? a.fwd[cur] : a.rev[cur];
+            if (nb >= 0) {
+                cur = nb;
+                w += w > 0 ? -1 : 1;
+            } else {
+                const int f = a.pin[cur];
+                if (nw >= 8 || (f != 0 && f != 1)) return false;   // not on a surface
+                surf[nw++] = f;
+                w = -w;
+            }
+        } else {
+            return false;
+        }
+    }
+    if (cur < 0 || cur >= s.n || a.status[cur] == OV_EMPTY) return false;
+    out[0] = a.x[cur]; out[1] = a.y[cur]; out[2] = a.z[cur];
+    for (int m = nw - 1; m >= 0; --m) {
+        double q[3];
+        if (!sph_invert(out, surf[m] == 0 ? s.ri : s.ro, q)) return false;
+        out[0] = q[0]; out[1] = q[1]; out[2] = q[2];
+    }
+    return true;
+}
+
+__device__ __forceinline__ double sph_wrapped_len(const Geometry &g, const double r1[3], const double r2in[3])
+{
+    double r2[3] = {r2in[0], r2in[1], r2in[2]};
+    sph_pwrap(g, r1, r2);
+    return len3_ref(rn_sub(r1[0], r2[0]), rn_sub(r1[1], r2[1]), rn_sub(r1[2], r2[2]));
+}
+
+// update_tangent_normal of the fork (tangle.c:483-560): the five-point
+// finite differences of the flat geometry on angularly wrapped segments.
+__global__ void k_sph_tangents(SphArgs s, int *counters)
+{
+    const VelArgs &a = s.v;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= s.n || a.status[k] == OV_EMPTY) return;
+    const Geometry &g = a.geo;
+    double s0[3] = {a.x[k], a.y[k], a.z[k]}, s1[3], s2[3], sm1[3], sm2[3];
+    bool ok = sph_step_node(s, k, 1, s1) & sph_step_node(s, k, 2, s2) & sph_step_node(s, k, -1, sm1) &
+              sph_step_node(s, k, -2, sm2);
+    if (!ok) {
+        atomicOr(&counters[TC_ERR], OV_EW_WALK);
+        return;
+    }
+    double w2[3] = {s2[0], s2[1], s2[2]}, w1[3] = {s1[0], s1[1], s1[2]};
+    double wm1[3] = {sm1[0], sm1[1], sm1[2]}, wm2[3] = {sm2[0], sm2[1], sm2[2]};
+    sph_pwrap(g, s0, w2);
+    sph_pwrap(g, s0, w1);
+    sph_pwrap(g, s0, wm1);
+    sph_pwrap(g, s0, wm2);
+    double d1 = len3_ref(rn_sub(s0[0], w1[0]), rn_sub(s0[1], w1[1]), rn_sub(s0[2], w1[2]));
+    double d2 = rn_add(d1, sph_wrapped_len(g, s1, s2));
+    double dm1 = len3_ref(rn_sub(s0[0], wm1[0]), rn_sub(s0[1], wm1[1]), rn_sub(s0[2], wm1[2]));
+    double dm2 = rn_add(dm1, sph_wrapped_len(g, sm1, sm2));
+    double den[4] = {
+        rn_mul(rn_mul(rn_mul(d2, rn_sub(d2, d1)), rn_add(dm1, d2)), rn_add(dm2, d2)),
+        rn_mul(rn_mul(rn_mul(d1, rn_sub(d2, d1)), rn_add(dm1, d1)), rn_add(dm2, d1)),
+        rn_mul(rn_mul(rn_mul(dm1, rn_add(dm1, d1)), rn_add(dm1, d2)), rn_sub(dm2, dm1)),
+        rn_mul(rn_mul(rn_mul(dm2, rn_add(dm2, d1)), rn_add(dm2, d2)), rn_sub(dm2, dm1))};
+    double c1[4] = {rn_mul(rn_mul(-d1, dm1), dm2), rn_mul(rn_mul(d2, dm1), dm2), rn_mul(rn_mul(-d1, d2), dm2),
+                    rn_mul(rn_mul(d1, d2), dm1)};
+    double c2[4] = {
+        rn_mul(2.0, rn_sub(rn_mul(rn_sub(dm1, d1), dm2), rn_mul(d1, dm1))),
+        rn_mul(-2.0, rn_sub(rn_mul(rn_sub(dm1, d2), dm2), rn_mul(d2, dm1))),
+        rn_mul(2.0, rn_sub(rn_mul(rn_add(d2, d1), dm2), rn_mul(d1, d2))),
+        rn_mul(-2.0, rn_sub(rn_mul(rn_add(d2, d1), dm1), rn_mul(d1, d2)))};
+    double ds[4][3];
+    for (int ax = 0; ax < 3; ++ax) {
+        ds[0][ax] = rn_sub(w2[ax], s0[ax]);
+        ds[1][ax] = rn_sub(w1[ax], s0[ax]);
+        ds[2][ax] = rn_sub(wm1[ax], s0[ax]);
+        ds[3][ax] = rn_sub(wm2[ax], s0[ax]);
+    }
+    double *T[3] = {(double *)a.tx, (double *)a.ty, (double *)a.tz};
+    double *Nn[3] = {(double *)a.nx, (double *)a.ny, (double *)a.nz};
+    for (int ax = 0; ax < 3; ++ax) {
+        double tt = 0, nn = 0;
+        for (int z = 0; z < 4; ++z) {
+            tt = rn_add(tt, rn_mul(rn_div(c1[z], den[z]), ds[z][ax]));
+            nn = rn_add(nn, rn_mul(rn_div(c2[z], den[z]), ds[z][ax]));
+        }
+        T[ax][k] = tt;
+        Nn[ax][k] = nn;
+    }
+}
+
+// The inner image (update_velocities of the fork, tangle.c:956-976):
+// slot n + k holds node k inverted through the inner surface.
+__global__ void k_sph_images(SphArgs s, double *x, double *y, double *z, int *counters)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= s.n || s.v.status[k] == OV_EMPTY) return;
+    const double p[3] = {x[k], y[k], z[k]};
+    double q[3];
+    if (!sph_invert(p, s.ri, q)) {
+        atomicOr(&counters[TC_ERR], OV_EW_INVERT);
+        q[0] = q[1] = q[2] = 0;
+    }
+    x[s.n + k] = q[0]; y[s.n + k] = q[1]; z[s.n + k] = q[2];
+}
+
+__device__ __forceinline__ void sph_normalize(const double p[3], double out[3])
+{
+    if (p[0] == 0 && p[1] == 0 && p[2] == 0) { out[0] = out[1] = out[2] = 0; return; }
+    const double m = rn_div(1.0, len3_ref(p[0], p[1], p[2]));
+    for (int ax = 0; ax < 3; ++ax) out[ax] = rn_mul(p[ax], m);
+}
+
+// update_velocity of the fork (tangle.c:638-865, outer surface open): one
+// warp per 32 targets of the tangle's traversal order.
+__global__ void __launch_bounds__(128) k_vel_sph(SphArgs s)
+{
+    const VelArgs &a = s.v;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nne = a.tt[TT_NNE];   // member 0: the tangle, first in sorted order
+    if (warp * 32 >= nne) return;
+    const int loc = warp * 32 + lane;
+    bool valid = loc < nne;
+    int id = valid ? a.order[loc] : 0;
+    if (valid && (id < 0 || id >= s.n)) { bad_index(a, 9, id); valid = false; id = 0; }
+    const int st = valid ? a.status[id] : OV_EMPTY;
+    const bool part = valid && st != OV_PINNED && st != OV_EMPTY;
+    double p[3] = {0, 0, 0};
+    if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
+    unsigned long long visits = 0, accepts = 0, steps = 0;
+    bool overflow = false;
+    double own[3] = {0, 0, 0}, tot[3] = {0, 0, 0};
+    for (int m = 0; m < 2; ++m) {
+        const int root = a.tt[m * TT_WORDS + TT_ROOT], end = a.tt[m * TT_WORDS + TT_END];
+        const bool go = part && end > root;
+        double v[3];
+        bh_query64(a, p, go, root, end, v, visits, accepts, steps, overflow);
+        if (m == 0) { own[0] = v[0]; own[1] = v[1]; own[2] = v[2]; }
+        else for (int ax = 0; ax < 3; ++ax) tot[ax] = rn_sub(tot[ax], v[ax]);
+        // rotations of the section (tangle.c:677-719): +-az, +-pl, then the corners
+        for (int j = 0; j < 8; ++j) {
+            const double ua = j < 2 ? (j == 0 ? 1.0 : -1.0) : (j < 4 ? 0.0 : ((j & 1) ? -1.0 : 1.0));
+            const double up = j < 2 ? 0.0 : (j < 4 ? (j == 2 ? 1.0 : -1.0) : (j < 6 ? 1.0 : -1.0));
+            const double da = rn_mul(ua, s.d_az), dp = rn_mul(up, s.d_pl);
+            double q[3], w[3];
+            sph_rotate(p, da, dp, q);
+            bh_query64(a, q, go, root, end, v, visits, accepts, steps, overflow);
+            sph_rotate(v, -da, -dp, w);
+            for (int ax = 0; ax < 3; ++ax) tot[ax] = m == 0 ? rn_add(tot[ax], w[ax]) : rn_sub(tot[ax], w[ax]);
+        }
+    }
+    if (a.stat) {
+        for (int o = 16; o > 0; o >>= 1) {
+            visits += __shfl_xor_sync(0xffffffffu, visits, o);
+            accepts += __shfl_xor_sync(0xffffffffu, accepts, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&a.stat[ST_VISITS], visits);
+            atomicAdd(&a.stat[ST_ACCEPTS], accepts);
+            atomicAdd(&a.stat[ST_STEPS], steps);
+        }
+    }
+    if (overflow) atomicOr((int *)&a.counters[TC_ERR], OV_EW_ITER);
+    if (!valid || st == OV_EMPTY) return;
+    if (st == OV_PINNED) {   // the node rests; its velocity is left as it was
+        a.sx[id] = a.sy[id] = a.sz[id] = 0;
+        return;
+    }
+    // LIA with the fork's limits on the neighbour distances (tangle.c:581-611)
+    double nx_[3], pv[3];
+    if (!(sph_step_node(s, id, 1, nx_) && sph_step_node(s, id, -1, pv))) {
+        atomicOr((int *)&a.counters[TC_ERR], OV_EW_WALK);
+        return;
+    }
+    double l_next = sph_wrapped_len(a.geo, p, nx_);
+    double l_prev = sph_wrapped_len(a.geo, pv, p);
+    const double hi = rn_mul(4.0, s.dl_max), lo = rn_div(s.dl_min, 4.0);
+    if (l_next > hi) l_next = hi;
+    if (l_prev > hi) l_prev = hi;
+    if (l_next < lo) l_next = lo;
+    if (l_prev < lo) l_prev = lo;
+    const double f = rn_div(
+        rn_div(rn_mul(s.kappa, log(rn_div(rn_div(rn_mul(2.0, sqrt(rn_mul(l_next, l_prev))), sqrt(M_E)), s.a0))), 4.0),
+        M_PI);
+    const double tg[3] = {a.tx[id], a.ty[id], a.tz[id]}, nm[3] = {a.nx[id], a.ny[id], a.nz[id]};
+    double vs[3] = {rn_mul(rn_sub(rn_mul(tg[1], nm[2]), rn_mul(tg[2], nm[1])), f),
+                    rn_mul(rn_sub(rn_mul(tg[2], nm[0]), rn_mul(tg[0], nm[2])), f),
+                    rn_mul(rn_sub(rn_mul(tg[0], nm[1]), rn_mul(tg[1], nm[0])), f)};
+    int terr = 0;
+    double T = 0, rhat[3] = {0, 0, 0};
+    const double rad = sph_radius(p);
+    if (s.use_temperature) {
+        T = helium::temperature(rad, s.t_bath, s.prof_a);
+        sph_normalize(p, rhat);
+        const double vsr = helium::vs_radial(rad, T, s.q_dot, &terr);
+        for (int ax = 0; ax < 3; ++ax) vs[ax] = rn_add(vs[ax], rn_mul(rhat[ax], vsr));
+    }
+    for (int ax = 0; ax < 3; ++ax) vs[ax] = rn_add(vs[ax], own[ax]);
+    for (int ax = 0; ax < 3; ++ax) vs[ax] = rn_add(vs[ax], tot[ax]);
+    double vel[3] = {vs[0], vs[1], vs[2]};
+    if (s.friction) {
+        double dv[3] = {0, 0, 0}, al = s.alpha, alp = s.alpha_p;
+        if (s.use_temperature) {
+            const double vnr = helium::vn_radial(rad, T, s.q_dot, &terr);
+            for (int ax = 0; ax < 3; ++ax) dv[ax] = rn_mul(rhat[ax], vnr);
+            al = helium::friction_alpha(T, &terr);
+            alp = helium::friction_alpha_p(T, &terr);
+        }
+        for (int ax = 0; ax < 3; ++ax) dv[ax] = rn_sub(dv[ax], vs[ax]);
+        double c1[3] = {rn_sub(rn_mul(tg[1], dv[2]), rn_mul(tg[2], dv[1])), rn_sub(rn_mul(tg[2], dv[0]), rn_mul(tg[0], dv[2])),
+                        rn_sub(rn_mul(tg[0], dv[1]), rn_mul(tg[1], dv[0]))};
+        for (int ax = 0; ax < 3; ++ax) vel[ax] = rn_add(vel[ax], rn_mul(c1[ax], al));
+        double c2[3] = {rn_sub(rn_mul(tg[1], c1[2]), rn_mul(tg[2], c1[1])), rn_sub(rn_mul(tg[2], c1[0]), rn_mul(tg[0], c1[2])),
+                        rn_sub(rn_mul(tg[0], c1[1]), rn_mul(tg[1], c1[0]))};
+        const double mm = -alp;
+        for (int ax = 0; ax < 3; ++ax) vel[ax] = rn_add(vel[ax], rn_mul(c2[ax], mm));
+    }
+    if (st == OV_PINNED_SLIP) {
+        // surface_normal (boundaries.c:13-27 of the fork): outward from the inner surface
+        double n[3];
+        sph_normalize(p, n);
+        if (a.pin[id] != 0) for (int ax = 0; ax < 3; ++ax) n[ax] = rn_mul(n[ax], -1.0);
+        const double nv = dot3_ref(n[0], n[1], n[2], vel[0], vel[1], vel[2]);
+        for (int ax = 0; ax < 3; ++ax) vel[ax] = rn_sub(vel[ax], rn_mul(n[ax], nv));
+    }
+    if (terr) atomicOr((int *)&a.counters[TC_ERR], OV_EW_TEMP);
+    a.sx[id] = vs[0]; a.sy[id] = vs[1]; a.sz[id] = vs[2];
+    a.vx[id] = vel[0]; a.vy[id] = vel[1]; a.vz[id] = vel[2];
+}
+
+SphArgs make_sph_args(ov_ctx *c, const SphDomain &d, const SphSettings &p)
+{
+    SphArgs s;
+    s.v = make_args(c, c->node, 0.0, ov_stat_ptr(c));
+    s.v.tid = nullptr; s.v.tprm = nullptr; s.v.mrange = nullptr; s.v.qorder = nullptr;
+    s.n = d.n;
+    s.ri = d.ri; s.ro = d.ro;
+    s.d_az = 2 * d.az; s.d_pl = 2 * d.pl;
+    s.kappa = p.kappa; s.a0 = p.a0; s.alpha = p.alpha; s.alpha_p = p.alpha_p;
+    s.dl_min = p.dl_min; s.dl_max = p.dl_max;
+    s.friction = p.friction; s.use_temperature = p.use_temperature;
+    s.q_dot = p.q_dot; s.t_bath = p.t_bath; s.prof_a = p.prof_a;
+    s.v.prm.theta = p.theta;
+    s.v.f4pi = p.kappa / 4 / M_PI;
+    return s;
+}
+
+}  // namespace
+
+void ov_launch_sph_tangents(ov_ctx *c, const SphDomain &d, const SphSettings &p)
+{
+    SphArgs s = make_sph_args(c, d, p);
+    k_sph_tangents<<<(d.n + 255) / 256, 256, 0, c->stream>>>(s, c->tree.counters);
+    c->launches++;
+}
+
+void ov_launch_sph_images(ov_ctx *c, const SphDomain &d, const SphSettings &p)
+{
+    SphArgs s = make_sph_args(c, d, p);
+    k_sph_images<<<(d.n + 255) / 256, 256, 0, c->stream>>>(s, c->node.x, c->node.y, c->node.z, c->tree.counters);
+    c->launches++;
+}
+
+void ov_launch_sph_velocities(ov_ctx *c, const SphDomain &d, const SphSettings &p)
+{
+    SphArgs s = make_sph_args(c, d, p);
+    const int warps = (d.n + 31) / 32;
+    k_vel_sph<<<(warps + 3) / 4, 128, 0, c->stream>>>(s);
+    c->launches++;
+}

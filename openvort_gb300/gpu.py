@@ -101,6 +101,12 @@ def load(path: str | None = None):
         "ov_get_injection": (C.c_int, [P, C.c_int, C.POINTER(abi.Injection)]),
         "ov_inject_vortices": (C.c_int, [P, C.c_double]),
         "ov_erand48": (C.c_double, [C.POINTER(C.c_ushort)]),
+        "ov_sph_params_default": (None, [C.POINTER(abi.SphParams)]),
+        "ov_sph_update_tangents_normals": (C.c_int, [P, C.POINTER(abi.SphTangleState), C.POINTER(abi.SphParams)]),
+        "ov_sph_update_velocities": (C.c_int, [P, C.POINTER(abi.SphTangleState), C.POINTER(abi.SphParams),
+                                               C.c_double]),
+        "ov_sph_update_tangle": (C.c_int, [P, C.POINTER(abi.SphTangleState), C.POINTER(abi.SphParams), C.c_double]),
+        "ov_sph_helium": (C.c_int, [C.c_double, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -123,6 +129,22 @@ def declared_symbols() -> list[str]:
         for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b((?:ov|ovd)_\w+)\s*\(", txt, flags=re.M):
             names.append(m.group(1))
     return sorted(set(names))
+
+
+def sph_params_default() -> abi.SphParams:
+    p = abi.SphParams()
+    load().ov_sph_params_default(C.byref(p))
+    return p
+
+
+def sph_helium(T: float) -> np.ndarray:
+    """The spherical fork's He II model at T (host): superfluid, total and
+    normal density, entropy, alpha(T), alpha'(T)."""
+    out = (C.c_double * 6)()
+    rc = load().ov_sph_helium(float(T), out)
+    if rc:
+        raise OVError(rc, f"temperature {T} outside the model's range")
+    return np.array(out[:])
 
 
 def erand48(state) -> float:
@@ -347,6 +369,19 @@ class Context:
 
     def inject_vortices(self, t: float):
         self._check(self.lib.ov_inject_vortices(self._h, float(t)))
+
+    def sph_update(self, sph, params: abi.SphParams, t: float = 0.0, tangents: bool = True, velocities: bool = True):
+        """The spherical fork's update_tangents_normals / update_velocities /
+        update_tangle on a workloads.SphTangle (arrays updated in place)."""
+        st = sph.state()
+        if tangents and velocities:
+            rc = self.lib.ov_sph_update_tangle(self._h, C.byref(st), C.byref(params), t)
+        elif tangents:
+            rc = self.lib.ov_sph_update_tangents_normals(self._h, C.byref(st), C.byref(params))
+        else:
+            rc = self.lib.ov_sph_update_velocities(self._h, C.byref(st), C.byref(params), t)
+        self._check(rc)
+        return sph
 
     def enforce_walls(self, t: float = 0.0):
         self._check(self.lib.ov_enforce_wall_boundaries(self._h, t))

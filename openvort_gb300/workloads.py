@@ -148,6 +148,102 @@ class HostTangle:
         return s
 
 
+class SphTangle:
+    """Host tangle of the spherical fork (section of a spherical shell),
+    numpy-backed; ``state()`` gives its ``struct tangle_state``."""
+
+    def __init__(self, pos, fwd, rev, status, pin, domain=(0.02, 0.1, np.radians(15), np.radians(15))):
+        n = len(pos)
+        self.pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(n, 3)
+        self.vels = np.zeros((n, 3))
+        self.vs = np.zeros((n, 3))
+        self.tangents = np.zeros((n, 3))
+        self.normals = np.zeros((n, 3))
+        self.recalc = np.zeros(n, dtype=np.int32)
+        self.conn = np.ascontiguousarray(np.stack([fwd, rev], 1), dtype=np.int32)
+        self.stat = np.ascontiguousarray(np.stack([status, pin], 1), dtype=np.int32)
+        self.domain = tuple(float(v) for v in domain)
+
+    @property
+    def n(self):
+        return len(self.pos)
+
+    def state(self) -> abi.SphTangleState:
+        s = abi.SphTangleState()
+        dp = lambda a: a.ctypes.data_as(C.POINTER(abi.Vec3))  # noqa: E731
+        s.vnodes, s.vels, s.vs = dp(self.pos), dp(self.vels), dp(self.vs)
+        s.tangents, s.normals = dp(self.tangents), dp(self.normals)
+        s.recalculate = self.recalc.ctypes.data_as(C.POINTER(C.c_int))
+        s.connections = self.conn.ctypes.data_as(C.POINTER(abi.Neighbour))
+        s.status = self.stat.ctypes.data_as(C.POINTER(abi.NodeStatus))
+        d = s.domain_section
+        d.inner_radius, d.outer_radius, d.azimut_angle, d.polar_angle = self.domain
+        s.N = self.n
+        s.next_empty = -1
+        s.total_empty = int((self.stat[:, 0] == abi.OV_EMPTY).sum())
+        self._state = s
+        return s
+
+
+def spherical_tangle(n_rings: int = 12, ring_radius: float = 0.004, dl: float = 1e-3, seed: int = 7,
+                     line: bool = True, empty: int = 3) -> SphTangle:
+    """Seeded rings inside the spherical fork's default section (radii 0.02
+    to 0.1 cm, +-15 degrees in both angles), a few of them across an angular
+    edge, plus a radial line pinned on the inner surface (slipping) and the
+    outer one, and some EMPTY slots."""
+    rng = np.random.default_rng(seed)
+    A = np.radians(15)
+    pos, fwd, rev, st, pin = [], [], [], [], []
+    base = 0
+    npts = max(8, int(round(2 * np.pi * ring_radius / dl)))
+    for r in range(n_rings):
+        rad = rng.uniform(0.035, 0.085)
+        az = rng.uniform(-0.8, 0.8) * A if r % 4 else 0.97 * A    # every fourth ring near the azimuth edge
+        pl = rng.uniform(-0.8, 0.8) * A
+        c = rad * np.array([np.cos(az) * np.cos(pl), np.cos(az) * np.sin(pl), np.sin(az)])
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        u = np.cross(axis, [1.0, 0.0, 0.0] if abs(axis[0]) < 0.9 else [0.0, 1.0, 0.0])
+        u /= np.linalg.norm(u)
+        v = np.cross(axis, u)
+        phi = 2 * np.pi * np.arange(npts) / npts
+        pos.append(c + ring_radius * (np.cos(phi)[:, None] * u + np.sin(phi)[:, None] * v))
+        k = np.arange(npts)
+        fwd.append(base + (k + 1) % npts)
+        rev.append(base + (k - 1) % npts)
+        st.append(np.full(npts, abi.OV_FREE))
+        pin.append(np.full(npts, -1))
+        base += npts
+    if line:
+        m = int(round((0.1 - 0.02) / dl))
+        rr = np.linspace(0.02, 0.1, m + 1)
+        ang = np.array([0.3 * A, -0.4 * A])
+        d = np.array([np.cos(ang[0]) * np.cos(ang[1]), np.cos(ang[0]) * np.sin(ang[1]), np.sin(ang[0])])
+        pos.append(rr[:, None] * d[None, :])
+        k = np.arange(m + 1)
+        f = base + k + 1
+        f[-1] = -1
+        b = base + k - 1
+        b[0] = -1
+        fwd.append(f)
+        rev.append(b)
+        s_ = np.full(m + 1, abi.OV_FREE)
+        s_[0], s_[-1] = abi.OV_PINNED_SLIP, abi.OV_PINNED
+        p_ = np.full(m + 1, -1)
+        p_[0], p_[-1] = abi.OV_INNER, abi.OV_OUTER
+        st.append(s_)
+        pin.append(p_)
+        base += m + 1
+    if empty:
+        pos.append(np.zeros((empty, 3)))
+        fwd.append(np.full(empty, -1))
+        rev.append(np.full(empty, -1))
+        st.append(np.full(empty, abi.OV_EMPTY))
+        pin.append(np.full(empty, -1))
+    return SphTangle(np.concatenate(pos), np.concatenate(fwd), np.concatenate(rev), np.concatenate(st),
+                     np.concatenate(pin))
+
+
 def random_walk_tangle(n_loops: int, per_loop: int = 256, D: float = 0.1, delta: float = 1e-3,
                        sigma: float = 0.3, seed: int = 1, n_images: int = 26) -> HostTangle:
     """Closed random-walk loops in the periodic cube [0, D)^3."""

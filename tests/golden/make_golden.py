@@ -6,7 +6,7 @@ and stores inputs and outputs as small .npz files.  The GPU machine has no
 reference checkout; there the tests compare against these files and against
 the C restatement (oracle/ov_oracle.c), which these files also pin.
 
-Usage:  python tests/golden/make_golden.py [walls | injection]
+Usage:  python tests/golden/make_golden.py [walls | injection | spherical]
 """
 from __future__ import annotations
 
@@ -249,12 +249,90 @@ def inject_steps(ref):
     save("inject_steps.npz", **out)
 
 
+class _quiet_stdout:
+    """The spherical fork prints from its inner loops: silence fd 1 around calls."""
+
+    def __enter__(self):
+        import sys as _s
+        _s.stdout.flush()
+        self.saved = os.dup(1)
+        self.null = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(self.null, 1)
+
+    def __exit__(self, *exc):
+        import ctypes as C
+        C.CDLL(None).fflush(None)   # C stdio's buffer goes to the silenced descriptor
+        os.dup2(self.saved, 1)
+        os.close(self.null)
+        os.close(self.saved)
+
+
+SPH_CASES = {"plain": dict(use_temperature=0), "temperature": dict(use_temperature=1)}
+
+
+def spherical():
+    """The spherical fork's update_tangents_normals and update_velocities
+    (outer surface open) on seeded rings in its default section, a radial
+    line pinned on both surfaces, and EMPTY slots; with and without the He II
+    temperature model.  Also the model's values on a grid of temperatures."""
+    import ctypes as C
+    from openvort_gb300 import abi
+    L = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libovref_sph.so"))
+    TS = C.POINTER(abi.SphTangleState)
+    L.create_tangle.argtypes = [TS, C.c_size_t]
+    L.free_tangle.argtypes = [TS]
+    L.update_tangents_normals.argtypes = [TS]
+    L.update_velocities.argtypes = [TS, C.c_double]
+    sph = W.spherical_tangle()
+    out = dict(pos=sph.pos, conn=sph.conn, status=sph.stat, domain=np.array(sph.domain))
+    dbl = lambda n, v: setattr(C.c_double.in_dll(L, n), "value", float(v))  # noqa: E731
+    i32 = lambda n, v: setattr(C.c_int.in_dll(L, n), "value", int(v))  # noqa: E731
+    for tag, case in SPH_CASES.items():
+        dbl("KAPPA", 9.97e-4); dbl("VORTEX_WIDTH", 1e-8); dbl("alpha", 0.034); dbl("alpha_p", 1.383e-2)
+        i32("use_mutual_friction", 1); dbl("BH_resolution", 0.4); dbl("global_dl_min", 0.5e-3)
+        dbl("global_dl_max", 1.5e-3); dbl("q_dot", 0.03); dbl("temp_bath", 1.65); i32("outer_surface", 0)
+        i32("global_num_threads", 8); i32("use_temperature", case["use_temperature"])
+        ts = abi.SphTangleState()
+        L.create_tangle(C.byref(ts), sph.n)
+        n = sph.n
+        for name, arr in (("vnodes", sph.pos), ("vels", sph.vels), ("vs", sph.vs), ("tangents", sph.tangents),
+                          ("normals", sph.normals)):
+            abi.vec3_view(getattr(ts, name), n)[:] = arr
+        abi.int_view(ts.connections, n, 2)[:] = sph.conn
+        abi.int_view(ts.status, n, 2)[:] = sph.stat
+        d = ts.domain_section
+        d.inner_radius, d.outer_radius, d.azimut_angle, d.polar_angle = sph.domain
+        with _quiet_stdout():
+            L.update_tangents_normals(C.byref(ts))
+            L.update_velocities(C.byref(ts), 0.0)
+        for name in ("tangents", "normals", "vels", "vs"):
+            out[f"{tag}_{name}"] = np.array(abi.vec3_view(getattr(ts, name), n))
+        L.free_tangle(C.byref(ts))
+    names = ["superfluid_density", "total_density", "normal_density", "entropy", "mutual_firction_alpha",
+             "mutual_firction_alpha_p"]
+    Ts = np.linspace(1.31, 2.17, 44)
+    vals = []
+    with _quiet_stdout():
+        for T in Ts:
+            row = []
+            for nm in names:
+                f = getattr(L, nm)
+                f.restype, f.argtypes = C.c_double, [C.c_double]
+                row.append(f(T))
+            vals.append(row)
+    out["helium_T"], out["helium"] = Ts, np.array(vals)
+    save("spherical.npz", **out)
+
+
 def main():
     build(ref=True)
     ref = Checker("reference")
     if len(sys.argv) > 1 and sys.argv[1] == "walls":
         walls(ref)
         wall_steps(ref)
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "spherical":
+        spherical()
         return
     if len(sys.argv) > 1 and sys.argv[1] == "injection":
         injection(ref)
@@ -353,6 +431,9 @@ def main():
     # 7. Injection (add_loop, add_line_in_zdir, inject_vortices in the main loop)
     injection(ref)
     inject_steps(ref)
+
+    # 8. The spherical fork's velocity path
+    spherical()
 
 
 if __name__ == "__main__":
