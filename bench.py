@@ -35,6 +35,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "biot_savart_node_evals_per_s"
+# DRAM bytes (read + write) of one FP64 traversal launch on this workload, from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum of k_vel_fp64, two launches: 9.87 and 9.92 MB)
+K_VEL_FP64_DRAM_BYTES = 9.895e6
 UNIT = "node-evals/s"
 WORKLOAD = dict(workload="random-walk tangle, 256 loops x 256 nodes (65,536), D=0.1 cm, periodic_26, "
                          "theta=0.4, one update_tangle per step",
@@ -442,6 +445,86 @@ def run_large(args, device=0):
     }
 
 
+def run_next_rows(args, device=0):
+    """The rows beside the benchmarked path: mirror walls (wall_2_4) on the
+    headline tangle, frame files, injection, and the spherical fork's
+    velocity path."""
+    import tempfile
+    from openvort_gb300 import abi, gpu, workloads as W
+    out = {}
+    base = make_tangle()
+    n = base.n
+    hw = W.HostTangle(base.pos.copy(), base.conn[:, 0].copy(), base.conn[:, 1].copy(), base.box_lo, base.box_hi,
+                      image_set="wall_2_4")
+    ctx = gpu.Context(device, params=make_params(1))
+    ctx.upload(hw)
+    walls = {"config": "the 65,536-node tangle with mirror walls in z (wall_2_4: 4 periodic images, "
+                       "4 reflected; theta 0.4)"}
+    res = {}
+    for name, prec in (("fp64", abi.OV_PREC_FP64), ("mixed", abi.OV_PREC_MIXED)):
+        ctx.set_precision(prec)
+        ctx.upload(hw)
+        ctx.update_tangle(0.0)
+        ms = eval_ms(ctx, max(3, args.steps // 2))
+        res[name] = (ms, np.array(ctx.download(hw, abi.OV_F_VELS).vels))
+        walls[name] = {"value": n / (ms * 1e-3), "unit": UNIT, "ms_per_eval": ms}
+    walls["mixed"]["rel_l2_vs_fp64_tree"] = rel_l2(res["mixed"][1], res["fp64"][1])
+    if args.cpu_sections:
+        threads = os.cpu_count() or 1
+        kind = cpu_kind()
+        t = min(cpu_eval_time(kind, threads, 1, hw))
+        walls["cpu_baseline"] = {"value": n / t, "unit": UNIT, "cores": threads, "kind": kind,
+                                 "sample": "1 full update_tangle of the wall tangle"}
+    out["walls"] = walls
+    # frames: the reference's text format, host code
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "frame.dat")
+        t0 = time.perf_counter()
+        gpu.write_frame(base, path, 15)
+        tw = time.perf_counter() - t0
+        size = os.path.getsize(path)
+        t0 = time.perf_counter()
+        gpu.read_frame(path, n0=1)
+        tr = time.perf_counter() - t0
+    out["frames"] = {"nodes": n, "bytes": size, "write_ms": tw * 1e3, "read_ms": tr * 1e3,
+                     "write_mb_per_s": size / tw / 1e6, "read_mb_per_s": size / tr / 1e6}
+    # injection: one loop and one pinned line pair into the resident wall tangle
+    ctx.set_precision(abi.OV_PREC_FP64)
+    ctx.upload(hw)
+    ctx.set_injection(abi.make_injection(seed=5, loop_frequency=1.0, line_n=1, line_frequency=1.0,
+                                         line_polarized=True))
+    t0 = time.perf_counter()
+    ctx.inject_vortices(2.0)
+    ti = time.perf_counter() - t0
+    out["injection"] = {"nodes_added": ctx.stats()["injected_nodes"], "ms": ti * 1e3,
+                        "includes": "draws, slot allocation with pool growth, push of positions and topology"}
+    ctx.close()
+    # the spherical fork's update_tangle (tangents + velocities, temperature model on)
+    sph = W.spherical_tangle(n_rings=640)
+    p = gpu.sph_params_default()
+    ctx = gpu.Context(device)
+    for _ in range(2):
+        ctx.sph_update(sph, p, 0.0)
+    ts = []
+    for _ in range(max(3, args.steps // 2)):
+        t0 = time.perf_counter()
+        ctx.sph_update(sph, p, 0.0)
+        ts.append(time.perf_counter() - t0)
+    st = ctx.stats()
+    ctx.close()
+    live = int((sph.stat[:, 0] != abi.OV_EMPTY).sum())
+    ms = statistics.mean(ts) * 1e3
+    out["spherical"] = {
+        "config": f"spherical fork's default section (r 0.02..0.1 cm, +-15 deg), {live} nodes: 640 rings + a "
+                  "pinned radial line; temperature model on; one update_tangle (tangents, both trees, 18 "
+                  "queries per node) per call, through the C ABI with host buffers",
+        "value": live / (ms * 1e-3), "unit": UNIT, "ms_per_call": ms, "visits": st["visits"],
+        "accepts": st["accepts"],
+        "cpu_baseline": "unavailable on the GPU host: the fork is pinned through its own build, which "
+                        "needs the OpenVort checkout, and is not restated in the oracle"}
+    return out
+
+
 def run_ours(args):
     from openvort_gb300 import abi, gpu
     world, rank, local, dist = dist_setup()
@@ -556,7 +639,7 @@ def run_ours(args):
     if isinstance(mixed, dict) and "value" in mixed:
         mixed["rel_l2_vs_direct_subsample"] = rel_l2(mixed_vels[sub], direct_v)
 
-    ensemble = precision_form = large = None
+    ensemble = precision_form = large = next_rows = None
     if world == 1 and args.ensemble_steps >= 0:
         try:
             ensemble = run_ensemble(args, device)
@@ -572,6 +655,11 @@ def run_ours(args):
             large = run_large(args, device)
         except Exception as e:
             large = {"error": str(e)[:300]}
+    if world == 1 and args.next_rows:
+        try:
+            next_rows = run_next_rows(args, device)
+        except Exception as e:
+            next_rows = {"error": str(e)[:300]}
     clk.__exit__(None, None, None)
 
     # ---- CPU baseline (rank 0 only, bounded sample)
@@ -594,7 +682,8 @@ def run_ours(args):
                        parallelism="replicas" if world > 1 else "single GPU"),
         "phases_ms": {"tangents": phases[0], "tree_build": phases[1], "traversal": phases[2]},
         "roofline": {"bound": "fma", "pipe": "fp64", "achieved": achieved, "peak": fp64_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                     "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": K_VEL_FP64_DRAM_BYTES,
+                     "traffic_note": "DRAM bytes per launch from ncu; the traversal is FP64-pipe bound",
                      "peak_source": "measured in this run (FP64 FMA chains, all SMs)",
                      "work": "42 flops per accepted interaction + 9 per visited cell",
                      "accepts": acc, "visits": vis, "fp32_fma_peak_tflops": fp32_peak,
@@ -609,6 +698,7 @@ def run_ours(args):
         "ensemble": ensemble,
         "precision_form": precision_form,
         "large": large,
+        "next_rows": next_rows,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "peaks_source": peak_src,
@@ -628,6 +718,8 @@ def main():
     ap.add_argument("--large-steps", type=int, default=5,
                     help="full time steps of the 1,048,576-node tangle (-1: skip that section)")
     ap.add_argument("--precision-form", type=int, default=1, help="262,144-node theta 0.3/0.5 section (0: skip)")
+    ap.add_argument("--next-rows", type=int, default=1,
+                    help="walls, frames, injection and spherical-fork sections (0: skip)")
     ap.add_argument("--cpu-sections", type=int, default=1,
                     help="time the CPU baseline of the ensemble, precision-form and large sections too (0: skip)")
     args = ap.parse_args()
