@@ -1201,7 +1201,7 @@ static int sph_run(ov_ctx *c, ov_sph_tangle_state *t, const ov_sph_params *p, do
         ov_launch_sph_images(c, sd, ss);
         for (int attempt = 0;; ++attempt) {
             if ((r = ov_tree_build(c, c->node, c->stream))) return r;
-            ov_launch_sph_velocities(c, sd, ss);
+            if ((r = ov_launch_sph_velocities(c, sd, ss))) return r;
             OV_CUDA(c, cudaGetLastError());
             if ((r = collect_stats(c, true))) return r;
             if (!(c->stats.error_word & OV_EW_CELLS)) break;

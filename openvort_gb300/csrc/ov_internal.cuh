@@ -332,7 +332,7 @@ struct SphSettings {
 };
 void ov_launch_sph_tangents(ov_ctx *c, const SphDomain &d, const SphSettings &p);
 void ov_launch_sph_images(ov_ctx *c, const SphDomain &d, const SphSettings &p);
-void ov_launch_sph_velocities(ov_ctx *c, const SphDomain &d, const SphSettings &p);
+int ov_launch_sph_velocities(ov_ctx *c, const SphDomain &d, const SphSettings &p);
 void ov_launch_periodic_wrap(ov_ctx *c, cudaStream_t s);
 
 // ------------------------------------------------------------ device helpers

@@ -831,14 +831,23 @@ __global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mix
                 }
             }
             if (j >= 0 && a.geo.nreflect[j] > 0) {
-                // mirror images (wall geometries) keep their own FP64 sum
-                double q[3], v[3];
+                // mirror images (wall geometries): the reflected query point split
+                // on the grid, its own sums, reflected before they join the rest
+                double q[3];
                 image_point(a.geo, j, p, q);
-                unsigned long long vi = 0, ac = 0, sp = 0;
-                bh_query64(a, q, part, w.root, w.end, v, vi, ac, sp, overflow);
+                for (int ax = 0; ax < 3; ++ax) {
+                    double G = rint(q[ax] * a.inv_h) * a.grid_h;
+                    g[ax] = (float)G;
+                    f[ax] = (float)(q[ax] - G);
+                }
+                MixedAcc mr = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
+                double wr[3] = {0, 0, 0};   // FP64 terms of this image when the near list is full
+                bh_query32(a, g, f, p, j, part, w.root, w.end, mr, near_list, nnear, wr, overflow);
+                double v[3] = {((double)mr.s0 - (double)mr.c0) + wr[0], ((double)mr.s1 - (double)mr.c1) + wr[1],
+                               ((double)mr.s2 - (double)mr.c2) + wr[2]};
                 for (int r = 0; r < a.geo.nreflect[j]; ++r) mirror_vec(a.geo.reflect[j][r], v);
                 img64[0] += v[0]; img64[1] += v[1]; img64[2] += v[2];
-                m.nvis += (unsigned)vi; m.nacc += (unsigned)ac; m.nstep += (unsigned)sp;
+                m.nvis += mr.nvis; m.nacc += mr.nacc; m.nstep += mr.nstep; m.nfb += mr.nfb; m.nnear += mr.nnear;
                 continue;
             }
             bh_query32(a, g, f, p, j, part, w.root, w.end, m, near_list, nnear, w64, overflow);
@@ -853,6 +862,8 @@ __global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mix
             else image_point(a.geo, j, p, q);
             decide64(a.cells + c, q, a.prm.theta, true, dxyz, &d64);
             if (interact64(a.cells + c, dxyz, d64, a.f4pi, wv)) {
+                if (j >= 0)   // a mirror image's term is reflected back
+                    for (int r = 0; r < a.geo.nreflect[j]; ++r) mirror_vec(a.geo.reflect[j][r], wv);
                 w64[0] += wv[0]; w64[1] += wv[1]; w64[2] += wv[2];
             }
         }
@@ -2018,44 +2029,44 @@ __device__ __forceinline__ void sph_normalize(const double p[3], double out[3])
     for (int ax = 0; ax < 3; ++ax) out[ax] = rn_mul(p[ax], m);
 }
 
-// update_velocity of the fork (tangle.c:638-865, outer surface open): one
-// warp per 32 targets of the tangle's traversal order.
-__global__ void __launch_bounds__(128) k_vel_sph(SphArgs s)
+// The 18 tree queries of update_velocity (tangle.c:669-761 of the fork,
+// outer surface open), one warp per (32 targets, query): query q < 9 walks
+// the tangle's tree, q >= 9 the inner image's; q % 9 == 0 at the node, else
+// at rotation q % 9 - 1 (+-az, +-pl, then the corners), its result rotated
+// back.  part[(q * 3 + axis) * n + node] holds the result.
+__global__ void __launch_bounds__(128) k_sph_query(SphArgs s, double *__restrict__ part)
 {
     const VelArgs &a = s.v;
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nne = a.tt[TT_NNE];   // member 0: the tangle, first in sorted order
-    if (warp * 32 >= nne) return;
-    const int loc = warp * 32 + lane;
+    const int tiles = (nne + 31) / 32;
+    if (warp >= 18 * tiles) return;
+    const int q = warp / tiles, tile = warp - q * tiles;
+    const int loc = tile * 32 + lane;
     bool valid = loc < nne;
     int id = valid ? a.order[loc] : 0;
     if (valid && (id < 0 || id >= s.n)) { bad_index(a, 9, id); valid = false; id = 0; }
     const int st = valid ? a.status[id] : OV_EMPTY;
-    const bool part = valid && st != OV_PINNED && st != OV_EMPTY;
+    const bool take = valid && st != OV_PINNED && st != OV_EMPTY;
     double p[3] = {0, 0, 0};
     if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
     unsigned long long visits = 0, accepts = 0, steps = 0;
     bool overflow = false;
-    double own[3] = {0, 0, 0}, tot[3] = {0, 0, 0};
-    for (int m = 0; m < 2; ++m) {
-        const int root = a.tt[m * TT_WORDS + TT_ROOT], end = a.tt[m * TT_WORDS + TT_END];
-        const bool go = part && end > root;
-        double v[3];
-        bh_query64(a, p, go, root, end, v, visits, accepts, steps, overflow);
-        if (m == 0) { own[0] = v[0]; own[1] = v[1]; own[2] = v[2]; }
-        else for (int ax = 0; ax < 3; ++ax) tot[ax] = rn_sub(tot[ax], v[ax]);
-        // rotations of the section (tangle.c:677-719): +-az, +-pl, then the corners
-        for (int j = 0; j < 8; ++j) {
-            const double ua = j < 2 ? (j == 0 ? 1.0 : -1.0) : (j < 4 ? 0.0 : ((j & 1) ? -1.0 : 1.0));
-            const double up = j < 2 ? 0.0 : (j < 4 ? (j == 2 ? 1.0 : -1.0) : (j < 6 ? 1.0 : -1.0));
-            const double da = rn_mul(ua, s.d_az), dp = rn_mul(up, s.d_pl);
-            double q[3], w[3];
-            sph_rotate(p, da, dp, q);
-            bh_query64(a, q, go, root, end, v, visits, accepts, steps, overflow);
-            sph_rotate(v, -da, -dp, w);
-            for (int ax = 0; ax < 3; ++ax) tot[ax] = m == 0 ? rn_add(tot[ax], w[ax]) : rn_sub(tot[ax], w[ax]);
-        }
+    const int m = q / 9, j = q % 9 - 1;
+    const int root = a.tt[m * TT_WORDS + TT_ROOT], end = a.tt[m * TT_WORDS + TT_END];
+    const bool go = take && end > root;
+    double v[3], w[3];
+    if (j < 0) {
+        bh_query64(a, p, go, root, end, w, visits, accepts, steps, overflow);
+    } else {
+        const double ua = j < 2 ? (j == 0 ? 1.0 : -1.0) : (j < 4 ? 0.0 : ((j & 1) ? -1.0 : 1.0));
+        const double up = j < 2 ? 0.0 : (j < 4 ? (j == 2 ? 1.0 : -1.0) : (j < 6 ? 1.0 : -1.0));
+        const double da = rn_mul(ua, s.d_az), dp = rn_mul(up, s.d_pl);
+        double qp[3];
+        sph_rotate(p, da, dp, qp);
+        bh_query64(a, qp, go, root, end, v, visits, accepts, steps, overflow);
+        sph_rotate(v, -da, -dp, w);
     }
     if (a.stat) {
         for (int o = 16; o > 0; o >>= 1) {
@@ -2068,12 +2079,33 @@ __global__ void __launch_bounds__(128) k_vel_sph(SphArgs s)
             atomicAdd(&a.stat[ST_STEPS], steps);
         }
     }
-    if (overflow) atomicOr((int *)&a.counters[TC_ERR], OV_EW_ITER);
-    if (!valid || st == OV_EMPTY) return;
+    if (overflow && lane == 0) atomicOr((int *)&a.counters[TC_ERR], OV_EW_ITER);
+    if (!valid) return;
+    for (int ax = 0; ax < 3; ++ax) part[((size_t)q * 3 + ax) * s.n + id] = w[ax];
+}
+
+// The rest of update_velocity (tangle.c:644-665, 763-865 of the fork): the
+// query results summed in the fork's order, LIA with its segment-length
+// limits, the temperature model, mutual friction, PINNED_SLIP.
+__global__ void k_sph_finish(SphArgs s, const double *__restrict__ part)
+{
+    const VelArgs &a = s.v;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= s.n) return;
+    const int st = a.status[id];
+    if (st == OV_EMPTY) return;
     if (st == OV_PINNED) {   // the node rests; its velocity is left as it was
         a.sx[id] = a.sy[id] = a.sz[id] = 0;
         return;
     }
+    const double p[3] = {a.x[id], a.y[id], a.z[id]};
+    auto P = [&](int q, int ax) { return part[((size_t)q * 3 + ax) * s.n + id]; };
+    double own[3], tot[3] = {0, 0, 0};
+    for (int ax = 0; ax < 3; ++ax) own[ax] = P(0, ax);
+    for (int q = 1; q < 9; ++q)
+        for (int ax = 0; ax < 3; ++ax) tot[ax] = rn_add(tot[ax], P(q, ax));
+    for (int q = 9; q < 18; ++q)
+        for (int ax = 0; ax < 3; ++ax) tot[ax] = rn_sub(tot[ax], P(q, ax));
     // LIA with the fork's limits on the neighbour distances (tangle.c:581-611)
     double nx_[3], pv[3];
     if (!(sph_step_node(s, id, 1, nx_) && sph_step_node(s, id, -1, pv))) {
@@ -2169,10 +2201,19 @@ void ov_launch_sph_images(ov_ctx *c, const SphDomain &d, const SphSettings &p)
     c->launches++;
 }
 
-void ov_launch_sph_velocities(ov_ctx *c, const SphDomain &d, const SphSettings &p)
+int ov_launch_sph_velocities(ov_ctx *c, const SphDomain &d, const SphSettings &p)
 {
     SphArgs s = make_sph_args(c, d, p);
-    const int warps = (d.n + 31) / 32;
-    k_vel_sph<<<(warps + 3) / 4, 128, 0, c->stream>>>(s);
-    c->launches++;
+    const size_t need = (size_t)18 * 3 * (size_t)d.n;
+    if (c->part_cap < need) {
+        if (c->part) cudaFree(c->part);
+        c->part = nullptr;
+        OV_CUDA(c, cudaMalloc(&c->part, need * sizeof(double)));
+        c->part_cap = need;
+    }
+    const long long warps = 18LL * ((d.n + 31) / 32);
+    k_sph_query<<<(unsigned)((warps + 3) / 4), 128, 0, c->stream>>>(s, c->part);
+    k_sph_finish<<<(d.n + 127) / 128, 128, 0, c->stream>>>(s, c->part);
+    c->launches += 2;
+    return OV_OK;
 }
