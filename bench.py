@@ -511,15 +511,28 @@ def run_next_rows(args, device=0):
         ctx.sph_update(sph, p, 0.0)
         ts.append(time.perf_counter() - t0)
     st = ctx.stats()
+    v64 = sph.vels.copy()
+    # the same call in mixed precision
+    ctx.set_precision(abi.OV_PREC_MIXED)
+    ctx.sph_update(sph, p, 0.0)
+    tm = []
+    for _ in range(max(3, args.steps // 2)):
+        t0 = time.perf_counter()
+        ctx.sph_update(sph, p, 0.0)
+        tm.append(time.perf_counter() - t0)
     ctx.close()
     live = int((sph.stat[:, 0] != abi.OV_EMPTY).sum())
+    free = (sph.stat[:, 0] != abi.OV_EMPTY) & (sph.stat[:, 0] != abi.OV_PINNED)
     ms = statistics.mean(ts) * 1e3
+    ms32 = statistics.mean(tm) * 1e3
     out["spherical"] = {
         "config": f"spherical fork's default section (r 0.02..0.1 cm, +-15 deg), {live} nodes: 640 rings + a "
                   "pinned radial line; temperature model on; one update_tangle (tangents, both trees, 18 "
                   "queries per node) per call, through the C ABI with host buffers",
         "value": live / (ms * 1e-3), "unit": UNIT, "ms_per_call": ms, "visits": st["visits"],
         "accepts": st["accepts"],
+        "mixed": {"value": live / (ms32 * 1e-3), "unit": UNIT, "ms_per_call": ms32,
+                  "rel_l2_vs_fp64_tree": rel_l2(sph.vels[free], v64[free])},
         "cpu_baseline": "unavailable on the GPU host: the fork is pinned through its own build, which "
                         "needs the OpenVort checkout, and is not restated in the oracle"}
     return out

@@ -1148,6 +1148,8 @@ static int sph_run(ov_ctx *c, ov_sph_tangle_state *t, const ov_sph_params *p, do
     g.sph_az = dom.azimut_angle;
     g.sph_pl = dom.polar_angle;
     g.sph_seg_max = 5 * p->dl_max;
+    // grid step of the mixed path: every coordinate (|x| <= ro) below 2^22 steps
+    c->grid_h = ldexp(1.0, (int)ceil(log2(dom.outer_radius)) - 22);
     const double A = dom.azimut_angle, P = dom.polar_angle;
     const double ri = dom.inner_radius, ro = dom.outer_radius;
     const double lo0[3] = {ri, -A, -P}, hi0[3] = {ro, A, P};

@@ -2084,6 +2084,86 @@ __global__ void __launch_bounds__(128) k_sph_query(SphArgs s, double *__restrict
     for (int ax = 0; ax < 3; ++ax) part[((size_t)q * 3 + ax) * s.n + id] = w[ax];
 }
 
+// k_sph_query in mixed precision: the query point (rotated in FP64) split on
+// the grid, the FP32 walk with the FP64 path's decisions (guard bands),
+// near-field leaves in FP64 after the walk.
+__global__ void __launch_bounds__(128) k_sph_query_mixed(SphArgs s, double *__restrict__ part)
+{
+    const VelArgs &a = s.v;
+    __shared__ int s_near[4][kNearCap * 32];
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int *near_list = &s_near[threadIdx.x >> 5][lane];
+    const int nne = a.tt[TT_NNE];
+    const int tiles = (nne + 31) / 32;
+    if (warp >= 18 * tiles) return;
+    const int q = warp / tiles, tile = warp - q * tiles;
+    const int loc = tile * 32 + lane;
+    bool valid = loc < nne;
+    int id = valid ? a.order[loc] : 0;
+    if (valid && (id < 0 || id >= s.n)) { bad_index(a, 9, id); valid = false; id = 0; }
+    const int st = valid ? a.status[id] : OV_EMPTY;
+    const bool take = valid && st != OV_PINNED && st != OV_EMPTY;
+    double p[3] = {0, 0, 0};
+    if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
+    const int m = q / 9, j = q % 9 - 1;
+    const int root = a.tt[m * TT_WORDS + TT_ROOT], end = a.tt[m * TT_WORDS + TT_END];
+    const bool go = take && end > root;
+    double qp[3] = {p[0], p[1], p[2]}, da = 0, dp = 0;
+    if (j >= 0) {
+        const double ua = j < 2 ? (j == 0 ? 1.0 : -1.0) : (j < 4 ? 0.0 : ((j & 1) ? -1.0 : 1.0));
+        const double up = j < 2 ? 0.0 : (j < 4 ? (j == 2 ? 1.0 : -1.0) : (j < 6 ? 1.0 : -1.0));
+        da = rn_mul(ua, s.d_az);
+        dp = rn_mul(up, s.d_pl);
+        sph_rotate(p, da, dp, qp);
+    }
+    float g[3], f[3];
+    for (int ax = 0; ax < 3; ++ax) {
+        const double G = rint(qp[ax] * a.inv_h) * a.grid_h;
+        g[ax] = (float)G;
+        f[ax] = (float)(qp[ax] - G);
+    }
+    MixedAcc acc = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
+    double w64[3] = {0, 0, 0};
+    int nnear = 0;
+    bool overflow = false;
+    bh_query32(a, g, f, qp, -1, go, root, end, acc, near_list, nnear, w64, overflow);
+    for (int i = 0; i < nnear && i < kNearCap; ++i) {
+        const int e = near_list[32 * i];
+        const int c = e >> 5;
+        if (c < root || c >= end) { bad_index(a, 3, e); continue; }
+        double dxyz[3], d64, wv[3];
+        decide64(a.cells + c, qp, a.prm.theta, true, dxyz, &d64);
+        if (interact64(a.cells + c, dxyz, d64, a.f4pi, wv)) {
+            w64[0] += wv[0]; w64[1] += wv[1]; w64[2] += wv[2];
+        }
+    }
+    __syncwarp();
+    double v[3] = {((double)acc.s0 - (double)acc.c0) + w64[0], ((double)acc.s1 - (double)acc.c1) + w64[1],
+                   ((double)acc.s2 - (double)acc.c2) + w64[2]};
+    double w[3] = {v[0], v[1], v[2]};
+    if (j >= 0) sph_rotate(v, -da, -dp, w);
+    if (a.stat) {
+        unsigned long long vis = acc.nvis, ac = acc.nacc, fb = acc.nfb, nr = acc.nnear;
+        for (int o = 16; o > 0; o >>= 1) {
+            vis += __shfl_xor_sync(0xffffffffu, vis, o);
+            ac += __shfl_xor_sync(0xffffffffu, ac, o);
+            fb += __shfl_xor_sync(0xffffffffu, fb, o);
+            nr += __shfl_xor_sync(0xffffffffu, nr, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&a.stat[ST_VISITS], vis);
+            atomicAdd(&a.stat[ST_ACCEPTS], ac);
+            atomicAdd(&a.stat[ST_STEPS], (unsigned long long)acc.nstep);
+            atomicAdd(&a.stat[ST_FALLBACK], fb);
+            atomicAdd(&a.stat[ST_NEAR64], nr);
+        }
+    }
+    if (overflow && lane == 0) atomicOr((int *)&a.counters[TC_ERR], OV_EW_ITER);
+    if (!valid) return;
+    for (int ax = 0; ax < 3; ++ax) part[((size_t)q * 3 + ax) * s.n + id] = w[ax];
+}
+
 // The rest of update_velocity (tangle.c:644-665, 763-865 of the fork): the
 // query results summed in the fork's order, LIA with its segment-length
 // limits, the temperature model, mutual friction, PINNED_SLIP.
@@ -2212,7 +2292,10 @@ int ov_launch_sph_velocities(ov_ctx *c, const SphDomain &d, const SphSettings &p
         c->part_cap = need;
     }
     const long long warps = 18LL * ((d.n + 31) / 32);
-    k_sph_query<<<(unsigned)((warps + 3) / 4), 128, 0, c->stream>>>(s, c->part);
+    if (c->precision == OV_PREC_MIXED)
+        k_sph_query_mixed<<<(unsigned)((warps + 3) / 4), 128, 0, c->stream>>>(s, c->part);
+    else
+        k_sph_query<<<(unsigned)((warps + 3) / 4), 128, 0, c->stream>>>(s, c->part);
     k_sph_finish<<<(d.n + 127) / 128, 128, 0, c->stream>>>(s, c->part);
     c->launches += 2;
     return OV_OK;

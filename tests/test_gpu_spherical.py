@@ -105,3 +105,23 @@ def test_outer_surface_wall_is_refused(golden):
     with pytest.raises(gpu.OVError):
         ctx.sph_update(sph_from_golden(g), p, 0.0)
     ctx.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_mixed_precision_matches_fp64_tree(golden, case):
+    """The mixed path on the fork's geometry: FP32 walks with the FP64
+    decisions (same visits and accepts), within 1e-6 relative L2 of FP64."""
+    g = golden("spherical.npz")
+    a, b = sph_from_golden(g), sph_from_golden(g)
+    ctx = gpu.Context(0)
+    ctx.sph_update(a, params(case), 0.0)
+    s64 = ctx.stats()
+    ctx.set_precision(abi.OV_PREC_MIXED)
+    ctx.sph_update(b, params(case), 0.0)
+    s32 = ctx.stats()
+    ctx.close()
+    free = (g["status"][:, 0] != abi.OV_EMPTY) & (g["status"][:, 0] != abi.OV_PINNED)
+    err = np.linalg.norm(b.vels[free] - a.vels[free]) / np.linalg.norm(a.vels[free])
+    assert err < 1e-6
+    assert s32["visits"] == s64["visits"] and s32["accepts"] == s64["accepts"]
