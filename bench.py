@@ -523,6 +523,16 @@ def run_next_rows(args, device=0):
     ctx.close()
     live = int((sph.stat[:, 0] != abi.OV_EMPTY).sum())
     free = (sph.stat[:, 0] != abi.OV_EMPTY) & (sph.stat[:, 0] != abi.OV_PINNED)
+    sph_cpu = None
+    if args.cpu_sections:
+        from oracle.pyoracle import sph_update_tangle
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        sph_update_tangle(W.spherical_tangle(n_rings=640), p, threads=threads, fast=True)
+        tc = time.perf_counter() - t0
+        sph_cpu = {"value": live / tc, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": "one update_tangle of the same tangle in the C restatement of the fork "
+                             "(bit-identical to the fork on the committed golden vectors)"}
     ms = statistics.mean(ts) * 1e3
     ms32 = statistics.mean(tm) * 1e3
     out["spherical"] = {
@@ -533,8 +543,7 @@ def run_next_rows(args, device=0):
         "accepts": st["accepts"],
         "mixed": {"value": live / (ms32 * 1e-3), "unit": UNIT, "ms_per_call": ms32,
                   "rel_l2_vs_fp64_tree": rel_l2(sph.vels[free], v64[free])},
-        "cpu_baseline": "unavailable on the GPU host: the fork is pinned through its own build, which "
-                        "needs the OpenVort checkout, and is not restated in the oracle"}
+        "cpu_baseline": sph_cpu}
     return out
 
 

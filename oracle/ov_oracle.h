@@ -22,6 +22,7 @@
 
 #include "../include/ov_tangle.h"
 #include "../include/openvort_gpu.h"
+#include "../include/ov_spherical.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -77,6 +78,12 @@ void orc_step(ov_tangle_state *t, double time, double dt, const ov_params *p,
               int *n_recs);
 
 /* add_loop (vortex_injection.c:49): ring geometry used by the small config. */
+/* The spherical fork's update_tangents_normals (tangents != 0) and
+   update_velocities with the outer surface open (ov_oracle_sph.c). */
+int orc_sph_update_tangle(ov_sph_tangle_state *t, const ov_sph_params *p, double time, int threads, int tangents);
+/* Its He II model at T: superfluid, total, normal density, entropy, alpha, alpha'. */
+int orc_sph_helium(double T, double out[6]);
+
 void orc_add_loop(ov_tangle_state *t, const ov_vec3 *center, const ov_vec3 *dir, double r,
                   const ov_params *p);
 

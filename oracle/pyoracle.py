@@ -268,3 +268,19 @@ class Checker:
 
 def reference_available() -> bool:
     return os.path.exists(REF_SO)
+
+
+def sph_update_tangle(sph, params, threads: int = 1, tangents: bool = True, fast: bool = False) -> None:
+    """The spherical fork's update_tangents_normals + update_velocities in the
+    C restatement (oracle/ov_oracle_sph.c), in place on a workloads.SphTangle."""
+    path = PORT_FAST_SO if fast else PORT_SO
+    if not os.path.exists(path):
+        build(ref=False)
+    L = C.CDLL(path)
+    f = L.orc_sph_update_tangle
+    f.argtypes = [C.POINTER(abi.SphTangleState), C.POINTER(abi.SphParams), C.c_double, C.c_int, C.c_int]
+    f.restype = C.c_int
+    st = sph.state()
+    rc = f(C.byref(st), C.byref(params), 0.0, int(threads), int(tangents))
+    if rc:
+        raise RuntimeError(f"oracle spherical update failed ({rc})")

@@ -49,6 +49,19 @@ def test_helium_model_matches_the_fork(golden):
         gpu.sph_helium(2.5)   # above the lambda point: the fork exits
 
 
+def test_oracle_restatement_is_bit_identical_to_fork(golden):
+    """The C restatement of the fork's velocity path (oracle/ov_oracle_sph.c)
+    reproduces the fork's tangents, normals and velocities bit for bit."""
+    from oracle.pyoracle import sph_update_tangle
+    g = golden("spherical.npz")
+    for case in CASES:
+        sph = sph_from_golden(g)
+        sph_update_tangle(sph, params(case), threads=4)
+        live = g["status"][:, 0] != abi.OV_EMPTY
+        for name in ("tangents", "normals", "vels", "vs"):
+            np.testing.assert_array_equal(getattr(sph, name)[live], g[f"{case}_{name}"][live])
+
+
 def test_workload_matches_golden(golden):
     g = golden("spherical.npz")
     s = W.spherical_tangle()
@@ -125,3 +138,21 @@ def test_mixed_precision_matches_fp64_tree(golden, case):
     err = np.linalg.norm(b.vels[free] - a.vels[free]) / np.linalg.norm(a.vels[free])
     assert err < 1e-6
     assert s32["visits"] == s64["visits"] and s32["accepts"] == s64["accepts"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_larger_tangle_vs_oracle(case):
+    """A larger seeded tangle (96 rings, other seed) against the C restatement."""
+    from oracle.pyoracle import sph_update_tangle
+    a = W.spherical_tangle(n_rings=96, seed=11)
+    b = W.spherical_tangle(n_rings=96, seed=11)
+    ctx = gpu.Context(0)
+    ctx.sph_update(a, params(case), 0.0)
+    ctx.close()
+    sph_update_tangle(b, params(case), threads=8)
+    free = (b.stat[:, 0] != abi.OV_EMPTY) & (b.stat[:, 0] != abi.OV_PINNED)
+    live = b.stat[:, 0] != abi.OV_EMPTY
+    assert node_rel_err(a.tangents[live], b.tangents[live]) < 1e-12
+    assert node_rel_err(a.vels[free], b.vels[free]) < 1e-10
+    assert node_rel_err(a.vs[live], b.vs[live]) < 1e-10
