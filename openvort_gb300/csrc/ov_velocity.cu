@@ -1235,11 +1235,12 @@ __device__ __forceinline__ bool rec_term64_fast(const RecArgs &r, int m, int f, 
 constexpr int kRecThreads = 256;
 constexpr int kRecVals = 7;   // 3 sums, FP32 magnitude, 3 spare (|FP64 terms|)
 
-__global__ void __launch_bounds__(kRecThreads) k_rec_sums(RecArgs r, const int *__restrict__ nodes, int n,
+__global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const int *__restrict__ nodes, int n,
                                                           int span, int max_chunks, int force64,
                                                           double *__restrict__ part)
 {
-    __shared__ float s_q[OV_MAX_IMAGES + 1][6];   // split query points: self, then images
+    // split query points (self, then images): (g, mirror flag), (f, 0)
+    __shared__ float4 s_q[OV_MAX_IMAGES + 1][2];
     __shared__ double red[kRecVals][kRecThreads];
     const int b = blockIdx.x, chunk = blockIdx.y;
     if (b >= n) return;
@@ -1256,13 +1257,17 @@ __global__ void __launch_bounds__(kRecThreads) k_rec_sums(RecArgs r, const int *
     const int nq = r.geo.n_img + 1;
     if (threadIdx.x < nq) {
         const int j = (int)threadIdx.x - 1;
+        float g[3], f[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            float g = r.sp[(size_t)a * r.cap + k], f = r.sp[(size_t)(3 + a) * r.cap + k];
-            if (j >= 0) { g -= r.shift_g[j][a]; f -= r.shift_f[j][a]; }
-            s_q[threadIdx.x][a] = g;
-            s_q[threadIdx.x][3 + a] = f;
+            g[a] = r.sp[(size_t)a * r.cap + k];
+            f[a] = r.sp[(size_t)(3 + a) * r.cap + k];
+            if (j >= 0) { g[a] -= r.shift_g[j][a]; f[a] -= r.shift_f[j][a]; }
         }
+        // mirror images (reflected query points): FP64, as the split shift tables hold translations only
+        const float mirror = (j >= 0 && r.geo.nreflect[j] > 0) ? 1.0f : 0.0f;
+        s_q[threadIdx.x][0] = make_float4(g[0], g[1], g[2], mirror);
+        s_q[threadIdx.x][1] = make_float4(f[0], f[1], f[2], 0.0f);
     }
     __syncthreads();
     float s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0, mag = 0;
@@ -1289,29 +1294,30 @@ __global__ void __launch_bounds__(kRecThreads) k_rec_sums(RecArgs r, const int *
             sv[a] = (bg - ag[a]) + (bf - af[a]);
         }
         const float slen = sqrtf(fmaf(sv[0], sv[0], fmaf(sv[1], sv[1], sv[2] * sv[2])));
+        const bool own = (m == k || f == k);   // the node's own segments: skipped at the primary point
         float t0 = 0, t1 = 0, t2 = 0;   // this segment's terms over the query points
-        for (int qi = 0; qi < nq; ++qi) {
-            const int j = qi - 1;
-            if (j < 0 && (m == k || f == k)) continue;   // the node's own segments (primary only)
-            float R[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) R[a] = (ag[a] - s_q[qi][a]) + (af[a] - s_q[qi][3 + a]);
-            const float lR2 = fmaf(R[0], R[0], fmaf(R[1], R[1], R[2] * R[2]));
-            const float P0 = R[0] + sv[0], P1 = R[1] + sv[1], P2 = R[2] + sv[2];
+        float ms = 0;                   // sum over the query points of sc |R|
+        for (int qi = own ? 1 : 0; qi < nq; ++qi) {
+            const float4 qg = s_q[qi][0], qf = s_q[qi][1];
+            const float R0 = (ag[0] - qg.x) + (af[0] - qf.x);
+            const float R1 = (ag[1] - qg.y) + (af[1] - qf.y);
+            const float R2 = (ag[2] - qg.z) + (af[2] - qf.z);
+            const float lR2 = fmaf(R0, R0, fmaf(R1, R1, R2 * R2));
+            const float P0 = R0 + sv[0], P1 = R1 + sv[1], P2 = R2 + sv[2];
             const float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
-            // mirror images (reflected query points): FP64, as the split shift tables hold translations only
-            bool use64 = seg64 || lR2 < r.rnear2 || lp2 < r.rnear2 || (j >= 0 && r.geo.nreflect[j] > 0);
+            bool use64 = seg64 || lR2 < r.rnear2 || lp2 < r.rnear2 || qg.w != 0.0f;
             float ra = 0, rb = 0, ab = 0, dot = 0, nd = 0;
             if (!use64) {
                 ra = rsqrtf(lR2);
                 rb = rsqrtf(lp2);
                 ab = ra * rb;
-                dot = fmaf(R[0], P0, fmaf(R[1], P1, R[2] * P2));
+                dot = fmaf(R0, P0, fmaf(R1, P1, R2 * P2));
                 nd = dot * ab;
                 if (fabsf(nd - 1e-8f) < 1e-4f) use64 = true;   // filter near its threshold
             }
             if (use64) {
                 double w[3];
+                const int j = qi - 1;
                 if (force64 ? rec_term64_fast(r, m, f, j, p, w) : rec_term64(r, m, f, j, p, w)) {
                     d0 += w[0]; d1 += w[1]; d2 += w[2];
                     dabs += fabs(w[0]) + fabs(w[1]) + fabs(w[2]);
@@ -1321,11 +1327,12 @@ __global__ void __launch_bounds__(kRecThreads) k_rec_sums(RecArgs r, const int *
             if (nd < 1e-8f) continue;   // ndot filter (far from its threshold here)
             const float sc = __fdividef(r.f4pif * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
             // R x Rp1 = R x s
-            t0 = fmaf(fmaf(R[1], sv[2], -R[2] * sv[1]), sc, t0);
-            t1 = fmaf(fmaf(R[2], sv[0], -R[0] * sv[2]), sc, t1);
-            t2 = fmaf(fmaf(R[0], sv[1], -R[1] * sv[0]), sc, t2);
-            mag += sc * slen * lR2 * ra;   // sc |R| |s| >= |w| (per component)
+            t0 = fmaf(fmaf(R1, sv[2], -R2 * sv[1]), sc, t0);
+            t1 = fmaf(fmaf(R2, sv[0], -R0 * sv[2]), sc, t1);
+            t2 = fmaf(fmaf(R0, sv[1], -R1 * sv[0]), sc, t2);
+            ms = fmaf(sc, lR2 * ra, ms);   // sc |R|; times |s| below: >= |w| (per component)
         }
+        mag = fmaf(ms, slen, mag);
         kahan_add(s0, c0, t0);
         kahan_add(s1, c1, t1);
         kahan_add(s2, c2, t2);
