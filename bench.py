@@ -632,6 +632,32 @@ def run_ours(args):
     except Exception as e:  # mixed path not built yet
         mixed = {"unavailable": str(e)[:200]}
 
+    # ---- double-single interactions (OV_PREC_DD) on the same workload
+    dd = None
+    try:
+        ctx.set_precision(abi.OV_PREC_DD)
+        ctx.upload(ht)
+        for _ in range(args.warmup):
+            ctx.update_tangle(0.0)
+        dt_ = []
+        for _ in range(args.steps):
+            ctx.flush_l2(256 << 20)
+            ctx.timer_start()
+            ctx.update_tangle(0.0)
+            dt_.append(ctx.timer_stop())
+        ctx.download(ht, abi.OV_F_VELS)
+        dst = ctx.stats()
+        per_node = np.linalg.norm(ht.vels - fp64_vels, axis=1) / np.linalg.norm(fp64_vels, axis=1)
+        dd = {"value": world * n / (statistics.mean(dt_) * 1e-3), "unit": UNIT, "ms_per_step": statistics.mean(dt_),
+              "rel_l2_vs_fp64_tree": rel_l2(ht.vels, fp64_vels), "max_node_rel_err_vs_fp64_tree": float(per_node.max()),
+              "speedup_vs_fp64": mean_ms / statistics.mean(dt_),
+              "same_decisions_as_fp64": bool(dst["accepts"] == acc and dst["visits"] == vis),
+              "arithmetic": "FP32 walk and decisions (FP64 inside guard bands), each accepted interaction and "
+                            "the sums in double-single (two floats)"}
+        ctx.set_precision(abi.OV_PREC_FP64)
+    except Exception as e:
+        dd = {"unavailable": str(e)[:200]}
+
     # ---- RK4 steps/s: update_tangle (k1) + rk4_step (three stages + combine, one CUDA graph)
     rk4 = {}
     for name, prec in (("fp64", abi.OV_PREC_FP64), ("mixed", abi.OV_PREC_MIXED)):
@@ -716,6 +742,7 @@ def run_ours(args):
         "e2e": {"value": world * n / (e2e_mean * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "mixed": mixed,
+        "double_single": dd,
         "rk4": rk4,
         "ensemble": ensemble,
         "precision_form": precision_form,

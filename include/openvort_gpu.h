@@ -88,8 +88,11 @@ void ov_params_default(ov_params *p);
 /* ------------------------------------------------------------ precision */
 enum {
     OV_PREC_FP64 = 0,   /* bit-faithful FP64 traversal (reference semantics) */
-    OV_PREC_MIXED = 1   /* FP32 traversal on grid-split positions, compensated sums,
+    OV_PREC_MIXED = 1,  /* FP32 traversal on grid-split positions, compensated sums,
                            FP64 for LIA, near field, guard-band decisions, RK4 update */
+    OV_PREC_DD = 2      /* the mixed traversal's FP32 walk and decisions, each accepted
+                           interaction and the sums in double-single (two floats, about
+                           1e-14 per operation): FP64-class accuracy at FP32 speed */
 };
 
 /* Download field mask for ov_download_tangle. */

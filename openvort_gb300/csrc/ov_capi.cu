@@ -184,7 +184,7 @@ int ov_set_rk4_graph(ov_ctx *c, int on)
 
 int ov_set_precision(ov_ctx *c, int precision)
 {
-    if (!c || (precision != OV_PREC_FP64 && precision != OV_PREC_MIXED)) return OV_ERR_ARG;
+    if (!c || (precision != OV_PREC_FP64 && precision != OV_PREC_MIXED && precision != OV_PREC_DD)) return OV_ERR_ARG;
     c->precision = precision;
     return OV_OK;
 }

@@ -58,6 +58,13 @@ struct Cell32 {          // 48 bytes: FP32 view for the mixed traversal
     int count;
 };
 
+struct CellFF {           // 64 bytes: double-single view for OV_PREC_DD
+    float g[3];          // centre of mass, grid part (exact, as in Cell32)
+    float fh[3], fl[3];  // centre of mass, the rest as hi + lo
+    float qh[3], ql[3];  // circulation, hi + lo
+    float pad;
+};
+
 // Per-member results of a forest build (tree.tt, TT_WORDS ints a member).
 enum MemberWords {
     TT_NNE = 0,   // non-EMPTY nodes
@@ -83,6 +90,7 @@ struct TreeBuf {
     int cap_cells = 0;
     Cell64 *cells = nullptr;
     Cell32 *cells32 = nullptr;
+    CellFF *cellsff = nullptr;
     int *parent = nullptr;
     int *nchild = nullptr;
     int *arrive = nullptr;

@@ -548,6 +548,30 @@ __global__ void k_root(const int *__restrict__ order, const int *__restrict__ ce
     cells[root] = r;
 }
 
+// Double-single copy of every cell's centre of mass and circulation for
+// the OV_PREC_DD law: the centre of mass as its grid part (exact in FP32)
+// plus the rest (exact in FP64) as hi + lo floats, the circulation as hi + lo.
+__global__ void k_cellsff(const Cell64 *__restrict__ cells, const int *counters, double h, double inv_h,
+                          CellFF *__restrict__ out)
+{
+    int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci >= counters[TC_NCELL]) return;
+    const Cell64 c = cells[ci];
+    const double com[3] = {c.cx, c.cy, c.cz}, q[3] = {c.qx, c.qy, c.qz};
+    CellFF o;
+    for (int a = 0; a < 3; ++a) {
+        const double G = rint(com[a] * inv_h) * h;
+        const double f = com[a] - G;
+        o.g[a] = (float)G;
+        o.fh[a] = (float)f;
+        o.fl[a] = (float)(f - (double)o.fh[a]);
+        o.qh[a] = (float)q[a];
+        o.ql[a] = (float)(q[a] - (double)o.qh[a]);
+    }
+    o.pad = 0;
+    out[ci] = o;
+}
+
 // FP32 copy of every cell for the mixed traversal: COM split into a part on
 // the grid of step h (exact in FP32) and a small remainder.
 __global__ void k_cells32(const Cell64 *__restrict__ cells, const int *counters, double h, double inv_h,
@@ -574,12 +598,13 @@ int ov_tree_reserve_cells(ov_ctx *c, int cells)
 {
     TreeBuf &t = c->tree;
     if (t.cap_cells >= cells && t.cells) return OV_OK;
-    void *ptrs[] = {t.cells, t.cells32, t.parent, t.nchild, t.arrive, t.csum};
+    void *ptrs[] = {t.cells, t.cells32, t.cellsff, t.parent, t.nchild, t.arrive, t.csum};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     t.cap_cells = cells;
     OV_CUDA(c, cudaMalloc(&t.cells, (size_t)t.cap_cells * sizeof(Cell64)));
     OV_CUDA(c, cudaMalloc(&t.cells32, (size_t)t.cap_cells * sizeof(Cell32)));
+    OV_CUDA(c, cudaMalloc(&t.cellsff, (size_t)t.cap_cells * sizeof(CellFF)));
     OV_CUDA(c, cudaMalloc(&t.parent, (size_t)t.cap_cells * 4));
     OV_CUDA(c, cudaMalloc(&t.nchild, (size_t)t.cap_cells * 4));
     OV_CUDA(c, cudaMalloc(&t.arrive, (size_t)t.cap_cells * 4));
@@ -617,7 +642,8 @@ int ov_tree_reserve(ov_ctx *c, int cap)
 void ov_tree_free(TreeBuf &t)
 {
     void *ptrs[] = {t.keys, t.keys_alt, t.order, t.order_alt, t.torder, t.cpl, t.ncell_at, t.cell_off, t.scan_tmp,
-                    t.sort_hist, t.cells, t.cells32, t.parent, t.nchild, t.arrive, t.csum, t.counters, t.tt};
+                    t.sort_hist, t.cells, t.cells32, t.cellsff, t.parent, t.nchild, t.arrive, t.csum, t.counters,
+                    t.tt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     t = TreeBuf{};
@@ -692,9 +718,14 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     k_root<<<nt, 256, 0, s>>>(t.order, t.cell_off, t.counters, t.tt, na.x, na.y, na.z, c->fwd, c->geo, g, t.cells,
                               t.csum, t.cap_cells);
     c->launches += 3;
-    if (c->precision == OV_PREC_MIXED) {
+    if (c->precision == OV_PREC_MIXED || c->precision == OV_PREC_DD) {
         k_cells32<<<(t.cap_cells + 255) / 256, 256, 0, s>>>(t.cells, t.counters, c->grid_h, 1.0 / c->grid_h,
                                                            t.cells32);
+        c->launches++;
+    }
+    if (c->precision == OV_PREC_DD) {
+        k_cellsff<<<(t.cap_cells + 255) / 256, 256, 0, s>>>(t.cells, t.counters, c->grid_h, 1.0 / c->grid_h,
+                                                           t.cellsff);
         c->launches++;
     }
     OV_CUDA(c, cudaGetLastError());

@@ -41,6 +41,7 @@ struct VelArgs {
     int G;                  // query groups per node
     const Cell64 *cells;
     const Cell32 *cells32;
+    const CellFF *cellsff;      // OV_PREC_DD: double-single cell data
     const double *x, *y, *z, *tx, *ty, *tz, *nx, *ny, *nz;
     double *vx, *vy, *vz, *sx, *sy, *sz;
     const int *fwd, *rev, *status, *pin;
@@ -54,6 +55,7 @@ struct VelArgs {
     float shift_g[OV_MAX_IMAGES][3], shift_f[OV_MAX_IMAGES][3];   // L*shift split on the grid
     int cap;                // node slots (bounds checks)
     float th2f, near2f, f4pif;   // theta^2, near-field radius^2, KAPPA/4/pi in FP32
+    float f4pi_h, f4pi_l;        // KAPPA/4/pi in double-single
     double near2;           // mixed path: squared near-field radius
     unsigned long long *stat;
 };
@@ -673,6 +675,125 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
 
 constexpr int kNearCap = 24;   // deferred near-field leaves per lane
 
+// ------------------------------------------------ double-single arithmetic
+// A value as an unevaluated sum hi + lo of two floats (about 48 bits):
+// Knuth's TwoSum, Dekker's fast TwoSum, the FMA TwoProduct, and one Newton
+// step from the hardware reciprocal (square root) for 1/x and 1/sqrt(x).
+// FP32 runs at 64 times the FP64 rate on GB300, so these reach FP64-class
+// accuracy (about 1e-14 per operation) well above FP64's speed.
+struct ff { float hi, lo; };
+
+__device__ __forceinline__ ff ff_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return ff{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ ff ff_fast(float a, float b)   // |a| >= |b|
+{
+    const float s = __fadd_rn(a, b);
+    return ff{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_add(ff x, ff y)
+{
+    ff s = ff_two_sum(x.hi, y.hi), t = ff_two_sum(x.lo, y.lo);
+    s.lo = __fadd_rn(s.lo, t.hi);
+    s = ff_fast(s.hi, s.lo);
+    s.lo = __fadd_rn(s.lo, t.lo);
+    return ff_fast(s.hi, s.lo);
+}
+// x + y without the second TwoSum (error relative to |x| + |y|): for sums
+// whose terms do not cancel (squares, positive terms, running totals)
+__device__ __forceinline__ ff ff_add_sloppy(ff x, ff y)
+{
+    ff s = ff_two_sum(x.hi, y.hi);
+    s.lo = __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo));
+    return ff_fast(s.hi, s.lo);
+}
+// x + f for a float f
+__device__ __forceinline__ ff ff_add_f(ff x, float f)
+{
+    ff s = ff_two_sum(x.hi, f);
+    s.lo = __fadd_rn(s.lo, x.lo);
+    return ff_fast(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_neg(ff x) { return ff{-x.hi, -x.lo}; }
+__device__ __forceinline__ ff ff_sub(ff x, ff y) { return ff_add(x, ff_neg(y)); }
+__device__ __forceinline__ ff ff_mul(ff x, ff y)
+{
+    const float p = __fmul_rn(x.hi, y.hi);
+    float e = __fmaf_rn(x.hi, y.hi, -p);
+    e = __fmaf_rn(x.hi, y.lo, e);
+    e = __fmaf_rn(x.lo, y.hi, e);
+    return ff_fast(p, e);
+}
+__device__ __forceinline__ ff ff_mulf(ff x, float f)
+{
+    const float p = __fmul_rn(x.hi, f);
+    float e = __fmaf_rn(x.hi, f, -p);
+    e = __fmaf_rn(x.lo, f, e);
+    return ff_fast(p, e);
+}
+__device__ __forceinline__ ff ff_from(double v)
+{
+    const float h = (float)v;
+    return ff{h, (float)(v - (double)h)};
+}
+// 1/sqrt(x), x > 0: y0 from the hardware, then y = y0 + y0 (1 - x y0^2) / 2.
+// 1 - x y0^2 is of the order of y0's error: its leading part 1 - hi is exact
+// and the rest needs float precision only.
+__device__ __forceinline__ ff ff_rsqrt(ff x)
+{
+    const float y0 = rsqrtf(x.hi);
+    const ff t = ff_mulf(ff_mulf(x, y0), y0);
+    const float r = __fsub_rn(__fsub_rn(1.0f, t.hi), t.lo);
+    return ff_fast(y0, __fmul_rn(__fmul_rn(0.5f, y0), r));
+}
+// 1/x: y = y0 + y0 (1 - x y0), the correction in float as above
+__device__ __forceinline__ ff ff_rcp(ff x)
+{
+    const float y0 = __frcp_rn(x.hi);
+    const ff t = ff_mulf(x, y0);
+    const float r = __fsub_rn(__fsub_rn(1.0f, t.hi), t.lo);
+    return ff_fast(y0, __fmul_rn(y0, r));
+}
+
+// One accepted cell in double-single: the segment law for R = COM - q,
+// Rp1 = R + circulation (sc = f4pi (1/|R| + 1/|Rp1|) / (|R| |Rp1| + R.Rp1),
+// w = (R x circulation) sc), added into the double-single sums acc[3].  The
+// query point is split like the cell: grid part gq (exact) plus fq.
+__device__ __forceinline__ void ff_law(const CellFF *cp, const float gq[3], const ff fq[3], ff f4pi, ff acc[3])
+{
+    const float4 *c4 = reinterpret_cast<const float4 *>(cp);
+    const float4 A = __ldg(c4), B = __ldg(c4 + 1), Cc = __ldg(c4 + 2), D = __ldg(c4 + 3);
+    // A = (g0, g1, g2, fh0)  B = (fh1, fh2, fl0, fl1)  Cc = (fl2, qh0, qh1, qh2)  D = (ql0, ql1, ql2, -)
+    const float gc[3] = {A.x, A.y, A.z};
+    const ff fc[3] = {ff{A.w, B.z}, ff{B.x, B.w}, ff{B.y, Cc.x}};
+    const ff q[3] = {ff{Cc.y, D.x}, ff{Cc.z, D.y}, ff{Cc.w, D.z}};
+    ff R[3], P[3];
+    for (int a = 0; a < 3; ++a) {
+        // grid parts differ exactly; the rest in double-single
+        R[a] = ff_add_f(ff_sub(fc[a], fq[a]), __fsub_rn(gc[a], gq[a]));
+        P[a] = ff_add(R[a], q[a]);
+    }
+    const ff lR2 = ff_add_sloppy(ff_add_sloppy(ff_mul(R[0], R[0]), ff_mul(R[1], R[1])), ff_mul(R[2], R[2]));
+    const ff lp2 = ff_add_sloppy(ff_add_sloppy(ff_mul(P[0], P[0]), ff_mul(P[1], P[1])), ff_mul(P[2], P[2]));
+    const ff dot = ff_add(ff_add(ff_mul(R[0], P[0]), ff_mul(R[1], P[1])), ff_mul(R[2], P[2]));
+    const ff ra = ff_rsqrt(lR2), rb = ff_rsqrt(lp2);
+    const ff ab = ff_mul(ra, rb);
+    const ff den = ff_add_f(ff_mul(dot, ab), 1.0f);
+    const ff sc = ff_mul(ff_mul(ff_mul(f4pi, ff_add_sloppy(ra, rb)), ab), ff_rcp(den));
+    const ff w[3] = {ff_sub(ff_mul(R[1], q[2]), ff_mul(R[2], q[1])), ff_sub(ff_mul(R[2], q[0]), ff_mul(R[0], q[2])),
+                     ff_sub(ff_mul(R[0], q[1]), ff_mul(R[1], q[0]))};
+    for (int a = 0; a < 3; ++a) acc[a] = ff_add_sloppy(acc[a], ff_mul(w[a], sc));
+}
+
+
+// value of a (sum, compensation) pair: Kahan's sum - compensation, or a
+// double-single's hi + lo
+__device__ __forceinline__ double acc_value(float s, float c, bool dd)
+{
+    return dd ? (double)s + (double)c : (double)s - (double)c;
+}
 
 struct MixedAcc {
     float s0, s1, s2, c0, c1, c2;   // Kahan sums over every query point
@@ -682,11 +803,15 @@ struct MixedAcc {
 // One query point (g + f split, image j; j < 0 the node itself) for the 32
 // lanes of a warp.  Near-field leaves are appended to the lane's list
 // (cell, image) and evaluated in FP64 after all query points.
+template <bool DD>
 __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], const float f[3], const double p[3],
                                            int j, bool part, int root, int ncell, MixedAcc &m, int *near_list,
                                            int &nnear,
-                                           double w64[3], bool &overflow)
-// near_list: this lane's column of a shared [kNearCap][32] array, stride 32
+                                           double w64[3], bool &overflow, const float *gqq = nullptr,
+                                           const ff *qff = nullptr)
+// near_list: this lane's column of a shared [kNearCap][32] array, stride 32.
+// DD: accepted interactions in double-single at the query point qff, summed
+// into (m.s, m.c) as (hi, lo) pairs; the near field needs no FP64 then.
 {
     const float th2 = a.th2f;
     const float near2 = a.near2f;
@@ -739,7 +864,7 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
                 const float ra = rsqrtf(d2), rb = rsqrtf(lp2);
                 const float ab = ra * rb;
                 const float nd = dot * ab;
-                const bool defer = exact || (leaf && d2 < near2) || lp2 < d2hi || fabsf(nd - 1e-8f) < 4e-6f;
+                const bool defer = exact || (!DD && leaf && d2 < near2) || lp2 < d2hi || fabsf(nd - 1e-8f) < 4e-6f;
                 if (defer) {
                     // near field, or a filter inside its guard band: FP64, after the traversal
                     ++m.nnear;
@@ -756,11 +881,19 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
                         }
                     }
                 } else if (nd >= 1e-8f) {
-                    const float sc = __fdividef(f4pi * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
-                    // R x Rp1 = R x q
-                    p0 = fmaf(fmaf(R1, qz, -R2 * qy), sc, p0);
-                    p1 = fmaf(fmaf(R2, qx, -R0 * qz), sc, p1);
-                    p2 = fmaf(fmaf(R0, qy, -R1 * qx), sc, p2);
+                    if (DD) {
+                        ff acc[3] = {ff{m.s0, m.c0}, ff{m.s1, m.c1}, ff{m.s2, m.c2}};
+                        ff_law(a.cellsff + c, gqq, qff, ff{a.f4pi_h, a.f4pi_l}, acc);
+                        m.s0 = acc[0].hi; m.c0 = acc[0].lo;
+                        m.s1 = acc[1].hi; m.c1 = acc[1].lo;
+                        m.s2 = acc[2].hi; m.c2 = acc[2].lo;
+                    } else {
+                        const float sc = __fdividef(f4pi * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
+                        // R x Rp1 = R x q
+                        p0 = fmaf(fmaf(R1, qz, -R2 * qy), sc, p0);
+                        p1 = fmaf(fmaf(R2, qx, -R0 * qz), sc, p1);
+                        p2 = fmaf(fmaf(R0, qy, -R1 * qx), sc, p2);
+                    }
                 }
                 resume = nxt;
             } else if (skip) {
@@ -770,7 +903,7 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
             }
         }
         ++steps;
-        if ((steps & 15) == 0) {   // warp-uniform
+        if (!DD && (steps & 15) == 0) {   // warp-uniform
             kahan_add(m.s0, m.c0, p0);
             kahan_add(m.s1, m.c1, p1);
             kahan_add(m.s2, m.c2, p2);
@@ -779,13 +912,15 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
         c = __any_sync(0xffffffffu, open) ? c + 1 : nxt;
         if (steps > guard_max) { overflow = true; break; }
     }
-    kahan_add(m.s0, m.c0, p0);
-    kahan_add(m.s1, m.c1, p1);
-    kahan_add(m.s2, m.c2, p2);
+    if (!DD) {
+        kahan_add(m.s0, m.c0, p0);
+        kahan_add(m.s1, m.c1, p1);
+        kahan_add(m.s2, m.c2, p2);
+    }
     m.nstep += steps;
 }
 
-template <int W, int HI>
+template <int W, int HI, bool DD>
 __global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mixed(VelArgs a,
                                                                                   double *__restrict__ part_out)
 {
@@ -842,15 +977,33 @@ __global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mix
                 }
                 MixedAcc mr = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
                 double wr[3] = {0, 0, 0};   // FP64 terms of this image when the near list is full
-                bh_query32(a, g, f, p, j, part, w.root, w.end, mr, near_list, nnear, wr, overflow);
-                double v[3] = {((double)mr.s0 - (double)mr.c0) + wr[0], ((double)mr.s1 - (double)mr.c1) + wr[1],
-                               ((double)mr.s2 - (double)mr.c2) + wr[2]};
+                ff qr[3];
+                for (int ax = 0; ax < 3; ++ax) qr[ax] = ff_from(q[ax] - rint(q[ax] * a.inv_h) * a.grid_h);
+                bh_query32<DD>(a, g, f, p, j, part, w.root, w.end, mr, near_list, nnear, wr, overflow, g, qr);
+                double v[3] = {acc_value(mr.s0, mr.c0, DD) + wr[0], acc_value(mr.s1, mr.c1, DD) + wr[1],
+                               acc_value(mr.s2, mr.c2, DD) + wr[2]};
                 for (int r = 0; r < a.geo.nreflect[j]; ++r) mirror_vec(a.geo.reflect[j][r], v);
                 img64[0] += v[0]; img64[1] += v[1]; img64[2] += v[2];
                 m.nvis += mr.nvis; m.nacc += mr.nacc; m.nstep += mr.nstep; m.nfb += mr.nfb; m.nnear += mr.nnear;
                 continue;
             }
-            bh_query32(a, g, f, p, j, part, w.root, w.end, m, near_list, nnear, w64, overflow);
+            if (DD) {
+                // the query point split as the cells are: the grid part exact, the rest
+                // (exact in FP64) in double-single
+                double q[3];
+                if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+                else image_point(a.geo, j, p, q);
+                float gq[3];
+                ff qf[3];
+                for (int ax = 0; ax < 3; ++ax) {
+                    const double G = rint(q[ax] * a.inv_h) * a.grid_h;
+                    gq[ax] = (float)G;
+                    qf[ax] = ff_from(q[ax] - G);
+                }
+                bh_query32<DD>(a, g, f, p, j, part, w.root, w.end, m, near_list, nnear, w64, overflow, gq, qf);
+            } else {
+                bh_query32<DD>(a, g, f, p, j, part, w.root, w.end, m, near_list, nnear, w64, overflow);
+            }
         }
         // deferred near-field interactions, all lanes together
         for (int i = 0; i < nnear && i < kNearCap; ++i) {
@@ -868,9 +1021,9 @@ __global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mix
             }
         }
         __syncwarp();   // the list is rewritten by the next item
-        double bh[3] = {((double)m.s0 - (double)m.c0) + w64[0] + img64[0],
-                        ((double)m.s1 - (double)m.c1) + w64[1] + img64[1],
-                        ((double)m.s2 - (double)m.c2) + w64[2] + img64[2]};
+        double bh[3] = {acc_value(m.s0, m.c0, DD) + w64[0] + img64[0],
+                        acc_value(m.s1, m.c1, DD) + w64[1] + img64[1],
+                        acc_value(m.s2, m.c2, DD) + w64[2] + img64[2]};
         if (valid) {
             const size_t cap = (size_t)a.cap;
             for (int ax = 0; ax < 3; ++ax) {
@@ -927,6 +1080,7 @@ VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long 
     a.counters = c->tree.counters;
     a.cells = c->tree.cells;
     a.cells32 = c->tree.cells32;
+    a.cellsff = c->tree.cellsff;
     a.x = na.x; a.y = na.y; a.z = na.z;
     a.tx = na.tx; a.ty = na.ty; a.tz = na.tz;
     a.nx = na.nx; a.ny = na.ny; a.nz = na.nz;
@@ -964,6 +1118,8 @@ VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long 
     a.th2f = (float)(a.prm.theta * a.prm.theta);
     a.near2f = (float)a.near2;
     a.f4pif = (float)a.f4pi;
+    a.f4pi_h = (float)a.f4pi;
+    a.f4pi_l = (float)(a.f4pi - (double)a.f4pi_h);
     return a;
 }
 
@@ -995,13 +1151,18 @@ static VelKernel vel_kernel(int precision, int warps, int hi_occ)
 {
     if (precision == OV_PREC_MIXED) {
         if (hi_occ) {
-            if (warps == 2) return k_vel_mixed<2, 1>;
-            if (warps == 8) return k_vel_mixed<8, 1>;
-            return k_vel_mixed<4, 1>;
+            if (warps == 2) return k_vel_mixed<2, 1, false>;
+            if (warps == 8) return k_vel_mixed<8, 1, false>;
+            return k_vel_mixed<4, 1, false>;
         }
-        if (warps == 2) return k_vel_mixed<2, 0>;
-        if (warps == 8) return k_vel_mixed<8, 0>;
-        return k_vel_mixed<4, 0>;
+        if (warps == 2) return k_vel_mixed<2, 0, false>;
+        if (warps == 8) return k_vel_mixed<8, 0, false>;
+        return k_vel_mixed<4, 0, false>;
+    }
+    if (precision == OV_PREC_DD) {
+        if (warps == 2) return k_vel_mixed<2, 0, true>;
+        if (warps == 8) return k_vel_mixed<8, 0, true>;
+        return k_vel_mixed<4, 0, true>;
     }
     if (warps == 2) return k_vel_fp64<2>;
     if (warps == 8) return k_vel_fp64<8>;
@@ -2134,7 +2295,7 @@ __global__ void __launch_bounds__(128) k_sph_query_mixed(SphArgs s, double *__re
     double w64[3] = {0, 0, 0};
     int nnear = 0;
     bool overflow = false;
-    bh_query32(a, g, f, qp, -1, go, root, end, acc, near_list, nnear, w64, overflow);
+    bh_query32<false>(a, g, f, qp, -1, go, root, end, acc, near_list, nnear, w64, overflow);
     for (int i = 0; i < nnear && i < kNearCap; ++i) {
         const int e = near_list[32 * i];
         const int c = e >> 5;

@@ -60,3 +60,22 @@ def test_mixed_rk4_and_edge_cases():
         out.append(np.array(h.pos))
     start = W.random_walk_tangle(16, 64, D=0.1, seed=50).pos
     assert rel_l2(out[1] - start, out[0] - start) < MIXED_TOL
+
+
+@pytest.mark.parametrize("n_loops,theta,images", [(256, 0.4, None), (1024, 0.3, None), (64, 0.4, "wall_2_4")])
+def test_double_single_vs_fp64_tree(n_loops, theta, images):
+    """OV_PREC_DD: the mixed walk's decisions with every accepted interaction
+    and the sums in double-single: within 1e-10 of the FP64 tree per node and
+    1e-12 in relative L2."""
+    base = W.random_walk_tangle(n_loops, 256, D=0.1, seed=1)
+    ht = base if images is None else W.HostTangle(base.pos.copy(), base.conn[:, 0].copy(), base.conn[:, 1].copy(),
+                                                   base.box_lo, base.box_hi, image_set=images)
+    p = W.config_params("rw", bh_resolution=theta)
+    v64, s64, st64 = _eval(ht, p, abi.OV_PREC_FP64)
+    vdd, sdd, stdd = _eval(ht, p, abi.OV_PREC_DD)
+    assert stdd["error_word"] == 0
+    assert stdd["accepts"] == st64["accepts"] and stdd["visits"] == st64["visits"]
+    per_node = np.linalg.norm(vdd - v64, axis=1) / np.linalg.norm(v64, axis=1)
+    assert per_node.max() < 1e-10
+    assert rel_l2(vdd, v64) < 1e-12
+    assert rel_l2(sdd, s64) < 1e-12
