@@ -761,6 +761,24 @@ __device__ __forceinline__ ff ff_rcp(ff x)
 // Rp1 = R + circulation (sc = f4pi (1/|R| + 1/|Rp1|) / (|R| |Rp1| + R.Rp1),
 // w = (R x circulation) sc), added into the double-single sums acc[3].  The
 // query point is split like the cell: grid part gq (exact) plus fq.
+// The segment law for R (start - query) and S (segment vector) in
+// double-single: w = (R x S) f4pi (1/|R| + 1/|R+S|) / (|R| |R+S| + R.(R+S)).
+__device__ __forceinline__ void ff_segment(const ff R[3], const ff S[3], ff f4pi, ff w[3])
+{
+    ff P[3];
+    for (int a = 0; a < 3; ++a) P[a] = ff_add(R[a], S[a]);
+    const ff lR2 = ff_add_sloppy(ff_add_sloppy(ff_mul(R[0], R[0]), ff_mul(R[1], R[1])), ff_mul(R[2], R[2]));
+    const ff lp2 = ff_add_sloppy(ff_add_sloppy(ff_mul(P[0], P[0]), ff_mul(P[1], P[1])), ff_mul(P[2], P[2]));
+    const ff dot = ff_add(ff_add(ff_mul(R[0], P[0]), ff_mul(R[1], P[1])), ff_mul(R[2], P[2]));
+    const ff ra = ff_rsqrt(lR2), rb = ff_rsqrt(lp2);
+    const ff ab = ff_mul(ra, rb);
+    const ff den = ff_add_f(ff_mul(dot, ab), 1.0f);
+    const ff sc = ff_mul(ff_mul(ff_mul(f4pi, ff_add_sloppy(ra, rb)), ab), ff_rcp(den));
+    const ff x[3] = {ff_sub(ff_mul(R[1], S[2]), ff_mul(R[2], S[1])), ff_sub(ff_mul(R[2], S[0]), ff_mul(R[0], S[2])),
+                     ff_sub(ff_mul(R[0], S[1]), ff_mul(R[1], S[0]))};
+    for (int a = 0; a < 3; ++a) w[a] = ff_mul(x[a], sc);
+}
+
 __device__ __forceinline__ void ff_law(const CellFF *cp, const float gq[3], const ff fq[3], ff f4pi, ff acc[3])
 {
     const float4 *c4 = reinterpret_cast<const float4 *>(cp);
@@ -1315,6 +1333,8 @@ struct RecArgs {
     Geometry geo;
     float shift_g[OV_MAX_IMAGES][3], shift_f[OV_MAX_IMAGES][3];
     float Lg[3], Lf[3], hL[3];   // period split on the grid, half period
+    float Lfl[3];             // the rest of Lf (Lf + Lfl = L - Lg to double-single precision)
+    double inv_h, grid_h;     // the grid step of the split
     double f4pi;
     float f4pif;
     float rnear2;             // squared FP64 radius
@@ -1333,8 +1353,10 @@ __global__ void k_split(const double *__restrict__ x, const double *__restrict__
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         double G = rint(p[a] * inv_h) * h;
+        const float fh = (float)(p[a] - G);
         sp[(size_t)a * cap + i] = (float)G;
-        sp[(size_t)(3 + a) * cap + i] = (float)(p[a] - G);
+        sp[(size_t)(3 + a) * cap + i] = fh;
+        sp[(size_t)(6 + a) * cap + i] = (float)((p[a] - G) - (double)fh);   // the rest, for double-single
     }
 }
 
@@ -1396,12 +1418,14 @@ __device__ __forceinline__ bool rec_term64_fast(const RecArgs &r, int m, int f, 
 constexpr int kRecThreads = 256;
 constexpr int kRecVals = 7;   // 3 sums, FP32 magnitude, 3 spare (|FP64 terms|)
 
+template <int MODE>
 __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const int *__restrict__ nodes, int n,
-                                                          int span, int max_chunks, int force64,
-                                                          double *__restrict__ part)
+                                                          int span, int max_chunks, double *__restrict__ part)
+// MODE: 0 FP32 far / FP64 near, 1 all FP64, 2 double-single far / FP64 near
 {
-    // split query points (self, then images): (g, mirror flag), (f, 0)
-    __shared__ float4 s_q[OV_MAX_IMAGES + 1][2];
+    constexpr int force64 = MODE;
+    // split query points (self, then images): (g, mirror flag), (f, 0), (f's rest, 0)
+    __shared__ float4 s_q[OV_MAX_IMAGES + 1][3];
     __shared__ double red[kRecVals][kRecThreads];
     const int b = blockIdx.x, chunk = blockIdx.y;
     if (b >= n) return;
@@ -1418,41 +1442,66 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
     const int nq = r.geo.n_img + 1;
     if (threadIdx.x < nq) {
         const int j = (int)threadIdx.x - 1;
-        float g[3], f[3];
+        float g[3], f[3], fl[3] = {0, 0, 0};
+        if (MODE == 2) {
+            // double-single: the query point in FP64, split on the grid exactly
+            double q[3];
+            if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+            else image_point(r.geo, j, p, q);
+            for (int a = 0; a < 3; ++a) {
+                const double G = rint(q[a] * r.inv_h) * r.grid_h;
+                g[a] = (float)G;
+                f[a] = (float)(q[a] - G);
+                fl[a] = (float)((q[a] - G) - (double)f[a]);
+            }
+        } else {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            g[a] = r.sp[(size_t)a * r.cap + k];
-            f[a] = r.sp[(size_t)(3 + a) * r.cap + k];
-            if (j >= 0) { g[a] -= r.shift_g[j][a]; f[a] -= r.shift_f[j][a]; }
+            for (int a = 0; a < 3; ++a) {
+                g[a] = r.sp[(size_t)a * r.cap + k];
+                f[a] = r.sp[(size_t)(3 + a) * r.cap + k];
+                if (j >= 0) { g[a] -= r.shift_g[j][a]; f[a] -= r.shift_f[j][a]; }
+            }
         }
-        // mirror images (reflected query points): FP64, as the split shift tables hold translations only
-        const float mirror = (j >= 0 && r.geo.nreflect[j] > 0) ? 1.0f : 0.0f;
+        // mirror images (reflected query points): FP64 unless double-single
+        const float mirror = (force64 != 2 && j >= 0 && r.geo.nreflect[j] > 0) ? 1.0f : 0.0f;
         s_q[threadIdx.x][0] = make_float4(g[0], g[1], g[2], mirror);
         s_q[threadIdx.x][1] = make_float4(f[0], f[1], f[2], 0.0f);
+        s_q[threadIdx.x][2] = make_float4(fl[0], fl[1], fl[2], 0.0f);
     }
     __syncthreads();
     float s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0, mag = 0;
     double d0 = 0, d1 = 0, d2 = 0, dabs = 0;
+    ff dd[3] = {ff{0, 0}, ff{0, 0}, ff{0, 0}};   // double-single terms (mode 2)
+    float magdd = 0;
+    const ff f4pi_ff = ff{r.f4pif, (float)(r.f4pi - (double)r.f4pif)};
     const float eps_band = 1e-3f;
     for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
         const int f = r.fwd[m];
         if (f < 0 || f >= r.cap) continue;
         float ag[3], af[3], sv[3];
-        bool seg64 = force64 != 0;
+        ff fa[3], S[3];   // mode 2: the start's rest and the segment vector in double-single
+        bool seg64 = force64 == 1;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             ag[a] = r.sp[(size_t)a * r.cap + m];
             af[a] = r.sp[(size_t)(3 + a) * r.cap + m];
             float bg = r.sp[(size_t)a * r.cap + f], bf = r.sp[(size_t)(3 + a) * r.cap + f];
             float d = (bg - ag[a]) + (bf - af[a]);
+            int ws = 0;
             if (r.geo.periodic[a]) {
                 // seg_pwrap: the end moved by a period toward the start
                 if (fabsf(fabsf(d) - r.hL[a]) < eps_band * r.hL[a]) seg64 = true;
-                if (d > r.hL[a]) { bg -= r.Lg[a]; bf -= r.Lf[a]; }
-                else if (d < -r.hL[a]) { bg += r.Lg[a]; bf += r.Lf[a]; }
+                if (d > r.hL[a]) { bg -= r.Lg[a]; bf -= r.Lf[a]; ws = -1; }
+                else if (d < -r.hL[a]) { bg += r.Lg[a]; bf += r.Lf[a]; ws = 1; }
                 if (fabsf(d) > 3.0f * r.hL[a]) seg64 = true;   // more than one period: FP64 loop
             }
             sv[a] = (bg - ag[a]) + (bf - af[a]);
+            if (MODE == 2) {
+                fa[a] = ff{af[a], r.sp[(size_t)(6 + a) * r.cap + m]};
+                ff fb = ff{r.sp[(size_t)(3 + a) * r.cap + f], r.sp[(size_t)(6 + a) * r.cap + f]};
+                if (ws) fb = ff_add(fb, ff{ws * r.Lf[a], ws * r.Lfl[a]});
+                S[a] = ff_add_f(ff_sub(fb, fa[a]), __fsub_rn(bg, ag[a]));   // grid parts exact (wrapped bg)
+            }
         }
         const float slen = sqrtf(fmaf(sv[0], sv[0], fmaf(sv[1], sv[1], sv[2] * sv[2])));
         const bool own = (m == k || f == k);   // the node's own segments: skipped at the primary point
@@ -1479,13 +1528,23 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
             if (use64) {
                 double w[3];
                 const int j = qi - 1;
-                if (force64 ? rec_term64_fast(r, m, f, j, p, w) : rec_term64(r, m, f, j, p, w)) {
+                if (force64 == 1 ? rec_term64_fast(r, m, f, j, p, w) : rec_term64(r, m, f, j, p, w)) {
                     d0 += w[0]; d1 += w[1]; d2 += w[2];
                     dabs += fabs(w[0]) + fabs(w[1]) + fabs(w[2]);
                 }
                 continue;
             }
             if (nd < 1e-8f) continue;   // ndot filter (far from its threshold here)
+            if (MODE == 2) {
+                const float4 qfl = s_q[qi][2];
+                const float gq[3] = {qg.x, qg.y, qg.z}, fqh[3] = {qf.x, qf.y, qf.z}, fql[3] = {qfl.x, qfl.y, qfl.z};
+                ff Rd[3], w[3];
+                for (int a = 0; a < 3; ++a) Rd[a] = ff_add_f(ff_sub(fa[a], ff{fqh[a], fql[a]}), __fsub_rn(ag[a], gq[a]));
+                ff_segment(Rd, S, f4pi_ff, w);
+                for (int a = 0; a < 3; ++a) dd[a] = ff_add(dd[a], w[a]);
+                magdd += fabsf(w[0].hi) + fabsf(w[1].hi) + fabsf(w[2].hi);
+                continue;
+            }
             const float sc = __fdividef(r.f4pif * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
             // R x Rp1 = R x s
             t0 = fmaf(fmaf(R1, sv[2], -R2 * sv[1]), sc, t0);
@@ -1498,13 +1557,13 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
         kahan_add(s1, c1, t1);
         kahan_add(s2, c2, t2);
     }
-    red[0][threadIdx.x] = ((double)s0 - (double)c0) + d0;
-    red[1][threadIdx.x] = ((double)s1 - (double)c1) + d1;
-    red[2][threadIdx.x] = ((double)s2 - (double)c2) + d2;
+    red[0][threadIdx.x] = ((double)s0 - (double)c0) + d0 + ((double)dd[0].hi + (double)dd[0].lo);
+    red[1][threadIdx.x] = ((double)s1 - (double)c1) + d1 + ((double)dd[1].hi + (double)dd[1].lo);
+    red[2][threadIdx.x] = ((double)s2 - (double)c2) + d2 + ((double)dd[2].hi + (double)dd[2].lo);
     red[3][threadIdx.x] = (double)mag;
     red[4][threadIdx.x] = dabs;
     red[5][threadIdx.x] = fabs((double)s0) + fabs((double)s1) + fabs((double)s2);
-    red[6][threadIdx.x] = 0.0;
+    red[6][threadIdx.x] = (double)magdd;
     __syncthreads();
     for (int off = blockDim.x / 2; off > 0; off >>= 1) {
         if (threadIdx.x < off)
@@ -1526,8 +1585,11 @@ __global__ void k_rec_finish(const double *__restrict__ part, int n, int max_chu
         for (int v = 0; v < kRecVals; ++v) acc[v] += part[((size_t)b * max_chunks + ch) * kRecVals + v];
     const double eps32 = 5.9604644775390625e-8;
     for (int a = 0; a < 3; ++a) out[5 * (size_t)b + a] = acc[a];
-    out[5 * (size_t)b + 3] = 1.01 * ((64.0 + 28.0) * eps32 * acc[3] + 4.0 * eps32 * acc[5]) + 1e-12 * (acc[4] + acc[3]);
-    out[5 * (size_t)b + 4] = 1.01 * (acc[3] + acc[4]);
+    // double-single terms (acc[6]: their magnitudes): 1e-10 of each covers the
+    // law's error (about 1e-13) and their running sums with a wide margin
+    out[5 * (size_t)b + 3] = 1.01 * ((64.0 + 28.0) * eps32 * acc[3] + 4.0 * eps32 * acc[5]) + 1e-12 * (acc[4] + acc[3]) +
+                             1.01e-10 * acc[6];
+    out[5 * (size_t)b + 4] = 1.01 * (acc[3] + acc[4] + acc[6]);
 }
 
 struct RecChange {
@@ -1644,10 +1706,13 @@ RecArgs make_rec_args(ov_ctx *c)
         double G = rint(c->geo.L[a] / h) * h;
         r.Lg[a] = (float)G;
         r.Lf[a] = (float)(c->geo.L[a] - G);
+        r.Lfl[a] = (float)((c->geo.L[a] - G) - (double)r.Lf[a]);
         r.hL[a] = (float)(c->geo.L[a] * 0.5);
     }
     r.f4pi = c->params.kappa / 4 / M_PI;
     r.f4pif = (float)r.f4pi;
+    r.grid_h = h;
+    r.inv_h = 1.0 / h;
     // FP64 within 4 dl_max (segments are shorter than 2 dl_max after remesh)
     double dl = 0;
     for (const Member &m : c->mem) dl = std::max(dl, m.params.dl_max);
@@ -1685,13 +1750,14 @@ int rec_reserve(ov_ctx *c, int n, int max_chunks)
     if (c->rec_split_cap < c->cap) {
         if (c->rec_split) cudaFree(c->rec_split);
         c->rec_split = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->rec_split, (size_t)c->cap * 6 * sizeof(float)));
+        OV_CUDA(c, cudaMalloc(&c->rec_split, (size_t)c->cap * 9 * sizeof(float)));
         c->rec_split_cap = c->cap;
     }
     return OV_OK;
 }
 
-int rec_launch_sums(ov_ctx *c, const int *d_nodes, int n, bool force64, double *out_host)
+// mode: 0 mixed (FP32 far, FP64 near), 1 FP64, 2 double-single far, FP64 near
+int rec_launch_sums(ov_ctx *c, const int *d_nodes, int n, int mode, double *out_host)
 {
     int maxcap = 0;
     for (const Member &m : c->mem) maxcap = std::max(maxcap, c->mem.size() == 1 ? c->cap : m.cap);
@@ -1701,7 +1767,12 @@ int rec_launch_sums(ov_ctx *c, const int *d_nodes, int n, bool force64, double *
     if (r) return r;
     RecArgs ra = make_rec_args(c);
     dim3 grid(n, max_chunks);
-    k_rec_sums<<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, force64 ? 1 : 0, c->rec_part);
+    if (mode == 1)
+        k_rec_sums<1><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
+    else if (mode == 2)
+        k_rec_sums<2><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
+    else
+        k_rec_sums<0><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
     k_rec_finish<<<(n + 127) / 128, 128, 0, c->stream>>>(c->rec_part, n, max_chunks, c->rec_out);
     c->launches += 2;
     OV_CUDA(c, cudaGetLastError());
@@ -1728,23 +1799,33 @@ int ov_rec_begin(ov_ctx *c, const int *cand, int n, double *out)
     k_split<<<(c->cap + 255) / 256, 256, 0, c->stream>>>(c->node.x, c->node.y, c->node.z, c->cap, c->grid_h,
                                                         1.0 / c->grid_h, c->rec_split);
     c->launches++;
-    return rec_launch_sums(c, c->rec_nodes, n, false, out);
+    return rec_launch_sums(c, c->rec_nodes, n, 0, out);
 }
 
-// FP64 sums (every term in FP64) of nodes k and l, laid out as ov_rec_begin's.
+// Tight sums of nodes k and l on the current device positions and
+// connections, laid out as ov_rec_begin's: far terms in double-single (bound
+// 1e-10 of their magnitudes), near ones in FP64.
 int ov_rec_exact(ov_ctx *c, int k, int l, double out[10])
 {
     int nodes[2] = {k, l};
+    int maxcap = 0;
+    for (const Member &m : c->mem) maxcap = std::max(maxcap, c->mem.size() == 1 ? c->cap : m.cap);
+    int r = rec_reserve(c, 2, std::max(1, (maxcap + 8191) / 8192));
+    if (r) return r;
     if (!c->rec_pair) OV_CUDA(c, cudaMalloc(&c->rec_pair, 2 * sizeof(int)));
     OV_CUDA(c, cudaMemcpyAsync(c->rec_pair, nodes, 2 * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    return rec_launch_sums(c, c->rec_pair, 2, true, out);
+    // the split positions of the current device positions
+    k_split<<<(c->cap + 255) / 256, 256, 0, c->stream>>>(c->node.x, c->node.y, c->node.z, c->cap, c->grid_h,
+                                                        1.0 / c->grid_h, c->rec_split);
+    c->launches++;
+    return rec_launch_sums(c, c->rec_pair, 2, 2, out);
 }
 
 extern "C" int ov_direct_sums_bounded(ov_ctx *c, const int *nodes, int n, int precision, double *out)
 {
     if (!c || n < 0 || (n > 0 && (!nodes || !out))) return OV_ERR_ARG;
     if (!c->uploaded) return ov_fail(c, OV_ERR_STATE, "no tangle uploaded");
-    if (precision != OV_PREC_FP64 && precision != OV_PREC_MIXED) return OV_ERR_ARG;
+    if (precision != OV_PREC_FP64 && precision != OV_PREC_MIXED && precision != OV_PREC_DD) return OV_ERR_ARG;
     cudaSetDevice(c->device);
     for (int i = 0; i < n; ++i)
         if (nodes[i] < 0 || nodes[i] >= c->cap) return ov_fail(c, OV_ERR_ARG, "node %d out of range", nodes[i]);
@@ -1757,7 +1838,7 @@ extern "C" int ov_direct_sums_bounded(ov_ctx *c, const int *nodes, int n, int pr
     k_split<<<(c->cap + 255) / 256, 256, 0, c->stream>>>(c->node.x, c->node.y, c->node.z, c->cap, c->grid_h,
                                                         1.0 / c->grid_h, c->rec_split);
     c->launches++;
-    return rec_launch_sums(c, c->rec_nodes, n, precision == OV_PREC_FP64, out);
+    return rec_launch_sums(c, c->rec_nodes, n, precision == OV_PREC_FP64 ? 1 : (precision == OV_PREC_DD ? 2 : 0), out);
 }
 
 // ov_direct_velocities: FP64 direct sums in (node, segment chunk) blocks,
@@ -1773,8 +1854,8 @@ int ov_direct_sum_chunked(ov_ctx *c, const int *nodes, int n, double *d_out_vel,
     k_split<<<(c->cap + 255) / 256, 256, 0, c->stream>>>(c->node.x, c->node.y, c->node.z, c->cap, c->grid_h,
                                                         1.0 / c->grid_h, c->rec_split);
     RecArgs ra = make_rec_args(c);
-    k_rec_sums<<<dim3(n, max_chunks), kRecThreads, 0, c->stream>>>(ra, c->rec_nodes, n, span, max_chunks, 1,
-                                                                   c->rec_part);
+    k_rec_sums<1><<<dim3(n, max_chunks), kRecThreads, 0, c->stream>>>(ra, c->rec_nodes, n, span, max_chunks,
+                                                                      c->rec_part);
     k_rec_finish<<<(n + 127) / 128, 128, 0, c->stream>>>(c->rec_part, n, max_chunks, c->rec_out);
     VelArgs a = make_args(c, c->node, t, nullptr);
     k_direct_finish<<<(n + 127) / 128, 128, 0, c->stream>>>(a, c->rec_nodes, n, c->rec_out, 5, d_out_vel, d_out_vs);

@@ -136,10 +136,16 @@ def test_reconnect_sums_within_their_bound(n_loops, D):
     nodes = np.arange(0, ht.n, max(1, ht.n // 300))
     s32, b32, mag = ctx.direct_sums_bounded(nodes, abi.OV_PREC_MIXED)
     s64, b64, _ = ctx.direct_sums_bounded(nodes, abi.OV_PREC_FP64)
+    # double-single far terms: the refinement reconnect uses for undecided pairs
+    sdd, bdd, _ = ctx.direct_sums_bounded(nodes, abi.OV_PREC_DD)
     ctx.close()
     err = np.abs(s32 - s64).max(axis=1)
     assert np.all(err <= b32 + b64), (err / b32).max()
     assert np.all(b32 > 0) and np.all(b32 < 1e-4 * mag + 1e-300)
+    err_dd = np.abs(sdd - s64).max(axis=1)
+    assert np.all(err_dd <= bdd + b64), (err_dd / bdd).max()
+    assert np.all(bdd < 2e-10 * mag + 1e-300)
+    assert np.all(err_dd <= 1e-3 * bdd + b64)   # the bound is loose by orders of magnitude
     # with zero tangents/normals (as uploaded) and no v_s, the oracle's
     # update_velocity(k, NULL) is the nonlocal sum alone
     assert not ht.tangents.any() and not ht.normals.any()
