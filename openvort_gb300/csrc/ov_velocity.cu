@@ -1507,6 +1507,7 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
         const bool own = (m == k || f == k);   // the node's own segments: skipped at the primary point
         float t0 = 0, t1 = 0, t2 = 0;   // this segment's terms over the query points
         float ms = 0;                   // sum over the query points of sc |R|
+        unsigned mask64 = 0;            // query points whose term is done in FP64
         for (int qi = own ? 1 : 0; qi < nq; ++qi) {
             const float4 qg = s_q[qi][0], qf = s_q[qi][1];
             const float R0 = (ag[0] - qg.x) + (af[0] - qf.x);
@@ -1525,13 +1526,8 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
                 nd = dot * ab;
                 if (fabsf(nd - 1e-8f) < 1e-4f) use64 = true;   // filter near its threshold
             }
-            if (use64) {
-                double w[3];
-                const int j = qi - 1;
-                if (force64 == 1 ? rec_term64_fast(r, m, f, j, p, w) : rec_term64(r, m, f, j, p, w)) {
-                    d0 += w[0]; d1 += w[1]; d2 += w[2];
-                    dabs += fabs(w[0]) + fabs(w[1]) + fabs(w[2]);
-                }
+            if (use64) {   // FP64 after the loop over the query points
+                mask64 |= 1u << qi;
                 continue;
             }
             if (nd < 1e-8f) continue;   // ndot filter (far from its threshold here)
@@ -1551,6 +1547,14 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
             t1 = fmaf(fmaf(R2, sv[0], -R0 * sv[2]), sc, t1);
             t2 = fmaf(fmaf(R0, sv[1], -R1 * sv[0]), sc, t2);
             ms = fmaf(sc, lR2 * ra, ms);   // sc |R|; times |s| below: >= |w| (per component)
+        }
+        for (; mask64; mask64 &= mask64 - 1) {
+            const int j = __ffs(mask64) - 2;
+            double w[3];
+            if (force64 == 1 ? rec_term64_fast(r, m, f, j, p, w) : rec_term64(r, m, f, j, p, w)) {
+                d0 += w[0]; d1 += w[1]; d2 += w[2];
+                dabs += fabs(w[0]) + fabs(w[1]) + fabs(w[2]);
+            }
         }
         mag = fmaf(ms, slen, mag);
         kahan_add(s0, c0, t0);
