@@ -1508,6 +1508,7 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
         float t0 = 0, t1 = 0, t2 = 0;   // this segment's terms over the query points
         float ms = 0;                   // sum over the query points of sc |R|
         unsigned mask64 = 0;            // query points whose term is done in FP64
+#pragma unroll 3
         for (int qi = own ? 1 : 0; qi < nq; ++qi) {
             const float4 qg = s_q[qi][0], qf = s_q[qi][1];
             const float R0 = (ag[0] - qg.x) + (af[0] - qf.x);
