@@ -584,7 +584,7 @@ def run_ours(args):
 
     # ---- roofline of the dominant kernel (the FP64 traversal: FMA-pipe bound)
     acc, vis = st["accepts"], st["visits"]
-    flops = 42 * acc + 9 * vis                      # algorithmic FP ops per launch (fixed convention)
+    flops = 42 * acc        # FP64 flops per launch (fixed convention; the walk's tests run in FP32)
     trav_s = phases[2] * 1e-3
     achieved = flops / trav_s / 1e12
     fp64_peak = ctx.fma_peak_tflops(abi.OV_PREC_FP64)
@@ -603,6 +603,36 @@ def run_ours(args):
     d2h = n * 3 * 8
 
     fp64_vels = np.array(ht.vels)   # the FP64 tree's velocities (accuracy check at the end)
+
+    # ---- the FP64 path with every walk test in FP64 (OV_WALK_FP64), for comparison
+    walk64 = None
+    try:
+        ctx.set_walk(abi.OV_WALK_FP64)
+        ctx.upload(ht)
+        for _ in range(args.warmup):
+            ctx.update_tangle(0.0)
+        wt, wp = [], []
+        for _ in range(args.steps):
+            ctx.flush_l2(256 << 20)
+            ctx.timer_start()
+            ctx.update_tangle(0.0)
+            wt.append(ctx.timer_stop())
+            wp.append(ctx.phase_times()[2])
+        ctx.download(ht, abi.OV_F_VELS)
+        wst = ctx.stats()
+        per_node = np.linalg.norm(ht.vels - fp64_vels, axis=1) / np.linalg.norm(fp64_vels, axis=1)
+        walk64 = {"value": world * n / (statistics.mean(wt) * 1e-3), "unit": UNIT, "ms_per_step": statistics.mean(wt),
+                  "traversal_ms": statistics.mean(wp),
+                  "split_walk_speedup": statistics.mean(wt) / mean_ms,
+                  "same_decisions": bool(wst["accepts"] == st["accepts"] and wst["visits"] == st["visits"]),
+                  "max_node_rel_diff": float(per_node.max()),
+                  "arithmetic": "every distance and opening test in FP64 with the reference's rounding, each "
+                                "accepted cell evaluated where the walk meets it"}
+        ctx.set_walk(abi.OV_WALK_SPLIT)
+        ctx.upload(ht)
+        ctx.update_tangle(0.0)
+    except Exception as e:
+        walk64 = {"unavailable": str(e)[:200]}
 
     # ---- mixed precision on the same workload (reported beside FP64)
     mixed = None
@@ -733,7 +763,7 @@ def run_ours(args):
                      "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": K_VEL_FP64_DRAM_BYTES,
                      "traffic_note": "DRAM bytes per launch from ncu; the traversal is FP64-pipe bound",
                      "peak_source": "measured in this run (FP64 FMA chains, all SMs)",
-                     "work": "42 flops per accepted interaction + 9 per visited cell",
+                     "work": "42 FP64 flops per accepted interaction (the walk's tests run in FP32)",
                      "accepts": acc, "visits": vis, "fp32_fma_peak_tflops": fp32_peak,
                      "warp_efficiency": vis / max(1, 32 * st["warp_steps"])},
         "accuracy": {"fp64_tree_rel_l2_vs_direct_subsample": fp64_vs_direct,
@@ -743,6 +773,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h},
         "mixed": mixed,
         "double_single": dd,
+        "fp64_walk": walk64,
         "rk4": rk4,
         "ensemble": ensemble,
         "precision_form": precision_form,

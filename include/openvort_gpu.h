@@ -87,7 +87,8 @@ void ov_params_default(ov_params *p);
 
 /* ------------------------------------------------------------ precision */
 enum {
-    OV_PREC_FP64 = 0,   /* bit-faithful FP64 traversal (reference semantics) */
+    OV_PREC_FP64 = 0,   /* FP64 traversal: the reference's decisions, FP64 interactions
+                           (reference semantics; walk arithmetic: ov_set_walk) */
     OV_PREC_MIXED = 1,  /* FP32 traversal on grid-split positions, compensated sums,
                            FP64 for LIA, near field, guard-band decisions, RK4 update */
     OV_PREC_DD = 2      /* the mixed traversal's FP32 walk and decisions, each accepted
@@ -134,6 +135,17 @@ int ov_ctx_destroy(ov_ctx *ctx);
 const char *ov_last_error(const ov_ctx *ctx);
 int ov_set_params(ov_ctx *ctx, const ov_params *p);
 int ov_set_precision(ov_ctx *ctx, int precision);
+/* How OV_PREC_FP64 walks the tree.  Both give the FP64 decisions (which
+   cells each node accepts, skips and opens) and FP64 interactions. */
+enum {
+    OV_WALK_SPLIT = 0,  /* default: the distance and opening tests in FP32 on
+                           grid-split positions, the FP64 test inside their guard
+                           bands; accepted cells evaluated in FP64 by full warps */
+    OV_WALK_FP64 = 1    /* every test in FP64 with the reference's rounding, each
+                           accepted cell evaluated where the walk meets it */
+};
+int ov_set_walk(ov_ctx *ctx, int walk);
+int ov_get_walk(const ov_ctx *ctx);
 /* RK4 steps run as one captured CUDA graph (default on); off launches the
    same kernels one by one (identical results). */
 int ov_set_rk4_graph(ov_ctx *ctx, int on);

@@ -15,6 +15,9 @@ OV_EMPTY, OV_FREE, OV_PINNED, OV_PINNED_SLIP = -1, 0, 1, 2
 OV_WALL_OPEN, OV_WALL_PERIODIC, OV_WALL_MIRROR = 0, 1, 2
 OV_NO_FLOW, OV_SIMPLE, OV_DECREASING = 0, 1, 2
 OV_PREC_FP64, OV_PREC_MIXED, OV_PREC_DD = 0, 1, 2
+# OV_PREC_FP64's tree walk: FP32 tests on split positions with FP64 inside
+# guard bands (default), or every test in FP64
+OV_WALK_SPLIT, OV_WALK_FP64 = 0, 1
 OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS, OV_F_TOPOLOGY, OV_F_ALL = 1, 2, 4, 8, 16, 32, 63
 
 STATUS_NAMES = {

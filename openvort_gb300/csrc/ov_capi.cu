@@ -189,6 +189,15 @@ int ov_set_precision(ov_ctx *c, int precision)
     return OV_OK;
 }
 
+int ov_set_walk(ov_ctx *c, int walk)
+{
+    if (!c || (walk != OV_WALK_SPLIT && walk != OV_WALK_FP64)) return OV_ERR_ARG;
+    c->walk = walk;
+    return OV_OK;
+}
+
+int ov_get_walk(const ov_ctx *c) { return c ? c->walk : -1; }
+
 void *ov_ctx_stream(ov_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 int ov_capacity(const ov_ctx *c) { return c ? c->cap : 0; }
@@ -848,8 +857,8 @@ static unsigned long long graph_key(ov_ctx *c)
     unsigned long long h = 1469598103934665603ull;
     h = mix64(h, &c->params, sizeof c->params);
     h = mix64(h, &c->geo, sizeof c->geo);
-    int ints[9] = {c->cap, c->tree.cap_cells, c->precision, (int)c->mem.size(), c->tune.warps, c->tune.groups,
-                   c->tune.blocks_per_sm, c->tune.largest_first, c->tune.hi_occ};
+    int ints[10] = {c->cap, c->tree.cap_cells, c->precision, (int)c->mem.size(), c->tune.warps, c->tune.groups,
+                    c->tune.blocks_per_sm, c->tune.largest_first, c->tune.hi_occ, c->walk};
     h = mix64(h, ints, sizeof ints);
     for (const Member &m : c->mem) {
         int lay[3] = {m.lo, m.n, m.cap};

@@ -194,6 +194,7 @@ struct ov_ctx {
     cudaStream_t stream = nullptr;
     ov_params params{};
     int precision = OV_PREC_FP64;
+    int walk = OV_WALK_SPLIT;    // OV_PREC_FP64's tree walk (ov_set_walk)
     bool tree_built = false;     // the tree matches node positions (tree queries)
     std::string err;
     int cap = 0;                 // node slots

@@ -718,7 +718,7 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     k_root<<<nt, 256, 0, s>>>(t.order, t.cell_off, t.counters, t.tt, na.x, na.y, na.z, c->fwd, c->geo, g, t.cells,
                               t.csum, t.cap_cells);
     c->launches += 3;
-    if (c->precision == OV_PREC_MIXED || c->precision == OV_PREC_DD) {
+    if (c->precision == OV_PREC_MIXED || c->precision == OV_PREC_DD || c->walk == OV_WALK_SPLIT) {
         k_cells32<<<(t.cap_cells + 255) / 256, 256, 0, s>>>(t.cells, t.counters, c->grid_h, 1.0 / c->grid_h,
                                                            t.cells32);
         c->launches++;

@@ -1075,6 +1075,220 @@ __global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mix
     }
 }
 
+// ------------------------------------------- FP64 path, split walk (default)
+// The walk (distance and opening tests) runs in FP32 on the grid-split cells
+// exactly as the mixed traversal's, with the FP64 test inside the guard
+// bands, so every lane accepts, skips and opens the cells the FP64 walk
+// does.  Accepted cells go to the lane's list in shared memory; the warp
+// evaluates the lists in FP64 when one nears its capacity and at the end of
+// each query point, every lane its own entries in walk order (the FP64
+// walk's summation order).  GB300 runs FP64 at 1/64 of the FP32 rate: this
+// keeps the FP64 pipe for the interactions, in warp instructions with most
+// lanes busy, instead of spending it on every visited cell.
+
+constexpr int kListCap = 64;   // accepted cells per lane between evaluations
+
+// The segment law (octree.c:321-342) for an accepted cell, in FP64 with
+// Newton-refined reciprocal square roots and reciprocal instead of the
+// reference's correctly rounded sqrt and divisions (each term within a few
+// ulps of the reference's).  R and Rp1 are the reference's own values.  The
+// filters |Rp1| < 1e-8 and ndot < 1e-8 are decided as the reference decides
+// them: near their thresholds segment_law64 redoes them with its rounding.
+// |R| >= 1e-8 holds for every accepted cell (the walk's skip test).
+__device__ __forceinline__ void law64_cell(const Cell64 *cp, const double q[3], double f4pi, double v[3])
+{
+    const double2 *c2 = reinterpret_cast<const double2 *>(cp);
+    const double2 A = __ldg(c2), B = __ldg(c2 + 1), C = __ldg(c2 + 2);
+    // A = (cx, cy)  B = (cz, qx)  C = (qy, qz)
+    const double R[3] = {-(q[0] - A.x), -(q[1] - A.y), -(q[2] - B.x)};
+    const double P[3] = {R[0] + B.y, R[1] + C.x, R[2] + C.y};
+    const double lp2 = fma(P[0], P[0], fma(P[1], P[1], P[2] * P[2]));
+    if (lp2 < 1e-16 * (1.0 - 1e-12)) return;   // |Rp1| < 1e-8
+    const double lR2 = fma(R[0], R[0], fma(R[1], R[1], R[2] * R[2]));
+    const double dot = fma(R[0], P[0], fma(R[1], P[1], R[2] * P[2]));
+    const double ra = rsqrt_nr(lR2), rb = rsqrt_nr(lp2), ab = ra * rb;
+    const double nd = dot * ab;
+    if (lp2 <= 1e-16 * (1.0 + 1e-12) || fabs(nd - 1e-8) < 1e-12) {
+        double w[3];
+        if (segment_law64(R, P, len3_ref(R[0], R[1], R[2]), f4pi, w)) {
+            v[0] += w[0]; v[1] += w[1]; v[2] += w[2];
+        }
+        return;
+    }
+    if (nd < 1e-8) return;
+    const double sc = f4pi * (ra + rb) * ab * recip_1_2(1.0 + nd);
+    v[0] = fma(fma(R[1], P[2], -R[2] * P[1]), sc, v[0]);
+    v[1] = fma(fma(R[2], P[0], -R[0] * P[2]), sc, v[1]);
+    v[2] = fma(fma(R[0], P[1], -R[1] * P[0]), sc, v[2]);
+}
+
+// The lanes' lists (this lane: list[32 i], i < n), all lanes together.
+__device__ __forceinline__ void flush_list(const VelArgs &a, const int *list, int n, const double q[3], double v[3])
+{
+    const int nmax = __reduce_max_sync(0xffffffffu, n);
+    for (int i = 0; i < nmax; ++i)
+        if (i < n) law64_cell(a.cells + list[32 * i], q, a.f4pi, v);
+}
+
+// One query point (split g + f for the tests, q in FP64 for the law) for the
+// 32 lanes of a warp; the lane's FP64 velocity in v.
+__device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], const float f[3], const double q[3],
+                                           bool part, int root, int ncell, int *list, double v[3], MixedAcc &m,
+                                           bool &overflow)
+{
+    const float th2 = a.th2f;
+    const float d2lo = 1e-16f * (1.0f - 1e-5f), d2hi = 1e-16f * (1.0f + 1e-5f);
+    v[0] = v[1] = v[2] = 0;
+    int c = root;
+    int resume = part ? 0 : 0x7fffffff;
+    const int guard_max = 4 * (ncell - root) + 64;
+    int steps = 0, n = 0;
+    while (c < ncell) {
+        if (c < root) { bad_index(a, 1, c); break; }
+        const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
+        const float4 A = __ldg(cp4), B = __ldg(cp4 + 1), Cc = __ldg(cp4 + 2);
+        // A = (gx, gy, gz, fx)  B = (fy, fz, qx, qy)  Cc = (qz, lm, next, count)
+        int nxt = __float_as_int(Cc.z);
+        if (nxt <= c || nxt > ncell) { bad_index(a, 2, c); nxt = ncell; }
+        bool open = false;
+        if (c >= resume) {
+            ++m.nvis;
+            const float dx = (g[0] - A.x) + (f[0] - A.w);
+            const float dy = (g[1] - A.y) + (f[1] - B.x);
+            const float dz = (g[2] - A.z) + (f[2] - B.y);
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const bool leaf = (nxt == c + 1);
+            const float lm2 = Cc.y * Cc.y, b = th2 * d2;
+            // the mixed traversal's tests and guard bands
+            bool skip = d2 < d2lo;
+            bool acc = !skip && (leaf || lm2 < b * (1.0f - 2e-5f));
+            const bool opn = !skip && !leaf && lm2 > b * (1.0f + 2e-5f);
+            if ((!skip && d2 <= d2hi) || (!skip && !acc && !opn)) {
+                ++m.nfb;
+                double dxyz[3], d64;
+                const int dec = decide64(a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
+                skip = dec == 1;
+                acc = dec == 2;
+            }
+            if (acc) {
+                ++m.nacc;
+                list[32 * n] = c;
+                ++n;
+                resume = nxt;
+            } else if (skip) {
+                resume = nxt;
+            } else {
+                open = true;
+            }
+        }
+        ++steps;
+        // a lane adds at most one entry a step: room for 16 more after this test
+        if ((steps & 15) == 0 && __any_sync(0xffffffffu, n > kListCap - 16)) {
+            flush_list(a, list, n, q, v);
+            n = 0;
+        }
+        c = __any_sync(0xffffffffu, open) ? c + 1 : nxt;
+        if (steps > guard_max) { overflow = true; break; }
+    }
+    flush_list(a, list, n, q, v);
+    m.nstep += steps;
+}
+
+// Resident blocks per SM the register budget is sized for (about 20 warps)
+template <int W> constexpr int min_blocks_split() { return W == 2 ? 10 : (W == 4 ? 5 : 2); }
+
+template <int W>
+__global__ void __launch_bounds__(32 * W, min_blocks_split<W>()) k_vel_split(VelArgs a, double *__restrict__ part_out)
+{
+    const int lane = threadIdx.x & 31;
+    const int tiles = a.counters[TC_ITEMS];
+    const int items = tiles * a.G;
+    __shared__ int s_list[W][kListCap * 32];   // per warp: [entry][lane]
+    int *list = &s_list[threadIdx.x >> 5][lane];
+    unsigned long long visits = 0, accepts = 0, steps = 0, fallback = 0;
+    bool overflow = false;
+    for (int it = next_item(a); it < items; it = next_item(a)) {
+        const WorkItem w = decode_item(a, it, tiles);
+        const int loc = 32 * w.tile + lane;
+        const int tix = w.st + loc;
+        bool valid = loc < w.nne && tix < a.cap;
+        int id = valid ? a.order[tix] : 0;
+        if (valid && (id < 0 || id >= a.cap)) { bad_index(a, 4, id); valid = false; id = 0; }
+        const int st = valid ? a.status[id] : OV_EMPTY;
+        const bool part = valid && st != OV_PINNED && st != OV_EMPTY && a.prm.use_bh;
+        double p[3] = {0, 0, 0};
+        if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
+        float g0[3], f0[3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const double G = rint(p[ax] * a.inv_h) * a.grid_h;
+            g0[ax] = (float)G;
+            f0[ax] = (float)(p[ax] - G);
+        }
+        MixedAcc m = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
+        double prim[3] = {0, 0, 0}, img[3] = {0, 0, 0};
+        for (int qi = w.grp; qi <= a.geo.n_img; qi += a.G) {
+            const int j = qi - 1;
+            double q[3];
+            float g[3], f[3];
+            if (j < 0) {
+                q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
+                for (int ax = 0; ax < 3; ++ax) { g[ax] = g0[ax]; f[ax] = f0[ax]; }
+            } else {
+                image_point(a.geo, j, p, q);
+                if (a.geo.nreflect[j] > 0) {
+                    // a mirror image: the reflected point split on the grid
+                    for (int ax = 0; ax < 3; ++ax) {
+                        const double G = rint(q[ax] * a.inv_h) * a.grid_h;
+                        g[ax] = (float)G;
+                        f[ax] = (float)(q[ax] - G);
+                    }
+                } else {
+                    // p - L*shift: grid parts subtract exactly
+                    for (int ax = 0; ax < 3; ++ax) {
+                        g[ax] = g0[ax] - a.shift_g[j][ax];
+                        f[ax] = f0[ax] - a.shift_f[j][ax];
+                    }
+                }
+            }
+            double v[3];
+            walk_split(a, g, f, q, part, w.root, w.end, list, v, m, overflow);
+            if (j < 0) {
+                prim[0] = v[0]; prim[1] = v[1]; prim[2] = v[2];
+            } else {
+                for (int r = 0; r < a.geo.nreflect[j]; ++r) mirror_vec(a.geo.reflect[j][r], v);
+                img[0] = rn_add(img[0], v[0]); img[1] = rn_add(img[1], v[1]); img[2] = rn_add(img[2], v[2]);
+            }
+        }
+        if (valid) {
+            const size_t cap = (size_t)a.cap;
+            for (int ax = 0; ax < 3; ++ax) {
+                part_out[((size_t)(2 * w.grp) * 3 + ax) * cap + tix] = prim[ax];
+                part_out[((size_t)(2 * w.grp + 1) * 3 + ax) * cap + tix] = img[ax];
+            }
+        }
+        visits += m.nvis;
+        accepts += m.nacc;
+        steps += m.nstep;
+        fallback += m.nfb;
+    }
+    int err = overflow ? OV_EW_ITER : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        visits += __shfl_xor_sync(0xffffffffu, visits, o);
+        accepts += __shfl_xor_sync(0xffffffffu, accepts, o);
+        fallback += __shfl_xor_sync(0xffffffffu, fallback, o);
+        err |= __shfl_xor_sync(0xffffffffu, err, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&a.stat[ST_VISITS], visits);
+        atomicAdd(&a.stat[ST_ACCEPTS], accepts);
+        atomicAdd(&a.stat[ST_STEPS], steps);
+        atomicAdd(&a.stat[ST_FALLBACK], fallback);
+        if (err) atomicOr((int *)&a.counters[TC_ERR], err);
+    }
+}
+
 }  // namespace
 
 // Query groups per node: the tuned value, else enough warps for ~32 per SM
@@ -1165,7 +1379,7 @@ int ov_reserve_velocity_scratch(ov_ctx *c)
 
 // Traversal kernel for a precision and block shape.
 typedef void (*VelKernel)(VelArgs, double *);
-static VelKernel vel_kernel(int precision, int warps, int hi_occ)
+static VelKernel vel_kernel(int precision, int walk, int warps, int hi_occ)
 {
     if (precision == OV_PREC_MIXED) {
         if (hi_occ) {
@@ -1182,6 +1396,11 @@ static VelKernel vel_kernel(int precision, int warps, int hi_occ)
         if (warps == 8) return k_vel_mixed<8, 0, true>;
         return k_vel_mixed<4, 0, true>;
     }
+    if (walk == OV_WALK_SPLIT) {
+        if (warps == 2) return k_vel_split<2>;
+        if (warps == 8) return k_vel_split<8>;
+        return k_vel_split<4>;
+    }
     if (warps == 2) return k_vel_fp64<2>;
     if (warps == 8) return k_vel_fp64<8>;
     return k_vel_fp64<4>;
@@ -1191,7 +1410,7 @@ static VelKernel vel_kernel(int precision, int warps, int hi_occ)
 // every SM, but no more blocks than there can be work items.
 int ov_traversal_blocks(ov_ctx *c, int precision, int warps, int *per_sm)
 {
-    VelKernel k = vel_kernel(precision, warps, c->tune.hi_occ);
+    VelKernel k = vel_kernel(precision, c->walk, warps, c->tune.hi_occ);
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * warps, 0) != cudaSuccess || occ < 1) {
         cudaGetLastError();
@@ -1218,7 +1437,7 @@ int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precisio
     if (warps != 2 && warps != 8) warps = 4;
     int blocks = ov_traversal_blocks(c, precision, warps, nullptr);
     OV_CUDA(c, cudaMemsetAsync(a.work, 0, sizeof(int), s));
-    vel_kernel(precision, warps, c->tune.hi_occ)<<<blocks, 32 * warps, 0, s>>>(a, c->part);
+    vel_kernel(precision, c->walk, warps, c->tune.hi_occ)<<<blocks, 32 * warps, 0, s>>>(a, c->part);
     k_vel_finish<<<(c->cap + 127) / 128, 128, 0, s>>>(a, c->part);
     c->launches += 2;
     return OV_OK;

@@ -49,6 +49,8 @@ def load(path: str | None = None):
         "ov_last_error": (C.c_char_p, [P]),
         "ov_set_params": (C.c_int, [P, C.POINTER(abi.Params)]),
         "ov_set_precision": (C.c_int, [P, C.c_int]),
+        "ov_set_walk": (C.c_int, [P, C.c_int]),
+        "ov_get_walk": (C.c_int, [P]),
         "ov_ctx_stream": (P, [P]),
         "ov_upload_tangle": (C.c_int, [P, TS]),
         "ov_download_tangle": (C.c_int, [P, TS, C.c_uint]),
@@ -238,6 +240,14 @@ class Context:
 
     def set_precision(self, prec: int):
         self._check(self.lib.ov_set_precision(self._h, prec))
+
+    def set_walk(self, walk: int):
+        """OV_PREC_FP64's tree walk: abi.OV_WALK_SPLIT (default) or abi.OV_WALK_FP64."""
+        self._check(self.lib.ov_set_walk(self._h, walk))
+
+    @property
+    def walk(self) -> int:
+        return self.lib.ov_get_walk(self._h)
 
     # ----------------------------------------------------------------- data
     def upload(self, host):

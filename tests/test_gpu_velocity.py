@@ -23,8 +23,12 @@ def port():
     return Checker("port")
 
 
-def _gpu_eval(ht, p, t=0.0):
+WALKS = [abi.OV_WALK_SPLIT, abi.OV_WALK_FP64]
+
+
+def _gpu_eval(ht, p, t=0.0, walk=abi.OV_WALK_SPLIT):
     ctx = gpu.Context(0, params=p)
+    ctx.set_walk(walk)
     ctx.upload(ht)
     ctx.update_tangle(t)
     ctx.download(ht)
@@ -33,12 +37,13 @@ def _gpu_eval(ht, p, t=0.0):
     return st
 
 
+@pytest.mark.parametrize("walk", WALKS)
 @pytest.mark.parametrize("theta", [0.3, 0.4, 0.5])
-def test_bh_matches_reference_golden(golden, theta):
+def test_bh_matches_reference_golden(golden, theta, walk):
     g = golden("rw16x64.npz")
     ht = host_from_arrays(g)
     p = W.config_params("rw", bh_resolution=theta)
-    st = _gpu_eval(ht, p)
+    st = _gpu_eval(ht, p, walk=walk)
     tag = f"{int(theta * 10)}"
     assert st["error_word"] == 0
     assert node_rel_err(ht.vels, g[f"vels_{tag}"]) < FP64_TOL
@@ -48,14 +53,15 @@ def test_bh_matches_reference_golden(golden, theta):
         assert rel_err(ht.normals, g["normals"]) < 1e-12
 
 
-def test_interaction_counts_match_oracle_tree(port, golden):
+@pytest.mark.parametrize("walk", WALKS)
+def test_interaction_counts_match_oracle_tree(port, golden, walk):
     """Same tree, same decisions: per-target visits/accepts equal the pointer octree's."""
     import ctypes as C
 
     g = golden("rw16x64.npz")
     ht = host_from_arrays(g)
     p = W.config_params("rw")
-    st = _gpu_eval(ht, p)
+    st = _gpu_eval(ht, p, walk=walk)
     t = port.tangle(ht)
     from oracle.pyoracle import Checker as _C  # noqa: F401
 
@@ -99,6 +105,24 @@ def test_config_b_full_size_vs_oracle(port, golden):
     assert node_rel_err(ht.vels[g["nodes"]], g["vels"]) < FP64_TOL
 
 
+@pytest.mark.parametrize("images", [None, "wall_2_4"])
+def test_split_walk_equals_fp64_walk(images):
+    """OV_PREC_FP64's two walks: the same decisions (visits, accepts) and FP64
+    velocities a few ulps apart (the law's square roots and divisions)."""
+    base = W.random_walk_tangle(256, 256, D=0.1, seed=1)
+    ht = base if images is None else W.HostTangle(base.pos.copy(), base.conn[:, 0].copy(), base.conn[:, 1].copy(),
+                                                   base.box_lo, base.box_hi, image_set=images)
+    p = W.config_params("rw")
+    out = []
+    for walk in WALKS:
+        st = _gpu_eval(ht, p, walk=walk)
+        assert st["error_word"] == 0
+        out.append((np.array(ht.vels), st))
+    (v_split, st_split), (v_64, st_64) = out
+    assert st_split["visits"] == st_64["visits"] and st_split["accepts"] == st_64["accepts"]
+    assert node_rel_err(v_split, v_64) < 1e-12
+
+
 def test_theta_zero_equals_direct_sum():
     """theta = 0 accepts only leaves, so the tree sum is the direct sum."""
     ht = W.random_walk_tangle(6, 40, D=0.1, seed=31)
@@ -113,8 +137,9 @@ def test_theta_zero_equals_direct_sum():
     assert node_rel_err(ht.vels, dv) < 1e-12
 
 
+@pytest.mark.parametrize("walk", WALKS)
 @pytest.mark.parametrize("case", ["out_of_box", "empty_slots", "single_loop", "mixed_loop_sizes"])
-def test_edge_cases_vs_oracle(port, case):
+def test_edge_cases_vs_oracle(port, case, walk):
     rng = np.random.default_rng(5)
     if case == "out_of_box":
         ht = W.random_walk_tangle(10, 48, D=0.1, seed=24)
@@ -141,7 +166,7 @@ def test_edge_cases_vs_oracle(port, case):
         ht = W.HostTangle(np.concatenate([a.pos, b.pos]), np.concatenate([a.fwd, b.fwd + n]),
                           np.concatenate([a.rev, b.rev + n]), a.box_lo, a.box_hi)
     p = W.config_params("rw")
-    st = _gpu_eval(ht, p)
+    st = _gpu_eval(ht, p, walk=walk)
     assert st["error_word"] == 0
     port.set_params(p)
     t = port.tangle(ht)
