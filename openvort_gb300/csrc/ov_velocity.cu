@@ -1079,62 +1079,136 @@ __global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mix
 // The walk (distance and opening tests) runs in FP32 on the grid-split cells
 // exactly as the mixed traversal's, with the FP64 test inside the guard
 // bands, so every lane accepts, skips and opens the cells the FP64 walk
-// does.  Accepted cells go to the lane's list in shared memory; the warp
-// evaluates the lists in FP64 when one nears its capacity and at the end of
-// each query point, every lane its own entries in walk order (the FP64
-// walk's summation order).  GB300 runs FP64 at 1/64 of the FP32 rate: this
-// keeps the FP64 pipe for the interactions, in warp instructions with most
-// lanes busy, instead of spending it on every visited cell.
+// does.  Accepted cells go to the lane's list in shared memory.  When a list
+// nears its capacity, and at the end of each query point, the warp
+// evaluates all lists together in FP64, 32 entries at a time whoever owns
+// them (the owner's query point comes by shuffle), and every owner adds its
+// own terms in walk order (the FP64 walk's summation order).  GB300 runs
+// FP64 at 1/64 of the FP32 rate: this keeps the FP64 pipe for the
+// interactions, in warp instructions with all lanes busy, instead of
+// spending it on every visited cell and on idle lanes.
 
 constexpr int kListCap = 64;   // accepted cells per lane between evaluations
 
-// The segment law (octree.c:321-342) for an accepted cell, in FP64 with
-// Newton-refined reciprocal square roots and reciprocal instead of the
+// A warp's lists and the scratch of their evaluation (shared memory).
+struct WarpLists {
+    int entry[kListCap * 32];   // entry i of lane l at [32 i + l]
+    unsigned row_mask[kListCap];   // row i: the lanes holding an entry i
+    int row_start[kListCap];       // entries in rows before row i
+    double w[32][3];               // the terms of one batch of 32 entries
+};
+
+// 1/sqrt(x) and 1/x (x normal, positive) from the hardware approximations
+// (relative error below 2^-20 on sm_103a) with one third-order correction:
+// for e = 1 - x y0^2, y0 (1 + e/2 + 3e^2/8) leaves 5e^3/16, and for
+// e = 1 - x y0, y0 (1 + e + e^2) leaves e^3: below 2^-53 for |e| < 2^-18.
+__device__ __forceinline__ double rsqrt3(double x)
+{
+    const double y0 = rsqrt_seed(x);
+    const double e = fma(-(x * y0), y0, 1.0);
+    return fma(y0 * e, fma(0.375, e, 0.5), y0);
+}
+__device__ __forceinline__ double rcp3(double x)
+{
+    const double y0 = rcp_seed(x);
+    const double e = fma(-x, y0, 1.0);
+    return fma(y0, fma(e, e, e), y0);
+}
+
+// IEEE bits of a double: for x >= 0, or any x against a positive bound, the
+// order of the bits as signed integers is the order of the values (tests on
+// the integer pipe instead of the FP64 one).
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+
+// The segment law (octree.c:321-342) for an accepted cell without the
+// factor kappa / 4 pi (applied to the query point's sum), in FP64 with
+// corrected hardware reciprocal square roots and reciprocal instead of the
 // reference's correctly rounded sqrt and divisions (each term within a few
 // ulps of the reference's).  R and Rp1 are the reference's own values.  The
 // filters |Rp1| < 1e-8 and ndot < 1e-8 are decided as the reference decides
 // them: near their thresholds segment_law64 redoes them with its rounding.
-// |R| >= 1e-8 holds for every accepted cell (the walk's skip test).
-__device__ __forceinline__ void law64_cell(const Cell64 *cp, const double q[3], double f4pi, double v[3])
+// |R| >= 1e-8 holds for every accepted cell (the walk's skip test).  w is
+// zero when a filter drops the cell.
+__device__ __forceinline__ void law64_term(const Cell64 *cp, const double q[3], double w[3])
 {
+    w[0] = w[1] = w[2] = 0.0;
     const double2 *c2 = reinterpret_cast<const double2 *>(cp);
     const double2 A = __ldg(c2), B = __ldg(c2 + 1), C = __ldg(c2 + 2);
-    // A = (cx, cy)  B = (cz, qx)  C = (qy, qz)
-    const double R[3] = {-(q[0] - A.x), -(q[1] - A.y), -(q[2] - B.x)};
+    // A = (cx, cy)  B = (cz, qx)  C = (qy, qz); R = -(q - COM), rounded alike
+    const double R[3] = {A.x - q[0], A.y - q[1], B.x - q[2]};
     const double P[3] = {R[0] + B.y, R[1] + C.x, R[2] + C.y};
     const double lp2 = fma(P[0], P[0], fma(P[1], P[1], P[2] * P[2]));
-    if (lp2 < 1e-16 * (1.0 - 1e-12)) return;   // |Rp1| < 1e-8
+    const long long lp2_lo = dbits(1e-16 * (1.0 - 1e-12)), lp2_hi = dbits(1e-16 * (1.0 + 1e-12));
+    const long long nd_lo = dbits(1e-8 - 1e-12), nd_hi = dbits(1e-8 + 1e-12);
+    if (dbits(lp2) < lp2_lo) return;   // |Rp1| < 1e-8
     const double lR2 = fma(R[0], R[0], fma(R[1], R[1], R[2] * R[2]));
     const double dot = fma(R[0], P[0], fma(R[1], P[1], R[2] * P[2]));
-    const double ra = rsqrt_nr(lR2), rb = rsqrt_nr(lp2), ab = ra * rb;
+    const double ra = rsqrt3(lR2), rb = rsqrt3(lp2), ab = ra * rb;
     const double nd = dot * ab;
-    if (lp2 <= 1e-16 * (1.0 + 1e-12) || fabs(nd - 1e-8) < 1e-12) {
-        double w[3];
-        if (segment_law64(R, P, len3_ref(R[0], R[1], R[2]), f4pi, w)) {
-            v[0] += w[0]; v[1] += w[1]; v[2] += w[2];
-        }
+    if (dbits(lp2) <= lp2_hi || (dbits(nd) >= nd_lo && dbits(nd) <= nd_hi)) {
+        if (!segment_law64(R, P, len3_ref(R[0], R[1], R[2]), 1.0, w)) w[0] = w[1] = w[2] = 0.0;
         return;
     }
-    if (nd < 1e-8) return;
-    const double sc = f4pi * (ra + rb) * ab * recip_1_2(1.0 + nd);
-    v[0] = fma(fma(R[1], P[2], -R[2] * P[1]), sc, v[0]);
-    v[1] = fma(fma(R[2], P[0], -R[0] * P[2]), sc, v[1]);
-    v[2] = fma(fma(R[0], P[1], -R[1] * P[0]), sc, v[2]);
+    if (dbits(nd) < nd_lo) return;   // ndot < 1e-8
+    const double sc = (ra + rb) * ab * rcp3(1.0 + nd);
+    w[0] = fma(R[1], P[2], -R[2] * P[1]) * sc;
+    w[1] = fma(R[2], P[0], -R[0] * P[2]) * sc;
+    w[2] = fma(R[0], P[1], -R[1] * P[0]) * sc;
 }
 
-// The lanes' lists (this lane: list[32 i], i < n), all lanes together.
-__device__ __forceinline__ void flush_list(const VelArgs &a, const int *list, int n, const double q[3], double v[3])
+// Evaluate the warp's lists (this lane holds n entries) at the lanes' query
+// points q and add each lane's terms to its v, in entry order.
+__device__ __forceinline__ void flush_lists(const VelArgs &a, WarpLists &L, int lane, int n, const double q[3],
+                                            double v[3])
 {
     const int nmax = __reduce_max_sync(0xffffffffu, n);
-    for (int i = 0; i < nmax; ++i)
-        if (i < n) law64_cell(a.cells + list[32 * i], q, a.f4pi, v);
+    if (nmax == 0) return;
+    // rows, in entry order: row i holds the i-th entry of every lane that has one
+    int total = 0;
+    for (int i = 0; i < nmax; ++i) {
+        const unsigned m = __ballot_sync(0xffffffffu, n > i);
+        if (lane == 0) { L.row_mask[i] = m; L.row_start[i] = total; }
+        total += __popc(m);
+    }
+    __syncwarp();
+    const unsigned below = (1u << lane) - 1u;
+    int own = 0;   // this lane's next entry to add
+    for (int base = 0; base < total; base += 32) {
+        // entry base + lane: its row (the last one starting at or before it) and owner
+        const int k = base + lane;
+        int owner = lane, cell = -1;
+        if (k < total) {
+            int lo = 0, hi = nmax - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (L.row_start[mid] <= k) lo = mid; else hi = mid - 1;
+            }
+            owner = __fns(L.row_mask[lo], 0, k - L.row_start[lo] + 1);
+            cell = L.entry[32 * lo + owner];
+        }
+        double qo[3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) qo[ax] = __shfl_sync(0xffffffffu, q[ax], owner);
+        double w[3] = {0.0, 0.0, 0.0};
+        if (cell >= 0) law64_term(a.cells + cell, qo, w);
+        L.w[lane][0] = w[0]; L.w[lane][1] = w[1]; L.w[lane][2] = w[2];
+        __syncwarp();
+        // this lane's own entries in the batch, in order
+        while (own < n) {
+            const int ko = L.row_start[own] + __popc(L.row_mask[own] & below) - base;
+            if (ko >= 32) break;
+            v[0] += L.w[ko][0]; v[1] += L.w[ko][1]; v[2] += L.w[ko][2];
+            ++own;
+        }
+        __syncwarp();
+    }
 }
 
 // One query point (split g + f for the tests, q in FP64 for the law) for the
 // 32 lanes of a warp; the lane's FP64 velocity in v.
 __device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], const float f[3], const double q[3],
-                                           bool part, int root, int ncell, int *list, double v[3], MixedAcc &m,
-                                           bool &overflow)
+                                           bool part, int root, int ncell, WarpLists &L, int lane, double v[3],
+                                           MixedAcc &m, bool &overflow)
 {
     const float th2 = a.th2f;
     const float d2lo = 1e-16f * (1.0f - 1e-5f), d2hi = 1e-16f * (1.0f + 1e-5f);
@@ -1172,7 +1246,7 @@ __device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], c
             }
             if (acc) {
                 ++m.nacc;
-                list[32 * n] = c;
+                L.entry[32 * n + lane] = c;
                 ++n;
                 resume = nxt;
             } else if (skip) {
@@ -1184,13 +1258,14 @@ __device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], c
         ++steps;
         // a lane adds at most one entry a step: room for 16 more after this test
         if ((steps & 15) == 0 && __any_sync(0xffffffffu, n > kListCap - 16)) {
-            flush_list(a, list, n, q, v);
+            flush_lists(a, L, lane, n, q, v);
             n = 0;
         }
         c = __any_sync(0xffffffffu, open) ? c + 1 : nxt;
         if (steps > guard_max) { overflow = true; break; }
     }
-    flush_list(a, list, n, q, v);
+    flush_lists(a, L, lane, n, q, v);
+    v[0] *= a.f4pi; v[1] *= a.f4pi; v[2] *= a.f4pi;
     m.nstep += steps;
 }
 
@@ -1203,8 +1278,8 @@ __global__ void __launch_bounds__(32 * W, min_blocks_split<W>()) k_vel_split(Vel
     const int lane = threadIdx.x & 31;
     const int tiles = a.counters[TC_ITEMS];
     const int items = tiles * a.G;
-    __shared__ int s_list[W][kListCap * 32];   // per warp: [entry][lane]
-    int *list = &s_list[threadIdx.x >> 5][lane];
+    __shared__ WarpLists s_lists[W];
+    WarpLists &lists = s_lists[threadIdx.x >> 5];
     unsigned long long visits = 0, accepts = 0, steps = 0, fallback = 0;
     bool overflow = false;
     for (int it = next_item(a); it < items; it = next_item(a)) {
@@ -1252,7 +1327,7 @@ __global__ void __launch_bounds__(32 * W, min_blocks_split<W>()) k_vel_split(Vel
                 }
             }
             double v[3];
-            walk_split(a, g, f, q, part, w.root, w.end, list, v, m, overflow);
+            walk_split(a, g, f, q, part, w.root, w.end, lists, lane, v, m, overflow);
             if (j < 0) {
                 prim[0] = v[0]; prim[1] = v[1]; prim[2] = v[2];
             } else {
@@ -1292,14 +1367,17 @@ __global__ void __launch_bounds__(32 * W, min_blocks_split<W>()) k_vel_split(Vel
 }  // namespace
 
 // Query groups per node: the tuned value, else enough warps for ~32 per SM
-// on small tangles.
+// on small tangles (~96 for the FP64 split walk, whose work items are
+// longer: finer items balance the end of the launch).
 int ov_query_groups(ov_ctx *c)
 {
     int maxg = c->geo.n_img + 1;
     if (c->tune.groups > 0) return std::min(c->tune.groups, std::min(maxg, 27));
     int warps = (c->cap + 31) / 32;
-    int G = (32 * c->sm_count + warps - 1) / warps;
-    G = G < 1 ? 1 : (G > 8 ? 8 : G);
+    const bool split = c->precision == OV_PREC_FP64 && c->walk == OV_WALK_SPLIT;
+    const int per_sm = split ? 96 : 32, gmax = split ? 9 : 8;
+    int G = (per_sm * c->sm_count + warps - 1) / warps;
+    G = G < 1 ? 1 : (G > gmax ? gmax : G);
     return std::min(G, maxg);
 }
 
