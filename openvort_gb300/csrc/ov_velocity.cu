@@ -2715,6 +2715,70 @@ __global__ void __launch_bounds__(128) k_sph_query_mixed(SphArgs s, double *__re
     for (int ax = 0; ax < 3; ++ax) part[((size_t)q * 3 + ax) * s.n + id] = w[ax];
 }
 
+// k_sph_query on the FP64 path's split walk: the rotated query point split on
+// the grid for the FP32 tests (FP64 inside the guard bands), the accepted
+// cells evaluated in FP64 by the whole warp.
+__global__ void __launch_bounds__(128) k_sph_query_split(SphArgs s, double *__restrict__ part)
+{
+    const VelArgs &a = s.v;
+    __shared__ WarpLists s_lists[4];
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    WarpLists &lists = s_lists[threadIdx.x >> 5];
+    const int nne = a.tt[TT_NNE];
+    const int tiles = (nne + 31) / 32;
+    if (warp >= 18 * tiles) return;
+    const int q = warp / tiles, tile = warp - q * tiles;
+    const int loc = tile * 32 + lane;
+    bool valid = loc < nne;
+    int id = valid ? a.order[loc] : 0;
+    if (valid && (id < 0 || id >= s.n)) { bad_index(a, 9, id); valid = false; id = 0; }
+    const int st = valid ? a.status[id] : OV_EMPTY;
+    const bool take = valid && st != OV_PINNED && st != OV_EMPTY;
+    double p[3] = {0, 0, 0};
+    if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
+    const int m = q / 9, j = q % 9 - 1;
+    const int root = a.tt[m * TT_WORDS + TT_ROOT], end = a.tt[m * TT_WORDS + TT_END];
+    const bool go = take && end > root;
+    double qp[3] = {p[0], p[1], p[2]}, da = 0, dp = 0;
+    if (j >= 0) {
+        const double ua = j < 2 ? (j == 0 ? 1.0 : -1.0) : (j < 4 ? 0.0 : ((j & 1) ? -1.0 : 1.0));
+        const double up = j < 2 ? 0.0 : (j < 4 ? (j == 2 ? 1.0 : -1.0) : (j < 6 ? 1.0 : -1.0));
+        da = rn_mul(ua, s.d_az);
+        dp = rn_mul(up, s.d_pl);
+        sph_rotate(p, da, dp, qp);
+    }
+    float g[3], f[3];
+    for (int ax = 0; ax < 3; ++ax) {
+        const double G = rint(qp[ax] * a.inv_h) * a.grid_h;
+        g[ax] = (float)G;
+        f[ax] = (float)(qp[ax] - G);
+    }
+    MixedAcc acc = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
+    bool overflow = false;
+    double v[3];
+    walk_split(a, g, f, qp, go, root, end, lists, lane, v, acc, overflow);
+    double w[3] = {v[0], v[1], v[2]};
+    if (j >= 0) sph_rotate(v, -da, -dp, w);
+    if (a.stat) {
+        unsigned long long vis = acc.nvis, ac = acc.nacc, fb = acc.nfb;
+        for (int o = 16; o > 0; o >>= 1) {
+            vis += __shfl_xor_sync(0xffffffffu, vis, o);
+            ac += __shfl_xor_sync(0xffffffffu, ac, o);
+            fb += __shfl_xor_sync(0xffffffffu, fb, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&a.stat[ST_VISITS], vis);
+            atomicAdd(&a.stat[ST_ACCEPTS], ac);
+            atomicAdd(&a.stat[ST_STEPS], (unsigned long long)acc.nstep);
+            atomicAdd(&a.stat[ST_FALLBACK], fb);
+        }
+    }
+    if (overflow && lane == 0) atomicOr((int *)&a.counters[TC_ERR], OV_EW_ITER);
+    if (!valid) return;
+    for (int ax = 0; ax < 3; ++ax) part[((size_t)q * 3 + ax) * s.n + id] = w[ax];
+}
+
 // The rest of update_velocity (tangle.c:644-665, 763-865 of the fork): the
 // query results summed in the fork's order, LIA with its segment-length
 // limits, the temperature model, mutual friction, PINNED_SLIP.
@@ -2845,6 +2909,8 @@ int ov_launch_sph_velocities(ov_ctx *c, const SphDomain &d, const SphSettings &p
     const long long warps = 18LL * ((d.n + 31) / 32);
     if (c->precision == OV_PREC_MIXED)
         k_sph_query_mixed<<<(unsigned)((warps + 3) / 4), 128, 0, c->stream>>>(s, c->part);
+    else if (c->walk == OV_WALK_SPLIT)
+        k_sph_query_split<<<(unsigned)((warps + 3) / 4), 128, 0, c->stream>>>(s, c->part);
     else
         k_sph_query<<<(unsigned)((warps + 3) / 4), 128, 0, c->stream>>>(s, c->part);
     k_sph_finish<<<(d.n + 127) / 128, 128, 0, c->stream>>>(s, c->part);

@@ -26,6 +26,7 @@ from tests._util import node_rel_err
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CASES = ["plain", "temperature"]
+WALKS = [abi.OV_WALK_SPLIT, abi.OV_WALK_FP64]
 
 
 def sph_from_golden(g):
@@ -70,11 +71,13 @@ def test_workload_matches_golden(golden):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("walk", WALKS)
 @pytest.mark.parametrize("case", CASES)
-def test_update_tangle_matches_fork(golden, case):
+def test_update_tangle_matches_fork(golden, case, walk):
     g = golden("spherical.npz")
     sph = sph_from_golden(g)
     ctx = gpu.Context(0)
+    ctx.set_walk(walk)
     ctx.sph_update(sph, params(case), 0.0)
     st = ctx.stats()
     ctx.close()
@@ -141,13 +144,15 @@ def test_mixed_precision_matches_fp64_tree(golden, case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("walk", WALKS)
 @pytest.mark.parametrize("case", CASES)
-def test_larger_tangle_vs_oracle(case):
+def test_larger_tangle_vs_oracle(case, walk):
     """A larger seeded tangle (96 rings, other seed) against the C restatement."""
     from oracle.pyoracle import sph_update_tangle
     a = W.spherical_tangle(n_rings=96, seed=11)
     b = W.spherical_tangle(n_rings=96, seed=11)
     ctx = gpu.Context(0)
+    ctx.set_walk(walk)
     ctx.sph_update(a, params(case), 0.0)
     ctx.close()
     sph_update_tangle(b, params(case), threads=8)
@@ -156,3 +161,21 @@ def test_larger_tangle_vs_oracle(case):
     assert node_rel_err(a.tangents[live], b.tangents[live]) < 1e-12
     assert node_rel_err(a.vels[free], b.vels[free]) < 1e-10
     assert node_rel_err(a.vs[live], b.vs[live]) < 1e-10
+
+
+@pytest.mark.gpu
+def test_split_walk_equals_fp64_walk():
+    """The FP64 path's two walks on the fork's geometry: the same visits and
+    accepts, velocities a few ulps apart."""
+    out = []
+    for walk in WALKS:
+        t = W.spherical_tangle(n_rings=160, seed=3)
+        ctx = gpu.Context(0)
+        ctx.set_walk(walk)
+        ctx.sph_update(t, params("temperature"), 0.0)
+        out.append((t, ctx.stats()))
+        ctx.close()
+    (a, sa), (b, sb) = out
+    assert sa["visits"] == sb["visits"] and sa["accepts"] == sb["accepts"]
+    free = (a.stat[:, 0] != abi.OV_EMPTY) & (a.stat[:, 0] != abi.OV_PINNED)
+    assert node_rel_err(a.vels[free], b.vels[free]) < 1e-12
