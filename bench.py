@@ -37,7 +37,7 @@ sys.path.insert(0, ROOT)
 METRIC = "biot_savart_node_evals_per_s"
 # DRAM bytes (read + write) of one FP64 traversal launch on this workload, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum of k_vel_fp64, two launches: 9.87 and 9.92 MB)
-K_VEL_FP64_DRAM_BYTES = 9.895e6
+K_VEL_FP64_DRAM_BYTES = 15.108e6   # k_vel_split: 14.63 MB read + 0.48 MB written (ncu)
 UNIT = "node-evals/s"
 WORKLOAD = dict(workload="random-walk tangle, 256 loops x 256 nodes (65,536), D=0.1 cm, periodic_26, "
                          "theta=0.4, one update_tangle per step",
