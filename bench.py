@@ -395,6 +395,14 @@ def run_large(args, device=0):
     ctx.update_tangle(0.0)
     mixed_ms = eval_ms(ctx, max(3, args.steps))
     v32 = ctx.download(ht, abi.OV_F_VELS).vels.copy()
+    ctx.set_phase_timing(True)
+    ph = []
+    for _ in range(3):
+        ctx.flush_l2(256 << 20)
+        ctx.update_tangle(0.0)
+        ph.append(ctx.phase_times())
+    ctx.set_phase_timing(False)
+    ph = np.median(np.array(ph), axis=0).tolist()
     dt = E["dt"]
     ctx.upload(ht)
     for w in range(2):
@@ -436,7 +444,8 @@ def run_large(args, device=0):
         "config": E, "nodes": n, "tuning": tune, "cpu_baseline": cpu,
         "fp64": {"value": n / (fp64_ms * 1e-3), "unit": UNIT, "ms_per_eval": fp64_ms},
         "mixed": {"value": n / (mixed_ms * 1e-3), "unit": UNIT, "ms_per_eval": mixed_ms,
-                  "rel_l2_vs_fp64_tree": rel_l2(v32, v64)},
+                  "rel_l2_vs_fp64_tree": rel_l2(v32, v64),
+                  "phases_ms": {"tangents": ph[0], "tree_build": ph[1], "traversal": ph[2]}},
         "mixed_speedup_vs_fp64": fp64_ms / mixed_ms,
         "rk4_mixed": {"steps_per_s": 1e3 / rk4_ms, "ms_per_step": rk4_ms, "node_evals_per_s": 4 * n / (rk4_ms * 1e-3)},
         "full_steps_mixed": {"steps": K, "ms_per_step_wall": full_ms, "steps_per_s": 1e3 / full_ms if K else None,
@@ -787,6 +796,28 @@ def run_ours(args):
     return 0
 
 
+def run_build_profile(args):
+    """The large tangle's tree build (keys, radix sort, cells, moments, FP32
+    cell copy) repeated; one line with the phase times (CUDA events)."""
+    from openvort_gb300 import abi, gpu, workloads as W
+    E = LARGE
+    ht = W.random_walk_tangle(E["n_loops"], E["per_loop"], D=E["D"], seed=E["seed"])
+    ctx = gpu.Context(0, params=W.config_params("large", bh_resolution=E["theta"]), precision=abi.OV_PREC_MIXED)
+    ctx.upload(ht)
+    ctx.set_phase_timing(True)
+    ph = []
+    for _ in range(args.build_profile):
+        ctx.flush_l2(256 << 20)
+        ctx.update_tangle(0.0)
+        ph.append(ctx.phase_times())
+    ctx.close()
+    ph = np.array(ph)
+    print(json.dumps({"mode": "build_profile", "workload": E["workload"], "nodes": ht.n,
+                      "tree_build_ms": float(np.median(ph[:, 1])), "tangents_ms": float(np.median(ph[:, 0])),
+                      "traversal_ms": float(np.median(ph[:, 2])), "repeats": args.build_profile}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -802,9 +833,14 @@ def main():
                     help="walls, frames, injection and spherical-fork sections (0: skip)")
     ap.add_argument("--cpu-sections", type=int, default=1,
                     help="time the CPU baseline of the ensemble, precision-form and large sections too (0: skip)")
+    ap.add_argument("--build-profile", type=int, default=0,
+                    help="only rebuild the 1,048,576-node tangle's tree this many times and print the build "
+                         "times (a workload for profiling the sort and build kernels)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.build_profile > 0:
+        return run_build_profile(args)
     return run_ours(args)
 
 

@@ -34,7 +34,8 @@ __global__ void rs_hist(const uint64_t *__restrict__ keys, int n, int shift, int
     for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d * ntiles + blockIdx.x] = h[d];
 }
 
-// Exclusive scan of the digit-major table hist[256*ntiles] in one block.
+// Exclusive scan of the digit-major table hist[256*ntiles] in one block
+// (small tables: one launch instead of the device-wide scan's three).
 __global__ void rs_scan(int *__restrict__ hist, int total)
 {
     __shared__ int part[1024];
@@ -227,6 +228,12 @@ __global__ void scan_add(int *__restrict__ out, int n_max, const int *n_dev, con
 
 }  // namespace
 
+void ov_scan_exclusive(ov_ctx *c, const int *in, int *out, int n_max, const int *n_dev, int add, int *tmp,
+                       cudaStream_t s);
+
+// Radix sort of t.keys / t.order (n slots); the digit tables of more than
+// 32 tiles are scanned in place by the device-wide scan (the table has room
+// for its total).
 void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
 {
     if (n <= 0) return;
@@ -236,9 +243,14 @@ void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
     for (int pass = 0; pass < 4; ++pass) {
         int shift = 32 + 8 * pass;
         rs_hist<<<ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, t.sort_hist);
-        rs_scan<<<1, 1024, 0, s>>>(t.sort_hist, 256 * ntiles);
+        if (ntiles <= 32) {
+            rs_scan<<<1, 1024, 0, s>>>(t.sort_hist, 256 * ntiles);
+            c->launches += 1;
+        } else {
+            ov_scan_exclusive(c, t.sort_hist, t.sort_hist, 256 * ntiles, nullptr, 0, t.scan_tmp, s);
+        }
         rs_scatter<<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, ntiles, t.sort_hist);
-        c->launches += 3;
+        c->launches += 2;
         uint64_t *tk = ka; ka = kb; kb = tk;
         int *tv = va; va = vb; vb = tv;
     }

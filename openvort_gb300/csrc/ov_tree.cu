@@ -32,6 +32,7 @@ namespace {
 
 struct KeyGeom {
     double lo[3], hi[3], L[3];
+    double invL[3];    // 1 / L, rounded
     int fast;          // fixed-point digits allowed (rounding bound is small)
     int tb;            // member-id bits on top of the key
     int levels;        // levels the key holds
@@ -179,7 +180,7 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
     const uint64_t low = (1ull << 41) - 1, margin = 1ull << 22;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        double u = rn_div(rn_sub(p[a], g.lo[a]), g.L[a]);
+        double u = rn_mul(rn_sub(p[a], g.lo[a]), g.invL[a]);
         u = fmin(fmax(u, 0.0), 1.0);
         U[a] = (uint64_t)(u * 4611686018427387904.0);   // u * 2^62
         uint64_t r = U[a] & low;
@@ -658,10 +659,12 @@ static KeyGeom key_geom(const ov_ctx *c)
         g.lo[a] = geo.lo[a];
         g.hi[a] = geo.hi[a];
         g.L[a] = geo.L[a];
+        g.invL[a] = 1.0 / geo.L[a];
         // bound on how far the reference's rounded faces (21 levels) and the
-        // fixed-point image may sit from the exact dyadic faces, in box units
+        // fixed-point image (a subtraction, a product with the rounded 1/L)
+        // may sit from the exact dyadic faces, in box units
         double bound = (fabs(geo.lo[a]) + fabs(geo.hi[a])) / geo.L[a] * 64 * 2.220446049250313e-16 +
-                       4 * 2.220446049250313e-16;
+                       6 * 2.220446049250313e-16;
         if (!(bound < ldexp(1.0, -44))) fast = false;
     }
     g.fast = fast ? 1 : 0;
