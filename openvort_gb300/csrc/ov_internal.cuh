@@ -254,9 +254,8 @@ struct ov_ctx {
     float *rec_split = nullptr;
     double *h_corr = nullptr;    // pinned host copy of the corrections
     size_t h_corr_cap = 0;
-    double *rec_pf = nullptr, *h_pf = nullptr;   // prefetched corrections (device, pinned host)
-    int *rec_pf_idx = nullptr;
-    int rec_pf_cap = 0;
+    double *h_pf = nullptr;      // prefetched corrections (pinned, mapped host memory)
+    double *h_pf_dev = nullptr;  // the same as the device sees it
     cudaEvent_t rec_ev = nullptr;
     int rec_cap = 0, rec_split_cap = 0;
     size_t rec_part_cap = 0;
@@ -321,9 +320,9 @@ int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out
 // reconnection velocities (ov_velocity.cu)
 int ov_rec_begin(ov_ctx *c, const int *cand, int n, double *out);
 int ov_rec_exact(ov_ctx *c, int k, int l, double out[10]);
-int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const double *sign, int nch);
+int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const double *sign, int nch,
+                   const int *pf, int npf);
 int ov_rec_fetch(ov_ctx *c, int c0, int n, double *out);
-int ov_rec_prefetch(ov_ctx *c, const int *idx, int n);
 int ov_rec_wait(ov_ctx *c);
 void ov_launch_euler(ov_ctx *c, const NodeArrays &src, const double *vx, const double *vy,
                      const double *vz, double dt, NodeArrays &dst, cudaStream_t s);

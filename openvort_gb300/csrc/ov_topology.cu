@@ -1709,7 +1709,9 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     std::vector<int> corr_gen(C, 0), pf_gen(C, -1), pf_pos(C, 0);
     int gen = 0;
     bool pf_waited = true;
-    const int kFetch = 256, kAhead = 48;
+    const int kFetch = 256, kAhead = 48;   // 2 kAhead candidates at most: within the correction's read-back list
+    std::vector<int> ahead;
+    ahead.reserve(2 * kAhead);
     int64_t evaluated = 0;
     c->stats.reconnect_candidates = C;
     c->stats.reconnect_fp64_pairs = 0;
@@ -1886,12 +1888,11 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
             // candidates still to come (pairs are (k, l > k), sorted by k)
             const int cfrom = cand_index(k) + 1;
             const auto tc = clk();
-            if (ce > cfrom && (r = ov_rec_correct(c, cfrom, ce - cfrom, cm, cfw, csg, 4))) return r;
             ++gen;
-            {
-                // read back ahead the corrections of the next pairs' candidates
-                std::vector<int> ahead;
-                ahead.reserve(2 * kAhead);
+            if (ce > cfrom) {
+                // the correction, and the read-back of the next pairs' candidates'
+                // corrections after it (one launch, straight into host memory)
+                ahead.clear();
                 for (size_t qq = e; qq < pairs.size() && qq < e + kAhead; ++qq) {
                     for (int node : {pairs[qq].first, pairs[qq].second}) {
                         int cj = cand_index(node);
@@ -1901,10 +1902,9 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
                         ahead.push_back(cj);
                     }
                 }
-                if (!ahead.empty()) {
-                    if ((r = ov_rec_prefetch(c, ahead.data(), (int)ahead.size()))) return r;
-                    pf_waited = false;
-                }
+                if ((r = ov_rec_correct(c, cfrom, ce - cfrom, cm, cfw, csg, 4, ahead.data(), (int)ahead.size())))
+                    return r;
+                pf_waited = false;
             }
             c->step_ms[13] += ms_since(tc);
             recalc[k]++; recalc[h.fwd(k)]++; recalc[h.rev(k)]++; recalc[kn]++; recalc[kp]++;

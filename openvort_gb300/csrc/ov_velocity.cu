@@ -1900,21 +1900,15 @@ struct RecChange {
     int n;
 };
 
-// Contribution of the changed segments to candidates [c0, c0 + nc) of the
-// sorted candidate list, one thread per (candidate, query point): FP32 on
-// the split positions with the error bound of k_rec_sums, FP64 near the
-// query point.  part: 4 doubles per thread (3 sums, bound).
-__global__ void k_corr(RecArgs r, const int *__restrict__ cand, int c0, int nc, RecChange ch,
-                       double *__restrict__ part)
+// Contribution of the changed segments to candidate node k at query point j
+// (j < 0 the node itself): FP32 on the split positions with the error bound
+// of k_rec_sums, FP64 near the query point.  out: 3 sums, bound.
+__device__ __forceinline__ void corr_point(const RecArgs &r, int k, int j, const RecChange &ch, double out[4])
 {
-    const int nq = r.geo.n_img + 1;
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= nc * nq) return;
-    int ci = idx / nq, qi = idx - ci * nq;
-    const int j = qi - 1;
-    int k = cand[c0 + ci];
-    double acc[3] = {0, 0, 0};
+    double acc[3] = {0, 0, 0};   // FP64 terms
     double bound = 0;
+    float tf[3] = {0, 0, 0};     // FP32 terms, their magnitudes' sum sc |R| |s|
+    float mag = 0;
     if (k >= 0 && k < r.cap) {
         const double p[3] = {r.x[k], r.y[k], r.z[k]};
         float qg[3], qf[3];
@@ -1966,26 +1960,60 @@ __global__ void k_corr(RecArgs r, const int *__restrict__ cand, int c0, int nc, 
             if (nd < 1e-8f) continue;
             const float sc = __fdividef(r.f4pif * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
             const float slen = sqrtf(fmaf(sv[0], sv[0], fmaf(sv[1], sv[1], sv[2] * sv[2])));
-            acc[0] += ch.sign[i] * (double)(fmaf(R[1], sv[2], -R[2] * sv[1]) * sc);
-            acc[1] += ch.sign[i] * (double)(fmaf(R[2], sv[0], -R[0] * sv[2]) * sc);
-            acc[2] += ch.sign[i] * (double)(fmaf(R[0], sv[1], -R[1] * sv[0]) * sc);
-            bound += 1.01 * 64.0 * 5.9604644775390625e-8 * (double)(sc * slen * lR2 * ra);
+            const float sg = (float)ch.sign[i];   // +-1
+            tf[0] += sg * (fmaf(R[1], sv[2], -R[2] * sv[1]) * sc);
+            tf[1] += sg * (fmaf(R[2], sv[0], -R[0] * sv[2]) * sc);
+            tf[2] += sg * (fmaf(R[0], sv[1], -R[1] * sv[0]) * sc);
+            mag += sc * slen * lR2 * ra;
         }
     }
-    for (int a = 0; a < 3; ++a) part[(size_t)idx * 4 + a] = acc[a];
-    part[(size_t)idx * 4 + 3] = bound;
+    // per term 64 eps32 of sc |R| |s| (as k_rec_sums), plus at most 8 eps32 of
+    // the same for the FP32 additions of up to 8 terms; 1.01 covers the
+    // rounding of mag itself
+    for (int a = 0; a < 3; ++a) out[a] = acc[a] + (double)tf[a];
+    out[3] = bound + 1.01 * 72.0 * 5.9604644775390625e-8 * (double)mag;
 }
 
-// corr[4 c + {0,1,2}] += the query points' sums in order, corr[4 c + 3] += bound
-__global__ void k_corr_finish(const double *__restrict__ part, int nc, int nq, double *__restrict__ corr)
+// Prefetch list of a correction: candidates whose corrections go straight to
+// the mapped host buffer after the update (position i: 4 doubles at 4 i).
+constexpr int kPrefetchMax = 128;
+struct RecPrefetch {
+    int idx[kPrefetchMax];
+    int n;
+};
+
+// Contributions of the changed segments to candidates [c0, c0 + nc) of the
+// sorted candidate list, one thread per (candidate, query point).  part: 4
+// doubles per thread (3 sums, bound).
+__global__ void k_corr(RecArgs r, const int *__restrict__ cand, int c0, int nc, RecChange ch,
+                       double *__restrict__ part)
 {
-    int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nq = r.geo.n_img + 1;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nc * nq) return;
+    const int ci = idx / nq, qi = idx - ci * nq;
+    double out[4];
+    corr_point(r, cand[c0 + ci], qi - 1, ch, out);
+    for (int a = 0; a < 4; ++a) part[(size_t)idx * 4 + a] = out[a];
+}
+
+// corr[4 c + {0,1,2}] += the query points' sums in order, corr[4 c + 3] +=
+// bound; then the prefetched candidates' corrections into host memory (h_out,
+// mapped: position i of the list at 4 i).
+__global__ void k_corr_finish(const double *__restrict__ part, int c0, int nc, int nq, double *__restrict__ corr,
+                              RecPrefetch pf, double *h_out)
+{
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
     if (ci >= nc) return;
     double acc[4] = {0, 0, 0, 0};
     for (int q = 0; q < nq; ++q)
         for (int a = 0; a < 4; ++a) acc[a] += part[((size_t)ci * nq + q) * 4 + a];
-    for (int a = 0; a < 3; ++a) corr[4 * (size_t)ci + a] += acc[a];
-    corr[4 * (size_t)ci + 3] += acc[3] * (1.0 + 1e-9) + 1e-15 * (fabs(acc[0]) + fabs(acc[1]) + fabs(acc[2]));
+    double *cc = corr + 4 * (size_t)(c0 + ci);
+    for (int a = 0; a < 3; ++a) cc[a] += acc[a];
+    cc[3] += acc[3] * (1.0 + 1e-9) + 1e-15 * (fabs(acc[0]) + fabs(acc[1]) + fabs(acc[2]));
+    for (int i = 0; i < pf.n && i < kPrefetchMax; ++i)
+        if (pf.idx[i] == c0 + ci)
+            for (int a = 0; a < 4; ++a) h_out[4 * i + a] = cc[a];
 }
 
 RecArgs make_rec_args(ov_ctx *c)
@@ -2169,57 +2197,32 @@ int ov_direct_sum_chunked(ov_ctx *c, const int *nodes, int n, double *d_out_vel,
 // Add the changed segments' contributions (and their error bounds) to
 // candidates [c0, c0 + nc) on the device (asynchronous; ov_rec_fetch reads
 // them back).
-int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const double *sign, int nch)
+// The changed segments' contributions to candidates [c0, c0 + nc), then the
+// corrections of candidates pf[0..npf) (all within that range) read back into
+// the pinned, mapped buffer c->h_pf; ov_rec_wait waits for both.
+int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const double *sign, int nch,
+                   const int *pf, int npf)
 {
     if (nc <= 0) return OV_OK;
+    if (npf < 0 || npf > kPrefetchMax) return ov_fail(c, OV_ERR_ARG, "reconnect: %d prefetched candidates", npf);
+    if (!c->h_pf) {
+        OV_CUDA(c, cudaHostAlloc(&c->h_pf, kPrefetchMax * 4 * sizeof(double), cudaHostAllocMapped));
+        OV_CUDA(c, cudaHostGetDevicePointer((void **)&c->h_pf_dev, c->h_pf, 0));
+    }
+    if (!c->rec_ev) OV_CUDA(c, cudaEventCreateWithFlags(&c->rec_ev, cudaEventDisableTiming));
     RecChange ch;
     memset(&ch, 0, sizeof ch);
     ch.n = std::min(nch, 8);
     for (int i = 0; i < ch.n; ++i) { ch.m[i] = m[i]; ch.f[i] = f[i]; ch.sign[i] = sign[i]; }
+    RecPrefetch list;
+    list.n = npf;
+    for (int i = 0; i < npf; ++i) list.idx[i] = pf[i];
     RecArgs ra = make_rec_args(c);
     const int nq = c->geo.n_img + 1;
-    const int threads = nc * nq;
-    k_corr<<<(threads + 127) / 128, 128, 0, c->stream>>>(ra, c->rec_nodes, c0, nc, ch, c->rec_part);
-    k_corr_finish<<<(nc + 127) / 128, 128, 0, c->stream>>>(c->rec_part, nc, nq, c->rec_corr + 4 * (size_t)c0);
+    k_corr<<<(nc * nq + 127) / 128, 128, 0, c->stream>>>(ra, c->rec_nodes, c0, nc, ch, c->rec_part);
+    k_corr_finish<<<(nc + 127) / 128, 128, 0, c->stream>>>(c->rec_part, c0, nc, nq, c->rec_corr, list, c->h_pf_dev);
     c->launches += 2;
     OV_CUDA(c, cudaGetLastError());
-    return OV_OK;
-}
-
-namespace {
-__global__ void k_corr_gather(const double *__restrict__ corr, const int *__restrict__ idx, int n,
-                              double *__restrict__ out)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 4 * n) return;
-    out[i] = corr[4 * (size_t)idx[i >> 2] + (i & 3)];
-}
-}  // namespace
-
-// Start reading back the corrections of candidates idx[0..n) (after every
-// correction launched so far) into the pinned buffer c->h_pf; ov_rec_wait
-// waits for it.
-int ov_rec_prefetch(ov_ctx *c, const int *idx, int n)
-{
-    if (n <= 0) return OV_OK;
-    if (c->rec_pf_cap < n) {
-        if (c->rec_pf) cudaFree(c->rec_pf);
-        if (c->rec_pf_idx) cudaFree(c->rec_pf_idx);
-        if (c->h_pf) cudaFreeHost(c->h_pf);
-        c->rec_pf = nullptr; c->rec_pf_idx = nullptr; c->h_pf = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->rec_pf, (size_t)n * 4 * sizeof(double)));
-        OV_CUDA(c, cudaMalloc(&c->rec_pf_idx, (size_t)n * sizeof(int)));
-        OV_CUDA(c, cudaMallocHost(&c->h_pf, (size_t)n * (4 * sizeof(double) + sizeof(int))));
-        c->rec_pf_cap = n;
-    }
-    if (!c->rec_ev) OV_CUDA(c, cudaEventCreateWithFlags(&c->rec_ev, cudaEventDisableTiming));
-    int *h_idx = (int *)(c->h_pf + 4 * (size_t)c->rec_pf_cap);
-    memcpy(h_idx, idx, (size_t)n * sizeof(int));
-    OV_CUDA(c, cudaMemcpyAsync(c->rec_pf_idx, h_idx, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    k_corr_gather<<<(4 * n + 127) / 128, 128, 0, c->stream>>>(c->rec_corr, c->rec_pf_idx, n, c->rec_pf);
-    c->launches++;
-    OV_CUDA(c, cudaMemcpyAsync(c->h_pf, c->rec_pf, (size_t)n * 4 * sizeof(double), cudaMemcpyDeviceToHost,
-                               c->stream));
     OV_CUDA(c, cudaEventRecord(c->rec_ev, c->stream));
     return OV_OK;
 }
