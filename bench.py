@@ -262,7 +262,7 @@ def run_ensemble(args, device=0):
     recs = added = 0
     passes = {}
     rstat = {"reconnect_candidates": 0, "reconnect_evaluated": 0, "reconnect_fp64_pairs": 0,
-             "reconnect_exact_pairs": 0}
+             "reconnect_exact_pairs": 0, "reconnect_lazy_evals": 0}
     t0 = time.perf_counter()
     for k in range(K):
         ctx.step(k * dt, dt)
@@ -419,7 +419,7 @@ def run_large(args, device=0):
     K = args.large_steps
     passes, recs, added = {}, 0, 0
     rstat = {"reconnect_candidates": 0, "reconnect_evaluated": 0, "reconnect_fp64_pairs": 0,
-             "reconnect_exact_pairs": 0}
+             "reconnect_exact_pairs": 0, "reconnect_lazy_evals": 0}
     t0 = time.perf_counter()
     for k in range(K):
         ctx.step(k * dt, dt)

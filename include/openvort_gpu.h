@@ -125,6 +125,7 @@ typedef struct ov_stats {
     int64_t wall_clipped;           /* last wall pass: nodes connected to a wall */
     int64_t wall_removed;           /* last wall pass: nodes removed behind a wall */
     int64_t injected_nodes;         /* last injection pass: nodes added */
+    int64_t reconnect_lazy_evals;   /* candidate velocities decided with a bound on corrections not yet read back */
 } ov_stats;
 
 typedef struct ov_ctx ov_ctx;

@@ -111,7 +111,8 @@ class Stats(C.Structure):
         "node_evals", "cells", "max_depth", "visits", "accepts", "warp_steps", "fp64_fallbacks",
         "near_field_fp64", "out_of_root", "reconnections", "remesh_added", "remesh_removed",
         "small_loops_removed", "error_word", "reconnect_candidates", "reconnect_fp64_pairs",
-        "reconnect_exact_pairs", "reconnect_evaluated", "wall_clipped", "wall_removed", "injected_nodes")]
+        "reconnect_exact_pairs", "reconnect_evaluated", "wall_clipped", "wall_removed", "injected_nodes",
+        "reconnect_lazy_evals")]
 
 
 class Injection(C.Structure):

@@ -1710,8 +1710,14 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     int gen = 0;
     bool pf_waited = true;
     const int kFetch = 256, kAhead = 48;   // 2 kAhead candidates at most: within the correction's read-back list
+    const int kLazy = 16;                  // rewirings a copy may lack (bounded instead of read back)
     std::vector<int> ahead;
     ahead.reserve(2 * kAhead);
+    struct Rewire {
+        double a[4][3], b[4][3];
+    };
+    std::vector<Rewire> rw;   // rewiring r: its four changed segments
+    c->stats.reconnect_lazy_evals = 0;
     int64_t evaluated = 0;
     c->stats.reconnect_candidates = C;
     c->stats.reconnect_fp64_pairs = 0;
@@ -1744,25 +1750,76 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     // bound on how far it may sit from the reference's update_velocity: the
     // error of our sum plus the rounding of the reference's own sequential
     // sum of 27 N terms (at most (27 N - 1) eps64 times their magnitudes)
-    auto velocity = [&](int k, const double tg[3], const double nm[3], double vel[3], double *bound) -> bool {
+    // Rewirings whose corrections a candidate's copy lacks may be covered by a
+    // bound instead of waiting for the device: a straight segment S at
+    // distance d from a point adds at most kappa |S| / (4 pi d^2) to its
+    // velocity (|dl x r| / |r|^3 <= |dl| / d^2 along it), summed over the
+    // changed segments and every query point.  A pair it does not decide
+    // waits for the exact corrections.
+    auto pending_bound = [&](int ci, int k) -> double {
+        double x[3], qs[OV_MAX_IMAGES + 1][3];
+        h.pos(k, x);
+        const int nq = g.n_img + 1;
+        for (int a = 0; a < 3; ++a) qs[0][a] = x[a];
+        for (int j = 0; j < g.n_img; ++j) himage(g, j, x, qs[j + 1]);
+        double b = 0;
+        for (int r = corr_gen[ci]; r < gen; ++r)
+            for (int sgi = 0; sgi < 4; ++sgi) {
+                const double *A = rw[r].a[sgi], *B = rw[r].b[sgi];
+                double S[3];
+                hsub(S, B, A);
+                const double s2 = hdot(S, S);
+                if (!(s2 > 0)) continue;   // a segment of zero length adds nothing
+                for (int qi = 0; qi < nq; ++qi) {
+                    double QA[3];
+                    hsub(QA, qs[qi], A);
+                    double u = hdot(QA, S) / s2;
+                    u = u < 0 ? 0 : (u > 1 ? 1 : u);
+                    double d[3];
+                    for (int a = 0; a < 3; ++a) d[a] = QA[a] - u * S[a];
+                    const double d2 = hdot(d, d);
+                    if (!(d2 > 0)) return HUGE_VAL;
+                    b += sqrt(s2) / d2;
+                }
+            }
+        return b * h.P->kappa / (4 * M_PI) * (1.0 + 1e-9);
+    };
+    // copy the corrections of the last correction's read-back list (complete
+    // once ov_rec_wait returned)
+    auto take_prefetch = [&]() {
+        for (size_t i = 0; i < ahead.size(); ++i) {
+            const int cj = ahead[i];
+            if (pf_gen[cj] != gen || corr_gen[cj] >= gen) continue;
+            for (int a = 0; a < 4; ++a) corr[4 * (size_t)cj + a] = c->h_pf[4 * i + a];
+            corr_gen[cj] = gen;
+        }
+    };
+    // lazy: the copy may lack the last kLazy rewirings (covered by the bound)
+    auto velocity = [&](int k, const double tg[3], const double nm[3], double vel[3], double *bound,
+                        bool lazy, bool *used_lazy) -> bool {
         double vs[3];
         if (!hlia(h, k, tg, nm, t, vs)) return false;
         int ci = cand_index(k);
         static const double zero4[4] = {0, 0, 0, 0};
         const double *rc, *cc;
+        double extra = 0;
+        if (used_lazy) *used_lazy = false;
         if (ex_gen[ci] == gen) {
             rc = &ex[5 * (size_t)ci];   // FP64 on the current topology: no corrections
             cc = zero4;
         } else {
-            if (corr_gen[ci] < gen) {
+            if (corr_gen[ci] < gen && lazy && gen - corr_gen[ci] <= kLazy) {
+                extra = pending_bound(ci, k);
+                if (used_lazy) *used_lazy = true;
+                ++c->stats.reconnect_lazy_evals;
+            } else if (corr_gen[ci] < gen) {
                 const auto tf = clk();
                 if (pf_gen[ci] == gen) {
                     if (!pf_waited) {
                         if (ov_rec_wait(c)) return false;
                         pf_waited = true;
                     }
-                    for (int a = 0; a < 4; ++a) corr[4 * (size_t)ci + a] = c->h_pf[4 * (size_t)pf_pos[ci] + a];
-                    corr_gen[ci] = gen;
+                    take_prefetch();
                 } else {
                     const int n = std::min(ce, ci + kFetch) - ci;
                     if (ov_rec_fetch(c, ci, n, corr + 4 * (size_t)ci)) return false;
@@ -1779,7 +1836,8 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         hfriction(h, k, tg, vs, t, vel);
         const double tl = hlen(tg);
         const double n_terms = (double)(h.hi - h.lo) * (g.n_img + 1);
-        const double comp = rc[3] + cc[3] + n_terms * 1.1102230246251565e-16 * rc[4];
+        // the reference's rounding covers the missing terms' magnitudes too
+        const double comp = rc[3] + cc[3] + n_terms * 1.1102230246251565e-16 * (rc[4] + extra) + extra;
         // the friction terms are linear in vs: |d vel| <= |d vs| (1 + alpha |t| + alpha' |t|^2)
         *bound = comp * 1.7320508075688772 * 1.01 * (1.0 + fabs(h.P->alpha) * tl + fabs(h.P->alpha_p) * tl * tl);
         return true;
@@ -1811,7 +1869,8 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
             if (hlen(tk) < 0.5 || hlen(tl) < 0.5) continue;
             if (hdot(tk, tl) / hlen(tk) / hlen(tl) > cos_cut) continue;
             double vk[3], vl[3], bk = 0, bl = 0;
-            if (!velocity(k, tk, nk, vk, &bk) || !velocity(l, tl, nl_, vl, &bl))
+            bool lk = false, ll = false;
+            if (!velocity(k, tk, nk, vk, &bk, true, &lk) || !velocity(l, tl, nl_, vl, &bl, true, &ll))
                 return ov_fail(c, OV_ERR_TOPOLOGY, "reconnect: velocity of %d or %d failed", k, l);
             double v1[3], v2[3], dx[3], dv[3];
             h.pos(k, v1);
@@ -1820,6 +1879,13 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
             hsub(dx, v1, v2);
             hsub(dv, vk, vl);
             double proj = hdot(dx, dv);
+            if ((lk || ll) && fabs(proj) <= hlen(dx) * (bk + bl) + 1e-9 * hlen(dx) * hlen(dv)) {
+                // the bound on the missing corrections does not decide: the exact ones
+                if (!velocity(k, tk, nk, vk, &bk, false, nullptr) || !velocity(l, tl, nl_, vl, &bl, false, nullptr))
+                    return ov_fail(c, OV_ERR_TOPOLOGY, "reconnect: velocity of %d or %d failed", k, l);
+                hsub(dv, vk, vl);
+                proj = hdot(dx, dv);
+            }
             if (fabs(proj) <= hlen(dx) * (bk + bl) + 1e-9 * hlen(dx) * hlen(dv)) {
                 // the mixed-precision sums cannot decide: FP64 sums of both
                 // on the current topology (the device's connections are
@@ -1842,8 +1908,8 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
                         ex[5 * (size_t)cl + a] = exv[5 + a];
                     }
                     ex_gen[ck] = ex_gen[cl] = gen;
-                    velocity(k, tk, nk, vk, &bk);
-                    velocity(l, tl, nl_, vl, &bl);
+                    velocity(k, tk, nk, vk, &bk, false, nullptr);
+                    velocity(l, tl, nl_, vl, &bl, false, nullptr);
                     hsub(dv, vk, vl);
                     proj = hdot(dx, dv);
                 }
@@ -1888,6 +1954,16 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
             // candidates still to come (pairs are (k, l > k), sorted by k)
             const int cfrom = cand_index(k) + 1;
             const auto tc = clk();
+            {
+                // the four changed segments as the sums see them (wrapped end)
+                Rewire rr;
+                for (int sgi = 0; sgi < 4; ++sgi) {
+                    h.pos(cm[sgi], rr.a[sgi]);
+                    h.pos(cfw[sgi], rr.b[sgi]);
+                    hpwrap(g, rr.a[sgi], rr.b[sgi]);
+                }
+                rw.push_back(rr);
+            }
             ++gen;
             if (ce > cfrom) {
                 // the correction, and the read-back of the next pairs' candidates'
