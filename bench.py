@@ -651,14 +651,17 @@ def run_ours(args):
         ctx.upload(ht)
         for _ in range(args.warmup):
             ctx.update_tangle(0.0)
-        mt = []
+        mt, mph = [], []
         for _ in range(args.steps):
             ctx.flush_l2(256 << 20)
             ctx.timer_start()
             ctx.update_tangle(0.0)
             mt.append(ctx.timer_stop())
+            mph.append(ctx.phase_times()[2])
         ctx.download(ht, abi.OV_F_VELS)
         mst = ctx.stats()
+        # the same flop convention on the FP32 pipe (the walk's tests are FP32 here)
+        m_achieved = (42 * mst["accepts"] + 9 * mst["visits"]) / (statistics.mean(mph) * 1e-3) / 1e12
         err = float(np.linalg.norm(ht.vels - ref_v) / np.linalg.norm(ref_v))
         mixed_vels = np.array(ht.vels)
         mixed = {"value": world * n / (statistics.mean(mt) * 1e-3), "unit": UNIT,
@@ -666,7 +669,12 @@ def run_ours(args):
                  "speedup_vs_fp64": mean_ms / statistics.mean(mt),
                  "same_decisions_as_fp64": bool(mst["accepts"] == acc and mst["visits"] == vis),
                  "fp64_guard_band_decisions": mst["fp64_fallbacks"], "fp64_near_field": mst["near_field_fp64"],
-                 "warp_efficiency": mst["visits"] / max(1, 32 * mst["warp_steps"])}
+                 "warp_efficiency": mst["visits"] / max(1, 32 * mst["warp_steps"]),
+                 "roofline": {"bound": "issue", "pipe": "fp32", "achieved": m_achieved, "peak": fp32_peak,
+                              "unit": "TFLOP/s", "frac": m_achieved / fp32_peak,
+                              "traversal_ms": statistics.mean(mph),
+                              "work": "42 flops per accepted interaction + 9 per visited cell",
+                              "note": "instruction issue and latency bound (the walk), not the FMA pipe"}}
         ctx.set_precision(abi.OV_PREC_FP64)
     except Exception as e:  # mixed path not built yet
         mixed = {"unavailable": str(e)[:200]}
