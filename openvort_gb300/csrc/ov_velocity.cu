@@ -1715,10 +1715,11 @@ __device__ __forceinline__ bool rec_term64_fast(const RecArgs &r, int m, int f, 
 constexpr int kRecThreads = 256;
 constexpr int kRecVals = 7;   // 3 sums, FP32 magnitude, 3 spare (|FP64 terms|)
 
-template <int MODE>
+template <int MODE, bool MIRROR>
 __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const int *__restrict__ nodes, int n,
                                                           int span, int max_chunks, double *__restrict__ part)
-// MODE: 0 FP32 far / FP64 near, 1 all FP64, 2 double-single far / FP64 near
+// MODE: 0 FP32 far / FP64 near, 1 all FP64, 2 double-single far / FP64 near.
+// MIRROR: the image set has mirror images (their query points in FP64).
 {
     constexpr int force64 = MODE;
     // split query points (self, then images): (g, mirror flag), (f, 0), (f's rest, 0)
@@ -1814,21 +1815,21 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
             const float lR2 = fmaf(R0, R0, fmaf(R1, R1, R2 * R2));
             const float P0 = R0 + sv[0], P1 = R1 + sv[1], P2 = R2 + sv[2];
             const float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
-            bool use64 = seg64 || lR2 < r.rnear2 || lp2 < r.rnear2 || qg.w != 0.0f;
-            float ra = 0, rb = 0, ab = 0, dot = 0, nd = 0;
-            if (!use64) {
-                ra = rsqrtf(lR2);
-                rb = rsqrtf(lp2);
-                ab = ra * rb;
-                dot = fmaf(R0, P0, fmaf(R1, P1, R2 * P2));
-                nd = dot * ab;
-                if (fabsf(nd - 1e-8f) < 1e-4f) use64 = true;   // filter near its threshold
+            const float ra = rsqrtf(lR2), rb = rsqrtf(lp2);
+            const float ab = ra * rb;
+            const float dot = fmaf(R0, P0, fmaf(R1, P1, R2 * P2));
+            const float nd = dot * ab;
+            // the common case in one test: both ends beyond r_near, the filter
+            // clear of its band and passing
+            if (seg64 || fminf(lR2, lp2) < r.rnear2 || !(nd > 1e-8f + 1e-4f) || (MIRROR && qg.w != 0.0f)) {
+                const bool use64 = seg64 || lR2 < r.rnear2 || lp2 < r.rnear2 || (MIRROR && qg.w != 0.0f) ||
+                                   fabsf(nd - 1e-8f) < 1e-4f;   // filter near its threshold
+                if (use64) {   // FP64 after the loop over the query points
+                    mask64 |= 1u << qi;
+                    continue;
+                }
+                if (nd < 1e-8f) continue;   // ndot filter (far from its threshold here)
             }
-            if (use64) {   // FP64 after the loop over the query points
-                mask64 |= 1u << qi;
-                continue;
-            }
-            if (nd < 1e-8f) continue;   // ndot filter (far from its threshold here)
             if (MODE == 2) {
                 const float4 qfl = s_q[qi][2];
                 const float gq[3] = {qg.x, qg.y, qg.z}, fqh[3] = {qf.x, qf.y, qf.z}, fql[3] = {qfl.x, qfl.y, qfl.z};
@@ -1839,7 +1840,7 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
                 magdd += fabsf(w[0].hi) + fabsf(w[1].hi) + fabsf(w[2].hi);
                 continue;
             }
-            const float sc = __fdividef(r.f4pif * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
+            const float sc = __fdividef((ra + rb) * ab, fmaf(dot, ab, 1.0f));   // kappa / 4 pi: on the sums
             // R x Rp1 = R x s
             t0 = fmaf(fmaf(R1, sv[2], -R2 * sv[1]), sc, t0);
             t1 = fmaf(fmaf(R2, sv[0], -R0 * sv[2]), sc, t1);
@@ -1859,12 +1860,14 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
         kahan_add(s1, c1, t1);
         kahan_add(s2, c2, t2);
     }
-    red[0][threadIdx.x] = ((double)s0 - (double)c0) + d0 + ((double)dd[0].hi + (double)dd[0].lo);
-    red[1][threadIdx.x] = ((double)s1 - (double)c1) + d1 + ((double)dd[1].hi + (double)dd[1].lo);
-    red[2][threadIdx.x] = ((double)s2 - (double)c2) + d2 + ((double)dd[2].hi + (double)dd[2].lo);
-    red[3][threadIdx.x] = (double)mag;
+    // the FP32 terms lack kappa / 4 pi (one more rounding: within the bound's 1.01)
+    const double f4 = r.f4pi;
+    red[0][threadIdx.x] = ((double)s0 - (double)c0) * f4 + d0 + ((double)dd[0].hi + (double)dd[0].lo);
+    red[1][threadIdx.x] = ((double)s1 - (double)c1) * f4 + d1 + ((double)dd[1].hi + (double)dd[1].lo);
+    red[2][threadIdx.x] = ((double)s2 - (double)c2) * f4 + d2 + ((double)dd[2].hi + (double)dd[2].lo);
+    red[3][threadIdx.x] = (double)mag * f4;
     red[4][threadIdx.x] = dabs;
-    red[5][threadIdx.x] = fabs((double)s0) + fabs((double)s1) + fabs((double)s2);
+    red[5][threadIdx.x] = (fabs((double)s0) + fabs((double)s1) + fabs((double)s2)) * f4;
     red[6][threadIdx.x] = (double)magdd;
     __syncthreads();
     for (int off = blockDim.x / 2; off > 0; off >>= 1) {
@@ -2097,12 +2100,18 @@ int rec_launch_sums(ov_ctx *c, const int *d_nodes, int n, int mode, double *out_
     if (r) return r;
     RecArgs ra = make_rec_args(c);
     dim3 grid(n, max_chunks);
+    bool mirror = false;
+    for (int j = 0; j < c->geo.n_img; ++j) mirror = mirror || c->geo.nreflect[j] > 0;
     if (mode == 1)
-        k_rec_sums<1><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
+        k_rec_sums<1, true><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
+    else if (mode == 2 && mirror)
+        k_rec_sums<2, true><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
     else if (mode == 2)
-        k_rec_sums<2><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
+        k_rec_sums<2, false><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
+    else if (mirror)
+        k_rec_sums<0, true><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
     else
-        k_rec_sums<0><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
+        k_rec_sums<0, false><<<grid, kRecThreads, 0, c->stream>>>(ra, d_nodes, n, span, max_chunks, c->rec_part);
     k_rec_finish<<<(n + 127) / 128, 128, 0, c->stream>>>(c->rec_part, n, max_chunks, c->rec_out);
     c->launches += 2;
     OV_CUDA(c, cudaGetLastError());
@@ -2184,7 +2193,7 @@ int ov_direct_sum_chunked(ov_ctx *c, const int *nodes, int n, double *d_out_vel,
     k_split<<<(c->cap + 255) / 256, 256, 0, c->stream>>>(c->node.x, c->node.y, c->node.z, c->cap, c->grid_h,
                                                         1.0 / c->grid_h, c->rec_split);
     RecArgs ra = make_rec_args(c);
-    k_rec_sums<1><<<dim3(n, max_chunks), kRecThreads, 0, c->stream>>>(ra, c->rec_nodes, n, span, max_chunks,
+    k_rec_sums<1, true><<<dim3(n, max_chunks), kRecThreads, 0, c->stream>>>(ra, c->rec_nodes, n, span, max_chunks,
                                                                       c->rec_part);
     k_rec_finish<<<(n + 127) / 128, 128, 0, c->stream>>>(c->rec_part, n, max_chunks, c->rec_out);
     VelArgs a = make_args(c, c->node, t, nullptr);
