@@ -841,13 +841,13 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
     int steps = 0;
     // plain FP32 sub-sums, folded into the Kahan sums every 16 warp steps
     float p0 = 0, p1 = 0, p2 = 0;
+    // c only grows (nxt > c is checked), so it stays within [root, ncell)
     while (c < ncell) {
-        if (c < root) { bad_index(a, 1, c); break; }
         const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
         float4 A = __ldg(cp4), B = __ldg(cp4 + 1), Cc = __ldg(cp4 + 2);
         // A = (gx, gy, gz, fx)  B = (fy, fz, qx, qy)  Cc = (qz, lm, next, count)
         int nxt = __float_as_int(Cc.z);
-        if (nxt <= c || nxt > ncell) { bad_index(a, 2, c); nxt = ncell; }
+        if ((unsigned)(nxt - c - 1) >= (unsigned)(ncell - c)) { bad_index(a, 2, c); nxt = ncell; }
         bool open = false;
         if (c >= resume) {
             ++m.nvis;
@@ -882,7 +882,12 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
                 const float ra = rsqrtf(d2), rb = rsqrtf(lp2);
                 const float ab = ra * rb;
                 const float nd = dot * ab;
-                const bool defer = exact || (!DD && leaf && d2 < near2) || lp2 < d2hi || fabsf(nd - 1e-8f) < 4e-6f;
+                // the common case in one test: no deferral, the filter passing clear of its band
+                bool defer = false, keep = true;
+                if (exact || (!DD && leaf && d2 < near2) || lp2 < d2hi || !(nd > 1e-8f + 4e-6f)) {
+                    defer = exact || (!DD && leaf && d2 < near2) || lp2 < d2hi || fabsf(nd - 1e-8f) < 4e-6f;
+                    keep = nd >= 1e-8f;
+                }
                 if (defer) {
                     // near field, or a filter inside its guard band: FP64, after the traversal
                     ++m.nnear;
@@ -898,7 +903,7 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
                             w64[0] += w[0]; w64[1] += w[1]; w64[2] += w[2];
                         }
                     }
-                } else if (nd >= 1e-8f) {
+                } else if (keep) {
                     if (DD) {
                         ff acc[3] = {ff{m.s0, m.c0}, ff{m.s1, m.c1}, ff{m.s2, m.c2}};
                         ff_law(a.cellsff + c, gqq, qff, ff{a.f4pi_h, a.f4pi_l}, acc);
@@ -921,14 +926,16 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
             }
         }
         ++steps;
-        if (!DD && (steps & 15) == 0) {   // warp-uniform
-            kahan_add(m.s0, m.c0, p0);
-            kahan_add(m.s1, m.c1, p1);
-            kahan_add(m.s2, m.c2, p2);
-            p0 = p1 = p2 = 0;
+        if ((steps & 15) == 0) {   // warp-uniform
+            if (!DD) {
+                kahan_add(m.s0, m.c0, p0);
+                kahan_add(m.s1, m.c1, p1);
+                kahan_add(m.s2, m.c2, p2);
+                p0 = p1 = p2 = 0;
+            }
+            if (steps > guard_max) { overflow = true; break; }
         }
         c = __any_sync(0xffffffffu, open) ? c + 1 : nxt;
-        if (steps > guard_max) { overflow = true; break; }
     }
     if (!DD) {
         kahan_add(m.s0, m.c0, p0);
