@@ -149,6 +149,7 @@ int ov_ctx_destroy(ov_ctx *c)
     if (c->part) cudaFree(c->part);
     if (c->flush_buf) cudaFree(c->flush_buf);
     if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->d_stage) cudaFree(c->d_stage);
     if (c->h_corr) cudaFreeHost(c->h_corr);
     if (c->h_pf) cudaFreeHost(c->h_pf);
     if (c->rec_ev) cudaEventDestroy(c->rec_ev);
@@ -337,6 +338,84 @@ static int ensure_stage(ov_ctx *c, size_t bytes)
     OV_CUDA(c, cudaMallocHost(&c->h_stage, bytes));
     c->h_stage_bytes = bytes;
     return OV_OK;
+}
+
+// The device copy of a host tangle's arrays (raw layout: the five vec3 fields
+// at f * n * 24 bytes, then connections and status at 120 n and 128 n).
+static int ensure_dstage(ov_ctx *c, size_t bytes)
+{
+    if (c->d_stage_bytes >= bytes) return OV_OK;
+    if (c->d_stage) cudaFree(c->d_stage);
+    c->d_stage = nullptr;
+    OV_CUDA(c, cudaMalloc(&c->d_stage, bytes));
+    c->d_stage_bytes = bytes;
+    return OV_OK;
+}
+
+struct NodePtrs {
+    double *d[15];   // x y z, vx vy vz, sx sy sz, tx ty tz, nx ny nz
+    int *fwd, *rev, *status, *pin;
+};
+
+__host__ __device__ inline size_t stage_topo_off(int n) { return (size_t)n * 120; }
+
+// Host layout (vec3 fields, ov_neighbour, ov_node_status) -> device arrays for
+// slots [0, cap): slots past n get zeros, -1 links, EMPTY, no wall.
+__global__ void k_unpack(const char *__restrict__ stage, unsigned fields, unsigned have, int n, int cap, NodePtrs d)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= cap) return;
+    const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
+#pragma unroll
+    for (int f = 0; f < 5; ++f) {
+        if (!(fields & bits[f])) continue;
+        const double *src = reinterpret_cast<const double *>(stage + (size_t)f * n * 24);
+        const bool in = k < n && (have & bits[f]);
+        for (int a = 0; a < 3; ++a) d.d[3 * f + a][k] = in ? src[3 * (size_t)k + a] : 0.0;
+    }
+    if (fields & OV_F_TOPOLOGY) {
+        const ov_neighbour *con = reinterpret_cast<const ov_neighbour *>(stage + stage_topo_off(n));
+        const ov_node_status *st = reinterpret_cast<const ov_node_status *>(stage + stage_topo_off(n) + (size_t)n * 8);
+        const bool in = k < n;
+        d.fwd[k] = in ? con[k].forward : -1;
+        d.rev[k] = in ? con[k].reverse : -1;
+        d.status[k] = in ? st[k].status : OV_EMPTY;
+        d.pin[k] = in ? st[k].pin_wall : OV_NOT_A_FACE;
+    }
+}
+
+// Device slots [lo, lo + n) -> host layout, links shifted by -lo.
+__global__ void k_pack(unsigned fields, int lo, int n, NodePtrs d, char *__restrict__ stage)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
+#pragma unroll
+    for (int f = 0; f < 5; ++f) {
+        if (!(fields & bits[f])) continue;
+        double *dst = reinterpret_cast<double *>(stage + (size_t)f * n * 24);
+        for (int a = 0; a < 3; ++a) dst[3 * (size_t)k + a] = d.d[3 * f + a][lo + k];
+    }
+    if (fields & OV_F_TOPOLOGY) {
+        ov_neighbour *con = reinterpret_cast<ov_neighbour *>(stage + stage_topo_off(n));
+        ov_node_status *st = reinterpret_cast<ov_node_status *>(stage + stage_topo_off(n) + (size_t)n * 8);
+        const int f = d.fwd[lo + k], b = d.rev[lo + k];
+        con[k].forward = f >= 0 ? f - lo : -1;
+        con[k].reverse = b >= 0 ? b - lo : -1;
+        st[k].status = d.status[lo + k];
+        st[k].pin_wall = d.pin[lo + k];
+    }
+}
+
+static NodePtrs node_ptrs(ov_ctx *c)
+{
+    NodePtrs p;
+    double *dd[15] = {c->node.x, c->node.y, c->node.z, c->node.vx, c->node.vy, c->node.vz,
+                      c->node.sx, c->node.sy, c->node.sz, c->node.tx, c->node.ty, c->node.tz,
+                      c->node.nx, c->node.ny, c->node.nz};
+    for (int i = 0; i < 15; ++i) p.d[i] = dd[i];
+    p.fwd = c->fwd; p.rev = c->rev; p.status = c->status; p.pin = c->pin;
+    return p;
 }
 
 static void set_geometry(ov_ctx *c, const ov_domain_box &box, const ov_boundary_images &bimg)
@@ -581,44 +660,44 @@ int ov_upload_tangle_fields(ov_ctx *c, const ov_tangle_state *t, unsigned fields
     set_geometry(c, t->box, t->bimg);
     if ((r = ov_upload_member_tables(c))) return r;
     size_t cap = (size_t)c->cap;
-    if ((r = ensure_stage(c, cap * 3 * sizeof(double) * 5 + cap * 4 * sizeof(int)))) return r;
-    double *h = c->h_stage;
-    int *hi = (int *)(h + 15 * cap);
-    // positions, vels, vs, tangents, normals: AoS -> SoA
-    const ov_vec3 *src[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
-    const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
-    double *dd[15] = {c->node.x, c->node.y, c->node.z, c->node.vx, c->node.vy, c->node.vz,
-                      c->node.sx, c->node.sy, c->node.sz, c->node.tx, c->node.ty, c->node.tz,
-                      c->node.nx, c->node.ny, c->node.nz};
-    c->last_h2d = 0;
-    for (int f = 0; f < 5; ++f) {
-        if (!(fields & bits[f])) continue;
-        double *dst = h + 3 * cap * f;
-        for (int a = 0; a < 3; ++a)
-            for (size_t k = 0; k < cap; ++k) dst[a * cap + k] = (src[f] && (int)k < n) ? src[f][k].p[a] : 0.0;
-        for (int a = 0; a < 3; ++a)
-            OV_CUDA(c, cudaMemcpyAsync(dd[3 * f + a], dst + a * cap, cap * sizeof(double), cudaMemcpyHostToDevice,
-                                       c->stream));
-        c->last_h2d += 3 * cap * sizeof(double);
-    }
     if (fields & OV_F_TOPOLOGY) {
         for (int k = 0; k < n; ++k) {
             int f = t->connections[k].forward, b = t->connections[k].reverse, st = t->status[k].status;
             if (f < -1 || f >= n || b < -1 || b >= n || st < OV_EMPTY || st > OV_PINNED_SLIP)
                 return ov_fail(c, OV_ERR_TOPOLOGY, "node %d: connections (%d,%d) / status %d out of range", k, f, b, st);
         }
-        for (size_t k = 0; k < cap; ++k) {
-            bool in = (int)k < n;
-            hi[k] = in ? t->connections[k].forward : -1;
-            hi[cap + k] = in ? t->connections[k].reverse : -1;
-            hi[2 * cap + k] = in ? t->status[k].status : OV_EMPTY;
-            hi[3 * cap + k] = in ? t->status[k].pin_wall : OV_NOT_A_FACE;
-        }
-        int *di[4] = {c->fwd, c->rev, c->status, c->pin};
-        for (int i = 0; i < 4; ++i)
-            OV_CUDA(c, cudaMemcpyAsync(di[i], hi + i * cap, cap * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-        c->last_h2d += 4 * cap * sizeof(int);
     }
+    // the host arrays as they are into pinned memory, one copy each, then the
+    // transposition to the device's arrays (k_unpack)
+    const size_t bytes = stage_topo_off(n) + (size_t)n * 16;
+    if ((r = ensure_stage(c, std::max(bytes, (size_t)16)))) return r;
+    if ((r = ensure_dstage(c, std::max(bytes, (size_t)16)))) return r;
+    char *h = reinterpret_cast<char *>(c->h_stage);
+    const ov_vec3 *src[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
+    const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
+    unsigned have = 0;
+    c->last_h2d = 0;
+    for (int f = 0; f < 5; ++f) {
+        if (!(fields & bits[f])) continue;
+        if (src[f] && n > 0) {
+            memcpy(h + (size_t)f * n * 24, src[f], (size_t)n * 24);
+            OV_CUDA(c, cudaMemcpyAsync(c->d_stage + (size_t)f * n * 24, h + (size_t)f * n * 24, (size_t)n * 24,
+                                       cudaMemcpyHostToDevice, c->stream));
+            have |= bits[f];
+        }
+        c->last_h2d += 3 * cap * sizeof(double);
+    }
+    if ((fields & OV_F_TOPOLOGY) && n > 0) {
+        memcpy(h + stage_topo_off(n), t->connections, (size_t)n * 8);
+        memcpy(h + stage_topo_off(n) + (size_t)n * 8, t->status, (size_t)n * 8);
+        OV_CUDA(c, cudaMemcpyAsync(c->d_stage + stage_topo_off(n), h + stage_topo_off(n), (size_t)n * 16,
+                                   cudaMemcpyHostToDevice, c->stream));
+    }
+    if (fields & OV_F_TOPOLOGY) c->last_h2d += 4 * cap * sizeof(int);
+    k_unpack<<<(unsigned)((cap + 255) / 256), 256, 0, c->stream>>>(c->d_stage, fields, have, n, (int)cap,
+                                                                    node_ptrs(c));
+    c->launches++;
+    OV_CUDA(c, cudaGetLastError());
     OV_CUDA(c, cudaStreamSynchronize(c->stream));
     c->uploaded = true;
     return OV_OK;
@@ -631,47 +710,39 @@ static int download_range(ov_ctx *c, ov_tangle_state *t, unsigned fields, int lo
                           int total_empty)
 {
     const int n = std::min(t->N, span);
-    const size_t m = (size_t)std::max(n, 1);
     int r;
-    if ((r = ensure_stage(c, m * 3 * sizeof(double) * 5 + m * 4 * sizeof(int)))) return r;
-    double *h = c->h_stage;
-    int *hi = (int *)(h + 15 * m);
+    const size_t bytes = stage_topo_off(n) + (size_t)n * 16;
+    if ((r = ensure_stage(c, std::max(bytes, (size_t)16)))) return r;
+    if ((r = ensure_dstage(c, std::max(bytes, (size_t)16)))) return r;
+    char *h = reinterpret_cast<char *>(c->h_stage);
     const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
-    double *dd[15] = {c->node.x, c->node.y, c->node.z, c->node.vx, c->node.vy, c->node.vz,
-                      c->node.sx, c->node.sy, c->node.sz, c->node.tx, c->node.ty, c->node.tz,
-                      c->node.nx, c->node.ny, c->node.nz};
+    ov_vec3 *dst[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
     if (n > 0) {
+        // the device's arrays transposed to the host layout (k_pack), one copy each
+        k_pack<<<(n + 255) / 256, 256, 0, c->stream>>>(fields, lo, n, node_ptrs(c), c->d_stage);
+        c->launches++;
         for (int f = 0; f < 5; ++f) {
-            if (!(fields & bits[f])) continue;
-            for (int a = 0; a < 3; ++a)
-                OV_CUDA(c, cudaMemcpyAsync(h + (3 * f + a) * m, dd[3 * f + a] + lo, (size_t)n * sizeof(double),
-                                           cudaMemcpyDeviceToHost, c->stream));
+            if (!(fields & bits[f]) || !dst[f]) continue;
+            OV_CUDA(c, cudaMemcpyAsync(h + (size_t)f * n * 24, c->d_stage + (size_t)f * n * 24, (size_t)n * 24,
+                                       cudaMemcpyDeviceToHost, c->stream));
         }
-        int *di[4] = {c->fwd, c->rev, c->status, c->pin};
         if (fields & OV_F_TOPOLOGY)
-            for (int i = 0; i < 4; ++i)
-                OV_CUDA(c, cudaMemcpyAsync(hi + i * m, di[i] + lo, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost,
-                                           c->stream));
+            OV_CUDA(c, cudaMemcpyAsync(h + stage_topo_off(n), c->d_stage + stage_topo_off(n), (size_t)n * 16,
+                                       cudaMemcpyDeviceToHost, c->stream));
         OV_CUDA(c, cudaStreamSynchronize(c->stream));
     }
-    ov_vec3 *dst[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
     for (int f = 0; f < 5; ++f) {
         if (!(fields & bits[f]) || !dst[f]) continue;
-        const double *s = h + 3 * m * f;
-        for (int k = 0; k < n; ++k)
-            for (int a = 0; a < 3; ++a) dst[f][k].p[a] = s[a * m + k];
+        if (n > 0) memcpy(dst[f], h + (size_t)f * n * 24, (size_t)n * 24);
         for (int k = n; k < t->N; ++k)
             for (int a = 0; a < 3; ++a) dst[f][k].p[a] = 0.0;
     }
     if (fields & OV_F_TOPOLOGY) {
         t->next_empty = next_empty;
         t->total_empty = total_empty;
-        for (int k = 0; k < n; ++k) {
-            int f = hi[k], b = hi[m + k];
-            t->connections[k].forward = f >= 0 ? f - lo : -1;
-            t->connections[k].reverse = b >= 0 ? b - lo : -1;
-            t->status[k].status = hi[2 * m + k];
-            t->status[k].pin_wall = hi[3 * m + k];
+        if (n > 0) {
+            memcpy(t->connections, h + stage_topo_off(n), (size_t)n * 8);
+            memcpy(t->status, h + stage_topo_off(n) + (size_t)n * 8, (size_t)n * 8);
         }
         for (int k = n; k < t->N; ++k) {
             t->connections[k].forward = t->connections[k].reverse = -1;

@@ -266,6 +266,8 @@ struct ov_ctx {
     // pinned host staging
     double *h_stage = nullptr;
     size_t h_stage_bytes = 0;
+    char *d_stage = nullptr;     // device copy of the host tangle's arrays as laid out there
+    size_t d_stage_bytes = 0;
     // spherical sections: (r, az, pl) bounds of each tree member's root cell
     double sph_lo[OV_SPH_MEMBERS][3] = {}, sph_hi[OV_SPH_MEMBERS][3] = {};
     // per-phase timing of the last evaluation
