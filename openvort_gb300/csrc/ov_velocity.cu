@@ -105,6 +105,38 @@ __device__ bool step_node_dev(const VelArgs &a, int i, int where, double out[3])
     return true;
 }
 
+// FP64 hardware approximations (PTX rcp.approx / rsqrt.approx; relative
+// error below 2^-20, measured on sm_103a), refined by the functions below.
+__device__ __forceinline__ double rcp_seed(double x)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return y;
+}
+__device__ __forceinline__ double rsqrt_seed(double x)
+{
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return y;
+}
+
+// 1/sqrt(x) and 1/x (x normal, positive) from the hardware approximations
+// (relative error below 2^-20 on sm_103a) with one third-order correction:
+// for e = 1 - x y0^2, y0 (1 + e/2 + 3e^2/8) leaves 5e^3/16, and for
+// e = 1 - x y0, y0 (1 + e + e^2) leaves e^3: below 2^-53 for |e| < 2^-18.
+__device__ __forceinline__ double rsqrt3(double x)
+{
+    const double y0 = rsqrt_seed(x);
+    const double e = fma(-(x * y0), y0, 1.0);
+    return fma(y0 * e, fma(0.375, e, 0.5), y0);
+}
+__device__ __forceinline__ double rcp3(double x)
+{
+    const double y0 = rcp_seed(x);
+    const double e = fma(-x, y0, 1.0);
+    return fma(y0, fma(e, e, e), y0);
+}
+
 __device__ __forceinline__ double wrapped_len(const Geometry &g, const double r1[3], const double r2in[3])
 {
     double r2[3] = {r2in[0], r2in[1], r2in[2]};
@@ -146,9 +178,15 @@ __global__ void k_tangents(VelArgs a, int cap, int *counters)
         rn_mul(-2.0, rn_sub(rn_mul(rn_sub(dm1, d2), dm2), rn_mul(d2, dm1))),
         rn_mul(2.0, rn_sub(rn_mul(rn_add(d2, d1), dm2), rn_mul(d1, d2))),
         rn_mul(-2.0, rn_sub(rn_mul(rn_add(d2, d1), dm1), rn_mul(d1, d2)))};
+    // the reference divides c1 and c2 by den; one corrected reciprocal each
+    // (within 2 ulp of the quotients) keeps GB300's FP64 pipe to a third
     double r1[4], r2[4];
 #pragma unroll
-    for (int z = 0; z < 4; ++z) { r1[z] = rn_div(c1[z], den[z]); r2[z] = rn_div(c2[z], den[z]); }
+    for (int z = 0; z < 4; ++z) {
+        const double inv = rcp3(den[z]);
+        r1[z] = c1[z] * inv;
+        r2[z] = c2[z] * inv;
+    }
     double ds[4][3];
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
@@ -235,23 +273,8 @@ __device__ __forceinline__ bool segment_law64(const double R[3], const double Rp
     return true;
 }
 
-// FP64 hardware approximations (PTX rcp.approx / rsqrt.approx, about 20
-// correct bits) refined by two Newton-Raphson steps each (20 -> 40 -> 80
-// bits): full double precision without the correctly rounded sequences.
-__device__ __forceinline__ double rcp_seed(double x)
-{
-    double y;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    return y;
-}
-__device__ __forceinline__ double rsqrt_seed(double x)
-{
-    double y;
-    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    return y;
-}
-
-// 1/x (x normal and positive)
+// 1/x (x normal and positive): two Newton-Raphson steps (20 -> 40 -> 80
+// bits), full double precision without the correctly rounded sequence
 __device__ __forceinline__ double recip_1_2(double x)
 {
     double y = rcp_seed(x);
@@ -1104,23 +1127,6 @@ struct WarpLists {
     int row_start[kListCap];       // entries in rows before row i
     double w[32][3];               // the terms of one batch of 32 entries
 };
-
-// 1/sqrt(x) and 1/x (x normal, positive) from the hardware approximations
-// (relative error below 2^-20 on sm_103a) with one third-order correction:
-// for e = 1 - x y0^2, y0 (1 + e/2 + 3e^2/8) leaves 5e^3/16, and for
-// e = 1 - x y0, y0 (1 + e + e^2) leaves e^3: below 2^-53 for |e| < 2^-18.
-__device__ __forceinline__ double rsqrt3(double x)
-{
-    const double y0 = rsqrt_seed(x);
-    const double e = fma(-(x * y0), y0, 1.0);
-    return fma(y0 * e, fma(0.375, e, 0.5), y0);
-}
-__device__ __forceinline__ double rcp3(double x)
-{
-    const double y0 = rcp_seed(x);
-    const double e = fma(-x, y0, 1.0);
-    return fma(y0, fma(e, e, e), y0);
-}
 
 // IEEE bits of a double: for x >= 0, or any x against a positive bound, the
 // order of the bits as signed integers is the order of the values (tests on
