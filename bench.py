@@ -593,7 +593,7 @@ def run_ours(args):
 
     # ---- roofline of the dominant kernel (the FP64 traversal: FMA-pipe bound)
     acc, vis = st["accepts"], st["visits"]
-    flops = 42 * acc        # FP64 flops per launch (fixed convention; the walk's tests run in FP32)
+    flops = 42 * acc + 9 * vis   # algorithmic flops per launch (fixed convention, whatever pipe runs them)
     trav_s = phases[2] * 1e-3
     achieved = flops / trav_s / 1e12
     fp64_peak = ctx.fma_peak_tflops(abi.OV_PREC_FP64)
@@ -780,7 +780,8 @@ def run_ours(args):
                      "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": K_VEL_FP64_DRAM_BYTES,
                      "traffic_note": "DRAM bytes per launch from ncu; the traversal is FP64-pipe bound",
                      "peak_source": "measured in this run (FP64 FMA chains, all SMs)",
-                     "work": "42 FP64 flops per accepted interaction (the walk's tests run in FP32)",
+                     "work": "42 flops per accepted interaction + 9 per visited cell (fixed convention); the split "
+                             "walk runs the visits' tests in FP32 and the interactions in FP64",
                      "accepts": acc, "visits": vis, "fp32_fma_peak_tflops": fp32_peak,
                      "warp_efficiency": vis / max(1, 32 * st["warp_steps"])},
         "accuracy": {"fp64_tree_rel_l2_vs_direct_subsample": fp64_vs_direct,
