@@ -688,6 +688,47 @@ __device__ __forceinline__ bool interact64(const Cell64 *cp, const double dxyz[3
     return segment_law64(R, Rp1, d, f4pi, w);
 }
 
+// IEEE bits of a double: for x >= 0, or any x against a positive bound, the
+// order of the bits as signed integers is the order of the values (tests on
+// the integer pipe instead of the FP64 one).
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+
+// The segment law (octree.c:321-342) for an accepted cell without the
+// factor kappa / 4 pi (applied to the query point's sum), in FP64 with
+// corrected hardware reciprocal square roots and reciprocal instead of the
+// reference's correctly rounded sqrt and divisions (each term within a few
+// ulps of the reference's).  R and Rp1 are the reference's own values.  The
+// filters |Rp1| < 1e-8 and ndot < 1e-8 are decided as the reference decides
+// them: near their thresholds segment_law64 redoes them with its rounding.
+// |R| >= 1e-8 holds for every accepted cell (the walk's skip test).  w is
+// zero when a filter drops the cell.
+__device__ __forceinline__ void law64_term(const Cell64 *cp, const double q[3], double w[3])
+{
+    w[0] = w[1] = w[2] = 0.0;
+    const double2 *c2 = reinterpret_cast<const double2 *>(cp);
+    const double2 A = __ldg(c2), B = __ldg(c2 + 1), C = __ldg(c2 + 2);
+    // A = (cx, cy)  B = (cz, qx)  C = (qy, qz); R = -(q - COM), rounded alike
+    const double R[3] = {A.x - q[0], A.y - q[1], B.x - q[2]};
+    const double P[3] = {R[0] + B.y, R[1] + C.x, R[2] + C.y};
+    const double lp2 = fma(P[0], P[0], fma(P[1], P[1], P[2] * P[2]));
+    const long long lp2_lo = dbits(1e-16 * (1.0 - 1e-12)), lp2_hi = dbits(1e-16 * (1.0 + 1e-12));
+    const long long nd_lo = dbits(1e-8 - 1e-12), nd_hi = dbits(1e-8 + 1e-12);
+    if (dbits(lp2) < lp2_lo) return;   // |Rp1| < 1e-8
+    const double lR2 = fma(R[0], R[0], fma(R[1], R[1], R[2] * R[2]));
+    const double dot = fma(R[0], P[0], fma(R[1], P[1], R[2] * P[2]));
+    const double ra = rsqrt3(lR2), rb = rsqrt3(lp2), ab = ra * rb;
+    const double nd = dot * ab;
+    if (dbits(lp2) <= lp2_hi || (dbits(nd) >= nd_lo && dbits(nd) <= nd_hi)) {
+        if (!segment_law64(R, P, len3_ref(R[0], R[1], R[2]), 1.0, w)) w[0] = w[1] = w[2] = 0.0;
+        return;
+    }
+    if (dbits(nd) < nd_lo) return;   // ndot < 1e-8
+    const double sc = (ra + rb) * ab * rcp3(1.0 + nd);
+    w[0] = fma(R[1], P[2], -R[2] * P[1]) * sc;
+    w[1] = fma(R[2], P[0], -R[0] * P[2]) * sc;
+    w[2] = fma(R[0], P[1], -R[1] * P[0]) * sc;
+}
+
 __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
 {
     float y = v - c;
@@ -1058,15 +1099,13 @@ __global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mix
             int e = near_list[32 * i];
             int c = e >> 5, j = (e & 31) - 1;
             if (c < w.root || c >= w.end || j < -1 || j >= a.geo.n_img) { bad_index(a, 3, e); continue; }
-            double q[3], dxyz[3], d64, wv[3];
+            double q[3], wv[3];
             if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
             else image_point(a.geo, j, p, q);
-            decide64(a.cells + c, q, a.prm.theta, true, dxyz, &d64);
-            if (interact64(a.cells + c, dxyz, d64, a.f4pi, wv)) {
-                if (j >= 0)   // a mirror image's term is reflected back
-                    for (int r = 0; r < a.geo.nreflect[j]; ++r) mirror_vec(a.geo.reflect[j][r], wv);
-                w64[0] += wv[0]; w64[1] += wv[1]; w64[2] += wv[2];
-            }
+            law64_term(a.cells + c, q, wv);   // zero when a filter drops it
+            if (j >= 0)   // a mirror image's term is reflected back
+                for (int r = 0; r < a.geo.nreflect[j]; ++r) mirror_vec(a.geo.reflect[j][r], wv);
+            w64[0] += wv[0] * a.f4pi; w64[1] += wv[1] * a.f4pi; w64[2] += wv[2] * a.f4pi;
         }
         __syncwarp();   // the list is rewritten by the next item
         double bh[3] = {acc_value(m.s0, m.c0, DD) + w64[0] + img64[0],
@@ -1127,47 +1166,6 @@ struct WarpLists {
     int row_start[kListCap];       // entries in rows before row i
     double w[32][3];               // the terms of one batch of 32 entries
 };
-
-// IEEE bits of a double: for x >= 0, or any x against a positive bound, the
-// order of the bits as signed integers is the order of the values (tests on
-// the integer pipe instead of the FP64 one).
-__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
-
-// The segment law (octree.c:321-342) for an accepted cell without the
-// factor kappa / 4 pi (applied to the query point's sum), in FP64 with
-// corrected hardware reciprocal square roots and reciprocal instead of the
-// reference's correctly rounded sqrt and divisions (each term within a few
-// ulps of the reference's).  R and Rp1 are the reference's own values.  The
-// filters |Rp1| < 1e-8 and ndot < 1e-8 are decided as the reference decides
-// them: near their thresholds segment_law64 redoes them with its rounding.
-// |R| >= 1e-8 holds for every accepted cell (the walk's skip test).  w is
-// zero when a filter drops the cell.
-__device__ __forceinline__ void law64_term(const Cell64 *cp, const double q[3], double w[3])
-{
-    w[0] = w[1] = w[2] = 0.0;
-    const double2 *c2 = reinterpret_cast<const double2 *>(cp);
-    const double2 A = __ldg(c2), B = __ldg(c2 + 1), C = __ldg(c2 + 2);
-    // A = (cx, cy)  B = (cz, qx)  C = (qy, qz); R = -(q - COM), rounded alike
-    const double R[3] = {A.x - q[0], A.y - q[1], B.x - q[2]};
-    const double P[3] = {R[0] + B.y, R[1] + C.x, R[2] + C.y};
-    const double lp2 = fma(P[0], P[0], fma(P[1], P[1], P[2] * P[2]));
-    const long long lp2_lo = dbits(1e-16 * (1.0 - 1e-12)), lp2_hi = dbits(1e-16 * (1.0 + 1e-12));
-    const long long nd_lo = dbits(1e-8 - 1e-12), nd_hi = dbits(1e-8 + 1e-12);
-    if (dbits(lp2) < lp2_lo) return;   // |Rp1| < 1e-8
-    const double lR2 = fma(R[0], R[0], fma(R[1], R[1], R[2] * R[2]));
-    const double dot = fma(R[0], P[0], fma(R[1], P[1], R[2] * P[2]));
-    const double ra = rsqrt3(lR2), rb = rsqrt3(lp2), ab = ra * rb;
-    const double nd = dot * ab;
-    if (dbits(lp2) <= lp2_hi || (dbits(nd) >= nd_lo && dbits(nd) <= nd_hi)) {
-        if (!segment_law64(R, P, len3_ref(R[0], R[1], R[2]), 1.0, w)) w[0] = w[1] = w[2] = 0.0;
-        return;
-    }
-    if (dbits(nd) < nd_lo) return;   // ndot < 1e-8
-    const double sc = (ra + rb) * ab * rcp3(1.0 + nd);
-    w[0] = fma(R[1], P[2], -R[2] * P[1]) * sc;
-    w[1] = fma(R[2], P[0], -R[0] * P[2]) * sc;
-    w[2] = fma(R[0], P[1], -R[1] * P[0]) * sc;
-}
 
 // Evaluate the warp's lists (this lane holds n entries) at the lanes' query
 // points q and add each lane's terms to its v, in entry order.
@@ -2708,11 +2706,9 @@ __global__ void __launch_bounds__(128) k_sph_query_mixed(SphArgs s, double *__re
         const int e = near_list[32 * i];
         const int c = e >> 5;
         if (c < root || c >= end) { bad_index(a, 3, e); continue; }
-        double dxyz[3], d64, wv[3];
-        decide64(a.cells + c, qp, a.prm.theta, true, dxyz, &d64);
-        if (interact64(a.cells + c, dxyz, d64, a.f4pi, wv)) {
-            w64[0] += wv[0]; w64[1] += wv[1]; w64[2] += wv[2];
-        }
+        double wv[3];
+        law64_term(a.cells + c, qp, wv);   // zero when a filter drops it
+        w64[0] += wv[0] * a.f4pi; w64[1] += wv[1] * a.f4pi; w64[2] += wv[2] * a.f4pi;
     }
     __syncwarp();
     double v[3] = {((double)acc.s0 - (double)acc.c0) + w64[0], ((double)acc.s1 - (double)acc.c1) + w64[1],
