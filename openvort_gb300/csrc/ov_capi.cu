@@ -111,6 +111,9 @@ int ov_ctx_create(ov_ctx **out, int device)
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     ov_params_default(&c->params);
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
         delete c;
         return OV_ERR_CUDA;
@@ -161,6 +164,9 @@ int ov_ctx_destroy(ov_ctx *c)
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    if (c->join_ev) cudaEventDestroy(c->join_ev);
     delete c;
     return OV_OK;
 }
@@ -834,15 +840,27 @@ static int clear_call_words(ov_ctx *c)
     return OV_OK;
 }
 
+// The tangents run on the side stream beside the tree build (neither reads
+// what the other writes); the traversal waits for both.  Phase events:
+// tangents ph[0] -> ph[1] (side stream), tree ph[0] -> ph[2], traversal
+// ph[2] -> ph[3].
 static int eval_async(ov_ctx *c, NodeArrays &na, double t, bool tangents, cudaStream_t s)
 {
     bool ph = c->phase_timing && c->time_dev_index < 0;
     if (ph) OV_CUDA(c, cudaEventRecord(c->ph[0], s));
-    if (tangents) ov_launch_tangents(c, na, s);
-    if (ph) OV_CUDA(c, cudaEventRecord(c->ph[1], s));
+    if (tangents) {
+        OV_CUDA(c, cudaEventRecord(c->fork_ev, s));
+        OV_CUDA(c, cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+        ov_launch_tangents(c, na, c->side);
+        if (ph) OV_CUDA(c, cudaEventRecord(c->ph[1], c->side));
+        OV_CUDA(c, cudaEventRecord(c->join_ev, c->side));
+    } else if (ph) {
+        OV_CUDA(c, cudaEventRecord(c->ph[1], s));
+    }
     int r = ov_tree_build(c, na, s);
     if (r) return r;
     if (ph) OV_CUDA(c, cudaEventRecord(c->ph[2], s));
+    if (tangents) OV_CUDA(c, cudaStreamWaitEvent(s, c->join_ev, 0));
     if ((r = ov_launch_velocities(c, na, t, c->precision, s))) return r;
     if (ph) OV_CUDA(c, cudaEventRecord(c->ph[3], s));
     OV_CUDA(c, cudaGetLastError());
@@ -1164,7 +1182,9 @@ int ov_phase_times(ov_ctx *c, float ms[3])
     if (!c || !ms) return OV_ERR_ARG;
     if (!c->phase_timing || !c->ph[0]) return ov_fail(c, OV_ERR_STATE, "phase timing is off");
     OV_CUDA(c, cudaEventSynchronize(c->ph[3]));
-    for (int i = 0; i < 3; ++i) OV_CUDA(c, cudaEventElapsedTime(&ms[i], c->ph[i], c->ph[i + 1]));
+    OV_CUDA(c, cudaEventElapsedTime(&ms[0], c->ph[0], c->ph[1]));   // tangents (side stream)
+    OV_CUDA(c, cudaEventElapsedTime(&ms[1], c->ph[0], c->ph[2]));   // tree build, beside them
+    OV_CUDA(c, cudaEventElapsedTime(&ms[2], c->ph[2], c->ph[3]));   // traversal and finish
     return OV_OK;
 }
 

@@ -192,6 +192,8 @@ struct ov_ctx {
     int tcap = 0;                          // members the per-member device arrays hold
     Tuning tune;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;            // tangents beside the tree build
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     ov_params params{};
     int precision = OV_PREC_FP64;
     int walk = OV_WALK_SPLIT;    // OV_PREC_FP64's tree walk (ov_set_walk)
