@@ -145,7 +145,7 @@ int ov_ctx_destroy(ov_ctx *c)
     if (c->d_mrange) cudaFree(c->d_mrange);
     void *scratch[] = {c->d_pairs, c->d_npairs, c->d_loop_off, c->d_loop_nodes, c->d_loop_buf, c->d_loop_cut,
                        c->rec_nodes, c->rec_pair, c->rec_out, c->rec_corr, c->rec_part, c->rec_split,
-                       c->fft_buf, c->fft_tw, c->long_buf};
+                       c->fft_buf, c->fft_tw, c->long_buf, c->d_rm, c->d_rm_lim};
     for (void *p : scratch)
         if (p) cudaFree(p);
     if (c->dsum) cudaFree(c->dsum);

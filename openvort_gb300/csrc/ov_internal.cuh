@@ -186,6 +186,9 @@ struct ov_ctx {
     int key_tbits = 0;                     // member-id bits on top of the path keys
     int key_levels = OV_MAX_LEVEL;         // tree levels below each root
     int *d_tid = nullptr;                  // member of each slot (ensembles only)
+    int *d_rm = nullptr;                   // remesh: slots to visit, then their count
+    double *d_rm_lim = nullptr;            // remesh: (dl_min, dl_max) per member
+    int rm_cap = 0, rm_lim_cap = 0;
     DevParams *d_tprm = nullptr;           // per-member parameters (ensembles only)
     int *d_qorder = nullptr;               // members in work-queue order
     int2 *d_mrange = nullptr;              // per-member slot range [lo, lo + cap)

@@ -40,6 +40,8 @@
 
 #include "ov_internal.cuh"
 
+#include <queue>
+
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
 #endif
@@ -403,6 +405,47 @@ __global__ void k_pairs(const uint64_t *__restrict__ keys, const int *__restrict
                     if (slot < pair_cap) { pairs[2 * slot] = k; pairs[2 * slot + 1] = l; }
                 }
             }
+}
+
+// remesh (tangle.c:1018-1061): the slots whose lengths could make the pass
+// act (remove or insert), for the host pass to visit in index order.  The
+// thresholds are widened by 1e-9 relative, so the list holds every slot the
+// reference's tests would act on; the host redoes each test exactly.
+__global__ void k_remesh_flags(const int *__restrict__ status, const int *__restrict__ fwd,
+                               const int *__restrict__ rev, const double *__restrict__ x,
+                               const double *__restrict__ y, const double *__restrict__ z,
+                               const int *__restrict__ tid, const double *__restrict__ lim, int nmem, Geometry geo,
+                               int n, int *__restrict__ list, int *__restrict__ count, int cap_list)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || status[s] == OV_EMPTY) return;
+    const int m = tid ? tid[s] : 0;
+    const int nx = fwd[s], pv = rev[s];
+    bool act;
+    if (m < 0 || m >= nmem || nx >= n || pv >= n) {
+        act = true;   // let the host see it
+    } else {
+        const double mn = lim[2 * m], mx = lim[2 * m + 1];
+        const double p[3] = {x[s], y[s], z[s]};
+        double lf = 0, lr = 0;
+        if (nx >= 0) {
+            double q[3] = {x[nx], y[nx], z[nx]};
+            pwrap_dev(geo, p, q);
+            lf = len3_ref(rn_sub(p[0], q[0]), rn_sub(p[1], q[1]), rn_sub(p[2], q[2]));
+        }
+        if (pv >= 0) {
+            double q[3] = {x[pv], y[pv], z[pv]};
+            pwrap_dev(geo, p, q);
+            lr = len3_ref(rn_sub(p[0], q[0]), rn_sub(p[1], q[1]), rn_sub(p[2], q[2]));
+        }
+        const double up = 1.0 + 1e-9, dn = 1.0 - 1e-9;
+        act = (nx >= 0 && pv >= 0 && (lf < mn * up || lr < mn * up) && (lf + lr) < mx * up) ||
+              (nx >= 0 && lf > mx * dn);
+    }
+    if (act) {
+        const int i = atomicAdd(count, 1);
+        if (i < cap_list) list[i] = s;
+    }
 }
 
 __global__ void k_zero_vel(const int *__restrict__ ids, int n, double *vx, double *vy, double *vz, double *sx,
@@ -1134,11 +1177,22 @@ inline bool any_solid_wall(const Geometry &g)
 
 // remesh (tangle.c:1018-1061) of member mi: slots in index order, including
 // the ones it inserts (and the range it grows into)
+// The pass in index order over the member's local slots `visit` (sorted:
+// every slot whose tests could act) and the slots an earlier action of the
+// pass touched: a removal changes its neighbours' lengths, an insertion its
+// old forward neighbour's and the new node's.  Every other slot keeps the
+// lengths its test failed on, so visiting only these is the reference's pass.
 int hremesh(ov_ctx *c, int mi, double min_dist, double max_dist, double time, int *added_out, int *removed_out,
-            std::vector<int> &new_nodes)
+            std::vector<int> &new_nodes, const std::vector<int> &visit)
 {
     int added = 0, removed = 0;
-    for (int k = 0; k < c->mem[mi].n; ++k) {
+    std::priority_queue<int, std::vector<int>, std::greater<int>> todo(visit.begin(), visit.end());
+    int last = -1;
+    while (!todo.empty()) {
+        const int k = todo.top();
+        todo.pop();
+        if (k <= last || k >= c->mem[mi].n) continue;
+        last = k;
         Host h = host_of(c, mi);
         const int s = h.lo + k;
         if (h.st(s) == OV_EMPTY) continue;
@@ -1150,10 +1204,16 @@ int hremesh(ov_ctx *c, int mi, double min_dist, double max_dist, double time, in
         if (nx >= 0 && pv >= 0 && ((lf < min_dist || lr < min_dist) && (lf + lr) < max_dist)) {
             hremove(c, s);
             removed++;
+            if (pv - h.lo > k) todo.push(pv - h.lo);
+            if (nx - h.lo > k) todo.push(nx - h.lo);
         }
         if (nx >= 0 && lf > max_dist) {
             added++;
-            if (hadd_point(c, mi, s, new_nodes) < 0) return OV_ERR_ALLOC;
+            const int np = hadd_point(c, mi, s, new_nodes);
+            if (np < 0) return OV_ERR_ALLOC;
+            const int lo = host_of(c, mi).lo;
+            if (np - lo > k) todo.push(np - lo);
+            if (nx - lo > k) todo.push(nx - lo);
         }
     }
     if (added) {
@@ -1629,12 +1689,62 @@ int ov_remesh(ov_ctx *c, double min_dist, double max_dist, double t)
     c->host_valid = false;
     int added = 0, removed = 0;
     std::vector<int> new_nodes;
-    for (int mi = 0; mi < (int)c->mem.size(); ++mi) {
+    const int nmem = (int)c->mem.size();
+    std::vector<double> lim(2 * (size_t)nmem);
+    for (int mi = 0; mi < nmem; ++mi) {
         // a single tangle takes the arguments; ensemble members their own dl_min / dl_max
-        double lo = c->mem.size() == 1 ? min_dist : c->mem[mi].params.dl_min;
-        double hi = c->mem.size() == 1 ? max_dist : c->mem[mi].params.dl_max;
+        lim[2 * mi] = nmem == 1 ? min_dist : c->mem[mi].params.dl_min;
+        lim[2 * mi + 1] = nmem == 1 ? max_dist : c->mem[mi].params.dl_max;
+    }
+    // the slots whose tests could act, from the device (host and device agree here)
+    std::vector<std::vector<int>> visit(nmem);
+    {
+        const int n = c->n_live;
+        if (c->rm_cap < n + 1) {
+            if (c->d_rm) cudaFree(c->d_rm);
+            c->d_rm = nullptr;
+            OV_CUDA(c, cudaMalloc(&c->d_rm, (size_t)(n + 1) * sizeof(int)));
+            c->rm_cap = n + 1;
+        }
+        if (c->rm_lim_cap < 2 * nmem) {
+            if (c->d_rm_lim) cudaFree(c->d_rm_lim);
+            c->d_rm_lim = nullptr;
+            OV_CUDA(c, cudaMalloc(&c->d_rm_lim, 2 * (size_t)nmem * sizeof(double)));
+            c->rm_lim_cap = 2 * nmem;
+        }
+        OV_CUDA(c, cudaMemcpyAsync(c->d_rm_lim, lim.data(), lim.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                   c->stream));
+        int *d_count = c->d_rm + n;
+        OV_CUDA(c, cudaMemsetAsync(d_count, 0, sizeof(int), c->stream));
+        if (n > 0) {
+            k_remesh_flags<<<(n + 255) / 256, 256, 0, c->stream>>>(c->status, c->fwd, c->rev, c->node.x, c->node.y,
+                                                                   c->node.z, nmem > 1 ? c->d_tid : nullptr,
+                                                                   c->d_rm_lim, nmem, c->geo, n, c->d_rm, d_count, n);
+            c->launches++;
+        }
+        int cnt = 0;
+        OV_CUDA(c, cudaMemcpyAsync(&cnt, d_count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        OV_CUDA(c, cudaStreamSynchronize(c->stream));
+        cnt = std::min(cnt, n);
+        std::vector<int> slots(cnt);
+        if (cnt) {
+            OV_CUDA(c, cudaMemcpy(slots.data(), c->d_rm, (size_t)cnt * sizeof(int), cudaMemcpyDeviceToHost));
+        }
+        for (int sl : slots) {
+            int m = 0, lo2 = 0, hi2 = nmem - 1;
+            while (lo2 < hi2) {   // the member holding slot sl
+                const int mid = (lo2 + hi2 + 1) >> 1;
+                if (c->mem[mid].lo <= sl) lo2 = mid; else hi2 = mid - 1;
+            }
+            m = lo2;
+            visit[m].push_back(sl - c->mem[m].lo);
+        }
+        for (auto &v : visit) std::sort(v.begin(), v.end());
+    }
+    for (int mi = 0; mi < nmem; ++mi) {
+        const double lo = lim[2 * mi], hi = lim[2 * mi + 1];
         int a = 0, d = 0;
-        if ((r = hremesh(c, mi, lo, hi, t, &a, &d, new_nodes))) {
+        if ((r = hremesh(c, mi, lo, hi, t, &a, &d, new_nodes, visit[mi]))) {
             // keep host and device consistent before reporting
             ov_push_device(c, 1);
             return r == OV_ERR_ALLOC ? ov_fail(c, r, "remesh: no empty slot could be had") : r;
