@@ -448,6 +448,28 @@ __global__ void k_remesh_flags(const int *__restrict__ status, const int *__rest
     }
 }
 
+// eliminate_small_loops (tangle.c:1063-1128): the slots of structures the
+// pass could remove from (a closed loop of at most `cutoff` nodes, or a slot
+// fewer than `cutoff` forward steps from an open end or a link out of range),
+// for the host pass to visit from each structure's first slot.
+__global__ void k_small_flags(const int *__restrict__ status, const int *__restrict__ fwd, int n, int cutoff,
+                              int *__restrict__ list, int *__restrict__ count, int cap_list)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || status[k] == OV_EMPTY) return;
+    bool flag = false;
+    int here = k;
+    for (int st = 0; st < cutoff; ++st) {
+        const int nx = fwd[here];
+        if (nx < 0 || nx >= n || nx == k) { flag = true; break; }
+        here = nx;
+    }
+    if (flag) {
+        const int i = atomicAdd(count, 1);
+        if (i < cap_list) list[i] = k;
+    }
+}
+
 __global__ void k_zero_vel(const int *__restrict__ ids, int n, double *vx, double *vy, double *vz, double *sx,
                            double *sy, double *sz)
 {
@@ -892,14 +914,19 @@ void hperiodic(ov_ctx *c, int lo, int hi)
 }
 
 // eliminate_small_loops (tangle.c:1063-1128) in member mi; returns nodes removed
-int hsmall_loops(ov_ctx *c, int mi)
+// The pass over member mi, from the given first slots of its structures
+// (sorted; every structure it could remove from): the reference visits a
+// structure first at its lowest slot, and the others are left as they are.
+int hsmall_loops(ov_ctx *c, int mi, const std::vector<int> &starts)
 {
     Host h = host_of(c, mi);
     const int lo = h.lo, hi = h.hi, N = hi - lo;
     int removed = 0;
+    if (starts.empty()) return 0;
     std::vector<char> seen(N > 0 ? N : 1, 0);
     auto mark = [&](int slot) { if (slot >= lo && slot < hi) seen[slot - lo] = 1; };
-    for (int k = lo; k < hi; ++k) {
+    for (int k : starts) {
+        if (k < lo || k >= hi) continue;
         if (h.st(k) == OV_EMPTY || seen[k - lo]) continue;
         seen[k - lo] = 1;
         int steps = 0, here = k, nx = h.fwd(here);
@@ -1674,7 +1701,63 @@ int ov_eliminate_small_loops(ov_ctx *c)
     if ((r = ov_pull_host(c))) return r;
     c->host_valid = false;   // until the mirror is pushed (or found unchanged)
     int removed = 0;
-    for (int mi = 0; mi < (int)c->mem.size(); ++mi) removed += hsmall_loops(c, mi);
+    // the slots of structures the pass could remove from, from the device
+    // (host and device agree here), then each structure's first slot
+    const int n = c->n_live, nmem = (int)c->mem.size();
+    int cutoff = 0;
+    for (const Member &m : c->mem) cutoff = std::max(cutoff, m.params.small_loop_cutoff);
+    std::vector<int> slots;
+    if (n > 0 && cutoff > 0) {
+        if (c->rm_cap < n + 1) {
+            if (c->d_rm) cudaFree(c->d_rm);
+            c->d_rm = nullptr;
+            OV_CUDA(c, cudaMalloc(&c->d_rm, (size_t)(n + 1) * sizeof(int)));
+            c->rm_cap = n + 1;
+        }
+        int *d_count = c->d_rm + n;
+        OV_CUDA(c, cudaMemsetAsync(d_count, 0, sizeof(int), c->stream));
+        k_small_flags<<<(n + 255) / 256, 256, 0, c->stream>>>(c->status, c->fwd, n, cutoff, c->d_rm, d_count, n);
+        c->launches++;
+        int cnt = 0;
+        OV_CUDA(c, cudaMemcpyAsync(&cnt, d_count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        OV_CUDA(c, cudaStreamSynchronize(c->stream));
+        cnt = std::min(cnt, n);
+        slots.resize(cnt);
+        if (cnt) OV_CUDA(c, cudaMemcpy(slots.data(), c->d_rm, (size_t)cnt * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    std::vector<std::vector<int>> starts(nmem);
+    for (int sl : slots) {
+        int lo2 = 0, hi2 = nmem - 1;
+        while (lo2 < hi2) {   // the member holding slot sl
+            const int mid = (lo2 + hi2 + 1) >> 1;
+            if (c->mem[mid].lo <= sl) lo2 = mid; else hi2 = mid - 1;
+        }
+        Host h = host_of(c, lo2);
+        // the structure's lowest slot: forward until back or an end, then backward
+        int first = sl, cur = sl, guard = 0;
+        bool closed = false;
+        for (int nx = h.fwd(cur); guard <= n; ++guard, nx = h.fwd(cur)) {
+            if (nx == sl) { closed = true; break; }
+            if (nx < h.lo || nx >= h.hi) break;
+            cur = nx;
+            first = std::min(first, cur);
+        }
+        if (!closed) {
+            cur = sl;
+            guard = 0;
+            for (int pv = h.rev(cur); pv >= h.lo && pv < h.hi && pv != sl && guard <= n; ++guard, pv = h.rev(cur)) {
+                cur = pv;
+                first = std::min(first, cur);
+            }
+        }
+        starts[lo2].push_back(first);
+    }
+    for (int mi = 0; mi < nmem; ++mi) {
+        auto &v = starts[mi];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        removed += hsmall_loops(c, mi, v);
+    }
     c->stats.small_loops_removed = removed;
     if (removed) return ov_push_device(c, 0);
     c->host_valid = true;
