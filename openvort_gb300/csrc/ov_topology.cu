@@ -1907,7 +1907,8 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     std::vector<int> ahead;
     ahead.reserve(2 * kAhead);
     struct Rewire {
-        double a[4][3], b[4][3];
+        double a[4][3], b[4][3];   // the changed segments (wrapped end)
+        double c[3], rho, slen;    // a sphere around them (centre, radius, 1.01 x radius), sum of lengths
     };
     std::vector<Rewire> rw;   // rewiring r: its four changed segments
     c->stats.reconnect_lazy_evals = 0;
@@ -1956,14 +1957,25 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         for (int a = 0; a < 3; ++a) qs[0][a] = x[a];
         for (int j = 0; j < g.n_img; ++j) himage(g, j, x, qs[j + 1]);
         double b = 0;
-        for (int r = corr_gen[ci]; r < gen; ++r)
-            for (int sgi = 0; sgi < 4; ++sgi) {
-                const double *A = rw[r].a[sgi], *B = rw[r].b[sgi];
-                double S[3];
-                hsub(S, B, A);
-                const double s2 = hdot(S, S);
-                if (!(s2 > 0)) continue;   // a segment of zero length adds nothing
-                for (int qi = 0; qi < nq; ++qi) {
+        for (int r = corr_gen[ci]; r < gen; ++r) {
+            const Rewire &w = rw[r];
+            for (int qi = 0; qi < nq; ++qi) {
+                // far from the four segments' bounding sphere: every point of
+                // them is at least |q - c| - rho away
+                double qc[3];
+                hsub(qc, qs[qi], w.c);
+                const double D = sqrt(hdot(qc, qc));
+                if (D > 4 * w.rho) {
+                    const double d = D - w.rho;
+                    b += w.slen / (d * d);
+                    continue;
+                }
+                for (int sgi = 0; sgi < 4; ++sgi) {
+                    const double *A = w.a[sgi], *B = w.b[sgi];
+                    double S[3];
+                    hsub(S, B, A);
+                    const double s2 = hdot(S, S);
+                    if (!(s2 > 0)) continue;   // a segment of zero length adds nothing
                     double QA[3];
                     hsub(QA, qs[qi], A);
                     double u = hdot(QA, S) / s2;
@@ -1975,6 +1987,7 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
                     b += sqrt(s2) / d2;
                 }
             }
+        }
         return b * h.P->kappa / (4 * M_PI) * (1.0 + 1e-9);
     };
     // copy the corrections of the last correction's read-back list (complete
@@ -2155,6 +2168,18 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
                     h.pos(cfw[sgi], rr.b[sgi]);
                     hpwrap(g, rr.a[sgi], rr.b[sgi]);
                 }
+                for (int a = 0; a < 3; ++a) rr.c[a] = rr.a[0][a];
+                double rho = 0, sl = 0;
+                for (int sgi = 0; sgi < 4; ++sgi) {
+                    double da[3], db[3], sv[3];
+                    hsub(da, rr.a[sgi], rr.c);
+                    hsub(db, rr.b[sgi], rr.c);
+                    hsub(sv, rr.b[sgi], rr.a[sgi]);
+                    rho = std::max(rho, std::max(sqrt(hdot(da, da)), sqrt(hdot(db, db))));
+                    sl += sqrt(hdot(sv, sv));
+                }
+                rr.rho = rho * 1.01;   // covers the rounding of the distances above
+                rr.slen = sl * 1.01;
                 rw.push_back(rr);
             }
             ++gen;
