@@ -35,6 +35,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <climits>
 #include <chrono>
 #include <vector>
 
@@ -1911,6 +1912,12 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         double c[3], rho, slen;    // a sphere around them (centre, radius, 1.01 x radius), sum of lengths
     };
     std::vector<Rewire> rw;   // rewiring r: its four changed segments
+    // rewirings whose corrections are not launched yet (up to 8 go in one
+    // launch): their segments and the first candidate they apply to
+    std::vector<int> pend_m, pend_f;
+    std::vector<double> pend_s;
+    int pend_from = INT_MAX, launched_gen = 0;
+    size_t cur_q = 0;   // the pair being decided (the read-back list starts there)
     c->stats.reconnect_lazy_evals = 0;
     int64_t evaluated = 0;
     c->stats.reconnect_candidates = C;
@@ -1990,6 +1997,31 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         }
         return b * h.P->kappa / (4 * M_PI) * (1.0 + 1e-9);
     };
+    // launch the pending corrections with the read-back of the candidates of
+    // the pairs from the current one on
+    auto flush = [&]() -> int {
+        if (pend_m.empty()) {
+            launched_gen = gen;
+            return OV_OK;
+        }
+        ahead.clear();
+        for (size_t qq = cur_q; qq < pairs.size() && qq < cur_q + kAhead; ++qq) {
+            for (int node : {pairs[qq].first, pairs[qq].second}) {
+                int cj = cand_index(node);
+                if (cj < pend_from || cj >= ce || pf_gen[cj] == gen) continue;
+                pf_gen[cj] = gen;
+                pf_pos[cj] = (int)ahead.size();
+                ahead.push_back(cj);
+            }
+        }
+        const int rr = ov_rec_correct(c, pend_from, ce - pend_from, pend_m.data(), pend_f.data(), pend_s.data(),
+                                      (int)pend_m.size(), ahead.data(), (int)ahead.size());
+        pend_m.clear(); pend_f.clear(); pend_s.clear();
+        pend_from = INT_MAX;
+        launched_gen = gen;
+        pf_waited = false;
+        return rr;
+    };
     // copy the corrections of the last correction's read-back list (complete
     // once ov_rec_wait returned)
     auto take_prefetch = [&]() {
@@ -2020,6 +2052,7 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
                 ++c->stats.reconnect_lazy_evals;
             } else if (corr_gen[ci] < gen) {
                 const auto tf = clk();
+                if (launched_gen < gen && flush()) return false;
                 if (pf_gen[ci] == gen) {
                     if (!pf_waited) {
                         if (ov_rec_wait(c)) return false;
@@ -2055,6 +2088,8 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         size_t e = i;
         while (e < pairs.size() && pairs[e].first == k) ++e;
         int mk = member_of(k);
+        cur_q = i;
+        if (mk != cur_member && cur_member >= 0 && (r = flush())) return r;
         if (mk != cur_member) {
             cur_member = mk;
             h = host_of(c, mk);
@@ -2066,6 +2101,7 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
         int sk = h.st(k);
         if (sk == OV_EMPTY || pinned(sk) || recalc[k]) { i = e; continue; }
         for (size_t q = i; q < e; ++q) {
+            cur_q = q;
             int l = pairs[q].second;
             int sl = h.st(l);
             if (sl == OV_EMPTY || pinned(sl) || h.fwd(k) == l || h.rev(k) == l || recalc[l]) continue;
@@ -2184,21 +2220,20 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
             }
             ++gen;
             if (ce > cfrom) {
-                // the correction, and the read-back of the next pairs' candidates'
-                // corrections after it (one launch, straight into host memory)
-                ahead.clear();
-                for (size_t qq = e; qq < pairs.size() && qq < e + kAhead; ++qq) {
-                    for (int node : {pairs[qq].first, pairs[qq].second}) {
-                        int cj = cand_index(node);
-                        if (cj < cfrom || cj >= ce || pf_gen[cj] == gen) continue;
-                        pf_gen[cj] = gen;
-                        pf_pos[cj] = (int)ahead.size();
-                        ahead.push_back(cj);
-                    }
+                // the correction joins the pending ones (launched 8 rewirings at a
+                // time, or when a pair needs the exact corrections); a launch may
+                // correct candidates between two rewirings' first candidates for a
+                // later rewiring too: those are not decided again in this pass
+                for (int sgi = 0; sgi < 4; ++sgi) {
+                    pend_m.push_back(cm[sgi]);
+                    pend_f.push_back(cfw[sgi]);
+                    pend_s.push_back(csg[sgi]);
                 }
-                if ((r = ov_rec_correct(c, cfrom, ce - cfrom, cm, cfw, csg, 4, ahead.data(), (int)ahead.size())))
-                    return r;
-                pf_waited = false;
+                pend_from = std::min(pend_from, cfrom);
+                if (pend_m.size() + 4 > 32) {
+                    cur_q = e;
+                    if ((r = flush())) return r;
+                }
             }
             c->step_ms[13] += ms_since(tc);
             recalc[k]++; recalc[h.fwd(k)]++; recalc[h.rev(k)]++; recalc[kn]++; recalc[kp]++;

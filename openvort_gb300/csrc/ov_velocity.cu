@@ -1908,9 +1908,10 @@ __global__ void k_rec_finish(const double *__restrict__ part, int n, int max_chu
     out[5 * (size_t)b + 4] = 1.01 * (acc[3] + acc[4] + acc[6]);
 }
 
+constexpr int kRecChangeMax = 32;   // changed segments one correction launch takes (8 rewirings)
 struct RecChange {
-    int m[8], f[8];
-    double sign[8];
+    int m[kRecChangeMax], f[kRecChangeMax];
+    double sign[kRecChangeMax];
     int n;
 };
 
@@ -1931,7 +1932,7 @@ __device__ __forceinline__ void corr_point(const RecArgs &r, int k, int j, const
             qf[a] = r.sp[(size_t)(3 + a) * r.cap + k];
             if (j >= 0) { qg[a] -= r.shift_g[j][a]; qf[a] -= r.shift_f[j][a]; }
         }
-        for (int i = 0; i < ch.n && i < 8; ++i) {
+        for (int i = 0; i < ch.n && i < kRecChangeMax; ++i) {
             int m = ch.m[i], f = ch.f[i];
             if (m < 0 || m >= r.cap || f < 0 || f >= r.cap) continue;
             float ag[3], af[3], sv[3];
@@ -2230,9 +2231,10 @@ int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const 
         OV_CUDA(c, cudaHostGetDevicePointer((void **)&c->h_pf_dev, c->h_pf, 0));
     }
     if (!c->rec_ev) OV_CUDA(c, cudaEventCreateWithFlags(&c->rec_ev, cudaEventDisableTiming));
+    if (nch < 0 || nch > kRecChangeMax) return ov_fail(c, OV_ERR_ARG, "reconnect: %d changed segments", nch);
     RecChange ch;
     memset(&ch, 0, sizeof ch);
-    ch.n = std::min(nch, 8);
+    ch.n = nch;
     for (int i = 0; i < ch.n; ++i) { ch.m[i] = m[i]; ch.f[i] = f[i]; ch.sign[i] = sign[i]; }
     RecPrefetch list;
     list.n = npf;
