@@ -24,6 +24,8 @@
 // ceil(log2 T) bits and the keys hold floor((63 - bits) / 3) levels.
 #include "ov_internal.cuh"
 
+#include <cuda/atomic>
+
 void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s);
 int ov_sort_hist_ints(int cap);
 int ov_scan_tmp_ints(int n_max);
@@ -482,10 +484,10 @@ __global__ void k_moments(const uint64_t *__restrict__ keys, const int *__restri
     for (int guard = 0; guard < 64; ++guard) {
         int p = parent[cur];
         if (p <= root) break;
-        __threadfence();
-        int old = atomicAdd(&arrive[p], 1);
+        // release this cell's sums, and (last child) acquire the siblings'
+        cuda::atomic_ref<int, cuda::thread_scope_device> arr(arrive[p]);
+        const int old = arr.fetch_add(1, cuda::memory_order_acq_rel);
         if (old != nchild[p] - 1) break;
-        __threadfence();
         double sum[6] = {0, 0, 0, 0, 0, 0};
         int end = __ldcg(&cells[p].next);
         for (int ch = p + 1; ch != end && ch > 0; ch = __ldcg(&cells[ch].next)) {
