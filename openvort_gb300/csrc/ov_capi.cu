@@ -673,12 +673,10 @@ int ov_upload_tangle_fields(ov_ctx *c, const ov_tangle_state *t, unsigned fields
                 return ov_fail(c, OV_ERR_TOPOLOGY, "node %d: connections (%d,%d) / status %d out of range", k, f, b, st);
         }
     }
-    // the host arrays as they are into pinned memory, one copy each, then the
-    // transposition to the device's arrays (k_unpack)
+    // the host arrays as they are, one copy each, then the transposition to
+    // the device's arrays (k_unpack)
     const size_t bytes = stage_topo_off(n) + (size_t)n * 16;
-    if ((r = ensure_stage(c, std::max(bytes, (size_t)16)))) return r;
     if ((r = ensure_dstage(c, std::max(bytes, (size_t)16)))) return r;
-    char *h = reinterpret_cast<char *>(c->h_stage);
     const ov_vec3 *src[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
     const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
     unsigned have = 0;
@@ -686,17 +684,16 @@ int ov_upload_tangle_fields(ov_ctx *c, const ov_tangle_state *t, unsigned fields
     for (int f = 0; f < 5; ++f) {
         if (!(fields & bits[f])) continue;
         if (src[f] && n > 0) {
-            memcpy(h + (size_t)f * n * 24, src[f], (size_t)n * 24);
-            OV_CUDA(c, cudaMemcpyAsync(c->d_stage + (size_t)f * n * 24, h + (size_t)f * n * 24, (size_t)n * 24,
+            OV_CUDA(c, cudaMemcpyAsync(c->d_stage + (size_t)f * n * 24, src[f], (size_t)n * 24,
                                        cudaMemcpyHostToDevice, c->stream));
             have |= bits[f];
         }
         c->last_h2d += 3 * cap * sizeof(double);
     }
     if ((fields & OV_F_TOPOLOGY) && n > 0) {
-        memcpy(h + stage_topo_off(n), t->connections, (size_t)n * 8);
-        memcpy(h + stage_topo_off(n) + (size_t)n * 8, t->status, (size_t)n * 8);
-        OV_CUDA(c, cudaMemcpyAsync(c->d_stage + stage_topo_off(n), h + stage_topo_off(n), (size_t)n * 16,
+        OV_CUDA(c, cudaMemcpyAsync(c->d_stage + stage_topo_off(n), t->connections, (size_t)n * 8,
+                                   cudaMemcpyHostToDevice, c->stream));
+        OV_CUDA(c, cudaMemcpyAsync(c->d_stage + stage_topo_off(n) + (size_t)n * 8, t->status, (size_t)n * 8,
                                    cudaMemcpyHostToDevice, c->stream));
     }
     if (fields & OV_F_TOPOLOGY) c->last_h2d += 4 * cap * sizeof(int);
@@ -718,38 +715,35 @@ static int download_range(ov_ctx *c, ov_tangle_state *t, unsigned fields, int lo
     const int n = std::min(t->N, span);
     int r;
     const size_t bytes = stage_topo_off(n) + (size_t)n * 16;
-    if ((r = ensure_stage(c, std::max(bytes, (size_t)16)))) return r;
     if ((r = ensure_dstage(c, std::max(bytes, (size_t)16)))) return r;
-    char *h = reinterpret_cast<char *>(c->h_stage);
     const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
     ov_vec3 *dst[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
     if (n > 0) {
         // the device's arrays transposed to the host layout (k_pack), one copy each
         k_pack<<<(n + 255) / 256, 256, 0, c->stream>>>(fields, lo, n, node_ptrs(c), c->d_stage);
         c->launches++;
+        // straight into the caller's arrays
         for (int f = 0; f < 5; ++f) {
             if (!(fields & bits[f]) || !dst[f]) continue;
-            OV_CUDA(c, cudaMemcpyAsync(h + (size_t)f * n * 24, c->d_stage + (size_t)f * n * 24, (size_t)n * 24,
+            OV_CUDA(c, cudaMemcpyAsync(dst[f], c->d_stage + (size_t)f * n * 24, (size_t)n * 24,
                                        cudaMemcpyDeviceToHost, c->stream));
         }
-        if (fields & OV_F_TOPOLOGY)
-            OV_CUDA(c, cudaMemcpyAsync(h + stage_topo_off(n), c->d_stage + stage_topo_off(n), (size_t)n * 16,
+        if (fields & OV_F_TOPOLOGY) {
+            OV_CUDA(c, cudaMemcpyAsync(t->connections, c->d_stage + stage_topo_off(n), (size_t)n * 8,
                                        cudaMemcpyDeviceToHost, c->stream));
+            OV_CUDA(c, cudaMemcpyAsync(t->status, c->d_stage + stage_topo_off(n) + (size_t)n * 8, (size_t)n * 8,
+                                       cudaMemcpyDeviceToHost, c->stream));
+        }
         OV_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     for (int f = 0; f < 5; ++f) {
         if (!(fields & bits[f]) || !dst[f]) continue;
-        if (n > 0) memcpy(dst[f], h + (size_t)f * n * 24, (size_t)n * 24);
         for (int k = n; k < t->N; ++k)
             for (int a = 0; a < 3; ++a) dst[f][k].p[a] = 0.0;
     }
     if (fields & OV_F_TOPOLOGY) {
         t->next_empty = next_empty;
         t->total_empty = total_empty;
-        if (n > 0) {
-            memcpy(t->connections, h + stage_topo_off(n), (size_t)n * 8);
-            memcpy(t->status, h + stage_topo_off(n) + (size_t)n * 8, (size_t)n * 8);
-        }
         for (int k = n; k < t->N; ++k) {
             t->connections[k].forward = t->connections[k].reverse = -1;
             t->status[k].status = OV_EMPTY;
