@@ -170,6 +170,32 @@ def cpu_kind():
     return "reference" if pyoracle.reference_available() else "port"
 
 
+def port_vs_reference():
+    """The restatement's speed over OpenVort's own build at equal threads,
+    measured where OpenVort's sources exist (oracle/port_vs_reference.py)."""
+    path = os.path.join(ROOT, "oracle", "port_vs_reference.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f)
+
+
+def cpu_line(value, threads, kind, sample):
+    """A cpu_baseline object; for the restatement, with its measured speed
+    ratio to OpenVort's own build and the reference rate that implies."""
+    out = {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample}
+    pvr = port_vs_reference() if kind == "port" else None
+    if pvr:
+        out["port_over_reference"] = pvr["port_over_reference"]
+        out["reference_estimate"] = value / pvr["port_over_reference"]
+        out["port_over_reference_measured"] = (f"{pvr['machine']}, {pvr['threads']} threads each: "
+                                               f"{pvr['workload']}")
+        out["note"] = ("OpenVort's sources are not on this host, so the C restatement runs (bit-identical results); "
+                       "it is port_over_reference times faster than OpenVort's own build, so ratios against this "
+                       "value understate the speed-up over the reference")
+    return out
+
+
 def run_reference(args):
     world, rank, local, dist = dist_setup()
     if rank != 0:
@@ -187,8 +213,8 @@ def run_reference(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic", "impl": "reference", "config": WORKLOAD,
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
-                         "kind": kind, "sample": f"{args.steps} full update_tangle of the 65,536-node tangle"},
+        "l2": "inputs rebuilt per step on the host (CPU run)", "parallelism": "host threads",
+        "cpu_baseline": cpu_line(value, threads, kind, f"{args.steps} full update_tangle of the 65,536-node tangle"),
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -281,8 +307,8 @@ def run_ensemble(args, device=0):
     if args.cpu_sections:
         threads = os.cpu_count() or 1
         cpu_s = sum(min(cpu_eval_time(cpu_kind(), threads, 1, h, p)) for h, p in zip(hosts, params))
-        cpu = {"value": n / cpu_s, "unit": UNIT, "cores": threads, "kind": cpu_kind(),
-               "sample": "one full update_tangle of every member, members one after another"}
+        cpu = cpu_line(n / cpu_s, threads, cpu_kind(),
+                       "one full update_tangle of every member, members one after another")
     return {
         "cpu_baseline": cpu,
         "config": E, "members": len(hosts), "nodes": n, "nodes_per_member_min_max": [min(h.n for h in hosts),
@@ -361,9 +387,8 @@ def run_precision_form(args, device=0):
             threads = os.cpu_count() or 1
             cpu_s = min(cpu_eval_time(cpu_kind(), threads, 1, ht, W.config_params("rw", bh_resolution=theta)))
         out["by_theta"][str(theta)] = {
-            "cpu_baseline": None if cpu_s is None else {
-                "value": n / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": cpu_kind(),
-                "sample": "one full update_tangle of the 262,144-node tangle"},
+            "cpu_baseline": None if cpu_s is None else cpu_line(
+                n / cpu_s, os.cpu_count() or 1, cpu_kind(), "one full update_tangle of the 262,144-node tangle"),
             "fp64": {"value": n / (fp64_ms * 1e-3), "unit": UNIT, "ms_per_eval": fp64_ms,
                      "rel_l2_vs_direct_subsample": rel_l2(v64[sub], direct)},
             "mixed": {"value": n / (mixed_ms * 1e-3), "unit": UNIT, "ms_per_eval": mixed_ms,
@@ -437,9 +462,9 @@ def run_large(args, device=0):
     if args.cpu_sections:
         threads = os.cpu_count() or 1
         cpu_s = min(cpu_eval_time(cpu_kind(), threads, 1, ht, W.config_params("large", bh_resolution=E["theta"])))
-        cpu = {"value": n / cpu_s, "unit": UNIT, "cores": threads, "kind": cpu_kind(),
-               "sample": "one full update_tangle of the 1,048,576-node tangle (a full step is reconnect-dominated "
-                         "and not run on the CPU)"}
+        cpu = cpu_line(n / cpu_s, threads, cpu_kind(),
+                       "one full update_tangle of the 1,048,576-node tangle (a full step is reconnect-dominated "
+                       "and not run on the CPU)")
     return {
         "config": E, "nodes": n, "tuning": tune, "cpu_baseline": cpu,
         "fp64": {"value": n / (fp64_ms * 1e-3), "unit": UNIT, "ms_per_eval": fp64_ms},
@@ -452,6 +477,62 @@ def run_large(args, device=0):
                              "reconnections": recs, "remesh_added": added, "pass_ms": passes,
                              "reconnect_counts": rstat},
     }
+
+
+CONFIG_A = dict(workload="8 vortex rings of radius 0.02 cm (add_loop placement, 62 nodes each, 496 nodes), centres "
+                         "uniform and axes uniform on the sphere (seeded), D=0.1 cm, periodic_26, dl_min 1e-3, "
+                         "dl_max 3e-3, rec_dist 8e-4, alpha 0.098, alpha' 0.016, v_n 0.5 x, theta 0.4, dt 5e-5, "
+                         "200 main-loop steps (small loops, reconnect, periodic wrap, remesh, update_tangle, "
+                         "rk4_step); FP64",
+                steps=200, dt=5e-5,
+                crossing="the same step on 8 pairs of crossing rings (992 nodes; 12 reconnections in 200 steps)")
+
+
+def run_config_a(args, device=0):
+    """The small configuration's full 200-step run: GPU (FP64 path through
+    ov_step) and the CPU path on all host cores, steps/s; and the same for
+    crossing ring pairs, whose steps reconnect."""
+    from openvort_gb300 import abi, gpu, workloads as W
+    from oracle.pyoracle import Checker
+    A = CONFIG_A
+    out = {"config": A}
+    for name, ht in (("rings8", W.ring_tangle()), ("crossing_rings", W.crossing_rings())):
+        p = W.config_params("rings8")
+        ctx = gpu.Context(device, params=p, precision=abi.OV_PREC_FP64)
+        ctx.upload(ht)
+        for w in range(3):                       # warm-up on a copy of the run (graph capture, buffers)
+            ctx.step(w * A["dt"], A["dt"])
+        ctx.upload(ht)
+        recs = 0
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for k in range(A["steps"]):
+            ctx.step(k * A["dt"], A["dt"])
+            recs += ctx.stats()["reconnections"]
+        ctx.synchronize()
+        g_s = time.perf_counter() - t0
+        ctx.close()
+        sec = {"nodes": ht.n, "steps": A["steps"], "reconnections": recs,
+               "gpu": {"steps_per_s": A["steps"] / g_s, "ms_per_step": g_s * 1e3 / A["steps"],
+                       "timing": "host wall clock around the 200 ov_step calls"}}
+        if args.cpu_sections:
+            threads = os.cpu_count() or 1
+            port = Checker("port", fast=True)
+            p.num_threads = threads
+            port.set_params(p)
+            t = port.tangle(ht)
+            t0 = time.perf_counter()
+            crecs = sum(port.step(t, k * A["dt"], A["dt"]) for k in range(A["steps"]))
+            c_s = time.perf_counter() - t0
+            t.free()
+            pvr = port_vs_reference()
+            sec["cpu_baseline"] = {"steps_per_s": A["steps"] / c_s, "cores": threads, "kind": "port",
+                                   "reconnections": crecs, "sample": "the full 200 steps"}
+            if pvr:
+                sec["cpu_baseline"]["port_over_reference"] = pvr["port_over_reference"]
+            sec["gpu_over_cpu"] = c_s / g_s
+        out[name] = sec
+    return out
 
 
 def run_next_rows(args, device=0):
@@ -482,8 +563,7 @@ def run_next_rows(args, device=0):
         threads = os.cpu_count() or 1
         kind = cpu_kind()
         t = min(cpu_eval_time(kind, threads, 1, hw))
-        walls["cpu_baseline"] = {"value": n / t, "unit": UNIT, "cores": threads, "kind": kind,
-                                 "sample": "1 full update_tangle of the wall tangle"}
+        walls["cpu_baseline"] = cpu_line(n / t, threads, kind, "1 full update_tangle of the wall tangle")
     out["walls"] = walls
     # frames: the reference's text format, host code
     with tempfile.TemporaryDirectory() as d:
@@ -734,7 +814,12 @@ def run_ours(args):
     if isinstance(mixed, dict) and "value" in mixed:
         mixed["rel_l2_vs_direct_subsample"] = rel_l2(mixed_vels[sub], direct_v)
 
-    ensemble = precision_form = large = next_rows = None
+    ensemble = precision_form = large = next_rows = config_a = None
+    if world == 1 and args.config_a:
+        try:
+            config_a = run_config_a(args, device)
+        except Exception as e:
+            config_a = {"error": str(e)[:300]}
     if world == 1 and args.ensemble_steps >= 0:
         try:
             ensemble = run_ensemble(args, device)
@@ -763,8 +848,7 @@ def run_ours(args):
         threads = os.cpu_count() or 1
         kind = cpu_kind()
         times = cpu_eval_time(kind, threads, 2, ht)
-        cpu = {"value": n / min(times), "unit": UNIT, "cores": threads, "kind": kind,
-               "sample": "2 full update_tangle of the 65,536-node tangle (best of 2)"}
+        cpu = cpu_line(n / min(times), threads, kind, "2 full update_tangle of the 65,536-node tangle (best of 2)")
 
     ctx.close()
     if rank != 0:
@@ -773,8 +857,9 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox random-walk tangle)",
-        "config": dict(WORKLOAD, l2="flushed between timed steps (256 MiB write)",
-                       parallelism="replicas" if world > 1 else "single GPU"),
+        "config": WORKLOAD,
+        "l2": "flushed between timed steps (256 MiB write)",
+        "parallelism": "replicas" if world > 1 else "single GPU",
         "phases_ms": {"tangents": phases[0], "tree_build": phases[1], "traversal": phases[2]},
         "roofline": {"bound": "fma", "pipe": "fp64", "achieved": achieved, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": K_VEL_FP64_DRAM_BYTES,
@@ -793,6 +878,7 @@ def run_ours(args):
         "double_single": dd,
         "fp64_walk": walk64,
         "rk4": rk4,
+        "config_a": config_a,
         "ensemble": ensemble,
         "precision_form": precision_form,
         "large": large,
@@ -833,11 +919,13 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--ensemble-steps", type=int, default=10,
+    ap.add_argument("--ensemble-steps", type=int, default=100,
                     help="full time steps of the 48-tangle ensemble (-1: skip the ensemble section)")
-    ap.add_argument("--large-steps", type=int, default=5,
+    ap.add_argument("--large-steps", type=int, default=50,
                     help="full time steps of the 1,048,576-node tangle (-1: skip that section)")
     ap.add_argument("--precision-form", type=int, default=1, help="262,144-node theta 0.3/0.5 section (0: skip)")
+    ap.add_argument("--config-a", type=int, default=1,
+                    help="the 8-ring configuration's 200 steps (and crossing rings), GPU and CPU (0: skip)")
     ap.add_argument("--next-rows", type=int, default=1,
                     help="walls, frames, injection and spherical-fork sections (0: skip)")
     ap.add_argument("--cpu-sections", type=int, default=1,

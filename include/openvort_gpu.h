@@ -265,6 +265,9 @@ int ov_direct_sums_bounded(ov_ctx *ctx, const int *nodes, int n, int precision, 
  * writes every partial sum it later reads, so nothing carries over.
  * The first call on each device looks up the array's device address (with
  * that device current); make that first call before any stream capture.
+ * The address is kept for the life of the process: after cudaDeviceReset
+ * (which unloads the library's device code) do not call this entry point
+ * again in that process.
  *
  * Inputs (device pointers, n_slots node slots in the reference's indexing):
  *   d_pos       x[n_slots], y[n_slots], z[n_slots]          (SoA doubles)
@@ -273,7 +276,8 @@ int ov_direct_sums_bounded(ov_ctx *ctx, const int *nodes, int n, int precision, 
  *   d_tangents  / d_normals  SoA like d_pos
  *   d_nodes     n_nodes node ids, each in [0, n_slots)
  * Outputs (device, AoS): d_vels, d_vs  n_nodes x 3 doubles (d_vs may be NULL).
- * A node id out of range gives NaN outputs for that entry.
+ * An EMPTY slot gives zeros, as ov_direct_velocities does; a node id out of
+ * range gives NaN outputs for that entry.
  * Returns OV_ERR_ARG when n_nodes > OV_NOALLOC_MAX_NODES, n_nodes < 0 or a
  * required pointer is NULL; OV_ERR_CUDA when the launch or the address
  * look-up fails.  Asynchronous: synchronize `stream` before reading outputs.
@@ -394,6 +398,23 @@ int64_t ov_kernel_launches(const ov_ctx *ctx);
    ms[2] traversal. */
 int ov_set_phase_timing(ov_ctx *ctx, int on);
 int ov_phase_times(ov_ctx *ctx, float ms[3]);
+/* Per-target tree statistics (octree.c's walk, counted node by node): with
+   counting on, every velocity evaluation outside the RK4 graph records for
+   each slot the cells its 1 + n_img query points visited and the cells they
+   accepted; ov_get_node_counts copies the counts of the last evaluation for
+   slots [0, n) of a member (0 for a single tangle), n at most its slot count
+   (OV_ERR_STATE before the first evaluation).  A target whose counts differ
+   from the reference tree's took a different opening decision. */
+int ov_set_node_counting(ov_ctx *ctx, int on);
+
+/* Error-path testing: after `after` more successful device or pinned host
+   allocations of this context, the next one fails as if the device were out
+   of memory (no allocation is attempted); -1 switches it off.  Any allocation
+   failure, real or injected, returns OV_ERR_ALLOC, frees every buffer of the
+   context and leaves it holding no tangle: upload again to go on.  No
+   counterpart in the reference (its allocations are unchecked malloc). */
+int ov_inject_alloc_failure(ov_ctx *ctx, int after);
+int ov_get_node_counts(ov_ctx *ctx, int member, unsigned *visits, unsigned *accepts, int n);
 /* Measured multiply-add throughput of this GPU in TFLOP/s for FP64
    (precision OV_PREC_FP64) or FP32 (OV_PREC_MIXED): the roofline peak of
    the traversal, which is FMA-pipe bound. */

@@ -11,7 +11,7 @@
  * the reference program and redirect its calls with the linker, e.g.
  *   -Wl,--wrap=update_velocities -Wl,--wrap=rk4_step ...
  * after compiling ov_dropin.c with -DOV_DROPIN_WRAP, which adds the
- * __wrap_<name> aliases (see INTEGRATION.md).
+ * __wrap_<name> aliases.
  *
  * Failures: the reference functions are void; these print one line to
  * stderr and leave the status in ovd_last_status() (0 = OV_OK).

@@ -22,7 +22,7 @@ OBJ = os.path.join(LIB, "_obj")
 SO = os.path.join(LIB, "libovgpu.so")
 DROPIN = os.path.join(LIB, "libovdropin.a")
 
-CU_SOURCES = ["ov_sort.cu", "ov_tree.cu", "ov_velocity.cu", "ov_mixed.cu", "ov_capi.cu", "ov_topology.cu", "ov_peak.cu",
+CU_SOURCES = ["ov_sort.cu", "ov_tree.cu", "ov_velocity.cu", "ov_capi.cu", "ov_topology.cu", "ov_peak.cu",
               "ov_frames.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -130,37 +130,86 @@ static void free_nodes(NodeArrays &a)
     a = NodeArrays{};
 }
 
+}  // extern "C"
+
+// Free every device and pinned buffer of the context and forget their sizes
+// (streams, events and parameters stay): what the context holds after it is
+// what it held when created.
+static void release_buffers(ov_ctx *c)
+{
+    cudaStreamSynchronize(c->stream);
+    if (c->side) cudaStreamSynchronize(c->side);
+    free_nodes(c->node);
+    for (auto &s : c->stage) free_nodes(s);
+    ov_tree_free(c->tree);
+    void *dev[] = {c->fwd, c->rev, c->status, c->pin, c->dnodes, c->d_tid, c->d_qorder, c->d_tprm, c->d_mrange,
+                   c->d_pairs, c->d_npairs, c->d_loop_off, c->d_loop_nodes, c->d_loop_buf, c->d_loop_cut,
+                   c->rec_nodes, c->rec_pair, c->rec_out, c->rec_corr, c->rec_part, c->rec_split, c->fft_buf,
+                   c->fft_tw, c->long_buf, c->d_rm, c->d_rm_lim, c->dsum, c->part, c->d_node_counts, c->flush_buf,
+                   c->d_stage, c->d_time};
+    for (void *p : dev)
+        if (p) cudaFree(p);
+    void *pinned[] = {c->h_stage, c->h_corr, c->h_pf, c->h_time};
+    for (void *p : pinned)
+        if (p) cudaFreeHost(p);
+    if (c->rk4_exec) cudaGraphExecDestroy(c->rk4_exec);
+    c->rk4_exec = nullptr;
+    c->rk4_key = 0;
+    c->fwd = c->rev = c->status = c->pin = c->dnodes = c->d_tid = c->d_qorder = nullptr;
+    c->d_tprm = nullptr;
+    c->d_mrange = nullptr;
+    c->d_pairs = c->d_npairs = c->d_loop_off = c->d_loop_nodes = nullptr;
+    c->d_loop_buf = c->d_loop_cut = nullptr;
+    c->rec_nodes = c->rec_pair = nullptr;
+    c->rec_out = c->rec_corr = c->rec_part = nullptr;
+    c->rec_split = nullptr;
+    c->fft_buf = c->fft_tw = nullptr;
+    c->long_buf = nullptr;
+    c->d_rm = nullptr;
+    c->d_rm_lim = nullptr;
+    c->dsum = c->part = nullptr;
+    c->d_node_counts = nullptr;
+    c->flush_buf = nullptr;
+    c->d_stage = nullptr;
+    c->d_time = nullptr;
+    c->h_stage = c->h_corr = c->h_pf = c->h_pf_dev = c->h_time = nullptr;
+    c->cap = c->n_live = 0;
+    c->tcap = c->rm_cap = c->rm_lim_cap = c->pair_cap = c->loop_cap = c->loop_nodes_cap = 0;
+    c->rec_cap = c->rec_split_cap = c->dsum_cap = 0;
+    c->fft_cap = c->long_cap = c->loop_buf_cap = c->part_cap = c->rec_part_cap = c->h_corr_cap = 0;
+    c->h_stage_bytes = c->d_stage_bytes = c->node_counts_cap = c->flush_bytes = 0;
+    c->fft_M = 0;
+    c->time_dev_index = -1;
+    c->uploaded = c->tree_built = c->host_valid = false;
+}
+
+int ov_alloc_gate(ov_ctx *c)
+{
+    if (c->alloc_fail_after < 0) return OV_OK;
+    if (c->alloc_fail_after == 0) {
+        c->alloc_fail_after = -1;   // one failure, then allocations run again
+        return OV_ERR_ALLOC;
+    }
+    --c->alloc_fail_after;
+    return OV_OK;
+}
+
+int ov_alloc_failed(ov_ctx *c, const char *why, const char *what)
+{
+    release_buffers(c);
+    return ov_fail(c, OV_ERR_ALLOC, "allocation failed (%s): %s; the context holds no tangle now", why, what);
+}
+
+extern "C" {
+
 int ov_ctx_destroy(ov_ctx *c)
 {
     if (!c) return OV_OK;
     cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
-    free_nodes(c->node);
-    for (auto &s : c->stage) free_nodes(s);
-    ov_tree_free(c->tree);
-    int *is[] = {c->fwd, c->rev, c->status, c->pin, c->dnodes, c->d_tid, c->d_qorder};
-    for (int *p : is)
-        if (p) cudaFree(p);
-    if (c->d_tprm) cudaFree(c->d_tprm);
-    if (c->d_mrange) cudaFree(c->d_mrange);
-    void *scratch[] = {c->d_pairs, c->d_npairs, c->d_loop_off, c->d_loop_nodes, c->d_loop_buf, c->d_loop_cut,
-                       c->rec_nodes, c->rec_pair, c->rec_out, c->rec_corr, c->rec_part, c->rec_split,
-                       c->fft_buf, c->fft_tw, c->long_buf, c->d_rm, c->d_rm_lim};
-    for (void *p : scratch)
-        if (p) cudaFree(p);
-    if (c->dsum) cudaFree(c->dsum);
-    if (c->part) cudaFree(c->part);
-    if (c->flush_buf) cudaFree(c->flush_buf);
-    if (c->h_stage) cudaFreeHost(c->h_stage);
-    if (c->d_stage) cudaFree(c->d_stage);
-    if (c->h_corr) cudaFreeHost(c->h_corr);
-    if (c->h_pf) cudaFreeHost(c->h_pf);
+    release_buffers(c);
     if (c->rec_ev) cudaEventDestroy(c->rec_ev);
-    if (c->rk4_exec) cudaGraphExecDestroy(c->rk4_exec);
     for (int i = 0; i < 4; ++i)
         if (c->ph[i]) cudaEventDestroy(c->ph[i]);
-    if (c->d_time) cudaFree(c->d_time);
-    if (c->h_time) cudaFreeHost(c->h_time);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -168,6 +217,13 @@ int ov_ctx_destroy(ov_ctx *c)
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
     delete c;
+    return OV_OK;
+}
+
+int ov_inject_alloc_failure(ov_ctx *c, int after)
+{
+    if (!c || after < -1) return OV_ERR_ARG;
+    c->alloc_fail_after = after;
     return OV_OK;
 }
 
@@ -269,7 +325,7 @@ static int alloc_nodes(ov_ctx *c, NodeArrays &a, int cap)
     double **ps[] = {&a.x, &a.y, &a.z, &a.tx, &a.ty, &a.tz, &a.nx, &a.ny, &a.nz, &a.vx, &a.vy, &a.vz,
                      &a.sx, &a.sy, &a.sz};
     for (double **p : ps) {
-        OV_CUDA(c, cudaMalloc(p, b));
+        OV_ALLOC(c, cudaMalloc(p, b));
         OV_CUDA(c, cudaMemsetAsync(*p, 0, b, c->stream));
     }
     return OV_OK;
@@ -289,10 +345,10 @@ static int ensure_capacity(ov_ctx *c, int cap)
     if ((r = alloc_nodes(c, c->node, cap))) return r;
     for (auto &s : c->stage)
         if ((r = alloc_nodes(c, s, cap))) return r;
-    OV_CUDA(c, cudaMalloc(&c->fwd, (size_t)cap * 4));
-    OV_CUDA(c, cudaMalloc(&c->rev, (size_t)cap * 4));
-    OV_CUDA(c, cudaMalloc(&c->status, (size_t)cap * 4));
-    OV_CUDA(c, cudaMalloc(&c->pin, (size_t)cap * 4));
+    OV_ALLOC(c, cudaMalloc(&c->fwd, (size_t)cap * 4));
+    OV_ALLOC(c, cudaMalloc(&c->rev, (size_t)cap * 4));
+    OV_ALLOC(c, cudaMalloc(&c->status, (size_t)cap * 4));
+    OV_ALLOC(c, cudaMalloc(&c->pin, (size_t)cap * 4));
     if ((r = ov_tree_reserve(c, cap))) return r;
     c->cap = cap;
     return OV_OK;
@@ -309,7 +365,7 @@ int ov_grow_preserving(ov_ctx *c, int cap)
                      &c->node.sz};
     for (double **p : ps) {
         double *q = nullptr;
-        OV_CUDA(c, cudaMalloc(&q, nn));
+        OV_ALLOC(c, cudaMalloc(&q, nn));
         OV_CUDA(c, cudaMemsetAsync(q, 0, nn, c->stream));
         OV_CUDA(c, cudaMemcpyAsync(q, *p, nb, cudaMemcpyDeviceToDevice, c->stream));
         OV_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -319,7 +375,7 @@ int ov_grow_preserving(ov_ctx *c, int cap)
     int **is[] = {&c->fwd, &c->rev, &c->status, &c->pin};
     for (int **p : is) {
         int *q = nullptr;
-        OV_CUDA(c, cudaMalloc(&q, (size_t)cap * 4));
+        OV_ALLOC(c, cudaMalloc(&q, (size_t)cap * 4));
         OV_CUDA(c, cudaMemsetAsync(q, 0xFF, (size_t)cap * 4, c->stream));   // -1: EMPTY / no link
         OV_CUDA(c, cudaMemcpyAsync(q, *p, (size_t)old * 4, cudaMemcpyDeviceToDevice, c->stream));
         OV_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -341,7 +397,7 @@ static int ensure_stage(ov_ctx *c, size_t bytes)
     if (c->h_stage_bytes >= bytes) return OV_OK;
     if (c->h_stage) cudaFreeHost(c->h_stage);
     c->h_stage = nullptr;
-    OV_CUDA(c, cudaMallocHost(&c->h_stage, bytes));
+    OV_ALLOC(c, cudaMallocHost(&c->h_stage, bytes));
     c->h_stage_bytes = bytes;
     return OV_OK;
 }
@@ -353,7 +409,7 @@ static int ensure_dstage(ov_ctx *c, size_t bytes)
     if (c->d_stage_bytes >= bytes) return OV_OK;
     if (c->d_stage) cudaFree(c->d_stage);
     c->d_stage = nullptr;
-    OV_CUDA(c, cudaMalloc(&c->d_stage, bytes));
+    OV_ALLOC(c, cudaMalloc(&c->d_stage, bytes));
     c->d_stage_bytes = bytes;
     return OV_OK;
 }
@@ -465,11 +521,11 @@ int ov_reserve_members(ov_ctx *c, int nt)
     if (c->d_mrange) cudaFree(c->d_mrange);
     c->tree.tt = nullptr; c->d_tprm = nullptr; c->d_qorder = nullptr; c->d_mrange = nullptr;
     c->tcap = 0;
-    OV_CUDA(c, cudaMalloc(&c->tree.tt, (size_t)nt * TT_WORDS * 4));
+    OV_ALLOC(c, cudaMalloc(&c->tree.tt, (size_t)nt * TT_WORDS * 4));
     OV_CUDA(c, cudaMemset(c->tree.tt, 0, (size_t)nt * TT_WORDS * 4));
-    OV_CUDA(c, cudaMalloc(&c->d_tprm, (size_t)nt * sizeof(DevParams)));
-    OV_CUDA(c, cudaMalloc(&c->d_qorder, (size_t)nt * 4));
-    OV_CUDA(c, cudaMalloc(&c->d_mrange, (size_t)nt * sizeof(int2)));
+    OV_ALLOC(c, cudaMalloc(&c->d_tprm, (size_t)nt * sizeof(DevParams)));
+    OV_ALLOC(c, cudaMalloc(&c->d_qorder, (size_t)nt * 4));
+    OV_ALLOC(c, cudaMalloc(&c->d_mrange, (size_t)nt * sizeof(int2)));
     c->tcap = nt;
     return OV_OK;
 }
@@ -499,7 +555,7 @@ int ov_upload_member_tables(ov_ctx *c)
     if (nt > 1) {
         if (c->d_tid) cudaFree(c->d_tid);
         c->d_tid = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->d_tid, (size_t)std::max(c->cap, 1) * 4));
+        OV_ALLOC(c, cudaMalloc(&c->d_tid, (size_t)std::max(c->cap, 1) * 4));
         std::vector<int> tid(std::max(c->cap, 1), 0);
         for (int i = 0; i < nt; ++i)
             for (int k = 0; k < c->mem[i].cap; ++k) tid[c->mem[i].lo + k] = i;
@@ -515,7 +571,7 @@ int ov_move_device_slots(ov_ctx *c, const std::vector<Member> &old)
 {
     size_t n = (size_t)std::max(c->n_live, 1);
     double *tmp = nullptr;
-    OV_CUDA(c, cudaMalloc(&tmp, n * sizeof(double)));
+    OV_ALLOC(c, cudaMalloc(&tmp, n * sizeof(double)));
     double *arrs[12] = {c->node.tx, c->node.ty, c->node.tz, c->node.nx, c->node.ny, c->node.nz,
                         c->node.vx, c->node.vy, c->node.vz, c->node.sx, c->node.sy, c->node.sz};
     int r = OV_OK;
@@ -960,8 +1016,8 @@ int ov_rk4_step(ov_ctx *c, double t, double dt)
     c->host_valid = false;
     cudaStream_t s = c->stream;
     if (!c->d_time) {
-        OV_CUDA(c, cudaMalloc(&c->d_time, 8 * sizeof(double)));
-        OV_CUDA(c, cudaMallocHost(&c->h_time, 8 * sizeof(double)));
+        OV_ALLOC(c, cudaMalloc(&c->d_time, 8 * sizeof(double)));
+        OV_ALLOC(c, cudaMallocHost(&c->h_time, 8 * sizeof(double)));
     }
     if ((r = ov_reserve_velocity_scratch(c))) return r;
     for (int attempt = 0; attempt < 3; ++attempt) {
@@ -1145,7 +1201,7 @@ int ov_flush_l2(ov_ctx *c, size_t bytes)
     if (c->flush_bytes < bytes) {
         if (c->flush_buf) cudaFree(c->flush_buf);
         c->flush_buf = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->flush_buf, bytes));
+        OV_ALLOC(c, cudaMalloc(&c->flush_buf, bytes));
         c->flush_bytes = bytes;
     }
     static int v = 0;
@@ -1168,6 +1224,29 @@ int ov_set_phase_timing(ov_ctx *c, int on)
     if (on && !c->ph[0])
         for (int i = 0; i < 4; ++i) OV_CUDA(c, cudaEventCreate(&c->ph[i]));
     c->phase_timing = on != 0;
+    return OV_OK;
+}
+
+int ov_set_node_counting(ov_ctx *c, int on)
+{
+    if (!c) return OV_ERR_ARG;
+    c->count_nodes = on != 0;
+    return OV_OK;
+}
+
+int ov_get_node_counts(ov_ctx *c, int member, unsigned *visits, unsigned *accepts, int n)
+{
+    if (!c || member < 0 || member >= (int)c->mem.size() || n < 0 || n > c->mem[member].n ||
+        (n > 0 && (!visits || !accepts)))
+        return OV_ERR_ARG;
+    if (!c->count_nodes || !c->d_node_counts || c->node_counts_cap < 2 * (size_t)c->cap)
+        return ov_fail(c, OV_ERR_STATE, "node counting is off or no evaluation ran since it was switched on");
+    const size_t lo = (size_t)c->mem[member].lo;
+    OV_CUDA(c, cudaMemcpyAsync(visits, c->d_node_counts + lo, (size_t)n * sizeof(unsigned), cudaMemcpyDeviceToHost,
+                               c->stream));
+    OV_CUDA(c, cudaMemcpyAsync(accepts, c->d_node_counts + c->cap + lo, (size_t)n * sizeof(unsigned),
+                               cudaMemcpyDeviceToHost, c->stream));
+    OV_CUDA(c, cudaStreamSynchronize(c->stream));
     return OV_OK;
 }
 

@@ -275,6 +275,13 @@ struct ov_ctx {
     size_t d_stage_bytes = 0;
     // spherical sections: (r, az, pl) bounds of each tree member's root cell
     double sph_lo[OV_SPH_MEMBERS][3] = {}, sph_hi[OV_SPH_MEMBERS][3] = {};
+    // allocation failure injection (ov_inject_alloc_failure): the number of
+    // device or pinned allocations that still succeed before one fails; -1 off
+    int alloc_fail_after = -1;
+    // per-target visit / accept counters of the last evaluation (ov_set_node_counting)
+    bool count_nodes = false;
+    unsigned *d_node_counts = nullptr;
+    size_t node_counts_cap = 0;
     // per-phase timing of the last evaluation
     bool phase_timing = false;
     cudaEvent_t ph[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -290,6 +297,22 @@ int ov_fail(ov_ctx *c, int code, const char *fmt, ...);
                            #call, cudaGetErrorString(e_));                        \
     } while (0)
 #define OV_LAUNCHED(ctx) ((ctx)->launches++)
+
+// Device and pinned host allocations.  A failure (or an injected one) frees
+// every buffer the context holds and leaves it without a tangle (the next
+// call must upload again), then returns OV_ERR_ALLOC: no buffer is left
+// half-sized and no later launch can use one.
+int ov_alloc_gate(ov_ctx *c);
+int ov_alloc_failed(ov_ctx *c, const char *why, const char *what);
+#define OV_ALLOC(ctx, call)                                                        \
+    do {                                                                           \
+        if (ov_alloc_gate(ctx)) return ov_alloc_failed((ctx), "injected failure", #call); \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess) {                                                   \
+            cudaGetLastError();                                                    \
+            return ov_alloc_failed((ctx), cudaGetErrorString(e_), #call);          \
+        }                                                                          \
+    } while (0)
 
 DevParams ov_dev_params(const ov_params &p);
 

@@ -33,7 +33,7 @@ extern "C" int ov_measure_fma_peak(ov_ctx *c, int precision, double *tflops)
     int blocks = sms * 8, threads = 256;
     int iters = precision == OV_PREC_FP64 ? 2048 : 32768;
     void *buf = nullptr;
-    OV_CUDA(c, cudaMalloc(&buf, 64));
+    OV_ALLOC(c, cudaMalloc(&buf, 64));
     float best = 1e30f;
     for (int rep = 0; rep < 4; ++rep) {
         OV_CUDA(c, cudaEventRecord(c->ev0, c->stream));

@@ -1264,8 +1264,8 @@ int ensure_pairs(ov_ctx *c, int need)
     if (c->pair_cap >= need && c->d_pairs) return OV_OK;
     if (c->d_pairs) cudaFree(c->d_pairs);
     c->d_pairs = nullptr;
-    OV_CUDA(c, cudaMalloc(&c->d_pairs, (size_t)need * 2 * sizeof(int)));
-    if (!c->d_npairs) OV_CUDA(c, cudaMalloc(&c->d_npairs, sizeof(int)));
+    OV_ALLOC(c, cudaMalloc(&c->d_pairs, (size_t)need * 2 * sizeof(int)));
+    if (!c->d_npairs) OV_ALLOC(c, cudaMalloc(&c->d_npairs, sizeof(int)));
     c->pair_cap = need;
     return OV_OK;
 }
@@ -1337,7 +1337,7 @@ int bluestein3(ov_ctx *c, const double *re, const double2 *cin, int N, double2 *
     if (c->fft_cap < need) {
         if (c->fft_buf) cudaFree(c->fft_buf);
         c->fft_buf = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->fft_buf, need * sizeof(double2)));
+        OV_ALLOC(c, cudaMalloc(&c->fft_buf, need * sizeof(double2)));
         c->fft_cap = need;
         c->fft_M = 0;
     }
@@ -1346,7 +1346,7 @@ int bluestein3(ov_ctx *c, const double *re, const double2 *cin, int N, double2 *
     if (c->fft_M != M) {
         if (c->fft_tw) cudaFree(c->fft_tw);
         c->fft_tw = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->fft_tw, (size_t)std::max(M / 2, 1) * sizeof(double2)));
+        OV_ALLOC(c, cudaMalloc(&c->fft_tw, (size_t)std::max(M / 2, 1) * sizeof(double2)));
         tw = c->fft_tw;
         k_twiddles<<<(M / 2 + 255) / 256, 256, 0, st>>>(tw, M);
         c->fft_M = M;
@@ -1418,7 +1418,7 @@ int smooth_long_loop(ov_ctx *c, const int *nodes, int len, double freq_to_cutoff
     if (c->long_cap < need) {
         if (c->long_buf) cudaFree(c->long_buf);
         c->long_buf = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->long_buf, need));
+        OV_ALLOC(c, cudaMalloc(&c->long_buf, need));
         c->long_cap = need;
     }
     // complex arrays first: every double2 stays 16-byte aligned
@@ -1673,7 +1673,7 @@ int push_added(ov_ctx *c, const std::vector<int> &added)
     int r = ov_push_device(c, 1);
     if (r || added.empty()) return r;
     int *d = nullptr;
-    OV_CUDA(c, cudaMalloc(&d, added.size() * sizeof(int)));
+    OV_ALLOC(c, cudaMalloc(&d, added.size() * sizeof(int)));
     OV_CUDA(c, cudaMemcpy(d, added.data(), added.size() * sizeof(int), cudaMemcpyHostToDevice));
     k_zero_vel<<<((int)added.size() + 255) / 256, 256, 0, c->stream>>>(
         d, (int)added.size(), c->node.vx, c->node.vy, c->node.vz, c->node.sx, c->node.sy, c->node.sz);
@@ -1712,7 +1712,7 @@ int ov_eliminate_small_loops(ov_ctx *c)
         if (c->rm_cap < n + 1) {
             if (c->d_rm) cudaFree(c->d_rm);
             c->d_rm = nullptr;
-            OV_CUDA(c, cudaMalloc(&c->d_rm, (size_t)(n + 1) * sizeof(int)));
+            OV_ALLOC(c, cudaMalloc(&c->d_rm, (size_t)(n + 1) * sizeof(int)));
             c->rm_cap = n + 1;
         }
         int *d_count = c->d_rm + n;
@@ -1787,13 +1787,13 @@ int ov_remesh(ov_ctx *c, double min_dist, double max_dist, double t)
         if (c->rm_cap < n + 1) {
             if (c->d_rm) cudaFree(c->d_rm);
             c->d_rm = nullptr;
-            OV_CUDA(c, cudaMalloc(&c->d_rm, (size_t)(n + 1) * sizeof(int)));
+            OV_ALLOC(c, cudaMalloc(&c->d_rm, (size_t)(n + 1) * sizeof(int)));
             c->rm_cap = n + 1;
         }
         if (c->rm_lim_cap < 2 * nmem) {
             if (c->d_rm_lim) cudaFree(c->d_rm_lim);
             c->d_rm_lim = nullptr;
-            OV_CUDA(c, cudaMalloc(&c->d_rm_lim, 2 * (size_t)nmem * sizeof(double)));
+            OV_ALLOC(c, cudaMalloc(&c->d_rm_lim, 2 * (size_t)nmem * sizeof(double)));
             c->rm_lim_cap = 2 * nmem;
         }
         OV_CUDA(c, cudaMemcpyAsync(c->d_rm_lim, lim.data(), lim.size() * sizeof(double), cudaMemcpyHostToDevice,
@@ -1845,7 +1845,7 @@ int ov_remesh(ov_ctx *c, double min_dist, double max_dist, double t)
     if ((r = ov_push_device(c, 1))) return r;
     if (!new_nodes.empty()) {
         int *d = nullptr;
-        OV_CUDA(c, cudaMalloc(&d, new_nodes.size() * sizeof(int)));
+        OV_ALLOC(c, cudaMalloc(&d, new_nodes.size() * sizeof(int)));
         OV_CUDA(c, cudaMemcpy(d, new_nodes.data(), new_nodes.size() * sizeof(int), cudaMemcpyHostToDevice));
         k_zero_vel<<<((int)new_nodes.size() + 255) / 256, 256, 0, c->stream>>>(
             d, (int)new_nodes.size(), c->node.vx, c->node.vy, c->node.vz, c->node.sx, c->node.sy, c->node.sz);
@@ -1886,7 +1886,7 @@ int ov_reconnect(ov_ctx *c, double t, int *nrecs, int *log_k, int *log_l, int lo
     if (c->h_corr_cap < 4 * (size_t)std::max(C, 1)) {
         if (c->h_corr) cudaFreeHost(c->h_corr);
         c->h_corr = nullptr;
-        OV_CUDA(c, cudaMallocHost(&c->h_corr, 4 * (size_t)std::max(C, 1) * sizeof(double)));
+        OV_ALLOC(c, cudaMallocHost(&c->h_corr, 4 * (size_t)std::max(C, 1) * sizeof(double)));
         c->h_corr_cap = 4 * (size_t)std::max(C, 1);
     }
     double *corr = c->h_corr;
@@ -2320,16 +2320,17 @@ int ov_smooth(ov_ctx *c)
         if (c->d_loop_nodes) cudaFree(c->d_loop_nodes);
         if (c->d_loop_cut) cudaFree(c->d_loop_cut);
         c->d_loop_off = nullptr; c->d_loop_nodes = nullptr; c->d_loop_cut = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->d_loop_off, (size_t)(nloops + 1) * 4));
-        OV_CUDA(c, cudaMalloc(&c->d_loop_cut, (size_t)(nloops + 1) * sizeof(double)));
-        OV_CUDA(c, cudaMalloc(&c->d_loop_nodes, std::max(total, (size_t)1) * 4));
+        OV_ALLOC(c, cudaMalloc(&c->d_loop_off, (size_t)(nloops + 1) * 4));
+        OV_ALLOC(c, cudaMalloc(&c->d_loop_cut, (size_t)(nloops + 1) * sizeof(double)));
+        OV_ALLOC(c, cudaMalloc(&c->d_loop_nodes, std::max(total, (size_t)1) * 4));
         c->loop_cap = nloops + 1;
         c->loop_nodes_cap = (int)total;
     }
     size_t need = total * 2 * 3 * sizeof(double);
     if (c->loop_buf_cap < need) {
         if (c->d_loop_buf) cudaFree(c->d_loop_buf);
-        OV_CUDA(c, cudaMalloc(&c->d_loop_buf, need));
+        c->d_loop_buf = nullptr;
+        OV_ALLOC(c, cudaMalloc(&c->d_loop_buf, need));
         c->loop_buf_cap = need;
     }
     OV_CUDA(c, cudaMemcpyAsync(c->d_loop_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice, c->stream));
@@ -2381,7 +2382,7 @@ int ov_enforce_wall_boundaries(ov_ctx *c, double t)
     if ((r = ov_push_device(c, 1))) return r;
     if (!new_nodes.empty()) {
         int *d = nullptr;
-        OV_CUDA(c, cudaMalloc(&d, new_nodes.size() * sizeof(int)));
+        OV_ALLOC(c, cudaMalloc(&d, new_nodes.size() * sizeof(int)));
         OV_CUDA(c, cudaMemcpy(d, new_nodes.data(), new_nodes.size() * sizeof(int), cudaMemcpyHostToDevice));
         k_zero_vel<<<((int)new_nodes.size() + 255) / 256, 256, 0, c->stream>>>(
             d, (int)new_nodes.size(), c->node.vx, c->node.vy, c->node.vz, c->node.sx, c->node.sy, c->node.sz);

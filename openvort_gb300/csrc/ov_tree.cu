@@ -605,13 +605,13 @@ int ov_tree_reserve_cells(ov_ctx *c, int cells)
     for (void *p : ptrs)
         if (p) cudaFree(p);
     t.cap_cells = cells;
-    OV_CUDA(c, cudaMalloc(&t.cells, (size_t)t.cap_cells * sizeof(Cell64)));
-    OV_CUDA(c, cudaMalloc(&t.cells32, (size_t)t.cap_cells * sizeof(Cell32)));
-    OV_CUDA(c, cudaMalloc(&t.cellsff, (size_t)t.cap_cells * sizeof(CellFF)));
-    OV_CUDA(c, cudaMalloc(&t.parent, (size_t)t.cap_cells * 4));
-    OV_CUDA(c, cudaMalloc(&t.nchild, (size_t)t.cap_cells * 4));
-    OV_CUDA(c, cudaMalloc(&t.arrive, (size_t)t.cap_cells * 4));
-    OV_CUDA(c, cudaMalloc(&t.csum, (size_t)t.cap_cells * 6 * 8));
+    OV_ALLOC(c, cudaMalloc(&t.cells, (size_t)t.cap_cells * sizeof(Cell64)));
+    OV_ALLOC(c, cudaMalloc(&t.cells32, (size_t)t.cap_cells * sizeof(Cell32)));
+    OV_ALLOC(c, cudaMalloc(&t.cellsff, (size_t)t.cap_cells * sizeof(CellFF)));
+    OV_ALLOC(c, cudaMalloc(&t.parent, (size_t)t.cap_cells * 4));
+    OV_ALLOC(c, cudaMalloc(&t.nchild, (size_t)t.cap_cells * 4));
+    OV_ALLOC(c, cudaMalloc(&t.arrive, (size_t)t.cap_cells * 4));
+    OV_ALLOC(c, cudaMalloc(&t.csum, (size_t)t.cap_cells * 6 * 8));
     return OV_OK;
 }
 
@@ -625,17 +625,17 @@ int ov_tree_reserve(ov_ctx *c, int cap)
     t.tt = tt;
     t.cap = cap;
     size_t n = (size_t)cap;
-    OV_CUDA(c, cudaMalloc(&t.keys, n * 8));
-    OV_CUDA(c, cudaMalloc(&t.keys_alt, n * 8));
-    OV_CUDA(c, cudaMalloc(&t.order, n * 4));
-    OV_CUDA(c, cudaMalloc(&t.order_alt, n * 4));
-    OV_CUDA(c, cudaMalloc(&t.torder, n * 4));
-    OV_CUDA(c, cudaMalloc(&t.cpl, n * 4 + 4));
-    OV_CUDA(c, cudaMalloc(&t.ncell_at, n * 4 + 4));
-    OV_CUDA(c, cudaMalloc(&t.cell_off, n * 4 + 8));
-    OV_CUDA(c, cudaMalloc(&t.scan_tmp, (size_t)ov_scan_tmp_ints(cap) * 4));
-    OV_CUDA(c, cudaMalloc(&t.sort_hist, (size_t)ov_sort_hist_ints(cap) * 4));
-    OV_CUDA(c, cudaMalloc(&t.counters, TC_WORDS * 4));
+    OV_ALLOC(c, cudaMalloc(&t.keys, n * 8));
+    OV_ALLOC(c, cudaMalloc(&t.keys_alt, n * 8));
+    OV_ALLOC(c, cudaMalloc(&t.order, n * 4));
+    OV_ALLOC(c, cudaMalloc(&t.order_alt, n * 4));
+    OV_ALLOC(c, cudaMalloc(&t.torder, n * 4));
+    OV_ALLOC(c, cudaMalloc(&t.cpl, n * 4 + 4));
+    OV_ALLOC(c, cudaMalloc(&t.ncell_at, n * 4 + 4));
+    OV_ALLOC(c, cudaMalloc(&t.cell_off, n * 4 + 8));
+    OV_ALLOC(c, cudaMalloc(&t.scan_tmp, (size_t)ov_scan_tmp_ints(cap) * 4));
+    OV_ALLOC(c, cudaMalloc(&t.sort_hist, (size_t)ov_sort_hist_ints(cap) * 4));
+    OV_ALLOC(c, cudaMalloc(&t.counters, TC_WORDS * 4));
     OV_CUDA(c, cudaMemset(t.counters, 0, TC_WORDS * 4));
     // cells: about 1.3 per node for filament tangles (plus a root per
     // member); grown on demand

@@ -58,7 +58,18 @@ struct VelArgs {
     float f4pi_h, f4pi_l;        // KAPPA/4/pi in double-single
     double near2;           // mixed path: squared near-field radius
     unsigned long long *stat;
+    unsigned *node_counts;  // when set: visits[cap], then accepts[cap], per target slot
 };
+
+// Add one work item's visits and accepts of target slot id to the per-node
+// counters (only when they were asked for: ov_set_node_counting).
+__device__ __forceinline__ void count_node(const VelArgs &a, bool valid, int id, unsigned vis, unsigned acc)
+{
+    if (a.node_counts && valid) {
+        atomicAdd(&a.node_counts[id], vis);
+        atomicAdd(&a.node_counts[a.cap + id], acc);
+    }
+}
 
 // Record the first failed bounds check (code, index) and raise the error bit.
 __device__ __forceinline__ void bad_index(const VelArgs &a, int code, int idx)
@@ -499,6 +510,7 @@ __global__ void __launch_bounds__(32 * W, min_blocks<W>()) k_vel_fp64(VelArgs a,
         double p[3] = {0, 0, 0};
         if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
         double prim[3] = {0, 0, 0}, img[3] = {0, 0, 0};
+        const unsigned long long vis0 = visits, acc0 = accepts;
         for (int qi = w.grp; qi <= a.geo.n_img; qi += a.G) {
             const int j = qi - 1;
             double q[3], v[3];
@@ -519,6 +531,7 @@ __global__ void __launch_bounds__(32 * W, min_blocks<W>()) k_vel_fp64(VelArgs a,
                 part_out[((size_t)(2 * w.grp + 1) * 3 + ax) * cap + tix] = img[ax];
             }
         }
+        count_node(a, valid, id, (unsigned)(visits - vis0), (unsigned)(accepts - acc0));
     }
     int err = overflow ? OV_EW_ITER : 0;
 #pragma unroll
@@ -1118,6 +1131,7 @@ __global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mix
                 part_out[((size_t)(2 * w.grp + 1) * 3 + ax) * cap + tix] = 0.0;
             }
         }
+        count_node(a, valid, id, m.nvis, m.nacc);
         visits += m.nvis;
         accepts += m.nacc;
         steps += m.nstep;
@@ -1353,6 +1367,7 @@ __global__ void __launch_bounds__(32 * W, min_blocks_split<W>()) k_vel_split(Vel
                 part_out[((size_t)(2 * w.grp + 1) * 3 + ax) * cap + tix] = img[ax];
             }
         }
+        count_node(a, valid, id, m.nvis, m.nacc);
         visits += m.nvis;
         accepts += m.nacc;
         steps += m.nstep;
@@ -1441,6 +1456,7 @@ VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long 
     a.f4pif = (float)a.f4pi;
     a.f4pi_h = (float)a.f4pi;
     a.f4pi_l = (float)(a.f4pi - (double)a.f4pi_h);
+    a.node_counts = nullptr;
     return a;
 }
 
@@ -1460,7 +1476,7 @@ int ov_reserve_velocity_scratch(ov_ctx *c)
     if (c->part_cap < need) {
         if (c->part) cudaFree(c->part);
         c->part = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->part, need * sizeof(double)));
+        OV_ALLOC(c, cudaMalloc(&c->part, need * sizeof(double)));
         c->part_cap = need;
     }
     return OV_OK;
@@ -1525,6 +1541,19 @@ int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precisio
     int warps = c->tune.warps;
     if (warps != 2 && warps != 8) warps = 4;
     int blocks = ov_traversal_blocks(c, precision, warps, nullptr);
+    if (c->count_nodes && c->time_dev_index < 0) {
+        // per-target counters (not inside the captured RK4 graph)
+        const size_t need = 2 * (size_t)c->cap;
+        if (c->node_counts_cap < need) {
+            if (c->d_node_counts) cudaFree(c->d_node_counts);
+            c->d_node_counts = nullptr;
+            c->node_counts_cap = 0;
+            OV_ALLOC(c, cudaMalloc(&c->d_node_counts, need * sizeof(unsigned)));
+            c->node_counts_cap = need;
+        }
+        OV_CUDA(c, cudaMemsetAsync(c->d_node_counts, 0, need * sizeof(unsigned), s));
+        a.node_counts = c->d_node_counts;
+    }
     OV_CUDA(c, cudaMemsetAsync(a.work, 0, sizeof(int), s));
     vel_kernel(precision, c->walk, warps, c->tune.hi_occ)<<<blocks, 32 * warps, 0, s>>>(a, c->part);
     k_vel_finish<<<(c->cap + 127) / 128, 128, 0, s>>>(a, c->part);
@@ -1541,8 +1570,8 @@ int ov_direct_sum(ov_ctx *c, const int *nodes, int n, double t, double *vels_out
         if (c->dsum) cudaFree(c->dsum);
         if (c->dnodes) cudaFree(c->dnodes);
         c->dsum = nullptr; c->dnodes = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->dsum, (size_t)n * 9 * sizeof(double)));
-        OV_CUDA(c, cudaMalloc(&c->dnodes, (size_t)n * sizeof(int)));
+        OV_ALLOC(c, cudaMalloc(&c->dsum, (size_t)n * 9 * sizeof(double)));
+        OV_ALLOC(c, cudaMalloc(&c->dnodes, (size_t)n * sizeof(int)));
         c->dsum_cap = n;
     }
     double *vo = c->dsum + 3 * (size_t)n, *so = c->dsum + 6 * (size_t)n;
@@ -1601,8 +1630,8 @@ extern "C" int ov_tree_velocity_at(ov_ctx *c, const double *points, int n, doubl
         if (c->dsum) cudaFree(c->dsum);
         if (c->dnodes) cudaFree(c->dnodes);
         c->dsum = nullptr; c->dnodes = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->dsum, (size_t)n * 9 * sizeof(double)));
-        OV_CUDA(c, cudaMalloc(&c->dnodes, (size_t)n * sizeof(int)));
+        OV_ALLOC(c, cudaMalloc(&c->dsum, (size_t)n * 9 * sizeof(double)));
+        OV_ALLOC(c, cudaMalloc(&c->dnodes, (size_t)n * sizeof(int)));
         c->dsum_cap = n;
     }
     double *dp = c->dsum, *dout = c->dsum + 3 * (size_t)n;
@@ -2079,7 +2108,7 @@ int rec_reserve(ov_ctx *c, int n, int max_chunks)
     if (c->rec_part_cap < need_part) {
         if (c->rec_part) cudaFree(c->rec_part);
         c->rec_part = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->rec_part, need_part * sizeof(double)));
+        OV_ALLOC(c, cudaMalloc(&c->rec_part, need_part * sizeof(double)));
         c->rec_part_cap = need_part;
     }
     if (c->rec_cap < n) {
@@ -2087,15 +2116,15 @@ int rec_reserve(ov_ctx *c, int n, int max_chunks)
         if (c->rec_out) cudaFree(c->rec_out);
         if (c->rec_corr) cudaFree(c->rec_corr);
         c->rec_nodes = nullptr; c->rec_out = nullptr; c->rec_corr = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->rec_nodes, (size_t)n * sizeof(int)));
-        OV_CUDA(c, cudaMalloc(&c->rec_out, (size_t)n * 5 * sizeof(double)));
-        OV_CUDA(c, cudaMalloc(&c->rec_corr, (size_t)n * 4 * sizeof(double)));
+        OV_ALLOC(c, cudaMalloc(&c->rec_nodes, (size_t)n * sizeof(int)));
+        OV_ALLOC(c, cudaMalloc(&c->rec_out, (size_t)n * 5 * sizeof(double)));
+        OV_ALLOC(c, cudaMalloc(&c->rec_corr, (size_t)n * 4 * sizeof(double)));
         c->rec_cap = n;
     }
     if (c->rec_split_cap < c->cap) {
         if (c->rec_split) cudaFree(c->rec_split);
         c->rec_split = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->rec_split, (size_t)c->cap * 9 * sizeof(float)));
+        OV_ALLOC(c, cudaMalloc(&c->rec_split, (size_t)c->cap * 9 * sizeof(float)));
         c->rec_split_cap = c->cap;
     }
     return OV_OK;
@@ -2163,7 +2192,7 @@ int ov_rec_exact(ov_ctx *c, int k, int l, double out[10])
     for (const Member &m : c->mem) maxcap = std::max(maxcap, c->mem.size() == 1 ? c->cap : m.cap);
     int r = rec_reserve(c, 2, std::max(1, (maxcap + 8191) / 8192));
     if (r) return r;
-    if (!c->rec_pair) OV_CUDA(c, cudaMalloc(&c->rec_pair, 2 * sizeof(int)));
+    if (!c->rec_pair) OV_ALLOC(c, cudaMalloc(&c->rec_pair, 2 * sizeof(int)));
     OV_CUDA(c, cudaMemcpyAsync(c->rec_pair, nodes, 2 * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     // the split positions of the current device positions
     k_split<<<(c->cap + 255) / 256, 256, 0, c->stream>>>(c->node.x, c->node.y, c->node.z, c->cap, c->grid_h,
@@ -2227,7 +2256,7 @@ int ov_rec_correct(ov_ctx *c, int c0, int nc, const int *m, const int *f, const 
     if (nc <= 0) return OV_OK;
     if (npf < 0 || npf > kPrefetchMax) return ov_fail(c, OV_ERR_ARG, "reconnect: %d prefetched candidates", npf);
     if (!c->h_pf) {
-        OV_CUDA(c, cudaHostAlloc(&c->h_pf, kPrefetchMax * 4 * sizeof(double), cudaHostAllocMapped));
+        OV_ALLOC(c, cudaHostAlloc(&c->h_pf, kPrefetchMax * 4 * sizeof(double), cudaHostAllocMapped));
         OV_CUDA(c, cudaHostGetDevicePointer((void **)&c->h_pf_dev, c->h_pf, 0));
     }
     if (!c->rec_ev) OV_CUDA(c, cudaEventCreateWithFlags(&c->rec_ev, cudaEventDisableTiming));
@@ -2304,7 +2333,9 @@ void ov_launch_periodic_wrap(ov_ctx *c, cudaStream_t s)
 // ov_direct_velocities keeps in a context buffer live here in a fixed array
 // compiled into the library.  Host code never uses the array's name as a
 // pointer (on the host it is only a stand-in); the device address is looked
-// up once per device and passed to the kernels.
+// up once per device and passed to the kernels.  That address belongs to the
+// device's context as it was at the first call: after cudaDeviceReset the
+// entry point must not be called again in the process.
 // ----------------------------------------------------------------------------
 #include <mutex>
 
@@ -2369,15 +2400,18 @@ __global__ void k_direct_noalloc_finish(VelArgs a, const int *__restrict__ nodes
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     int k = nodes[b];
+    // as k_direct_finish: an EMPTY slot gives zeros; only an id outside the
+    // slot range (which the allocating call never sees) gives NaN
     const double nan = __longlong_as_double(0x7ff8000000000000ll);
-    double vs[3] = {nan, nan, nan}, vel[3] = {nan, nan, nan};
-    if (k >= 0 && k < n_slots && a.status[k] != OV_EMPTY) {
+    double vs[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
+    if (k < 0 || k >= n_slots) {
+        for (int ax = 0; ax < 3; ++ax) vs[ax] = vel[ax] = nan;
+    } else if (a.status[k] != OV_EMPTY) {
         double p[3] = {a.x[k], a.y[k], a.z[k]};
         double prim[3] = {sums[3 * (size_t)b], sums[3 * (size_t)b + 1], sums[3 * (size_t)b + 2]};
         double zero[3] = {0, 0, 0};
         int err = 0;
-        if (!finish_node(a, k, p, prim, zero, &err, vs, vel))
-            for (int ax = 0; ax < 3; ++ax) vs[ax] = vel[ax] = nan;
+        finish_node(a, k, p, prim, zero, &err, vs, vel);
     }
     for (int ax = 0; ax < 3; ++ax) {
         vout[3 * (size_t)b + ax] = vel[ax];
@@ -2926,7 +2960,7 @@ int ov_launch_sph_velocities(ov_ctx *c, const SphDomain &d, const SphSettings &p
     if (c->part_cap < need) {
         if (c->part) cudaFree(c->part);
         c->part = nullptr;
-        OV_CUDA(c, cudaMalloc(&c->part, need * sizeof(double)));
+        OV_ALLOC(c, cudaMalloc(&c->part, need * sizeof(double)));
         c->part_cap = need;
     }
     const long long warps = 18LL * ((d.n + 31) / 32);

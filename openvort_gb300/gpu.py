@@ -78,6 +78,9 @@ def load(path: str | None = None):
         "ov_upload_tangle_fields": (C.c_int, [P, TS, C.c_uint]),
         "ov_set_phase_timing": (C.c_int, [P, C.c_int]),
         "ov_phase_times": (C.c_int, [P, C.POINTER(C.c_float)]),
+        "ov_set_node_counting": (C.c_int, [P, C.c_int]),
+        "ov_inject_alloc_failure": (C.c_int, [P, C.c_int]),
+        "ov_get_node_counts": (C.c_int, [P, C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_uint), C.c_int]),
         "ov_measure_fma_peak": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
         "ov_set_rk4_graph": (C.c_int, [P, C.c_int]),
         "ov_tangle_info": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
@@ -458,6 +461,23 @@ class Context:
         ms = (C.c_float * 3)()
         self._check(self.lib.ov_phase_times(self._h, ms))
         return list(ms)
+
+    def inject_alloc_failure(self, after: int = 0):
+        """The allocation after `after` more successful ones fails (-1: off)."""
+        self._check(self.lib.ov_inject_alloc_failure(self._h, int(after)))
+
+    def set_node_counting(self, on: bool = True):
+        self._check(self.lib.ov_set_node_counting(self._h, int(on)))
+
+    def node_counts(self, member: int = 0, n: int | None = None):
+        """(visits, accepts) per slot of a member (or the tangle) in the last
+        evaluation (node counting on)."""
+        n = self.member_info(member)[0] if n is None else n
+        vis = np.zeros(n, dtype=np.uint32)
+        acc = np.zeros(n, dtype=np.uint32)
+        self._check(self.lib.ov_get_node_counts(self._h, member, vis.ctypes.data_as(C.POINTER(C.c_uint)),
+                                                acc.ctypes.data_as(C.POINTER(C.c_uint)), n))
+        return vis.astype(np.int64), acc.astype(np.int64)
 
     def fma_peak_tflops(self, precision: int) -> float:
         v = C.c_double(0)

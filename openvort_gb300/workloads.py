@@ -331,6 +331,46 @@ def ring_tangle(n_rings: int = 8, radius: float = 0.02, D: float = 0.1, dl_min: 
     return ht
 
 
+def crossing_rings(n_pairs: int = 8, radius: float = 0.02, D: float = 0.1, dl_min: float = 1e-3,
+                   dl_max: float = 3e-3, seed: int = 43, gap_min: float = 2e-4, gap_max: float = 2e-3,
+                   n_images: int = 26) -> HostTangle:
+    """Pairs of rings that pass close to one another, so that the time steps
+    reconnect: ring A of each pair is placed as in ring_tangle (seeded centre
+    and axis); ring B passes A's point at angle 0 at a seeded gap in
+    [gap_min, gap_max], outside A, its plane tilted about A's radius there by
+    a seeded angle in [20, 160] degrees.  Node placement as add_loop's."""
+    npts = int(4 * np.pi * radius / (dl_max + dl_min))
+    ids = np.arange(n_pairs, dtype=np.uint64)
+    cx, cy = uniform2(seed, ids, 0, 30)
+    cz, ug = uniform2(seed, ids, 0, 31)
+    ub, _ = uniform2(seed, ids, 0, 32)
+    g0, g1 = normal2(seed, ids, 0, 33)
+    g2, _ = normal2(seed, ids, 0, 34)
+    centers = np.stack([cx, cy, cz], axis=1) * D
+    axes = _unit(np.stack([g0, g1, g2], axis=1))
+    phi = 2 * np.pi / npts * np.arange(npts)
+    pos = []
+    for i in range(n_pairs):
+        d = axes[i]
+        z = _perpendicular(d)
+        u = _unit(np.cross(z, d))
+        v = np.cross(d, u)
+        pos.append(centers[i] + radius * (np.cos(phi)[:, None] * u + np.sin(phi)[:, None] * v))
+        gap = gap_min + ug[i] * (gap_max - gap_min)
+        beta = np.radians(20 + 140 * ub[i])
+        w = np.cos(beta) * d + np.sin(beta) * v
+        cb = centers[i] + (2 * radius + gap) * u
+        pos.append(cb + radius * (np.cos(phi + np.pi)[:, None] * u + np.sin(phi + np.pi)[:, None] * w))
+    lo, hi = np.zeros(3), np.full(3, float(D))
+    pos = _wrap_into_box(np.concatenate(pos), lo, hi)
+    k = np.arange(2 * n_pairs * npts)
+    base = (k // npts) * npts
+    j = k % npts
+    ht = HostTangle(pos, base + (j + 1) % npts, base + (j - 1) % npts, lo, hi, n_images=n_images)
+    ht.meta = dict(kind="crossing_rings", n_pairs=n_pairs, radius=radius, D=D, npts=npts, seed=seed)
+    return ht
+
+
 @dataclass
 class EnsembleMember:
     tangle: HostTangle

@@ -523,6 +523,31 @@ void orc_count_interactions(const ov_tangle_state *t, double resolution, orc_cou
     orc_octree_destroy(tree);
 }
 
+/* Per-target visits and accepts of the reference tree (the counts of
+ * orc_count_interactions, node by node): visits[k], accepts[k] over node k's
+ * 1 + n_img query points; zero for EMPTY slots.  threads <= 0: one. */
+void orc_node_interactions(const ov_tangle_state *t, double resolution, int threads, long long *visits,
+                           long long *accepts)
+{
+    orc_cell *tree = orc_octree_build(t);
+    const int nthr = threads > 0 ? threads : 1;
+#pragma omp parallel for num_threads(nthr) schedule(dynamic, 64)
+    for (int k = 0; k < t->N; ++k) {
+        orc_counts o;
+        memset(&o, 0, sizeof o);
+        if (t->status[k].status != OV_EMPTY) {
+            count_walk(tree, &t->vnodes[k], resolution, &o);
+            for (int j = 0; j < t->bimg.n; ++j) {
+                ov_vec3 q = image_point(&t->bimg.images[j], t, t->vnodes[k]);
+                count_walk(tree, &q, resolution, &o);
+            }
+        }
+        visits[k] = o.visits;
+        accepts[k] = o.accepts;
+    }
+    orc_octree_destroy(tree);
+}
+
 /* ------------------------------------------------------------- velocity */
 
 /* lia_velocity (tangle.c:568-592) */

@@ -53,6 +53,9 @@ void orc_octree_destroy(orc_cell *tree);
 void orc_octree_get_vs(const ov_tangle_state *t, const orc_cell *tree, const ov_vec3 *r,
                        double resolution, const ov_params *p, ov_vec3 *res);
 void orc_count_interactions(const ov_tangle_state *t, double resolution, orc_counts *out);
+/* the same counts per target node (visits[N], accepts[N]) */
+void orc_node_interactions(const ov_tangle_state *t, double resolution, int threads, long long *visits,
+                           long long *accepts);
 
 /* velocity path (tangle.c) */
 void orc_update_tangent_normal(ov_tangle_state *t, int k);

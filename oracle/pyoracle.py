@@ -253,6 +253,18 @@ class Checker:
         v = t.views()
         return np.array(v["vels"][nodes]), np.array(v["vs"][nodes])
 
+    def node_interactions(self, t: CTangle, resolution: float, threads: int = 1):
+        """Per-target (visits, accepts) of the reference tree at `resolution`
+        over each node's 1 + n_img query points (int64 arrays of t.n)."""
+        assert self.kind == "port"
+        f = self.lib.orc_node_interactions
+        f.argtypes = [_TS, C.c_double, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+        vis = np.zeros(t.n, dtype=np.int64)
+        acc = np.zeros(t.n, dtype=np.int64)
+        f(C.byref(t.ts), resolution, int(threads), vis.ctypes.data_as(C.POINTER(C.c_longlong)),
+          acc.ctypes.data_as(C.POINTER(C.c_longlong)))
+        return vis, acc
+
     def low_pass_filter(self, x, freq_to_cutoff):
         assert self.kind == "port"
         a = np.ascontiguousarray(x, dtype=np.float64).copy()

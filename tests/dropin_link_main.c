@@ -1,7 +1,7 @@
 /*
  * A reference-side program that keeps OpenVort's own main-loop calls
  * (main.c:125-141) and is linked with -Wl,--wrap=... so those calls run on
- * libovgpu.  Built by tests/test_dropin_link.py.
+ * libovgpu.  Built and run by tests/test_dropin_link.py.
  */
 #include <stdio.h>
 

@@ -6,7 +6,7 @@ and stores inputs and outputs as small .npz files.  The GPU machine has no
 reference checkout; there the tests compare against these files and against
 the C restatement (oracle/ov_oracle.c), which these files also pin.
 
-Usage:  python tests/golden/make_golden.py [walls | injection | spherical]
+Usage:  python tests/golden/make_golden.py [walls | injection | spherical | events]
 """
 from __future__ import annotations
 
@@ -53,6 +53,78 @@ def ref_step(c, t, time, dt):
     c.rk4_step(t, time, dt)
     c.enforce_periodic(t)
     return n
+
+
+def port_step(c, t, time, dt):
+    """ref_step in the C restatement, returning the reconnection log too."""
+    c.eliminate_small_loops(t)
+    n, log = c.reconnect(t, 0.0, log=True)
+    c.eliminate_small_loops(t)
+    c.enforce_periodic(t)
+    c.remesh(t, c.params.dl_min, c.params.dl_max, 0.0)
+    c.eliminate_small_loops(t)
+    c.update_tangle(t, time)
+    c.rk4_step(t, time, dt)
+    c.enforce_periodic(t)
+    return n, log
+
+
+def event_trajectory(ref, ht, p, n_steps, dt, name):
+    """n_steps main-loop steps (main.c:125-141, periodic box, no smoothing)
+    of the reference, with the event log: reconnections per step, the
+    (k, l) pairs in order (from the C restatement run beside it, which must
+    leave the reference's connections, status and positions bit for bit at
+    every step), the slot arrays after every step whose topology changed,
+    and positions at a few steps."""
+    port = Checker("port")
+    p.num_threads = 8
+    ref.set_params(p)
+    port.set_params(p)
+    t, u = ref.tangle(ht), port.tangle(ht)
+    recs, pairs, n_slots, ev_steps, ev_conn, ev_status, traj, traj_steps = [], [], [], [], [], [], [], []
+    keep = {0, 4, 9, 19, 49, 99, 149, n_steps - 1}
+    prev = (t.copy("conn"), t.copy("status"))
+    v0 = None
+    for s in range(n_steps):
+        n = ref_step(ref, t, s * dt, dt)
+        n_port, log = port_step(port, u, s * dt, dt)
+        conn, status, pos = t.copy("conn"), t.copy("status"), t.copy("pos")
+        assert n_port == n, (s, n, n_port)
+        assert np.array_equal(u.copy("conn"), conn) and np.array_equal(u.copy("status"), status), s
+        assert np.array_equal(u.copy("pos"), pos), s
+        recs.append(n)
+        pairs += [(s, k, l) for k, l in log]
+        n_slots.append(t.n)
+        if s == 0:
+            v0 = t.copy("vels")
+        if conn.shape != prev[0].shape or not (np.array_equal(conn, prev[0]) and np.array_equal(status, prev[1])):
+            ev_steps.append(s)
+            ev_conn.append(conn)
+            ev_status.append(status)
+        prev = (conn, status)
+        if s in keep or (ev_steps and ev_steps[-1] == s):
+            live = status[:, 0] != -1
+            traj.append(np.where(live[:, None], pos, 0.0))
+            traj_steps.append(s)
+    cap = max(n_slots)
+
+    def pad(a, fill):
+        out = np.full((cap,) + a.shape[1:], fill, dtype=a.dtype)
+        out[:len(a)] = a
+        return out
+
+    out = dict(tangle_arrays(ht), dt=dt, recs=np.array(recs), n_slots=np.array(n_slots),
+               rec_pairs=np.array(pairs, dtype=np.int32).reshape(-1, 3),
+               event_steps=np.array(ev_steps, dtype=np.int32), traj=np.stack([pad(a, 0.0) for a in traj]),
+               traj_steps=np.array(traj_steps), vels_step0=v0, conn_final=t.copy("conn"),
+               status_final=t.copy("status"))
+    if ev_steps:
+        out["event_conn"] = np.stack([pad(a, -1) for a in ev_conn])
+        out["event_status"] = np.stack([pad(a, -1) for a in ev_status])
+    print(name, "reconnections", sum(recs), "pairs", len(pairs), "event steps", ev_steps)
+    save(name, **out)
+    t.free()
+    u.free()
 
 
 WALL_SETS = ("wall_1_open", "wall_1_18", "wall_1_26", "wall_2_4", "wall_2_2", "wall_parallel_planes",
@@ -331,6 +403,10 @@ def main():
         walls(ref)
         wall_steps(ref)
         return
+    if len(sys.argv) > 1 and sys.argv[1] == "events":
+        event_trajectory(ref, W.ring_tangle(), W.config_params("rings8"), 200, 5e-5, "rings8_steps.npz")
+        event_trajectory(ref, W.crossing_rings(), W.config_params("rings8"), 200, 5e-5, "crossing_steps.npz")
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "spherical":
         spherical()
         return
@@ -362,25 +438,11 @@ def main():
     p.bh_resolution = 0.4
     save("rw16x64.npz", **out)
 
-    # 2. Ring configuration (8 rings, 496 nodes): 20 full steps with the event counts
-    ht = W.ring_tangle()
-    p = W.config_params("rings8")
-    p.num_threads = 8
-    ref.set_params(p)
-    t = ref.tangle(ht)
+    # 2. Ring configuration (8 rings, 496 nodes): 200 full steps with the event log;
+    #    and crossing ring pairs (16 rings, 992 nodes), whose 200 steps reconnect
     dt = 5e-5
-    traj, recs = [], []
-    v0 = None
-    for s in range(20):
-        recs.append(ref_step(ref, t, s * dt, dt))
-        if s == 0:
-            v0 = t.copy("vels")
-        traj.append(t.copy("pos"))
-    keep = [0, 4, 9, 19]
-    save("rings8_steps.npz", **tangle_arrays(ht), traj=np.stack(traj)[keep], traj_steps=np.array(keep),
-         recs=np.array(recs),
-         vels_step0=v0, conn_final=t.copy("conn"), status_final=t.copy("status"), dt=dt)
-    t.free()
+    event_trajectory(ref, W.ring_tangle(), W.config_params("rings8"), 200, dt, "rings8_steps.npz")
+    event_trajectory(ref, W.crossing_rings(), W.config_params("rings8"), 200, dt, "crossing_steps.npz")
 
     # 3. Dense random walk: reconnections and remeshing in the first steps
     ht = W.random_walk_tangle(24, 64, D=0.03, seed=5)

@@ -15,15 +15,26 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_INC = "/root/reference/include"
 OBJ = os.path.join(ROOT, "oracle", "_ref", "obj")
+
+
+def _ref_include() -> str:
+    """The reference's include/ directory, as recorded by oracle/Makefile's ref target."""
+    rec = os.path.join(ROOT, "oracle", "_ref", "ref_dir.txt")
+    if not os.path.exists(rec):
+        return ""
+    with open(rec) as f:
+        return os.path.join(f.read().strip(), "include")
+
+
+REF_INC = _ref_include()
 WRAPPED = ["update_tangents_normals", "update_velocities", "update_velocity", "rk4_step", "reconnect", "remesh",
            "eliminate_small_loops", "enforce_periodic_boundaries", "smooth", "octree_build", "octree_get_vs",
            "octree_destroy", "enforce_wall_boundaries", "save_tangle", "load_tangle", "add_loop", "add_line_in_zdir",
            "inject_vortices"]
 
 
-@pytest.mark.skipif(not (os.path.isdir(REF_INC) and glob.glob(os.path.join(OBJ, "*.o"))),
+@pytest.mark.skipif(not (REF_INC and os.path.isdir(REF_INC) and glob.glob(os.path.join(OBJ, "*.o"))),
                     reason="OpenVort checkout / reference objects not present")
 def test_reference_program_links_against_dropin(tmp_path):
     from openvort_gb300 import build
@@ -42,3 +53,23 @@ def test_reference_program_links_against_dropin(tmp_path):
     syms = subprocess.run(["nm", str(exe)], capture_output=True, text=True).stdout
     for n in WRAPPED:
         assert f"__wrap_{n}" in syms
+    # Run it.  Every wrapped call of the loop goes to the drop-in: with a GPU
+    # the loop runs on it; without one each call reports that it found no
+    # device and leaves the tangle as it was, and the program still ends.
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300,
+                         env={**os.environ, "LD_LIBRARY_PATH": libdir})
+    assert run.returncode == 0, run.stderr
+    assert run.stdout.startswith("nodes "), run.stdout
+    failures = [ln for ln in run.stderr.splitlines() if ln.startswith("libovgpu ")]
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        assert not failures, run.stderr
+    else:
+        # add_loop, then 3 steps of the main loop's 11 wrapped calls
+        # (update_tangle is update_tangents_normals + update_velocities)
+        assert len(failures) == 1 + 3 * 11, run.stderr
+        assert all("error" in ln for ln in failures)

@@ -11,12 +11,52 @@ import pytest
 
 from openvort_gb300 import abi, gpu, workloads as W
 from oracle.pyoracle import Checker
-from tests._util import host_from_arrays, rel_err, used
+from tests._util import check_event_trajectory, host_from_arrays, rel_err, used
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name,cfg", [("dense_steps.npz", "rw"), ("rings8_steps.npz", "rings8")])
+@pytest.mark.parametrize("name", ["rings8_steps.npz", "crossing_steps.npz"])
+@pytest.mark.parametrize("mode", ["step", "passes"])
+def test_200_steps_event_log_matches_reference(golden, name, mode):
+    """The 8-ring configuration (496 nodes; no reconnection in 200 steps) and
+    crossing ring pairs (992 nodes; 12 reconnections at steps 0-158): 200
+    main-loop steps on the GPU leave the reference's reconnection counts, the
+    topology after every step that changed it, and positions within 1e-10.
+    mode "step" runs ov_step; "passes" runs the passes one by one and also
+    checks the (k, l) pairs of every reconnection, in order."""
+    g = golden(name)
+    ht = host_from_arrays(g)
+    p = W.config_params("rings8")
+    ctx = gpu.Context(0, params=p)
+    ctx.upload(ht)
+    dt = float(g["dt"])
+
+    def step(s):
+        if mode == "step":
+            ctx.step(s * dt, dt)
+            return ctx.stats()["reconnections"]
+        ctx.eliminate_small_loops()
+        r = ctx.reconnect(0.0, log=True)
+        ctx.eliminate_small_loops()
+        ctx.enforce_periodic()
+        ctx.remesh(p.dl_min, p.dl_max, 0.0)
+        ctx.eliminate_small_loops()
+        ctx.update_tangle(s * dt)
+        ctx.rk4_step(s * dt, dt)
+        ctx.enforce_periodic()
+        return r
+
+    def snapshot():
+        out = ctx.download_resized(ht)
+        return out.conn.copy(), out.stat.copy(), out.pos.copy()
+
+    recs = check_event_trajectory(g, step, snapshot, 1e-10, pass_log=(mode == "passes"))
+    ctx.close()
+    assert sum(recs) == (0 if name.startswith("rings8") else 12)
+
+
+@pytest.mark.parametrize("name,cfg", [("dense_steps.npz", "rw")])
 def test_full_steps_match_reference(golden, name, cfg):
     g = golden(name)
     ht = host_from_arrays(g)

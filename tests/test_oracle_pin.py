@@ -13,7 +13,7 @@ import pytest
 
 from oracle.pyoracle import Checker, reference_available
 from openvort_gb300 import workloads as W
-from tests._util import host_from_arrays, node_rel_err, rel_err, used
+from tests._util import check_event_trajectory, host_from_arrays, node_rel_err, rel_err, used
 
 # Same build flags on the same machine give identical bits; across machines
 # libm's log() may differ in the last place, so cross-machine checks allow a
@@ -26,9 +26,9 @@ def port():
     return Checker("port")
 
 
-def _ref_step(c, t, time, dt):
+def _ref_step(c, t, time, dt, log=False):
     c.eliminate_small_loops(t)
-    n = c.reconnect(t, 0.0)
+    n = c.reconnect(t, 0.0, log=log)
     c.eliminate_small_loops(t)
     c.enforce_periodic(t)
     c.remesh(t, c.params.dl_min, c.params.dl_max, 0.0)
@@ -69,7 +69,32 @@ def test_direct_sum_matches_golden(port, golden):
     assert node_rel_err(vs, g["direct_vs"]) < CROSS_MACHINE_TOL
 
 
-@pytest.mark.parametrize("name,cfg", [("rings8_steps.npz", "rings8"), ("dense_steps.npz", "rw")])
+@pytest.mark.parametrize("name", ["rings8_steps.npz", "crossing_steps.npz"])
+def test_200_steps_event_log_matches_golden(port, golden, name):
+    """The 8-ring configuration (no reconnection in 200 steps) and the
+    crossing ring pairs (12 reconnections in 200 steps): per-step
+    reconnection counts and (k, l) pairs, topology after every event step,
+    positions at the stored steps."""
+    g = golden(name)
+    ht = host_from_arrays(g)
+    p = W.config_params("rings8")
+    p.num_threads = 4
+    port.set_params(p)
+    t = port.tangle(ht)
+    dt = float(g["dt"])
+
+    def step(s):
+        return _ref_step(port, t, s * dt, dt, log=True)
+
+    def snapshot():
+        return t.copy("conn"), t.copy("status"), t.copy("pos")
+
+    recs = check_event_trajectory(g, step, snapshot, CROSS_MACHINE_TOL, pass_log=True)
+    assert sum(recs) == (0 if name.startswith("rings8") else 12)
+    t.free()
+
+
+@pytest.mark.parametrize("name,cfg", [("dense_steps.npz", "rw")])
 def test_steps_match_golden(port, golden, name, cfg):
     g = golden(name)
     ht = host_from_arrays(g)
