@@ -45,7 +45,7 @@ typedef enum ov_status {
     OV_ERR_ARG = 1,      /* bad argument (null pointer, negative size, ...) */
     OV_ERR_CUDA = 2,     /* a CUDA runtime call failed */
     OV_ERR_ALLOC = 3,    /* device or host allocation failed */
-    OV_ERR_DEPTH = 4,    /* two nodes share a cell at the deepest tree level */
+    OV_ERR_DEPTH = 4,    /* two nodes share a cell at the deepest tree level (strict depth policy) */
     OV_ERR_STACK = 5,    /* a traversal exceeded its iteration bound */
     OV_ERR_NAN = 6,      /* a non-finite position or velocity was produced */
     OV_ERR_TIMEOUT = 7,  /* a bounded device wait gave up */
@@ -406,6 +406,17 @@ int ov_phase_times(ov_ctx *ctx, float ms[3]);
    (OV_ERR_STATE before the first evaluation).  A target whose counts differ
    from the reference tree's took a different opening decision. */
 int ov_set_node_counting(ov_ctx *ctx, int on);
+
+/* Nodes closer than the deepest tree cell (21 levels below the root: about
+   D * 5e-7 for one tangle; fewer levels in an ensemble, whose member id takes
+   key bits).  OpenVort's octree keeps splitting there (octree.c:116-160) and
+   never ends for two nodes at one position - which its own smoothing makes:
+   with freq_to_cutoff 0.8, vortex_smooth.c:146-160 keeps only the mean of a
+   closed loop of 6 to 19 nodes, so every node of it lands on one point.
+   Default (strict = 0): the shared deepest cell is one leaf (its nodes'
+   centre of mass and summed circulation) and the call succeeds with
+   OV_EW_DEPTH (1) in ov_stats.error_word.  strict = 1: OV_ERR_DEPTH. */
+int ov_set_depth_policy(ov_ctx *ctx, int strict);
 
 /* Error-path testing: after `after` more successful device or pinned host
    allocations of this context, the next one fails as if the device were out

@@ -220,6 +220,13 @@ int ov_ctx_destroy(ov_ctx *c)
     return OV_OK;
 }
 
+int ov_set_depth_policy(ov_ctx *c, int strict)
+{
+    if (!c) return OV_ERR_ARG;
+    c->strict_depth = strict != 0;
+    return OV_OK;
+}
+
 int ov_inject_alloc_failure(ov_ctx *c, int after)
 {
     if (!c || after < -1) return OV_ERR_ARG;
@@ -535,8 +542,11 @@ int ov_upload_member_tables(ov_ctx *c)
     const int nt = (int)c->mem.size();
     int r;
     if ((r = ov_reserve_members(c, nt))) return r;
+    // member-id bits above each key: ids 0..nt-1 are never all ones (an
+    // all-ones upper half marks an EMPTY slot for the sort's fix-up)
     c->key_tbits = 0;
-    while ((1 << c->key_tbits) < nt) ++c->key_tbits;
+    if (nt > 1)
+        while ((1 << c->key_tbits) <= nt) ++c->key_tbits;
     c->key_levels = std::min(OV_MAX_LEVEL, (63 - c->key_tbits) / 3);
     c->rk4_key = 0;   // the graph bakes the layout in
     std::vector<DevParams> prm(nt);
@@ -873,8 +883,9 @@ static int error_from_word(ov_ctx *c)
         return ov_fail(c, OV_ERR_STATE, "device bounds check failed: code %d index %d (error word 0x%x)",
                        (bad >> 24) & 0x3F, bad & 0xFFFFFF, w);
     }
-    if (w & OV_EW_DEPTH)
-        return ov_fail(c, OV_ERR_DEPTH, "two nodes share a cell at tree level %d (error word 0x%x)", OV_MAX_LEVEL, w);
+    if ((w & OV_EW_DEPTH) && c->strict_depth)
+        return ov_fail(c, OV_ERR_DEPTH, "two nodes share a cell at tree level %d (error word 0x%x)", c->key_levels,
+                       w);
     if (w & OV_EW_TEMP)
         return ov_fail(c, OV_ERR_ARG, "a node's temperature is outside the He II model's range (error word 0x%x)", w);
     if (w & OV_EW_INVERT)

@@ -275,6 +275,8 @@ struct ov_ctx {
     size_t d_stage_bytes = 0;
     // spherical sections: (r, az, pl) bounds of each tree member's root cell
     double sph_lo[OV_SPH_MEMBERS][3] = {}, sph_hi[OV_SPH_MEMBERS][3] = {};
+    // nodes sharing the deepest tree cell: an error (true) or one leaf (ov_set_depth_policy)
+    bool strict_depth = false;
     // allocation failure injection (ov_inject_alloc_failure): the number of
     // device or pinned allocations that still succeed before one fails; -1 off
     int alloc_fail_after = -1;

@@ -1,7 +1,7 @@
 // ov_sort.cu - radix sort of the octree path keys and a device-wide scan.
 //
-// Keys are 64-bit (bit 63 clear for nodes inside the root box); the payload
-// is the node id.  An LSD radix sort with 8-bit digits runs over the upper
+// Keys are 64-bit (member id, out-of-box bit, cell path; EMPTY slots all
+// ones); the payload is the node id.  An LSD radix sort with 8-bit digits runs over the upper
 // 32 bits (4 passes: 10 octree levels and one bit); nodes that still share
 // those bits (the same level-10 cell) are then put in full-key order by an
 // insertion sort per run.  LSD passes are stable, so input (node id) order
@@ -123,13 +123,16 @@ __global__ void rs_scatter(const uint64_t *__restrict__ kin, const int *__restri
 }
 
 // Order each run of equal upper-32-bit keys by the full key (insertion
-// sort, stable).  Runs of out-of-box / EMPTY keys are already in id order.
+// sort, stable): in-box and out-of-box keys of every member.  Only EMPTY
+// slots have all-ones upper bits (the key layout keeps every other key
+// below: member ids are never all ones, out-of-box keys keep the bit under
+// the out-of-box bit clear); their run stays in id order.
 __global__ void rs_fixup(uint64_t *__restrict__ keys, int *__restrict__ vals, int n, int *counters)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t hi = (uint32_t)(keys[i] >> 32);
-    if (hi & 0x80000000u) return;
+    if (hi == 0xFFFFFFFFu) return;
     if (i > 0 && (uint32_t)(keys[i - 1] >> 32) == hi) return;
     int e = i + 1;
     while (e < n && (uint32_t)(keys[e] >> 32) == hi) ++e;

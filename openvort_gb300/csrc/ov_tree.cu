@@ -150,7 +150,7 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
             if (!(v[a] >= g.sb[m][a])) v[a] = g.sb[m][a];   // non-finite input
         }
         const uint64_t path = sph_key(v, g, m);
-        if (!inside) keys[i] = prefix | (1ull << (63 - g.tb)) | (path >> (g.tb + 1));
+        if (!inside) keys[i] = prefix | (1ull << (63 - g.tb)) | (path >> (g.tb + 2));
         else keys[i] = prefix | ((path >> g.tb) & g.lvmask);
         return;
     }
@@ -174,7 +174,9 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
             uint64_t xb = (W[0] >> sh) & 1, yb = (W[1] >> sh) & 1, zb = (W[2] >> sh) & 1;
             k2 |= ((zb << 2) | (yb << 1) | (xb ^ 1)) << (63 - 3 * lev);
         }
-        keys[i] = prefix | (1ull << (63 - g.tb)) | (k2 >> (g.tb + 1));
+        // (the bit below the out-of-box bit stays clear: no key but an
+        // EMPTY slot's has all-ones upper bits)
+        keys[i] = prefix | (1ull << (63 - g.tb)) | (k2 >> (g.tb + 2));
         return;
     }
     uint64_t U[3];
@@ -232,7 +234,7 @@ __device__ __forceinline__ uint64_t inbox_path(const KeyGeom &g, uint64_t k)
 }
 __device__ __forceinline__ uint64_t out_path(const KeyGeom &g, uint64_t k)
 {
-    return (k & ((1ull << (63 - g.tb)) - 1)) << 1;
+    return (k & ((1ull << (63 - g.tb)) - 1)) << 2;
 }
 
 // Traversal order: the in-box nodes in path order merged with the root-only

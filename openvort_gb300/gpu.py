@@ -80,6 +80,7 @@ def load(path: str | None = None):
         "ov_phase_times": (C.c_int, [P, C.POINTER(C.c_float)]),
         "ov_set_node_counting": (C.c_int, [P, C.c_int]),
         "ov_inject_alloc_failure": (C.c_int, [P, C.c_int]),
+        "ov_set_depth_policy": (C.c_int, [P, C.c_int]),
         "ov_get_node_counts": (C.c_int, [P, C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_uint), C.c_int]),
         "ov_measure_fma_peak": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
         "ov_set_rk4_graph": (C.c_int, [P, C.c_int]),
@@ -461,6 +462,11 @@ class Context:
         ms = (C.c_float * 3)()
         self._check(self.lib.ov_phase_times(self._h, ms))
         return list(ms)
+
+    def set_depth_policy(self, strict: bool):
+        """strict: nodes sharing the deepest tree cell raise OV_ERR_DEPTH;
+        otherwise (default) that cell is one leaf and the call succeeds."""
+        self._check(self.lib.ov_set_depth_policy(self._h, int(strict)))
 
     def inject_alloc_failure(self, after: int = 0):
         """The allocation after `after` more successful ones fails (-1: off)."""

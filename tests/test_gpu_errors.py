@@ -7,7 +7,8 @@ status code instead and leaves the caller's tangle as it was:
   * a NaN position                      -> OV_ERR_NAN, host tangle unchanged
   * a forward index out of range        -> OV_ERR_TOPOLOGY at upload, before any launch
   * a forward link onto an EMPTY slot   -> OV_ERR_TOPOLOGY (the filament walk stops)
-  * two nodes at the same position      -> OV_ERR_DEPTH (the reference recurses forever)
+  * two nodes at the same position      -> OV_ERR_DEPTH under the strict depth policy (the
+                                           reference recurses forever); one leaf by default
   * a device allocation that fails      -> OV_ERR_ALLOC; the context frees its buffers, holds
                                            no tangle, and works again after a new upload
 
@@ -103,13 +104,31 @@ def test_forward_link_onto_empty_slot():
     ctx.close()
 
 
-def test_coincident_nodes_report_depth():
+def test_coincident_nodes_report_depth_when_strict():
     ht = _tangle()
     ht.pos[200] = ht.pos[3]             # nodes of two different loops at one point
     ctx = gpu.Context(0, params=W.config_params("rw"))
+    ctx.set_depth_policy(True)
     ctx.upload(ht)
     _expect(OV_ERR_DEPTH, ctx.update_tangle, 0.0)
     ctx.close()
+
+
+def test_coincident_nodes_share_one_leaf_by_default():
+    """Default policy: the deepest shared cell is one leaf.  The two nodes at
+    one point skip each other (d < 1e-8, octree.c:311); every other target
+    sees the leaf's monopole, whose centre of mass is that point."""
+    ht = _tangle()
+    ht.pos[200] = ht.pos[3]
+    ctx = gpu.Context(0, params=W.config_params("rw"))
+    ctx.upload(ht)
+    ctx.update_tangle(0.0)
+    st = ctx.stats()
+    out = ctx.download(ht, abi.OV_F_VELS)
+    ctx.close()
+    assert st["error_word"] & 1            # OV_EW_DEPTH: reported, not fatal
+    assert st["max_depth"] == 21
+    assert np.all(np.isfinite(out.vels))
 
 
 @pytest.mark.parametrize("after", [0, 3, 17, 40])
