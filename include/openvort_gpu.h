@@ -205,7 +205,10 @@ typedef struct ov_tuning {
     int query_groups;
     int blocks_per_sm;
     int largest_first;
-    int high_occupancy;
+    int high_occupancy;   /* mixed traversal variant: 0 the general kernel, 1 the same under a
+                             tighter register budget; 2, 3, 4 the periodic-image kernel with
+                             fewer values held per lane (mirror images: as 0) with the
+                             compiler's register count, 80 and 64 registers */
 } ov_tuning;
 int ov_get_tuning(const ov_ctx *ctx, ov_tuning *out);
 int ov_set_tuning(ov_ctx *ctx, const ov_tuning *tu);

@@ -313,7 +313,7 @@ int ov_set_tuning(ov_ctx *c, const ov_tuning *tu)
     if (!c || !tu) return OV_ERR_ARG;
     if ((tu->warps_per_block != 2 && tu->warps_per_block != 4 && tu->warps_per_block != 8) ||
         tu->query_groups < 0 || tu->query_groups > 27 || tu->blocks_per_sm < 0 || tu->blocks_per_sm > 64 ||
-        (tu->high_occupancy != 0 && tu->high_occupancy != 1))
+        tu->high_occupancy < 0 || tu->high_occupancy > 4)
         return ov_fail(c, OV_ERR_ARG, "tuning out of range");
     c->tune.warps = tu->warps_per_block;
     c->tune.groups = tu->query_groups;
@@ -1124,7 +1124,7 @@ int ov_autotune(ov_ctx *c, double t, ov_tuning *best_out, float *ms_best)
         std::vector<Tuning> cand;
         if (stage == 0)
             for (int w : warps)
-                for (int ho = 0; ho <= (c->precision == OV_PREC_MIXED ? 1 : 0); ++ho) {
+                for (int ho = 0; ho <= (c->precision == OV_PREC_MIXED ? 4 : 0); ++ho) {
                     Tuning tu = best;
                     tu.warps = w;
                     tu.hi_occ = ho;

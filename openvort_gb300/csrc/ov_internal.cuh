@@ -49,13 +49,13 @@ struct Cell64 {          // 64 bytes, one per cell, pre-order
     int count;           // nodes in the cell
 };
 
-struct Cell32 {          // 48 bytes: FP32 view for the mixed traversal
+struct Cell32 {          // 48 bytes: FP32 view for the FP32 walks; a walk step reads the first 32
     float gx, gy, gz;    // COM, grid part (multiple of the grid step h)
+    float thr;           // (Lm / theta)^2 (1 + 2e-5), rounded up: d^2 above it accepts the cell clear of the test's band
     float fx, fy, fz;    // COM, fine part
+    int next;            // first cell after the subtree
     float qx, qy, qz;    // circulation
     float lm;            // Lm (rounded up)
-    int next;
-    int count;
 };
 
 struct CellFF {           // 64 bytes: double-single view for OV_PREC_DD

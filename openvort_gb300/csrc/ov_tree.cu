@@ -579,8 +579,11 @@ __global__ void k_cellsff(const Cell64 *__restrict__ cells, const int *counters,
 
 // FP32 copy of every cell for the mixed traversal: COM split into a part on
 // the grid of step h (exact in FP32) and a small remainder.
+// The opening test Lm / d < theta becomes d^2 > (Lm / theta)^2: thr holds
+// that bound times (1 + 2e-5), rounded up, so that d^2 > thr accepts clear
+// of the guard band and d^2 < thr (1 - 2e-5) / (1 + 2e-5) opens clear of it.
 __global__ void k_cells32(const Cell64 *__restrict__ cells, const int *counters, double h, double inv_h,
-                          Cell32 *__restrict__ out)
+                          double theta, Cell32 *__restrict__ out)
 {
     int ci = blockIdx.x * blockDim.x + threadIdx.x;
     if (ci >= counters[TC_NCELL]) return;
@@ -589,11 +592,12 @@ __global__ void k_cells32(const Cell64 *__restrict__ cells, const int *counters,
     double cx = c.cx, cy = c.cy, cz = c.cz;
     double gx = rint(cx * inv_h) * h, gy = rint(cy * inv_h) * h, gz = rint(cz * inv_h) * h;
     o.gx = (float)gx; o.gy = (float)gy; o.gz = (float)gz;
+    const double r = c.lm / theta;
+    o.thr = theta > 0 ? __double2float_ru(r * r * (1.0 + 2e-5)) : __int_as_float(0x7f800000);
     o.fx = (float)(cx - gx); o.fy = (float)(cy - gy); o.fz = (float)(cz - gz);
+    o.next = c.next;
     o.qx = (float)c.qx; o.qy = (float)c.qy; o.qz = (float)c.qz;
     o.lm = __double2float_ru(c.lm);
-    o.next = c.next;
-    o.count = c.count;
     out[ci] = o;
 }
 
@@ -727,7 +731,7 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     c->launches += 3;
     if (c->precision == OV_PREC_MIXED || c->precision == OV_PREC_DD || c->walk == OV_WALK_SPLIT) {
         k_cells32<<<(t.cap_cells + 255) / 256, 256, 0, s>>>(t.cells, t.counters, c->grid_h, 1.0 / c->grid_h,
-                                                           t.cells32);
+                                                           c->params.bh_resolution, t.cells32);
         c->launches++;
     }
     if (c->precision == OV_PREC_DD) {

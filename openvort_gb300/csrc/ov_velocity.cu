@@ -751,6 +751,8 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
 }
 
 constexpr int kNearCap = 24;   // deferred near-field leaves per lane
+// d^2 below Cell32::thr times this opens a cell clear of the guard band
+constexpr float kThrLo = (1.0f - 2e-5f) / (1.0f + 2e-5f);
 
 // ------------------------------------------------ double-single arithmetic
 // A value as an unevaluated sum hi + lo of two floats (about 48 bits):
@@ -908,7 +910,6 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
 // DD: accepted interactions in double-single at the query point qff, summed
 // into (m.s, m.c) as (hi, lo) pairs; the near field needs no FP64 then.
 {
-    const float th2 = a.th2f;
     const float near2 = a.near2f;
     const float f4pi = a.f4pif;
     const float d2lo = 1e-16f * (1.0f - 1e-5f), d2hi = 1e-16f * (1.0f + 1e-5f);
@@ -922,22 +923,21 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
     while (c < ncell) {
         const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
         float4 A = __ldg(cp4), B = __ldg(cp4 + 1), Cc = __ldg(cp4 + 2);
-        // A = (gx, gy, gz, fx)  B = (fy, fz, qx, qy)  Cc = (qz, lm, next, count)
-        int nxt = __float_as_int(Cc.z);
+        // A = (gx, gy, gz, thr)  B = (fx, fy, fz, next)  Cc = (qx, qy, qz, lm)
+        int nxt = __float_as_int(B.w);
         if ((unsigned)(nxt - c - 1) >= (unsigned)(ncell - c)) { bad_index(a, 2, c); nxt = ncell; }
         bool open = false;
         if (c >= resume) {
             ++m.nvis;
-            const float dx = (g[0] - A.x) + (f[0] - A.w);
-            const float dy = (g[1] - A.y) + (f[1] - B.x);
-            const float dz = (g[2] - A.z) + (f[2] - B.y);
+            const float dx = (g[0] - A.x) + (f[0] - B.x);
+            const float dy = (g[1] - A.y) + (f[1] - B.y);
+            const float dz = (g[2] - A.z) + (f[2] - B.z);
             const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             const bool leaf = (nxt == c + 1);
-            const float lm2 = Cc.y * Cc.y, b = th2 * d2;
             // decisions taken in FP32 only when clear of their thresholds
             bool skip = d2 < d2lo;
-            bool acc = !skip && (leaf || lm2 < b * (1.0f - 2e-5f));
-            bool opn = !skip && !leaf && lm2 > b * (1.0f + 2e-5f);
+            bool acc = !skip && (leaf || d2 > A.w);
+            bool opn = !skip && !leaf && d2 < A.w * kThrLo;
             bool exact = (!skip && d2 <= d2hi) || (!skip && !acc && !opn);
             if (exact) {
                 // rare: inside a guard band, decided exactly as the FP64 path
@@ -952,7 +952,7 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
             if (acc) {
                 ++m.nacc;
                 const float R0 = -dx, R1 = -dy, R2 = -dz;
-                const float qx = B.z, qy = B.w, qz = Cc.x;
+                const float qx = Cc.x, qy = Cc.y, qz = Cc.z;
                 const float P0 = R0 + qx, P1 = R1 + qy, P2 = R2 + qz;
                 const float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
                 const float dot = fmaf(R0, P0, fmaf(R1, P1, R2 * P2));
@@ -1158,6 +1158,240 @@ __global__ void __launch_bounds__(32 * W, (min_blocks_mixed<W, HI>())) k_vel_mix
     }
 }
 
+// --------------------------------------- mixed precision, periodic images
+// k_vel_mixed for periodic image sets, with fewer values held per lane: no
+// mirror-image sums, the node's FP64 position re-read in the rare FP64
+// paths instead of kept, those paths out of line, and the circulation of a
+// cell read only when some lane accepts it.  Same decisions, arithmetic and
+// summation order as k_vel_mixed; the register budget is a template
+// parameter (more resident warps against spills), picked by the autotuner.
+
+// (the rare paths are kept out of line: their FP64 temporaries would
+// otherwise raise the register count of the walk loop)
+__device__ __noinline__ void mixp_term64(const VelArgs &a, int c, int j, int id, double w64[3])
+{
+    double p[3] = {a.x[id], a.y[id], a.z[id]}, q[3], dxyz[3], d64, w[3];
+    if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+    else image_point(a.geo, j, p, q);
+    decide64(a.cells + c, q, a.prm.theta, true, dxyz, &d64);
+    if (interact64(a.cells + c, dxyz, d64, a.f4pi, w)) {
+        w64[0] += w[0]; w64[1] += w[1]; w64[2] += w[2];
+    }
+}
+
+// The FP64 path's decision for cell c at node id's query point j: 1 skip,
+// 2 accept, 0 open.
+__device__ __noinline__ int mixp_decide64(const VelArgs &a, int c, int j, int id, bool leaf)
+{
+    double p[3] = {a.x[id], a.y[id], a.z[id]}, q[3], dxyz[3], d64;
+    if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+    else image_point(a.geo, j, p, q);
+    return decide64(a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
+}
+
+// An accepted cell whose term needs FP64 (near field, a decision or filter
+// taken in FP64): deferred to after the walk, or evaluated now when the
+// lane's deferred list is full.
+__device__ __forceinline__ void mixp_defer(const VelArgs &a, MixedAcc &m, int *near_list, int &nnear, int c, int j,
+                                           int id, double w64[3])
+{
+    ++m.nnear;
+    if (nnear < kNearCap) {
+        near_list[32 * nnear] = (c << 5) | (j + 1);
+        ++nnear;
+        return;
+    }
+    mixp_term64(a, c, j, id, w64);
+}
+
+// One periodic query point (g + f split; image j, j < 0 the node itself) for
+// the 32 lanes of a warp.
+__device__ __forceinline__ void walk_mixp(const VelArgs &a, const float g[3], const float f[3], int id, int j,
+                                          bool part, int root, int ncell, MixedAcc &m, int *near_list, int &nnear,
+                                          double w64[3], bool &overflow)
+{
+    const float near2 = a.near2f;
+    const float f4pi = a.f4pif;
+    const float d2lo = 1e-16f * (1.0f - 1e-5f), d2hi = 1e-16f * (1.0f + 1e-5f);
+    int c = root;
+    int resume = part ? 0 : 0x7fffffff;
+    const int guard_max = 4 * (ncell - root) + 64;
+    int steps = 0;
+    // plain FP32 sub-sums, folded into the Kahan sums every 16 warp steps
+    float p0 = 0, p1 = 0, p2 = 0;
+    // c only grows (nxt > c is checked), so it stays within [root, ncell)
+    while (c < ncell) {
+        const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
+        const float4 A = __ldg(cp4), B = __ldg(cp4 + 1);
+        // A = (gx, gy, gz, thr)  B = (fx, fy, fz, next)
+        int nxt = __float_as_int(B.w);
+        if ((unsigned)(nxt - c - 1) >= (unsigned)(ncell - c)) { bad_index(a, 2, c); nxt = ncell; }
+        bool open = false;
+        if (c >= resume) {
+            ++m.nvis;
+            const float dx = (g[0] - A.x) + (f[0] - B.x);
+            const float dy = (g[1] - A.y) + (f[1] - B.y);
+            const float dz = (g[2] - A.z) + (f[2] - B.z);
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const bool leaf = (nxt == c + 1);
+            // decisions in FP32 clear of their thresholds, else as the FP64 path
+            bool skip = d2 < d2lo;
+            bool acc = !skip && (leaf || d2 > A.w);
+            bool opn = !skip && !leaf && d2 < A.w * kThrLo;
+            const bool exact = (!skip && d2 <= d2hi) || (!skip && !acc && !opn);
+            if (exact) {
+                ++m.nfb;
+                const int dec = mixp_decide64(a, c, j, id, leaf);
+                skip = dec == 1;
+                acc = dec == 2;
+            }
+            if (acc) {
+                ++m.nacc;
+                if (exact || (leaf && d2 < near2)) {
+                    mixp_defer(a, m, near_list, nnear, c, j, id, w64);
+                } else {
+                    const float4 Q = __ldg(cp4 + 2);   // (qx, qy, qz, lm)
+                    const float R0 = -dx, R1 = -dy, R2 = -dz;
+                    const float P0 = R0 + Q.x, P1 = R1 + Q.y, P2 = R2 + Q.z;
+                    const float lp2 = fmaf(P0, P0, fmaf(P1, P1, P2 * P2));
+                    const float dot = fmaf(R0, P0, fmaf(R1, P1, R2 * P2));
+                    const float ra = rsqrtf(d2), rb = rsqrtf(lp2);
+                    const float ab = ra * rb;
+                    const float nd = dot * ab;
+                    if (lp2 < d2hi || !(nd > 1e-8f + 4e-6f)) {
+                        // a filter near its threshold: FP64; clearly below ndot's: dropped
+                        if (lp2 < d2hi || fabsf(nd - 1e-8f) < 4e-6f) mixp_defer(a, m, near_list, nnear, c, j, id, w64);
+                    } else {
+                        const float sc = __fdividef(f4pi * (ra + rb) * ab, fmaf(dot, ab, 1.0f));
+                        // R x Rp1 = R x q
+                        p0 = fmaf(fmaf(R1, Q.z, -R2 * Q.y), sc, p0);
+                        p1 = fmaf(fmaf(R2, Q.x, -R0 * Q.z), sc, p1);
+                        p2 = fmaf(fmaf(R0, Q.y, -R1 * Q.x), sc, p2);
+                    }
+                }
+                resume = nxt;
+            } else if (skip) {
+                resume = nxt;
+            } else {
+                open = true;
+            }
+        }
+        ++steps;
+        if ((steps & 15) == 0) {   // warp-uniform
+            kahan_add(m.s0, m.c0, p0);
+            kahan_add(m.s1, m.c1, p1);
+            kahan_add(m.s2, m.c2, p2);
+            p0 = p1 = p2 = 0;
+            if (steps > guard_max) { overflow = true; break; }
+        }
+        c = __any_sync(0xffffffffu, open) ? c + 1 : nxt;
+    }
+    kahan_add(m.s0, m.c0, p0);
+    kahan_add(m.s1, m.c1, p1);
+    kahan_add(m.s2, m.c2, p2);
+    m.nstep += steps;
+}
+
+// register budget: R = 0 the compiler's choice, else R registers a thread
+template <int W, int R> constexpr int min_blocks_mixp() { return R == 0 ? 1 : 65536 / (32 * W * R); }
+
+template <int W, int R>
+__global__ void __launch_bounds__(32 * W, (min_blocks_mixp<W, R>())) k_vel_mixp(VelArgs a,
+                                                                              double *__restrict__ part_out)
+{
+    const int lane = threadIdx.x & 31;
+    const int tiles = a.counters[TC_ITEMS];
+    const int items = tiles * a.G;
+    __shared__ int s_near[W][kNearCap * 32];   // per warp: [entry][lane]
+    int *near_list = &s_near[threadIdx.x >> 5][lane];
+    unsigned visits = 0, accepts = 0, steps = 0, fallback = 0, near64 = 0;   // per lane
+    bool overflow = false;
+    for (int it = next_item(a); it < items; it = next_item(a)) {
+        const WorkItem w = decode_item(a, it, tiles);
+        const int loc = 32 * w.tile + lane;
+        const int tix = w.st + loc;
+        bool valid = loc < w.nne && tix < a.cap;
+        int id = valid ? a.order[tix] : 0;
+        if (valid && (id < 0 || id >= a.cap)) { bad_index(a, 4, id); valid = false; id = 0; }
+        const int st = valid ? a.status[id] : OV_EMPTY;
+        const bool part = valid && st != OV_PINNED && st != OV_EMPTY && a.prm.use_bh;
+        float g0[3], f0[3];
+        {
+            double p[3] = {0, 0, 0};
+            if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                const double G = rint(p[ax] * a.inv_h) * a.grid_h;
+                g0[ax] = (float)G;
+                f0[ax] = (float)(p[ax] - G);
+            }
+        }
+        MixedAcc m = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
+        double w64[3] = {0, 0, 0};        // FP64 terms: near field and deferred-list overflow
+        int nnear = 0;
+        for (int qi = w.grp; qi <= a.geo.n_img; qi += a.G) {
+            const int j = qi - 1;
+            float g[3], f[3];
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                // image query p - L*shift: grid parts subtract exactly
+                g[ax] = j < 0 ? g0[ax] : g0[ax] - a.shift_g[j][ax];
+                f[ax] = j < 0 ? f0[ax] : f0[ax] - a.shift_f[j][ax];
+            }
+            walk_mixp(a, g, f, id, j, part, w.root, w.end, m, near_list, nnear, w64, overflow);
+        }
+        // deferred FP64 terms, all lanes together
+        {
+            double p[3] = {0, 0, 0};
+            if (valid) { p[0] = a.x[id]; p[1] = a.y[id]; p[2] = a.z[id]; }
+            for (int i = 0; i < nnear && i < kNearCap; ++i) {
+                const int e = near_list[32 * i];
+                const int c = e >> 5, j = (e & 31) - 1;
+                if (c < w.root || c >= w.end || j < -1 || j >= a.geo.n_img) { bad_index(a, 3, e); continue; }
+                double q[3], wv[3];
+                if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+                else image_point(a.geo, j, p, q);
+                law64_term(a.cells + c, q, wv);   // zero when a filter drops it
+                w64[0] += wv[0] * a.f4pi; w64[1] += wv[1] * a.f4pi; w64[2] += wv[2] * a.f4pi;
+            }
+        }
+        __syncwarp();   // the list is rewritten by the next item
+        if (valid) {
+            const size_t cap = (size_t)a.cap;
+            const double bh[3] = {acc_value(m.s0, m.c0, false) + w64[0], acc_value(m.s1, m.c1, false) + w64[1],
+                                  acc_value(m.s2, m.c2, false) + w64[2]};
+            for (int ax = 0; ax < 3; ++ax) {
+                part_out[((size_t)(2 * w.grp) * 3 + ax) * cap + tix] = bh[ax];
+                part_out[((size_t)(2 * w.grp + 1) * 3 + ax) * cap + tix] = 0.0;
+            }
+        }
+        count_node(a, valid, id, m.nvis, m.nacc);
+        visits += m.nvis;
+        accepts += m.nacc;
+        steps += m.nstep;
+        fallback += m.nfb;
+        near64 += m.nnear;
+    }
+    int err = overflow ? OV_EW_ITER : 0;
+    unsigned long long v64 = visits, a64 = accepts, f64 = fallback, n64 = near64;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v64 += __shfl_xor_sync(0xffffffffu, v64, o);
+        a64 += __shfl_xor_sync(0xffffffffu, a64, o);
+        f64 += __shfl_xor_sync(0xffffffffu, f64, o);
+        n64 += __shfl_xor_sync(0xffffffffu, n64, o);
+        err |= __shfl_xor_sync(0xffffffffu, err, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&a.stat[ST_VISITS], v64);
+        atomicAdd(&a.stat[ST_ACCEPTS], a64);
+        atomicAdd(&a.stat[ST_STEPS], (unsigned long long)steps);
+        atomicAdd(&a.stat[ST_FALLBACK], f64);
+        atomicAdd(&a.stat[ST_NEAR64], n64);
+        if (err) atomicOr((int *)&a.counters[TC_ERR], err);
+    }
+}
+
 // ------------------------------------------- FP64 path, split walk (default)
 // The walk (distance and opening tests) runs in FP32 on the grid-split cells
 // exactly as the mixed traversal's, with the FP64 test inside the guard
@@ -1235,7 +1469,6 @@ __device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], c
                                            bool part, int root, int ncell, WarpLists &L, int lane, double v[3],
                                            MixedAcc &m, bool &overflow)
 {
-    const float th2 = a.th2f;
     const float d2lo = 1e-16f * (1.0f - 1e-5f), d2hi = 1e-16f * (1.0f + 1e-5f);
     v[0] = v[1] = v[2] = 0;
     int c = root;
@@ -1245,23 +1478,22 @@ __device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], c
     while (c < ncell) {
         if (c < root) { bad_index(a, 1, c); break; }
         const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
-        const float4 A = __ldg(cp4), B = __ldg(cp4 + 1), Cc = __ldg(cp4 + 2);
-        // A = (gx, gy, gz, fx)  B = (fy, fz, qx, qy)  Cc = (qz, lm, next, count)
-        int nxt = __float_as_int(Cc.z);
+        const float4 A = __ldg(cp4), B = __ldg(cp4 + 1);
+        // A = (gx, gy, gz, thr)  B = (fx, fy, fz, next)
+        int nxt = __float_as_int(B.w);
         if (nxt <= c || nxt > ncell) { bad_index(a, 2, c); nxt = ncell; }
         bool open = false;
         if (c >= resume) {
             ++m.nvis;
-            const float dx = (g[0] - A.x) + (f[0] - A.w);
-            const float dy = (g[1] - A.y) + (f[1] - B.x);
-            const float dz = (g[2] - A.z) + (f[2] - B.y);
+            const float dx = (g[0] - A.x) + (f[0] - B.x);
+            const float dy = (g[1] - A.y) + (f[1] - B.y);
+            const float dz = (g[2] - A.z) + (f[2] - B.z);
             const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             const bool leaf = (nxt == c + 1);
-            const float lm2 = Cc.y * Cc.y, b = th2 * d2;
             // the mixed traversal's tests and guard bands
             bool skip = d2 < d2lo;
-            bool acc = !skip && (leaf || lm2 < b * (1.0f - 2e-5f));
-            const bool opn = !skip && !leaf && lm2 > b * (1.0f + 2e-5f);
+            bool acc = !skip && (leaf || d2 > A.w);
+            const bool opn = !skip && !leaf && d2 < A.w * kThrLo;
             if ((!skip && d2 <= d2hi) || (!skip && !acc && !opn)) {
                 ++m.nfb;
                 double dxyz[3], d64;
@@ -1484,9 +1716,28 @@ int ov_reserve_velocity_scratch(ov_ctx *c)
 
 // Traversal kernel for a precision and block shape.
 typedef void (*VelKernel)(VelArgs, double *);
-static VelKernel vel_kernel(int precision, int walk, int warps, int hi_occ)
+static bool has_mirror_images(const Geometry &g)
+{
+    for (int j = 0; j < g.n_img; ++j)
+        if (g.nreflect[j] > 0) return true;
+    return false;
+}
+
+// variant (Tuning::hi_occ) of the mixed traversal: 0 k_vel_mixed, 1 the
+// same under a tighter register budget, 2-4 k_vel_mixp (periodic image sets
+// only) with the compiler's register count, 80 and 64 registers
+template <int R> static VelKernel mixp_kernel(int warps)
+{
+    if (warps == 2) return k_vel_mixp<2, R>;
+    if (warps == 8) return k_vel_mixp<8, R>;
+    return k_vel_mixp<4, R>;
+}
+
+static VelKernel vel_kernel(int precision, int walk, int warps, int hi_occ, bool mirror)
 {
     if (precision == OV_PREC_MIXED) {
+        if (hi_occ >= 2 && !mirror) return hi_occ == 2 ? mixp_kernel<0>(warps)
+                                         : (hi_occ == 3 ? mixp_kernel<80>(warps) : mixp_kernel<64>(warps));
         if (hi_occ) {
             if (warps == 2) return k_vel_mixed<2, 1, false>;
             if (warps == 8) return k_vel_mixed<8, 1, false>;
@@ -1515,7 +1766,7 @@ static VelKernel vel_kernel(int precision, int walk, int warps, int hi_occ)
 // every SM, but no more blocks than there can be work items.
 int ov_traversal_blocks(ov_ctx *c, int precision, int warps, int *per_sm)
 {
-    VelKernel k = vel_kernel(precision, c->walk, warps, c->tune.hi_occ);
+    VelKernel k = vel_kernel(precision, c->walk, warps, c->tune.hi_occ, has_mirror_images(c->geo));
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * warps, 0) != cudaSuccess || occ < 1) {
         cudaGetLastError();
@@ -1555,7 +1806,8 @@ int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precisio
         a.node_counts = c->d_node_counts;
     }
     OV_CUDA(c, cudaMemsetAsync(a.work, 0, sizeof(int), s));
-    vel_kernel(precision, c->walk, warps, c->tune.hi_occ)<<<blocks, 32 * warps, 0, s>>>(a, c->part);
+    vel_kernel(precision, c->walk, warps, c->tune.hi_occ, has_mirror_images(c->geo))<<<blocks, 32 * warps, 0, s>>>(
+        a, c->part);
     k_vel_finish<<<(c->cap + 127) / 128, 128, 0, s>>>(a, c->part);
     c->launches += 2;
     return OV_OK;

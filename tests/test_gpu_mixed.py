@@ -79,3 +79,26 @@ def test_double_single_vs_fp64_tree(n_loops, theta, images):
     assert per_node.max() < 1e-10
     assert rel_l2(vdd, v64) < 1e-12
     assert rel_l2(sdd, s64) < 1e-12
+
+
+def test_mixed_kernel_variants_agree():
+    """The periodic-image mixed kernel (variants 2-4, three register budgets)
+    takes the decisions and sums of the general one (variants 0, 1) bit for
+    bit: same arithmetic, same summation order."""
+    ht = W.random_walk_tangle(64, 256, D=0.1, seed=4)
+    p = W.config_params("rw")
+    ctx = gpu.Context(0, params=p, precision=abi.OV_PREC_MIXED)
+    ctx.upload(ht)
+    out = []
+    for ho in range(5):
+        for warps in (4, 8):
+            ctx.set_tuning(warps_per_block=warps, high_occupancy=ho)
+            ctx.update_tangle(0.0)
+            st = ctx.stats()
+            assert st["error_word"] == 0
+            out.append((ho, warps, st["accepts"], st["visits"], np.array(ctx.download(ht, abi.OV_F_VELS).vels)))
+    ctx.close()
+    _, _, acc0, vis0, v0 = out[0]
+    for ho, warps, acc, vis, v in out[1:]:
+        assert acc == acc0 and vis == vis0, (ho, warps)
+        np.testing.assert_array_equal(v, v0, err_msg=f"variant {ho}, {warps} warps")
