@@ -225,3 +225,30 @@ def test_rk4_graph_equals_stream_launches(prec):
         ctx.close()
         outs.append(np.array(ht.pos))
     np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("time", [0.0, 3e-5, 1e-4, 2.5e-4])
+def test_decreasing_flow_vs_oracle(port, time):
+    """v_n and v_s DECREASING (external_velocity.c:39-56; ramps over 1e-4 s):
+    update_tangle and an RK4 step whose stage times straddle the ramp's end,
+    against the oracle (itself bit-identical to OpenVort on these cases)."""
+    from tests.test_oracle_pin import _decreasing_params
+    ht = W.random_walk_tangle(8, 48, D=0.1, seed=19)
+    p = _decreasing_params()
+    p.num_threads = 4
+    ctx = gpu.Context(0, params=p)
+    ctx.upload(ht)
+    ctx.update_tangle(time)
+    v1 = np.array(ctx.download(ht, abi.OV_F_VELS | abi.OV_F_VS).vels)
+    s1 = np.array(ht.vs)
+    ctx.rk4_step(time, 5e-5)
+    pos = np.array(ctx.download(ht, abi.OV_F_POS).pos)
+    ctx.close()
+    port.set_params(p)
+    t = port.tangle(W.random_walk_tangle(8, 48, D=0.1, seed=19))
+    port.update_tangle(t, time)
+    assert node_rel_err(v1, t.copy("vels")) < FP64_TOL
+    assert node_rel_err(s1, t.copy("vs")) < FP64_TOL
+    port.rk4_step(t, time, 5e-5)
+    assert rel_err(pos, t.copy("pos")) < FP64_TOL
+    t.free()

@@ -235,3 +235,36 @@ def test_wall_configurations_match_golden(port, golden, name):
     dv, _ = port.direct_velocities(t, g["direct_nodes"], 0.0)
     assert node_rel_err(dv, g[f"{name}_direct_vels"]) < 1e-12
     t.free()
+
+
+def _decreasing_params():
+    """v_n and v_s both DECREASING (external_velocity.c:39-56): linear ramps
+    from a starting strength to the final one over 1e-4 s."""
+    from openvort_gb300 import abi
+    p = W.config_params("rw")
+    for flow, (s0, s1, d) in ((p.vn, (1.0, 0.2, (1.0, 0.5, 0.0))), (p.vs, (-0.3, 0.1, (0.0, 1.0, 2.0)))):
+        flow.type = abi.OV_DECREASING
+        flow.starting_strength = s0
+        flow.strength = s1
+        flow.time_of_linear_decrease = 1e-4
+        flow.direction.p[:] = d
+    return p
+
+
+@pytest.mark.skipif(not reference_available(), reason="OpenVort checkout not built here")
+@pytest.mark.parametrize("time", [0.0, 3e-5, 1e-4, 2.5e-4])
+def test_decreasing_flow_bit_identical_to_live_reference(time):
+    ht = W.random_walk_tangle(8, 48, D=0.1, seed=19)
+    p = _decreasing_params()
+    p.num_threads = 4
+    out = {}
+    for kind in ("port", "reference"):
+        c = Checker(kind)
+        c.set_params(p)
+        t = c.tangle(ht)
+        c.update_tangle(t, time)
+        c.rk4_step(t, time, 5e-5)
+        out[kind] = (t.copy("vels"), t.copy("vs"), t.copy("pos"))
+        t.free()
+    for a, b in zip(out["port"], out["reference"]):
+        np.testing.assert_array_equal(a, b)
