@@ -500,6 +500,8 @@ def run_config_a(args, device=0):
         p = W.config_params("rings8")
         ctx = gpu.Context(device, params=p, precision=abi.OV_PREC_FP64)
         ctx.upload(ht)
+        tune, _ = ctx.autotune(0.0)              # launch shape for this size (query groups, block shape)
+        ctx.upload(ht)
         for w in range(3):                       # warm-up on a copy of the run (graph capture, buffers)
             ctx.step(w * A["dt"], A["dt"])
         ctx.upload(ht)
@@ -512,7 +514,7 @@ def run_config_a(args, device=0):
         ctx.synchronize()
         g_s = time.perf_counter() - t0
         ctx.close()
-        sec = {"nodes": ht.n, "steps": A["steps"], "reconnections": recs,
+        sec = {"nodes": ht.n, "steps": A["steps"], "reconnections": recs, "tuning": tune,
                "gpu": {"steps_per_s": A["steps"] / g_s, "ms_per_step": g_s * 1e3 / A["steps"],
                        "timing": "host wall clock around the 200 ov_step calls"}}
         if args.cpu_sections:

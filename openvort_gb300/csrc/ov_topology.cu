@@ -2279,18 +2279,24 @@ int ov_smooth(ov_ctx *c)
         for (int i = lo; i < h.hi; ++i) {
             if (seen[i - lo]) continue;
             if (h.st(i) == OV_EMPTY) { seen[i - lo] = 1; continue; }
-            int j = i, guard = 0;
-            while (h.rev(j) != i && h.rev(j) != -1 && guard++ <= N) j = h.rev(j);
-            if (h.rev(j) == -1 || guard > N) { seen[i - lo] = 1; continue; }   // open line: not smoothed
+            // one forward walk from i: back at i closes a loop (none of whose
+            // nodes can have been seen); the end of an open line, or a node a
+            // walk along the same line already passed, leaves it unsmoothed
             int len = 0;
             int m = i;
+            bool closed = false;
             const size_t start = nodes.size();
-            do {
+            while (m >= lo && m < h.hi && !seen[m - lo] && len <= N) {
+                seen[m - lo] = 1;
                 nodes.push_back(m);
-                if (m >= lo && m < h.hi) seen[m - lo] = 1;
-                m = h.fwd(m);
                 ++len;
-            } while (m != i && m >= 0 && len <= N);
+                m = h.fwd(m);
+                if (m == i) { closed = true; break; }
+            }
+            if (!closed) {   // open line: not smoothed
+                nodes.resize(start);
+                continue;
+            }
             if (len > kLongLoop) {
                 // long loop: the FFT path, after the short ones
                 long_off.push_back((int)long_nodes.size());
