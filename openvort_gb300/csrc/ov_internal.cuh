@@ -95,6 +95,7 @@ struct TreeBuf {
     int *nchild = nullptr;
     int *arrive = nullptr;
     double *csum = nullptr;      // 6 doubles per cell: position sum, circulation sum
+    int *first = nullptr;        // first sorted position of each cell's nodes
     int *counters = nullptr;     // device scalars, see TreeCounters
 };
 

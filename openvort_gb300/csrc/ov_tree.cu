@@ -43,6 +43,7 @@ struct KeyGeom {
     // spherical sections: per member (r, az, pl) bounds of the root cell
     double sb[OV_SPH_MEMBERS][3], st[OV_SPH_MEMBERS][3];
     int sph_root;      // the root cells' Lm from those bounds
+    double root_lm;    // Lm of the (box) root cell
 };
 
 // bit offset of the level-`lev` digit
@@ -348,7 +349,7 @@ template <bool SPH>
 __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict__ cpl,
                         const int *__restrict__ cell_off, int *counters, const int *__restrict__ tt, KeyGeom g,
                         int cap, Cell64 *__restrict__ cells, int *__restrict__ parent, int *__restrict__ nchild,
-                        int *__restrict__ arrive, int cap_cells)
+                        int *__restrict__ arrive, int *__restrict__ first, int cap_cells)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     int nne_all = counters[TC_NNE];
@@ -372,34 +373,38 @@ __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict
     int cn = loc + 1 < M ? cpl[s] : 0;
     int L = min(max(cp, cn) + 1, g.levels);
     const int base = cell_off[s] + (loc == 0);
-    // exact box of the first cell starting here, walked from the root
+    // Box cells: Lm is the root's scaled by 2^-lev, within a few ulps of the
+    // reference's rounded child boxes (octree.c:165-232); the traversals'
+    // opening tests take it outside a 1e-12 band and walk the exact box
+    // (cell_lm_exact) inside it.  Spherical cells: the exact box, walked from
+    // the root (their Lm is not a scaled copy).
     double b[3], t[3];
     const int mem = key_member(g, key) < OV_SPH_MEMBERS ? key_member(g, key) : 0;
-    for (int a = 0; a < 3; ++a) {
-        b[a] = SPH ? g.sb[mem][a] : g.lo[a];
-        t[a] = SPH ? g.st[mem][a] : g.hi[a];
-    }
-    for (int lev = 1; lev <= cp; ++lev) {
-        double cb[3], ct[3];
-        if (SPH) sph_child_box(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
-        else child_box_dev(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
-        for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
+    if (SPH) {
+        for (int a = 0; a < 3; ++a) { b[a] = g.sb[mem][a]; t[a] = g.st[mem][a]; }
+        for (int lev = 1; lev <= cp; ++lev) {
+            double cb[3], ct[3];
+            sph_child_box(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
+            for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
+        }
     }
     for (int lev = cp + 1; lev <= L; ++lev) {
         int ci = base + (lev - cp - 1);
-        double cb[3], ct[3];
-        if (SPH) sph_child_box(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
-        else child_box_dev(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
-        for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
+        if (SPH) {
+            double cb[3], ct[3];
+            sph_child_box(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
+            for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
+        }
         int sh = dsh(g, lev);
         int e = (lev < L) ? upper_prefix(keys, s + 1, end, sh, key >> sh) - 1 : s;
         if (lev == g.levels) e = upper_prefix(keys, s + 1, end, sh, key >> sh) - 1;
         Cell64 cell;
-        cell.lm = SPH ? sph_box_lm(b, t) : box_lm(b, t);
+        cell.lm = SPH ? sph_box_lm(b, t) : ldexp(g.root_lm, -lev);
         cell.count = e - s + 1;
         cell.next = cell_off[e + 1];   // the member's end of cells when e + 1 == end
         cell.cx = cell.cy = cell.cz = cell.qx = cell.qy = cell.qz = 0;
         cells[ci] = cell;
+        first[ci] = s;
         int par;
         if (lev == 1) par = root;
         else if (cp < lev - 1) par = ci - 1;
@@ -506,7 +511,7 @@ __global__ void k_moments(const uint64_t *__restrict__ keys, const int *__restri
 __global__ void k_root(const int *__restrict__ order, const int *__restrict__ cell_off, int *counters,
                        int *tt, const double *__restrict__ x, const double *__restrict__ y,
                        const double *__restrict__ z, const int *__restrict__ fwd, Geometry geo, KeyGeom g,
-                       Cell64 *cells, const double *csum, int cap_cells)
+                       Cell64 *cells, const double *csum, int *first, int cap_cells)
 {
     __shared__ double red[6][256];
     int *w = tt + blockIdx.x * TT_WORDS;
@@ -551,6 +556,7 @@ __global__ void k_root(const int *__restrict__ order, const int *__restrict__ ce
     r.next = end;
     r.count = nne;
     cells[root] = r;
+    first[root] = st;
 }
 
 // Double-single copy of every cell's centre of mass and circulation for
@@ -607,17 +613,21 @@ int ov_tree_reserve_cells(ov_ctx *c, int cells)
 {
     TreeBuf &t = c->tree;
     if (t.cap_cells >= cells && t.cells) return OV_OK;
-    void *ptrs[] = {t.cells, t.cells32, t.cellsff, t.parent, t.nchild, t.arrive, t.csum};
+    void *ptrs[] = {t.cells, t.cells32, t.cellsff, t.parent, t.nchild, t.arrive, t.csum, t.first};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    t.cells = nullptr; t.cells32 = nullptr; t.cellsff = nullptr; t.parent = t.nchild = t.arrive = t.first = nullptr;
+    t.csum = nullptr;
+    t.cap_cells = 0;
+    OV_ALLOC(c, cudaMalloc(&t.cells, (size_t)cells * sizeof(Cell64)));
+    OV_ALLOC(c, cudaMalloc(&t.cells32, (size_t)cells * sizeof(Cell32)));
+    OV_ALLOC(c, cudaMalloc(&t.cellsff, (size_t)cells * sizeof(CellFF)));
+    OV_ALLOC(c, cudaMalloc(&t.parent, (size_t)cells * 4));
+    OV_ALLOC(c, cudaMalloc(&t.nchild, (size_t)cells * 4));
+    OV_ALLOC(c, cudaMalloc(&t.arrive, (size_t)cells * 4));
+    OV_ALLOC(c, cudaMalloc(&t.csum, (size_t)cells * 6 * 8));
+    OV_ALLOC(c, cudaMalloc(&t.first, (size_t)cells * 4));
     t.cap_cells = cells;
-    OV_ALLOC(c, cudaMalloc(&t.cells, (size_t)t.cap_cells * sizeof(Cell64)));
-    OV_ALLOC(c, cudaMalloc(&t.cells32, (size_t)t.cap_cells * sizeof(Cell32)));
-    OV_ALLOC(c, cudaMalloc(&t.cellsff, (size_t)t.cap_cells * sizeof(CellFF)));
-    OV_ALLOC(c, cudaMalloc(&t.parent, (size_t)t.cap_cells * 4));
-    OV_ALLOC(c, cudaMalloc(&t.nchild, (size_t)t.cap_cells * 4));
-    OV_ALLOC(c, cudaMalloc(&t.arrive, (size_t)t.cap_cells * 4));
-    OV_ALLOC(c, cudaMalloc(&t.csum, (size_t)t.cap_cells * 6 * 8));
     return OV_OK;
 }
 
@@ -651,8 +661,8 @@ int ov_tree_reserve(ov_ctx *c, int cap)
 void ov_tree_free(TreeBuf &t)
 {
     void *ptrs[] = {t.keys, t.keys_alt, t.order, t.order_alt, t.torder, t.cpl, t.ncell_at, t.cell_off, t.scan_tmp,
-                    t.sort_hist, t.cells, t.cells32, t.cellsff, t.parent, t.nchild, t.arrive, t.csum, t.counters,
-                    t.tt};
+                    t.sort_hist, t.cells, t.cells32, t.cellsff, t.parent, t.nchild, t.arrive, t.csum, t.first,
+                    t.counters, t.tt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     t = TreeBuf{};
@@ -681,6 +691,10 @@ static KeyGeom key_geom(const ov_ctx *c)
     g.lvmask = ((g.levels >= 21 ? ~0ull >> 1 : (1ull << (3 * g.levels)) - 1)) << (63 - g.tb - 3 * g.levels);
     g.nt = (int)c->mem.size();
     g.sph_root = c->geo.sph;
+    {
+        const double Lx = geo.hi[0] - geo.lo[0], Ly = geo.hi[1] - geo.lo[1], Lz = geo.hi[2] - geo.lo[2];
+        g.root_lm = Lx > Ly ? (Lx > Lz ? Lx : Lz) : (Ly > Lz ? Ly : Lz);   // box_lm's ternary
+    }
     for (int m = 0; m < OV_SPH_MEMBERS; ++m)
         for (int a = 0; a < 3; ++a) {
             g.sb[m][a] = c->sph_lo[m][a];
@@ -720,14 +734,14 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     ov_scan_exclusive(c, t.ncell_at, t.cell_off, cap, t.counters + TC_NNE, 0, t.scan_tmp, s);
     if (c->geo.sph)
         k_cells<true><<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.parent,
-                                         t.nchild, t.arrive, t.cap_cells);
+                                         t.nchild, t.arrive, t.first, t.cap_cells);
     else
         k_cells<false><<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.parent,
-                                          t.nchild, t.arrive, t.cap_cells);
+                                          t.nchild, t.arrive, t.first, t.cap_cells);
     k_moments<<<nb, 256, 0, s>>>(t.keys, t.order, t.cpl, t.cell_off, t.counters, t.tt, g, cap, na.x, na.y, na.z,
                                  c->fwd, c->geo, t.cells, t.parent, t.nchild, t.arrive, t.csum, t.cap_cells);
     k_root<<<nt, 256, 0, s>>>(t.order, t.cell_off, t.counters, t.tt, na.x, na.y, na.z, c->fwd, c->geo, g, t.cells,
-                              t.csum, t.cap_cells);
+                              t.csum, t.first, t.cap_cells);
     c->launches += 3;
     if (c->precision == OV_PREC_MIXED || c->precision == OV_PREC_DD || c->walk == OV_WALK_SPLIT) {
         k_cells32<<<(t.cap_cells + 255) / 256, 256, 0, s>>>(t.cells, t.counters, c->grid_h, 1.0 / c->grid_h,

@@ -59,7 +59,46 @@ struct VelArgs {
     double near2;           // mixed path: squared near-field radius
     unsigned long long *stat;
     unsigned *node_counts;  // when set: visits[cap], then accepts[cap], per target slot
+    // box cells store Lm scaled from the root's (null for spherical trees,
+    // whose stored Lm is exact): the exact one is walked on demand
+    const int *cell_first;  // first sorted position of each cell's nodes
+    const uint64_t *keys;   // sorted path keys
+    int key_tb;             // member-id bits above the path
+    double root_lm;         // Lm of the root box
+    double lm_ulp;          // 2^-44 max |box coordinate|: per-level slack of a scaled Lm
 };
+
+// Largest side of cell cp's box as the reference rounds it (make_child_box,
+// octree.c:165-232; octree.c:302-306), walked from the root along the path of
+// the cell's first node.  Only the opening tests within their band need it.
+__device__ __noinline__ double cell_lm_exact(const VelArgs &a, const Cell64 *cp)
+{
+    const double lm = cp->lm;
+    if (!a.cell_first) return lm;
+    const int c = (int)(cp - a.cells);
+    const int lev = ilogb(a.root_lm) - ilogb(lm);
+    if (lev <= 0 || lev > OV_MAX_LEVEL || c < 0) return lm;
+    const int s = a.cell_first[c];
+    if (s < 0 || s >= a.cap) return lm;
+    const uint64_t key = a.keys[s];
+    double b[3] = {a.geo.lo[0], a.geo.lo[1], a.geo.lo[2]}, t[3] = {a.geo.hi[0], a.geo.hi[1], a.geo.hi[2]};
+    for (int l = 1; l <= lev; ++l) {
+        double cb[3], ct[3];
+        child_box_dev(b, t, (int)((key >> (63 - a.key_tb - 3 * l)) & 7), cb, ct);
+        for (int x = 0; x < 3; ++x) { b[x] = cb[x]; t[x] = ct[x]; }
+    }
+    return box_lm(b, t);
+}
+
+// Bound on |stored Lm - exact Lm| for a box cell: each level's midpoint and
+// child bounds add a few roundings of the box coordinates (the parents'
+// errors average, they do not add up); (lev + 2) 2^-44 max|coordinate| is
+// far above them.
+__device__ __forceinline__ double lm_slack(const VelArgs &a, double lm)
+{
+    if (!a.cell_first) return 0.0;
+    return (double)(ilogb(a.root_lm) - ilogb(lm) + 2) * a.lm_ulp;
+}
 
 // Add one work item's visits and accepts of target slot id to the per-node
 // counters (only when they were asked for: ov_set_node_counting).
@@ -338,9 +377,10 @@ __device__ __forceinline__ void bh_query64(const VelArgs &a, const double q[3], 
                     acc = true;   // leaf (or a cell at the deepest level)
                 } else {
                     double td = theta * d;
-                    if (lm < td * (1.0 - 1e-12)) acc = true;
-                    else if (lm > td * (1.0 + 1e-12)) acc = false;
-                    else acc = rn_div(lm, d) < theta;
+                    const double sl = lm_slack(a, lm);
+                    if (lm + sl < td * (1.0 - 1e-12)) acc = true;
+                    else if (lm - sl > td * (1.0 + 1e-12)) acc = false;
+                    else acc = rn_div(cell_lm_exact(a, cp), d) < theta;
                 }
                 if (acc) {
                     ++accepts;
@@ -678,8 +718,8 @@ __global__ void k_wrap(const int *__restrict__ status, double *x, double *y, dou
 // are done in FP64.  Per-query sums use Kahan compensation.
 
 // decision of the FP64 path for cell c: 1 skip (d < 1e-8), 2 accept, 0 open
-__device__ __forceinline__ int decide64(const Cell64 *cp, const double q[3], double theta, bool leaf, double dxyz[3],
-                                        double *dout)
+__device__ __forceinline__ int decide64(const VelArgs &a, const Cell64 *cp, const double q[3], double theta, bool leaf,
+                                        double dxyz[3], double *dout)
 {
     double dx = rn_sub(q[0], __ldg(&cp->cx)), dy = rn_sub(q[1], __ldg(&cp->cy)), dz = rn_sub(q[2], __ldg(&cp->cz));
     double d = len3_ref(dx, dy, dz);
@@ -689,9 +729,10 @@ __device__ __forceinline__ int decide64(const Cell64 *cp, const double q[3], dou
     if (leaf) return 2;
     double lm = __ldg(&cp->lm);
     double td = theta * d;
-    if (lm < td * (1.0 - 1e-12)) return 2;
-    if (lm > td * (1.0 + 1e-12)) return 0;
-    return rn_div(lm, d) < theta ? 2 : 0;
+    const double sl = lm_slack(a, lm);
+    if (lm + sl < td * (1.0 - 1e-12)) return 2;
+    if (lm - sl > td * (1.0 + 1e-12)) return 0;
+    return rn_div(cell_lm_exact(a, cp), d) < theta ? 2 : 0;
 }
 
 __device__ __forceinline__ bool interact64(const Cell64 *cp, const double dxyz[3], double d, double f4pi, double w[3])
@@ -945,7 +986,7 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
                 double q[3], dxyz[3], d64;
                 if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
                 else image_point(a.geo, j, p, q);
-                int dec = decide64(a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
+                int dec = decide64(a, a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
                 skip = dec == 1;
                 acc = dec == 2;
             }
@@ -975,7 +1016,7 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
                         double q[3], dxyz[3], d64, w[3];
                         if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
                         else image_point(a.geo, j, p, q);
-                        decide64(a.cells + c, q, a.prm.theta, true, dxyz, &d64);
+                        decide64(a, a.cells + c, q, a.prm.theta, true, dxyz, &d64);
                         if (interact64(a.cells + c, dxyz, d64, a.f4pi, w)) {
                             w64[0] += w[0]; w64[1] += w[1]; w64[2] += w[2];
                         }
@@ -1173,7 +1214,7 @@ __device__ __noinline__ void mixp_term64(const VelArgs &a, int c, int j, int id,
     double p[3] = {a.x[id], a.y[id], a.z[id]}, q[3], dxyz[3], d64, w[3];
     if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
     else image_point(a.geo, j, p, q);
-    decide64(a.cells + c, q, a.prm.theta, true, dxyz, &d64);
+    decide64(a, a.cells + c, q, a.prm.theta, true, dxyz, &d64);
     if (interact64(a.cells + c, dxyz, d64, a.f4pi, w)) {
         w64[0] += w[0]; w64[1] += w[1]; w64[2] += w[2];
     }
@@ -1186,7 +1227,7 @@ __device__ __noinline__ int mixp_decide64(const VelArgs &a, int c, int j, int id
     double p[3] = {a.x[id], a.y[id], a.z[id]}, q[3], dxyz[3], d64;
     if (j < 0) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
     else image_point(a.geo, j, p, q);
-    return decide64(a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
+    return decide64(a, a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
 }
 
 // An accepted cell whose term needs FP64 (near field, a decision or filter
@@ -1497,7 +1538,7 @@ __device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], c
             if ((!skip && d2 <= d2hi) || (!skip && !acc && !opn)) {
                 ++m.nfb;
                 double dxyz[3], d64;
-                const int dec = decide64(a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
+                const int dec = decide64(a, a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
                 skip = dec == 1;
                 acc = dec == 2;
             }
@@ -1689,6 +1730,17 @@ VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long 
     a.f4pi_h = (float)a.f4pi;
     a.f4pi_l = (float)(a.f4pi - (double)a.f4pi_h);
     a.node_counts = nullptr;
+    a.cell_first = c->geo.sph ? nullptr : c->tree.first;
+    a.keys = c->tree.keys;
+    a.key_tb = c->key_tbits;
+    {
+        const Geometry &g = c->geo;
+        const double Lx = g.hi[0] - g.lo[0], Ly = g.hi[1] - g.lo[1], Lz = g.hi[2] - g.lo[2];
+        a.root_lm = Lx > Ly ? (Lx > Lz ? Lx : Lz) : (Ly > Lz ? Ly : Lz);
+        double m = 0;
+        for (int x = 0; x < 3; ++x) m = std::max(m, std::max(fabs(g.lo[x]), fabs(g.hi[x])));
+        a.lm_ulp = ldexp(m, -44);
+    }
     return a;
 }
 
