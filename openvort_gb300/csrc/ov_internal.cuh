@@ -76,6 +76,9 @@ enum MemberWords {
     TT_WORDS = 8
 };
 
+constexpr int TREE_LV_SLOTS = 32;   // levels 0..OV_MAX_LEVEL of the per-level cell lists
+constexpr int TREE_INV_COUNT = 4096; // table of 1 / count for the cell means
+
 struct TreeBuf {
     int cap = 0;
     int *tt = nullptr;           // TT_WORDS ints per member
@@ -91,11 +94,15 @@ struct TreeBuf {
     Cell64 *cells = nullptr;
     Cell32 *cells32 = nullptr;
     CellFF *cellsff = nullptr;
-    int *parent = nullptr;
-    int *nchild = nullptr;
-    int *arrive = nullptr;
-    double *csum = nullptr;      // 6 doubles per cell: position sum, circulation sum
+    double *psum = nullptr;      // 3 doubles per cell of more than one node: position sum (a one-node
+                                 // cell's mean is its sum; every cell's circulation is a sum)
+    uint8_t *lvl8 = nullptr;     // level of each cell (0 for roots)
     int *first = nullptr;        // first sorted position of each cell's nodes
+    int *lvl_list = nullptr;     // non-root cells grouped by level (ascending levels)
+    int *lvl_cnt = nullptr;      // TREE_LV_SLOTS cells per level, then as many fill counters
+    double *nm = nullptr;        // 6 doubles per node slot: position, wrapped forward segment
+    double *inv_count = nullptr; // TREE_INV_COUNT entries: 1 / k, rounded (entry 0 unused)
+    float *lev_tab = nullptr;    // per level: FP32 opening threshold and Lm of a box cell
     int *counters = nullptr;     // device scalars, see TreeCounters
 };
 

@@ -19,62 +19,117 @@ constexpr int kSortItems = 16;                       // items per thread
 constexpr int kTile = kSortThreads * kSortItems;     // 4096 slots per block
 constexpr int kWarps = kSortThreads / 32;
 
-__global__ void rs_hist(const uint64_t *__restrict__ keys, int n, int shift, int ntiles,
-                        int *__restrict__ hist)
+// Exclusive scan of one int per thread over the block (blockDim a multiple
+// of 32, at most 1024); total gets the block's sum.
+__device__ __forceinline__ int block_excl_scan(int v, int *sh, int &total)
 {
-    __shared__ int h[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[warp] = x;
     __syncthreads();
-    int base = blockIdx.x * kTile;
-    for (int i = threadIdx.x; i < kTile; i += blockDim.x) {
-        int g = base + i;
-        if (g < n) atomicAdd(&h[(keys[g] >> shift) & 0xFF], 1);
+    if (warp == 0) {
+        int w = lane < (blockDim.x >> 5) ? sh[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        sh[lane] = w;
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d * ntiles + blockIdx.x] = h[d];
+    int warp_off = warp > 0 ? sh[warp - 1] : 0;
+    total = sh[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warp_off + x - v;
 }
 
-// Exclusive scan of the digit-major table hist[256*ntiles] in one block
-// (small tables: one launch instead of the device-wide scan's three).
-__global__ void rs_scan(int *__restrict__ hist, int total)
+// Per-tile histogram of the pass's digit (digit-major table hist[d * ntiles
+// + tile]); with tot, also the totals of all four digits over every key,
+// which the later passes' digit offsets start from (the keys of a pass are
+// a permutation of the first pass's).  Same-digit lanes of a warp add once.
+__global__ void rs_hist(const uint64_t *__restrict__ keys, int n, int shift, int ntiles,
+                        int *__restrict__ hist, int *__restrict__ tot)
 {
-    __shared__ int part[1024];
-    int per = (total + blockDim.x - 1) / blockDim.x;
-    int b = threadIdx.x * per, e = min(total, b + per);
-    int s = 0;
-    for (int i = b; i < e; ++i) s += hist[i];
-    part[threadIdx.x] = s;
+    __shared__ int h[4][256];
+    const int np = tot ? 4 : 1;
+    for (int i = threadIdx.x; i < np * 256; i += blockDim.x) (&h[0][0])[i] = 0;
     __syncthreads();
-    for (int off = 1; off < blockDim.x; off <<= 1) {
-        int v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
+    const int base = blockIdx.x * kTile;
+    uint64_t k[kSortItems];
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int g = base + r * kSortThreads + threadIdx.x;
+        k[r] = g < n ? keys[g] : 0;
     }
-    int run = part[threadIdx.x] - s;
-    for (int i = b; i < e; ++i) {
-        int v = hist[i];
-        hist[i] = run;
-        run += v;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int g = base + r * kSortThreads + threadIdx.x;
+        const unsigned act = __ballot_sync(0xffffffffu, g < n);
+        if (g < n) {
+            for (int p = 0; p < np; ++p) {
+                const int sh = tot ? 32 + 8 * p : shift;
+                const int d = (int)((k[r] >> sh) & 0xFF);
+                const unsigned m = __match_any_sync(act, d);
+                if (lane == __ffs(m) - 1) atomicAdd(&h[p][d], __popc(m));
+            }
+        }
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d * ntiles + blockIdx.x] = h[tot ? (shift - 32) / 8 : 0][d];
+    if (tot)
+        for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x)
+            if ((&h[0][0])[i]) atomicAdd(&tot[i], (&h[0][0])[i]);
+}
+
+// Digit offsets of a pass: block d turns row d of the table into global
+// output offsets, the keys of smaller digits (from the totals) plus the
+// row's prefix over tiles.
+__global__ void rs_rowscan(int *__restrict__ hist, int ntiles, const int *__restrict__ tot)
+{
+    __shared__ int sh[32];
+    const int d = blockIdx.x;
+    int total;
+    block_excl_scan(threadIdx.x < d ? tot[threadIdx.x] : 0, sh, total);
+    int run = total;
+    int *row = hist + (size_t)d * ntiles;
+    for (int b = 0; b < ntiles; b += blockDim.x) {
+        const int i = b + threadIdx.x;
+        const int v = i < ntiles ? row[i] : 0;
+        const int off = block_excl_scan(v, sh, total);
+        if (i < ntiles) row[i] = run + off;
+        run += total;
     }
 }
 
 // Stable scatter: items of a tile are ordered (warp, round, lane); each warp
 // counts digits with match_any, the per-warp counts are scanned across warps
-// and a running per-(warp,digit) counter hands out ranks.
+// and a running per-(warp,digit) counter hands out ranks.  The tile is put in
+// digit order in shared memory first, so that each digit's run is written
+// out by consecutive threads (keys, then the ids through the same buffer).
 __global__ void rs_scatter(const uint64_t *__restrict__ kin, const int *__restrict__ vin,
                            uint64_t *__restrict__ kout, int *__restrict__ vout, int n, int shift,
                            int ntiles, const int *__restrict__ hist)
 {
+    __shared__ uint64_t sk[kTile];        // the tile in digit order (keys, then ids)
+    __shared__ uint8_t sd[kTile];         // digit of each staged slot
     __shared__ int wc[kWarps][256];
-    __shared__ int gbase[256];
+    __shared__ int gbase[256], boff[256];
+    __shared__ int sh[32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int i = threadIdx.x; i < kWarps * 256; i += blockDim.x) (&wc[0][0])[i] = 0;
     for (int d = threadIdx.x; d < 256; d += blockDim.x) gbase[d] = hist[d * ntiles + blockIdx.x];
     __syncthreads();
-    const int wbase = blockIdx.x * kTile + warp * (kSortItems * 32);
+    const int tbase = blockIdx.x * kTile;
+    const int tn = min(kTile, n - tbase);
+    const int wbase = tbase + warp * (kSortItems * 32);
     uint64_t k[kSortItems];
-    int v[kSortItems];
+    int v[kSortItems], lp[kSortItems];
 #pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         int g = wbase + r * 32 + lane;
@@ -94,7 +149,9 @@ __global__ void rs_scatter(const uint64_t *__restrict__ kin, const int *__restri
         __syncwarp();
     }
     __syncthreads();
-    // exclusive scan over warps per digit
+    // exclusive scan over warps per digit; the tile's digit totals scanned
+    // over digits give each digit's start in the staged tile
+    int dig_total = 0;
     for (int d = threadIdx.x; d < 256; d += blockDim.x) {
         int run = 0;
         for (int w = 0; w < kWarps; ++w) {
@@ -102,23 +159,45 @@ __global__ void rs_scatter(const uint64_t *__restrict__ kin, const int *__restri
             wc[w][d] = run;
             run += c;
         }
+        dig_total = run;
+    }
+    {
+        int tot_all;
+        const int off = block_excl_scan(threadIdx.x < 256 ? dig_total : 0, sh, tot_all);
+        if (threadIdx.x < 256) boff[threadIdx.x] = off;
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         int g = wbase + r * 32 + lane;
         unsigned act = __ballot_sync(0xffffffffu, g < n);
+        lp[r] = -1;
         if (g < n) {
             int d = (int)((k[r] >> shift) & 0xFF);
             unsigned m = __match_any_sync(act, d);
             int base = wc[warp][d];
-            int pos = gbase[d] + base + __popc(m & lt);
-            kout[pos] = k[r];
-            vout[pos] = v[r];
+            lp[r] = boff[d] + base + __popc(m & lt);
+            sk[lp[r]] = k[r];
+            sd[lp[r]] = (uint8_t)d;
             __syncwarp(m);
             if ((m & lt) == 0) wc[warp][d] = base + __popc(m);
         }
         __syncwarp();
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < tn; j += blockDim.x) {
+        const int d = sd[j];
+        kout[gbase[d] + j - boff[d]] = sk[j];
+    }
+    __syncthreads();
+    int *sv = reinterpret_cast<int *>(sk);
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r)
+        if (lp[r] >= 0) sv[lp[r]] = v[r];
+    __syncthreads();
+    for (int j = threadIdx.x; j < tn; j += blockDim.x) {
+        const int d = sd[j];
+        vout[gbase[d] + j - boff[d]] = sv[j];
     }
 }
 
@@ -156,33 +235,6 @@ __global__ void rs_fixup(uint64_t *__restrict__ keys, int *__restrict__ vals, in
 constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
-
-__device__ __forceinline__ int block_excl_scan(int v, int *sh, int &total)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) sh[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        int w = lane < (blockDim.x >> 5) ? sh[lane] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
-        }
-        sh[lane] = w;
-    }
-    __syncthreads();
-    int warp_off = warp > 0 ? sh[warp - 1] : 0;
-    total = sh[(blockDim.x >> 5) - 1];
-    __syncthreads();
-    return warp_off + x - v;
-}
 
 __global__ void scan_tiles(const int *__restrict__ in, int *__restrict__ out, int n_max,
                            const int *n_dev, int *__restrict__ tile_sums)
@@ -234,26 +286,23 @@ __global__ void scan_add(int *__restrict__ out, int n_max, const int *n_dev, con
 void ov_scan_exclusive(ov_ctx *c, const int *in, int *out, int n_max, const int *n_dev, int add, int *tmp,
                        cudaStream_t s);
 
-// Radix sort of t.keys / t.order (n slots); the digit tables of more than
-// 32 tiles are scanned in place by the device-wide scan (the table has room
-// for its total).
+// Radix sort of t.keys / t.order (n slots): per pass a tile histogram, the
+// digit offsets (one block per digit) and the scatter; the digit totals of
+// all passes come with the first histogram.
 void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
 {
     if (n <= 0) return;
     int ntiles = (n + kTile - 1) / kTile;
     uint64_t *ka = t.keys, *kb = t.keys_alt;
     int *va = t.order, *vb = t.order_alt;
+    int *tot = t.sort_hist + 256 * (size_t)ntiles;   // 4 x 256 digit totals
+    cudaMemsetAsync(tot, 0, 4 * 256 * sizeof(int), s);
     for (int pass = 0; pass < 4; ++pass) {
         int shift = 32 + 8 * pass;
-        rs_hist<<<ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, t.sort_hist);
-        if (ntiles <= 32) {
-            rs_scan<<<1, 1024, 0, s>>>(t.sort_hist, 256 * ntiles);
-            c->launches += 1;
-        } else {
-            ov_scan_exclusive(c, t.sort_hist, t.sort_hist, 256 * ntiles, nullptr, 0, t.scan_tmp, s);
-        }
+        rs_hist<<<ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, t.sort_hist, pass == 0 ? tot : nullptr);
+        rs_rowscan<<<256, kSortThreads, 0, s>>>(t.sort_hist, ntiles, tot + 256 * pass);
         rs_scatter<<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, ntiles, t.sort_hist);
-        c->launches += 2;
+        c->launches += 3;
         uint64_t *tk = ka; ka = kb; kb = tk;
         int *tv = va; va = vb; vb = tv;
     }
@@ -262,7 +311,7 @@ void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
     c->launches += 1;
 }
 
-int ov_sort_hist_ints(int cap) { return 256 * ((cap + kTile - 1) / kTile) + 256; }
+int ov_sort_hist_ints(int cap) { return 256 * ((cap + kTile - 1) / kTile) + 4 * 256; }
 
 // out[i] = add + sum(in[0..i)) for i in [0, n], n = min(*n_dev, n_max).
 void ov_scan_exclusive(ov_ctx *c, const int *in, int *out, int n_max, const int *n_dev, int add,

@@ -24,8 +24,6 @@
 // ceil(log2 T) bits and the keys hold floor((63 - bits) / 3) levels.
 #include "ov_internal.cuh"
 
-#include <cuda/atomic>
-
 void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s);
 int ov_sort_hist_ints(int cap);
 int ov_scan_tmp_ints(int n_max);
@@ -35,6 +33,7 @@ namespace {
 struct KeyGeom {
     double lo[3], hi[3], L[3];
     double invL[3];    // 1 / L, rounded
+    double invL62[3];  // invL * 2^62 (exact)
     int fast;          // fixed-point digits allowed (rounding bound is small)
     int tb;            // member-id bits on top of the key
     int levels;        // levels the key holds
@@ -103,12 +102,36 @@ __device__ __forceinline__ uint64_t sph_key(const double u[3], const KeyGeom &g,
     return key;
 }
 
+__device__ __forceinline__ void node_moment(int id, const double *x, const double *y, const double *z,
+                                            const int *fwd, const Geometry &geo, double out[6])
+{
+    double p[3] = {x[id], y[id], z[id]};
+    out[0] = p[0]; out[1] = p[1]; out[2] = p[2];
+    int f = fwd[id];
+    if (f > -1) {
+        double r2[3] = {x[f], y[f], z[f]};
+        if (geo.sph) sph_pwrap(geo, p, r2);
+        else pwrap_dev(geo, p, r2);
+        out[3] = rn_sub(r2[0], p[0]); out[4] = rn_sub(r2[1], p[1]); out[5] = rn_sub(r2[2], p[2]);
+        // the spherical fork leaves segments longer than 5 dl_max out (octree.c:316-322)
+        if (geo.sph && len3_ref(out[3], out[4], out[5]) > geo.sph_seg_max) out[3] = out[4] = out[5] = 0;
+    } else {
+        out[3] = out[4] = out[5] = 0;
+    }
+}
+
+// Path keys of all slots (EMPTY slots sort last), the member counts, and
+// each live node's moment (position, wrapped forward segment) in id order,
+// where the positions are read coalesced; the leaves of the tree gather it.
 template <bool SPH>
 __global__ void k_keys(const int *__restrict__ status, const double *__restrict__ x,
                        const double *__restrict__ y, const double *__restrict__ z, const int *__restrict__ tid,
                        int cap, KeyGeom g, uint64_t *__restrict__ keys, int *__restrict__ order,
-                       int *counters, int *tt)
+                       int *counters, int *tt, const int *__restrict__ fwd, Geometry geo, double *__restrict__ nm)
 {
+    __shared__ int bc[4];   // the block's live, in-box, out-of-box counts and NaN flag
+    if (threadIdx.x < 4) bc[threadIdx.x] = 0;
+    __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     bool live = i < cap && status[i] != OV_EMPTY;
@@ -125,22 +148,44 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
         inside = live && in_closed_box_dev(g.lo, g.hi, p);
     }
     bool bad = live && !(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]));
-    // one atomic per warp for each counter, one per member present in the warp
+    // one global atomic per block for each counter (a single tree's member
+    // counts are the same), one per warp and member present for a forest
     unsigned b_live = __ballot_sync(0xffffffffu, live), b_in = __ballot_sync(0xffffffffu, inside);
     unsigned peers = __match_any_sync(0xffffffffu, live ? m : -1) & b_live;
     if (lane == 0 && b_live) {
-        atomicAdd(&counters[TC_NNE], __popc(b_live));
-        atomicAdd(&counters[TC_M], __popc(b_in));
-        atomicAdd(&counters[TC_OUT], __popc(b_live & ~b_in));
+        atomicAdd(&bc[0], __popc(b_live));
+        atomicAdd(&bc[1], __popc(b_in));
+        atomicAdd(&bc[2], __popc(b_live & ~b_in));
     }
-    if (live && lane == __ffs(peers) - 1) {
+    if (tid && live && lane == __ffs(peers) - 1) {
         atomicAdd(&tt[m * TT_WORDS + TT_NNE], __popc(peers));
         atomicAdd(&tt[m * TT_WORDS + TT_M], __popc(peers & b_in));
     }
-    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&counters[TC_ERR], OV_EW_NAN);
+    if (__any_sync(0xffffffffu, bad) && lane == 0) bc[3] = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (bc[0]) {
+            atomicAdd(&counters[TC_NNE], bc[0]);
+            atomicAdd(&counters[TC_M], bc[1]);
+            atomicAdd(&counters[TC_OUT], bc[2]);
+            if (!tid) {
+                atomicAdd(&tt[TT_NNE], bc[0]);
+                atomicAdd(&tt[TT_M], bc[1]);
+            }
+        }
+        if (bc[3]) atomicOr(&counters[TC_ERR], OV_EW_NAN);
+    }
     if (i >= cap) return;
     order[i] = i;
     if (!live) { keys[i] = OV_KEY_EMPTY; return; }
+    {
+        double mo[6];
+        node_moment(i, x, y, z, fwd, geo, mo);
+        double2 *o = reinterpret_cast<double2 *>(nm + 6 * (size_t)i);
+        o[0] = make_double2(mo[0], mo[1]);
+        o[1] = make_double2(mo[2], mo[3]);
+        o[2] = make_double2(mo[4], mo[5]);
+    }
     const uint64_t prefix = g.tb ? (uint64_t)m << (64 - g.tb) : 0;
     if (SPH) {
         // outside the member's section: root only, ordered by the path of
@@ -185,9 +230,11 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
     const uint64_t low = (1ull << 41) - 1, margin = 1ull << 22;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        double u = rn_mul(rn_sub(p[a], g.lo[a]), g.invL[a]);
-        u = fmin(fmax(u, 0.0), 1.0);
-        U[a] = (uint64_t)(u * 4611686018427387904.0);   // u * 2^62
+        // (p - lo) / L * 2^62 clamped to [0, 2^62]: the 2^62 scaling is exact,
+        // so this equals the truncated product of the clamped unit image;
+        // the conversion saturates (p >= lo here)
+        const double v = rn_mul(rn_sub(p[a], g.lo[a]), g.invL62[a]);
+        U[a] = min((unsigned long long)__double2ull_rz(v), 1ull << 62);
         uint64_t r = U[a] & low;
         safe = safe && r >= margin && r <= low + 1 - margin;
     }
@@ -207,11 +254,26 @@ __global__ void k_keys(const int *__restrict__ status, const double *__restrict_
     keys[i] = prefix | ((key >> g.tb) & g.lvmask);
 }
 
+__device__ __forceinline__ float cell_thr(double lm, double theta)
+{
+    const double r = lm / theta;
+    return theta > 0 ? __double2float_ru(r * r * (1.0 + 2e-5)) : __int_as_float(0x7f800000);
+}
+
 // Member layout: first sorted position of each member (members in id order)
 // and the first work tile of each in the traversal queue (queue order).
-__global__ void k_layout(int *tt, int nt, const int *__restrict__ qorder, int *counters)
+// Lanes also fill the per-level table of box cells (Lm = the root's Lm
+// scaled by 2^-lev): the FP32 opening threshold and Lm rounded up.
+__global__ void k_layout(int *tt, int nt, const int *__restrict__ qorder, int *counters, float *lev_tab,
+                         double root_lm, double theta)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0) return;
+    if (threadIdx.x < TREE_LV_SLOTS) {
+        const double lm = ldexp(root_lm, -(int)threadIdx.x);
+        lev_tab[threadIdx.x] = cell_thr(lm, theta);
+        lev_tab[TREE_LV_SLOTS + threadIdx.x] = __double2float_ru(lm);
+    }
+    if (threadIdx.x != 0) return;
     int acc = 0;
     for (int m = 0; m < nt; ++m) {
         tt[m * TT_WORDS + TT_START] = acc;
@@ -286,13 +348,21 @@ __device__ __forceinline__ int cpl_of(const KeyGeom &g, uint64_t a, uint64_t b)
 
 // cpl[s] (common levels with the next in-box key of the member) and the
 // number of cells that start at sorted position s: the member's root at its
-// first position, then the cells of the levels the node starts.
+// first position, then the cells of the levels the node starts.  Also counts
+// the non-root, non-leaf cells of every level (lvl_cnt[lev]) for the
+// per-level lists the moment sums run over, and the depth, one global atomic
+// per block and counter.
 __global__ void k_cpl(const uint64_t *__restrict__ keys, int cap, int *counters, const int *__restrict__ tt,
-                      KeyGeom g, int *__restrict__ cpl, int *__restrict__ ncell_at)
+                      KeyGeom g, int *__restrict__ cpl, int *__restrict__ ncell_at, int *lvl_cnt)
 {
+    __shared__ int h[TREE_LV_SLOTS];
+    __shared__ int bmax, bdeep;
+    if (threadIdx.x < TREE_LV_SLOTS) h[threadIdx.x] = 0;
+    if (threadIdx.x == 0) bmax = bdeep = 0;
+    __syncthreads();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     int nne_all = counters[TC_NNE];
-    int L = 0, nne = 0;
+    int L = 0, nne = 0, lo = 1, hi = 0;
     bool deep = false;
     if (s < nne_all && s < cap) {
         uint64_t key = keys[s];
@@ -311,9 +381,18 @@ __global__ void k_cpl(const uint64_t *__restrict__ keys, int cap, int *counters,
             L = max(cp, cn) + 1;
             if (L > g.levels) { deep = true; L = g.levels; }
             ncell_at[s] = ((nne >= 2) ? max(L - cp, 0) : 0) + (loc == 0);
+            if (nne >= 2) { lo = cp + 1; hi = L - 1; }   // the non-leaf cells
         } else {
             cpl[s] = 0;
             ncell_at[s] = (loc == 0);
+        }
+    }
+    {
+        const int wlo = __reduce_min_sync(0xffffffffu, lo <= hi ? lo : OV_MAX_LEVEL + 1);
+        const int whi = __reduce_max_sync(0xffffffffu, lo <= hi ? hi : 0);
+        for (int lev = wlo; lev <= whi; ++lev) {
+            const unsigned m = __ballot_sync(0xffffffffu, lo <= lev && lev <= hi);
+            if ((threadIdx.x & 31) == 0 && m) atomicAdd(&h[lev], __popc(m));
         }
     }
     int Lmax = (nne >= 2) ? L : 0;
@@ -321,58 +400,211 @@ __global__ void k_cpl(const uint64_t *__restrict__ keys, int cap, int *counters,
     for (int o = 16; o > 0; o >>= 1) Lmax = max(Lmax, __shfl_xor_sync(0xffffffffu, Lmax, o));
     bool anydeep = __any_sync(0xffffffffu, deep);
     if ((threadIdx.x & 31) == 0) {
-        if (Lmax > 0) atomicMax(&counters[TC_MAXDEPTH], Lmax);
-        if (anydeep) atomicOr(&counters[TC_ERR], OV_EW_DEPTH);
+        if (Lmax > 0) atomicMax(&bmax, Lmax);
+        if (anydeep) bdeep = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x < TREE_LV_SLOTS && h[threadIdx.x]) atomicAdd(&lvl_cnt[threadIdx.x], h[threadIdx.x]);
+    if (threadIdx.x == 0) {
+        if (bmax > 0) atomicMax(&counters[TC_MAXDEPTH], bmax);
+        if (bdeep) atomicOr(&counters[TC_ERR], OV_EW_DEPTH);
     }
 }
 
-// first index j in [lo, hi) with (keys[j] >> sh) > P  (keys sorted)
-__device__ __forceinline__ int upper_prefix(const uint64_t *keys, int lo, int hi, int sh, uint64_t P)
+// FP32 view of a cell for the mixed traversal: COM split into a part on
+// the grid of step h (exact in FP32) and a small remainder.  The opening
+// test Lm / d < theta becomes d^2 > (Lm / theta)^2: thr holds that bound
+// times (1 + 2e-5), rounded up, so that d^2 > thr accepts clear of the guard
+// band and d^2 < thr (1 - 2e-5) / (1 + 2e-5) opens clear of it.
+__device__ __forceinline__ void write_cell32(Cell32 *out, int ci, const double c[3], const double q[3], float thr,
+                                             float lm32, int next, double h, double inv_h)
 {
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if ((keys[mid] >> sh) > P) hi = mid; else lo = mid + 1;
-    }
-    return lo;
+    double gx = rint(c[0] * inv_h) * h, gy = rint(c[1] * inv_h) * h, gz = rint(c[2] * inv_h) * h;
+    float4 *o = reinterpret_cast<float4 *>(out + ci);
+    o[0] = make_float4((float)gx, (float)gy, (float)gz, thr);
+    o[1] = make_float4((float)(c[0] - gx), (float)(c[1] - gy), (float)(c[2] - gz), __int_as_float(next));
+    o[2] = make_float4((float)q[0], (float)q[1], (float)q[2], lm32);
 }
-// first index j in [lo, hi) with (keys[j] >> sh) >= P
-__device__ __forceinline__ int lower_prefix(const uint64_t *keys, int lo, int hi, int sh, uint64_t P)
+
+// Double-single view for the OV_PREC_DD law: the centre of mass as its grid
+// part (exact in FP32) plus the rest (exact in FP64) as hi + lo floats, the
+// circulation as hi + lo.
+__device__ __forceinline__ void write_cellff(CellFF *out, int ci, const double c[3], const double q[3], double h,
+                                             double inv_h)
 {
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if ((keys[mid] >> sh) >= P) hi = mid; else lo = mid + 1;
+    CellFF o;
+    for (int a = 0; a < 3; ++a) {
+        const double G = rint(c[a] * inv_h) * h;
+        const double f = c[a] - G;
+        o.g[a] = (float)G;
+        o.fh[a] = (float)f;
+        o.fl[a] = (float)(f - (double)o.fh[a]);
+        o.qh[a] = (float)q[a];
+        o.ql[a] = (float)(q[a] - (double)o.qh[a]);
+    }
+    o.pad = 0;
+    out[ci] = o;
+}
+
+// What the traversals read of a cell once its sums are known: the means and
+// the circulation in the FP64 cell, the FP32 and double-single views.
+struct CellViews {
+    Cell32 *c32;
+    CellFF *cff;
+    double h, inv_h, theta;
+    const double *inv_count;   // 1 / k for k < TREE_INV_COUNT
+    const float *lev_tab;      // box cells: threshold and Lm per level (null: spherical cells)
+};
+
+// Write a cell whole (64 bytes) once its sums are known: the means and the
+// circulation, Lm, successor and count, then the FP32 and double-single
+// views the traversals read.
+// (The mean of a one-node cell is its sum: a product with 1.0.  1 / count
+// comes from a table of the rounded quotients for the usual counts.)
+__device__ __forceinline__ void store_cell(Cell64 *cells, int ci, const double s[6], int count, double lm, int lev,
+                                           int next, const CellViews &v)
+{
+    double c[3] = {s[0], s[1], s[2]};
+    if (count != 1) {
+        const double inv = count < TREE_INV_COUNT ? v.inv_count[count] : 1.0 / (double)count;
+        c[0] = rn_mul(s[0], inv); c[1] = rn_mul(s[1], inv); c[2] = rn_mul(s[2], inv);
+    }
+    const double q[3] = {s[3], s[4], s[5]};
+    double2 *o = reinterpret_cast<double2 *>(cells + ci);
+    o[0] = make_double2(c[0], c[1]);
+    o[1] = make_double2(c[2], q[0]);
+    o[2] = make_double2(q[1], q[2]);
+    reinterpret_cast<int4 *>(cells + ci)[3] = make_int4(__double2loint(lm), __double2hiint(lm), next, count);
+    if (v.c32) {
+        const float thr = v.lev_tab ? v.lev_tab[lev] : cell_thr(lm, v.theta);
+        const float lm32 = v.lev_tab ? v.lev_tab[TREE_LV_SLOTS + lev] : __double2float_ru(lm);
+        write_cell32(v.c32, ci, c, q, thr, lm32, next, v.h, v.inv_h);
+    }
+    if (v.cff) write_cellff(v.cff, ci, c, q, v.h, v.inv_h);
+}
+
+__device__ __forceinline__ void store_psum(double *psum, int ci, const double acc[6])
+{
+    psum[3 * (size_t)ci] = acc[0];
+    psum[3 * (size_t)ci + 1] = acc[1];
+    psum[3 * (size_t)ci + 2] = acc[2];
+}
+
+// Add a finished cell's sums to acc (position sum, circulation sum), in
+// the order of a sum over its children: a one-node cell's mean is its
+// position (a product with 1.0), larger cells keep the sum in psum.
+__device__ __forceinline__ void add_cell_sums(const Cell64 &c, const double *psum, int ci, double acc[6])
+{
+    double p0 = c.cx, p1 = c.cy, p2 = c.cz;
+    if (c.count != 1) {
+        p0 = psum[3 * (size_t)ci];
+        p1 = psum[3 * (size_t)ci + 1];
+        p2 = psum[3 * (size_t)ci + 2];
+    }
+    acc[0] = rn_add(acc[0], p0); acc[1] = rn_add(acc[1], p1); acc[2] = rn_add(acc[2], p2);
+    acc[3] = rn_add(acc[3], c.qx); acc[4] = rn_add(acc[4], c.qy); acc[5] = rn_add(acc[5], c.qz);
+}
+
+// A node's moment as k_keys stored it (6 doubles at 48-byte stride).
+__device__ __forceinline__ void load_moment(const double *nm, int id, double m[6])
+{
+    const double2 *q = reinterpret_cast<const double2 *>(nm + 6 * (size_t)id);
+    const double2 a = q[0], b = q[1], c = q[2];
+    m[0] = a.x; m[1] = a.y; m[2] = b.x; m[3] = b.y; m[4] = c.x; m[5] = c.y;
+}
+
+// Last index j in [s, end) with (keys[j] >> sh) == P, given that keys[s]
+// has that prefix (keys sorted): probes at s + 1, 2, 4, ... then a binary
+// search in the last gap, so a cell of c nodes costs about 2 log2(c) loads.
+__device__ __forceinline__ int last_sharing(const uint64_t *keys, int s, int end, int sh, uint64_t P)
+{
+    int lo = s, hi = end, step = 1;
+    while (true) {
+        const int probe = lo + step;
+        if (probe >= end) break;
+        if ((keys[probe] >> sh) != P) { hi = probe; break; }
+        lo = probe;
+        step = step < (1 << 29) ? 2 * step : step;
+    }
+    while (hi - lo > 1) {
+        const int mid = lo + ((hi - lo) >> 1);
+        if ((keys[mid] >> sh) == P) lo = mid; else hi = mid;
     }
     return lo;
 }
 
+// Start of level `lev` in the per-level cell lists (levels ascending).
+__device__ __forceinline__ int level_start(const int *lvl_cnt, int lev)
+{
+    int st = 0;
+    for (int l = 0; l < lev; ++l) st += lvl_cnt[l];
+    return st;
+}
+
+// The cells that start at each sorted position: levels cp+1 .. L of the
+// node's path, each with its level, first sorted node and Lm.  The deepest,
+// level L, is the node's leaf (one node, or the run of nodes sharing the
+// deepest cell): it is finished here, since it depends on no other cell
+// (octree.c:264-283 for a one-node cell).  The others hold at least this
+// node and the next; each is entered in its level's list (lvl_list; slots
+// handed out per block, any order within a level) for k_level, which sums
+// their children and derives their counts and successors.
 template <bool SPH>
 __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict__ cpl,
                         const int *__restrict__ cell_off, int *counters, const int *__restrict__ tt, KeyGeom g,
-                        int cap, Cell64 *__restrict__ cells, int *__restrict__ parent, int *__restrict__ nchild,
-                        int *__restrict__ arrive, int *__restrict__ first, int cap_cells)
+                        int cap, Cell64 *__restrict__ cells, int *__restrict__ first, uint8_t *__restrict__ lvl8,
+                        int *lvl_cnt, int *__restrict__ lvl_list, int cap_cells, const int *__restrict__ order,
+                        const double *__restrict__ nm, double *__restrict__ psum, CellViews views)
 {
+    __shared__ int h[TREE_LV_SLOTS], hbase[TREE_LV_SLOTS];
     int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
     int nne_all = counters[TC_NNE];
-    if (s >= nne_all || s >= cap) return;
     int ncell = cell_off[nne_all];
-    if (ncell > cap_cells) {
+    if (ncell > cap_cells) {   // the same for every block
         if (s == 0) {
             atomicMax(&counters[TC_NEED], ncell);
             atomicOr(&counters[TC_ERR], OV_EW_CELLS);
         }
         return;
     }
-    uint64_t key = keys[s];
-    const int *w = tt + key_member(g, key) * TT_WORDS;
-    const int st = w[TT_START], M = w[TT_M], nne = w[TT_NNE];
+    if (threadIdx.x < TREE_LV_SLOTS) h[threadIdx.x] = 0;
+    __syncthreads();
+    uint64_t key = 0;
+    int st = 0, M = 0, cp = 0, L = 0;
+    bool mine = false;
+    if (s < nne_all && s < cap) {
+        key = keys[s];
+        const int *w = tt + key_member(g, key) * TT_WORDS;
+        st = w[TT_START];
+        M = w[TT_M];
+        const int nne = w[TT_NNE], loc = s - st;
+        if (loc == 0) lvl8[cell_off[s]] = 0;   // the member's root
+        if (loc >= 0 && loc < M && nne >= 2) {
+            cp = loc > 0 ? cpl[s - 1] : 0;
+            int cn = loc + 1 < M ? cpl[s] : 0;
+            L = min(max(cp, cn) + 1, g.levels);
+            mine = L > cp;
+        }
+    }
+    // the warp's range of levels; its non-leaf cells counted per level with
+    // one shared atomic per warp and level
+    const int lv_lo = __reduce_min_sync(0xffffffffu, mine ? cp + 1 : OV_MAX_LEVEL + 1);
+    const int lv_hi = __reduce_max_sync(0xffffffffu, mine ? L : 0);
+    for (int lev = lv_lo; lev < lv_hi; ++lev) {
+        const unsigned m = __ballot_sync(0xffffffffu, mine && cp < lev && lev < L);
+        if (lane == 0 && m) atomicAdd(&h[lev], __popc(m));
+    }
+    __syncthreads();
+    if (threadIdx.x < TREE_LV_SLOTS) {
+        const int n = h[threadIdx.x];
+        hbase[threadIdx.x] = n ? level_start(lvl_cnt, threadIdx.x) +
+                                     atomicAdd(&lvl_cnt[TREE_LV_SLOTS + threadIdx.x], n) : 0;
+        h[threadIdx.x] = 0;
+    }
+    __syncthreads();
     const int loc = s - st;
-    if (loc < 0 || loc >= M || nne < 2) return;
-    const int end = st + M;   // the member's in-box positions are [st, end)
-    const int root = cell_off[st];
-    int cp = loc > 0 ? cpl[s - 1] : 0;
-    int cn = loc + 1 < M ? cpl[s] : 0;
-    int L = min(max(cp, cn) + 1, g.levels);
-    const int base = cell_off[s] + (loc == 0);
+    const int base = mine ? cell_off[s] + (loc == 0) : 0;
     // Box cells: Lm is the root's scaled by 2^-lev, within a few ulps of the
     // reference's rounded child boxes (octree.c:165-232); the traversals'
     // opening tests take it outside a 1e-12 band and walk the exact box
@@ -380,7 +612,7 @@ __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict
     // the root (their Lm is not a scaled copy).
     double b[3], t[3];
     const int mem = key_member(g, key) < OV_SPH_MEMBERS ? key_member(g, key) : 0;
-    if (SPH) {
+    if (SPH && mine) {
         for (int a = 0; a < 3; ++a) { b[a] = g.sb[mem][a]; t[a] = g.st[mem][a]; }
         for (int lev = 1; lev <= cp; ++lev) {
             double cb[3], ct[3];
@@ -388,130 +620,120 @@ __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict
             for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
         }
     }
-    for (int lev = cp + 1; lev <= L; ++lev) {
-        int ci = base + (lev - cp - 1);
+    // every cell but the leaf: level, first node, Lm, list slot (the rest is
+    // k_level's)
+    for (int lev = lv_lo; lev < lv_hi; ++lev) {
+        const bool in = mine && cp < lev && lev < L;
+        const unsigned m = __ballot_sync(0xffffffffu, in);
+        if (!m) continue;
+        int wofs = 0;
+        if (lane == __ffs(m) - 1) wofs = atomicAdd(&h[lev], __popc(m));
+        wofs = __shfl_sync(0xffffffffu, wofs, __ffs(m) - 1);
+        if (!in) continue;
+        const int ci = base + (lev - cp - 1);
+        double lm;
         if (SPH) {
             double cb[3], ct[3];
             sph_child_box(b, t, (int)((key >> dsh(g, lev)) & 7), cb, ct);
             for (int a = 0; a < 3; ++a) { b[a] = cb[a]; t[a] = ct[a]; }
+            lm = sph_box_lm(b, t);
+        } else {
+            lm = ldexp(g.root_lm, -lev);
         }
-        int sh = dsh(g, lev);
-        int e = (lev < L) ? upper_prefix(keys, s + 1, end, sh, key >> sh) - 1 : s;
-        if (lev == g.levels) e = upper_prefix(keys, s + 1, end, sh, key >> sh) - 1;
-        Cell64 cell;
-        cell.lm = SPH ? sph_box_lm(b, t) : ldexp(g.root_lm, -lev);
-        cell.count = e - s + 1;
-        cell.next = cell_off[e + 1];   // the member's end of cells when e + 1 == end
-        cell.cx = cell.cy = cell.cz = cell.qx = cell.qy = cell.qz = 0;
-        cells[ci] = cell;
         first[ci] = s;
-        int par;
-        if (lev == 1) par = root;
-        else if (cp < lev - 1) par = ci - 1;
-        else {
-            int psh = dsh(g, lev - 1);
-            int sp = lower_prefix(keys, st, s, psh, key >> psh);
-            int cpp = sp > st ? cpl[sp - 1] : 0;
-            par = cell_off[sp] + (sp == st) + (lev - 1 - cpp - 1);
-        }
-        parent[ci] = par;
-        arrive[ci] = 0;
-        atomicAdd(&nchild[par], 1);
+        lvl8[ci] = (uint8_t)lev;
+        cells[ci].lm = lm;
+        const int slot = hbase[lev] + wofs + __popc(m & ((1u << lane) - 1u));
+        if (slot < cap_cells) lvl_list[slot] = ci;
+        else atomicOr(&counters[TC_ERR], OV_EW_BOUNDS);
     }
-}
-
-__device__ __forceinline__ void node_moment(int id, const double *x, const double *y, const double *z,
-                                            const int *fwd, const Geometry &geo, double out[6])
-{
-    double p[3] = {x[id], y[id], z[id]};
-    out[0] = p[0]; out[1] = p[1]; out[2] = p[2];
-    int f = fwd[id];
-    if (f > -1) {
-        double r2[3] = {x[f], y[f], z[f]};
-        if (geo.sph) sph_pwrap(geo, p, r2);
-        else pwrap_dev(geo, p, r2);
-        out[3] = rn_sub(r2[0], p[0]); out[4] = rn_sub(r2[1], p[1]); out[5] = rn_sub(r2[2], p[2]);
-        // the spherical fork leaves segments longer than 5 dl_max out (octree.c:316-322)
-        if (geo.sph && len3_ref(out[3], out[4], out[5]) > geo.sph_seg_max) out[3] = out[4] = out[5] = 0;
+    if (!mine) return;
+    // the leaf: one node, or at the deepest level the run sharing its key
+    const int ci = base + (L - cp - 1);
+    double lm;
+    if (SPH) {
+        double cb[3], ct[3];
+        sph_child_box(b, t, (int)((key >> dsh(g, L)) & 7), cb, ct);
+        lm = sph_box_lm(cb, ct);
     } else {
-        out[3] = out[4] = out[5] = 0;
+        lm = ldexp(g.root_lm, -L);
     }
-}
-
-__device__ __forceinline__ void finalize_cell(Cell64 *cells, int ci, const double s[6], int count)
-{
-    double inv = 1.0 / (double)count;
-    cells[ci].cx = rn_mul(s[0], inv);
-    cells[ci].cy = rn_mul(s[1], inv);
-    cells[ci].cz = rn_mul(s[2], inv);
-    cells[ci].qx = s[3];
-    cells[ci].qy = s[4];
-    cells[ci].qz = s[5];
-}
-
-// Leaves from the nodes, then each parent from its children by the last
-// child to arrive (one atomic per edge, no waiting).
-__global__ void k_moments(const uint64_t *__restrict__ keys, const int *__restrict__ order,
-                          const int *__restrict__ cpl, const int *__restrict__ cell_off, int *counters,
-                          const int *__restrict__ tt, KeyGeom g, int cap,
-                          const double *__restrict__ x, const double *__restrict__ y,
-                          const double *__restrict__ z, const int *__restrict__ fwd, Geometry geo,
-                          Cell64 *cells, const int *__restrict__ parent, const int *__restrict__ nchild,
-                          int *arrive, double *csum, int cap_cells)
-{
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    int nne_all = counters[TC_NNE];
-    if (s >= nne_all || s >= cap || cell_off[nne_all] > cap_cells) return;
-    const int *w = tt + key_member(g, keys[s]) * TT_WORDS;
-    const int st = w[TT_START], M = w[TT_M], nne = w[TT_NNE];
-    const int loc = s - st;
-    if (loc < 0 || loc >= M || nne < 2) return;
-    const int root = cell_off[st];
-    int cp = loc > 0 ? cpl[s - 1] : 0;
-    int cn = loc + 1 < M ? cpl[s] : 0;
-    int L = min(max(cp, cn) + 1, g.levels);
-    int leaf = cell_off[s] + (loc == 0) + (L - cp - 1);
-    int cnt = cells[leaf].count;
+    first[ci] = s;
+    lvl8[ci] = (uint8_t)L;
+    const int sh = dsh(g, L);
+    const int e = L == g.levels ? last_sharing(keys, s, st + M, sh, key >> sh) : s;
+    const int count = e - s + 1, next = cell_off[e + 1];   // the member's end of cells when e + 1 == st + M
     double acc[6];
-    if (cnt == 1) {
-        node_moment(order[s], x, y, z, fwd, geo, acc);
+    if (count == 1) {
+        load_moment(nm, order[s], acc);
     } else {
-        // deepest level still shared (depth overflow): sum its nodes
+        // depth overflow: sum its nodes in sorted order
         for (int k = 0; k < 6; ++k) acc[k] = 0;
-        for (int j = 0; j < cnt; ++j) {
-            double m[6];
-            node_moment(order[s + j], x, y, z, fwd, geo, m);
-            for (int k = 0; k < 6; ++k) acc[k] = rn_add(acc[k], m[k]);
+        for (int j = 0; j < count; ++j) {
+            double m6[6];
+            load_moment(nm, order[s + j], m6);
+            for (int k = 0; k < 6; ++k) acc[k] = rn_add(acc[k], m6[k]);
         }
-        if (loc > 0 && cpl[s - 1] >= L) return;   // only the first node of the run
+        store_psum(psum, ci, acc);
     }
-    for (int k = 0; k < 6; ++k) csum[6 * (size_t)leaf + k] = acc[k];
-    finalize_cell(cells, leaf, acc, cnt);
-    int cur = leaf;
-    for (int guard = 0; guard < 64; ++guard) {
-        int p = parent[cur];
-        if (p <= root) break;
-        // release this cell's sums, and (last child) acquire the siblings'
-        cuda::atomic_ref<int, cuda::thread_scope_device> arr(arrive[p]);
-        const int old = arr.fetch_add(1, cuda::memory_order_acq_rel);
-        if (old != nchild[p] - 1) break;
-        double sum[6] = {0, 0, 0, 0, 0, 0};
-        int end = __ldcg(&cells[p].next);
-        for (int ch = p + 1; ch != end && ch > 0; ch = __ldcg(&cells[ch].next)) {
-            for (int k = 0; k < 6; ++k) sum[k] = rn_add(sum[k], __ldcg(&csum[6 * (size_t)ch + k]));
+    store_cell(cells, ci, acc, count, lm, L, next, views);
+}
+
+// One level of the bottom-up moment sums (octree_update_means,
+// octree.c:264-283, here per subtree): every non-leaf cell of level `lev`
+// sums its children in child order (pre-order: ci + 1, then each child's
+// successor, until a cell that is not of level lev + 1), and takes its count
+// as theirs and its successor as the last child's.  The children are the
+// leaves of k_cells and the previous launch's level.  No atomics: the levels
+// are separate launches, deepest first.
+__global__ void k_level(int lev, const int *__restrict__ lvl_cnt, const int *__restrict__ lvl_list,
+                        const int *__restrict__ cell_off, int *counters, int cap_cells, Cell64 *__restrict__ cells,
+                        const uint8_t *__restrict__ lvl8, double *__restrict__ psum, CellViews views)
+{
+    __shared__ int sh_start;
+    const int n = lvl_cnt[lev];
+    if (n == 0) return;
+    const int ncell = cell_off[counters[TC_NNE]];
+    if (ncell > cap_cells) return;   // flagged by k_cells; the host grows the storage
+    if (threadIdx.x == 0) sh_start = level_start(lvl_cnt, lev);
+    __syncthreads();
+    const int start = sh_start;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int ci = start + i < cap_cells ? lvl_list[start + i] : -1;
+        if (ci <= 0 || ci >= ncell) { atomicOr(&counters[TC_ERR], OV_EW_BOUNDS); continue; }
+        const double lm = cells[ci].lm;
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        int ch = ci + 1, cnt = 0, nc = 0;
+        for (; nc < 8 && ch < ncell; ++nc) {
+            // the child's level, cell and position sum in one round trip
+            // (the sum is only used for a cell of more than one node)
+            const int lv = lvl8[ch];
+            const Cell64 c = cells[ch];
+            const double ps0 = psum[3 * (size_t)ch], ps1 = psum[3 * (size_t)ch + 1], ps2 = psum[3 * (size_t)ch + 2];
+            if (lv != lev + 1) break;
+            const bool one = c.count == 1;
+            acc[0] = rn_add(acc[0], one ? c.cx : ps0);
+            acc[1] = rn_add(acc[1], one ? c.cy : ps1);
+            acc[2] = rn_add(acc[2], one ? c.cz : ps2);
+            acc[3] = rn_add(acc[3], c.qx); acc[4] = rn_add(acc[4], c.qy); acc[5] = rn_add(acc[5], c.qz);
+            cnt += c.count;
+            if (c.next <= ch) { nc = 9; break; }
+            ch = c.next;
         }
-        for (int k = 0; k < 6; ++k) csum[6 * (size_t)p + k] = sum[k];
-        finalize_cell(cells, p, sum, __ldcg(&cells[p].count));
-        cur = p;
+        if (nc == 0 || nc > 8 || (nc == 8 && ch < ncell && lvl8[ch] == lev + 1)) {
+            atomicOr(&counters[TC_ERR], OV_EW_BOUNDS);
+            continue;
+        }
+        store_psum(psum, ci, acc);
+        store_cell(cells, ci, acc, cnt, lm, lev, ch, views);
     }
 }
 
 // Roots, one block per member: level-1 children plus the nodes outside the
 // root box; also the one-node and empty members.
 __global__ void k_root(const int *__restrict__ order, const int *__restrict__ cell_off, int *counters,
-                       int *tt, const double *__restrict__ x, const double *__restrict__ y,
-                       const double *__restrict__ z, const int *__restrict__ fwd, Geometry geo, KeyGeom g,
-                       Cell64 *cells, const double *csum, int *first, int cap_cells)
+                       int *tt, const double *__restrict__ nm, KeyGeom g, Cell64 *cells, const double *psum,
+                       int *first, int cap_cells, CellViews views)
 {
     __shared__ double red[6][256];
     int *w = tt + blockIdx.x * TT_WORDS;
@@ -528,10 +750,10 @@ __global__ void k_root(const int *__restrict__ order, const int *__restrict__ ce
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int j = threadIdx.x; j < nout; j += blockDim.x) {
         double m[6];
-        node_moment(order[st + M + j], x, y, z, fwd, geo, m);
+        load_moment(nm, order[st + M + j], m);
         for (int k = 0; k < 6; ++k) acc[k] = rn_add(acc[k], m[k]);
     }
-    if (nne == 1 && M == 1 && threadIdx.x == 0) node_moment(order[st], x, y, z, fwd, geo, acc);
+    if (nne == 1 && M == 1 && threadIdx.x == 0) load_moment(nm, order[st], acc);
     for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = acc[k];
     __syncthreads();
     for (int off = blockDim.x / 2; off > 0; off >>= 1) {
@@ -544,7 +766,7 @@ __global__ void k_root(const int *__restrict__ order, const int *__restrict__ ce
     for (int k = 0; k < 6; ++k) sum[k] = 0;
     if (nne >= 2) {
         for (int ch = root + 1; ch < end && ch > root; ch = cells[ch].next)
-            for (int k = 0; k < 6; ++k) sum[k] = rn_add(sum[k], csum[6 * (size_t)ch + k]);
+            add_cell_sums(cells[ch], psum, ch, sum);
     }
     for (int k = 0; k < 6; ++k) sum[k] = rn_add(sum[k], red[k][0]);
     Cell64 r;
@@ -557,54 +779,11 @@ __global__ void k_root(const int *__restrict__ order, const int *__restrict__ ce
     r.count = nne;
     cells[root] = r;
     first[root] = st;
-}
-
-// Double-single copy of every cell's centre of mass and circulation for
-// the OV_PREC_DD law: the centre of mass as its grid part (exact in FP32)
-// plus the rest (exact in FP64) as hi + lo floats, the circulation as hi + lo.
-__global__ void k_cellsff(const Cell64 *__restrict__ cells, const int *counters, double h, double inv_h,
-                          CellFF *__restrict__ out)
-{
-    int ci = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ci >= counters[TC_NCELL]) return;
-    const Cell64 c = cells[ci];
-    const double com[3] = {c.cx, c.cy, c.cz}, q[3] = {c.qx, c.qy, c.qz};
-    CellFF o;
-    for (int a = 0; a < 3; ++a) {
-        const double G = rint(com[a] * inv_h) * h;
-        const double f = com[a] - G;
-        o.g[a] = (float)G;
-        o.fh[a] = (float)f;
-        o.fl[a] = (float)(f - (double)o.fh[a]);
-        o.qh[a] = (float)q[a];
-        o.ql[a] = (float)(q[a] - (double)o.qh[a]);
-    }
-    o.pad = 0;
-    out[ci] = o;
-}
-
-// FP32 copy of every cell for the mixed traversal: COM split into a part on
-// the grid of step h (exact in FP32) and a small remainder.
-// The opening test Lm / d < theta becomes d^2 > (Lm / theta)^2: thr holds
-// that bound times (1 + 2e-5), rounded up, so that d^2 > thr accepts clear
-// of the guard band and d^2 < thr (1 - 2e-5) / (1 + 2e-5) opens clear of it.
-__global__ void k_cells32(const Cell64 *__restrict__ cells, const int *counters, double h, double inv_h,
-                          double theta, Cell32 *__restrict__ out)
-{
-    int ci = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ci >= counters[TC_NCELL]) return;
-    Cell64 c = cells[ci];
-    Cell32 o;
-    double cx = c.cx, cy = c.cy, cz = c.cz;
-    double gx = rint(cx * inv_h) * h, gy = rint(cy * inv_h) * h, gz = rint(cz * inv_h) * h;
-    o.gx = (float)gx; o.gy = (float)gy; o.gz = (float)gz;
-    const double r = c.lm / theta;
-    o.thr = theta > 0 ? __double2float_ru(r * r * (1.0 + 2e-5)) : __int_as_float(0x7f800000);
-    o.fx = (float)(cx - gx); o.fy = (float)(cy - gy); o.fz = (float)(cz - gz);
-    o.next = c.next;
-    o.qx = (float)c.qx; o.qy = (float)c.qy; o.qz = (float)c.qz;
-    o.lm = __double2float_ru(c.lm);
-    out[ci] = o;
+    const double c[3] = {r.cx, r.cy, r.cz}, q[3] = {r.qx, r.qy, r.qz};
+    if (views.c32)
+        write_cell32(views.c32, root, c, q, cell_thr(r.lm, views.theta), __double2float_ru(r.lm), r.next, views.h,
+                     views.inv_h);
+    if (views.cff) write_cellff(views.cff, root, c, q, views.h, views.inv_h);
 }
 
 }  // namespace
@@ -613,20 +792,20 @@ int ov_tree_reserve_cells(ov_ctx *c, int cells)
 {
     TreeBuf &t = c->tree;
     if (t.cap_cells >= cells && t.cells) return OV_OK;
-    void *ptrs[] = {t.cells, t.cells32, t.cellsff, t.parent, t.nchild, t.arrive, t.csum, t.first};
+    void *ptrs[] = {t.cells, t.cells32, t.cellsff, t.psum, t.first, t.lvl_list, t.lvl8};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    t.cells = nullptr; t.cells32 = nullptr; t.cellsff = nullptr; t.parent = t.nchild = t.arrive = t.first = nullptr;
-    t.csum = nullptr;
+    t.cells = nullptr; t.cells32 = nullptr; t.cellsff = nullptr; t.first = t.lvl_list = nullptr;
+    t.psum = nullptr;
+    t.lvl8 = nullptr;
     t.cap_cells = 0;
     OV_ALLOC(c, cudaMalloc(&t.cells, (size_t)cells * sizeof(Cell64)));
     OV_ALLOC(c, cudaMalloc(&t.cells32, (size_t)cells * sizeof(Cell32)));
     OV_ALLOC(c, cudaMalloc(&t.cellsff, (size_t)cells * sizeof(CellFF)));
-    OV_ALLOC(c, cudaMalloc(&t.parent, (size_t)cells * 4));
-    OV_ALLOC(c, cudaMalloc(&t.nchild, (size_t)cells * 4));
-    OV_ALLOC(c, cudaMalloc(&t.arrive, (size_t)cells * 4));
-    OV_ALLOC(c, cudaMalloc(&t.csum, (size_t)cells * 6 * 8));
+    OV_ALLOC(c, cudaMalloc(&t.psum, (size_t)cells * 3 * 8));
+    OV_ALLOC(c, cudaMalloc(&t.lvl8, (size_t)cells));
     OV_ALLOC(c, cudaMalloc(&t.first, (size_t)cells * 4));
+    OV_ALLOC(c, cudaMalloc(&t.lvl_list, (size_t)cells * 4));
     t.cap_cells = cells;
     return OV_OK;
 }
@@ -652,6 +831,15 @@ int ov_tree_reserve(ov_ctx *c, int cap)
     OV_ALLOC(c, cudaMalloc(&t.scan_tmp, (size_t)ov_scan_tmp_ints(cap) * 4));
     OV_ALLOC(c, cudaMalloc(&t.sort_hist, (size_t)ov_sort_hist_ints(cap) * 4));
     OV_ALLOC(c, cudaMalloc(&t.counters, TC_WORDS * 4));
+    OV_ALLOC(c, cudaMalloc(&t.lvl_cnt, 2 * TREE_LV_SLOTS * 4));
+    OV_ALLOC(c, cudaMalloc(&t.nm, n * 6 * 8));
+    OV_ALLOC(c, cudaMalloc(&t.lev_tab, 2 * TREE_LV_SLOTS * sizeof(float)));
+    OV_ALLOC(c, cudaMalloc(&t.inv_count, TREE_INV_COUNT * sizeof(double)));
+    {
+        std::vector<double> inv(TREE_INV_COUNT, 0.0);
+        for (int k = 1; k < TREE_INV_COUNT; ++k) inv[k] = 1.0 / (double)k;   // IEEE quotients, as on the device
+        OV_CUDA(c, cudaMemcpy(t.inv_count, inv.data(), TREE_INV_COUNT * sizeof(double), cudaMemcpyHostToDevice));
+    }
     OV_CUDA(c, cudaMemset(t.counters, 0, TC_WORDS * 4));
     // cells: about 1.3 per node for filament tangles (plus a root per
     // member); grown on demand
@@ -661,7 +849,7 @@ int ov_tree_reserve(ov_ctx *c, int cap)
 void ov_tree_free(TreeBuf &t)
 {
     void *ptrs[] = {t.keys, t.keys_alt, t.order, t.order_alt, t.torder, t.cpl, t.ncell_at, t.cell_off, t.scan_tmp,
-                    t.sort_hist, t.cells, t.cells32, t.cellsff, t.parent, t.nchild, t.arrive, t.csum, t.first,
+                    t.sort_hist, t.cells, t.cells32, t.cellsff, t.psum, t.first, t.lvl_list, t.lvl8, t.lvl_cnt, t.nm, t.lev_tab, t.inv_count,
                     t.counters, t.tt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -678,6 +866,7 @@ static KeyGeom key_geom(const ov_ctx *c)
         g.hi[a] = geo.hi[a];
         g.L[a] = geo.L[a];
         g.invL[a] = 1.0 / geo.L[a];
+        g.invL62[a] = ldexp(g.invL[a], 62);
         // bound on how far the reference's rounded faces (21 levels) and the
         // fixed-point image (a subtraction, a product with the rounded 1/L)
         // may sit from the exact dyadic faces, in box units
@@ -717,42 +906,46 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     OV_CUDA(c, cudaMemsetAsync(t.counters, 0, TC_BUILD_CLEAR * 4, s));
     OV_CUDA(c, cudaMemsetAsync(t.counters + TC_STAT64, 0, (TC_WORDS - TC_STAT64) * 4, s));
     OV_CUDA(c, cudaMemsetAsync(t.tt, 0, (size_t)nt * TT_WORDS * 4, s));
-    OV_CUDA(c, cudaMemsetAsync(t.nchild, 0, (size_t)t.cap_cells * 4, s));
+    OV_CUDA(c, cudaMemsetAsync(t.lvl_cnt, 0, 2 * TREE_LV_SLOTS * 4, s));
     int nb = (cap + 255) / 256;
     if (c->geo.sph)
         k_keys<true><<<nb, 256, 0, s>>>(c->status, na.x, na.y, na.z, nt > 1 ? c->d_tid : nullptr, cap, g, t.keys,
-                                        t.order, t.counters, t.tt);
+                                        t.order, t.counters, t.tt, c->fwd, c->geo, t.nm);
     else
         k_keys<false><<<nb, 256, 0, s>>>(c->status, na.x, na.y, na.z, nt > 1 ? c->d_tid : nullptr, cap, g, t.keys,
-                                         t.order, t.counters, t.tt);
-    k_layout<<<1, 32, 0, s>>>(t.tt, nt, c->d_qorder, t.counters);
+                                         t.order, t.counters, t.tt, c->fwd, c->geo, t.nm);
+    k_layout<<<1, 32, 0, s>>>(t.tt, nt, c->d_qorder, t.counters, t.lev_tab, g.root_lm, c->params.bh_resolution);
     c->launches += 2;
     ov_sort_keys(c, t, cap, s);
-    k_cpl<<<nb, 256, 0, s>>>(t.keys, cap, t.counters, t.tt, g, t.cpl, t.ncell_at);
+    k_cpl<<<nb, 256, 0, s>>>(t.keys, cap, t.counters, t.tt, g, t.cpl, t.ncell_at, t.lvl_cnt);
     k_target_order<<<nb, 256, 0, s>>>(t.keys, t.order, cap, t.counters, t.tt, g, t.torder);
     c->launches += 2;
     ov_scan_exclusive(c, t.ncell_at, t.cell_off, cap, t.counters + TC_NNE, 0, t.scan_tmp, s);
+    CellViews views;
+    const bool fp32_view = c->precision == OV_PREC_MIXED || c->precision == OV_PREC_DD || c->walk == OV_WALK_SPLIT;
+    views.c32 = fp32_view ? t.cells32 : nullptr;
+    views.cff = c->precision == OV_PREC_DD ? t.cellsff : nullptr;
+    views.h = c->grid_h;
+    views.inv_h = 1.0 / c->grid_h;
+    views.theta = c->params.bh_resolution;
+    views.inv_count = t.inv_count;
+    views.lev_tab = c->geo.sph ? nullptr : t.lev_tab;
     if (c->geo.sph)
-        k_cells<true><<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.parent,
-                                         t.nchild, t.arrive, t.first, t.cap_cells);
+        k_cells<true><<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.first,
+                                         t.lvl8, t.lvl_cnt, t.lvl_list, t.cap_cells, t.order, t.nm, t.psum,
+                                         views);
     else
-        k_cells<false><<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.parent,
-                                          t.nchild, t.arrive, t.first, t.cap_cells);
-    k_moments<<<nb, 256, 0, s>>>(t.keys, t.order, t.cpl, t.cell_off, t.counters, t.tt, g, cap, na.x, na.y, na.z,
-                                 c->fwd, c->geo, t.cells, t.parent, t.nchild, t.arrive, t.csum, t.cap_cells);
-    k_root<<<nt, 256, 0, s>>>(t.order, t.cell_off, t.counters, t.tt, na.x, na.y, na.z, c->fwd, c->geo, g, t.cells,
-                              t.csum, t.first, t.cap_cells);
-    c->launches += 3;
-    if (c->precision == OV_PREC_MIXED || c->precision == OV_PREC_DD || c->walk == OV_WALK_SPLIT) {
-        k_cells32<<<(t.cap_cells + 255) / 256, 256, 0, s>>>(t.cells, t.counters, c->grid_h, 1.0 / c->grid_h,
-                                                           c->params.bh_resolution, t.cells32);
-        c->launches++;
-    }
-    if (c->precision == OV_PREC_DD) {
-        k_cellsff<<<(t.cap_cells + 255) / 256, 256, 0, s>>>(t.cells, t.counters, c->grid_h, 1.0 / c->grid_h,
-                                                           t.cellsff);
-        c->launches++;
-    }
+        k_cells<false><<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.first,
+                                          t.lvl8, t.lvl_cnt, t.lvl_list, t.cap_cells, t.order, t.nm, t.psum,
+                                          views);
+    // deepest level first; a level without cells returns at once
+    const int lvl_grid = 4 * c->sm_count;
+    for (int lev = g.levels - 1; lev >= 1; --lev)
+        k_level<<<lvl_grid, 256, 0, s>>>(lev, t.lvl_cnt, t.lvl_list, t.cell_off, t.counters, t.cap_cells, t.cells,
+                                         t.lvl8, t.psum, views);
+    k_root<<<nt, 256, 0, s>>>(t.order, t.cell_off, t.counters, t.tt, t.nm, g, t.cells, t.psum, t.first, t.cap_cells,
+                              views);
+    c->launches += 1 + g.levels;
     OV_CUDA(c, cudaGetLastError());
     return OV_OK;
 }
