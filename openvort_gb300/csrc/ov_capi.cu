@@ -135,6 +135,19 @@ static void free_nodes(NodeArrays &a)
 // Free every device and pinned buffer of the context and forget their sizes
 // (streams, events and parameters stay): what the context holds after it is
 // what it held when created.
+// Destroy the captured graphs (buffers, layout or sizes changed).
+static void ov_drop_graphs(ov_ctx *c)
+{
+    if (c->rk4_exec) cudaGraphExecDestroy(c->rk4_exec);
+    c->rk4_exec = nullptr;
+    c->rk4_key = 0;
+    for (int i = 0; i < 4; ++i) {
+        if (c->eval_exec[i]) cudaGraphExecDestroy(c->eval_exec[i]);
+        c->eval_exec[i] = nullptr;
+        c->eval_key[i] = 0;
+    }
+}
+
 static void release_buffers(ov_ctx *c)
 {
     cudaStreamSynchronize(c->stream);
@@ -152,9 +165,7 @@ static void release_buffers(ov_ctx *c)
     void *pinned[] = {c->h_stage, c->h_corr, c->h_pf, c->h_time};
     for (void *p : pinned)
         if (p) cudaFreeHost(p);
-    if (c->rk4_exec) cudaGraphExecDestroy(c->rk4_exec);
-    c->rk4_exec = nullptr;
-    c->rk4_key = 0;
+    ov_drop_graphs(c);
     c->fwd = c->rev = c->status = c->pin = c->dnodes = c->d_tid = c->d_qorder = nullptr;
     c->d_tprm = nullptr;
     c->d_mrange = nullptr;
@@ -347,7 +358,7 @@ static int ensure_capacity(ov_ctx *c, int cap)
     int *is[] = {c->fwd, c->rev, c->status, c->pin};
     for (int *p : is)
         if (p) cudaFree(p);
-    if (c->rk4_exec) { cudaGraphExecDestroy(c->rk4_exec); c->rk4_exec = nullptr; }
+    ov_drop_graphs(c);
     int r;
     if ((r = alloc_nodes(c, c->node, cap))) return r;
     for (auto &s : c->stage)
@@ -393,7 +404,7 @@ int ov_grow_preserving(ov_ctx *c, int cap)
     int r;
     for (auto &s : c->stage)
         if ((r = alloc_nodes(c, s, cap))) return r;
-    if (c->rk4_exec) { cudaGraphExecDestroy(c->rk4_exec); c->rk4_exec = nullptr; }
+    ov_drop_graphs(c);
     if ((r = ov_tree_reserve(c, cap))) return r;
     c->cap = cap;
     return OV_OK;
@@ -548,7 +559,7 @@ int ov_upload_member_tables(ov_ctx *c)
     if (nt > 1)
         while ((1 << c->key_tbits) <= nt) ++c->key_tbits;
     c->key_levels = std::min(OV_MAX_LEVEL, (63 - c->key_tbits) / 3);
-    c->rk4_key = 0;   // the graph bakes the layout in
+    ov_drop_graphs(c);   // the graphs bake the layout in
     std::vector<DevParams> prm(nt);
     std::vector<int> q(nt);
     std::vector<int2> rng(nt);
@@ -907,34 +918,86 @@ static int clear_call_words(ov_ctx *c)
 // ph[2] -> ph[3].
 static int eval_async(ov_ctx *c, NodeArrays &na, double t, bool tangents, cudaStream_t s)
 {
-    bool ph = c->phase_timing && c->time_dev_index < 0;
-    if (ph) OV_CUDA(c, cudaEventRecord(c->ph[0], s));
+    // phase events: plain records, or event-record nodes of the
+    // single-evaluation graph (time slot 5); none inside the RK4 graph
+    const bool in_graph = c->time_dev_index == 5;
+    const bool ph = c->phase_timing && (c->time_dev_index < 0 || in_graph);
+    const unsigned ev_flags = in_graph ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if (ph) OV_CUDA(c, cudaEventRecordWithFlags(c->ph[0], s, ev_flags));
     if (tangents) {
         OV_CUDA(c, cudaEventRecord(c->fork_ev, s));
         OV_CUDA(c, cudaStreamWaitEvent(c->side, c->fork_ev, 0));
         ov_launch_tangents(c, na, c->side);
-        if (ph) OV_CUDA(c, cudaEventRecord(c->ph[1], c->side));
+        if (ph) OV_CUDA(c, cudaEventRecordWithFlags(c->ph[1], c->side, ev_flags));
         OV_CUDA(c, cudaEventRecord(c->join_ev, c->side));
     } else if (ph) {
-        OV_CUDA(c, cudaEventRecord(c->ph[1], s));
+        OV_CUDA(c, cudaEventRecordWithFlags(c->ph[1], s, ev_flags));
     }
     int r = ov_tree_build(c, na, s);
     if (r) return r;
-    if (ph) OV_CUDA(c, cudaEventRecord(c->ph[2], s));
+    if (ph) OV_CUDA(c, cudaEventRecordWithFlags(c->ph[2], s, ev_flags));
     if (tangents) OV_CUDA(c, cudaStreamWaitEvent(s, c->join_ev, 0));
     if ((r = ov_launch_velocities(c, na, t, c->precision, s))) return r;
-    if (ph) OV_CUDA(c, cudaEventRecord(c->ph[3], s));
+    if (ph) OV_CUDA(c, cudaEventRecordWithFlags(c->ph[3], s, ev_flags));
     OV_CUDA(c, cudaGetLastError());
     return OV_OK;
 }
 
+extern "C" {
+static unsigned long long graph_key(ov_ctx *c);
+}
+
+// One evaluation of the context's nodes as a captured graph (captured on
+// first use and again whenever the key changes; the time comes from
+// d_time[5]): one launch instead of the forty-odd kernels of the tree build
+// and traversal.
+static int eval_graph(ov_ctx *c, double t, bool tangents, cudaStream_t s)
+{
+    if (!c->d_time) {
+        OV_ALLOC(c, cudaMalloc(&c->d_time, 8 * sizeof(double)));
+        OV_ALLOC(c, cudaMallocHost(&c->h_time, 8 * sizeof(double)));
+    }
+    int r = ov_reserve_velocity_scratch(c);
+    if (r) return r;
+    c->h_time[5] = t;
+    OV_CUDA(c, cudaMemcpyAsync(c->d_time + 5, c->h_time + 5, sizeof(double), cudaMemcpyHostToDevice, s));
+    const int gi = (tangents ? 1 : 0) + (c->phase_timing ? 2 : 0);
+    const unsigned long long key = graph_key(c);
+    if (!c->eval_exec[gi] || key != c->eval_key[gi]) {
+        if (c->eval_exec[gi]) { cudaGraphExecDestroy(c->eval_exec[gi]); c->eval_exec[gi] = nullptr; }
+        cudaGraph_t g = nullptr;
+        OV_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        c->time_dev_index = 5;
+        const int64_t l0 = c->launches;
+        r = eval_async(c, c->node, t, tangents, s);
+        c->eval_kernels[gi] = c->launches - l0;
+        c->launches = l0;
+        c->time_dev_index = -1;
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (r) { if (g) cudaGraphDestroy(g); return r; }
+        if (e != cudaSuccess) return ov_fail(c, OV_ERR_CUDA, "evaluation graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c->eval_exec[gi], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess)
+            return ov_fail(c, OV_ERR_CUDA, "evaluation graph instantiate: %s", cudaGetErrorString(e));
+        c->eval_key[gi] = key;
+    }
+    OV_CUDA(c, cudaGraphLaunch(c->eval_exec[gi], s));
+    c->launches += c->eval_kernels[gi];
+    return OV_OK;
+}
+
 // Evaluate, growing the cell storage and re-running when the tree did not fit.
+// The context's own nodes go through the evaluation graph unless node
+// counting (host-side per-call work) is on.
 int ov_eval_sync(ov_ctx *c, NodeArrays &na, double t, bool tangents)
 {
     int r;
+    const bool graph = c->use_graph && !c->count_nodes && &na == &c->node;
     for (int attempt = 0; attempt < 3; ++attempt) {
         if ((r = clear_call_words(c))) return r;
-        if ((r = eval_async(c, na, t, tangents, c->stream))) return r;
+        if ((r = graph ? eval_graph(c, t, tangents, c->stream) : eval_async(c, na, t, tangents, c->stream)))
+            return r;
         if ((r = collect_stats(c, true))) return r;
         if (!(c->stats.error_word & OV_EW_CELLS)) return error_from_word(c);
         int need = 0;

@@ -99,7 +99,8 @@ struct TreeBuf {
     uint8_t *lvl8 = nullptr;     // level of each cell (0 for roots)
     int *first = nullptr;        // first sorted position of each cell's nodes
     int *lvl_list = nullptr;     // non-root cells grouped by level (ascending levels)
-    int *lvl_cnt = nullptr;      // TREE_LV_SLOTS cells per level, then as many fill counters
+    int *lvl_cnt = nullptr;      // TREE_LV_SLOTS cells per level, as many fill counters, then the
+                                 // level sums' grid-barrier counter
     double *nm = nullptr;        // 6 doubles per node slot: position, wrapped forward segment
     double *inv_count = nullptr; // TREE_INV_COUNT entries: 1 / k, rounded (entry 0 unused)
     float *lev_tab = nullptr;    // per level: FP32 opening threshold and Lm of a box cell
@@ -247,9 +248,15 @@ struct ov_ctx {
     int loop_cap = 0, loop_nodes_cap = 0;
     size_t loop_buf_cap = 0;
     // RK4 graph: stage times and steps live in d_time = {t+dt/2, t+dt/2,
-    // t+dt, dt/2, dt}; kernels read them when time_dev_index >= 0
+    // t+dt, dt/2, dt, t of a single evaluation}; kernels read them when
+    // time_dev_index >= 0
     cudaGraphExec_t rk4_exec = nullptr;
     unsigned long long rk4_key = 0;
+    // single-evaluation graphs (tangents + tree + traversal of the context's
+    // nodes): index 1 with the tangents, + 2 with phase events
+    cudaGraphExec_t eval_exec[4] = {nullptr, nullptr, nullptr, nullptr};
+    unsigned long long eval_key[4] = {0, 0, 0, 0};
+    int64_t eval_kernels[4] = {0, 0, 0, 0};
     double *d_time = nullptr;
     double *h_time = nullptr;
     int time_dev_index = -1;

@@ -15,9 +15,12 @@
 namespace {
 
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;                       // items per thread
-constexpr int kTile = kSortThreads * kSortItems;     // 4096 slots per block
 constexpr int kWarps = kSortThreads / 32;
+// Items per thread: 16 (4096-slot tiles), or 4 (1024-slot tiles) when the
+// slots are few enough that 4096-slot tiles would leave most SMs idle.
+constexpr int kItemsLarge = 16, kItemsSmall = 4;
+constexpr int kSmallSortSlots = 1 << 19;
+__host__ __device__ constexpr int sort_tile(int items) { return kSortThreads * items; }
 
 // Exclusive scan of one int per thread over the block (blockDim a multiple
 // of 32, at most 1024); total gets the block's sum.
@@ -52,9 +55,11 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int &total)
 // + tile]); with tot, also the totals of all four digits over every key,
 // which the later passes' digit offsets start from (the keys of a pass are
 // a permutation of the first pass's).  Same-digit lanes of a warp add once.
+template <int kSortItems>
 __global__ void rs_hist(const uint64_t *__restrict__ keys, int n, int shift, int ntiles,
                         int *__restrict__ hist, int *__restrict__ tot)
 {
+    constexpr int kTile = sort_tile(kSortItems);
     __shared__ int h[4][256];
     const int np = tot ? 4 : 1;
     for (int i = threadIdx.x; i < np * 256; i += blockDim.x) (&h[0][0])[i] = 0;
@@ -112,10 +117,12 @@ __global__ void rs_rowscan(int *__restrict__ hist, int ntiles, const int *__rest
 // and a running per-(warp,digit) counter hands out ranks.  The tile is put in
 // digit order in shared memory first, so that each digit's run is written
 // out by consecutive threads (keys, then the ids through the same buffer).
+template <int kSortItems>
 __global__ void rs_scatter(const uint64_t *__restrict__ kin, const int *__restrict__ vin,
                            uint64_t *__restrict__ kout, int *__restrict__ vout, int n, int shift,
                            int ntiles, const int *__restrict__ hist)
 {
+    constexpr int kTile = sort_tile(kSortItems);
     __shared__ uint64_t sk[kTile];        // the tile in digit order (keys, then ids)
     __shared__ uint8_t sd[kTile];         // digit of each staged slot
     __shared__ int wc[kWarps][256];
@@ -289,19 +296,20 @@ void ov_scan_exclusive(ov_ctx *c, const int *in, int *out, int n_max, const int 
 // Radix sort of t.keys / t.order (n slots): per pass a tile histogram, the
 // digit offsets (one block per digit) and the scatter; the digit totals of
 // all passes come with the first histogram.
-void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
+template <int kSortItems>
+static void sort_passes(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
 {
-    if (n <= 0) return;
-    int ntiles = (n + kTile - 1) / kTile;
+    const int ntiles = (n + sort_tile(kSortItems) - 1) / sort_tile(kSortItems);
     uint64_t *ka = t.keys, *kb = t.keys_alt;
     int *va = t.order, *vb = t.order_alt;
     int *tot = t.sort_hist + 256 * (size_t)ntiles;   // 4 x 256 digit totals
     cudaMemsetAsync(tot, 0, 4 * 256 * sizeof(int), s);
     for (int pass = 0; pass < 4; ++pass) {
         int shift = 32 + 8 * pass;
-        rs_hist<<<ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, t.sort_hist, pass == 0 ? tot : nullptr);
+        rs_hist<kSortItems><<<ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, t.sort_hist,
+                                                           pass == 0 ? tot : nullptr);
         rs_rowscan<<<256, kSortThreads, 0, s>>>(t.sort_hist, ntiles, tot + 256 * pass);
-        rs_scatter<<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, ntiles, t.sort_hist);
+        rs_scatter<kSortItems><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, ntiles, t.sort_hist);
         c->launches += 3;
         uint64_t *tk = ka; ka = kb; kb = tk;
         int *tv = va; va = vb; vb = tv;
@@ -311,7 +319,18 @@ void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
     c->launches += 1;
 }
 
-int ov_sort_hist_ints(int cap) { return 256 * ((cap + kTile - 1) / kTile) + 4 * 256; }
+void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
+{
+    if (n <= 0) return;
+    if (n <= kSmallSortSlots) sort_passes<kItemsSmall>(c, t, n, s);
+    else sort_passes<kItemsLarge>(c, t, n, s);
+}
+
+int ov_sort_hist_ints(int cap)
+{
+    const int tile = cap <= kSmallSortSlots ? sort_tile(kItemsSmall) : sort_tile(kItemsLarge);
+    return 256 * ((cap + tile - 1) / tile) + 4 * 256;
+}
 
 // out[i] = add + sum(in[0..i)) for i in [0, n], n = min(*n_dev, n_max).
 void ov_scan_exclusive(ov_ctx *c, const int *in, int *out, int n_max, const int *n_dev, int add,

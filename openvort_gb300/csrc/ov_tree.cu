@@ -679,53 +679,99 @@ __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict
     store_cell(cells, ci, acc, count, lm, L, next, views);
 }
 
-// One level of the bottom-up moment sums (octree_update_means,
-// octree.c:264-283, here per subtree): every non-leaf cell of level `lev`
-// sums its children in child order (pre-order: ci + 1, then each child's
-// successor, until a cell that is not of level lev + 1), and takes its count
-// as theirs and its successor as the last child's.  The children are the
-// leaves of k_cells and the previous launch's level.  No atomics: the levels
-// are separate launches, deepest first.
-__global__ void k_level(int lev, const int *__restrict__ lvl_cnt, const int *__restrict__ lvl_list,
-                        const int *__restrict__ cell_off, int *counters, int cap_cells, Cell64 *__restrict__ cells,
-                        const uint8_t *__restrict__ lvl8, double *__restrict__ psum, CellViews views)
+// Grid-wide barrier of the cooperative k_levels (all blocks resident): one
+// arrival per block on a counter cleared by the build, then a bounded wait
+// for the epoch's total.  A wait that runs out sets OV_EW_ITER and returns
+// false in every thread of the block, which then leaves the kernel.
+constexpr unsigned kBarrierSpins = 1u << 22;   // of at least 64 ns each
+
+__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned epoch, int *counters)
 {
-    __shared__ int sh_start;
-    const int n = lvl_cnt[lev];
-    if (n == 0) return;
-    const int ncell = cell_off[counters[TC_NNE]];
-    if (ncell > cap_cells) return;   // flagged by k_cells; the host grows the storage
-    if (threadIdx.x == 0) sh_start = level_start(lvl_cnt, lev);
     __syncthreads();
-    const int start = sh_start;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int ci = start + i < cap_cells ? lvl_list[start + i] : -1;
-        if (ci <= 0 || ci >= ncell) { atomicOr(&counters[TC_ERR], OV_EW_BOUNDS); continue; }
-        const double lm = cells[ci].lm;
-        double acc[6] = {0, 0, 0, 0, 0, 0};
-        int ch = ci + 1, cnt = 0, nc = 0;
-        for (; nc < 8 && ch < ncell; ++nc) {
-            // the child's level, cell and position sum in one round trip
-            // (the sum is only used for a cell of more than one node)
-            const int lv = lvl8[ch];
-            const Cell64 c = cells[ch];
-            const double ps0 = psum[3 * (size_t)ch], ps1 = psum[3 * (size_t)ch + 1], ps2 = psum[3 * (size_t)ch + 2];
-            if (lv != lev + 1) break;
-            const bool one = c.count == 1;
-            acc[0] = rn_add(acc[0], one ? c.cx : ps0);
-            acc[1] = rn_add(acc[1], one ? c.cy : ps1);
-            acc[2] = rn_add(acc[2], one ? c.cz : ps2);
-            acc[3] = rn_add(acc[3], c.qx); acc[4] = rn_add(acc[4], c.qy); acc[5] = rn_add(acc[5], c.qz);
-            cnt += c.count;
-            if (c.next <= ch) { nc = 9; break; }
-            ch = c.next;
+    int ok = 1;
+    if (threadIdx.x == 0) {
+        __threadfence();   // this block's sums before the arrival
+        atomicAdd(count, 1u);
+        const unsigned target = (epoch + 1) * gridDim.x;
+        unsigned spins = 0;
+        while (atomicAdd(count, 0u) < target) {
+            if (++spins > kBarrierSpins) {
+                atomicOr(&counters[TC_ERR], OV_EW_ITER);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
         }
-        if (nc == 0 || nc > 8 || (nc == 8 && ch < ncell && lvl8[ch] == lev + 1)) {
-            atomicOr(&counters[TC_ERR], OV_EW_BOUNDS);
-            continue;
+        __threadfence();   // the other blocks' sums after it
+    }
+    return __syncthreads_and(ok) != 0;
+}
+
+// One non-leaf cell of the bottom-up moment sums (octree_update_means,
+// octree.c:264-283, here per subtree): the sum of its children in child
+// order (pre-order: ci + 1, then each child's successor, until a cell that
+// is not of level lev + 1); its count is theirs and its successor the last
+// child's.
+__device__ __forceinline__ void level_cell(int ci, int lev, int ncell, int *counters, Cell64 *__restrict__ cells,
+                                           const uint8_t *__restrict__ lvl8, double *__restrict__ psum,
+                                           const CellViews &views)
+{
+    if (ci <= 0 || ci >= ncell) { atomicOr(&counters[TC_ERR], OV_EW_BOUNDS); return; }
+    const double lm = __ldcg(&cells[ci].lm);
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    int ch = ci + 1, cnt = 0, nc = 0;
+    for (; nc < 8 && ch < ncell; ++nc) {
+        // the child's level, cell and position sum in one round trip (the
+        // sum is only used for a cell of more than one node); L2 loads: the
+        // children of the previous level were written in this launch
+        const int lv = __ldcg(&lvl8[ch]);
+        const double2 *cc = reinterpret_cast<const double2 *>(cells + ch);
+        const double2 c0 = __ldcg(cc), c1 = __ldcg(cc + 1), c2 = __ldcg(cc + 2);
+        const int4 c3 = __ldcg(reinterpret_cast<const int4 *>(cells + ch) + 3);
+        const double ps0 = __ldcg(&psum[3 * (size_t)ch]), ps1 = __ldcg(&psum[3 * (size_t)ch + 1]),
+                     ps2 = __ldcg(&psum[3 * (size_t)ch + 2]);
+        if (lv != lev + 1) break;
+        const int ccount = c3.w, cnext = c3.z;
+        const bool one = ccount == 1;
+        acc[0] = rn_add(acc[0], one ? c0.x : ps0);
+        acc[1] = rn_add(acc[1], one ? c0.y : ps1);
+        acc[2] = rn_add(acc[2], one ? c1.x : ps2);
+        acc[3] = rn_add(acc[3], c1.y); acc[4] = rn_add(acc[4], c2.x); acc[5] = rn_add(acc[5], c2.y);
+        cnt += ccount;
+        if (cnext <= ch) { nc = 9; break; }
+        ch = cnext;
+    }
+    if (nc == 0 || nc > 8 || (nc == 8 && ch < ncell && __ldcg(&lvl8[ch]) == lev + 1)) {
+        atomicOr(&counters[TC_ERR], OV_EW_BOUNDS);
+        return;
+    }
+    store_psum(psum, ci, acc);
+    store_cell(cells, ci, acc, cnt, lm, lev, ch, views);
+}
+
+// The bottom-up sums of every non-leaf cell, deepest level first, in one
+// cooperative launch: the blocks share each level's list, then meet at a
+// grid barrier (levels without cells are skipped by every block alike).
+// The leaves were finished by k_cells.
+__global__ void k_levels(int lev_hi, const int *__restrict__ lvl_cnt, const int *__restrict__ lvl_list,
+                         unsigned *barrier, const int *__restrict__ cell_off, int *counters, int cap_cells,
+                         Cell64 *__restrict__ cells, const uint8_t *__restrict__ lvl8, double *__restrict__ psum,
+                         CellViews views)
+{
+    const int ncell = cell_off[counters[TC_NNE]];
+    if (ncell > cap_cells) return;   // flagged by k_cells; the host grows the storage (every block alike)
+    int start = 0;
+    for (int l = 0; l <= lev_hi; ++l) start += lvl_cnt[l];
+    unsigned epoch = 0;
+    for (int lev = lev_hi; lev >= 1; --lev) {
+        const int n = lvl_cnt[lev];
+        start -= n;   // level lev's list is [start, start + n)
+        if (n == 0) continue;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+            const int ci = start + i < cap_cells ? lvl_list[start + i] : -1;
+            level_cell(ci, lev, ncell, counters, cells, lvl8, psum, views);
         }
-        store_psum(psum, ci, acc);
-        store_cell(cells, ci, acc, cnt, lm, lev, ch, views);
+        if (lev > 1 && !grid_barrier(barrier, epoch++, counters)) return;
     }
 }
 
@@ -831,7 +877,7 @@ int ov_tree_reserve(ov_ctx *c, int cap)
     OV_ALLOC(c, cudaMalloc(&t.scan_tmp, (size_t)ov_scan_tmp_ints(cap) * 4));
     OV_ALLOC(c, cudaMalloc(&t.sort_hist, (size_t)ov_sort_hist_ints(cap) * 4));
     OV_ALLOC(c, cudaMalloc(&t.counters, TC_WORDS * 4));
-    OV_ALLOC(c, cudaMalloc(&t.lvl_cnt, 2 * TREE_LV_SLOTS * 4));
+    OV_ALLOC(c, cudaMalloc(&t.lvl_cnt, 3 * TREE_LV_SLOTS * 4));
     OV_ALLOC(c, cudaMalloc(&t.nm, n * 6 * 8));
     OV_ALLOC(c, cudaMalloc(&t.lev_tab, 2 * TREE_LV_SLOTS * sizeof(float)));
     OV_ALLOC(c, cudaMalloc(&t.inv_count, TREE_INV_COUNT * sizeof(double)));
@@ -906,7 +952,7 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     OV_CUDA(c, cudaMemsetAsync(t.counters, 0, TC_BUILD_CLEAR * 4, s));
     OV_CUDA(c, cudaMemsetAsync(t.counters + TC_STAT64, 0, (TC_WORDS - TC_STAT64) * 4, s));
     OV_CUDA(c, cudaMemsetAsync(t.tt, 0, (size_t)nt * TT_WORDS * 4, s));
-    OV_CUDA(c, cudaMemsetAsync(t.lvl_cnt, 0, 2 * TREE_LV_SLOTS * 4, s));
+    OV_CUDA(c, cudaMemsetAsync(t.lvl_cnt, 0, 3 * TREE_LV_SLOTS * 4, s));
     int nb = (cap + 255) / 256;
     if (c->geo.sph)
         k_keys<true><<<nb, 256, 0, s>>>(c->status, na.x, na.y, na.z, nt > 1 ? c->d_tid : nullptr, cap, g, t.keys,
@@ -938,14 +984,24 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
         k_cells<false><<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.first,
                                           t.lvl8, t.lvl_cnt, t.lvl_list, t.cap_cells, t.order, t.nm, t.psum,
                                           views);
-    // deepest level first; a level without cells returns at once
-    const int lvl_grid = 4 * c->sm_count;
-    for (int lev = g.levels - 1; lev >= 1; --lev)
-        k_level<<<lvl_grid, 256, 0, s>>>(lev, t.lvl_cnt, t.lvl_list, t.cell_off, t.counters, t.cap_cells, t.cells,
-                                         t.lvl8, t.psum, views);
+    {
+        // the level sums: one cooperative launch, every block resident
+        static int per_sm = 0;
+        if (!per_sm) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_levels, 256, 0);
+            per_sm = per_sm > 0 ? per_sm : 1;
+        }
+        const int want = std::max(1, cap / 1024);   // about four non-leaf cells a thread on the fullest level
+        const int grid = std::max(1, std::min(per_sm * c->sm_count, want));
+        int lev_hi = g.levels - 1;
+        unsigned *barrier = reinterpret_cast<unsigned *>(t.lvl_cnt + 2 * TREE_LV_SLOTS);
+        void *args[] = {&lev_hi, &t.lvl_cnt, &t.lvl_list, &barrier, &t.cell_off, &t.counters, &t.cap_cells,
+                        &t.cells, &t.lvl8, &t.psum, &views};
+        OV_CUDA(c, cudaLaunchCooperativeKernel((const void *)k_levels, grid, 256, args, 0, s));
+    }
     k_root<<<nt, 256, 0, s>>>(t.order, t.cell_off, t.counters, t.tt, t.nm, g, t.cells, t.psum, t.first, t.cap_cells,
                               views);
-    c->launches += 1 + g.levels;
+    c->launches += 3;
     OV_CUDA(c, cudaGetLastError());
     return OV_OK;
 }

@@ -5,9 +5,10 @@ ov_direct_velocities on the same tangle.
 
 The caller owns every buffer here: torch allocates the inputs and outputs,
 and the entry point itself allocates nothing (the device's free memory is
-the same before and after a call).  Two calls in a row with different node
-lists must both match, which also shows that the working array the calls
-share carries nothing over from one call to the next.  An EMPTY slot in the
+the same before and after a call).  The reference's own direct-sum golden
+vectors are matched with its tangents and normals handed in.  Two calls in a
+row with different node lists must both match, which also shows that the
+working array the calls share carries nothing over from one call to the next.  An EMPTY slot in the
 list gives zeros, as the allocating call gives.  A wall geometry with mirror
 images runs with no superfluid-velocity output (d_vs NULL).  This file sorts
 last so that a run stopping at the first failure has run every other test
@@ -21,7 +22,7 @@ import numpy as np
 import pytest
 
 from openvort_gb300 import abi, gpu, workloads as W
-from tests._util import node_rel_err
+from tests._util import host_from_arrays, node_rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -136,6 +137,23 @@ def test_noalloc_direct_sum_matches_allocating_entry_point():
     big = torch.zeros(MAX_NODES + 1, dtype=torch.int32, device=c.dev)
     out = torch.zeros((MAX_NODES + 1, 3), dtype=torch.float64, device=c.dev)
     assert c.launch(big, MAX_NODES + 1, out, None) == 1   # OV_ERR_ARG
+
+
+def test_noalloc_matches_reference_golden(golden):
+    """OpenVort's own direct-sum velocities (147 nodes of the 1,024-node
+    random-walk golden, periodic_26), with the reference's tangents and
+    normals handed in as the caller's arrays."""
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    g = golden("rw16x64.npz")
+    ht = host_from_arrays(g)
+    ht.tangents[:] = g["tangents"]
+    ht.normals[:] = g["normals"]
+    c = _Caller(torch, ht, W.config_params("rw"))
+    nodes = np.asarray(g["direct_nodes"], dtype=np.int32)
+    v, s = c.call(nodes)
+    assert node_rel_err(v, g["direct_vels"]) < FP64_TOL
+    assert node_rel_err(s, g["direct_vs"]) < FP64_TOL
 
 
 def test_noalloc_mirror_images_without_vs_output():
