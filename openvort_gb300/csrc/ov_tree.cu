@@ -679,6 +679,9 @@ __global__ void k_cells(const uint64_t *__restrict__ keys, const int *__restrict
     store_cell(cells, ci, acc, count, lm, L, next, views);
 }
 
+// Above this many slots the level sums run as one launch per level.
+constexpr int kLevelLaunchSlots = 1 << 19;
+
 // Grid-wide barrier of the cooperative k_levels (all blocks resident): one
 // arrival per block on a counter cleared by the build, then a bounded wait
 // for the epoch's total.  A wait that runs out sets OV_EW_ITER and returns
@@ -749,8 +752,27 @@ __device__ __forceinline__ void level_cell(int ci, int lev, int ncell, int *coun
     store_cell(cells, ci, acc, cnt, lm, lev, ch, views);
 }
 
+// One level of the bottom-up sums per launch (large trees: the levels hold
+// enough cells to fill the GPU, and launches cost less than grid barriers).
+__global__ void k_level(int lev, const int *__restrict__ lvl_cnt, const int *__restrict__ lvl_list,
+                        const int *__restrict__ cell_off, int *counters, int cap_cells, Cell64 *__restrict__ cells,
+                        const uint8_t *__restrict__ lvl8, double *__restrict__ psum, CellViews views)
+{
+    const int n = lvl_cnt[lev];
+    if (n == 0) return;
+    const int ncell = cell_off[counters[TC_NNE]];
+    if (ncell > cap_cells) return;   // flagged by k_cells; the host grows the storage
+    int start = 0;
+    for (int l = 0; l < lev; ++l) start += lvl_cnt[l];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int ci = start + i < cap_cells ? lvl_list[start + i] : -1;
+        level_cell(ci, lev, ncell, counters, cells, lvl8, psum, views);
+    }
+}
+
 // The bottom-up sums of every non-leaf cell, deepest level first, in one
-// cooperative launch: the blocks share each level's list, then meet at a
+// cooperative launch (small trees, where a launch per level would cost more
+// than the level's work): the blocks share each level's list, then meet at a
 // grid barrier (levels without cells are skipped by every block alike).
 // The leaves were finished by k_cells.
 __global__ void k_levels(int lev_hi, const int *__restrict__ lvl_cnt, const int *__restrict__ lvl_list,
@@ -984,7 +1006,12 @@ int ov_tree_build(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
         k_cells<false><<<nb, 256, 0, s>>>(t.keys, t.cpl, t.cell_off, t.counters, t.tt, g, cap, t.cells, t.first,
                                           t.lvl8, t.lvl_cnt, t.lvl_list, t.cap_cells, t.order, t.nm, t.psum,
                                           views);
-    {
+    if (cap > kLevelLaunchSlots) {
+        for (int lev = g.levels - 1; lev >= 1; --lev)
+            k_level<<<4 * c->sm_count, 256, 0, s>>>(lev, t.lvl_cnt, t.lvl_list, t.cell_off, t.counters, t.cap_cells,
+                                                    t.cells, t.lvl8, t.psum, views);
+        c->launches += g.levels - 2;
+    } else {
         // the level sums: one cooperative launch, every block resident
         static int per_sm = 0;
         if (!per_sm) {
