@@ -39,6 +39,7 @@ struct VelArgs {
     int *work;              // work-queue counter
     int nt;                 // members
     int G;                  // query groups per node
+    int S;                  // sub-walks per query point (FP64 split walk of a small tangle), else 1
     const Cell64 *cells;
     const Cell32 *cells32;
     const CellFF *cellsff;      // OV_PREC_DD: double-single cell data
@@ -479,14 +480,16 @@ __device__ __forceinline__ bool finish_node(const VelArgs &a, int id, const doub
 // so they touch the same cells.  Tiles of 32 sorted targets never cross a
 // member; members come in queue order.
 struct WorkItem {
-    int m, st, nne, root, end, tile, grp;
+    int m, st, nne, root, end, tile, grp, sub;
 };
 
 __device__ __forceinline__ WorkItem decode_item(const VelArgs &a, int it, int tiles)
 {
     WorkItem w;
-    w.grp = it / tiles;
-    int tile = it - w.grp * tiles;
+    const int gs = it / tiles;   // (query group, sub-walk)
+    int tile = it - gs * tiles;
+    w.grp = gs / a.S;
+    w.sub = gs - w.grp * a.S;
     int k = 0;
     if (a.nt > 1) {
         // last member (in queue order) whose first tile is <= tile
@@ -600,7 +603,7 @@ __global__ void k_vel_finish(VelArgs a, const double *__restrict__ part_in)
     if (st == OV_EMPTY) return;
     const size_t cap = (size_t)a.cap;
     double prim[3] = {0, 0, 0}, img[3] = {0, 0, 0};
-    for (int g = 0; g < a.G; ++g)
+    for (int g = 0; g < a.G * a.S; ++g)
         for (int ax = 0; ax < 3; ++ax) {
             prim[ax] = rn_add(prim[ax], part_in[((size_t)(2 * g) * 3 + ax) * cap + tix]);
             img[ax] = rn_add(img[ax], part_in[((size_t)(2 * g + 1) * 3 + ax) * cap + tix]);
@@ -1506,17 +1509,55 @@ __device__ __forceinline__ void flush_lists(const VelArgs &a, WarpLists &L, int 
 
 // One query point (split g + f for the tests, q in FP64 for the law) for the
 // 32 lanes of a warp; the lane's FP64 velocity in v.
-__device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], const float f[3], const double q[3],
-                                           bool part, int root, int ncell, WarpLists &L, int lane, double v[3],
-                                           MixedAcc &m, bool &overflow)
+// The split walk's decision for cell c (A, B its first 32 bytes, nxt its
+// successor): the mixed traversal's FP32 tests outside their guard bands,
+// the FP64 path's (decide64) inside them.  0 open, 1 skip, 2 accept.
+__device__ __forceinline__ int split_decision(const VelArgs &a, int c, const float4 &A, const float4 &B, int nxt,
+                                              const float g[3], const float f[3], const double q[3], MixedAcc &m)
 {
     const float d2lo = 1e-16f * (1.0f - 1e-5f), d2hi = 1e-16f * (1.0f + 1e-5f);
+    const float dx = (g[0] - A.x) + (f[0] - B.x);
+    const float dy = (g[1] - A.y) + (f[1] - B.y);
+    const float dz = (g[2] - A.z) + (f[2] - B.z);
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const bool leaf = (nxt == c + 1);
+    bool skip = d2 < d2lo;
+    bool acc = !skip && (leaf || d2 > A.w);
+    const bool opn = !skip && !leaf && d2 < A.w * kThrLo;
+    if ((!skip && d2 <= d2hi) || (!skip && !acc && !opn)) {
+        ++m.nfb;
+        double dxyz[3], d64;
+        const int dec = decide64(a, a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
+        skip = dec == 1;
+        acc = dec == 2;
+    }
+    return acc ? 2 : (skip ? 1 : 0);
+}
+
+// Whether the split walk opens the root cell for this query point (the
+// root's decision, as the walk's first step takes it).
+__device__ __forceinline__ bool split_opens_root(const VelArgs &a, int root, int end, const float g[3],
+                                                 const float f[3], const double q[3], MixedAcc &m)
+{
+    const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + root);
+    const float4 A = __ldg(cp4), B = __ldg(cp4 + 1);
+    int nxt = __float_as_int(B.w);
+    if (nxt <= root || nxt > end) { bad_index(a, 2, root); nxt = end; }
+    return split_decision(a, root, A, B, nxt, g, f, q, m) == 0;
+}
+
+// The walk of cells [root, ncell) stops at `stop` (a sub-walk's end; ncell
+// otherwise); successors are checked against ncell.
+__device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], const float f[3], const double q[3],
+                                           bool part, int root, int ncell, int stop, WarpLists &L, int lane,
+                                           double v[3], MixedAcc &m, bool &overflow)
+{
     v[0] = v[1] = v[2] = 0;
     int c = root;
     int resume = part ? 0 : 0x7fffffff;
     const int guard_max = 4 * (ncell - root) + 64;
     int steps = 0, n = 0;
-    while (c < ncell) {
+    while (c < stop) {
         if (c < root) { bad_index(a, 1, c); break; }
         const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
         const float4 A = __ldg(cp4), B = __ldg(cp4 + 1);
@@ -1526,28 +1567,13 @@ __device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], c
         bool open = false;
         if (c >= resume) {
             ++m.nvis;
-            const float dx = (g[0] - A.x) + (f[0] - B.x);
-            const float dy = (g[1] - A.y) + (f[1] - B.y);
-            const float dz = (g[2] - A.z) + (f[2] - B.z);
-            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const bool leaf = (nxt == c + 1);
-            // the mixed traversal's tests and guard bands
-            bool skip = d2 < d2lo;
-            bool acc = !skip && (leaf || d2 > A.w);
-            const bool opn = !skip && !leaf && d2 < A.w * kThrLo;
-            if ((!skip && d2 <= d2hi) || (!skip && !acc && !opn)) {
-                ++m.nfb;
-                double dxyz[3], d64;
-                const int dec = decide64(a, a.cells + c, q, a.prm.theta, leaf, dxyz, &d64);
-                skip = dec == 1;
-                acc = dec == 2;
-            }
-            if (acc) {
+            const int dec = split_decision(a, c, A, B, nxt, g, f, q, m);
+            if (dec == 2) {
                 ++m.nacc;
                 L.entry[32 * n + lane] = c;
                 ++n;
                 resume = nxt;
-            } else if (skip) {
+            } else if (dec == 1) {
                 resume = nxt;
             } else {
                 open = true;
@@ -1575,7 +1601,7 @@ __global__ void __launch_bounds__(32 * W, min_blocks_split<W>()) k_vel_split(Vel
 {
     const int lane = threadIdx.x & 31;
     const int tiles = a.counters[TC_ITEMS];
-    const int items = tiles * a.G;
+    const int items = tiles * a.G * a.S;
     __shared__ WarpLists s_lists[W];
     WarpLists &lists = s_lists[threadIdx.x >> 5];
     unsigned long long visits = 0, accepts = 0, steps = 0, fallback = 0;
@@ -1625,7 +1651,28 @@ __global__ void __launch_bounds__(32 * W, min_blocks_split<W>()) k_vel_split(Vel
                 }
             }
             double v[3];
-            walk_split(a, g, f, q, part, w.root, w.end, lists, lane, v, m, overflow);
+            int c0 = w.root, c1 = w.end;
+            bool walk_part = part;
+            if (a.S > 1) {
+                // sub-walk w.sub: level-1 subtree w.sub of the root; part 0
+                // also takes the root cell itself
+                int ch = w.root + 1;
+                for (int k = 0; k < w.sub && ch < w.end; ++k) {
+                    const int nx = __float_as_int(__ldg(reinterpret_cast<const float4 *>(a.cells32 + ch) + 1).w);
+                    ch = nx > ch ? nx : w.end;
+                }
+                const int ch_next =
+                    ch < w.end ? __float_as_int(__ldg(reinterpret_cast<const float4 *>(a.cells32 + ch) + 1).w) : w.end;
+                c1 = ch_next > ch && ch_next <= w.end ? ch_next : w.end;
+                if (w.sub == 0) {
+                    c0 = w.root;
+                } else {
+                    c0 = ch;
+                    MixedAcc tmp = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
+                    walk_part = part && ch < w.end && split_opens_root(a, w.root, w.end, g, f, q, tmp);
+                }
+            }
+            walk_split(a, g, f, q, walk_part, c0, w.end, c1, lists, lane, v, m, overflow);
             if (j < 0) {
                 prim[0] = v[0]; prim[1] = v[1]; prim[2] = v[2];
             } else {
@@ -1634,10 +1681,10 @@ __global__ void __launch_bounds__(32 * W, min_blocks_split<W>()) k_vel_split(Vel
             }
         }
         if (valid) {
-            const size_t cap = (size_t)a.cap;
+            const size_t cap = (size_t)a.cap, gs = (size_t)w.grp * a.S + w.sub;
             for (int ax = 0; ax < 3; ++ax) {
-                part_out[((size_t)(2 * w.grp) * 3 + ax) * cap + tix] = prim[ax];
-                part_out[((size_t)(2 * w.grp + 1) * 3 + ax) * cap + tix] = img[ax];
+                part_out[((2 * gs) * 3 + ax) * cap + tix] = prim[ax];
+                part_out[((2 * gs + 1) * 3 + ax) * cap + tix] = img[ax];
             }
         }
         count_node(a, valid, id, m.nvis, m.nacc);
@@ -1724,6 +1771,7 @@ VelArgs make_args(ov_ctx *c, const NodeArrays &na, double t, unsigned long long 
     a.work = c->tree.counters + TC_WORK;
     a.nt = (int)c->mem.size();
     a.G = ov_query_groups(c);
+    a.S = 1;
     a.th2f = (float)(a.prm.theta * a.prm.theta);
     a.near2f = (float)a.near2;
     a.f4pif = (float)a.f4pi;
@@ -1753,10 +1801,19 @@ void ov_launch_tangents(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     c->launches++;
 }
 
+// Sub-walks per query point: the FP64 split walk of a tangle too small to
+// fill the GPU with (tile, query group) items splits each walk over the
+// root's level-1 subtrees (the root's own decision taken in every part).
+constexpr int kSubWalks = 8, kSubWalkSlots = 8192;
+static int ov_sub_walks(const ov_ctx *c, int precision)
+{
+    return precision == OV_PREC_FP64 && c->walk == OV_WALK_SPLIT && c->cap <= kSubWalkSlots ? kSubWalks : 1;
+}
+
 int ov_reserve_velocity_scratch(ov_ctx *c)
 {
     int G = ov_query_groups(c);
-    size_t need = (size_t)G * 6 * (size_t)c->cap;
+    size_t need = (size_t)G * (c->cap <= kSubWalkSlots ? kSubWalks : 1) * 6 * (size_t)c->cap;
     if (c->part_cap < need) {
         if (c->part) cudaFree(c->part);
         c->part = nullptr;
@@ -1835,6 +1892,7 @@ int ov_traversal_blocks(ov_ctx *c, int precision, int warps, int *per_sm)
 int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precision, cudaStream_t s)
 {
     VelArgs a = make_args(c, na, t, ov_stat_ptr(c));
+    a.S = ov_sub_walks(c, precision);
     if (c->time_dev_index >= 0) {
         a.t_dev = c->d_time;
         a.t_index = c->time_dev_index;
@@ -1860,7 +1918,10 @@ int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precisio
     OV_CUDA(c, cudaMemsetAsync(a.work, 0, sizeof(int), s));
     vel_kernel(precision, c->walk, warps, c->tune.hi_occ, has_mirror_images(c->geo))<<<blocks, 32 * warps, 0, s>>>(
         a, c->part);
-    k_vel_finish<<<(c->cap + 127) / 128, 128, 0, s>>>(a, c->part);
+    // with sub-walks a node adds G x S partials (FP64): small blocks spread
+    // the few nodes of such a tangle over many SMs
+    const int fin = a.S > 1 ? 32 : 128;
+    k_vel_finish<<<(c->cap + fin - 1) / fin, fin, 0, s>>>(a, c->part);
     c->launches += 2;
     return OV_OK;
 }
@@ -3118,7 +3179,7 @@ __global__ void __launch_bounds__(128) k_sph_query_split(SphArgs s, double *__re
     MixedAcc acc = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
     bool overflow = false;
     double v[3];
-    walk_split(a, g, f, qp, go, root, end, lists, lane, v, acc, overflow);
+    walk_split(a, g, f, qp, go, root, end, end, lists, lane, v, acc, overflow);
     double w[3] = {v[0], v[1], v[2]};
     if (j >= 0) sph_rotate(v, -da, -dp, w);
     if (a.stat) {
