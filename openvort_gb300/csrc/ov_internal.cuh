@@ -11,6 +11,10 @@
 //   cells            Cell64[ncell] pre-order cells: COM, circulation, Lm,
 //                                  subtree end (`next`) and node count
 //   cells32          Cell32[ncell] FP32 copy for the mixed traversal
+//   nm               double[6 cap] node moments (position, wrapped forward
+//                                  segment) in id order, for the leaves
+//   first,lvl8,psum  per cell: first sorted node, level, position sum
+//   lvl_list         non-root, non-leaf cells grouped by level
 #pragma once
 
 #include <cuda_runtime.h>
