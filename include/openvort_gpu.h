@@ -147,9 +147,18 @@ enum {
 };
 int ov_set_walk(ov_ctx *ctx, int walk);
 int ov_get_walk(const ov_ctx *ctx);
-/* RK4 steps run as one captured CUDA graph (default on); off launches the
-   same kernels one by one (identical results). */
+/* RK4 steps and single evaluations (update_tangle, update_velocities) run as
+   captured CUDA graphs (default on); off launches the same kernels one by
+   one (identical results). */
 int ov_set_rk4_graph(ov_ctx *ctx, int on);
+/* Uploads and downloads read and write the caller's tangle arrays in place
+   from the GPU when the device accesses pageable host memory through the
+   host's page tables (Grace-based systems; default on there), else through
+   one staged copy of each array; 0 forces the staged copies.  Identical
+   results either way.  ov_get_host_access returns 1 when the in-place path
+   is in effect. */
+int ov_set_host_access(ov_ctx *ctx, int direct);
+int ov_get_host_access(const ov_ctx *ctx);
 /* cudaStream_t the context launches on, as an opaque pointer (for callers that
    time or order their own work against it). */
 void *ov_ctx_stream(ov_ctx *ctx);

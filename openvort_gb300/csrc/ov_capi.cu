@@ -109,6 +109,12 @@ int ov_ctx_create(ov_ctx **out, int device)
     ov_ctx *c = new ov_ctx();
     c->device = device;
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    {
+        int pma = 0, pmt = 0;
+        cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, device);
+        cudaDeviceGetAttribute(&pmt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+        c->pageable = pma == 1 && pmt == 1;
+    }
     ov_params_default(&c->params);
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
@@ -255,6 +261,15 @@ int ov_set_params(ov_ctx *c, const ov_params *p)
     if (c->mem.size() > 1 && c->d_tprm) return ov_upload_member_tables(c);
     return OV_OK;
 }
+
+int ov_set_host_access(ov_ctx *c, int direct)
+{
+    if (!c) return OV_ERR_ARG;
+    c->host_direct = direct != 0;
+    return OV_OK;
+}
+
+int ov_get_host_access(const ov_ctx *c) { return c && c->pageable && c->host_direct ? 1 : 0; }
 
 int ov_set_rk4_graph(ov_ctx *c, int on)
 {
@@ -439,9 +454,27 @@ struct NodePtrs {
 
 __host__ __device__ inline size_t stage_topo_off(int n) { return (size_t)n * 120; }
 
+// Where the host-layout data of a transfer sits: the device stage (one copy
+// of each host array), or the caller's arrays themselves when the device
+// reads and writes pageable host memory.
+struct HostView {
+    ov_vec3 *f[5];           // positions, vels, vs, tangents, normals (null: absent)
+    ov_neighbour *con;
+    ov_node_status *st;
+};
+
+static HostView stage_view(char *stage, int n)
+{
+    HostView v;
+    for (int f = 0; f < 5; ++f) v.f[f] = reinterpret_cast<ov_vec3 *>(stage + (size_t)f * n * 24);
+    v.con = reinterpret_cast<ov_neighbour *>(stage + stage_topo_off(n));
+    v.st = reinterpret_cast<ov_node_status *>(stage + stage_topo_off(n) + (size_t)n * 8);
+    return v;
+}
+
 // Host layout (vec3 fields, ov_neighbour, ov_node_status) -> device arrays for
 // slots [0, cap): slots past n get zeros, -1 links, EMPTY, no wall.
-__global__ void k_unpack(const char *__restrict__ stage, unsigned fields, unsigned have, int n, int cap, NodePtrs d)
+__global__ void k_unpack(HostView src, unsigned fields, unsigned have, int n, int cap, NodePtrs d)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= cap) return;
@@ -449,41 +482,35 @@ __global__ void k_unpack(const char *__restrict__ stage, unsigned fields, unsign
 #pragma unroll
     for (int f = 0; f < 5; ++f) {
         if (!(fields & bits[f])) continue;
-        const double *src = reinterpret_cast<const double *>(stage + (size_t)f * n * 24);
         const bool in = k < n && (have & bits[f]);
-        for (int a = 0; a < 3; ++a) d.d[3 * f + a][k] = in ? src[3 * (size_t)k + a] : 0.0;
+        for (int a = 0; a < 3; ++a) d.d[3 * f + a][k] = in ? src.f[f][k].p[a] : 0.0;
     }
     if (fields & OV_F_TOPOLOGY) {
-        const ov_neighbour *con = reinterpret_cast<const ov_neighbour *>(stage + stage_topo_off(n));
-        const ov_node_status *st = reinterpret_cast<const ov_node_status *>(stage + stage_topo_off(n) + (size_t)n * 8);
         const bool in = k < n;
-        d.fwd[k] = in ? con[k].forward : -1;
-        d.rev[k] = in ? con[k].reverse : -1;
-        d.status[k] = in ? st[k].status : OV_EMPTY;
-        d.pin[k] = in ? st[k].pin_wall : OV_NOT_A_FACE;
+        d.fwd[k] = in ? src.con[k].forward : -1;
+        d.rev[k] = in ? src.con[k].reverse : -1;
+        d.status[k] = in ? src.st[k].status : OV_EMPTY;
+        d.pin[k] = in ? src.st[k].pin_wall : OV_NOT_A_FACE;
     }
 }
 
 // Device slots [lo, lo + n) -> host layout, links shifted by -lo.
-__global__ void k_pack(unsigned fields, int lo, int n, NodePtrs d, char *__restrict__ stage)
+__global__ void k_pack(unsigned fields, int lo, int n, NodePtrs d, HostView dst)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
 #pragma unroll
     for (int f = 0; f < 5; ++f) {
-        if (!(fields & bits[f])) continue;
-        double *dst = reinterpret_cast<double *>(stage + (size_t)f * n * 24);
-        for (int a = 0; a < 3; ++a) dst[3 * (size_t)k + a] = d.d[3 * f + a][lo + k];
+        if (!(fields & bits[f]) || !dst.f[f]) continue;
+        for (int a = 0; a < 3; ++a) dst.f[f][k].p[a] = d.d[3 * f + a][lo + k];
     }
     if (fields & OV_F_TOPOLOGY) {
-        ov_neighbour *con = reinterpret_cast<ov_neighbour *>(stage + stage_topo_off(n));
-        ov_node_status *st = reinterpret_cast<ov_node_status *>(stage + stage_topo_off(n) + (size_t)n * 8);
         const int f = d.fwd[lo + k], b = d.rev[lo + k];
-        con[k].forward = f >= 0 ? f - lo : -1;
-        con[k].reverse = b >= 0 ? b - lo : -1;
-        st[k].status = d.status[lo + k];
-        st[k].pin_wall = d.pin[lo + k];
+        dst.con[k].forward = f >= 0 ? f - lo : -1;
+        dst.con[k].reverse = b >= 0 ? b - lo : -1;
+        dst.st[k].status = d.status[lo + k];
+        dst.st[k].pin_wall = d.pin[lo + k];
     }
 }
 
@@ -533,6 +560,7 @@ int ov_reserve_members(ov_ctx *c, int nt)
 {
     nt = std::max(nt, 1);
     if (c->tree.tt && c->tcap >= nt) return OV_OK;
+    ov_drop_graphs(c);   // the tables move
     if (c->tree.tt) cudaFree(c->tree.tt);
     if (c->d_tprm) cudaFree(c->d_tprm);
     if (c->d_qorder) cudaFree(c->d_qorder);
@@ -559,7 +587,9 @@ int ov_upload_member_tables(ov_ctx *c)
     if (nt > 1)
         while ((1 << c->key_tbits) <= nt) ++c->key_tbits;
     c->key_levels = std::min(OV_MAX_LEVEL, (63 - c->key_tbits) / 3);
-    ov_drop_graphs(c);   // the graphs bake the layout in
+    // (the graphs' key covers the layout, parameters and table pointers; the
+    // per-slot member table of an ensemble is reallocated below)
+    if (nt > 1) ov_drop_graphs(c);
     std::vector<DevParams> prm(nt);
     std::vector<int> q(nt);
     std::vector<int2> rng(nt);
@@ -750,32 +780,39 @@ int ov_upload_tangle_fields(ov_ctx *c, const ov_tangle_state *t, unsigned fields
                 return ov_fail(c, OV_ERR_TOPOLOGY, "node %d: connections (%d,%d) / status %d out of range", k, f, b, st);
         }
     }
-    // the host arrays as they are, one copy each, then the transposition to
-    // the device's arrays (k_unpack)
-    const size_t bytes = stage_topo_off(n) + (size_t)n * 16;
-    if ((r = ensure_dstage(c, std::max(bytes, (size_t)16)))) return r;
+    // the transposition to the device's arrays (k_unpack) reads the caller's
+    // arrays in place when the device reads pageable host memory, else one
+    // copy of each into the device stage
     const ov_vec3 *src[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
     const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
+    const bool direct = c->pageable && c->host_direct;
+    HostView view = {};
+    if (direct) {
+        for (int f = 0; f < 5; ++f) view.f[f] = const_cast<ov_vec3 *>(src[f]);
+        view.con = t->connections;
+        view.st = t->status;
+    } else {
+        const size_t bytes = stage_topo_off(n) + (size_t)n * 16;
+        if ((r = ensure_dstage(c, std::max(bytes, (size_t)16)))) return r;
+        view = stage_view(c->d_stage, n);
+    }
     unsigned have = 0;
     c->last_h2d = 0;
     for (int f = 0; f < 5; ++f) {
         if (!(fields & bits[f])) continue;
         if (src[f] && n > 0) {
-            OV_CUDA(c, cudaMemcpyAsync(c->d_stage + (size_t)f * n * 24, src[f], (size_t)n * 24,
-                                       cudaMemcpyHostToDevice, c->stream));
+            if (!direct)
+                OV_CUDA(c, cudaMemcpyAsync(view.f[f], src[f], (size_t)n * 24, cudaMemcpyHostToDevice, c->stream));
             have |= bits[f];
         }
         c->last_h2d += 3 * cap * sizeof(double);
     }
-    if ((fields & OV_F_TOPOLOGY) && n > 0) {
-        OV_CUDA(c, cudaMemcpyAsync(c->d_stage + stage_topo_off(n), t->connections, (size_t)n * 8,
-                                   cudaMemcpyHostToDevice, c->stream));
-        OV_CUDA(c, cudaMemcpyAsync(c->d_stage + stage_topo_off(n) + (size_t)n * 8, t->status, (size_t)n * 8,
-                                   cudaMemcpyHostToDevice, c->stream));
+    if ((fields & OV_F_TOPOLOGY) && n > 0 && !direct) {
+        OV_CUDA(c, cudaMemcpyAsync(view.con, t->connections, (size_t)n * 8, cudaMemcpyHostToDevice, c->stream));
+        OV_CUDA(c, cudaMemcpyAsync(view.st, t->status, (size_t)n * 8, cudaMemcpyHostToDevice, c->stream));
     }
     if (fields & OV_F_TOPOLOGY) c->last_h2d += 4 * cap * sizeof(int);
-    k_unpack<<<(unsigned)((cap + 255) / 256), 256, 0, c->stream>>>(c->d_stage, fields, have, n, (int)cap,
-                                                                    node_ptrs(c));
+    k_unpack<<<(unsigned)((cap + 255) / 256), 256, 0, c->stream>>>(view, fields, have, n, (int)cap, node_ptrs(c));
     c->launches++;
     OV_CUDA(c, cudaGetLastError());
     OV_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -791,25 +828,36 @@ static int download_range(ov_ctx *c, ov_tangle_state *t, unsigned fields, int lo
 {
     const int n = std::min(t->N, span);
     int r;
-    const size_t bytes = stage_topo_off(n) + (size_t)n * 16;
-    if ((r = ensure_dstage(c, std::max(bytes, (size_t)16)))) return r;
     const unsigned bits[5] = {OV_F_POS, OV_F_VELS, OV_F_VS, OV_F_TANGENTS, OV_F_NORMALS};
     ov_vec3 *dst[5] = {t->vnodes, t->vels, t->vs, t->tangents, t->normals};
     if (n > 0) {
-        // the device's arrays transposed to the host layout (k_pack), one copy each
-        k_pack<<<(n + 255) / 256, 256, 0, c->stream>>>(fields, lo, n, node_ptrs(c), c->d_stage);
-        c->launches++;
-        // straight into the caller's arrays
-        for (int f = 0; f < 5; ++f) {
-            if (!(fields & bits[f]) || !dst[f]) continue;
-            OV_CUDA(c, cudaMemcpyAsync(dst[f], c->d_stage + (size_t)f * n * 24, (size_t)n * 24,
-                                       cudaMemcpyDeviceToHost, c->stream));
+        // the device's arrays transposed to the host layout (k_pack): straight
+        // into the caller's arrays when the device writes pageable host
+        // memory, else into the device stage and one copy each
+        const bool direct = c->pageable && c->host_direct;
+        HostView view = {};
+        if (direct) {
+            for (int f = 0; f < 5; ++f) view.f[f] = dst[f];
+            view.con = t->connections;
+            view.st = t->status;
+        } else {
+            const size_t bytes = stage_topo_off(n) + (size_t)n * 16;
+            if ((r = ensure_dstage(c, std::max(bytes, (size_t)16)))) return r;
+            view = stage_view(c->d_stage, n);
+            for (int f = 0; f < 5; ++f)
+                if (!dst[f]) view.f[f] = nullptr;
         }
-        if (fields & OV_F_TOPOLOGY) {
-            OV_CUDA(c, cudaMemcpyAsync(t->connections, c->d_stage + stage_topo_off(n), (size_t)n * 8,
-                                       cudaMemcpyDeviceToHost, c->stream));
-            OV_CUDA(c, cudaMemcpyAsync(t->status, c->d_stage + stage_topo_off(n) + (size_t)n * 8, (size_t)n * 8,
-                                       cudaMemcpyDeviceToHost, c->stream));
+        k_pack<<<(n + 255) / 256, 256, 0, c->stream>>>(fields, lo, n, node_ptrs(c), view);
+        c->launches++;
+        if (!direct) {
+            for (int f = 0; f < 5; ++f) {
+                if (!(fields & bits[f]) || !dst[f]) continue;
+                OV_CUDA(c, cudaMemcpyAsync(dst[f], view.f[f], (size_t)n * 24, cudaMemcpyDeviceToHost, c->stream));
+            }
+            if (fields & OV_F_TOPOLOGY) {
+                OV_CUDA(c, cudaMemcpyAsync(t->connections, view.con, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+                OV_CUDA(c, cudaMemcpyAsync(t->status, view.st, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+            }
         }
         OV_CUDA(c, cudaStreamSynchronize(c->stream));
     }
@@ -1078,7 +1126,8 @@ static unsigned long long graph_key(ov_ctx *c)
         h = mix64(h, lay, sizeof lay);
         h = mix64(h, &m.params, sizeof m.params);
     }
-    const void *ptrs[4] = {c->node.x, c->tree.cells, c->part, c->d_time};
+    const void *ptrs[9] = {c->node.x, c->tree.cells, c->part, c->d_time, c->d_tid, c->d_tprm, c->d_qorder, c->d_mrange,
+                           c->tree.tt};
     h = mix64(h, ptrs, sizeof ptrs);
     return h;
 }

@@ -195,6 +195,8 @@ struct Tuning {
 struct ov_ctx {
     int device = 0;
     int sm_count = 152;
+    bool pageable = false;       // the device reads and writes pageable host memory (host page tables)
+    bool host_direct = true;     // upload/download through the caller's arrays when pageable
     std::vector<Member> mem{Member{}};
     int key_tbits = 0;                     // member-id bits on top of the path keys
     int key_levels = OV_MAX_LEVEL;         // tree levels below each root

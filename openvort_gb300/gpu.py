@@ -84,6 +84,8 @@ def load(path: str | None = None):
         "ov_get_node_counts": (C.c_int, [P, C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_uint), C.c_int]),
         "ov_measure_fma_peak": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
         "ov_set_rk4_graph": (C.c_int, [P, C.c_int]),
+        "ov_set_host_access": (C.c_int, [P, C.c_int]),
+        "ov_get_host_access": (C.c_int, [P]),
         "ov_tangle_info": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "ov_upload_ensemble": (C.c_int, [P, C.POINTER(TS), C.POINTER(abi.Params), C.c_int, C.c_double]),
         "ov_ensemble_size": (C.c_int, [P]),
@@ -241,6 +243,15 @@ class Context:
 
     def set_rk4_graph(self, on: bool):
         self._check(self.lib.ov_set_rk4_graph(self._h, int(on)))
+
+    def set_host_access(self, direct: bool):
+        """In-place uploads/downloads of the caller's arrays where the device
+        reads pageable host memory (True, the default), or staged copies."""
+        self._check(self.lib.ov_set_host_access(self._h, int(direct)))
+
+    @property
+    def host_access_direct(self) -> bool:
+        return bool(self.lib.ov_get_host_access(self._h))
 
     def set_precision(self, prec: int):
         self._check(self.lib.ov_set_precision(self._h, prec))
