@@ -130,7 +130,9 @@ __global__ void rs_scatter(const uint64_t *__restrict__ kin, const int *__restri
     __shared__ int sh[32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int i = threadIdx.x; i < kWarps * 256; i += blockDim.x) (&wc[0][0])[i] = 0;
-    for (int d = threadIdx.x; d < 256; d += blockDim.x) gbase[d] = hist[d * ntiles + blockIdx.x];
+    // (hist null: the keys are one tile, and a digit's output offset is its
+    // start in the tile)
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) gbase[d] = hist ? hist[d * ntiles + blockIdx.x] : 0;
     __syncthreads();
     const int tbase = blockIdx.x * kTile;
     const int tn = min(kTile, n - tbase);
@@ -171,7 +173,10 @@ __global__ void rs_scatter(const uint64_t *__restrict__ kin, const int *__restri
     {
         int tot_all;
         const int off = block_excl_scan(threadIdx.x < 256 ? dig_total : 0, sh, tot_all);
-        if (threadIdx.x < 256) boff[threadIdx.x] = off;
+        if (threadIdx.x < 256) {
+            boff[threadIdx.x] = off;
+            if (!hist) gbase[threadIdx.x] = off;
+        }
     }
     __syncthreads();
 #pragma unroll
@@ -303,14 +308,19 @@ static void sort_passes(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
     uint64_t *ka = t.keys, *kb = t.keys_alt;
     int *va = t.order, *vb = t.order_alt;
     int *tot = t.sort_hist + 256 * (size_t)ntiles;   // 4 x 256 digit totals
-    cudaMemsetAsync(tot, 0, 4 * 256 * sizeof(int), s);
+    if (ntiles > 1) cudaMemsetAsync(tot, 0, 4 * 256 * sizeof(int), s);
     for (int pass = 0; pass < 4; ++pass) {
         int shift = 32 + 8 * pass;
-        rs_hist<kSortItems><<<ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, t.sort_hist,
-                                                           pass == 0 ? tot : nullptr);
-        rs_rowscan<<<256, kSortThreads, 0, s>>>(t.sort_hist, ntiles, tot + 256 * pass);
-        rs_scatter<kSortItems><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, ntiles, t.sort_hist);
-        c->launches += 3;
+        if (ntiles > 1) {
+            rs_hist<kSortItems><<<ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, t.sort_hist,
+                                                               pass == 0 ? tot : nullptr);
+            rs_rowscan<<<256, kSortThreads, 0, s>>>(t.sort_hist, ntiles, tot + 256 * pass);
+            c->launches += 2;
+        }
+        // one tile: the scatter's own digit starts are the offsets
+        rs_scatter<kSortItems><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, ntiles,
+                                                              ntiles > 1 ? t.sort_hist : nullptr);
+        c->launches += 1;
         uint64_t *tk = ka; ka = kb; kb = tk;
         int *tv = va; va = vb; vb = tv;
     }
@@ -322,13 +332,16 @@ static void sort_passes(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
 void ov_sort_keys(ov_ctx *c, TreeBuf &t, int n, cudaStream_t s)
 {
     if (n <= 0) return;
-    if (n <= kSmallSortSlots) sort_passes<kItemsSmall>(c, t, n, s);
-    else sort_passes<kItemsLarge>(c, t, n, s);
+    // one 4,096-slot tile when the keys fit in it; 1,024-slot tiles up to
+    // kSmallSortSlots (more blocks than SMs); 4,096-slot tiles above
+    if (n <= sort_tile(kItemsLarge) || n > kSmallSortSlots) sort_passes<kItemsLarge>(c, t, n, s);
+    else sort_passes<kItemsSmall>(c, t, n, s);
 }
 
 int ov_sort_hist_ints(int cap)
 {
-    const int tile = cap <= kSmallSortSlots ? sort_tile(kItemsSmall) : sort_tile(kItemsLarge);
+    const int tile = cap <= sort_tile(kItemsLarge) || cap > kSmallSortSlots ? sort_tile(kItemsLarge)
+                                                                            : sort_tile(kItemsSmall);
     return 256 * ((cap + tile - 1) / tile) + 4 * 256;
 }
 

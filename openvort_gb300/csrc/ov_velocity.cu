@@ -591,6 +591,27 @@ __global__ void __launch_bounds__(32 * W, min_blocks<W>()) k_vel_fp64(VelArgs a,
     }
 }
 
+// Parts of split walks: each group's S parts added in part order into its
+// first part's slot (one thread per group, component and target).
+__global__ void k_part_sum(VelArgs a, double *__restrict__ part)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nne = min(a.counters[TC_NNE], a.cap);
+    const long long per = 6LL * nne;
+    if (i >= per * a.G) return;
+    const int g = (int)(i / per);
+    const int r = (int)(i - (long long)g * per);
+    const int comp = r / nne, tix = r - comp * nne;   // comp: prim x,y,z then img x,y,z
+    const size_t cap = (size_t)a.cap;
+    const int half = comp / 3, ax = comp - 3 * half;
+    double s = 0;
+    for (int k = 0; k < a.S; ++k) {
+        const size_t gs = (size_t)g * a.S + k;
+        s = rn_add(s, part[((2 * gs + half) * 3 + ax) * cap + tix]);
+    }
+    part[((2 * (size_t)g * a.S + half) * 3 + ax) * cap + tix] = s;
+}
+
 // Sum the group partials in group order, then LIA, v_s and mutual friction.
 __global__ void k_vel_finish(VelArgs a, const double *__restrict__ part_in)
 {
@@ -603,7 +624,8 @@ __global__ void k_vel_finish(VelArgs a, const double *__restrict__ part_in)
     if (st == OV_EMPTY) return;
     const size_t cap = (size_t)a.cap;
     double prim[3] = {0, 0, 0}, img[3] = {0, 0, 0};
-    for (int g = 0; g < a.G * a.S; ++g)
+    // (with parts, k_part_sum has added each group's parts into its first)
+    for (int g = 0; g < a.G * a.S; g += a.S)
         for (int ax = 0; ax < 3; ++ax) {
             prim[ax] = rn_add(prim[ax], part_in[((size_t)(2 * g) * 3 + ax) * cap + tix]);
             img[ax] = rn_add(img[ax], part_in[((size_t)(2 * g + 1) * 3 + ax) * cap + tix]);
@@ -1534,27 +1556,46 @@ __device__ __forceinline__ int split_decision(const VelArgs &a, int c, const flo
     return acc ? 2 : (skip ? 1 : 0);
 }
 
-// Whether the split walk opens the root cell for this query point (the
-// root's decision, as the walk's first step takes it).
-__device__ __forceinline__ bool split_opens_root(const VelArgs &a, int root, int end, const float g[3],
-                                                 const float f[3], const double q[3], MixedAcc &m)
+// Where a lane of the full walk from `root` stands when the cursor reaches
+// cell b: the walk visits b's ancestors (root down to b's parent) in order,
+// and the first of them the lane accepts or skips keeps it out until that
+// ancestor's successor (past b); a lane that opens all of them takes part
+// from b on.  The decisions are the walk's own (split_decision); nothing is
+// counted.
+__device__ __forceinline__ int ancestor_resume(const VelArgs &a, int root, int end, int b, const float g[3],
+                                               const float f[3], const double q[3])
 {
-    const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + root);
-    const float4 A = __ldg(cp4), B = __ldg(cp4 + 1);
-    int nxt = __float_as_int(B.w);
-    if (nxt <= root || nxt > end) { bad_index(a, 2, root); nxt = end; }
-    return split_decision(a, root, A, B, nxt, g, f, q, m) == 0;
+    MixedAcc tmp = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
+    int c = root;
+    for (int guard = 0; c < b && guard < 32 * (OV_MAX_LEVEL + 2); ++guard) {
+        const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
+        const float4 A = __ldg(cp4), B = __ldg(cp4 + 1);
+        int nxt = __float_as_int(B.w);
+        if (nxt <= c || nxt > end) { bad_index(a, 2, c); return 0x7fffffff; }
+        if (split_decision(a, c, A, B, nxt, g, f, q, tmp) != 0) return nxt;   // accepted or skipped
+        // opened: on to the child holding b
+        int ch = c + 1;
+        for (int k = 0; k < 8; ++k) {
+            const int cn = __float_as_int(__ldg(reinterpret_cast<const float4 *>(a.cells32 + ch) + 1).w);
+            if (cn > b || cn <= ch) break;
+            ch = cn;
+        }
+        c = ch;
+    }
+    if (c != b) { bad_index(a, 3, b); return 0x7fffffff; }
+    return 0;
 }
 
 // The walk of cells [root, ncell) stops at `stop` (a sub-walk's end; ncell
-// otherwise); successors are checked against ncell.
+// otherwise); successors are checked against ncell.  resume0: the lane takes
+// part from that cell on (0: from the start; INT_MAX: not at all).
 __device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], const float f[3], const double q[3],
-                                           bool part, int root, int ncell, int stop, WarpLists &L, int lane,
+                                           int resume0, int root, int ncell, int stop, WarpLists &L, int lane,
                                            double v[3], MixedAcc &m, bool &overflow)
 {
     v[0] = v[1] = v[2] = 0;
     int c = root;
-    int resume = part ? 0 : 0x7fffffff;
+    int resume = resume0;
     const int guard_max = 4 * (ncell - root) + 64;
     int steps = 0, n = 0;
     while (c < stop) {
@@ -1652,27 +1693,16 @@ __global__ void __launch_bounds__(32 * W, min_blocks_split<W>()) k_vel_split(Vel
             }
             double v[3];
             int c0 = w.root, c1 = w.end;
-            bool walk_part = part;
+            int resume0 = part ? 0 : 0x7fffffff;
             if (a.S > 1) {
-                // sub-walk w.sub: level-1 subtree w.sub of the root; part 0
-                // also takes the root cell itself
-                int ch = w.root + 1;
-                for (int k = 0; k < w.sub && ch < w.end; ++k) {
-                    const int nx = __float_as_int(__ldg(reinterpret_cast<const float4 *>(a.cells32 + ch) + 1).w);
-                    ch = nx > ch ? nx : w.end;
-                }
-                const int ch_next =
-                    ch < w.end ? __float_as_int(__ldg(reinterpret_cast<const float4 *>(a.cells32 + ch) + 1).w) : w.end;
-                c1 = ch_next > ch && ch_next <= w.end ? ch_next : w.end;
-                if (w.sub == 0) {
-                    c0 = w.root;
-                } else {
-                    c0 = ch;
-                    MixedAcc tmp = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
-                    walk_part = part && ch < w.end && split_opens_root(a, w.root, w.end, g, f, q, tmp);
-                }
+                // part w.sub: an equal share of the pre-order cells; the lane's
+                // state at its first cell from the walk down its ancestors
+                const long long nc = (long long)(w.end - w.root);
+                c0 = w.root + (int)(nc * w.sub / a.S);
+                c1 = w.root + (int)(nc * (w.sub + 1) / a.S);
+                if (part && c0 > w.root && c0 < c1) resume0 = ancestor_resume(a, w.root, w.end, c0, g, f, q);
             }
-            walk_split(a, g, f, q, walk_part, c0, w.end, c1, lists, lane, v, m, overflow);
+            walk_split(a, g, f, q, resume0, c0, w.end, c1, lists, lane, v, m, overflow);
             if (j < 0) {
                 prim[0] = v[0]; prim[1] = v[1]; prim[2] = v[2];
             } else {
@@ -1801,19 +1831,21 @@ void ov_launch_tangents(ov_ctx *c, const NodeArrays &na, cudaStream_t s)
     c->launches++;
 }
 
-// Sub-walks per query point: the FP64 split walk of a tangle too small to
-// fill the GPU with (tile, query group) items splits each walk over the
-// root's level-1 subtrees (the root's own decision taken in every part).
-constexpr int kSubWalks = 8, kSubWalkSlots = 8192;
+// Parts per query point: the FP64 split walk of a tangle too small to fill
+// the GPU with (tile, query group) items splits each walk into equal shares
+// of the pre-order cells (32 parts up to 2,048 slots, 8 up to 8,192), so a
+// kernel is not as long as its longest walk.
+constexpr int kSubWalkSlots = 8192;
+static int sub_walks_for(int cap) { return cap <= 2048 ? 32 : (cap <= kSubWalkSlots ? 8 : 1); }
 static int ov_sub_walks(const ov_ctx *c, int precision)
 {
-    return precision == OV_PREC_FP64 && c->walk == OV_WALK_SPLIT && c->cap <= kSubWalkSlots ? kSubWalks : 1;
+    return precision == OV_PREC_FP64 && c->walk == OV_WALK_SPLIT ? sub_walks_for(c->cap) : 1;
 }
 
 int ov_reserve_velocity_scratch(ov_ctx *c)
 {
     int G = ov_query_groups(c);
-    size_t need = (size_t)G * (c->cap <= kSubWalkSlots ? kSubWalks : 1) * 6 * (size_t)c->cap;
+    size_t need = (size_t)G * sub_walks_for(c->cap) * 6 * (size_t)c->cap;
     if (c->part_cap < need) {
         if (c->part) cudaFree(c->part);
         c->part = nullptr;
@@ -1918,10 +1950,12 @@ int ov_launch_velocities(ov_ctx *c, const NodeArrays &na, double t, int precisio
     OV_CUDA(c, cudaMemsetAsync(a.work, 0, sizeof(int), s));
     vel_kernel(precision, c->walk, warps, c->tune.hi_occ, has_mirror_images(c->geo))<<<blocks, 32 * warps, 0, s>>>(
         a, c->part);
-    // with sub-walks a node adds G x S partials (FP64): small blocks spread
-    // the few nodes of such a tangle over many SMs
-    const int fin = a.S > 1 ? 32 : 128;
-    k_vel_finish<<<(c->cap + fin - 1) / fin, fin, 0, s>>>(a, c->part);
+    if (a.S > 1) {
+        const long long threads = 6LL * c->cap * a.G;
+        k_part_sum<<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(a, c->part);
+        c->launches++;
+    }
+    k_vel_finish<<<(c->cap + 127) / 128, 128, 0, s>>>(a, c->part);
     c->launches += 2;
     return OV_OK;
 }
@@ -3179,7 +3213,7 @@ __global__ void __launch_bounds__(128) k_sph_query_split(SphArgs s, double *__re
     MixedAcc acc = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
     bool overflow = false;
     double v[3];
-    walk_split(a, g, f, qp, go, root, end, end, lists, lane, v, acc, overflow);
+    walk_split(a, g, f, qp, go ? 0 : 0x7fffffff, root, end, end, lists, lane, v, acc, overflow);
     double w[3] = {v[0], v[1], v[2]};
     if (j >= 0) sph_rotate(v, -da, -dp, w);
     if (a.stat) {
