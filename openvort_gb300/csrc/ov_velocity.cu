@@ -2163,6 +2163,9 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
     constexpr int force64 = MODE;
     // split query points (self, then images): (g, mirror flag), (f, 0), (f's rest, 0)
     __shared__ float4 s_q[OV_MAX_IMAGES + 1][3];
+    // FP32 mode: the negated query points in pairs (0,1), (2,3), ... for the
+    // two-wide FP32 instructions: -g x, y, z then -f x, y, z of both points
+    __shared__ float2 s_qp[(OV_MAX_IMAGES + 2) / 2][6];
     __shared__ double red[kRecVals][kRecThreads];
     const int b = blockIdx.x, chunk = blockIdx.y;
     if (b >= n) return;
@@ -2204,6 +2207,11 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
         s_q[threadIdx.x][0] = make_float4(g[0], g[1], g[2], mirror);
         s_q[threadIdx.x][1] = make_float4(f[0], f[1], f[2], 0.0f);
         s_q[threadIdx.x][2] = make_float4(fl[0], fl[1], fl[2], 0.0f);
+        float *pr = reinterpret_cast<float *>(&s_qp[threadIdx.x >> 1][0]) + (threadIdx.x & 1);
+        for (int a = 0; a < 3; ++a) {
+            pr[2 * a] = -g[a];
+            pr[2 * (3 + a)] = -f[a];
+        }
     }
     __syncthreads();
     float s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0, mag = 0;
@@ -2245,8 +2253,67 @@ __global__ void __launch_bounds__(kRecThreads, 3) k_rec_sums(RecArgs r, const in
         float t0 = 0, t1 = 0, t2 = 0;   // this segment's terms over the query points
         float ms = 0;                   // sum over the query points of sc |R|
         unsigned mask64 = 0;            // query points whose term is done in FP64
+        int qstart = own ? 1 : 0;
+        if (MODE == 0 && !own && !seg64) {
+            // query points two at a time on the two-wide FP32 pipe (each
+            // element rounds as the one-wide instruction); the terms of even
+            // and odd points add in two chains, joined after the loop
+            const float2 ag2[3] = {make_float2(ag[0], ag[0]), make_float2(ag[1], ag[1]), make_float2(ag[2], ag[2])};
+            const float2 af2[3] = {make_float2(af[0], af[0]), make_float2(af[1], af[1]), make_float2(af[2], af[2])};
+            const float2 sv2[3] = {make_float2(sv[0], sv[0]), make_float2(sv[1], sv[1]), make_float2(sv[2], sv[2])};
+            const float2 nsv2[3] = {make_float2(-sv[0], -sv[0]), make_float2(-sv[1], -sv[1]),
+                                    make_float2(-sv[2], -sv[2])};   // -R2 s1 = R2 (-s1), exactly
+            float2 tt0 = make_float2(0.f, 0.f), tt1 = tt0, tt2 = tt0, mm = tt0;
+            int qi = 0;
+            for (; qi + 1 < nq; qi += 2) {
+                const float2 *qp = s_qp[qi >> 1];
+                const float2 R0 = __fadd2_rn(__fadd2_rn(ag2[0], qp[0]), __fadd2_rn(af2[0], qp[3]));
+                const float2 R1 = __fadd2_rn(__fadd2_rn(ag2[1], qp[1]), __fadd2_rn(af2[1], qp[4]));
+                const float2 R2 = __fadd2_rn(__fadd2_rn(ag2[2], qp[2]), __fadd2_rn(af2[2], qp[5]));
+                const float2 lR2 = __ffma2_rn(R0, R0, __ffma2_rn(R1, R1, __fmul2_rn(R2, R2)));
+                const float2 P0 = __fadd2_rn(R0, sv2[0]), P1 = __fadd2_rn(R1, sv2[1]), P2 = __fadd2_rn(R2, sv2[2]);
+                const float2 lp2 = __ffma2_rn(P0, P0, __ffma2_rn(P1, P1, __fmul2_rn(P2, P2)));
+                const float2 ra = make_float2(rsqrtf(lR2.x), rsqrtf(lR2.y)), rb = make_float2(rsqrtf(lp2.x), rsqrtf(lp2.y));
+                const float2 ab = __fmul2_rn(ra, rb);
+                const float2 dot = __ffma2_rn(R0, P0, __ffma2_rn(R1, P1, __fmul2_rn(R2, P2)));
+                const float2 nd = __fmul2_rn(dot, ab);
+                bool take[2];
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const float l1 = e ? lR2.y : lR2.x, l2 = e ? lp2.y : lp2.x, n1 = e ? nd.y : nd.x;
+                    take[e] = true;
+                    if (fminf(l1, l2) < r.rnear2 || !(n1 > 1e-8f + 1e-4f) || (MIRROR && s_q[qi + e][0].w != 0.0f)) {
+                        take[e] = false;
+                        if (l1 < r.rnear2 || l2 < r.rnear2 || (MIRROR && s_q[qi + e][0].w != 0.0f) ||
+                            fabsf(n1 - 1e-8f) < 1e-4f)
+                            mask64 |= 1u << (qi + e);   // FP64 after the loop
+                        // else: the ndot filter drops it (far from its threshold)
+                    }
+                }
+                const float2 num = __fmul2_rn(__fadd2_rn(ra, rb), ab);
+                const float2 den = __ffma2_rn(dot, ab, make_float2(1.0f, 1.0f));
+                const float2 sc = make_float2(take[0] ? __fdividef(num.x, den.x) : 0.0f,
+                                              take[1] ? __fdividef(num.y, den.y) : 0.0f);
+                // R x Rp1 = R x s
+                const float2 x0 = __ffma2_rn(R1, sv2[2], __fmul2_rn(R2, nsv2[1]));
+                const float2 x1 = __ffma2_rn(R2, sv2[0], __fmul2_rn(R0, nsv2[2]));
+                const float2 x2 = __ffma2_rn(R0, sv2[1], __fmul2_rn(R1, nsv2[0]));
+                tt0 = __ffma2_rn(x0, sc, tt0);
+                tt1 = __ffma2_rn(x1, sc, tt1);
+                tt2 = __ffma2_rn(x2, sc, tt2);
+                // sc |R| (times |s| below: >= |w|); a point left out adds
+                // nothing (its 1/|R| may be infinite)
+                const float2 ra_in = make_float2(take[0] ? ra.x : 0.0f, take[1] ? ra.y : 0.0f);
+                mm = __ffma2_rn(sc, __fmul2_rn(lR2, ra_in), mm);
+            }
+            t0 = tt0.x + tt0.y;
+            t1 = tt1.x + tt1.y;
+            t2 = tt2.x + tt2.y;
+            ms = mm.x + mm.y;
+            qstart = qi;   // an odd last point below
+        }
 #pragma unroll 3
-        for (int qi = own ? 1 : 0; qi < nq; ++qi) {
+        for (int qi = qstart; qi < nq; ++qi) {
             const float4 qg = s_q[qi][0], qf = s_q[qi][1];
             const float R0 = (ag[0] - qg.x) + (af[0] - qf.x);
             const float R1 = (ag[1] - qg.y) + (af[1] - qf.y);
