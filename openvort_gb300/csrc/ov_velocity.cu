@@ -985,6 +985,7 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
     int steps = 0;
     // plain FP32 sub-sums, folded into the Kahan sums every 16 warp steps
     float p0 = 0, p1 = 0, p2 = 0;
+    const float2 ng01 = make_float2(-g[0], -g[1]), nf01 = make_float2(-f[0], -f[1]);
     // c only grows (nxt > c is checked), so it stays within [root, ncell)
     while (c < ncell) {
         const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
@@ -995,8 +996,10 @@ __device__ __forceinline__ void bh_query32(const VelArgs &a, const float g[3], c
         bool open = false;
         if (c >= resume) {
             ++m.nvis;
-            const float dx = (g[0] - A.x) + (f[0] - B.x);
-            const float dy = (g[1] - A.y) + (f[1] - B.y);
+            // x and y two-wide as R = (A - g) + (B - f), the separation's
+            // negation bit for bit (round-to-nearest is symmetric)
+            const float2 Rxy = __fadd2_rn(__fadd2_rn(make_float2(A.x, A.y), ng01), __fadd2_rn(make_float2(B.x, B.y), nf01));
+            const float dx = -Rxy.x, dy = -Rxy.y;
             const float dz = (g[2] - A.z) + (f[2] - B.z);
             const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             const bool leaf = (nxt == c + 1);
@@ -1285,6 +1288,7 @@ __device__ __forceinline__ void walk_mixp(const VelArgs &a, const float g[3], co
     int steps = 0;
     // plain FP32 sub-sums, folded into the Kahan sums every 16 warp steps
     float p0 = 0, p1 = 0, p2 = 0;
+    const float2 ng01 = make_float2(-g[0], -g[1]), nf01 = make_float2(-f[0], -f[1]);
     // c only grows (nxt > c is checked), so it stays within [root, ncell)
     while (c < ncell) {
         const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
@@ -1295,8 +1299,10 @@ __device__ __forceinline__ void walk_mixp(const VelArgs &a, const float g[3], co
         bool open = false;
         if (c >= resume) {
             ++m.nvis;
-            const float dx = (g[0] - A.x) + (f[0] - B.x);
-            const float dy = (g[1] - A.y) + (f[1] - B.y);
+            // x and y two-wide as R = (A - g) + (B - f), the separation's
+            // negation bit for bit (round-to-nearest is symmetric)
+            const float2 Rxy = __fadd2_rn(__fadd2_rn(make_float2(A.x, A.y), ng01), __fadd2_rn(make_float2(B.x, B.y), nf01));
+            const float dx = -Rxy.x, dy = -Rxy.y;
             const float dz = (g[2] - A.z) + (f[2] - B.z);
             const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             const bool leaf = (nxt == c + 1);
