@@ -1541,11 +1541,14 @@ __device__ __forceinline__ void flush_lists(const VelArgs &a, WarpLists &L, int 
 // successor): the mixed traversal's FP32 tests outside their guard bands,
 // the FP64 path's (decide64) inside them.  0 open, 1 skip, 2 accept.
 __device__ __forceinline__ int split_decision(const VelArgs &a, int c, const float4 &A, const float4 &B, int nxt,
-                                              const float g[3], const float f[3], const double q[3], MixedAcc &m)
+                                              const float g[3], const float f[3], const float2 &ng01,
+                                              const float2 &nf01, const double q[3], MixedAcc &m)
 {
     const float d2lo = 1e-16f * (1.0f - 1e-5f), d2hi = 1e-16f * (1.0f + 1e-5f);
-    const float dx = (g[0] - A.x) + (f[0] - B.x);
-    const float dy = (g[1] - A.y) + (f[1] - B.y);
+    // x and y two-wide as (A - g) + (B - f) (ng01, nf01: -g and -f of x, y),
+    // the separation's negation bit for bit
+    const float2 Rxy = __fadd2_rn(__fadd2_rn(make_float2(A.x, A.y), ng01), __fadd2_rn(make_float2(B.x, B.y), nf01));
+    const float dx = -Rxy.x, dy = -Rxy.y;
     const float dz = (g[2] - A.z) + (f[2] - B.z);
     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const bool leaf = (nxt == c + 1);
@@ -1572,13 +1575,14 @@ __device__ __forceinline__ int ancestor_resume(const VelArgs &a, int root, int e
                                                const float f[3], const double q[3])
 {
     MixedAcc tmp = {0, 0, 0, 0, 0, 0, 0u, 0u, 0u, 0u, 0u};
+    const float2 ng01 = make_float2(-g[0], -g[1]), nf01 = make_float2(-f[0], -f[1]);
     int c = root;
     for (int guard = 0; c < b && guard < 32 * (OV_MAX_LEVEL + 2); ++guard) {
         const float4 *cp4 = reinterpret_cast<const float4 *>(a.cells32 + c);
         const float4 A = __ldg(cp4), B = __ldg(cp4 + 1);
         int nxt = __float_as_int(B.w);
         if (nxt <= c || nxt > end) { bad_index(a, 2, c); return 0x7fffffff; }
-        if (split_decision(a, c, A, B, nxt, g, f, q, tmp) != 0) return nxt;   // accepted or skipped
+        if (split_decision(a, c, A, B, nxt, g, f, ng01, nf01, q, tmp) != 0) return nxt;   // accepted or skipped
         // opened: on to the child holding b
         int ch = c + 1;
         for (int k = 0; k < 8; ++k) {
@@ -1600,6 +1604,7 @@ __device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], c
                                            double v[3], MixedAcc &m, bool &overflow)
 {
     v[0] = v[1] = v[2] = 0;
+    const float2 ng01 = make_float2(-g[0], -g[1]), nf01 = make_float2(-f[0], -f[1]);
     int c = root;
     int resume = resume0;
     const int guard_max = 4 * (ncell - root) + 64;
@@ -1614,7 +1619,7 @@ __device__ __forceinline__ void walk_split(const VelArgs &a, const float g[3], c
         bool open = false;
         if (c >= resume) {
             ++m.nvis;
-            const int dec = split_decision(a, c, A, B, nxt, g, f, q, m);
+            const int dec = split_decision(a, c, A, B, nxt, g, f, ng01, nf01, q, m);
             if (dec == 2) {
                 ++m.nacc;
                 L.entry[32 * n + lane] = c;
