@@ -6,7 +6,8 @@ oracle run on the host cores (needs a GB300).
   * large tangle: 1,048,576 nodes (4,096 loops x 256) in D = 0.2 - every node
     of one full update_tangle;
   * batching form: the 48-tangle ensemble at its real member sizes, each
-    member with its own alpha, alpha' and v_n - every node of every member.
+    member with its own alpha, alpha' and v_n - every node of every member;
+  * small tangles whose FP64 walks run in parts (1,024 to 12,288 nodes).
 
 Gates: velocities within 1e-10 relative per node of the oracle (the FP64
 bar: only summation order differs); and the decisions, node by node: each
@@ -74,6 +75,28 @@ def _gpu_single(ht, p, precision):
     st = ctx.stats()
     ctx.close()
     return np.array(out.vels), vis, acc, st
+
+
+@pytest.mark.parametrize("loops", [16, 64, 192])
+def test_split_walk_parts_every_node(port, loops):
+    """Small tangles run each query point's FP64 split walk in parts (32 up to
+    2,048 slots, 8 up to 8,192, whole above): 1,024, 4,096 and 12,288 nodes,
+    every node and every target's visit/accept counts against the oracle,
+    through the counting path and through the default evaluation graph."""
+    ht = W.random_walk_tangle(loops, 64, D=0.1, seed=70 + loops)
+    p = W.config_params("rw")
+    ov, ovis, oacc = _oracle(port, ht, p)
+    v64, gvis, gacc, st = _gpu_single(ht, p, abi.OV_PREC_FP64)
+    assert st["error_word"] == 0
+    assert _flips(gvis, gacc, ovis, oacc, np.ones(ht.n, dtype=bool)) == 0
+    assert _per_node_rel(v64, ov).max() < FP64_TOL
+    ctx = gpu.Context(0, params=p, precision=abi.OV_PREC_FP64)
+    ctx.upload(ht)
+    ctx.update_tangle(0.0)
+    vg = np.array(ctx.download(ht, abi.OV_F_VELS).vels)
+    assert ctx.stats()["accepts"] == int(oacc.sum())
+    ctx.close()
+    assert _per_node_rel(vg, ov).max() < FP64_TOL
 
 
 @pytest.mark.parametrize("theta", [0.3, 0.5])
