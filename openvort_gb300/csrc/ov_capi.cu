@@ -1041,6 +1041,7 @@ static int eval_graph(ov_ctx *c, double t, bool tangents, cudaStream_t s)
 int ov_eval_sync(ov_ctx *c, NodeArrays &na, double t, bool tangents)
 {
     int r;
+    c->tree_built = false;   // (a replayed graph does not run ov_tree_build's host side)
     const bool graph = c->use_graph && !c->count_nodes && &na == &c->node;
     for (int attempt = 0; attempt < 3; ++attempt) {
         if ((r = clear_call_words(c))) return r;
@@ -1137,6 +1138,7 @@ int ov_rk4_step(ov_ctx *c, double t, double dt)
     int r = check_ready(c);
     if (r) return r;
     c->host_valid = false;
+    c->tree_built = false;   // the tree buffers end up holding a stage's tree (also when a graph replays)
     cudaStream_t s = c->stream;
     if (!c->d_time) {
         OV_ALLOC(c, cudaMalloc(&c->d_time, 8 * sizeof(double)));
